@@ -1,0 +1,84 @@
+"""ctypes binding of libfricc_gb300.so (the C ABI in include/fricc_gb300.h).
+
+The library is built in-tree (``python -m fricc_gb300.build`` or
+``__graft_entry__.build()``).  Loading fails loudly when it is missing: there
+is no CPU fallback behind this module.
+"""
+from __future__ import annotations
+
+import ctypes
+import os
+
+_HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(_HERE, "_lib", "libfricc_gb300.so")
+
+FRICC_OK = 0
+STATUS_NAMES = {1: "FRICC_ERR_ARG", 2: "FRICC_ERR_TERM", 3: "FRICC_ERR_P_GT_ONE", 4: "FRICC_ERR_CUDA",
+                5: "FRICC_ERR_TIMEOUT", 6: "FRICC_ERR_INDEX", 7: "FRICC_ERR_UNSUPPORTED"}
+COMPRESSION = {"fri": 0, "largest": 1}
+SAMPLING = {"systematic": 0, "pivotal": 1}
+
+# (name, restype, argtypes) of every exported symbol
+_i64 = ctypes.c_int64
+_i64p = ctypes.POINTER(ctypes.c_int64)
+_dp = ctypes.c_void_p
+_vp = ctypes.c_void_p
+SIGNATURES = [
+    ("fricc_version", ctypes.c_int, []),
+    ("fricc_last_error", ctypes.c_char_p, []),
+    ("fricc_sp_create", ctypes.c_int, [_dp, _i64p, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_double, _vp,
+                                       ctypes.POINTER(_vp)]),
+    ("fricc_sp_recompress", ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, _vp]),
+    ("fricc_sp_create_empty", ctypes.c_int, [_i64p, _i64, _vp, ctypes.POINTER(_vp)]),
+    ("fricc_sp_destroy", ctypes.c_int, [_vp]),
+    ("fricc_sp_info", ctypes.c_int, [_vp, _i64p, _i64p, _i64p]),
+    ("fricc_sp_get", ctypes.c_int, [_vp, _i64, _i64p, ctypes.POINTER(ctypes.c_double)]),
+    ("fricc_sp_export", ctypes.c_int, [_vp, _vp, _vp, _vp]),
+    ("fricc_sp_device_arrays", ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
+    ("fricc_contract", ctypes.c_int, [ctypes.c_char_p, _dp, _i64p, _i64p, _vp, _dp, _i64p, _i64p, _vp]),
+    ("fricc_contract_flops", ctypes.c_double, [ctypes.c_char_p, _vp]),
+    ("fricc_compress", ctypes.c_int, [_dp, _i64, _i64, ctypes.c_int, ctypes.c_double, _dp, _dp, _i64p, _vp]),
+    ("fricc_seq_cumsum", ctypes.c_int, [_dp, _i64, _dp, _vp]),
+    ("fricc_energy_update", ctypes.c_int, [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _i64, _dp, _dp, _dp, _vp]),
+]
+
+_lib = None
+
+
+class FriccError(RuntimeError):
+    def __init__(self, status: int, message: str):
+        super().__init__(f"{STATUS_NAMES.get(status, status)}: {message}")
+        self.status = status
+
+
+def load(path: str = LIB_PATH):
+    """Load the shared library (once) and declare every prototype."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise ImportError(
+            f"{path} is missing: build the CUDA library first (python -m fricc_gb300.build); "
+            "the GPU path has no CPU fallback")
+    L = ctypes.CDLL(path)
+    for name, res, args in SIGNATURES:
+        f = getattr(L, name)
+        f.restype = res
+        f.argtypes = args
+    _lib = L
+    return L
+
+
+def check(status: int) -> None:
+    if status != FRICC_OK:
+        msg = load().fricc_last_error()
+        msg = msg.decode() if msg else ""
+        if status == 1:
+            raise ValueError(f"FRICC_ERR_ARG: {msg}")
+        if status == 7:
+            raise NotImplementedError(f"FRICC_ERR_UNSUPPORTED: {msg}")
+        raise FriccError(status, msg)
+
+
+def i64arr(vals):
+    return (ctypes.c_int64 * len(vals))(*[int(v) for v in vals])

@@ -1,0 +1,306 @@
+// extern "C" entry points of libfricc_gb300.so (declared in include/fricc_gb300.h).
+#include <cstdarg>
+#include <cstdint>
+#include <cstdio>
+#include <cstring>
+#include <mutex>
+
+#include "../../include/fricc_gb300.h"
+#include "common.cuh"
+#include "sparse.cuh"
+
+int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, double rn, cudaStream_t st, int64_t* flat,
+                          double* vals, int64_t* n_largest);
+int fricc_seq_cumsum_device(const double* x, int64_t n, double* out, cudaStream_t st);
+int fricc_unpack_device(const int64_t* flat, int64_t m, const int64_t dims[4], int* slots, cudaStream_t st);
+int fricc_contract_device(const char* term, const double* W, const int64_t Wd[4], const int64_t Ws[4], FriccSparse* T,
+                          double* out, const int64_t Od[4], const int64_t Os[4], cudaStream_t st);
+double fricc_contract_flops_impl(const char* term, const FriccSparse* T);
+int fricc_energy_update_device(const double* t1num, const double* t2num, const double* eia, const double* fov,
+                               const double* ovov, const double* t1old, const double* t2old, int64_t o, int64_t v,
+                               double* t1out, double* t2out, double* res, cudaStream_t st);
+
+// ------------------------------------------------------------------ errors
+static thread_local char g_err[512] = "";
+
+void fricc_set_error(const char* fmt, ...) {
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(g_err, sizeof(g_err), fmt, ap);
+  va_end(ap);
+}
+
+int fricc_cuda_check(cudaError_t e, const char* what) {
+  if (e == cudaSuccess) return FRICC_OK;
+  fricc_set_error("CUDA error %s (%s) in %s", cudaGetErrorName(e), cudaGetErrorString(e), what);
+  return FRICC_ERR_CUDA;
+}
+
+int fricc_cuda_fail(cudaError_t e, const char* what, const char* file, int line) {
+  fricc_set_error("CUDA error %s (%s) in %s at %s:%d", cudaGetErrorName(e), cudaGetErrorString(e), what, file, line);
+  return FRICC_ERR_CUDA;
+}
+
+// ------------------------------------------------------------------ memory
+static std::once_flag g_pool_once[64];
+
+int fricc_alloc(void** p, size_t bytes, cudaStream_t s) {
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (dev >= 0 && dev < 64) {
+    std::call_once(g_pool_once[dev], [dev]() {
+      cudaMemPool_t pool;
+      if (cudaDeviceGetDefaultMemPool(&pool, dev) == cudaSuccess) {
+        uint64_t thr = UINT64_MAX;  // keep freed blocks cached in the pool
+        cudaMemPoolSetAttribute(pool, cudaMemPoolAttrReleaseThreshold, &thr);
+      }
+    });
+  }
+  cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, s);
+  if (e != cudaSuccess) {
+    *p = nullptr;
+    return fricc_cuda_fail(e, "cudaMallocAsync", __FILE__, __LINE__);
+  }
+  return FRICC_OK;
+}
+
+void fricc_free(void* p, cudaStream_t s) {
+  if (p) cudaFreeAsync(p, s);
+}
+
+static cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
+
+static void free_sparse_arrays(FriccSparse* T, cudaStream_t st) {
+  fricc_free(T->flat, st);
+  fricc_free(T->vals, st);
+  fricc_free(T->slots, st);
+  T->flat = nullptr;
+  T->vals = nullptr;
+  T->slots = nullptr;
+  for (auto& b : T->buck) {
+    fricc_free(b.bptr, st);
+    fricc_free(b.order, st);
+    b = Bucketing{};
+  }
+}
+
+static void drop_bucketings(FriccSparse* T, cudaStream_t st) {
+  for (auto& b : T->buck) {
+    fricc_free(b.bptr, st);
+    fricc_free(b.order, st);
+    b = Bucketing{};
+  }
+}
+
+static bool bad_dims(const int64_t dims[4]) {
+  if (!dims) return true;
+  for (int k = 0; k < 4; ++k)
+    if (dims[k] <= 0 || dims[k] > 0x7fffffff) return true;
+  return false;
+}
+
+// ------------------------------------------------------------------ API
+extern "C" {
+
+int fricc_version(void) { return 100; }
+
+const char* fricc_last_error(void) { return g_err; }
+
+int fricc_sp_recompress(fricc_sparse* T, const double* t2, int compression, int sampling, double rn, void* stream) {
+  if (!T || !t2) {
+    fricc_set_error("sp_recompress: null argument");
+    return FRICC_ERR_ARG;
+  }
+  if (compression != FRICC_COMPRESSION_FRI && compression != FRICC_COMPRESSION_LARGEST) {
+    fricc_set_error("The compression method you chose isn't supported: compression must be 'largest' or 'fri'");
+    return FRICC_ERR_ARG;
+  }
+  if (compression == FRICC_COMPRESSION_FRI && sampling != FRICC_SAMPLING_SYSTEMATIC) {
+    fricc_set_error("sampling_method 'pivotal' is not implemented on the GPU path (use 'systematic')");
+    return FRICC_ERR_UNSUPPORTED;
+  }
+  cudaStream_t st = as_stream(stream);
+  drop_bucketings(T, st);
+  const int64_t n = T->dims[0] * T->dims[1] * T->dims[2] * T->dims[3];
+  int64_t nd = 0;
+  int rc = fricc_compress_device(t2, n, T->m, compression == FRICC_COMPRESSION_LARGEST ? 1 : 0, rn, st, T->flat,
+                                 T->vals, &nd);
+  if (rc) return rc;
+  T->n_largest = nd;
+  T->owner_stream = st;
+  return fricc_unpack_device(T->flat, T->m, T->dims, T->slots, st);
+}
+
+int fricc_sp_create(const double* t2, const int64_t dims[4], int64_t m, int compression, int sampling, double rn,
+                    void* stream, fricc_sparse** out) {
+  if (!out || !t2 || bad_dims(dims)) {
+    fricc_set_error("sp_create: null pointer or non-positive dims");
+    return FRICC_ERR_ARG;
+  }
+  *out = nullptr;
+  const int64_t n = dims[0] * dims[1] * dims[2] * dims[3];
+  if (m <= 0 || m > n) {
+    fricc_set_error("Bad m_keep value! The following condition wasn't met 0 < m_keep <= t2.size (m=%lld, size=%lld)",
+                    (long long)m, (long long)n);
+    return FRICC_ERR_ARG;
+  }
+  cudaStream_t st = as_stream(stream);
+  FriccSparse* T = new FriccSparse();
+  for (int k = 0; k < 4; ++k) T->dims[k] = dims[k];
+  T->m = m;
+  cudaGetDevice(&T->device);
+  int rc = fricc_alloc_t(&T->flat, m, st);
+  if (!rc) rc = fricc_alloc_t(&T->vals, m, st);
+  if (!rc) rc = fricc_alloc_t(&T->slots, 4 * m, st);
+  if (!rc) rc = fricc_sp_recompress(T, t2, compression, sampling, rn, stream);
+  if (rc) {
+    free_sparse_arrays(T, st);
+    cudaStreamSynchronize(st);
+    delete T;
+    return rc;
+  }
+  *out = T;
+  return FRICC_OK;
+}
+
+int fricc_sp_create_empty(const int64_t dims[4], int64_t nnz, void* stream, fricc_sparse** out) {
+  if (!out || bad_dims(dims) || nnz < 0) {
+    fricc_set_error("sp_create_empty: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  cudaStream_t st = as_stream(stream);
+  FriccSparse* T = new FriccSparse();
+  for (int k = 0; k < 4; ++k) T->dims[k] = dims[k];
+  T->m = nnz;
+  cudaGetDevice(&T->device);
+  int rc = fricc_alloc_t(&T->flat, nnz, st);
+  if (!rc) rc = fricc_alloc_t(&T->vals, nnz, st);
+  if (!rc) rc = fricc_alloc_t(&T->slots, 4 * nnz, st);
+  if (!rc) {
+    cudaMemsetAsync(T->flat, 0, nnz * sizeof(int64_t), st);
+    cudaMemsetAsync(T->vals, 0, nnz * sizeof(double), st);
+    cudaMemsetAsync(T->slots, 0, 4 * nnz * sizeof(int), st);
+    cudaError_t e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) rc = fricc_cuda_fail(e, "sp_create_empty", __FILE__, __LINE__);
+  }
+  if (rc) {
+    free_sparse_arrays(T, st);
+    delete T;
+    return rc;
+  }
+  T->owner_stream = st;
+  *out = T;
+  return FRICC_OK;
+}
+
+int fricc_sp_destroy(fricc_sparse* T) {
+  if (!T) return FRICC_OK;
+  free_sparse_arrays(T, T->owner_stream);
+  delete T;
+  return FRICC_OK;
+}
+
+int fricc_sp_info(const fricc_sparse* T, int64_t dims[4], int64_t* m, int64_t* n_largest) {
+  if (!T) {
+    fricc_set_error("sp_info: null handle");
+    return FRICC_ERR_ARG;
+  }
+  if (dims)
+    for (int k = 0; k < 4; ++k) dims[k] = T->dims[k];
+  if (m) *m = T->m;
+  if (n_largest) *n_largest = T->n_largest;
+  return FRICC_OK;
+}
+
+int fricc_sp_get(const fricc_sparse* T, int64_t mi, int64_t idx[4], double* value) {
+  if (!T || mi < 0 || mi >= T->m) {
+    fricc_set_error("get_element: index %lld out of range", (long long)mi);
+    return FRICC_ERR_ARG;
+  }
+  int s[4];
+  double v = 0.0;
+  cudaError_t e = cudaStreamSynchronize(T->owner_stream);
+  if (e == cudaSuccess) e = cudaMemcpy(s, T->slots + 4 * mi, sizeof(s), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(&v, T->vals + mi, sizeof(double), cudaMemcpyDeviceToHost);
+  if (e != cudaSuccess) return fricc_cuda_fail(e, "get_element", __FILE__, __LINE__);
+  if (idx)
+    for (int k = 0; k < 4; ++k) idx[k] = s[k];
+  if (value) *value = v;
+  return FRICC_OK;
+}
+
+int fricc_sp_export(const fricc_sparse* T, int64_t* flat_host, double* vals_host, void* stream) {
+  if (!T) {
+    fricc_set_error("sp_export: null handle");
+    return FRICC_ERR_ARG;
+  }
+  cudaStream_t st = as_stream(stream);
+  if (flat_host) FRICC_CUDA(cudaMemcpyAsync(flat_host, T->flat, T->m * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  if (vals_host) FRICC_CUDA(cudaMemcpyAsync(vals_host, T->vals, T->m * sizeof(double), cudaMemcpyDeviceToHost, st));
+  FRICC_CUDA(cudaStreamSynchronize(st));
+  return FRICC_OK;
+}
+
+int fricc_sp_device_arrays(const fricc_sparse* T, const int64_t** flat, const double** vals, const int** slots) {
+  if (!T) {
+    fricc_set_error("sp_device_arrays: null handle");
+    return FRICC_ERR_ARG;
+  }
+  if (flat) *flat = T->flat;
+  if (vals) *vals = T->vals;
+  if (slots) *slots = T->slots;
+  return FRICC_OK;
+}
+
+int fricc_contract(const char* term, const double* W, const int64_t W_dims[4], const int64_t W_strides[4],
+                   fricc_sparse* T, double* out, const int64_t out_dims[4], const int64_t out_strides[4],
+                   void* stream) {
+  if (!W_dims || !W_strides || !out_dims || !out_strides) {
+    fricc_set_error("contract: null shape argument");
+    return FRICC_ERR_ARG;
+  }
+  for (int k = 0; k < 4; ++k)
+    if (W_strides[k] < 0 || out_strides[k] < 0 || W_dims[k] < 0 || out_dims[k] < 0) {
+      fricc_set_error("contract: negative dims or strides are not supported");
+      return FRICC_ERR_ARG;
+    }
+  cudaStream_t st = as_stream(stream);
+  int rc = fricc_contract_device(term, W, W_dims, W_strides, T, out, out_dims, out_strides, st);
+  if (!rc && T) T->owner_stream = st;
+  return rc;
+}
+
+double fricc_contract_flops(const char* term, const fricc_sparse* T) {
+  return fricc_contract_flops_impl(term, T);
+}
+
+int fricc_compress(const double* x, int64_t n, int64_t m, int compression, double rn, int64_t* flat, double* vals,
+                   int64_t* n_largest, void* stream) {
+  if (!x || !flat || !vals) {
+    fricc_set_error("compress: null argument");
+    return FRICC_ERR_ARG;
+  }
+  if (compression != FRICC_COMPRESSION_FRI && compression != FRICC_COMPRESSION_LARGEST) {
+    fricc_set_error("compress: compression must be 'largest' or 'fri'");
+    return FRICC_ERR_ARG;
+  }
+  return fricc_compress_device(x, n, m, compression == FRICC_COMPRESSION_LARGEST ? 1 : 0, rn, as_stream(stream), flat,
+                               vals, n_largest);
+}
+
+int fricc_energy_update(const double* t1num, const double* t2num, const double* eia, const double* fov,
+                        const double* ovov, const double* t1old, const double* t2old, int64_t nocc, int64_t nvir,
+                        double* t1out, double* t2out, double* res, void* stream) {
+  if (!t1num || !t2num || !eia || !fov || !ovov || !t1old || !t2old || !t1out || !t2out || !res) {
+    fricc_set_error("energy_update: null argument");
+    return FRICC_ERR_ARG;
+  }
+  return fricc_energy_update_device(t1num, t2num, eia, fov, ovov, t1old, t2old, nocc, nvir, t1out, t2out, res,
+                                    as_stream(stream));
+}
+
+int fricc_seq_cumsum(const double* x, int64_t n, double* out, void* stream) {
+  return fricc_seq_cumsum_device(x, n, out, as_stream(stream));
+}
+
+}  // extern "C"

@@ -1,0 +1,120 @@
+// Shared definitions for the fricc_gb300 CUDA library (sm_103a).
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include <cstdio>
+
+// Status codes (FRICC_OK, FRICC_ERR_*) are those of the public C ABI.
+#include "../../include/fricc_gb300.h"
+
+// Device error word bits (written by kernels, read by the host after a sync).
+#define FRICC_DEV_P_GT_ONE 1u
+#define FRICC_DEV_TIMEOUT 2u
+#define FRICC_DEV_INDEX 4u
+
+void fricc_set_error(const char* fmt, ...);
+int fricc_cuda_fail(cudaError_t e, const char* what, const char* file, int line);
+int fricc_cuda_check(cudaError_t e, const char* what);  // FRICC_OK on success
+
+#define FRICC_CUDA(call)                                                         \
+  do {                                                                           \
+    cudaError_t _e = (call);                                                     \
+    if (_e != cudaSuccess) return fricc_cuda_fail(_e, #call, __FILE__, __LINE__); \
+  } while (0)
+
+#define FRICC_LAUNCH_CHECK() FRICC_CUDA(cudaGetLastError())
+
+// Stream-ordered scratch allocation (memory comes from the device's default
+// pool, whose release threshold is raised once so freed blocks are reused).
+int fricc_alloc(void** p, size_t bytes, cudaStream_t s);
+void fricc_free(void* p, cudaStream_t s);
+
+template <class T>
+inline int fricc_alloc_t(T** p, size_t n, cudaStream_t s) {
+  return fricc_alloc(reinterpret_cast<void**>(p), n * sizeof(T) + 16, s);
+}
+
+__host__ __device__ inline int64_t fricc_cdiv(int64_t a, int64_t b) { return (a + b - 1) / b; }
+
+// ---------------------------------------------------------------- warp/block
+__device__ __forceinline__ unsigned lane_id() { return threadIdx.x & 31u; }
+__device__ __forceinline__ unsigned warp_id() { return threadIdx.x >> 5; }
+
+template <class T>
+__device__ __forceinline__ T warp_sum(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+template <class T>
+__device__ __forceinline__ T warp_min(T v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    T w = __shfl_xor_sync(0xffffffffu, v, o);
+    v = w < v ? w : v;
+  }
+  return v;
+}
+
+// Block-wide minimum; every thread gets the result.  smem: >= 32 T.
+template <class T>
+__device__ __forceinline__ T block_min(T v, T* smem) {
+  v = warp_min(v);
+  const int nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane_id() == 0) smem[warp_id()] = v;
+  __syncthreads();
+  T r = smem[0];
+  for (int w = 1; w < nw; ++w) r = smem[w] < r ? smem[w] : r;
+  __syncthreads();
+  return r;
+}
+
+// Block-wide exclusive sum of int64 (thread order); returns the exclusive
+// prefix and writes the block total into *total.  smem: >= 33 int64.
+__device__ __forceinline__ int64_t block_excl_sum(int64_t v, int64_t* smem, int64_t* total) {
+  int64_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    int64_t w = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((int)lane_id() >= o) incl += w;
+  }
+  const int nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane_id() == 31) smem[warp_id()] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t run = 0;
+    for (int w = 0; w < nw; ++w) {
+      int64_t t = smem[w];
+      smem[w] = run;
+      run += t;
+    }
+    smem[32] = run;
+  }
+  __syncthreads();
+  int64_t r = smem[warp_id()] + incl - v;
+  *total = smem[32];
+  __syncthreads();
+  return r;
+}
+
+// Deterministic block sum of doubles (fixed tree for a fixed blockDim).
+__device__ __forceinline__ double block_sum_det(double v, double* smem) {
+  v = warp_sum(v);
+  const int nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane_id() == 0) smem[warp_id()] = v;
+  __syncthreads();
+  double r = 0.0;
+  if (threadIdx.x == 0) {
+    for (int w = 0; w < nw; ++w) r += smem[w];
+    smem[0] = r;
+  }
+  __syncthreads();
+  r = smem[0];
+  __syncthreads();
+  return r;
+}

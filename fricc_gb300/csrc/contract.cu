@@ -1,0 +1,329 @@
+// The eleven sparse-T2 x dense-W contraction terms of fri-cc
+// (src/sparse_tensor.cpp:12-346, dispatcher :349-382) as one bucketed
+// SpMM kernel driven by a term table.
+//
+// Every term has the form
+//     out'[P, q] += coef * sum_{e in bucket P} W'[key_e, q] * value_e
+// where P is the pair of index slots the reference filters on, key_e the
+// pair of slots that indexes W, and q the two dense indices of the inner
+// loops.  W' and out' are W and out with their axes permuted so that q is
+// the contiguous innermost pair; a W or out that already has that layout
+// (any strides that say so) is used in place, anything else is gathered
+// into a permuted copy first (and scattered back for out).
+//
+// The reference visits the nonzeros of each output element in slot order;
+// the bucketing is a stable sort, so each output element here receives its
+// contributions in the same order (fused multiply-add, one rounding per
+// term instead of two).
+#include <cmath>
+#include <cstring>
+
+#include "radix.cuh"
+#include "sparse.cuh"
+
+namespace {
+
+struct TermSpec {
+  const char* name;
+  int pa, pb;     // bucket slots (outer pair of the reference loop)
+  int ka, kb;     // slots that index W
+  int permW[4];   // W' axis j = W axis permW[j]
+  int permO[4];   // out' axis j = out axis permO[j]
+  double coef;
+};
+
+// Index algebra per term, from the loops of src/sparse_tensor.cpp.
+const TermSpec kTerms[] = {
+    // out(i,j,a,b) += W(k,l,i,j) T(k,l,a,b)                     :12-37
+    {"0101", 2, 3, 0, 1, {0, 1, 2, 3}, {2, 3, 0, 1}, 1.0},
+    // out(i,j,a,b) += W(a,b,c,d) T(i,j,c,d)                     :40-86
+    {"2323", 0, 1, 2, 3, {2, 3, 0, 1}, {0, 1, 2, 3}, 1.0},
+    // out(i,j,a,b) += 2 W(a,k,i,c) T(k,j,c,b)                   :89-115
+    {"1302", 1, 3, 0, 2, {1, 3, 2, 0}, {1, 3, 0, 2}, 2.0},
+    // out(i,j,a,b) -= W(a,k,c,i) T(k,j,c,b)                     :118-144
+    {"1202", 1, 3, 0, 2, {1, 2, 3, 0}, {1, 3, 0, 2}, -1.0},
+    // out(i,j,a,b) += W(a,k,i,c) T(k,j,b,c)                     :147-173
+    {"1303", 1, 2, 0, 3, {1, 3, 2, 0}, {1, 3, 0, 2}, 1.0},
+    // out(i,j,a,b) += W(b,k,c,i) T(k,j,a,c)                     :176-202
+    {"1203", 1, 2, 0, 3, {1, 2, 3, 0}, {1, 2, 0, 3}, 1.0},
+    // out(k,l,i,j) += ovov(k,c,l,d) T(i,j,c,d)                  :205-230
+    {"1323", 0, 1, 2, 3, {1, 3, 0, 2}, {2, 3, 0, 1}, 1.0},
+    // out(a,k,i,c) -= 0.5 ovov(l,d,k,c) T(i,l,d,a)              :233-259
+    {"0112", 3, 0, 1, 2, {0, 1, 2, 3}, {0, 2, 1, 3}, -0.5},
+    // out(a,k,i,c) += ovov(l,d,k,c) T(i,l,a,d)                  :292-317
+    {"0113", 2, 0, 1, 3, {0, 1, 2, 3}, {0, 2, 1, 3}, 1.0},
+    // out(a,k,i,c) -= 0.5 ovov(l,c,k,d) T(i,l,a,d)              :262-289
+    {"0313", 2, 0, 1, 3, {0, 3, 2, 1}, {0, 2, 1, 3}, -0.5},
+    // out(a,k,c,i) -= 0.5 ovov(l,c,k,d) T(i,l,d,a)              :320-346
+    {"0312", 3, 0, 1, 2, {0, 3, 2, 1}, {0, 3, 1, 2}, -0.5},
+};
+
+const TermSpec* find_term(const char* name) {
+  if (!name) return nullptr;
+  for (const auto& t : kTerms)
+    if (std::strcmp(t.name, name) == 0) return &t;
+  return nullptr;
+}
+
+__global__ void k_pair_keys(const int* __restrict__ slots, int64_t m, int pa, int pb, int64_t dpb,
+                            unsigned long long* __restrict__ keys, unsigned* __restrict__ idx) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m; s += (int64_t)gridDim.x * blockDim.x) {
+    keys[s] = (unsigned long long)slots[4 * s + pa] * (unsigned long long)dpb + (unsigned long long)slots[4 * s + pb];
+    idx[s] = (unsigned)s;
+  }
+}
+
+// bptr[P] = first position whose key >= P (keys sorted ascending)
+__global__ void k_bptr(const unsigned long long* __restrict__ keys, int64_t m, int64_t nb, int* __restrict__ bptr) {
+  for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P <= nb; P += (int64_t)gridDim.x * blockDim.x) {
+    int64_t lo = 0, hi = m;
+    while (lo < hi) {
+      const int64_t mid = (lo + hi) >> 1;
+      if (keys[mid] < (unsigned long long)P) lo = mid + 1;
+      else hi = mid;
+    }
+    bptr[P] = (int)lo;
+  }
+}
+
+// per-term entry list in bucket order: W' row and coef * value
+__global__ void k_entries(const int* __restrict__ slots, const double* __restrict__ vals,
+                          const unsigned* __restrict__ order, int64_t m, int ka, int kb, int64_t dkb, double coef,
+                          int* __restrict__ erow, double* __restrict__ eval) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned s = order[e];
+    erow[e] = (int)((int64_t)slots[4 * s + ka] * dkb + slots[4 * s + kb]);
+    eval[e] = coef * vals[s];  // coef is +-1, 2 or -1/2: exact
+  }
+}
+
+constexpr int SP_NT = 128;
+constexpr int SP_QPT = 2;
+
+__global__ void __launch_bounds__(SP_NT) k_spmm(const int* __restrict__ bptr, const int* __restrict__ erow,
+                                                const double* __restrict__ eval, const double* __restrict__ Wp,
+                                                double* __restrict__ Op, int64_t QS) {
+  __shared__ int srow[SP_NT];
+  __shared__ double sval[SP_NT];
+  const int64_t P = blockIdx.x;
+  const int e0 = bptr[P], e1 = bptr[P + 1];
+  if (e0 == e1) return;
+  const int64_t q0 = (int64_t)blockIdx.y * (SP_NT * SP_QPT) + threadIdx.x;
+  double* orow = Op + P * QS;
+  double acc[SP_QPT];
+#pragma unroll
+  for (int k = 0; k < SP_QPT; ++k) {
+    const int64_t q = q0 + k * SP_NT;
+    acc[k] = q < QS ? orow[q] : 0.0;
+  }
+  for (int eb = e0; eb < e1; eb += SP_NT) {
+    const int cnt = e1 - eb < SP_NT ? e1 - eb : SP_NT;
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      srow[threadIdx.x] = erow[eb + threadIdx.x];
+      sval[threadIdx.x] = eval[eb + threadIdx.x];
+    }
+    __syncthreads();
+    for (int j = 0; j < cnt; ++j) {
+      const double* w = Wp + (int64_t)srow[j] * QS;
+      const double v = sval[j];
+#pragma unroll
+      for (int k = 0; k < SP_QPT; ++k) {
+        const int64_t q = q0 + k * SP_NT;
+        if (q < QS) acc[k] = fma(w[q], v, acc[k]);
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < SP_QPT; ++k) {
+    const int64_t q = q0 + k * SP_NT;
+    if (q < QS) orow[q] = acc[k];
+  }
+}
+
+// dst (contiguous, extents e0..e3) = src viewed with strides s0..s3
+__global__ void k_gather4(const double* __restrict__ src, int64_t s0, int64_t s1, int64_t s2, int64_t s3, int64_t e0,
+                          int64_t e1, int64_t e2, int64_t e3, double* __restrict__ dst) {
+  const int64_t n = e0 * e1 * e2 * e3;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = t;
+    const int64_t i3 = r % e3; r /= e3;
+    const int64_t i2 = r % e2; r /= e2;
+    const int64_t i1 = r % e1;
+    const int64_t i0 = r / e1;
+    dst[t] = src[i0 * s0 + i1 * s1 + i2 * s2 + i3 * s3];
+  }
+}
+
+__global__ void k_scatter4(const double* __restrict__ src, int64_t s0, int64_t s1, int64_t s2, int64_t s3, int64_t e0,
+                           int64_t e1, int64_t e2, int64_t e3, double* __restrict__ dst) {
+  const int64_t n = e0 * e1 * e2 * e3;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    int64_t r = t;
+    const int64_t i3 = r % e3; r /= e3;
+    const int64_t i2 = r % e2; r /= e2;
+    const int64_t i1 = r % e1;
+    const int64_t i0 = r / e1;
+    dst[i0 * s0 + i1 * s1 + i2 * s2 + i3 * s3] = src[t];
+  }
+}
+
+inline unsigned grid_for(int64_t n, int nt) {
+  int64_t g = fricc_cdiv(n, nt);
+  if (g > 152 * 32) g = 152 * 32;
+  return (unsigned)(g < 1 ? 1 : g);
+}
+
+bool is_contig_perm(const int64_t dims[4], const int64_t strides[4], const int perm[4]) {
+  int64_t expect = 1;
+  for (int j = 3; j >= 0; --j) {
+    if (dims[perm[j]] > 1 && strides[perm[j]] != expect) return false;
+    expect *= dims[perm[j]];
+  }
+  return true;
+}
+
+}  // namespace
+
+int fricc_sparse_bucketing(FriccSparse* T, int pa, int pb, cudaStream_t st, Bucketing** out) {
+  for (auto& b : T->buck)
+    if (b.pa == pa && b.pb == pb && b.bptr) {
+      *out = &b;
+      return FRICC_OK;
+    }
+  Bucketing* slot = nullptr;
+  for (auto& b : T->buck)
+    if (!b.bptr) {
+      slot = &b;
+      break;
+    }
+  if (!slot) return FRICC_ERR_ARG;
+  const int64_t m = T->m;
+  const int64_t nb = T->dims[pa] * T->dims[pb];
+  int bits = 8;
+  while (bits < 64 && (1ll << bits) < nb) bits += 8;
+  unsigned long long *keys = nullptr, *ktmp = nullptr;
+  unsigned *vtmp = nullptr, *hist = nullptr;
+  int rc = fricc_alloc_t(&keys, m, st);
+  if (!rc) rc = fricc_alloc_t(&ktmp, m, st);
+  if (!rc) rc = fricc_alloc_t(&vtmp, m, st);
+  if (!rc) rc = fricc_alloc_t(&hist, 256 * fricc_cdiv(m, radix::TILE), st);
+  if (!rc) rc = fricc_alloc_t(&slot->order, m, st);
+  if (!rc) rc = fricc_alloc_t(&slot->bptr, nb + 1, st);
+  if (!rc) {
+    k_pair_keys<<<grid_for(m, 256), 256, 0, st>>>(T->slots, m, pa, pb, T->dims[pb], keys, slot->order);
+    rc = radix::sort_pairs(keys, slot->order, ktmp, vtmp, m, bits, false, hist, st);
+  }
+  if (!rc) {
+    k_bptr<<<grid_for(nb + 1, 256), 256, 0, st>>>(keys, m, nb, slot->bptr);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fricc_cuda_fail(e, "bucketing", __FILE__, __LINE__);
+  }
+  fricc_free(keys, st);
+  fricc_free(ktmp, st);
+  fricc_free(vtmp, st);
+  fricc_free(hist, st);
+  if (rc) {
+    fricc_free(slot->order, st);
+    fricc_free(slot->bptr, st);
+    slot->order = nullptr;
+    slot->bptr = nullptr;
+    return rc;
+  }
+  slot->pa = pa;
+  slot->pb = pb;
+  slot->nbuckets = nb;
+  *out = slot;
+  return FRICC_OK;
+}
+
+int fricc_contract_device(const char* term, const double* W, const int64_t Wd[4], const int64_t Ws[4], FriccSparse* T,
+                          double* out, const int64_t Od[4], const int64_t Os[4], cudaStream_t st) {
+  const TermSpec* ts = find_term(term);
+  if (!ts) {
+    fricc_set_error("CASE NOT IMPLEMENTED: contraction term '%s'", term ? term : "(null)");
+    return FRICC_ERR_TERM;
+  }
+  if (!W || !out || !T) {
+    fricc_set_error("contract: null argument");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t* td = T->dims;
+  // W' = (key0, key1, q0, q1), out' = (p0, p1, q0, q1)
+  int64_t we[4], oe[4], wsp[4], osp[4];
+  for (int j = 0; j < 4; ++j) {
+    we[j] = Wd[ts->permW[j]];
+    wsp[j] = Ws[ts->permW[j]];
+    oe[j] = Od[ts->permO[j]];
+    osp[j] = Os[ts->permO[j]];
+  }
+  if (we[0] != td[ts->ka] || we[1] != td[ts->kb] || oe[0] != td[ts->pa] || oe[1] != td[ts->pb] || we[2] != oe[2] ||
+      we[3] != oe[3]) {
+    fricc_set_error(
+        "contract %s: shapes do not match the sparse tensor dims (W %lldx%lldx%lldx%lld, out %lldx%lldx%lldx%lld, "
+        "T %lldx%lldx%lldx%lld)",
+        ts->name, (long long)Wd[0], (long long)Wd[1], (long long)Wd[2], (long long)Wd[3], (long long)Od[0],
+        (long long)Od[1], (long long)Od[2], (long long)Od[3], (long long)td[0], (long long)td[1], (long long)td[2],
+        (long long)td[3]);
+    return FRICC_ERR_ARG;
+  }
+  const int64_t QS = we[2] * we[3];
+  const int64_t nW = we[0] * we[1] * QS;
+  const int64_t nO = oe[0] * oe[1] * QS;
+  if (T->m == 0 || nO == 0) return FRICC_OK;
+
+  Bucketing* bk = nullptr;
+  int rc = fricc_sparse_bucketing(T, ts->pa, ts->pb, st, &bk);
+  if (rc) return rc;
+
+  const bool w_direct = is_contig_perm(Wd, Ws, ts->permW);
+  const bool o_direct = is_contig_perm(Od, Os, ts->permO);
+  double* Wp = nullptr;
+  double* Op = nullptr;
+  int* erow = nullptr;
+  double* eval = nullptr;
+  rc = fricc_alloc_t(&erow, T->m, st);
+  if (!rc) rc = fricc_alloc_t(&eval, T->m, st);
+  if (!rc && !w_direct) rc = fricc_alloc_t(&Wp, nW, st);
+  if (!rc && !o_direct) rc = fricc_alloc_t(&Op, nO, st);
+  if (!rc) {
+    k_entries<<<grid_for(T->m, 256), 256, 0, st>>>(T->slots, T->vals, bk->order, T->m, ts->ka, ts->kb, td[ts->kb],
+                                                   ts->coef, erow, eval);
+    if (!w_direct)
+      k_gather4<<<grid_for(nW, 256), 256, 0, st>>>(W, wsp[0], wsp[1], wsp[2], wsp[3], we[0], we[1], we[2], we[3], Wp);
+    if (!o_direct)
+      k_gather4<<<grid_for(nO, 256), 256, 0, st>>>(out, osp[0], osp[1], osp[2], osp[3], oe[0], oe[1], oe[2], oe[3],
+                                                   Op);
+    const double* Wuse = w_direct ? W : Wp;
+    double* Ouse = o_direct ? out : Op;
+    const int64_t ntq = fricc_cdiv(QS, SP_NT * SP_QPT);
+    if (ntq > 65535 || bk->nbuckets > 0x7fffffffLL) {
+      fricc_set_error("contract %s: problem too large for one launch", ts->name);
+      rc = FRICC_ERR_ARG;
+    } else {
+      dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq);
+      k_spmm<<<grid, SP_NT, 0, st>>>(bk->bptr, erow, eval, Wuse, Ouse, QS);
+      if (!o_direct)
+        k_scatter4<<<grid_for(nO, 256), 256, 0, st>>>(Op, osp[0], osp[1], osp[2], osp[3], oe[0], oe[1], oe[2], oe[3],
+                                                      out);
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) rc = fricc_cuda_fail(e, "contract", __FILE__, __LINE__);
+    }
+  }
+  fricc_free(erow, st);
+  fricc_free(eval, st);
+  fricc_free(Wp, st);
+  fricc_free(Op, st);
+  return rc;
+}
+
+// Flop count of one term (2 per multiply-add), for roofline accounting.
+double fricc_contract_flops_impl(const char* term, const FriccSparse* T) {
+  const TermSpec* ts = find_term(term);
+  if (!ts || !T) return 0.0;
+  const double o = (double)T->dims[0], v = (double)T->dims[2];
+  double q = o * v;                                                // the O^3V^3 terms
+  if (std::strcmp(ts->name, "2323") == 0) q = v * v;               // O^2V^4
+  else if (std::strcmp(ts->name, "0101") == 0 || std::strcmp(ts->name, "1323") == 0) q = o * o;  // O^4V^2
+  return 2.0 * (double)T->m * q;
+}

@@ -1,0 +1,134 @@
+// Stable LSD radix sort of (uint64 key, uint32 value) pairs, 8-bit digits.
+//
+// Used twice on the FRI path: to order the top-m candidates by descending
+// |x| with ties in ascending flat index (the order a stable merge sort by
+// |x| gives, fri-cc src/fri_utils.cpp:22-25), and to bucket the nonzeros
+// of a SparseTensor4d by an index pair while keeping nonzero-slot order
+// inside each bucket (the accumulation order of src/sparse_tensor.cpp).
+#pragma once
+#include "common.cuh"
+
+namespace radix {
+
+constexpr int NT = 256;
+constexpr int IPT = 8;
+constexpr int TILE = NT * IPT;
+
+__device__ __forceinline__ unsigned digit(unsigned long long k, int shift, int desc) {
+  const unsigned d = (unsigned)(k >> shift) & 255u;
+  return desc ? 255u - d : d;
+}
+
+static __global__ void __launch_bounds__(NT) k_hist(const unsigned long long* __restrict__ keys, int64_t n, int shift,
+                                             int desc, unsigned* __restrict__ hist, int64_t ntiles) {
+  __shared__ unsigned h[256];
+  h[threadIdx.x] = 0;
+  __syncthreads();
+  const int64_t base = (int64_t)blockIdx.x * TILE;
+#pragma unroll
+  for (int r = 0; r < IPT; ++r) {
+    const int64_t i = base + r * NT + threadIdx.x;
+    if (i < n) atomicAdd(&h[digit(keys[i], shift, desc)], 1u);
+  }
+  __syncthreads();
+  hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
+}
+
+// In-place exclusive scan of len uint32 counts (digit-major), one block.
+static __global__ void __launch_bounds__(1024) k_scan(unsigned* hist, int64_t len) {
+  __shared__ int64_t sm[33];
+  const int64_t per = fricc_cdiv(len, 1024);
+  const int64_t b = threadIdx.x * per;
+  const int64_t e = b + per < len ? b + per : len;
+  int64_t loc = 0;
+  for (int64_t i = b; i < e; ++i) loc += hist[i];
+  int64_t tot;
+  int64_t run = block_excl_sum(loc, sm, &tot);
+  for (int64_t i = b; i < e; ++i) {
+    const unsigned c = hist[i];
+    hist[i] = (unsigned)run;
+    run += c;
+  }
+}
+
+static __global__ void __launch_bounds__(NT) k_scatter(const unsigned long long* __restrict__ kin,
+                                                const unsigned* __restrict__ vin,
+                                                unsigned long long* __restrict__ kout, unsigned* __restrict__ vout,
+                                                int64_t n, int shift, int desc, const unsigned* __restrict__ offs,
+                                                int64_t ntiles) {
+  constexpr int NW = NT / 32;
+  __shared__ unsigned run[256];
+  __shared__ unsigned wc[NW][256];
+  run[threadIdx.x] = offs[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+  unsigned lt;
+  asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
+  const int w = threadIdx.x >> 5;
+  const int64_t base = (int64_t)blockIdx.x * TILE;
+  for (int r = 0; r < IPT; ++r) {
+#pragma unroll
+    for (int k = 0; k < NW; ++k) wc[k][threadIdx.x] = 0;
+    __syncthreads();
+    const int64_t i = base + r * NT + threadIdx.x;
+    const bool valid = i < n;
+    unsigned long long key = 0;
+    unsigned val = 0;
+    unsigned d = 256;
+    if (valid) {
+      key = kin[i];
+      val = vin[i];
+      d = digit(key, shift, desc);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, d);
+    const unsigned lrank = __popc(peers & lt);
+    if (valid && lrank == 0) wc[w][d] = __popc(peers);
+    __syncthreads();
+    {
+      unsigned acc = run[threadIdx.x];
+#pragma unroll
+      for (int k = 0; k < NW; ++k) {
+        const unsigned c = wc[k][threadIdx.x];
+        wc[k][threadIdx.x] = acc;
+        acc += c;
+      }
+      run[threadIdx.x] = acc;
+    }
+    __syncthreads();
+    if (valid) {
+      const unsigned pos = wc[w][d] + lrank;
+      kout[pos] = key;
+      vout[pos] = val;
+    }
+    __syncthreads();
+  }
+}
+
+// Sorts n pairs on key bits [0, bits).  The result ends in (keys, vals); the
+// tmp buffers must hold n entries, hist 256*ceil(n/TILE) counts.
+inline int sort_pairs(unsigned long long* keys, unsigned* vals, unsigned long long* ktmp, unsigned* vtmp,
+                      int64_t n, int bits, bool desc, unsigned* hist, cudaStream_t st) {
+  if (n <= 1) return FRICC_OK;
+  if (n > 0xffffffffLL) return FRICC_ERR_ARG;
+  const int64_t ntiles = fricc_cdiv(n, TILE);
+  unsigned long long *ka = keys, *kb = ktmp;
+  unsigned *va = vals, *vb = vtmp;
+  int passes = 0;
+  for (int shift = 0; shift < bits; shift += 8, ++passes) {
+    k_hist<<<(unsigned)ntiles, NT, 0, st>>>(ka, n, shift, desc ? 1 : 0, hist, ntiles);
+    k_scan<<<1, 1024, 0, st>>>(hist, 256 * ntiles);
+    k_scatter<<<(unsigned)ntiles, NT, 0, st>>>(ka, va, kb, vb, n, shift, desc ? 1 : 0, hist, ntiles);
+    unsigned long long* tk = ka;
+    ka = kb;
+    kb = tk;
+    unsigned* tv = va;
+    va = vb;
+    vb = tv;
+  }
+  FRICC_LAUNCH_CHECK();
+  if (passes & 1) {
+    FRICC_CUDA(cudaMemcpyAsync(keys, ka, n * sizeof(unsigned long long), cudaMemcpyDeviceToDevice, st));
+    FRICC_CUDA(cudaMemcpyAsync(vals, va, n * sizeof(unsigned), cudaMemcpyDeviceToDevice, st));
+  }
+  return FRICC_OK;
+}
+
+}  // namespace radix

@@ -1,0 +1,30 @@
+// Device-resident SparseTensor4d: the m kept nonzeros of a compressed T2 in
+// the reference's slot order (include/sparse_tensor.hpp:13-100), plus the
+// bucketed (CSR) views the contraction kernels read.
+#pragma once
+#include "common.cuh"
+
+// One bucketing of the nonzeros by an ordered pair of index slots (pa, pb):
+// bucket P = slot[pa] * dims[pb] + slot[pb].  order[] lists the nonzero slots
+// of bucket P in ascending slot order between bptr[P] and bptr[P+1].
+struct Bucketing {
+  int pa = -1, pb = -1;
+  int64_t nbuckets = 0;
+  int* bptr = nullptr;       // [nbuckets + 1]
+  unsigned* order = nullptr; // [m]
+};
+
+struct FriccSparse {
+  int64_t dims[4] = {0, 0, 0, 0};
+  int64_t m = 0;            // kept nonzeros
+  int64_t n_largest = 0;    // |D|: entries kept exactly (compression "fri")
+  int64_t* flat = nullptr;  // [m] flat C-order index into the dense tensor
+  double* vals = nullptr;   // [m]
+  int* slots = nullptr;     // [m][4] unpacked (i, j, a, b)
+  Bucketing buck[6];
+  cudaStream_t owner_stream = nullptr;
+  int device = 0;
+};
+
+// Index of the cached bucketing for (pa, pb), building it on first use.
+int fricc_sparse_bucketing(FriccSparse* T, int pa, int pb, cudaStream_t st, Bucketing** out);

@@ -1,0 +1,300 @@
+"""GPU FRI-CCSD: the amplitude iteration of fri-cc's fricc/friccsd.py on GB300.
+
+``FRICCSDGPU`` keeps the integrals, the amplitudes and the two compressed
+T2 handles resident in HBM and runs ``update_amps`` (fricc/friccsd.py:29-301)
+and ``kernel`` (:379-456) on the device:
+
+* both FRI compressions per iteration (:100-117) on the CUDA library, bit
+  for bit the reference's, with the reference's draws (libc ``rand()`` by
+  default, in the reference's order: the T2-term compression first, then the
+  W-intermediate one);
+* the eleven compressed terms (:214, :227, :247-267, :316, :348-356, :372)
+  through ``fricc_contract``;
+* the denominators, the CCSD energy and the step norm fused in
+  ``fricc_energy_update``;
+* the dense remainder (Fock-like intermediates, the T1 equation, the dense
+  W builds) as cuBLAS GEMMs through torch.
+
+Settings are the reference's ``fri_settings`` keys.  The reference reads
+``fri_settings["unbiased"]`` (:109), a key its defaults never set (they set
+"unbias"); a missing key is treated as False here.  The running-average
+("unbiased") mode is not implemented.
+
+``update_amps_host`` is the end-to-end entry: host (numpy) amplitudes in,
+host amplitudes out, the copies included.
+"""
+from __future__ import annotations
+
+import ctypes
+import time
+
+import numpy as np
+import torch
+
+from . import _lib as L
+from . import rccsd_dense as D
+from .py_rccsd import libc_uniform
+
+ALLOWED_CONTRACTIONS = ("O^2V^4", "O^3V^3", "O^4V^2")
+DEFAULT_SETTINGS = {
+    "m_keep": 1000,
+    "compression": "fri",
+    "sampling_method": "systematic",
+    "verbose": False,
+    "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"],
+    "burn_in": 100,
+    "unbias": False,
+}
+
+
+def _ptr(t: torch.Tensor) -> ctypes.c_void_p:
+    return ctypes.c_void_p(t.data_ptr())
+
+
+def _sym(x):
+    return x + x.permute(1, 0, 3, 2)
+
+
+class _Handle:
+    """A reusable compressed-T2 handle (device SparseTensor4d)."""
+
+    def __init__(self):
+        self.h = ctypes.c_void_p()
+        self.key = None
+
+    def compress(self, t2, m, compression, rn, stream):
+        lib = L.load()
+        key = (tuple(t2.shape), int(m))
+        comp = L.COMPRESSION[compression]
+        if self.h.value and self.key == key:
+            L.check(lib.fricc_sp_recompress(self.h, _ptr(t2), comp, 0, float(rn), stream))
+        else:
+            self.free()
+            L.check(lib.fricc_sp_create(_ptr(t2), L.i64arr(t2.shape), int(m), comp, 0, float(rn), stream,
+                                        ctypes.byref(self.h)))
+            self.key = key
+        return self.h
+
+    def free(self):
+        if self.h.value and L._lib is not None:
+            L._lib.fricc_sp_destroy(self.h)
+        self.h = ctypes.c_void_p()
+
+    def __del__(self):
+        self.free()
+
+
+class FRICCSDGPU:
+    def __init__(self, eris: D.DeviceERIs, fri_settings=None, level_shift=0.0, rn_draw=libc_uniform,
+                 wvvvv_t1t1="reference"):
+        s = dict(DEFAULT_SETTINGS)
+        s.update(fri_settings or {})
+        for c in s["compressed_contractions"]:
+            if c not in ALLOWED_CONTRACTIONS:
+                raise ValueError(f"Contraction ({c}) is not supported!")
+        if s["compression"] not in L.COMPRESSION:
+            raise ValueError(f"The compression method you chose ({s['compression']}) isn't supported")
+        if s["compression"] == "fri" and s["sampling_method"] != "systematic":
+            raise NotImplementedError("sampling_method 'pivotal' is not implemented on the GPU path")
+        if s.get("unbiased", False):
+            raise NotImplementedError("the running-average ('unbiased') mode is not implemented")
+        self.settings = s
+        self.eris = eris
+        self.level_shift = float(level_shift)
+        self.rn_draw = rn_draw
+        self.wvvvv_t1t1 = wvvvv_t1t1
+        self.lib = L.load()
+        self._sp = _Handle()
+        self._sp_w = _Handle()
+        self._res = torch.zeros(4, dtype=torch.float64, device=eris.device)
+        self._wT = None
+        self.timings = {}
+        self.last_energy = None
+        self.last_normt = None
+        self.launches = 0
+
+    # ------------------------------------------------------------------
+    def _contract(self, term, W, T, out, stream):
+        L.check(self.lib.fricc_contract(term.encode(), _ptr(W), L.i64arr(W.shape), L.i64arr(W.stride()), T,
+                                        _ptr(out), L.i64arr(out.shape), L.i64arr(out.stride()), stream))
+
+    def update_amps(self, t1, t2, rn=None, t1_old=None, t2_old=None):
+        """One iteration on device tensors; returns (t1new, t2new).
+
+        rn: the two uniform draws (compression #1, #2); default rn_draw().
+        After the call, last_energy is E_corr(t1new, t2new) and last_normt the
+        step norm against (t1_old, t2_old) (default: the inputs).
+        """
+        E = self.eris
+        s = self.settings
+        m = int(s["m_keep"])
+        if m > t2.numel() or m == 0:
+            raise ValueError("Bad m_keep value! The following condition wasn't met 0 < m_keep <= t2.size")
+        comp = s["compressed_contractions"]
+        o, v = t1.shape
+        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        t2 = t2.contiguous()
+        e_o = E.mo_energy[:o]
+        e_v = E.mo_energy[o:] + self.level_shift
+        fov = E.fock[:o, o:]
+        need_w = "O^3V^3" in comp or "O^4V^2" in comp
+        if rn is None:
+            kind = s["compression"]
+            rn = [self.rn_draw() if kind == "fri" else 0.0 for _ in range(2 if need_w else 1)]
+        T = self._sp.compress(t2, m, s["compression"], rn[0], st)
+        Tw = self._sp_w.compress(t2, m, s["compression"], rn[1], st) if need_w else None
+
+        Foo = D.cc_Foo(t1, t2, E)
+        Fvv = D.cc_Fvv(t1, t2, E)
+        Fov = D.cc_Fov(t1, t2, E)
+        Foo.diagonal().sub_(e_o)
+        Fvv.diagonal().sub_(e_v)
+
+        ein = torch.einsum
+        # T1 equation (fricc/friccsd.py:153-176)
+        t1new = -2 * ein("kc,ka,ic->ia", fov, t1, t1)
+        t1new += ein("ac,ic->ia", Fvv, t1)
+        t1new += -ein("ki,ka->ia", Foo, t1)
+        t1new += 2 * ein("kc,kica->ia", Fov, t2)
+        t1new += -ein("kc,ikca->ia", Fov, t2)
+        t1new += ein("kc,ic,ka->ia", Fov, t1, t1)
+        t1new += fov
+        t1new += 2 * ein("kcai,kc->ia", E.ovvo, t1)
+        t1new += -ein("kiac,kc->ia", E.oovv, t1)
+        t1new += 2 * ein("kdac,ikcd->ia", E.ovvv, t2)
+        t1new += -ein("kcad,ikcd->ia", E.ovvv, t2)
+        t1new += 2 * ein("kdac,kd,ic->ia", E.ovvv, t1, t1)
+        t1new += -ein("kcad,kd,ic->ia", E.ovvv, t1, t1)
+        t1new += -2 * ein("lcki,klac->ia", E.ovoo, t2)
+        t1new += ein("kcli,klac->ia", E.ovoo, t2)
+        t1new += -2 * ein("lcki,lc,ka->ia", E.ovoo, t1, t1)
+        t1new += ein("kcli,lc,ka->ia", E.ovoo, t1, t1)
+
+        # T2 driver terms (:179-187)
+        tmp2 = ein("kibc,ka->abic", E.oovv, -t1) + E.ovvv.permute(1, 3, 0, 2)
+        t2new = _sym(ein("abic,jc->ijab", tmp2, t1))
+        tmp2 = ein("kcai,jc->akij", E.ovvo, t1) + E.ovoo.permute(1, 3, 0, 2)
+        t2new -= _sym(ein("akij,kb->ijab", tmp2, t1))
+        t2new += E.ovov.permute(0, 2, 1, 3)
+        t2new = t2new.contiguous()
+
+        Loo = D.Loo(t1, t2, E)
+        Lvv = D.Lvv(t1, t2, E)
+        Loo.diagonal().sub_(e_o)
+        Lvv.diagonal().sub_(e_v)
+
+        if "O^4V^2" in comp:  # sparse_cc_Woooo (:309-322)
+            Woooo = ein("lcki,jc->klij", E.ovoo, t1) + ein("kclj,ic->klij", E.ovoo, t1)
+            Woooo = Woooo.contiguous()
+            self._contract("1323", E.ovov, Tw, Woooo, st)
+            Woooo += ein("kcld,ic,jd->klij", E.ovov, t1, t1)
+            Woooo += E.oooo.permute(0, 2, 1, 3)
+        else:
+            Woooo = D.cc_Woooo(t1, t2, E)
+
+        if "O^3V^3" in comp:  # sparse_cc_Wvoov / sparse_cc_Wvovo (:334-376)
+            Wvoov = (ein("kcad,id->akic", E.ovvv, t1) - ein("kcli,la->akic", E.ovoo, t1)
+                     + E.ovvo.permute(2, 0, 3, 1)).contiguous()
+            self._contract("0112", E.ovov, Tw, Wvoov, st)
+            self._contract("0313", E.ovov, Tw, Wvoov, st)
+            self._contract("0113", E.ovov, Tw, Wvoov, st)
+            Wvoov -= ein("ldkc,id,la->akic", E.ovov, t1, t1)
+            Wvovo = (ein("kdac,id->akci", E.ovvv, t1) - ein("lcki,la->akci", E.ovoo, t1)
+                     + E.oovv.permute(2, 0, 3, 1)).contiguous()
+            self._contract("0312", E.ovov, Tw, Wvovo, st)
+            Wvovo -= ein("lckd,id,la->akci", E.ovov, t1, t1)
+        else:
+            Wvoov = D.cc_Wvoov(t1, t2, E)
+            Wvovo = D.cc_Wvovo(t1, t2, E)
+
+        if self._wT is None or self._wT.shape != E.vvvvT.shape:
+            self._wT = torch.empty_like(E.vvvvT)
+        WT = D.wvvvv_T(t1, E, out=self._wT)  # Wvvvv as [c,d,a,b] (:325-331)
+        Wvvvv = WT.permute(2, 3, 0, 1)        # the (a,b,c,d) view
+
+        if "O^4V^2" in comp:
+            t2new += ein("klij,ka,lb->ijab", Woooo, t1, t1)
+            self._contract("0101", Woooo, T, t2new, st)
+        else:
+            tau = t2 + ein("ia,jb->ijab", t1, t1)
+            t2new += ein("klij,klab->ijab", Woooo, tau)
+
+        if self.wvvvv_t1t1 == "reference":
+            # fricc/friccsd.py:222: einsum("abcd,ia,jb->ijab") sums c,d inside W
+            S = WT.sum(dim=(0, 1))
+            t2new += S[None, None, :, :] * t1[:, None, :, None] * t1[None, :, None, :]
+        else:
+            t2new += ein("abcd,ic,jd->ijab", Wvvvv, t1, t1)
+        if "O^2V^4" in comp:
+            self._contract("2323", Wvvvv, T, t2new, st)
+        else:
+            t2new += ein("abcd,ijcd->ijab", Wvvvv, t2)
+
+        t2new += _sym(ein("ac,ijcb->ijab", Lvv, t2))
+        t2new -= _sym(ein("ki,kjab->ijab", Loo, t2))
+
+        if "O^3V^3" in comp:
+            tmp = torch.zeros_like(t2new)
+            self._contract("1302", Wvoov, T, tmp, st)
+            self._contract("1202", Wvovo, T, tmp, st)
+            t2new += _sym(tmp)
+            tmp.zero_()
+            self._contract("1303", Wvoov, T, tmp, st)
+            t2new -= _sym(tmp)
+            tmp.zero_()
+            self._contract("1203", Wvovo, T, tmp, st)
+            t2new -= _sym(tmp)
+        else:
+            tmp = 2 * ein("akic,kjcb->ijab", Wvoov, t2) - ein("akci,kjcb->ijab", Wvovo, t2)
+            t2new += _sym(tmp)
+            t2new -= _sym(ein("akic,kjbc->ijab", Wvoov, t2))
+            t2new -= _sym(ein("bkci,kjac->ijab", Wvovo, t2))
+
+        # denominators + energy + step norm (:281-284, :418-427)
+        eia = (e_o[:, None] - e_v[None, :]).contiguous()
+        t1new = t1new.contiguous()
+        t2new = t2new.contiguous()
+        t1o = t1 if t1_old is None else t1_old
+        t2o = t2 if t2_old is None else t2_old
+        L.check(self.lib.fricc_energy_update(_ptr(t1new), _ptr(t2new), _ptr(eia), _ptr(fov.contiguous()),
+                                             _ptr(E.ovov), _ptr(t1o.contiguous()), _ptr(t2o.contiguous()), o, v,
+                                             _ptr(t1new), _ptr(t2new), _ptr(self._res), st))
+        return t1new, t2new
+
+    def read_energy(self):
+        r = self._res[:2].cpu()
+        self.last_energy, self.last_normt = float(r[0]), float(r[1])
+        return self.last_energy, self.last_normt
+
+    def energy(self, t1, t2):
+        return D.ccsd_energy(t1, t2, self.eris)
+
+    def update_amps_host(self, t1_host: np.ndarray, t2_host: np.ndarray, rn=None):
+        """End-to-end step: numpy amplitudes in (copied to HBM), numpy out."""
+        t1 = torch.from_numpy(t1_host).to(self.eris.device, non_blocking=True)
+        t2 = torch.from_numpy(t2_host).to(self.eris.device, non_blocking=True)
+        t1n, t2n = self.update_amps(t1, t2, rn=rn)
+        return t1n.cpu().numpy(), t2n.cpu().numpy()
+
+    def kernel(self, t1=None, t2=None, max_cycle=50, tol=1e-8, tolnormt=1e-6, callback=None):
+        """The iteration loop of fricc/friccsd.py:379-456 (no DIIS).
+        Returns (converged, e_corr, t1, t2, energies)."""
+        if t1 is None or t2 is None:
+            raise ValueError("pass initial amplitudes (e.g. MP2) as device tensors")
+        eold, ecc = 0.0, self.energy(t1, t2)
+        energies = []
+        conv = False
+        for it in range(max_cycle):
+            t1, t2 = self.update_amps(t1, t2)
+            eold = ecc
+            ecc, normt = self.read_energy()
+            energies.append(ecc)
+            if callback is not None:
+                callback(it, t1, t2, ecc)
+            if abs(ecc - eold) < tol and normt < tolnormt:
+                conv = True
+                break
+            if np.isnan(ecc - eold) or abs(ecc - eold) > 1e5:
+                conv = False
+                break
+        return conv, ecc, t1, t2, energies

@@ -1,0 +1,85 @@
+"""Seeded synthetic closed-shell systems for FRI-CCSD.
+
+A system is defined by (nocc, nvir, naux, sigma, seed):
+
+* orbital energies: occupied uniform in [-1.5, -0.3] Eh, virtual uniform in
+  [0.2, 3.0] Eh, each sorted ascending; the Fock matrix is diagonal, so the
+  occupied-virtual block f_ov is zero;
+* two-electron integrals in chemists' notation
+  (pq|rs) = sum_P L[P,p,q] L[P,r,s], with L symmetric in (p,q) and its
+  independent entries drawn N(0, sigma^2);
+* amplitudes start at T1 = 0 and T2 = MP2, t_ijab = (ia|jb) / (e_i+e_j-e_a-e_b).
+
+These are the stand-in inputs for the reference's molecular runs (PySCF
+SCF on real molecules is not available); the named workloads below carry the
+sizes used by the tests and the benchmark.
+"""
+from __future__ import annotations
+
+from dataclasses import dataclass, field
+
+import numpy as np
+
+# Named workloads: nocc, nvir, naux, sigma, m (kept nonzeros), iterations.
+WORKLOADS = {
+    "o10v40": dict(nocc=10, nvir=40, naux=200, sigma=0.05, m=20000, iters=20),
+    "o30v150": dict(nocc=30, nvir=150, naux=900, sigma=0.03, m=2_000_000, iters=30),
+    "o20v100x64": dict(nocc=20, nvir=100, naux=600, sigma=0.04, m=200_000, iters=30, replicas=64),
+    "o40v200": dict(nocc=40, nvir=200, naux=1200, sigma=0.025, m=3_200_000, iters=40),
+}
+
+
+@dataclass
+class SyntheticSystem:
+    nocc: int
+    nvir: int
+    naux: int
+    sigma: float
+    seed: int = 0
+    mo_energy: np.ndarray = field(init=False)
+    L: np.ndarray = field(init=False)  # (naux, nmo, nmo), symmetric in the last two
+
+    def __post_init__(self):
+        rng = np.random.default_rng(self.seed)
+        eo = np.sort(rng.uniform(-1.5, -0.3, self.nocc))
+        ev = np.sort(rng.uniform(0.2, 3.0, self.nvir))
+        self.mo_energy = np.concatenate([eo, ev])
+        nmo = self.nmo
+        A = rng.standard_normal((self.naux, nmo, nmo)) * self.sigma
+        up = np.triu(A)
+        self.L = up + np.transpose(np.triu(A, 1), (0, 2, 1))
+
+    @property
+    def nmo(self) -> int:
+        return self.nocc + self.nvir
+
+    @property
+    def fock(self) -> np.ndarray:
+        return np.diag(self.mo_energy)
+
+    def _sl(self, c):
+        return slice(0, self.nocc) if c == "o" else slice(self.nocc, self.nmo)
+
+    def eri(self, block: str) -> np.ndarray:
+        """Chemists'-notation block, e.g. eri('ovov')[i,a,j,b] = (ia|jb), FP64 numpy."""
+        p, q, r, s = (self._sl(c) for c in block)
+        Lpq = self.L[:, p, q]
+        Lrs = self.L[:, r, s]
+        n1, n2 = Lpq.shape[1:]
+        n3, n4 = Lrs.shape[1:]
+        g = Lpq.reshape(self.naux, -1).T @ Lrs.reshape(self.naux, -1)
+        return g.reshape(n1, n2, n3, n4)
+
+    def mp2_amplitudes(self):
+        o = self.nocc
+        eo, ev = self.mo_energy[:o], self.mo_energy[o:]
+        eia = eo[:, None] - ev[None, :]
+        eijab = eia[:, None, :, None] + eia[None, :, None, :]
+        t2 = self.eri("ovov").transpose(0, 2, 1, 3) / eijab
+        t1 = np.zeros((o, self.nvir))
+        return t1, np.ascontiguousarray(t2)
+
+
+def make_system(name: str, seed: int = 0) -> SyntheticSystem:
+    w = WORKLOADS[name]
+    return SyntheticSystem(w["nocc"], w["nvir"], w["naux"], w["sigma"], seed)

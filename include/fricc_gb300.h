@@ -1,0 +1,130 @@
+/*
+ * fricc_gb300.h -- C ABI of the GB300 (sm_103a) FRI-CCSD hot path.
+ *
+ * Plain pointers and sizes only.  Every function returns an int status:
+ * FRICC_OK (0) or one of the FRICC_ERR_* codes, with a message available
+ * from fricc_last_error() (thread-local).  The reference terminates the
+ * process instead (exit(EXIT_FAILURE)); these entry points never do.
+ *
+ * Device pointers are CUDA global-memory addresses on the current device.
+ * `stream` is a cudaStream_t (NULL = the legacy default stream).  Functions
+ * are stream-ordered unless stated; those that return host values
+ * synchronise the stream they are given.  Strides are in ELEMENTS.
+ *
+ * Reference interfaces replaced (fri-cc, by file:line):
+ *   fricc_sp_create        SparseTensor4d(tensor_arr, dims, m, compression,
+ *                          sampling_method, verbose)  include/sparse_tensor.hpp:33-77,
+ *                          binding src/py_rccsd.cpp:34-39
+ *   fricc_sp_create_empty  SparseTensor4d(dims, nnz)  include/sparse_tensor.hpp:27-31,
+ *                          binding src/py_rccsd.cpp:33
+ *   fricc_sp_get           SparseTensor4d::get_element  include/sparse_tensor.hpp:138-143,
+ *                          binding src/py_rccsd.cpp:40-46
+ *   fricc_sp_export        (bulk get_element; the reference has none)
+ *   fricc_contract         contract_SparseTensor4d_wrapper  src/sparse_tensor.cpp:349-382,
+ *                          binding "contract_DTSpT" src/py_rccsd.cpp:50-51
+ *   fricc_compress         fri_compression  src/fri_utils.cpp:439-522 (systematic) and
+ *                          argsort-based "largest" include/sparse_tensor.hpp:46-56
+ *   fricc_seq_cumsum       the running sums of one_norm src/fri_utils.cpp:164-171 and of
+ *                          std::partial_sum in sample_systematic :142-143
+ *   fricc_energy_update    the denominator update of update_amps fricc/friccsd.py:281-284,
+ *                          the CCSD energy and the step norm of kernel :418-427
+ */
+#ifndef FRICC_GB300_H
+#define FRICC_GB300_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FRICC_OK 0
+#define FRICC_ERR_ARG 1          /* bad argument (sizes, m, dims, null) */
+#define FRICC_ERR_TERM 2         /* unknown contraction term */
+#define FRICC_ERR_P_GT_ONE 3     /* a sampling probability exceeded 1 */
+#define FRICC_ERR_CUDA 4         /* a CUDA runtime call failed */
+#define FRICC_ERR_TIMEOUT 5      /* a bounded device-side wait gave up */
+#define FRICC_ERR_INDEX 6        /* an index fell outside dims */
+#define FRICC_ERR_UNSUPPORTED 7  /* mode not implemented on this path */
+
+#define FRICC_COMPRESSION_FRI 0
+#define FRICC_COMPRESSION_LARGEST 1
+#define FRICC_SAMPLING_SYSTEMATIC 0
+#define FRICC_SAMPLING_PIVOTAL 1
+
+typedef struct FriccSparse fricc_sparse; /* opaque device-resident SparseTensor4d */
+
+/* Library version (major*10000 + minor*100 + patch). */
+int fricc_version(void);
+
+/* Message of the last failing call on this thread ("" if none). */
+const char* fricc_last_error(void);
+
+/* Compress the dense C-order tensor t2 (device, dims[0]*dims[1]*dims[2]*dims[3]
+ * doubles) keeping m nonzeros.  compression: FRICC_COMPRESSION_FRI (sampling
+ * must be FRICC_SAMPLING_SYSTEMATIC; rn is the one uniform draw
+ * rand()/RAND_MAX the reference consumes) or FRICC_COMPRESSION_LARGEST (rn
+ * unused).  Entries come out in the reference's slot order: the exactly kept
+ * largest entries in descending |t| (ties by ascending flat index), then the
+ * sampled ones in ascending flat index.  Synchronises `stream`. */
+int fricc_sp_create(const double* t2, const int64_t dims[4], int64_t m, int compression, int sampling, double rn,
+                    void* stream, fricc_sparse** out);
+
+/* Re-compress into an existing handle (same dims and m), reusing its memory. */
+int fricc_sp_recompress(fricc_sparse* T, const double* t2, int compression, int sampling, double rn, void* stream);
+
+/* An all-zero tensor of nnz entries (index 0, value 0). */
+int fricc_sp_create_empty(const int64_t dims[4], int64_t nnz, void* stream, fricc_sparse** out);
+
+int fricc_sp_destroy(fricc_sparse* T);
+
+/* dims, number of entries, and |D| (entries kept exactly, FRI only). */
+int fricc_sp_info(const fricc_sparse* T, int64_t dims[4], int64_t* m, int64_t* n_largest);
+
+/* Entry mi: unpacked index and value (synchronous device-to-host read). */
+int fricc_sp_get(const fricc_sparse* T, int64_t mi, int64_t idx[4], double* value);
+
+/* All entries to host memory: flat C-order index and value (either may be NULL). */
+int fricc_sp_export(const fricc_sparse* T, int64_t* flat_host, double* vals_host, void* stream);
+
+/* Device arrays of the handle: flat[m] (int64), vals[m] (double), slots[m][4] (int32). */
+int fricc_sp_device_arrays(const fricc_sparse* T, const int64_t** flat, const double** vals, const int** slots);
+
+/* out (device, any strides) += the term's contraction of W (device, any
+ * strides) with T.  term is one of "0101", "2323", "1302", "1202", "1303",
+ * "1203", "1323", "0112", "0113", "0313", "0312".  Each term reads
+ * W'[key0,key1,q0,q1] and out'[p0,p1,q0,q1], where (p0,p1) are the two
+ * index slots the reference's outer loop fixes, (key0,key1) the slots that
+ * index W and (q0,q1) the inner dense loop; e.g. "2323" reads W as (c,d,a,b)
+ * and out as (i,j,a,b).  A W or out whose strides already give that
+ * contiguous layout is used in place; any other layout is gathered into a
+ * permuted copy (and out scattered back).  Stream-ordered. */
+int fricc_contract(const char* term, const double* W, const int64_t W_dims[4], const int64_t W_strides[4],
+                   fricc_sparse* T, double* out, const int64_t out_dims[4], const int64_t out_strides[4],
+                   void* stream);
+
+/* Floating-point operations of one contract call (2 per multiply-add). */
+double fricc_contract_flops(const char* term, const fricc_sparse* T);
+
+/* The bare FRI compression of n doubles: flat[m] (int64) and vals[m] to device
+ * memory, |D| to *n_largest (host).  Synchronises `stream`. */
+int fricc_compress(const double* x, int64_t n, int64_t m, int compression, double rn, int64_t* flat, double* vals,
+                   int64_t* n_largest, void* stream);
+
+/* out[i] = fl(out[i-1] + |x[i]|) with out[-1] = 0 (device arrays of n
+ * doubles): the exact bits a single CPU thread's left-to-right FP64 sum
+ * produces, computed in parallel.  Stream-ordered. */
+int fricc_seq_cumsum(const double* x, int64_t n, double* out, void* stream);
+
+/* t1 = t1num/eia, t2 = t2num/(eia_ia + eia_jb); res[0] = E_corr of (t1, t2),
+ * res[1] = || (t1,t2) - (t1old,t2old) || in packed form.  All device, C order:
+ * t1* (o,v), t2* (o,o,v,v), eia (o,v), fov (o,v), ovov (o,v,o,v); res holds 4
+ * doubles.  t1out/t2out may alias t1num/t2num.  Stream-ordered. */
+int fricc_energy_update(const double* t1num, const double* t2num, const double* eia, const double* fov,
+                        const double* ovov, const double* t1old, const double* t2old, int64_t nocc, int64_t nvir,
+                        double* t1out, double* t2out, double* res, void* stream);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* FRICC_GB300_H */

@@ -1,0 +1,191 @@
+"""Generate the golden vectors in tests/golden/ from the reference itself.
+
+Runs only where the reference checkout is available (it reads
+/root/reference, or $FRICC_REFERENCE).  It compiles the reference's own
+py_rccsd module from its sources (``make -C oracle ref``), imports it, and
+records:
+
+* compress.npz  -- SparseTensor4d("fri"/"largest") outputs (index slots and
+                   values, bit for bit) on seeded inputs, with the libc
+                   ``rand()`` draw each "fri" call consumed;
+* contract.npz  -- contract_DTSpT outputs for all eleven terms, accumulated
+                   in place into a non-zero output, including strided W;
+* iteration.npz -- the reference's fricc/friccsd.py ``kernel`` run
+                   unmodified (on the PySCF stand-in in oracle/) for a small
+                   synthetic system: every iterate, every energy, every draw.
+
+Usage:  OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+"""
+from __future__ import annotations
+
+import ctypes
+import importlib.util
+import os
+import subprocess
+import sys
+import types
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+REPO = os.path.dirname(os.path.dirname(HERE))
+REF = os.environ.get("FRICC_REFERENCE", "/root/reference")
+sys.path.insert(0, REPO)
+
+from oracle import pyscf_standin  # noqa: E402
+from fricc_gb300.synthetic import SyntheticSystem  # noqa: E402
+
+TERMS = ("0101", "2323", "1302", "1202", "1303", "1203", "1323", "0112", "0113", "0313", "0312")
+W_SHAPE = {"0101": "oooo", "2323": "vvvv", "1302": "voov", "1202": "vovo", "1303": "voov",
+           "1203": "vovo", "1323": "ovov", "0112": "ovov", "0113": "ovov", "0313": "ovov",
+           "0312": "ovov"}
+OUT_SHAPE = {"1323": "oooo", "0112": "voov", "0113": "voov", "0313": "voov", "0312": "vovo"}
+
+
+def load_reference_module():
+    subprocess.run(["make", "-C", os.path.join(REPO, "oracle"), "ref", f"REF_DIR={REF}", "-s"],
+                   check=True)
+    sys.path.insert(0, os.path.join(REPO, "oracle", "_ref"))
+    import py_rccsd  # the reference's own module
+    return py_rccsd
+
+
+def load_reference_friccsd(py_rccsd):
+    pyscf_standin.install()
+    pkg = types.ModuleType("fricc")
+    pkg.__path__ = []
+    sys.modules["fricc"] = pkg
+    sys.modules["fricc.py_rccsd"] = py_rccsd
+    spec = importlib.util.spec_from_file_location("fricc.friccsd",
+                                                  os.path.join(REF, "fricc", "friccsd.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["fricc.friccsd"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+libc = ctypes.CDLL(None)
+
+
+def draws(seed, n):
+    libc.srand(seed)
+    return [libc.rand() / 2147483647.0 for _ in range(n)]
+
+
+def ref_sparse(R, x, m, kind, seed):
+    libc.srand(seed)
+    t = R.SparseTensor4d(x, x.shape, m, kind, "systematic", False)
+    idx = np.array([t.get_element(i)[0] for i in range(m)], dtype=np.int64).reshape(m, 4)
+    val = np.array([t.get_element(i)[1] for i in range(m)], dtype=np.float64)
+    return idx, val
+
+
+def compress_cases(R):
+    rng = np.random.default_rng(2024)
+    cases = []
+    # heavy-tailed small tensors, including ties, zeros, m = 1 and m = N
+    for c in range(14):
+        shp = tuple(int(s) for s in rng.integers(2, 7, size=4))
+        n = int(np.prod(shp))
+        x = rng.standard_normal(shp) * np.exp(2 * rng.standard_normal(shp))
+        if c % 4 == 1:
+            x = np.round(x)  # exact ties and zeros
+        if c % 4 == 2:
+            x[rng.random(shp) < 0.6] = 0.0
+        m = {0: 1, 3: n}.get(c, int(rng.integers(1, n + 1)))
+        cases.append((x, m))
+    # MP2 amplitudes of small synthetic systems
+    for (o, v, seed, frac) in ((6, 24, 1, 0.12), (6, 24, 2, 0.05), (5, 20, 3, 0.3)):
+        s = SyntheticSystem(o, v, 8 * (o + v), 0.05, seed)
+        x = s.mp2_amplitudes()[1]
+        cases.append((x, int(frac * x.size)))
+    out = {}
+    for k, (x, m) in enumerate(cases):
+        x = np.ascontiguousarray(x)
+        out[f"c{k}_x"] = x
+        out[f"c{k}_m"] = np.int64(m)
+        for kind in ("fri", "largest"):
+            seed = 100 + k
+            idx, val = ref_sparse(R, x, m, kind, seed)
+            key = f"c{k}_{kind}"
+            out[key + "_rn"] = np.float64(draws(seed, 1)[0] if kind == "fri" else -1.0)
+            out[key + "_idx"] = idx
+            out[key + "_val"] = val
+    out["n_cases"] = np.int64(len(cases))
+    return out
+
+
+def contract_cases(R):
+    rng = np.random.default_rng(77)
+    out = {}
+    for si, (no, nv, frac) in enumerate(((4, 8, 0.1), (5, 9, 0.05), (3, 7, 0.4))):
+        d = {"o": no, "v": nv}
+        t2 = np.zeros(no * no * nv * nv)
+        nz = rng.choice(t2.size, size=max(1, int(t2.size * frac)), replace=False)
+        t2[nz] = rng.standard_normal(nz.size)
+        t2 = t2.reshape(no, no, nv, nv)
+        m = nz.size
+        T = R.SparseTensor4d(t2, t2.shape, m, "largest")
+        for term in TERMS:
+            ws = tuple(d[c] for c in W_SHAPE[term])
+            osh = tuple(d[c] for c in OUT_SHAPE.get(term, "oovv"))
+            W = rng.standard_normal(ws)
+            out0 = rng.standard_normal(osh)
+            for strided in (0, 1):
+                Wuse = W if not strided else np.ascontiguousarray(W.transpose(3, 2, 1, 0)).transpose(3, 2, 1, 0)
+                o = out0.copy()
+                R.contract_DTSpT(Wuse, T, o, term)
+                out[f"s{si}_{term}_out{strided}"] = o
+            out[f"s{si}_{term}_W"] = W
+            out[f"s{si}_{term}_init"] = out0
+            out[f"s{si}_t2"] = t2
+            out[f"s{si}_m"] = np.int64(m)
+    return out
+
+
+def iteration_case(R):
+    F = load_reference_friccsd(R)
+    s = SyntheticSystem(4, 12, 60, 0.05, 7)
+    eris = pyscf_standin.make_eris(s)
+    settings = {"m_keep": 800, "compression": "fri", "sampling_method": "systematic",
+                "verbose": False, "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"],
+                "unbiased": False}
+
+    class Driver(pyscf_standin.CCSD):
+        def update_amps(self, t1, t2, eris):
+            return F.update_amps(self, t1, t2, eris)
+
+    cc = Driver(eris, settings)
+    n_iter = 8
+    cc.max_cycle = n_iter
+    t1, t2 = pyscf_standin.mp2_guess(eris)
+    iterates = [(t1, t2)]
+
+    def record(t1, t2, eris):
+        r = F.update_amps(cc, t1, t2, eris)
+        iterates.append(r)
+        return r
+
+    cc.update_amps = record
+    seed = 11
+    libc.srand(seed)
+    conv, e, _, _ = F.kernel(cc, eris, t1, t2)
+    return {
+        "L": s.L, "mo_energy": s.mo_energy, "nocc": np.int64(4), "m": np.int64(800),
+        "seed": np.int64(seed), "rn": np.array(draws(seed, 2 * n_iter)),
+        "energies": np.array(cc.energies),
+        "t1": np.stack([a for a, _ in iterates]), "t2": np.stack([b for _, b in iterates]),
+    }
+
+
+def main():
+    R = load_reference_module()
+    np.savez_compressed(os.path.join(HERE, "compress.npz"), **compress_cases(R))
+    np.savez_compressed(os.path.join(HERE, "contract.npz"), **contract_cases(R))
+    np.savez_compressed(os.path.join(HERE, "iteration.npz"), **iteration_case(R))
+    for f in ("compress.npz", "contract.npz", "iteration.npz"):
+        print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
+
+
+if __name__ == "__main__":
+    main()

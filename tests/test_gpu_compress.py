@@ -1,0 +1,126 @@
+"""GPU FRI compression against the oracle and the reference's golden vectors:
+indices, order and values bit for bit."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+
+def _gpu_sparse(x, m, kind, rn):
+    from fricc_gb300 import py_rccsd
+    t = py_rccsd.SparseTensor4d(x, x.shape, m, kind, "systematic", rn=rn if kind == "fri" else 0.0)
+    flat, vals = t.export()
+    idx = np.stack(np.unravel_index(flat, x.shape), axis=1)
+    return idx, vals, t
+
+
+def _same_bits(a, b):
+    return np.array_equal(np.asarray(a).view(np.int64), np.asarray(b).view(np.int64))
+
+
+def test_golden_bitexact(gpulib):
+    g = golden("compress.npz")
+    for k in range(int(g["n_cases"])):
+        x = g[f"c{k}_x"]
+        m = int(g[f"c{k}_m"])
+        for kind in ("fri", "largest"):
+            idx, vals, _ = _gpu_sparse(x, m, kind, float(g[f"c{k}_{kind}_rn"]))
+            np.testing.assert_array_equal(idx, g[f"c{k}_{kind}_idx"], err_msg=f"case {k} {kind}")
+            assert _same_bits(vals, g[f"c{k}_{kind}_val"]), f"case {k} {kind}"
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_mp2_o10v40_vs_oracle(gpulib, oracle, seed):
+    """The o10v40 workload (N = 160000, m = 20000), three draws."""
+    from fricc_gb300.synthetic import SyntheticSystem
+    s = SyntheticSystem(10, 40, 200, 0.05, seed)
+    x = s.mp2_amplitudes()[1]
+    rn = [0.8401877171547095, 0.3943829268190930, 0.7830992237586059][seed - 1]
+    idx, vals, t = _gpu_sparse(x, 20000, "fri", rn)
+    ref = oracle.SparseTensor4d(x, x.shape, 20000, "fri", "systematic", rn=rn)
+    np.testing.assert_array_equal(idx, ref.idx4)
+    assert _same_bits(vals, ref.vals)
+    assert t.n_largest() == ref.n_largest
+
+
+@pytest.mark.parametrize("n,m", [(1, 1), (7, 3), (4096, 100), (4097, 4097), (100_000, 1), (250_000, 60_000),
+                                 (300_001, 299_000)])
+def test_random_sizes_vs_oracle(gpulib, oracle, n, m):
+    rng = np.random.default_rng(n + m)
+    x = rng.standard_normal(n) * np.exp(3 * rng.standard_normal(n))
+    x = x.reshape(1, 1, 1, n)
+    rn = float(rng.random())
+    for kind in ("fri", "largest"):
+        idx, vals, _ = _gpu_sparse(x, m, kind, rn)
+        ref = oracle.SparseTensor4d(x, x.shape, m, kind, "systematic", rn=rn)
+        np.testing.assert_array_equal(idx, ref.idx4, err_msg=kind)
+        assert _same_bits(vals, ref.vals), kind
+
+
+def test_ties_zeros_and_degenerate(gpulib, oracle):
+    rng = np.random.default_rng(9)
+    cases = []
+    x = np.round(rng.standard_normal(50_000) * 3)  # many exact ties and zeros
+    cases.append((x, 9000))
+    x = np.zeros(20_000)
+    x[rng.choice(20_000, 300, replace=False)] = rng.standard_normal(300)
+    cases.append((x, 1000))  # m > nnz: remaining norm hits 0, samples keep index 0
+    x = np.full(10_000, 0.5)  # all equal
+    cases.append((x, 777))
+    y = rng.standard_normal(30_000)
+    y[::3] *= 1e-300  # subnormal and tiny values next to O(1) ones
+    cases.append((y, 5000))
+    for x, m in cases:
+        x = x.reshape(1, 1, 1, -1)
+        for rn in (0.0, 0.37, 1.0):
+            idx, vals, _ = _gpu_sparse(x, m, "fri", rn)
+            ref = oracle.SparseTensor4d(x, x.shape, m, "fri", "systematic", rn=rn)
+            np.testing.assert_array_equal(idx, ref.idx4)
+            assert _same_bits(vals, ref.vals)
+
+
+def test_exact_sequential_cumsum(gpulib):
+    """fricc_seq_cumsum reproduces a left-to-right FP64 running sum bit for bit
+    (numpy's add.accumulate is sequential) on adversarial inputs."""
+    import ctypes
+    from fricc_gb300 import _lib
+    rng = np.random.default_rng(4)
+    ulp_half = np.ldexp(1.0, -53)
+    cases = [
+        rng.random(1_000_003),
+        np.exp(40 * rng.standard_normal(200_000)),                  # huge dynamic range
+        np.concatenate([np.zeros(5000), rng.random(70_000)]),      # leading zeros
+        np.full(300_000, ulp_half),                                 # exact half-ulp ties against 1.0
+        np.concatenate([[1.0], np.full(100_000, ulp_half)]),        # ties, parity flips
+        np.concatenate([[1.0], np.tile([ulp_half, 3 * ulp_half], 50_000)]),
+        np.ldexp(1.0, rng.integers(-1074, -1000, 50_000)).astype(np.float64),  # subnormals
+        np.ldexp(1.0, np.arange(0, 200)).astype(np.float64),        # a binade crossing at every step
+        rng.random(4096) * 1e-3,
+        np.array([3.0]),
+    ]
+    for k, x in enumerate(cases):
+        xd = torch.from_numpy(np.ascontiguousarray(x)).cuda()
+        out = torch.empty_like(xd)
+        _lib.check(gpulib.fricc_seq_cumsum(ctypes.c_void_p(xd.data_ptr()), xd.numel(),
+                                           ctypes.c_void_p(out.data_ptr()),
+                                           ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+        ref = np.add.accumulate(np.abs(x))
+        got = out.cpu().numpy()
+        bad = np.flatnonzero(got.view(np.int64) != ref.view(np.int64))
+        assert bad.size == 0, f"case {k}: first mismatch at {bad[:3]} {got[bad[:3]]} vs {ref[bad[:3]]}"
+
+
+def test_errors_raise(gpulib):
+    from fricc_gb300 import py_rccsd
+    x = np.ones((2, 2, 2, 2))
+    with pytest.raises(ValueError):
+        py_rccsd.SparseTensor4d(x, x.shape, 17, "fri", "systematic")
+    with pytest.raises(ValueError):
+        py_rccsd.SparseTensor4d(x, x.shape, 4, "bogus", "systematic")
+    with pytest.raises(NotImplementedError):
+        py_rccsd.SparseTensor4d(x, x.shape, 4, "fri", "pivotal")
+    with pytest.raises(TypeError):
+        py_rccsd.SparseTensor4d(x.astype(np.float32), x.shape, 4, "fri", "systematic")

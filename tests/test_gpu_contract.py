@@ -1,0 +1,110 @@
+"""The eleven contraction terms on the GPU against the oracle (same nonzero
+order per output element; the GPU fuses each multiply-add, so the bound is
+a relative tolerance, not bit equality) and against the golden outputs of
+the reference's own contract_DTSpT.  Also the reference's own test pattern:
+each term equals np.einsum on a "largest"-compressed sparse T2."""
+import numpy as np
+import pytest
+import torch
+
+from conftest import golden
+
+pytestmark = pytest.mark.gpu
+
+TERMS = ("0101", "2323", "1302", "1202", "1303", "1203", "1323", "0112", "0113", "0313", "0312")
+W_SHAPE = {"0101": "oooo", "2323": "vvvv", "1302": "voov", "1202": "vovo", "1303": "voov", "1203": "vovo",
+           "1323": "ovov", "0112": "ovov", "0113": "ovov", "0313": "ovov", "0312": "ovov"}
+OUT_SHAPE = {"1323": "oooo", "0112": "voov", "0113": "voov", "0313": "voov", "0312": "vovo"}
+EINSUM = {"0101": ("klij,klab->ijab", 1.0), "2323": ("abcd,ijcd->ijab", 1.0), "1302": ("akic,kjcb->ijab", 2.0),
+          "1202": ("akci,kjcb->ijab", -1.0), "1303": ("akic,kjbc->ijab", 1.0), "1203": ("bkci,kjac->ijab", 1.0),
+          "1323": ("kcld,ijcd->klij", 1.0), "0112": ("ldkc,ilda->akic", -0.5), "0113": ("ldkc,ilad->akic", 1.0),
+          "0313": ("lckd,ilad->akic", -0.5), "0312": ("lckd,ilda->akci", -0.5)}
+RTOL = 1e-12  # relative to the largest |output| of the term
+
+
+def _close(a, b, rtol=RTOL):
+    scale = max(np.abs(b).max(), 1.0)
+    assert np.abs(a - b).max() <= rtol * scale, np.abs(a - b).max() / scale
+
+
+def test_golden(gpulib):
+    from fricc_gb300 import py_rccsd
+    g = golden("contract.npz")
+    for si in range(3):
+        t2 = g[f"s{si}_t2"]
+        T = py_rccsd.SparseTensor4d(t2, t2.shape, int(g[f"s{si}_m"]), "largest")
+        for term in TERMS:
+            W = g[f"s{si}_{term}_W"]
+            for strided in (0, 1):
+                Wuse = W if not strided else np.ascontiguousarray(W.transpose(3, 2, 1, 0)).transpose(3, 2, 1, 0)
+                out = g[f"s{si}_{term}_init"].copy()
+                py_rccsd.contract_DTSpT(Wuse, T, out, term)
+                _close(out, g[f"s{si}_{term}_out{strided}"])
+
+
+@pytest.mark.parametrize("no,nv,frac", [(4, 8, 0.1), (5, 10, 0.01), (10, 20, 0.001), (7, 31, 0.3)])
+def test_einsum_pattern(gpulib, no, nv, frac):
+    """fricc/tests/test_sparse_tensors.py: term(W, largest-compressed T) == einsum(W, T)."""
+    from fricc_gb300 import py_rccsd
+    rng = np.random.default_rng(int(no * 100 + nv))
+    d = {"o": no, "v": nv}
+    t2 = np.zeros(no * no * nv * nv)
+    nnz = max(1, int(t2.size * frac))
+    t2[rng.choice(t2.size, nnz, replace=False)] = rng.random(nnz)
+    t2 = t2.reshape(no, no, nv, nv)
+    T = py_rccsd.SparseTensor4d(t2, t2.shape, nnz, "largest")
+    for term in TERMS:
+        W = rng.random(tuple(d[c] for c in W_SHAPE[term]))
+        spec, coef = EINSUM[term]
+        ref = coef * np.einsum(spec, W, t2)
+        out = np.zeros(ref.shape)
+        py_rccsd.contract_DTSpT(W, T, out, term)
+        _close(out, ref)
+
+
+def test_vs_oracle_fri_tensor_and_device_views(gpulib, oracle):
+    """A FRI-compressed MP2 T2 (o10v40 sizes), W and out as torch CUDA views
+    with permuted strides, accumulated in place on top of nonzero data."""
+    from fricc_gb300 import py_rccsd
+    from fricc_gb300.synthetic import SyntheticSystem
+    s = SyntheticSystem(10, 40, 200, 0.05, 4)
+    x = s.mp2_amplitudes()[1]
+    rn = 0.25
+    T = py_rccsd.SparseTensor4d(x, x.shape, 20000, "fri", "systematic", rn=rn)
+    To = oracle.SparseTensor4d(x, x.shape, 20000, "fri", "systematic", rn=rn)
+    rng = np.random.default_rng(0)
+    d = {"o": 10, "v": 40}
+    for term in TERMS:
+        W = rng.standard_normal(tuple(d[c] for c in W_SHAPE[term]))
+        out0 = rng.standard_normal(tuple(d[c] for c in OUT_SHAPE.get(term, "oovv")))
+        ref = out0.copy()
+        oracle.contract_DTSpT(W, To, ref, term)
+        # device tensors stored transposed, passed as (W-shaped) strided views
+        Wd = torch.from_numpy(np.ascontiguousarray(W.transpose(2, 0, 3, 1))).cuda().permute(1, 3, 0, 2)
+        Od = torch.from_numpy(np.ascontiguousarray(out0.transpose(3, 1, 0, 2))).cuda().permute(2, 1, 3, 0)
+        py_rccsd.contract_DTSpT(Wd, T, Od, term)
+        _close(Od.cpu().numpy(), ref)
+
+
+def test_deterministic(gpulib):
+    from fricc_gb300 import py_rccsd
+    rng = np.random.default_rng(1)
+    x = rng.standard_normal((6, 6, 30, 30))
+    T = py_rccsd.SparseTensor4d(x, x.shape, 5000, "fri", "systematic", rn=0.5)
+    W = rng.standard_normal((30, 30, 30, 30))
+    outs = []
+    for _ in range(3):
+        o = np.zeros((6, 6, 30, 30))
+        py_rccsd.contract_DTSpT(W, T, o, "2323")
+        outs.append(o)
+    assert np.array_equal(outs[0], outs[1]) and np.array_equal(outs[1], outs[2])
+
+
+def test_bad_shapes_raise(gpulib):
+    from fricc_gb300 import py_rccsd
+    x = np.random.default_rng(2).standard_normal((3, 3, 5, 5))
+    T = py_rccsd.SparseTensor4d(x, x.shape, 20, "largest")
+    with pytest.raises(ValueError):
+        py_rccsd.contract_DTSpT(np.zeros((5, 5, 5, 4)), T, np.zeros((3, 3, 5, 5)), "2323")
+    with pytest.raises(ValueError):
+        py_rccsd.contract_DTSpT(np.zeros((5, 5, 5, 5)), T, np.zeros((3, 3, 5, 5)), "9999")

@@ -1,0 +1,92 @@
+"""The oracle (oracle/fri_oracle.c + oracle/ccsd_oracle.py) against golden
+vectors produced by the reference's own C++ and fricc/friccsd.py
+(tests/golden/make_golden.py).  CPU only."""
+import numpy as np
+import pytest
+
+from conftest import golden
+
+TERMS = ("0101", "2323", "1302", "1202", "1303", "1203", "1323", "0112", "0113", "0313", "0312")
+
+
+def test_compress_golden_bitexact(oracle):
+    g = golden("compress.npz")
+    n = int(g["n_cases"])
+    assert n >= 15
+    for k in range(n):
+        x = g[f"c{k}_x"]
+        m = int(g[f"c{k}_m"])
+        for kind in ("fri", "largest"):
+            rn = float(g[f"c{k}_{kind}_rn"]) if kind == "fri" else None
+            t = oracle.SparseTensor4d(x, x.shape, m, kind, "systematic", rn=rn)
+            ref_idx, ref_val = g[f"c{k}_{kind}_idx"], g[f"c{k}_{kind}_val"]
+            np.testing.assert_array_equal(t.idx4, ref_idx, err_msg=f"case {k} {kind}")
+            # bit for bit, NaN/inf included
+            assert np.array_equal(t.vals.view(np.int64), ref_val.view(np.int64)), f"case {k} {kind}"
+
+
+def test_contract_golden_bitexact(oracle):
+    g = golden("contract.npz")
+    for si in range(3):
+        t2 = g[f"s{si}_t2"]
+        m = int(g[f"s{si}_m"])
+        T = oracle.SparseTensor4d(t2, t2.shape, m, "largest")
+        for term in TERMS:
+            W = g[f"s{si}_{term}_W"]
+            for strided in (0, 1):
+                Wuse = W if not strided else np.ascontiguousarray(W.transpose(3, 2, 1, 0)).transpose(3, 2, 1, 0)
+                out = g[f"s{si}_{term}_init"].copy()
+                oracle.contract_DTSpT(Wuse, T, out, term)
+                np.testing.assert_array_equal(out, g[f"s{si}_{term}_out{strided}"], err_msg=f"{si} {term}")
+
+
+def _iteration_system():
+    from oracle import pyscf_standin as P
+    g = golden("iteration.npz")
+
+    class Sys:
+        pass
+
+    s = Sys()
+    s.nocc = int(g["nocc"])
+    s.L = g["L"]
+    s.mo_energy = g["mo_energy"]
+    s.nmo = s.mo_energy.size
+    s.nvir = s.nmo - s.nocc
+    s.fock = np.diag(s.mo_energy)
+    from fricc_gb300.synthetic import SyntheticSystem
+    s.eri = lambda b: SyntheticSystem.eri(s, b)
+    s._sl = lambda c: SyntheticSystem._sl(s, c)
+    s.naux = s.L.shape[0]
+    return g, P.make_eris(s)
+
+
+def test_iteration_golden_teacher_forced(oracle):
+    """Every reference iterate, fed to the oracle update with the same draws,
+    gives the next reference iterate."""
+    from oracle import ccsd_oracle as CO
+    g, eris = _iteration_system()
+    settings = {"m_keep": int(g["m"]), "compression": "fri", "sampling_method": "systematic",
+                "verbose": False, "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"]}
+    rn = list(g["rn"])
+    t1s, t2s, E = g["t1"], g["t2"], g["energies"]
+    from oracle import pyscf_standin as P
+    for it in range(len(E)):
+        draws = iter(rn[2 * it: 2 * it + 2])
+        t1n, t2n = CO.update_amps(settings, t1s[it], t2s[it], eris, rn_draw=lambda: next(draws))
+        np.testing.assert_allclose(t2n, t2s[it + 1], rtol=0, atol=1e-13)
+        np.testing.assert_allclose(t1n, t1s[it + 1], rtol=0, atol=1e-13)
+        assert abs(P.ccsd_energy(t1n, t2n, eris) - E[it]) < 1e-12
+
+
+def test_iteration_golden_free_running(oracle):
+    """The oracle's own loop, from the MP2 guess with the reference's draws,
+    follows the reference trajectory to 1e-10 Eh."""
+    from oracle import ccsd_oracle as CO
+    g, eris = _iteration_system()
+    settings = {"m_keep": int(g["m"]), "compression": "fri", "sampling_method": "systematic",
+                "verbose": False, "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"]}
+    draws = iter(list(g["rn"]))
+    conv, e, t1, t2, energies = CO.kernel(settings, eris, g["t1"][0], g["t2"][0], max_cycle=len(g["energies"]),
+                                          rn_draw=lambda: next(draws))
+    assert np.max(np.abs(np.array(energies) - g["energies"])) < 1e-10
