@@ -30,6 +30,12 @@ int fricc_cuda_check(cudaError_t e, const char* what);  // FRICC_OK on success
 int fricc_alloc(void** p, size_t bytes, cudaStream_t s);
 void fricc_free(void* p, cudaStream_t s);
 
+// Instrumentation: a count of every kernel this library launches, and CUDA
+// event timing of the sparse contraction kernel (off unless enabled).
+void fricc_note_launch(int n = 1);
+bool fricc_prof_on();
+void fricc_prof_record(cudaStream_t st, bool start, double flops);
+
 template <class T>
 inline int fricc_alloc_t(T** p, size_t n, cudaStream_t s) {
   return fricc_alloc(reinterpret_cast<void**>(p), n * sizeof(T) + 16, s);

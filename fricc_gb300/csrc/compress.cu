@@ -314,6 +314,7 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     cudaMemsetAsync(s.hist, 0, NDIG * sizeof(unsigned), st);
     cudaMemsetAsync(s.err, 0, sizeof(unsigned), st);
     k_hist12<<<grid_for(n, 256), 256, 0, st>>>(x, n, s.hist);
+    fricc_note_launch();
     std::vector<unsigned> hh(NDIG);
     TRY(fricc_cuda_check(cudaMemcpyAsync(hh.data(), s.hist, NDIG * sizeof(unsigned), cudaMemcpyDeviceToHost, st),
                          "histogram copy"));
@@ -339,10 +340,12 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     cudaMemsetAsync(s.tstate, 0, ntile * sizeof(unsigned long long), st);
     cudaMemsetAsync(s.ticket, 0, sizeof(unsigned), st);
     k_compact<<<(unsigned)ntile, 256, 0, st>>>(x, n, (unsigned)dmin, s.ckey, s.cidx, s.tstate, s.ticket, s.err);
+    fricc_note_launch();
     TRY(radix::sort_pairs(s.ckey, s.cidx, s.ktmp, s.vtmp, C, 64, true, s.rhist, st));
 
     if (mode == 1) {  // "largest": argsort(x, m) with unscaled values
       k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, flat, vals);
+      fricc_note_launch();
       TRY(fricc_cuda_check(cudaGetLastError(), "largest"));
       unsigned e = 0;
       cudaMemcpyAsync(&e, s.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
@@ -366,6 +369,7 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     TRY(fricc_alloc_t(&s.Rb, m + 1, st));
     TRY(fricc_alloc_t(&s.ffail, 1, st));
     k_set_u64<<<1, 1, 0, st>>>(s.ffail, (unsigned long long)m);
+    fricc_note_launch();
     ConsAccept ca{m, s.Rb, s.ffail};
     rc = exact::run_chain<GenSorted, ConsAccept, false, true>(GenSorted{s.ckey}, m, R0, true, ca, s.chain, s.err, st);
     fricc_free(R0, st);
@@ -390,6 +394,7 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     TRY(fricc_alloc_t(&s.S, mp > 0 ? mp : 1, st));
     if (mp > 0) {
       k_zero_u32<<<grid_for(mp, 256), 256, 0, st>>>(s.S, mp);
+      fricc_note_launch();
       if (R_h > 0.0 && std::isfinite(R_h)) {
         ConsSample cs{rn, mp, s.S};
         TRY((exact::run_chain<GenP, ConsSample, true, true>(gp, n, s.dzero, false, cs, s.chain, s.err, st)));
@@ -402,12 +407,14 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
           TRY(fricc_alloc_t(&s.chain.csum, nch + 1, st));
         }
         exact::k_chunk_sums<GenP, true><<<(unsigned)nch, 256, 0, st>>>(gp, n, s.chain.csum, s.err);
+        fricc_note_launch();
       }
     }
 
     // 6. output
     if (nd > 0) k_out_d<<<grid_for(nd, 256), 256, 0, st>>>(x, s.cidx, nd, flat, vals);
     if (mp > 0) k_out_s<<<grid_for(mp, 256), 256, 0, st>>>(gp, s.S, mp, nd, flat, vals);
+    fricc_note_launch((nd > 0) + (mp > 0));
     TRY(fricc_cuda_check(cudaGetLastError(), "output"));
     unsigned e = 0;
     cudaMemcpyAsync(&e, s.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
@@ -427,6 +434,7 @@ int fricc_unpack_device(const int64_t* flat, int64_t m, const int64_t dims[4], i
   if (rc) return rc;
   cudaMemsetAsync(err, 0, sizeof(unsigned), st);
   k_unpack<<<grid_for(m, 256), 256, 0, st>>>(flat, m, dims[0], dims[1], dims[2], dims[3], slots, err);
+  fricc_note_launch();
   unsigned e = 0;
   cudaMemcpyAsync(&e, err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
   cudaError_t ce = cudaStreamSynchronize(st);

@@ -185,6 +185,8 @@ bool is_contig_perm(const int64_t dims[4], const int64_t strides[4], const int p
 
 }  // namespace
 
+double fricc_contract_flops_impl(const char* term, const FriccSparse* T);
+
 int fricc_sparse_bucketing(FriccSparse* T, int pa, int pb, cudaStream_t st, Bucketing** out) {
   for (auto& b : T->buck)
     if (b.pa == pa && b.pb == pb && b.bptr) {
@@ -213,9 +215,11 @@ int fricc_sparse_bucketing(FriccSparse* T, int pa, int pb, cudaStream_t st, Buck
   if (!rc) {
     k_pair_keys<<<grid_for(m, 256), 256, 0, st>>>(T->slots, m, pa, pb, T->dims[pb], keys, slot->order);
     rc = radix::sort_pairs(keys, slot->order, ktmp, vtmp, m, bits, false, hist, st);
+    fricc_note_launch(1);
   }
   if (!rc) {
     k_bptr<<<grid_for(nb + 1, 256), 256, 0, st>>>(keys, m, nb, slot->bptr);
+    fricc_note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = fricc_cuda_fail(e, "bucketing", __FILE__, __LINE__);
   }
@@ -302,7 +306,11 @@ int fricc_contract_device(const char* term, const double* W, const int64_t Wd[4]
       rc = FRICC_ERR_ARG;
     } else {
       dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq);
+      const bool prof = fricc_prof_on();
+      if (prof) fricc_prof_record(st, true, 0.0);
       k_spmm<<<grid, SP_NT, 0, st>>>(bk->bptr, erow, eval, Wuse, Ouse, QS);
+      if (prof) fricc_prof_record(st, false, fricc_contract_flops_impl(term, T));
+      fricc_note_launch(2 + (w_direct ? 0 : 1) + (o_direct ? 0 : 2));
       if (!o_direct)
         k_scatter4<<<grid_for(nO, 256), 256, 0, st>>>(Op, osp[0], osp[1], osp[2], osp[3], oe[0], oe[1], oe[2], oe[3],
                                                       out);

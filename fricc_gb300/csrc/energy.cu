@@ -117,6 +117,7 @@ int fricc_energy_update_device(const double* t1num, const double* t2num, const d
   k_t2_energy<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, st>>>(t2num, t1out, eia, ovov, t2old, t2out, o, v, part,
                                                                 part + gx * gy);
   k_final<<<1, 256, 0, st>>>(part, part + gx * gy, gx * gy, res);
+  fricc_note_launch(3);
   cudaError_t e = cudaGetLastError();
   fricc_free(part, st);
   if (e != cudaSuccess) return fricc_cuda_fail(e, "energy_update", __FILE__, __LINE__);

@@ -433,6 +433,7 @@ int run_chain(const Gen& gen, int64_t len, const double* s_init_dev, bool sub, c
   k_chunk_maps<Gen><<<(unsigned)nch, 256, 0, st>>>(gen, len, sub ? 1 : 0, sc.cbin, sc.cmap);
   k_walk<Gen><<<1, 1024, 0, st>>>(gen, len, s_init_dev, sub ? 1 : 0, sc.cbin, sc.cmap, sc.cstart);
   if (EMIT) k_emit<Gen, Cons><<<(unsigned)nch, 256, 0, st>>>(gen, cons, len, sub ? 1 : 0, sc.cstart);
+  fricc_note_launch(EMIT ? 5 : 4);
   FRICC_LAUNCH_CHECK();
   return FRICC_OK;
 }

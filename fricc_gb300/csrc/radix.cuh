@@ -116,6 +116,7 @@ inline int sort_pairs(unsigned long long* keys, unsigned* vals, unsigned long lo
     k_hist<<<(unsigned)ntiles, NT, 0, st>>>(ka, n, shift, desc ? 1 : 0, hist, ntiles);
     k_scan<<<1, 1024, 0, st>>>(hist, 256 * ntiles);
     k_scatter<<<(unsigned)ntiles, NT, 0, st>>>(ka, va, kb, vb, n, shift, desc ? 1 : 0, hist, ntiles);
+    fricc_note_launch(3);
     unsigned long long* tk = ka;
     ka = kb;
     kb = tk;

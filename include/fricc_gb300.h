@@ -124,6 +124,15 @@ int fricc_energy_update(const double* t1num, const double* t2num, const double* 
                         const double* ovov, const double* t1old, const double* t2old, int64_t nocc, int64_t nvir,
                         double* t1out, double* t2out, double* res, void* stream);
 
+/* Instrumentation (no reference counterpart): the number of kernels this
+ * library has launched so far; and CUDA-event timing of every sparse
+ * contraction kernel launched while enabled (fricc_prof_enable(1) clears
+ * the record; fricc_prof_read synchronises on the recorded events and
+ * returns total milliseconds, launches and algorithmic flops). */
+long long fricc_launch_count(void);
+void fricc_prof_enable(int on);
+int fricc_prof_read(double* ms, long long* launches, double* flops);
+
 #ifdef __cplusplus
 }
 #endif

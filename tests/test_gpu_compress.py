@@ -18,7 +18,11 @@ def _gpu_sparse(x, m, kind, rn):
 
 
 def _same_bits(a, b):
-    return np.array_equal(np.asarray(a).view(np.int64), np.asarray(b).view(np.int64))
+    """Bit-for-bit equality; NaNs compare by position only (CUDA and the host
+    CPU generate different NaN payloads for 0/0 and x/NaN)."""
+    a, b = np.asarray(a), np.asarray(b)
+    na, nb = np.isnan(a), np.isnan(b)
+    return np.array_equal(na, nb) and np.array_equal(a[~na].view(np.int64), b[~nb].view(np.int64))
 
 
 def test_golden_bitexact(gpulib):
