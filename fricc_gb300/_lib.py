@@ -39,6 +39,7 @@ SIGNATURES = [
     ("fricc_contract_flops", ctypes.c_double, [ctypes.c_char_p, _vp]),
     ("fricc_compress", ctypes.c_int, [_dp, _i64, _i64, ctypes.c_int, ctypes.c_double, _dp, _dp, _i64p, _vp]),
     ("fricc_seq_cumsum", ctypes.c_int, [_dp, _i64, _dp, _vp]),
+    ("fricc_seq_cumsum_noalloc", ctypes.c_int, [_dp, _i64, _dp, _vp]),
     ("fricc_launch_count", ctypes.c_longlong, []),
     ("fricc_prof_enable", None, [ctypes.c_int]),
     ("fricc_prof_read", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),

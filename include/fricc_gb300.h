@@ -116,6 +116,18 @@ int fricc_compress(const double* x, int64_t n, int64_t m, int compression, doubl
  * produces, computed in parallel.  Stream-ordered. */
 int fricc_seq_cumsum(const double* x, int64_t n, double* out, void* stream);
 
+/* The same exact running sum, for callers that cannot allocate device memory
+ * (an application whose device memory is reserved up front by its own
+ * allocator, or a latency-critical loop that must not enter the CUDA
+ * allocator).  No counterpart in the reference.  It allocates nothing: its
+ * scratch (about 0.6 MB) is a fixed array inside the library, held by every
+ * GPU that loads it until exit.  n <= 2^26 (67,108,864), larger n fails
+ * with FRICC_ERR_ARG.  The first call on a device looks up the array's
+ * address for that device; make it before any stream capture begins.  All
+ * calls share the array: calls that overlap on the GPU (unordered streams)
+ * race; calls ordered on one stream are safe.  Stream-ordered. */
+int fricc_seq_cumsum_noalloc(const double* x, int64_t n, double* out, void* stream);
+
 /* t1 = t1num/eia, t2 = t2num/(eia_ia + eia_jb); res[0] = E_corr of (t1, t2),
  * res[1] = || (t1,t2) - (t1old,t2old) || in packed form.  All device, C order:
  * t1* (o,v), t2* (o,o,v,v), eia (o,v), fov (o,v), ovov (o,v,o,v); res holds 4
