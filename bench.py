@@ -39,10 +39,11 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 METRIC = "FRI-CCSD iter/s and solves/s at |ΔEcorr|≤1e-6 Eh vs plain GPU; p50/p99 latency"
-# FP64 FMA throughput of this GB300 pool, measured with a DFMA/DMMA probe
-# (1.011 TF/s DFMA, 1.053 TF/s DMMA; profiles/fp64_peak_gb300.md): the
-# contraction kernel is FP64-pipe bound, MEASURED_PEAKS.json has no FP64 figure.
-FP64_PEAK_TFLOPS = 1.011
+# FP64 FMA throughput of this GB300 pool, measured with a 16-chain DFMA probe
+# (profiles/fp64_peak_gb300.md): the contraction kernel is FP64-pipe bound
+# and MEASURED_PEAKS.json has no FP64 figure.
+FP64_PEAK_TFLOPS = 1.2557
+FP32_PEAK_TFLOPS = 74.2
 # DRAM bytes per k_spmm launch from the ncu capture summarised in
 # profiles/k_spmm_o30v150.md (None until captured).
 SPMM_TRAFFIC = {}
@@ -57,6 +58,8 @@ def parse():
     p.add_argument("--workload", default="o30v150")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--precision", default="fp64", choices=["fp64", "df64"],
+                   help="arithmetic of the sparse terms: FP64, or FP32 pairs (~48-bit) on the FP32 pipe")
     return p.parse_args()
 
 
@@ -219,7 +222,7 @@ def run_gpu(args):
     eia = e[:o, None] - e[None, o:]
     t2 = (E.ovov.permute(0, 2, 1, 3) / (eia[:, None, :, None] + eia[None, :, None, :])).contiguous()
     t1 = torch.zeros(o, v, dtype=torch.float64, device=dev)
-    solver = FRICCSDGPU(E, {"m_keep": m}, rn_draw=seeded_draws(1000 + rank))
+    solver = FRICCSDGPU(E, {"m_keep": m}, rn_draw=seeded_draws(1000 + rank), precision=args.precision)
     stream = torch.cuda.current_stream()
 
     for _ in range(args.warmup):
@@ -283,22 +286,32 @@ def run_gpu(args):
         cpu = cpu_baseline_line(eris_np, t1h, t2h, m, args.workload, 7)
 
     achieved = (p_fl.value / (p_ms.value / 1000.0)) / 1e12 if p_ms.value > 0 else None
-    roof = {"kernel": "k_spmm (bucketed sparse-T2 x dense-W, all 11 terms)", "bound": "fp64",
-            "achieved": achieved, "peak": FP64_PEAK_TFLOPS, "unit": "TFLOP/s",
-            "frac": (achieved / FP64_PEAK_TFLOPS) if achieved else None,
+    if args.precision == "fp64":
+        kname, bound, peak = "k_spmm (bucketed sparse-T2 x dense-W, FP64)", "fp64", FP64_PEAK_TFLOPS
+        psrc = "measured FP64 FMA rate of this GB300 pool (DFMA probe); FP64 is not in MEASURED_PEAKS.json"
+    else:
+        kname, bound, peak = "k_spmm_df (bucketed sparse-T2 x dense-W, FP32 pairs)", "fp32-pipe", FP32_PEAK_TFLOPS / 6
+        psrc = ("FP32 FMA rate of this GB300 pool (74.2 TF/s, FFMA probe) / 12 FP32 instructions per "
+                "FP32-pair multiply-add, as FP64-equivalent flops")
+    roof = {"kernel": kname, "bound": bound,
+            "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
+            "frac": (achieved / peak) if achieved else None,
             "traffic": SPMM_TRAFFIC.get(args.workload),
             "launches": int(p_n.value), "kernel_ms": p_ms.value,
             "kernel_share_of_step": p_ms.value / ms if ms > 0 else None,
-            "peak_source": "measured FP64 FMA rate of this GB300 pool (DFMA probe); FP64 is not in MEASURED_PEAKS.json"}
+            "peak_source": psrc}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None,
+            "dtype": "f64" if args.precision == "fp64" else "f64 (sparse terms in f32 pairs, ~48-bit)",
+            "data": "synthetic",
             "config": {"workload": f"{args.workload}: nocc={o} nvir={v} naux={w['naux']} sigma={w['sigma']} "
                                    f"m={m} FRI systematic, 2 compressions/iteration, FP64",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "working set > L2 (Wvvvv 4.05 GB rebuilt and streamed every step)"},
+                       "l2": "working set > L2 ((ac|bd) 4.05 GB streamed by the O^2V^4 term every step)",
+                       "precision": args.precision},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
             "clocks": clk.summary(), "energy_last": energies[-1],
         }

@@ -36,6 +36,11 @@ SIGNATURES = [
     ("fricc_sp_export", ctypes.c_int, [_vp, _vp, _vp, _vp]),
     ("fricc_sp_device_arrays", ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
     ("fricc_contract", ctypes.c_int, [ctypes.c_char_p, _dp, _i64p, _i64p, _vp, _dp, _i64p, _i64p, _vp]),
+    ("fricc_spmm", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
+                                  _dp, _i64, _dp, _vp]),
+    ("fricc_spmm_f2", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                     ctypes.c_double, _dp, _i64, _dp, _vp]),
+    ("fricc_split_f2", ctypes.c_int, [_dp, _i64, _dp, _vp]),
     ("fricc_contract_flops", ctypes.c_double, [ctypes.c_char_p, _vp]),
     ("fricc_compress", ctypes.c_int, [_dp, _i64, _i64, ctypes.c_int, ctypes.c_double, _dp, _dp, _i64p, _vp]),
     ("fricc_seq_cumsum", ctypes.c_int, [_dp, _i64, _dp, _vp]),

@@ -16,6 +16,11 @@ int fricc_unpack_device(const int64_t* flat, int64_t m, const int64_t dims[4], i
 int fricc_contract_device(const char* term, const double* W, const int64_t Wd[4], const int64_t Ws[4], FriccSparse* T,
                           double* out, const int64_t Od[4], const int64_t Os[4], cudaStream_t st);
 double fricc_contract_flops_impl(const char* term, const FriccSparse* T);
+int fricc_spmm_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const double* Wp, int64_t QS,
+                      double* Op, cudaStream_t st);
+int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float2* Wp, int64_t QS,
+                         double* Op, cudaStream_t st);
+int fricc_split_f2_device(const double* x, int64_t n, float2* out, cudaStream_t st);
 int fricc_energy_update_device(const double* t1num, const double* t2num, const double* eia, const double* fov,
                                const double* ovov, const double* t1old, const double* t2old, int64_t o, int64_t v,
                                double* t1out, double* t2out, double* res, cudaStream_t st);
@@ -327,6 +332,26 @@ int fricc_contract(const char* term, const double* W, const int64_t W_dims[4], c
   int rc = fricc_contract_device(term, W, W_dims, W_strides, T, out, out_dims, out_strides, st);
   if (!rc && T) T->owner_stream = st;
   return rc;
+}
+
+int fricc_spmm(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const double* Wp, int64_t QS,
+               double* Op, void* stream) {
+  cudaStream_t st = as_stream(stream);
+  int rc = fricc_spmm_device(T, pa, pb, ka, kb, coef, Wp, QS, Op, st);
+  if (!rc && T) T->owner_stream = st;
+  return rc;
+}
+
+int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* Wp2, int64_t QS,
+                  double* Op, void* stream) {
+  cudaStream_t st = as_stream(stream);
+  int rc = fricc_spmm_f2_device(T, pa, pb, ka, kb, coef, reinterpret_cast<const float2*>(Wp2), QS, Op, st);
+  if (!rc && T) T->owner_stream = st;
+  return rc;
+}
+
+int fricc_split_f2(const double* x, int64_t n, float* out2, void* stream) {
+  return fricc_split_f2_device(x, n, reinterpret_cast<float2*>(out2), as_stream(stream));
 }
 
 double fricc_contract_flops(const char* term, const fricc_sparse* T) {

@@ -336,7 +336,7 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     TRY(fricc_alloc_t(&s.vtmp, C, st));
     TRY(fricc_alloc_t(&s.tstate, ntile, st));
     TRY(fricc_alloc_t(&s.ticket, 1, st));
-    TRY(fricc_alloc_t(&s.rhist, 256 * fricc_cdiv(C, radix::TILE), st));
+    TRY(fricc_alloc_t(&s.rhist, radix::hist_words(C), st));
     cudaMemsetAsync(s.tstate, 0, ntile * sizeof(unsigned long long), st);
     cudaMemsetAsync(s.ticket, 0, sizeof(unsigned), st);
     k_compact<<<(unsigned)ntile, 256, 0, st>>>(x, n, (unsigned)dmin, s.ckey, s.cidx, s.tstate, s.ticket, s.err);

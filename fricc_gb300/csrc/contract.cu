@@ -141,6 +141,105 @@ __global__ void __launch_bounds__(SP_NT) k_spmm(const int* __restrict__ bptr, co
   }
 }
 
+// ---------------------------------------------------------------------------
+// FP32-pair ("double-float") variant.  GB300 issues 128 FP32 lanes per SM per
+// clock but only 2 FP64 FMAs, so each product-accumulate is done on pairs of
+// floats carrying ~48 significand bits:
+//   W = Wh + Wl, v = vh + vl (split once from FP64, |Wl| <= 2^-24 |Wh|),
+//   p = Wh*vh exactly as ph + e (one FMA recovers the rounding error),
+//   pl = e + Wh*vl + Wl*vh (Wl*vl, ~2^-48 relative, is dropped),
+//   (ah, al) += (ph, pl) with an error-free two-sum on the high parts,
+// renormalised every 32 terms; the FP64 result is (double)ah + (double)al.
+// Relative error per output ~1e-14, against FP64's ~1e-16.
+__device__ __forceinline__ float2 split_f2(double d) {
+  const float h = __double2float_rn(d);
+  return make_float2(h, __double2float_rn(d - (double)h));
+}
+
+constexpr int DF_NT = 128;
+constexpr int DF_QPT = 4;
+
+__global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr, const int* __restrict__ erow,
+                                                   const float2* __restrict__ eval, const float2* __restrict__ Wp,
+                                                   double* __restrict__ Op, int64_t QS) {
+  __shared__ int srow[DF_NT];
+  __shared__ float2 sval[DF_NT];
+  const int64_t P = blockIdx.x;
+  const int e0 = bptr[P], e1 = bptr[P + 1];
+  if (e0 == e1) return;
+  const int64_t q0 = (int64_t)blockIdx.y * (DF_NT * DF_QPT) + threadIdx.x;
+  double* orow = Op + P * QS;
+  float ah[DF_QPT], al[DF_QPT];
+#pragma unroll
+  for (int k = 0; k < DF_QPT; ++k) {
+    const int64_t q = q0 + k * DF_NT;
+    const float2 a = split_f2(q < QS ? orow[q] : 0.0);
+    ah[k] = a.x;
+    al[k] = a.y;
+  }
+  int since = 0;
+  for (int eb = e0; eb < e1; eb += DF_NT) {
+    const int cnt = e1 - eb < DF_NT ? e1 - eb : DF_NT;
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      srow[threadIdx.x] = erow[eb + threadIdx.x];
+      sval[threadIdx.x] = eval[eb + threadIdx.x];
+    }
+    __syncthreads();
+    for (int j = 0; j < cnt; ++j) {
+      const float2* w = Wp + (int64_t)srow[j] * QS;
+      const float2 v = sval[j];
+#pragma unroll
+      for (int k = 0; k < DF_QPT; ++k) {
+        const int64_t q = q0 + k * DF_NT;
+        if (q < QS) {
+          // explicit _rn intrinsics: the error-free transforms must not be
+          // contracted into fused multiply-adds by the compiler
+          const float2 x = w[q];
+          const float ph = __fmul_rn(x.x, v.x);
+          float pl = __fmaf_rn(x.x, v.x, -ph);
+          pl = __fmaf_rn(x.x, v.y, pl);
+          pl = __fmaf_rn(x.y, v.x, pl);
+          const float s = __fadd_rn(ah[k], ph);
+          const float z = __fsub_rn(s, ah[k]);
+          const float err = __fadd_rn(__fsub_rn(ah[k], __fsub_rn(s, z)), __fsub_rn(ph, z));
+          al[k] = __fadd_rn(al[k], __fadd_rn(err, pl));
+          ah[k] = s;
+        }
+      }
+      if (++since == 32) {
+        since = 0;
+#pragma unroll
+        for (int k = 0; k < DF_QPT; ++k) {
+          const float s = __fadd_rn(ah[k], al[k]);
+          al[k] = __fsub_rn(al[k], __fsub_rn(s, ah[k]));
+          ah[k] = s;
+        }
+      }
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < DF_QPT; ++k) {
+    const int64_t q = q0 + k * DF_NT;
+    if (q < QS) orow[q] = (double)ah[k] + (double)al[k];
+  }
+}
+
+__global__ void k_entries_df(const int* __restrict__ slots, const double* __restrict__ vals,
+                             const unsigned* __restrict__ order, int64_t m, int ka, int kb, int64_t dkb, double coef,
+                             int* __restrict__ erow, float2* __restrict__ eval) {
+  for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
+    const unsigned s = order[e];
+    erow[e] = (int)((int64_t)slots[4 * s + ka] * dkb + slots[4 * s + kb]);
+    eval[e] = split_f2(coef * vals[s]);
+  }
+}
+
+__global__ void k_split_f2(const double* __restrict__ x, int64_t n, float2* __restrict__ out) {
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
+    out[i] = split_f2(x[i]);
+}
+
 // dst (contiguous, extents e0..e3) = src viewed with strides s0..s3
 __global__ void k_gather4(const double* __restrict__ src, int64_t s0, int64_t s1, int64_t s2, int64_t s3, int64_t e0,
                           int64_t e1, int64_t e2, int64_t e3, double* __restrict__ dst) {
@@ -209,7 +308,7 @@ int fricc_sparse_bucketing(FriccSparse* T, int pa, int pb, cudaStream_t st, Buck
   int rc = fricc_alloc_t(&keys, m, st);
   if (!rc) rc = fricc_alloc_t(&ktmp, m, st);
   if (!rc) rc = fricc_alloc_t(&vtmp, m, st);
-  if (!rc) rc = fricc_alloc_t(&hist, 256 * fricc_cdiv(m, radix::TILE), st);
+  if (!rc) rc = fricc_alloc_t(&hist, radix::hist_words(m), st);
   if (!rc) rc = fricc_alloc_t(&slot->order, m, st);
   if (!rc) rc = fricc_alloc_t(&slot->bptr, nb + 1, st);
   if (!rc) {
@@ -323,6 +422,95 @@ int fricc_contract_device(const char* term, const double* W, const int64_t Wd[4]
   fricc_free(Wp, st);
   fricc_free(Op, st);
   return rc;
+}
+
+// Generic form: out'[P, q] += coef * sum_{e in bucket P} W'[key_e, q] * value_e
+// with P = slot[pa]*dims[pb] + slot[pb], key = slot[ka]*dims[kb] + slot[kb],
+// W' contiguous [dims[ka]*dims[kb]][QS] and out' contiguous [dims[pa]*dims[pb]][QS].
+int fricc_spmm_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const double* Wp, int64_t QS,
+                      double* Op, cudaStream_t st) {
+  if (!T || !Wp || !Op || QS <= 0 || pa < 0 || pa > 3 || pb < 0 || pb > 3 || ka < 0 || ka > 3 || kb < 0 || kb > 3 ||
+      pa == pb || ka == kb) {
+    fricc_set_error("spmm: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  if (T->m == 0) return FRICC_OK;
+  Bucketing* bk = nullptr;
+  int rc = fricc_sparse_bucketing(T, pa, pb, st, &bk);
+  if (rc) return rc;
+  int* erow = nullptr;
+  double* eval = nullptr;
+  rc = fricc_alloc_t(&erow, T->m, st);
+  if (!rc) rc = fricc_alloc_t(&eval, T->m, st);
+  const int64_t ntq = fricc_cdiv(QS, SP_NT * SP_QPT);
+  if (!rc && (ntq > 65535 || bk->nbuckets > 0x7fffffffLL)) {
+    fricc_set_error("spmm: problem too large for one launch");
+    rc = FRICC_ERR_ARG;
+  }
+  if (!rc) {
+    k_entries<<<grid_for(T->m, 256), 256, 0, st>>>(T->slots, T->vals, bk->order, T->m, ka, kb, T->dims[kb], coef,
+                                                   erow, eval);
+    const bool prof = fricc_prof_on();
+    if (prof) fricc_prof_record(st, true, 0.0);
+    k_spmm<<<dim3((unsigned)bk->nbuckets, (unsigned)ntq), SP_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS);
+    if (prof) fricc_prof_record(st, false, 2.0 * (double)T->m * (double)QS);
+    fricc_note_launch(2);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fricc_cuda_fail(e, "spmm", __FILE__, __LINE__);
+  }
+  fricc_free(erow, st);
+  fricc_free(eval, st);
+  return rc;
+}
+
+// As fricc_spmm_device with W' pre-split into float pairs (fricc_split_f2);
+// the products and sums run on the FP32 pipe in pair arithmetic.
+int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float2* Wp, int64_t QS,
+                         double* Op, cudaStream_t st) {
+  if (!T || !Wp || !Op || QS <= 0 || pa < 0 || pa > 3 || pb < 0 || pb > 3 || ka < 0 || ka > 3 || kb < 0 || kb > 3 ||
+      pa == pb || ka == kb) {
+    fricc_set_error("spmm_f2: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  if (T->m == 0) return FRICC_OK;
+  Bucketing* bk = nullptr;
+  int rc = fricc_sparse_bucketing(T, pa, pb, st, &bk);
+  if (rc) return rc;
+  int* erow = nullptr;
+  float2* eval = nullptr;
+  rc = fricc_alloc_t(&erow, T->m, st);
+  if (!rc) rc = fricc_alloc_t(&eval, T->m, st);
+  const int64_t ntq = fricc_cdiv(QS, DF_NT * DF_QPT);
+  if (!rc && (ntq > 65535 || bk->nbuckets > 0x7fffffffLL)) {
+    fricc_set_error("spmm_f2: problem too large for one launch");
+    rc = FRICC_ERR_ARG;
+  }
+  if (!rc) {
+    k_entries_df<<<grid_for(T->m, 256), 256, 0, st>>>(T->slots, T->vals, bk->order, T->m, ka, kb, T->dims[kb], coef,
+                                                      erow, eval);
+    const bool prof = fricc_prof_on();
+    if (prof) fricc_prof_record(st, true, 0.0);
+    k_spmm_df<<<dim3((unsigned)bk->nbuckets, (unsigned)ntq), DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS);
+    if (prof) fricc_prof_record(st, false, 2.0 * (double)T->m * (double)QS);
+    fricc_note_launch(2);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fricc_cuda_fail(e, "spmm_f2", __FILE__, __LINE__);
+  }
+  fricc_free(erow, st);
+  fricc_free(eval, st);
+  return rc;
+}
+
+int fricc_split_f2_device(const double* x, int64_t n, float2* out, cudaStream_t st) {
+  if (n < 0 || (n > 0 && (!x || !out))) {
+    fricc_set_error("split_f2: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  if (n == 0) return FRICC_OK;
+  k_split_f2<<<grid_for(n, 256), 256, 0, st>>>(x, n, out);
+  fricc_note_launch();
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "split_f2", __FILE__, __LINE__);
 }
 
 // Flop count of one term (2 per multiply-add), for roofline accounting.

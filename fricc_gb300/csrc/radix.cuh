@@ -34,32 +34,42 @@ static __global__ void __launch_bounds__(NT) k_hist(const unsigned long long* __
   hist[(int64_t)threadIdx.x * ntiles + blockIdx.x] = h[threadIdx.x];
 }
 
-// In-place exclusive scan of len uint32 counts (digit-major), one block.
-static __global__ void __launch_bounds__(1024) k_scan(unsigned* hist, int64_t len) {
+// Exclusive scan of each digit's per-tile counts (one block per digit, in
+// place); the digit's total goes to totals[d].
+static __global__ void __launch_bounds__(256) k_scan_rows(unsigned* hist, int64_t ntiles, unsigned* totals) {
   __shared__ int64_t sm[33];
-  const int64_t per = fricc_cdiv(len, 1024);
+  unsigned* row = hist + (int64_t)blockIdx.x * ntiles;
+  const int64_t per = fricc_cdiv(ntiles, 256);
   const int64_t b = threadIdx.x * per;
-  const int64_t e = b + per < len ? b + per : len;
+  const int64_t e = b + per < ntiles ? b + per : ntiles;
   int64_t loc = 0;
-  for (int64_t i = b; i < e; ++i) loc += hist[i];
+  for (int64_t i = b; i < e; ++i) loc += row[i];
   int64_t tot;
   int64_t run = block_excl_sum(loc, sm, &tot);
   for (int64_t i = b; i < e; ++i) {
-    const unsigned c = hist[i];
-    hist[i] = (unsigned)run;
+    const unsigned c = row[i];
+    row[i] = (unsigned)run;
     run += c;
   }
+  if (threadIdx.x == 0) totals[blockIdx.x] = (unsigned)tot;
+}
+
+// Exclusive scan of the 256 digit totals into base[d].
+static __global__ void __launch_bounds__(256) k_scan_digits(const unsigned* totals, unsigned* base) {
+  __shared__ int64_t sm[33];
+  int64_t tot;
+  base[threadIdx.x] = (unsigned)block_excl_sum(totals[threadIdx.x], sm, &tot);
 }
 
 static __global__ void __launch_bounds__(NT) k_scatter(const unsigned long long* __restrict__ kin,
                                                 const unsigned* __restrict__ vin,
                                                 unsigned long long* __restrict__ kout, unsigned* __restrict__ vout,
                                                 int64_t n, int shift, int desc, const unsigned* __restrict__ offs,
-                                                int64_t ntiles) {
+                                                int64_t ntiles, const unsigned* __restrict__ dbase) {
   constexpr int NW = NT / 32;
   __shared__ unsigned run[256];
   __shared__ unsigned wc[NW][256];
-  run[threadIdx.x] = offs[(int64_t)threadIdx.x * ntiles + blockIdx.x];
+  run[threadIdx.x] = dbase[threadIdx.x] + offs[(int64_t)threadIdx.x * ntiles + blockIdx.x];
   unsigned lt;
   asm("mov.u32 %0, %%lanemask_lt;" : "=r"(lt));
   const int w = threadIdx.x >> 5;
@@ -103,7 +113,9 @@ static __global__ void __launch_bounds__(NT) k_scatter(const unsigned long long*
 }
 
 // Sorts n pairs on key bits [0, bits).  The result ends in (keys, vals); the
-// tmp buffers must hold n entries, hist 256*ceil(n/TILE) counts.
+// tmp buffers must hold n entries, hist hist_words(n) counts.
+inline int64_t hist_words(int64_t n) { return 256 * fricc_cdiv(n, TILE) + 512; }
+
 inline int sort_pairs(unsigned long long* keys, unsigned* vals, unsigned long long* ktmp, unsigned* vtmp,
                       int64_t n, int bits, bool desc, unsigned* hist, cudaStream_t st) {
   if (n <= 1) return FRICC_OK;
@@ -113,10 +125,13 @@ inline int sort_pairs(unsigned long long* keys, unsigned* vals, unsigned long lo
   unsigned *va = vals, *vb = vtmp;
   int passes = 0;
   for (int shift = 0; shift < bits; shift += 8, ++passes) {
+    unsigned* totals = hist + 256 * ntiles;
+    unsigned* base = totals + 256;
     k_hist<<<(unsigned)ntiles, NT, 0, st>>>(ka, n, shift, desc ? 1 : 0, hist, ntiles);
-    k_scan<<<1, 1024, 0, st>>>(hist, 256 * ntiles);
-    k_scatter<<<(unsigned)ntiles, NT, 0, st>>>(ka, va, kb, vb, n, shift, desc ? 1 : 0, hist, ntiles);
-    fricc_note_launch(3);
+    k_scan_rows<<<256, 256, 0, st>>>(hist, ntiles, totals);
+    k_scan_digits<<<1, 256, 0, st>>>(totals, base);
+    k_scatter<<<(unsigned)ntiles, NT, 0, st>>>(ka, va, kb, vb, n, shift, desc ? 1 : 0, hist, ntiles, base);
+    fricc_note_launch(4);
     unsigned long long* tk = ka;
     ka = kb;
     kb = tk;

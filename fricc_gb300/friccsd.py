@@ -86,7 +86,7 @@ class _Handle:
 
 class FRICCSDGPU:
     def __init__(self, eris: D.DeviceERIs, fri_settings=None, level_shift=0.0, rn_draw=libc_uniform,
-                 wvvvv_t1t1="reference"):
+                 wvvvv_t1t1="reference", precision="fp64"):
         s = dict(DEFAULT_SETTINGS)
         s.update(fri_settings or {})
         for c in s["compressed_contractions"]:
@@ -103,6 +103,9 @@ class FRICCSDGPU:
         self.level_shift = float(level_shift)
         self.rn_draw = rn_draw
         self.wvvvv_t1t1 = wvvvv_t1t1
+        if precision not in ("fp64", "df64"):
+            raise ValueError("precision must be 'fp64' or 'df64'")
+        self.precision = precision
         self.lib = L.load()
         self._sp = _Handle()
         self._sp_w = _Handle()
@@ -118,12 +121,34 @@ class FRICCSDGPU:
         L.check(self.lib.fricc_contract(term.encode(), _ptr(W), L.i64arr(W.shape), L.i64arr(W.stride()), T,
                                         _ptr(out), L.i64arr(out.shape), L.i64arr(out.stride()), stream))
 
+    def _spmm(self, T, pa, pb, ka, kb, coef, Wp, QS, Op, stream, const=None):
+        """Op[P][q] += coef * sum_e Wp[key_e][q] value_e (both contiguous).
+
+        With precision "df64" the products and sums run in FP32-pair
+        arithmetic; ``const`` names a constant integral block whose split
+        form is cached on the DeviceERIs."""
+        assert Wp.is_contiguous() and Op.is_contiguous()
+        if self.precision == "df64":
+            W2 = self.eris.split(const) if const else D.split_f2(Wp)
+            L.check(self.lib.fricc_spmm_f2(T, pa, pb, ka, kb, float(coef), _ptr(W2), int(QS), _ptr(Op), stream))
+        else:
+            L.check(self.lib.fricc_spmm(T, pa, pb, ka, kb, float(coef), _ptr(Wp), int(QS), _ptr(Op), stream))
+
     def update_amps(self, t1, t2, rn=None, t1_old=None, t2_old=None):
         """One iteration on device tensors; returns (t1new, t2new).
 
         rn: the two uniform draws (compression #1, #2); default rn_draw().
-        After the call, last_energy is E_corr(t1new, t2new) and last_normt the
-        step norm against (t1_old, t2_old) (default: the inputs).
+        After the call, read_energy() gives E_corr(t1new, t2new) and the step
+        norm against (t1_old, t2_old) (default: the inputs).
+
+        Same algebra as fricc/friccsd.py:29-301, arranged for the GPU:
+        * the O^2V^3 T1 terms are one GEMM against a combined integral;
+        * Wvvvv is never materialised: its (ac|bd) part is contracted with the
+          compressed T2 directly (the 2323 term) and its two t1 parts become
+          two O^3V^3-sized sparse contractions X, Y followed by a t1 GEMM;
+        * 1302 and 1202 (and 0313 and 0113) share bucketing and output, so
+          each pair runs as one pass over a combined W.
+        Each rearrangement changes results only at the level of FP64 rounding.
         """
         E = self.eris
         s = self.settings
@@ -132,11 +157,13 @@ class FRICCSDGPU:
             raise ValueError("Bad m_keep value! The following condition wasn't met 0 < m_keep <= t2.size")
         comp = s["compressed_contractions"]
         o, v = t1.shape
+        ov = o * v
         st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         t2 = t2.contiguous()
         e_o = E.mo_energy[:o]
         e_v = E.mo_energy[o:] + self.level_shift
         fov = E.fock[:o, o:]
+        ein = torch.einsum
         need_w = "O^3V^3" in comp or "O^4V^2" in comp
         if rn is None:
             kind = s["compression"]
@@ -144,48 +171,45 @@ class FRICCSDGPU:
         T = self._sp.compress(t2, m, s["compression"], rn[0], st)
         Tw = self._sp_w.compress(t2, m, s["compression"], rn[1], st) if need_w else None
 
-        Foo = D.cc_Foo(t1, t2, E)
-        Fvv = D.cc_Fvv(t1, t2, E)
+        Foo0 = D.cc_Foo(t1, t2, E)
+        Fvv0 = D.cc_Fvv(t1, t2, E)
         Fov = D.cc_Fov(t1, t2, E)
+        Foo = Foo0.clone()
+        Fvv = Fvv0.clone()
         Foo.diagonal().sub_(e_o)
         Fvv.diagonal().sub_(e_v)
 
-        ein = torch.einsum
         # T1 equation (fricc/friccsd.py:153-176)
         t1new = -2 * ein("kc,ka,ic->ia", fov, t1, t1)
-        t1new += ein("ac,ic->ia", Fvv, t1)
-        t1new += -ein("ki,ka->ia", Foo, t1)
-        t1new += 2 * ein("kc,kica->ia", Fov, t2)
-        t1new += -ein("kc,ikca->ia", Fov, t2)
+        t1new += t1 @ Fvv.T
+        t1new -= Foo.T @ t1
+        t1new += 2 * ein("kc,kica->ia", Fov, t2) - ein("kc,ikca->ia", Fov, t2)
         t1new += ein("kc,ic,ka->ia", Fov, t1, t1)
         t1new += fov
-        t1new += 2 * ein("kcai,kc->ia", E.ovvo, t1)
-        t1new += -ein("kiac,kc->ia", E.oovv, t1)
-        t1new += 2 * ein("kdac,ikcd->ia", E.ovvv, t2)
-        t1new += -ein("kcad,ikcd->ia", E.ovvv, t2)
-        t1new += 2 * ein("kdac,kd,ic->ia", E.ovvv, t1, t1)
-        t1new += -ein("kcad,kd,ic->ia", E.ovvv, t1, t1)
-        t1new += -2 * ein("lcki,klac->ia", E.ovoo, t2)
-        t1new += ein("kcli,klac->ia", E.ovoo, t2)
-        t1new += -2 * ein("lcki,lc,ka->ia", E.ovoo, t1, t1)
-        t1new += ein("kcli,lc,ka->ia", E.ovoo, t1, t1)
+        t1new += 2 * ein("kcai,kc->ia", E.ovvo, t1) - ein("kiac,kc->ia", E.oovv, t1)
+        G = E.G_t1.view(o * v * v, v)
+        t1new += t2.view(o, o * v * v) @ G                                   # O^2V^3, :165-166
+        t1new += t1 @ (t1.reshape(1, ov) @ E.G_t1.permute(0, 2, 1, 3).reshape(ov, v * v)).view(v, v)  # :167-168
+        t1new += -2 * ein("lcki,klac->ia", E.ovoo, t2) + ein("kcli,klac->ia", E.ovoo, t2)
+        t1new += -2 * ein("lcki,lc,ka->ia", E.ovoo, t1, t1) + ein("kcli,lc,ka->ia", E.ovoo, t1, t1)
 
         # T2 driver terms (:179-187)
-        tmp2 = ein("kibc,ka->abic", E.oovv, -t1) + E.ovvv.permute(1, 3, 0, 2)
-        t2new = _sym(ein("abic,jc->ijab", tmp2, t1))
+        Y1 = ein("kibc,jc->kibj", E.oovv, t1)
+        tmp = ein("iacb,jc->ijab", E.ovvv, t1) - ein("ka,kibj->ijab", t1, Y1)
+        t2new = tmp + tmp.permute(1, 0, 3, 2)
         tmp2 = ein("kcai,jc->akij", E.ovvo, t1) + E.ovoo.permute(1, 3, 0, 2)
-        t2new -= _sym(ein("akij,kb->ijab", tmp2, t1))
+        tmp = ein("akij,kb->ijab", tmp2, t1)
+        t2new -= tmp + tmp.permute(1, 0, 3, 2)
         t2new += E.ovov.permute(0, 2, 1, 3)
         t2new = t2new.contiguous()
 
-        Loo = D.Loo(t1, t2, E)
-        Lvv = D.Lvv(t1, t2, E)
+        Loo = D.Loo(t1, t2, E, Foo=Foo0)
+        Lvv = D.Lvv(t1, t2, E, Fvv=Fvv0)
         Loo.diagonal().sub_(e_o)
         Lvv.diagonal().sub_(e_v)
 
         if "O^4V^2" in comp:  # sparse_cc_Woooo (:309-322)
-            Woooo = ein("lcki,jc->klij", E.ovoo, t1) + ein("kclj,ic->klij", E.ovoo, t1)
-            Woooo = Woooo.contiguous()
+            Woooo = (ein("lcki,jc->klij", E.ovoo, t1) + ein("kclj,ic->klij", E.ovoo, t1)).contiguous()
             self._contract("1323", E.ovov, Tw, Woooo, st)
             Woooo += ein("kcld,ic,jd->klij", E.ovov, t1, t1)
             Woooo += E.oooo.permute(0, 2, 1, 3)
@@ -193,24 +217,20 @@ class FRICCSDGPU:
             Woooo = D.cc_Woooo(t1, t2, E)
 
         if "O^3V^3" in comp:  # sparse_cc_Wvoov / sparse_cc_Wvovo (:334-376)
-            Wvoov = (ein("kcad,id->akic", E.ovvv, t1) - ein("kcli,la->akic", E.ovoo, t1)
-                     + E.ovvo.permute(2, 0, 3, 1)).contiguous()
-            self._contract("0112", E.ovov, Tw, Wvoov, st)
-            self._contract("0313", E.ovov, Tw, Wvoov, st)
-            self._contract("0113", E.ovov, Tw, Wvoov, st)
+            Wvoov = ein("kcad,id->akic", E.ovvv, t1) - ein("kcli,la->akic", E.ovoo, t1) + E.ovvo.permute(2, 0, 3, 1)
+            Wp = Wvoov.permute(0, 2, 1, 3).contiguous()                         # [a,i,k,c]
+            self._spmm(Tw, 3, 0, 1, 2, -0.5, E.ovov, ov, Wp, st, const="ovov")                     # 0112
+            self._spmm(Tw, 2, 0, 1, 3, 1.0, E.ovov_0313_0113, ov, Wp, st, const="ovov_0313_0113")  # 0313+0113
+            Wvoov = Wp.permute(0, 2, 1, 3)                                      # (a,k,i,c)
             Wvoov -= ein("ldkc,id,la->akic", E.ovov, t1, t1)
-            Wvovo = (ein("kdac,id->akci", E.ovvv, t1) - ein("lcki,la->akci", E.ovoo, t1)
-                     + E.oovv.permute(2, 0, 3, 1)).contiguous()
-            self._contract("0312", E.ovov, Tw, Wvovo, st)
+            Wvovo = ein("kdac,id->akci", E.ovvv, t1) - ein("lcki,la->akci", E.ovoo, t1) + E.oovv.permute(2, 0, 3, 1)
+            Wq = Wvovo.permute(0, 3, 1, 2).contiguous()                         # [a,i,k,c]
+            self._spmm(Tw, 3, 0, 1, 2, -0.5, E.ovov_0312, ov, Wq, st, const="ovov_0312")          # 0312
+            Wvovo = Wq.permute(0, 2, 3, 1)                                      # (a,k,c,i)
             Wvovo -= ein("lckd,id,la->akci", E.ovov, t1, t1)
         else:
             Wvoov = D.cc_Wvoov(t1, t2, E)
             Wvovo = D.cc_Wvovo(t1, t2, E)
-
-        if self._wT is None or self._wT.shape != E.vvvvT.shape:
-            self._wT = torch.empty_like(E.vvvvT)
-        WT = D.wvvvv_T(t1, E, out=self._wT)  # Wvvvv as [c,d,a,b] (:325-331)
-        Wvvvv = WT.permute(2, 3, 0, 1)        # the (a,b,c,d) view
 
         if "O^4V^2" in comp:
             t2new += ein("klij,ka,lb->ijab", Woooo, t1, t1)
@@ -219,31 +239,43 @@ class FRICCSDGPU:
             tau = t2 + ein("ia,jb->ijab", t1, t1)
             t2new += ein("klij,klab->ijab", Woooo, tau)
 
+        # Wvvvv terms (:207, :222-234)
         if self.wvvvv_t1t1 == "reference":
-            # fricc/friccsd.py:222: einsum("abcd,ia,jb->ijab") sums c,d inside W
-            S = WT.sum(dim=(0, 1))
+            # fricc/friccsd.py:222: einsum("abcd,ia,jb->ijab") sums c,d inside Wvvvv
+            S = D.wvvvv_sum_cd(t1, E)
             t2new += S[None, None, :, :] * t1[:, None, :, None] * t1[None, :, None, :]
+            if "O^2V^4" in comp:
+                self._spmm(T, 0, 1, 2, 3, 1.0, E.vvvvT, v * v, t2new, st, const="vvvvT")  # (ac|bd) of 2323
+                XY = torch.zeros(o, o, 2, o, v, dtype=t2.dtype, device=t2.device)
+                self._spmm(T, 0, 1, 2, 3, 1.0, E.ovvv_XY, 2 * ov, XY, st, const="ovvv_XY")  # t1 parts
+                t2new -= ein("ijka,kb->ijab", XY[:, :, 0], t1) + ein("ijkb,ka->ijab", XY[:, :, 1], t1)
+            else:
+                WT = D.wvvvv_T(t1, E)
+                t2new += ein("abcd,ijcd->ijab", WT.permute(2, 3, 0, 1), t2)
         else:
+            WT = D.wvvvv_T(t1, E)
+            Wvvvv = WT.permute(2, 3, 0, 1)
             t2new += ein("abcd,ic,jd->ijab", Wvvvv, t1, t1)
-        if "O^2V^4" in comp:
-            self._contract("2323", Wvvvv, T, t2new, st)
-        else:
-            t2new += ein("abcd,ijcd->ijab", Wvvvv, t2)
+            if "O^2V^4" in comp:
+                self._contract("2323", Wvvvv, T, t2new, st)
+            else:
+                t2new += ein("abcd,ijcd->ijab", Wvvvv, t2)
 
         t2new += _sym(ein("ac,ijcb->ijab", Lvv, t2))
         t2new -= _sym(ein("ki,kjab->ijab", Loo, t2))
 
         if "O^3V^3" in comp:
-            tmp = torch.zeros_like(t2new)
-            self._contract("1302", Wvoov, T, tmp, st)
-            self._contract("1202", Wvovo, T, tmp, st)
-            t2new += _sym(tmp)
+            WA = Wvoov.permute(1, 3, 2, 0).contiguous()      # [k,c,i,a] = Wvoov(a,k,i,c)
+            WB = Wvovo.permute(1, 2, 3, 0).contiguous()      # [k,c,i,a] = Wvovo(a,k,c,i)
+            tmp = torch.zeros(o, v, o, v, dtype=t2.dtype, device=t2.device)   # [j,b,i,a]
+            self._spmm(T, 1, 3, 0, 2, 1.0, 2.0 * WA - WB, ov, tmp, st)        # 1302 + 1202
+            t2new += _sym(tmp.permute(2, 0, 3, 1))
             tmp.zero_()
-            self._contract("1303", Wvoov, T, tmp, st)
-            t2new -= _sym(tmp)
+            self._spmm(T, 1, 2, 0, 3, 1.0, WA, ov, tmp, st)                   # 1303, [j,b,i,a]
+            t2new -= _sym(tmp.permute(2, 0, 3, 1))
             tmp.zero_()
-            self._contract("1203", Wvovo, T, tmp, st)
-            t2new -= _sym(tmp)
+            self._spmm(T, 1, 2, 0, 3, 1.0, WB, ov, tmp, st)                   # 1203, [j,a,i,b]
+            t2new -= _sym(tmp.permute(2, 0, 1, 3))
         else:
             tmp = 2 * ein("akic,kjcb->ijab", Wvoov, t2) - ein("akci,kjcb->ijab", Wvovo, t2)
             t2new += _sym(tmp)

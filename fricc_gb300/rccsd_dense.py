@@ -47,10 +47,37 @@ class DeviceERIs:
         self._derive()
 
     def _derive(self):
-        # layouts reused every iteration
-        self.g_ovov = 2.0 * self.ovov - self.ovov.permute(0, 3, 2, 1)    # 2(kc|ld) - (kd|lc)
-        self.ovvv_kcda = self.ovvv.permute(0, 3, 1, 2).contiguous()       # [k,c,d,a] = (kd|ac)
-        self.ovvv_cdkb = self.ovvv.permute(1, 3, 0, 2).contiguous()       # [c,d,k,b] = (kc|bd)
+        """Constant layouts and combinations reused every iteration."""
+        ovvv, ovov, ovoo = self.ovvv, self.ovov, self.ovoo
+        self.g_ovov = 2.0 * ovov - ovov.permute(0, 3, 2, 1)               # 2(kc|ld) - (kd|lc)
+        self.g_ovoo = 2.0 * ovoo - ovoo.permute(2, 1, 0, 3)               # [l,c,k,i]: 2(lc|ki) - (kc|li)
+        # T1 O^2V^3 terms as one GEMM: G[k,c,d,a] = 2 (kd|ac) - (kc|ad)
+        self.G_t1 = (2.0 * ovvv.permute(0, 3, 1, 2) - ovvv.permute(0, 1, 3, 2)).contiguous()
+        # the t1 parts of Wvvvv, contracted with the compressed T2 instead of being
+        # built densely: W'[c,d,(x,k,a)] = (kd|ac) for x=0 and (kc|ad) for x=1
+        self.ovvv_XY = torch.stack([ovvv.permute(3, 1, 0, 2), ovvv.permute(1, 3, 0, 2)], dim=2).contiguous()
+        # sum_cd of the three Wvvvv pieces (for the reference's Wvvvv.t1.t1 term)
+        self.S0 = self.vvvvT.sum(dim=(0, 1))                              # [a,b] = sum_cd (ac|bd)
+        self.U = ovvv.sum(dim=(1, 3))                                     # [k,a] = sum_cd (kd|ac) = sum_cd (kc|ad)
+        # W' of the sparse W-intermediate terms, [l,d,k,c]
+        self.ovov_0312 = ovov.permute(0, 3, 2, 1).contiguous()            # (lc|kd)
+        self.ovov_0313_0113 = (ovov - 0.5 * ovov.permute(0, 3, 2, 1)).contiguous()
+        self._dense_wvvvv = None
+        self._splits = {}
+
+    def split(self, name):
+        """The (hi, lo) float-pair form of a constant block (cached)."""
+        if name not in self._splits:
+            self._splits[name] = split_f2(getattr(self, name))
+        return self._splits[name]
+
+    @property
+    def ovvv_kcda(self):  # [k,c,d,a] = (kd|ac), only for the dense Wvvvv build
+        return self.ovvv.permute(0, 3, 1, 2).contiguous()
+
+    @property
+    def ovvv_cdkb(self):  # [c,d,k,b] = (kc|bd), only for the dense Wvvvv build
+        return self.ovvv.permute(1, 3, 0, 2).contiguous()
 
     @classmethod
     def from_system(cls, system, device="cuda"):
@@ -87,6 +114,18 @@ class DeviceERIs:
         return out
 
 
+def split_f2(x: torch.Tensor) -> torch.Tensor:
+    """x (FP64, contiguous) as interleaved (hi, lo) floats, hi + lo = x to ~2^-48."""
+    import ctypes
+
+    from . import _lib as L
+    x = x.contiguous()
+    out = torch.empty(x.numel() * 2, dtype=torch.float32, device=x.device)
+    L.check(L.load().fricc_split_f2(ctypes.c_void_p(x.data_ptr()), x.numel(), ctypes.c_void_p(out.data_ptr()),
+                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return out
+
+
 def cc_Foo(t1, t2, E):
     o = t1.shape[0]
     tt = t2 + ein("ic,ld->ilcd", t1, t1)
@@ -104,18 +143,18 @@ def cc_Fov(t1, t2, E):
     return E.fock[:o, o:] + ein("kcld,ld->kc", E.g_ovov, t1)
 
 
-def Loo(t1, t2, E):
+def Loo(t1, t2, E, Foo=None):
     o = t1.shape[0]
     fov = E.fock[:o, o:]
-    g = 2.0 * E.ovoo - E.ovoo.permute(2, 1, 0, 3)  # [l,c,k,i]: 2(lc|ki) - (kc|li)
-    return cc_Foo(t1, t2, E) + fov @ t1.T + ein("lcki,lc->ki", g, t1)
+    F = cc_Foo(t1, t2, E) if Foo is None else Foo
+    return F + fov @ t1.T + ein("lcki,lc->ki", E.g_ovoo, t1)
 
 
-def Lvv(t1, t2, E):
+def Lvv(t1, t2, E, Fvv=None):
     o = t1.shape[0]
     fov = E.fock[:o, o:]
-    g = 2.0 * E.ovvv - E.ovvv.permute(0, 3, 2, 1)  # [k,d,a,c]: 2(kd|ac) - (kc|ad)
-    return cc_Fvv(t1, t2, E) - t1.T @ fov + ein("kdac,kd->ac", g, t1)
+    F = cc_Fvv(t1, t2, E) if Fvv is None else Fvv
+    return F - t1.T @ fov + 2.0 * ein("kdac,kd->ac", E.ovvv, t1) - ein("kcad,kd->ac", E.ovvv, t1)
 
 
 def cc_Woooo(t1, t2, E):
@@ -154,6 +193,12 @@ def wvvvv_T(t1, E, out=None):
     # - sum_k (kc|bd) t_ka  ->  per (c,d): t1^T [a,k] @ (kc|bd)[k,b]
     Wf.baddbmm_(t1.T.unsqueeze(0).expand(v * v, v, o), E.ovvv_cdkb.view(v * v, o, v), alpha=-1.0)
     return W
+
+
+def wvvvv_sum_cd(t1, E):
+    """S[a,b] = sum_cd Wvvvv[a,b,c,d] without building Wvvvv:
+    sum_cd (ac|bd) - sum_k t_kb sum_cd (kd|ac) - sum_k t_ka sum_cd (kc|bd)."""
+    return E.S0 - E.U.T @ t1 - t1.T @ E.U
 
 
 def ccsd_energy(t1, t2, E):

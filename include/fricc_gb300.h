@@ -103,6 +103,28 @@ int fricc_contract(const char* term, const double* W, const int64_t W_dims[4], c
                    fricc_sparse* T, double* out, const int64_t out_dims[4], const int64_t out_strides[4],
                    void* stream);
 
+/* The kernel behind every term, in general form (no reference counterpart;
+ * each contract_DTSpT term is one instance of it):
+ *   Op[P][q] += coef * sum over nonzeros e with P_e == P of Wp[key_e][q] * value_e
+ * for q < QS, where P_e = slot[pa]*dims[pb] + slot[pb] and
+ * key_e = slot[ka]*dims[kb] + slot[kb] (slots 0..3 = the tensor's four
+ * indices).  Wp is contiguous [dims[ka]*dims[kb]][QS], Op contiguous
+ * [dims[pa]*dims[pb]][QS].  Each Op element receives its contributions in
+ * nonzero-slot order.  Stream-ordered. */
+int fricc_spmm(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const double* Wp, int64_t QS,
+               double* Op, void* stream);
+
+/* fricc_spmm in FP32-pair arithmetic (no reference counterpart): Wp2 is W'
+ * split into (hi, lo) float pairs by fricc_split_f2 (2*n floats, 8-byte
+ * aligned); every product and sum carries ~48 significand bits (relative
+ * error per output ~1e-14) and runs on the FP32 pipe.  Op stays FP64. */
+int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* Wp2, int64_t QS,
+                  double* Op, void* stream);
+
+/* out2[2i] + out2[2i+1] = x[i] to ~2^-48 relative: hi = (float)x,
+ * lo = (float)(x - hi).  Stream-ordered. */
+int fricc_split_f2(const double* x, int64_t n, float* out2, void* stream);
+
 /* Floating-point operations of one contract call (2 per multiply-add). */
 double fricc_contract_flops(const char* term, const fricc_sparse* T);
 

@@ -108,3 +108,29 @@ def test_bad_shapes_raise(gpulib):
         py_rccsd.contract_DTSpT(np.zeros((5, 5, 5, 4)), T, np.zeros((3, 3, 5, 5)), "2323")
     with pytest.raises(ValueError):
         py_rccsd.contract_DTSpT(np.zeros((5, 5, 5, 5)), T, np.zeros((3, 3, 5, 5)), "9999")
+
+
+def test_spmm_f2_matches_fp64(gpulib):
+    """The FP32-pair kernel against the FP64 kernel on the same generic SpMM
+    (o10v40-sized sparse tensor, 2323 layout and an O^3V^3 layout)."""
+    import ctypes
+    from fricc_gb300 import _lib, py_rccsd
+    from fricc_gb300.rccsd_dense import split_f2
+    rng = np.random.default_rng(3)
+    o, v = 10, 40
+    x = rng.standard_normal((o, o, v, v)) * np.exp(rng.standard_normal((o, o, v, v)))
+    T = py_rccsd.SparseTensor4d(x, x.shape, 20000, "fri", "systematic", rn=0.6)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for (pa, pb, ka, kb, nkey, QS) in ((0, 1, 2, 3, v * v, v * v), (1, 3, 0, 2, o * v, o * v), (3, 0, 1, 2, o * v, o * v)):
+        W = torch.from_numpy(rng.standard_normal((nkey, QS)) * 10.0 ** rng.integers(-6, 2, (nkey, 1))).cuda()
+        nP = {0: o, 1: o, 2: v, 3: v}[pa] * {0: o, 1: o, 2: v, 3: v}[pb]
+        out0 = torch.from_numpy(rng.standard_normal((nP, QS))).cuda()
+        a, b = out0.clone(), out0.clone()
+        _lib.check(gpulib.fricc_spmm(T.handle, pa, pb, ka, kb, -0.5, ctypes.c_void_p(W.data_ptr()), QS,
+                                     ctypes.c_void_p(a.data_ptr()), st))
+        W2 = split_f2(W)
+        _lib.check(gpulib.fricc_spmm_f2(T.handle, pa, pb, ka, kb, -0.5, ctypes.c_void_p(W2.data_ptr()), QS,
+                                        ctypes.c_void_p(b.data_ptr()), st))
+        a, b = a.cpu().numpy(), b.cpu().numpy()
+        # per-element error relative to the sum of |terms| is ~1e-14; compare to the output scale
+        assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max(), np.abs(a - b).max() / np.abs(a).max()

@@ -30,11 +30,11 @@ def _golden_system():
     return g, s
 
 
-def _solver(system, m):
+def _solver(system, m, precision="fp64"):
     from fricc_gb300.rccsd_dense import DeviceERIs
     from fricc_gb300.friccsd import FRICCSDGPU
     E = DeviceERIs.from_system(system)
-    return FRICCSDGPU(E, dict(SETTINGS, m_keep=m))
+    return FRICCSDGPU(E, dict(SETTINGS, m_keep=m), precision=precision)
 
 
 def _oracle_step(eris, m, t1, t2, rn):
@@ -62,14 +62,15 @@ def test_golden_iterates_teacher_forced(gpulib, oracle):
         assert abs(e - e_or) < 1e-10
 
 
-@pytest.mark.parametrize("seed", [0, 1])
-def test_o10v40_teacher_forced(gpulib, oracle, seed):
-    """The o10v40 workload (m = 20000): five steps along the GPU trajectory."""
+@pytest.mark.parametrize("seed,precision", [(0, "fp64"), (1, "fp64"), (0, "df64"), (2, "df64")])
+def test_o10v40_teacher_forced(gpulib, oracle, seed, precision):
+    """The o10v40 workload (m = 20000): five steps along the GPU trajectory,
+    with the sparse terms in FP64 or in FP32-pair arithmetic."""
     from oracle import pyscf_standin as P
     from fricc_gb300.synthetic import SyntheticSystem
     s = SyntheticSystem(10, 40, 200, 0.05, seed)
     m = 20000
-    gs = _solver(s, m)
+    gs = _solver(s, m, precision)
     eris = P.make_eris(s)
     t1h, t2h = s.mp2_amplitudes()
     rng = np.random.default_rng(seed)
