@@ -290,9 +290,9 @@ def run_gpu(args):
         kname, bound, peak = "k_spmm (bucketed sparse-T2 x dense-W, FP64)", "fp64", FP64_PEAK_TFLOPS
         psrc = "measured FP64 FMA rate of this GB300 pool (DFMA probe); FP64 is not in MEASURED_PEAKS.json"
     else:
-        kname, bound, peak = "k_spmm_df (bucketed sparse-T2 x dense-W, FP32 pairs)", "fp32-pipe", FP32_PEAK_TFLOPS / 6
-        psrc = ("FP32 FMA rate of this GB300 pool (74.2 TF/s, FFMA probe) / 12 FP32 instructions per "
-                "FP32-pair multiply-add, as FP64-equivalent flops")
+        kname, bound, peak = "k_spmm_df (bucketed sparse-T2 x dense-W, FP32 pairs)", "fp32-pipe", FP32_PEAK_TFLOPS / 12
+        psrc = ("FP32 FMA rate of this GB300 pool (74.2 TF/s = 37.1 T instructions/s, FFMA probe) / 12 FP32 "
+                "instructions per FP32-pair multiply-add, counted as 2 FP64-equivalent flops")
     roof = {"kernel": kname, "bound": bound,
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None,
