@@ -41,6 +41,8 @@ SIGNATURES = [
     ("fricc_spmm_f2", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_double, _dp, _i64, _dp, _vp]),
     ("fricc_split_f2", ctypes.c_int, [_dp, _i64, _dp, _vp]),
+    ("fricc_gemm_df", ctypes.c_int, [_dp, _dp, _dp, _i64, _i64, _i64, _i64, _i64p, _i64p, _i64p, ctypes.c_double,
+                                      ctypes.c_double, _vp]),
     ("fricc_contract_flops", ctypes.c_double, [ctypes.c_char_p, _vp]),
     ("fricc_compress", ctypes.c_int, [_dp, _i64, _i64, ctypes.c_int, ctypes.c_double, _dp, _dp, _i64p, _vp]),
     ("fricc_seq_cumsum", ctypes.c_int, [_dp, _i64, _dp, _vp]),

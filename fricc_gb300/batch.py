@@ -1,0 +1,227 @@
+"""Many FRI-CCSD solves on one GPU at once: replicas and served requests.
+
+* ``ReplicaBatch`` -- independent FRI replicas of one system (distinct seeds)
+  sharing the integrals in HBM; every replica keeps its own amplitudes, its
+  two compressed-T2 handles and its own copy of the reference's libc random
+  stream (``GlibcRand``), so each replica's trajectory is exactly the one a
+  lone run with that seed gives.  One ``step()`` advances every replica by
+  one iteration; replicas are spread over a pool of CUDA streams driven by
+  host threads, so their kernels overlap on the device.
+* ``SolveServer`` -- a request loop for solves of different (nocc, nvir):
+  requests arrive over time, are admitted while their estimated HBM footprint
+  fits a budget, keep their state resident while they iterate, and run
+  concurrently on the stream pool; it records arrival, admission, start and
+  finish times for latency percentiles and solves/s.
+
+Host threads release the GIL inside every CUDA-library call and inside
+torch's kernels, so the pool keeps several solves' work in flight.
+"""
+from __future__ import annotations
+
+import math
+import queue
+import threading
+import time
+from dataclasses import dataclass, field
+
+import numpy as np
+import torch
+
+from .friccsd import FRICCSDGPU
+from .rccsd_dense import DeviceERIs
+from .rng import GlibcRand
+from .synthetic import SyntheticSystem
+
+
+def mp2_device(E: DeviceERIs):
+    o = E.nocc
+    e = E.mo_energy
+    eia = e[:o, None] - e[None, o:]
+    t2 = (E.ovov.permute(0, 2, 1, 3) / (eia[:, None, :, None] + eia[None, :, None, :])).contiguous()
+    t1 = torch.zeros(o, e.numel() - o, dtype=torch.float64, device=E.device)
+    return t1, t2
+
+
+class ReplicaBatch:
+    def __init__(self, eris: DeviceERIs, settings: dict, seeds, n_streams: int = 8, precision: str = "df64"):
+        self.eris = eris
+        self.seeds = list(seeds)
+        self.n = len(self.seeds)
+        self.solvers = [FRICCSDGPU(eris, settings, rn_draw=GlibcRand(s), precision=precision) for s in self.seeds]
+        t1, t2 = mp2_device(eris)
+        self.t1 = [t1.clone() for _ in range(self.n)]
+        self.t2 = [t2.clone() for _ in range(self.n)]
+        self.k = max(1, min(n_streams, self.n))
+        self.streams = [torch.cuda.Stream(device=eris.device) for _ in range(self.k)]
+        self.history = [[] for _ in range(self.n)]
+        self._errors = []
+        self._dev = eris.device.index if eris.device.index is not None else torch.cuda.current_device()
+
+    def _work(self, w):
+        try:
+            torch.cuda.set_device(self._dev)
+            with torch.cuda.stream(self.streams[w]):
+                for r in range(w, self.n, self.k):
+                    self.t1[r], self.t2[r] = self.solvers[r].update_amps(self.t1[r], self.t2[r])
+        except BaseException as e:  # surfaced by step()
+            self._errors.append(e)
+
+    def step(self, record: bool = True):
+        """One iteration of every replica (all streams joined on return)."""
+        threads = [threading.Thread(target=self._work, args=(w,)) for w in range(self.k)]
+        for t in threads:
+            t.start()
+        for t in threads:
+            t.join()
+        if self._errors:
+            raise self._errors[0]
+        for s in self.streams:
+            s.synchronize()
+        if record:
+            for r in range(self.n):
+                self.history[r].append(self.solvers[r].read_energy()[0])
+
+    def energies(self) -> np.ndarray:
+        return np.array([h[-1] for h in self.history])
+
+    def stats(self):
+        e = self.energies()
+        return float(e.mean()), float(e.var(ddof=1)) if e.size > 1 else 0.0
+
+
+# ---------------------------------------------------------------------------
+@dataclass
+class Request:
+    rid: int
+    arrival: float           # seconds after the stream starts
+    nocc: int
+    nvir: int
+    naux: int
+    frac: float              # kept fraction of o^2 v^2
+    seed: int
+    sigma: float = 0.05
+    # filled in by the server
+    admitted: float = math.nan
+    started: float = math.nan
+    finished: float = math.nan
+    iterations: int = 0
+    converged: bool = False
+    e_corr: float = math.nan
+    energies: list = field(default_factory=list)
+
+    @property
+    def m(self):
+        return max(1, int(self.frac * self.nocc * self.nocc * self.nvir * self.nvir))
+
+
+def request_stream(n: int, rate: float, seed: int = 0, nocc=(5, 30), ratio=(4.0, 6.0), frac=(0.05, 0.20)):
+    """Poisson arrivals; nocc ~ U{lo..hi}, nvir = ceil(r nocc) with r ~ U[ratio],
+    naux = 8 (nocc + nvir), kept fraction ~ U[frac], a seed per request."""
+    rng = np.random.default_rng(seed)
+    t = 0.0
+    out = []
+    for i in range(n):
+        t += rng.exponential(1.0 / rate)
+        o = int(rng.integers(nocc[0], nocc[1] + 1))
+        v = int(math.ceil(rng.uniform(*ratio) * o))
+        out.append(Request(i, t, o, v, 8 * (o + v), float(rng.uniform(*frac)), int(rng.integers(1, 2**31 - 1))))
+    return out
+
+
+def footprint_bytes(o: int, v: int) -> int:
+    """HBM a resident solve needs: integral blocks and the layouts derived from
+    them (vvvv twice, ovvv six times), amplitudes and work arrays (~16 o^2v^2)."""
+    return 8 * (2 * v**4 + 7 * o * v**3 + 16 * o * o * v * v + 4 * o**4 + 8 * o**3 * v)
+
+
+class SolveServer:
+    def __init__(self, n_workers: int = 8, hbm_budget: float = 200e9, precision: str = "df64", max_cycle: int = 30,
+                 tol: float = 1e-7, device="cuda"):
+        self.k = n_workers
+        self.budget = hbm_budget
+        self.precision = precision
+        self.max_cycle = max_cycle
+        self.tol = tol
+        self.device = torch.device(device)
+        if self.device.index is None:
+            self.device = torch.device("cuda", torch.cuda.current_device())
+        self._in_use = 0
+        self._cv = threading.Condition()
+
+    def _solve(self, req: Request, t0: float, stream):
+        with torch.cuda.stream(stream):
+            system = SyntheticSystem(req.nocc, req.nvir, req.naux, req.sigma, req.seed)
+            E = DeviceERIs.from_system(system, device=self.device)
+            solver = FRICCSDGPU(E, {"m_keep": req.m}, rn_draw=GlibcRand(req.seed), precision=self.precision)
+            t1, t2 = mp2_device(E)
+            req.started = time.perf_counter() - t0
+            eold = solver.energy(t1, t2)
+            for it in range(self.max_cycle):
+                t1, t2 = solver.update_amps(t1, t2)
+                e, normt = solver.read_energy()
+                req.energies.append(e)
+                req.iterations = it + 1
+                if abs(e - eold) < self.tol:
+                    req.converged = True
+                    break
+                if not math.isfinite(e) or abs(e - eold) > 1e5:
+                    break
+                eold = e
+            req.e_corr = req.energies[-1] if req.energies else math.nan
+            stream.synchronize()
+            del solver, E, t1, t2
+
+    def run(self, requests, time_scale: float = 1.0):
+        """Serve the requests (arrival times scaled by time_scale); returns them filled in."""
+        reqs = sorted(requests, key=lambda r: r.arrival)
+        admitted = queue.Queue()
+        t0 = time.perf_counter()
+        errors = []
+
+        def dispatcher():
+            for r in reqs:
+                delay = r.arrival * time_scale - (time.perf_counter() - t0)
+                if delay > 0:
+                    time.sleep(delay)
+                need = footprint_bytes(r.nocc, r.nvir)
+                with self._cv:
+                    while self._in_use + need > self.budget and self._in_use > 0:
+                        self._cv.wait()
+                    self._in_use += need
+                r.admitted = time.perf_counter() - t0
+                admitted.put(r)
+            for _ in range(self.k):
+                admitted.put(None)
+
+        def worker(w):
+            torch.cuda.set_device(self.device)
+            stream = torch.cuda.Stream(device=self.device)
+            while True:
+                r = admitted.get()
+                if r is None:
+                    return
+                try:
+                    self._solve(r, t0, stream)
+                except BaseException as e:
+                    errors.append(e)
+                r.finished = time.perf_counter() - t0
+                with self._cv:
+                    self._in_use -= footprint_bytes(r.nocc, r.nvir)
+                    self._cv.notify_all()
+
+        th = [threading.Thread(target=dispatcher)] + [threading.Thread(target=worker, args=(w,)) for w in range(self.k)]
+        for t in th:
+            t.start()
+        for t in th:
+            t.join()
+        if errors:
+            raise errors[0]
+        return reqs
+
+
+def latency_summary(reqs, time_scale=1.0):
+    lat = np.array([r.finished - r.arrival * time_scale for r in reqs])
+    span = max(r.finished for r in reqs) - min(r.arrival * time_scale for r in reqs)
+    return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
+            "solves_per_s": len(reqs) / span, "iterations": int(sum(r.iterations for r in reqs)),
+            "converged": int(sum(r.converged for r in reqs)), "n": len(reqs)}

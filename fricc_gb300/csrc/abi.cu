@@ -21,6 +21,9 @@ int fricc_spmm_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coe
 int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float2* Wp, int64_t QS,
                          double* Op, cudaStream_t st);
 int fricc_split_f2_device(const double* x, int64_t n, float2* out, cudaStream_t st);
+int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
+                         const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
+                         cudaStream_t st);
 int fricc_energy_update_device(const double* t1num, const double* t2num, const double* eia, const double* fov,
                                const double* ovov, const double* t1old, const double* t2old, int64_t o, int64_t v,
                                double* t1out, double* t2out, double* res, cudaStream_t st);
@@ -352,6 +355,16 @@ int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, 
 
 int fricc_split_f2(const double* x, int64_t n, float* out2, void* stream) {
   return fricc_split_f2_device(x, n, reinterpret_cast<float2*>(out2), as_stream(stream));
+}
+
+int fricc_gemm_df(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
+                  const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
+                  void* stream) {
+  if (!sA || !sB || !sC) {
+    fricc_set_error("gemm_df: null stride array");
+    return FRICC_ERR_ARG;
+  }
+  return fricc_gemm_df_device(A, B, C, batch, M, N, K, sA, sB, sC, alpha, beta, as_stream(stream));
 }
 
 double fricc_contract_flops(const char* term, const fricc_sparse* T) {

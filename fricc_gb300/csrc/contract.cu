@@ -159,6 +159,33 @@ __device__ __forceinline__ float2 split_f2(double d) {
 constexpr int DF_NT = 128;
 constexpr int DF_QPT = 4;
 
+template <bool FULL>
+__device__ __forceinline__ void df_tile(const int* __restrict__ srow, const float2* __restrict__ sval, int cnt,
+                                        const float2* __restrict__ wq, int64_t QS, int64_t qrem, float* ah,
+                                        float* al) {
+  for (int j = 0; j < cnt; ++j) {
+    const float2* w = wq + (int64_t)srow[j] * QS;
+    const float2 v = sval[j];
+#pragma unroll
+    for (int k = 0; k < DF_QPT; ++k) {
+      if (FULL || k * DF_NT < qrem) {
+        // explicit _rn intrinsics: the error-free transforms must not be
+        // contracted into fused multiply-adds by the compiler
+        const float2 x = w[k * DF_NT];
+        const float ph = __fmul_rn(x.x, v.x);
+        float pl = __fmaf_rn(x.x, v.x, -ph);
+        pl = __fmaf_rn(x.x, v.y, pl);
+        pl = __fmaf_rn(x.y, v.x, pl);
+        const float s = __fadd_rn(ah[k], ph);
+        const float z = __fsub_rn(s, ah[k]);
+        const float err = __fadd_rn(__fsub_rn(ah[k], __fsub_rn(s, z)), __fsub_rn(ph, z));
+        al[k] = __fadd_rn(al[k], __fadd_rn(err, pl));
+        ah[k] = s;
+      }
+    }
+  }
+}
+
 __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr, const int* __restrict__ erow,
                                                    const float2* __restrict__ eval, const float2* __restrict__ Wp,
                                                    double* __restrict__ Op, int64_t QS) {
@@ -168,16 +195,17 @@ __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr,
   const int e0 = bptr[P], e1 = bptr[P + 1];
   if (e0 == e1) return;
   const int64_t q0 = (int64_t)blockIdx.y * (DF_NT * DF_QPT) + threadIdx.x;
+  const int64_t qrem = QS - q0;  // this thread's q values are q0 + k*DF_NT < QS  <=>  k*DF_NT < qrem
+  const bool full = (int64_t)(blockIdx.y + 1) * (DF_NT * DF_QPT) <= QS;  // uniform per block
   double* orow = Op + P * QS;
+  const float2* wq = Wp + q0;
   float ah[DF_QPT], al[DF_QPT];
 #pragma unroll
   for (int k = 0; k < DF_QPT; ++k) {
-    const int64_t q = q0 + k * DF_NT;
-    const float2 a = split_f2(q < QS ? orow[q] : 0.0);
+    const float2 a = split_f2(k * DF_NT < qrem ? orow[q0 + k * DF_NT] : 0.0);
     ah[k] = a.x;
     al[k] = a.y;
   }
-  int since = 0;
   for (int eb = e0; eb < e1; eb += DF_NT) {
     const int cnt = e1 - eb < DF_NT ? e1 - eb : DF_NT;
     __syncthreads();
@@ -186,43 +214,19 @@ __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr,
       sval[threadIdx.x] = eval[eb + threadIdx.x];
     }
     __syncthreads();
-    for (int j = 0; j < cnt; ++j) {
-      const float2* w = Wp + (int64_t)srow[j] * QS;
-      const float2 v = sval[j];
+    if (full) df_tile<true>(srow, sval, cnt, wq, QS, qrem, ah, al);
+    else df_tile<false>(srow, sval, cnt, wq, QS, qrem, ah, al);
+    // renormalise once per staged chunk (<= DF_NT terms): keeps |al| ~ ulp(ah)
 #pragma unroll
-      for (int k = 0; k < DF_QPT; ++k) {
-        const int64_t q = q0 + k * DF_NT;
-        if (q < QS) {
-          // explicit _rn intrinsics: the error-free transforms must not be
-          // contracted into fused multiply-adds by the compiler
-          const float2 x = w[q];
-          const float ph = __fmul_rn(x.x, v.x);
-          float pl = __fmaf_rn(x.x, v.x, -ph);
-          pl = __fmaf_rn(x.x, v.y, pl);
-          pl = __fmaf_rn(x.y, v.x, pl);
-          const float s = __fadd_rn(ah[k], ph);
-          const float z = __fsub_rn(s, ah[k]);
-          const float err = __fadd_rn(__fsub_rn(ah[k], __fsub_rn(s, z)), __fsub_rn(ph, z));
-          al[k] = __fadd_rn(al[k], __fadd_rn(err, pl));
-          ah[k] = s;
-        }
-      }
-      if (++since == 32) {
-        since = 0;
-#pragma unroll
-        for (int k = 0; k < DF_QPT; ++k) {
-          const float s = __fadd_rn(ah[k], al[k]);
-          al[k] = __fsub_rn(al[k], __fsub_rn(s, ah[k]));
-          ah[k] = s;
-        }
-      }
+    for (int k = 0; k < DF_QPT; ++k) {
+      const float s = __fadd_rn(ah[k], al[k]);
+      al[k] = __fsub_rn(al[k], __fsub_rn(s, ah[k]));
+      ah[k] = s;
     }
   }
 #pragma unroll
-  for (int k = 0; k < DF_QPT; ++k) {
-    const int64_t q = q0 + k * DF_NT;
-    if (q < QS) orow[q] = (double)ah[k] + (double)al[k];
-  }
+  for (int k = 0; k < DF_QPT; ++k)
+    if (k * DF_NT < qrem) orow[q0 + k * DF_NT] = (double)ah[k] + (double)al[k];
 }
 
 __global__ void k_entries_df(const int* __restrict__ slots, const double* __restrict__ vals,

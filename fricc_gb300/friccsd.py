@@ -171,8 +171,15 @@ class FRICCSDGPU:
         T = self._sp.compress(t2, m, s["compression"], rn[0], st)
         Tw = self._sp_w.compress(t2, m, s["compression"], rn[1], st) if need_w else None
 
-        Foo0 = D.cc_Foo(t1, t2, E)
-        Fvv0 = D.cc_Fvv(t1, t2, E)
+        mm = D.gemm_df if self.precision == "df64" else D.gemm_torch
+        f64, dev = t2.dtype, t2.device
+        # cc_Foo / cc_Fvv share tt[p,q,r,s] = t2 + t1[p,r] t1[q,s]
+        tt = t2 + ein("pr,qs->pqrs", t1, t1)
+        Foo0 = E.fock[:o, :o].clone()                     # f_ki + sum_lcd g[k,c,l,d] tt[i,l,c,d]
+        mm(E.g_klcd.view(o, o * v * v), tt.view(o, o * v * v).T, Foo0, 1.0, 1.0)
+        Fvv0 = E.fock[o:, o:].clone()                     # f_ac - sum_kld g[k,c,l,d] tt[k,l,a,d]
+        mm(tt.permute(2, 0, 1, 3).contiguous().view(v, o * o * v), E.g_kldc.view(o * o * v, v), Fvv0, -1.0, 1.0)
+        del tt
         Fov = D.cc_Fov(t1, t2, E)
         Foo = Foo0.clone()
         Fvv = Fvv0.clone()
@@ -187,15 +194,17 @@ class FRICCSDGPU:
         t1new += ein("kc,ic,ka->ia", Fov, t1, t1)
         t1new += fov
         t1new += 2 * ein("kcai,kc->ia", E.ovvo, t1) - ein("kiac,kc->ia", E.oovv, t1)
-        G = E.G_t1.view(o * v * v, v)
-        t1new += t2.view(o, o * v * v) @ G                                   # O^2V^3, :165-166
+        t1new = t1new.contiguous()
+        mm(t2.view(o, o * v * v), E.G_t1.view(o * v * v, v), t1new, 1.0, 1.0)  # O^2V^3, :165-166
         t1new += t1 @ (t1.reshape(1, ov) @ E.G_t1.permute(0, 2, 1, 3).reshape(ov, v * v)).view(v, v)  # :167-168
         t1new += -2 * ein("lcki,klac->ia", E.ovoo, t2) + ein("kcli,klac->ia", E.ovoo, t2)
         t1new += -2 * ein("lcki,lc,ka->ia", E.ovoo, t1, t1) + ein("kcli,lc,ka->ia", E.ovoo, t1, t1)
 
         # T2 driver terms (:179-187)
         Y1 = ein("kibc,jc->kibj", E.oovv, t1)
-        tmp = ein("iacb,jc->ijab", E.ovvv, t1) - ein("ka,kibj->ijab", t1, Y1)
+        R = torch.empty(o * v * v, o, dtype=f64, device=dev)   # R[(i,a,b), j] = sum_c (ia|cb) t_jc
+        mm(E.ovvv_iabc.view(o * v * v, v), t1.T, R, 1.0, 0.0)
+        tmp = R.view(o, v, v, o).permute(0, 3, 1, 2) - ein("ka,kibj->ijab", t1, Y1)
         t2new = tmp + tmp.permute(1, 0, 3, 2)
         tmp2 = ein("kcai,jc->akij", E.ovvo, t1) + E.ovoo.permute(1, 3, 0, 2)
         tmp = ein("akij,kb->ijab", tmp2, t1)
@@ -209,21 +218,28 @@ class FRICCSDGPU:
         Lvv.diagonal().sub_(e_v)
 
         if "O^4V^2" in comp:  # sparse_cc_Woooo (:309-322)
-            Woooo = (ein("lcki,jc->klij", E.ovoo, t1) + ein("kclj,ic->klij", E.ovoo, t1)).contiguous()
-            self._contract("1323", E.ovov, Tw, Woooo, st)
+            Wo = (ein("lcki,jc->klij", E.ovoo, t1) + ein("kclj,ic->klij", E.ovoo, t1)).permute(2, 3, 0, 1)
+            Wo = Wo.contiguous()                                                  # [i,j,k,l]
+            self._spmm(Tw, 0, 1, 2, 3, 1.0, E.ovov_cdkl, o * o, Wo, st, const="ovov_cdkl")  # 1323
+            Woooo = Wo.permute(2, 3, 0, 1)                                        # (k,l,i,j)
             Woooo += ein("kcld,ic,jd->klij", E.ovov, t1, t1)
             Woooo += E.oooo.permute(0, 2, 1, 3)
         else:
             Woooo = D.cc_Woooo(t1, t2, E)
 
         if "O^3V^3" in comp:  # sparse_cc_Wvoov / sparse_cc_Wvovo (:334-376)
-            Wvoov = ein("kcad,id->akic", E.ovvv, t1) - ein("kcli,la->akic", E.ovoo, t1) + E.ovvo.permute(2, 0, 3, 1)
+            R = torch.empty(o * v * v, o, dtype=f64, device=dev)   # R[(k,c,a), i] = sum_d (kc|ad) t_id
+            mm(E.ovvv.view(o * v * v, v), t1.T, R, 1.0, 0.0)
+            Wvoov = (R.view(o, v, v, o).permute(2, 0, 3, 1) - ein("kcli,la->akic", E.ovoo, t1)
+                     + E.ovvo.permute(2, 0, 3, 1))
             Wp = Wvoov.permute(0, 2, 1, 3).contiguous()                         # [a,i,k,c]
             self._spmm(Tw, 3, 0, 1, 2, -0.5, E.ovov, ov, Wp, st, const="ovov")                     # 0112
             self._spmm(Tw, 2, 0, 1, 3, 1.0, E.ovov_0313_0113, ov, Wp, st, const="ovov_0313_0113")  # 0313+0113
             Wvoov = Wp.permute(0, 2, 1, 3)                                      # (a,k,i,c)
             Wvoov -= ein("ldkc,id,la->akic", E.ovov, t1, t1)
-            Wvovo = ein("kdac,id->akci", E.ovvv, t1) - ein("lcki,la->akci", E.ovoo, t1) + E.oovv.permute(2, 0, 3, 1)
+            mm(E.ovvv_kacd.view(o * v * v, v), t1.T, R, 1.0, 0.0)   # R[(k,a,c), i] = sum_d (kd|ac) t_id
+            Wvovo = (R.view(o, v, v, o).permute(1, 0, 2, 3) - ein("lcki,la->akci", E.ovoo, t1)
+                     + E.oovv.permute(2, 0, 3, 1))
             Wq = Wvovo.permute(0, 3, 1, 2).contiguous()                         # [a,i,k,c]
             self._spmm(Tw, 3, 0, 1, 2, -0.5, E.ovov_0312, ov, Wq, st, const="ovov_0312")          # 0312
             Wvovo = Wq.permute(0, 2, 3, 1)                                      # (a,k,c,i)
@@ -234,7 +250,10 @@ class FRICCSDGPU:
 
         if "O^4V^2" in comp:
             t2new += ein("klij,ka,lb->ijab", Woooo, t1, t1)
-            self._contract("0101", Woooo, T, t2new, st)
+            Tp = t2new.permute(2, 3, 0, 1).contiguous()                           # [a,b,i,j]
+            self._spmm(T, 2, 3, 0, 1, 1.0, Woooo.contiguous(), o * o, Tp, st)     # 0101
+            t2new.copy_(Tp.permute(2, 3, 0, 1))
+            del Tp
         else:
             tau = t2 + ein("ia,jb->ijab", t1, t1)
             t2new += ein("klij,klab->ijab", Woooo, tau)
@@ -248,7 +267,10 @@ class FRICCSDGPU:
                 self._spmm(T, 0, 1, 2, 3, 1.0, E.vvvvT, v * v, t2new, st, const="vvvvT")  # (ac|bd) of 2323
                 XY = torch.zeros(o, o, 2, o, v, dtype=t2.dtype, device=t2.device)
                 self._spmm(T, 0, 1, 2, 3, 1.0, E.ovvv_XY, 2 * ov, XY, st, const="ovvv_XY")  # t1 parts
-                t2new -= ein("ijka,kb->ijab", XY[:, :, 0], t1) + ein("ijkb,ka->ijab", XY[:, :, 1], t1)
+                XYv = XY.view(o * o, 2, o, v)
+                t2v = t2new.view(o * o, v, v)
+                mm(XYv[:, 0].transpose(1, 2), t1.unsqueeze(0).expand(o * o, o, v), t2v, -1.0, 1.0)  # -X t1
+                mm(t1.T.unsqueeze(0).expand(o * o, v, o), XYv[:, 1], t2v, -1.0, 1.0)               # -t1 Y
             else:
                 WT = D.wvvvv_T(t1, E)
                 t2new += ein("abcd,ijcd->ijab", WT.permute(2, 3, 0, 1), t2)
@@ -261,8 +283,12 @@ class FRICCSDGPU:
             else:
                 t2new += ein("abcd,ijcd->ijab", Wvvvv, t2)
 
-        t2new += _sym(ein("ac,ijcb->ijab", Lvv, t2))
-        t2new -= _sym(ein("ki,kjab->ijab", Loo, t2))
+        tmpL = torch.empty_like(t2)
+        mm(Lvv.unsqueeze(0).expand(o * o, v, v), t2.view(o * o, v, v), tmpL.view(o * o, v, v), 1.0, 0.0)
+        t2new += _sym(tmpL)                                 # Lvv t2, :238-239
+        mm(Loo.T, t2.view(o, o * v * v), tmpL.view(o, o * v * v), 1.0, 0.0)
+        t2new -= _sym(tmpL)                                 # Loo t2, :240-241
+        del tmpL
 
         if "O^3V^3" in comp:
             WA = Wvoov.permute(1, 3, 2, 0).contiguous()      # [k,c,i,a] = Wvoov(a,k,i,c)

@@ -62,6 +62,12 @@ class DeviceERIs:
         # W' of the sparse W-intermediate terms, [l,d,k,c]
         self.ovov_0312 = ovov.permute(0, 3, 2, 1).contiguous()            # (lc|kd)
         self.ovov_0313_0113 = (ovov - 0.5 * ovov.permute(0, 3, 2, 1)).contiguous()
+        self.ovov_cdkl = ovov.permute(1, 3, 0, 2).contiguous()            # 1323: [c,d,k,l] = (kc|ld)
+        # GEMM-ready layouts for the dense O^2V^3 contractions
+        self.g_klcd = self.g_ovov.permute(0, 2, 1, 3).contiguous()       # cc_Foo
+        self.g_kldc = self.g_ovov.permute(0, 2, 3, 1).contiguous()       # cc_Fvv
+        self.ovvv_iabc = ovvv.permute(0, 1, 3, 2).contiguous()           # T2 driver term
+        self.ovvv_kacd = ovvv.permute(0, 2, 3, 1).contiguous()           # Wvovo t1 term
         self._dense_wvvvv = None
         self._splits = {}
 
@@ -112,6 +118,43 @@ class DeviceERIs:
         out = {k: getattr(self, k).cpu().numpy() for k in ("oooo", "ovoo", "ovov", "oovv", "ovvo", "ovvv")}
         out["vvvv"] = self.vvvvT.permute(2, 0, 3, 1).contiguous().cpu().numpy()  # (ab|cd)
         return out
+
+
+def _strides3(t: torch.Tensor):
+    if t.dim() == 2:
+        return (t.stride(0), t.stride(1), 0), 1
+    return (t.stride(1), t.stride(2), t.stride(0)), t.shape[0]
+
+
+def gemm_df(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.0, beta: float = 0.0):
+    """C = alpha A @ B + beta C on the FP32-pair GEMM kernel; FP64 tensors with
+    any strides, 2-D or batched 3-D (a batch stride of 0 shares an operand)."""
+    import ctypes
+
+    from . import _lib as L
+    sA, bA = _strides3(A)
+    sB, bB = _strides3(B)
+    sC, batch = _strides3(C)
+    M, N = C.shape[-2], C.shape[-1]
+    K = A.shape[-1]
+    assert A.shape[-2] == M and B.shape[-2] == K and B.shape[-1] == N and bA in (1, batch) and bB in (1, batch)
+    L.check(L.load().fricc_gemm_df(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
+                                   ctypes.c_void_p(C.data_ptr()), batch, M, N, K, L.i64arr(sA), L.i64arr(sB),
+                                   L.i64arr(sC), float(alpha), float(beta),
+                                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return C
+
+
+def gemm_torch(A, B, C, alpha=1.0, beta=0.0):
+    """The same contract on cuBLAS FP64."""
+    R = torch.matmul(A, B)
+    if beta == 0.0:
+        C.copy_(R.mul_(alpha) if alpha != 1.0 else R)
+    else:
+        if beta != 1.0:
+            C.mul_(beta)
+        C.add_(R, alpha=alpha)
+    return C
 
 
 def split_f2(x: torch.Tensor) -> torch.Tensor:

@@ -1,0 +1,93 @@
+"""Throughput of the batched and served forms (python -m fricc_gb300.serve_bench).
+
+  --mode replicas : R independent FRI replicas (distinct seeds) of the
+                    o20v100 system (naux=600, m = 5% of o^2 v^2), all resident,
+                    iterated together on a pool of streams; prints iterations/s
+                    of the whole batch and the replica mean and variance of E_corr.
+  --mode serve    : a Poisson stream of solve requests (nocc ~ U{5..30},
+                    nvir = ceil(r nocc) with r ~ U[4,6], naux = 8(o+v), kept
+                    fraction ~ U[5%,20%], converged at |dE| < 1e-7 Eh or
+                    after --max-cycle iterations) served concurrently, against
+                    the same requests solved one at a time in plain FP64;
+                    prints solves/s and p50/p99 time to converged energy.
+One JSON line per mode.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import time
+
+import numpy as np
+import torch
+
+from .batch import ReplicaBatch, SolveServer, latency_summary, request_stream
+from .rccsd_dense import DeviceERIs
+from .synthetic import WORKLOADS, make_system
+
+
+def run_replicas(args):
+    w = WORKLOADS["o20v100x64"]
+    system = make_system("o20v100x64", seed=0)
+    E = DeviceERIs.from_system(system)
+    settings = {"m_keep": w["m"]}
+    seeds = [1000 + r for r in range(args.replicas)]
+    batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision)
+    for _ in range(args.warmup):
+        batch.step()
+    torch.cuda.synchronize()
+    t = time.perf_counter()
+    for _ in range(args.steps):
+        batch.step()
+    torch.cuda.synchronize()
+    dt = time.perf_counter() - t
+    mean, var = batch.stats()
+    return {"mode": "replicas", "workload": "o20v100: nocc=20 nvir=100 naux=600 m=200000 per replica",
+            "replicas": args.replicas, "streams": args.streams, "precision": args.precision,
+            "iterations_per_s": args.replicas * args.steps / dt, "batch_steps_per_s": args.steps / dt,
+            "e_corr_mean": mean, "e_corr_var": var, "iterations_each": args.warmup + args.steps}
+
+
+def run_serve(args):
+    reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
+    server = SolveServer(n_workers=args.streams, precision=args.precision, max_cycle=args.max_cycle)
+    out = server.run(reqs, time_scale=1.0)
+    served = latency_summary(out)
+    line = {"mode": "serve", "requests": args.requests, "rate_per_s": args.rate, "workers": args.streams,
+            "precision": args.precision, "max_cycle": args.max_cycle, "served": served}
+    if args.plain:
+        # the same requests, one at a time, FP64, arriving all at once
+        plain_reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
+        for r in plain_reqs:
+            r.arrival = 0.0
+        plain = SolveServer(n_workers=1, precision="fp64", max_cycle=args.max_cycle).run(plain_reqs)
+        line["plain"] = latency_summary(plain)
+        diffs = [abs(a.e_corr - b.e_corr) for a, b in zip(sorted(out, key=lambda r: r.rid),
+                                                          sorted(plain_reqs, key=lambda r: r.rid))]
+        line["max_abs_dE_vs_plain"] = float(np.max(diffs))
+        line["speedup_solves_per_s"] = served["solves_per_s"] / line["plain"]["solves_per_s"]
+    return line
+
+
+def main():
+    p = argparse.ArgumentParser()
+    p.add_argument("--mode", default="replicas", choices=["replicas", "serve"])
+    p.add_argument("--replicas", type=int, default=64)
+    p.add_argument("--streams", type=int, default=8)
+    p.add_argument("--steps", type=int, default=3)
+    p.add_argument("--warmup", type=int, default=1)
+    p.add_argument("--precision", default="df64", choices=["fp64", "df64"])
+    p.add_argument("--requests", type=int, default=40)
+    p.add_argument("--rate", type=float, default=50.0)
+    p.add_argument("--seed", type=int, default=0)
+    p.add_argument("--nocc-min", type=int, default=5)
+    p.add_argument("--nocc-max", type=int, default=30)
+    p.add_argument("--max-cycle", type=int, default=30)
+    p.add_argument("--plain", action="store_true")
+    args = p.parse_args()
+    line = run_replicas(args) if args.mode == "replicas" else run_serve(args)
+    print(json.dumps(line))
+
+
+if __name__ == "__main__":
+    main()

@@ -125,6 +125,16 @@ int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, 
  * lo = (float)(x - hi).  Stream-ordered. */
 int fricc_split_f2(const double* x, int64_t n, float* out2, void* stream);
 
+/* Strided batched GEMM, FP64 in and out, products and sums in FP32 pairs
+ * (no reference counterpart; it runs the dense O^2V^3 contractions of the
+ * iteration):  C[b] = alpha * A[b] @ B[b] + beta * C[b], b < batch.
+ * sA = {row, col, batch} element strides of the M x K matrix A, likewise sB
+ * for K x N and sC for M x N.  Deterministic (a long K is split and the
+ * partials summed in a fixed order).  Stream-ordered. */
+int fricc_gemm_df(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
+                  const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
+                  void* stream);
+
 /* Floating-point operations of one contract call (2 per multiply-add). */
 double fricc_contract_flops(const char* term, const fricc_sparse* T);
 

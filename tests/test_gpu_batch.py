@@ -1,0 +1,47 @@
+"""Batched replicas and served requests: every result is the same alone and in
+the mix (same seed, same draws; kernels are deterministic, so the energies
+agree to rounding: bound 1e-10 Eh, in practice bit for bit)."""
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def test_replicas_alone_and_in_the_mix(gpulib):
+    from fricc_gb300.batch import ReplicaBatch, mp2_device
+    from fricc_gb300.friccsd import FRICCSDGPU
+    from fricc_gb300.rccsd_dense import DeviceERIs
+    from fricc_gb300.rng import GlibcRand
+    from fricc_gb300.synthetic import SyntheticSystem
+    s = SyntheticSystem(6, 24, 120, 0.05, 3)
+    E = DeviceERIs.from_system(s)
+    settings = {"m_keep": 4000}
+    seeds = [11, 12, 13, 14, 15]
+    batch = ReplicaBatch(E, settings, seeds, n_streams=3, precision="df64")
+    for _ in range(4):
+        batch.step()
+    for r, seed in enumerate(seeds):
+        lone = FRICCSDGPU(E, settings, rn_draw=GlibcRand(seed), precision="df64")
+        t1, t2 = mp2_device(E)
+        hist = []
+        for _ in range(4):
+            t1, t2 = lone.update_amps(t1, t2)
+            hist.append(lone.read_energy()[0])
+        assert np.max(np.abs(np.array(hist) - np.array(batch.history[r]))) < 1e-10, (r, hist, batch.history[r])
+    mean, var = batch.stats()
+    assert np.isfinite(mean) and var > 0.0  # distinct seeds give distinct samples
+
+
+def test_served_requests_match_lone_solves(gpulib):
+    from fricc_gb300.batch import SolveServer, request_stream
+    reqs = request_stream(6, rate=200.0, seed=5, nocc=(4, 7))
+    out = SolveServer(n_workers=3, precision="df64", max_cycle=4).run(reqs)
+    for r in out:
+        assert r.iterations >= 1 and np.isfinite(r.e_corr)
+        assert r.admitted >= r.arrival - 1e-6 and r.finished >= r.started
+    lone = request_stream(6, rate=200.0, seed=5, nocc=(4, 7))
+    for r in lone:
+        SolveServer(n_workers=1, precision="df64", max_cycle=4).run([r])
+    for a, b in zip(sorted(out, key=lambda r: r.rid), sorted(lone, key=lambda r: r.rid)):
+        assert abs(a.e_corr - b.e_corr) < 1e-10, (a.rid, a.e_corr, b.e_corr)
