@@ -58,7 +58,7 @@ def parse():
     p.add_argument("--workload", default="o30v150")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--precision", default="fp64", choices=["fp64", "df64"],
+    p.add_argument("--precision", default="df64", choices=["fp64", "df64"],
                    help="arithmetic of the sparse terms: FP64, or FP32 pairs (~48-bit) on the FP32 pipe")
     return p.parse_args()
 
@@ -229,6 +229,18 @@ def run_gpu(args):
         t1, t2 = solver.update_amps(t1, t2)
     torch.cuda.synchronize()
 
+    # |dE_corr| of one step against the plain FP64 GPU path on the same
+    # amplitudes and draws (outside the timed region)
+    delta_e = None
+    if args.precision != "fp64":
+        ref_solver = FRICCSDGPU(E, {"m_keep": m}, precision="fp64")
+        solver.update_amps(t1, t2, rn=[0.3141592653589793, 0.2718281828459045])
+        e_mixed = solver.read_energy()[0]
+        ref_solver.update_amps(t1, t2, rn=[0.3141592653589793, 0.2718281828459045])
+        delta_e = abs(ref_solver.read_energy()[0] - e_mixed)
+        del ref_solver
+        torch.cuda.empty_cache()
+
     def barrier():
         if world > 1:
             dist.barrier()
@@ -314,6 +326,7 @@ def run_gpu(args):
                        "precision": args.precision},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
             "clocks": clk.summary(), "energy_last": energies[-1],
+            "delta_e_vs_fp64_per_step": delta_e,
         }
         print(json.dumps(line))
     if world > 1:

@@ -56,6 +56,7 @@ class ReplicaBatch:
         self.history = [[] for _ in range(self.n)]
         self._errors = []
         self._dev = eris.device.index if eris.device.index is not None else torch.cuda.current_device()
+        torch.cuda.current_stream().synchronize()  # the clones above must land before other streams read them
 
     def _work(self, w):
         try:

@@ -107,6 +107,8 @@ class FRICCSDGPU:
             raise ValueError("precision must be 'fp64' or 'df64'")
         self.precision = precision
         self.lib = L.load()
+        if precision == "df64":
+            eris.prepare_splits()
         self._sp = _Handle()
         self._sp_w = _Handle()
         self._res = torch.zeros(4, dtype=torch.float64, device=eris.device)

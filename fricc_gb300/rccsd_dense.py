@@ -71,10 +71,21 @@ class DeviceERIs:
         self._dense_wvvvv = None
         self._splits = {}
 
+    SPLIT_BLOCKS = ("vvvvT", "ovvv_XY", "ovov", "ovov_0312", "ovov_0313_0113", "ovov_cdkl")
+
+    def prepare_splits(self):
+        """Build the (hi, lo) float-pair forms of the constant W' blocks once,
+        and wait for them: solvers on other streams read them afterwards."""
+        if len(self._splits) < len(self.SPLIT_BLOCKS):
+            for name in self.SPLIT_BLOCKS:
+                if name not in self._splits:
+                    self._splits[name] = split_f2(getattr(self, name))
+            torch.cuda.current_stream().synchronize()
+
     def split(self, name):
-        """The (hi, lo) float-pair form of a constant block (cached)."""
+        """The float-pair form of a constant block (prepare_splits() built it)."""
         if name not in self._splits:
-            self._splits[name] = split_f2(getattr(self, name))
+            raise RuntimeError(f"float-pair form of {name} missing: call prepare_splits() first")
         return self._splits[name]
 
     @property

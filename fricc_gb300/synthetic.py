@@ -7,13 +7,15 @@ A system is defined by (nocc, nvir, naux, sigma, seed):
   occupied-virtual block f_ov is zero;
 * two-electron integrals in chemists' notation
   (pq|rs) = sum_P L[P,p,q] L[P,r,s], with L symmetric in (p,q) and its
-  independent entries drawn N(0, sigma^2 / sqrt(naux)).  With entries
-  N(0, sigma^2) as such, every named workload is far outside the regime in
-  which CCSD iterates converge (o10v40: E_MP2 = -105 Eh, max |t2| = 0.44, and
-  undamped CCSD without any compression diverges within three iterations);
-  the 1/naux^(1/4) scale on L gives MP2 amplitudes of a few 1e-2 (o10v40:
-  E_MP2 = -0.525 Eh, CCSD -0.437 Eh) with the same sizes and the same work
-  per iteration;
+  independent entries drawn N(0, sigma^2 / naux): a normalised factor, so
+  the diagonal integrals (pq|pq) are ~sigma^2 whatever naux is.  With entries
+  N(0, sigma^2) as such, the named workloads are far outside the regime in
+  which undamped CCSD iterates converge (o10v40: E_MP2 = -105 Eh,
+  max |t2| = 0.44, and CCSD without any compression diverges within three
+  iterations; a 1/naux^(1/4) scale still leaves o20v100 oscillating between
+  -2.7 and -4.5 Eh).  With the normalised factor every workload converges
+  (o10v40: E_corr -0.0025875 Eh, o20v100: -0.0079092 Eh, FRI fluctuations
+  ~1e-7 Eh) with the same sizes and the same work per iteration;
 * amplitudes start at T1 = 0 and T2 = MP2, t_ijab = (ia|jb) / (e_i+e_j-e_a-e_b).
 
 These are the stand-in inputs for the reference's molecular runs (PySCF
@@ -51,7 +53,7 @@ class SyntheticSystem:
         ev = np.sort(rng.uniform(0.2, 3.0, self.nvir))
         self.mo_energy = np.concatenate([eo, ev])
         nmo = self.nmo
-        A = rng.standard_normal((self.naux, nmo, nmo)) * (self.sigma / self.naux ** 0.25)
+        A = rng.standard_normal((self.naux, nmo, nmo)) * (self.sigma / self.naux ** 0.5)
         up = np.triu(A)
         self.L = up + np.transpose(np.triu(A, 1), (0, 2, 1))
 

@@ -17,8 +17,8 @@ def test_replicas_alone_and_in_the_mix(gpulib):
     s = SyntheticSystem(6, 24, 120, 0.05, 3)
     E = DeviceERIs.from_system(s)
     settings = {"m_keep": 4000}
-    seeds = [11, 12, 13, 14, 15]
-    batch = ReplicaBatch(E, settings, seeds, n_streams=3, precision="df64")
+    seeds = [11, 12, 13, 14, 15, 16, 17, 18, 19, 20, 21, 22]
+    batch = ReplicaBatch(E, settings, seeds, n_streams=6, precision="df64")
     for _ in range(4):
         batch.step()
     for r, seed in enumerate(seeds):
