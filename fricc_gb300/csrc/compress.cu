@@ -48,6 +48,20 @@ __global__ void __launch_bounds__(256) k_hist12(const double* __restrict__ x, in
     if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
+// Values decided on the device between the phases of one compression.
+struct Ctl {
+  int64_t dmin;       // first select digit kept as a candidate
+  int64_t ncand;      // candidates (every element at or above dmin)
+  int64_t nd;         // |D|
+  int64_t mp;         // m - |D|
+  unsigned long long dkey;  // |x| bits of the last element of D
+  int64_t didx;       // its index (-1: D is empty)
+  double R;           // remaining norm
+  double mprime;      // (double)(m - |D|)
+  int sample;         // 1: R > 0 and finite, so samples can land in intervals
+  double rn;          // the uniform draw
+};
+
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
   unsigned long long v;
   asm volatile("ld.acquire.gpu.global.u64 %0, [%1];" : "=l"(v) : "l"(p) : "memory");
@@ -60,10 +74,11 @@ constexpr long long SPIN_LIMIT = 1ll << 22;
 // Stable compaction of {i : top digit of |x_i| >= dmin} into (ckey, cidx),
 // in ascending i.  Tiles take tickets in launch order; each publishes its
 // count and looks back over its predecessors for its output offset.
-__global__ void __launch_bounds__(256) k_compact(const double* __restrict__ x, int64_t n, unsigned dmin,
+__global__ void __launch_bounds__(256) k_compact(const double* __restrict__ x, int64_t n, const Ctl* __restrict__ c,
                                                  unsigned long long* __restrict__ ckey, unsigned* __restrict__ cidx,
                                                  unsigned long long* tstate, unsigned* ticket, unsigned* err) {
   constexpr int NT = 256, ITEMS = 16, TILE = NT * ITEMS;
+  const unsigned dmin = (unsigned)c->dmin;
   __shared__ int s_tile;
   __shared__ int64_t s_pre;
   __shared__ int64_t sm[33];
@@ -134,15 +149,24 @@ struct GenSorted {
 // is "at or before the last kept element in (|x| desc, index asc) order".
 struct GenP {
   const double* x;
-  const double* Rp;     // remaining norm R (device)
-  double mprime;        // (double)(m - |D|)
-  unsigned long long dkey;
-  int64_t didx;         // -1: D is empty
+  const Ctl* c;
   __device__ __forceinline__ double operator()(int64_t i) const {
     const double a = fabs(x[i]);
     const unsigned long long k = abs_key(a);
-    if (didx >= 0 && (k > dkey || (k == dkey && i <= didx))) return 0.0;
-    return __dmul_rn(__ddiv_rn(a, *Rp), mprime);
+    const int64_t didx = c->didx;
+    if (didx >= 0 && (k > c->dkey || (k == c->dkey && i <= didx))) return 0.0;
+    const double p = __dmul_rn(__ddiv_rn(a, c->R), c->mprime);
+    // with R <= 0 or not finite no sample can land anywhere: feed the exact
+    // chain zeros (NaN addends would only slow it down), but keep any p > 1
+    // visible to the check of make_probability_vector
+    return (c->sample || p > 1.0) ? p : 0.0;
+  }
+  __device__ __forceinline__ double value(int64_t i) const {  // the reference's p_i itself
+    const double a = fabs(x[i]);
+    const unsigned long long k = abs_key(a);
+    const int64_t didx = c->didx;
+    if (didx >= 0 && (k > c->dkey || (k == c->dkey && i <= didx))) return 0.0;
+    return __dmul_rn(__ddiv_rn(a, c->R), c->mprime);
   }
 };
 
@@ -171,16 +195,43 @@ __device__ __forceinline__ int64_t count_below(double I, double rn, int64_t mp) 
 
 // sample_systematic's interval search: the samples of interval j.
 struct ConsSample {
-  double rn;
-  int64_t mp;
+  const Ctl* c;
   unsigned* S;
   __device__ __forceinline__ void operator()(int64_t j, double lo, double hi, double p) const {
-    if (!(p > 0.0)) return;
+    if (!c->sample || !(p > 0.0)) return;
+    const double rn = c->rn;
+    const int64_t mp = c->mp;
     const int64_t k0 = count_below(lo, rn, mp);
     const int64_t k1 = count_below(hi, rn, mp);
     for (int64_t k = k0; k < k1; ++k) S[k] = (unsigned)j;
   }
 };
+
+// The select digit: the largest d with count(digit >= d) >= m (one thread).
+__global__ void k_select_digit(const unsigned* __restrict__ hist, int64_t m, Ctl* c) {
+  int64_t cum = 0;
+  int d = NDIG - 1;
+  for (; d >= 0; --d) {
+    cum += hist[d];
+    if (cum >= m) break;
+  }
+  c->dmin = d < 0 ? 0 : d;
+  c->ncand = cum;
+}
+
+// After the remaining-norm chain: |D|, R, the D threshold, m' (one thread).
+__global__ void k_finish_d(const unsigned long long* __restrict__ ffail, const double* __restrict__ Rb,
+                           const unsigned long long* __restrict__ ckey, const unsigned* __restrict__ cidx, int64_t m,
+                           Ctl* c) {
+  const int64_t nd = (int64_t)*ffail;
+  c->nd = nd;
+  c->mp = m - nd;
+  c->mprime = (double)(unsigned long long)(m - nd);
+  c->R = Rb[nd];
+  c->dkey = nd > 0 ? ckey[nd - 1] : 0ull;
+  c->didx = nd > 0 ? (int64_t)cidx[nd - 1] : -1;
+  c->sample = (c->R > 0.0 && isfinite(c->R)) ? 1 : 0;
+}
 
 __global__ void k_zero_u32(unsigned* p, int64_t n) {
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
@@ -188,8 +239,9 @@ __global__ void k_zero_u32(unsigned* p, int64_t n) {
 }
 
 // D part of the output: flat = sorted index, value = x (src/fri_utils.cpp:494,498-500)
-__global__ void k_out_d(const double* __restrict__ x, const unsigned* __restrict__ sidx, int64_t nd,
-                        int64_t* __restrict__ flat, double* __restrict__ vals) {
+__global__ void k_out_d(const double* __restrict__ x, const unsigned* __restrict__ sidx, int64_t nd_max,
+                        const Ctl* __restrict__ c, int64_t* __restrict__ flat, double* __restrict__ vals) {
+  const int64_t nd = c ? c->nd : nd_max;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
     const unsigned j = sidx[i];
     flat[i] = j;
@@ -198,12 +250,13 @@ __global__ void k_out_d(const double* __restrict__ x, const unsigned* __restrict
 }
 
 // S part: flat = S_k, value = x / p (src/fri_utils.cpp:495,502-504)
-__global__ void k_out_s(GenP gp, const unsigned* __restrict__ S, int64_t mp, int64_t nd, int64_t* __restrict__ flat,
+__global__ void k_out_s(GenP gp, const unsigned* __restrict__ S, int64_t* __restrict__ flat,
                         double* __restrict__ vals) {
+  const int64_t mp = gp.c->mp, nd = gp.c->nd;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < mp; k += (int64_t)gridDim.x * blockDim.x) {
     const unsigned j = S[k];
     flat[nd + k] = j;
-    vals[nd + k] = __ddiv_rn(gp.x[j], gp(j));
+    vals[nd + k] = __ddiv_rn(gp.x[j], gp.value(j));
   }
 }
 
@@ -288,7 +341,11 @@ static int dev_status(unsigned e) {
 
 // Compress x (device, n doubles) keeping m entries.  mode 0: "fri"
 // (systematic, one uniform draw rn), mode 1: "largest".  Writes flat[m],
-// vals[m] (device) and returns |D| in *n_largest.  Synchronises the stream.
+// vals[m] (device).  Every decision between phases (select digit, candidate
+// count, |D|, R, the D threshold) stays on the device, so the only host
+// round trip is the final one: with n_largest != nullptr the call
+// synchronises the stream, reads |D| and the error word and reports them;
+// with n_largest == nullptr it returns at once (nothing read back).
 int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, double rn, cudaStream_t st,
                           int64_t* flat, double* vals, int64_t* n_largest) {
   if (n < 0 || m <= 0 || m > n) {
@@ -301,6 +358,7 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     return FRICC_ERR_ARG;
   }
   CompressScratch s;
+  Ctl* ctl = nullptr;
   int rc = FRICC_OK;
 #define TRY(x)                  \
   do {                          \
@@ -309,55 +367,53 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
   } while (0)
 
   {
+    const int64_t ntile = fricc_cdiv(n, 4096);
+    TRY(fricc_alloc_t(&ctl, 1, st));
     TRY(fricc_alloc_t(&s.hist, NDIG, st));
     TRY(fricc_alloc_t(&s.err, 1, st));
-    cudaMemsetAsync(s.hist, 0, NDIG * sizeof(unsigned), st);
-    cudaMemsetAsync(s.err, 0, sizeof(unsigned), st);
-    k_hist12<<<grid_for(n, 256), 256, 0, st>>>(x, n, s.hist);
-    fricc_note_launch();
-    std::vector<unsigned> hh(NDIG);
-    TRY(fricc_cuda_check(cudaMemcpyAsync(hh.data(), s.hist, NDIG * sizeof(unsigned), cudaMemcpyDeviceToHost, st),
-                         "histogram copy"));
-    TRY(fricc_cuda_check(cudaStreamSynchronize(st), "histogram"));
-    int64_t cum = 0;
-    int dmin = NDIG - 1;
-    for (; dmin >= 0; --dmin) {
-      cum += hh[dmin];
-      if (cum >= m) break;
-    }
-    if (dmin < 0) dmin = 0;
-    const int64_t C = cum;  // candidates: every element with digit >= dmin
-
-    // 2. compaction + sort
-    const int64_t ntile = fricc_cdiv(n, 4096);
-    TRY(fricc_alloc_t(&s.ckey, C, st));
-    TRY(fricc_alloc_t(&s.cidx, C, st));
-    TRY(fricc_alloc_t(&s.ktmp, C, st));
-    TRY(fricc_alloc_t(&s.vtmp, C, st));
+    TRY(fricc_alloc_t(&s.ckey, n, st));
+    TRY(fricc_alloc_t(&s.cidx, n, st));
+    TRY(fricc_alloc_t(&s.ktmp, n, st));
+    TRY(fricc_alloc_t(&s.vtmp, n, st));
     TRY(fricc_alloc_t(&s.tstate, ntile, st));
     TRY(fricc_alloc_t(&s.ticket, 1, st));
-    TRY(fricc_alloc_t(&s.rhist, radix::hist_words(C), st));
-    cudaMemsetAsync(s.tstate, 0, ntile * sizeof(unsigned long long), st);
-    cudaMemsetAsync(s.ticket, 0, sizeof(unsigned), st);
-    k_compact<<<(unsigned)ntile, 256, 0, st>>>(x, n, (unsigned)dmin, s.ckey, s.cidx, s.tstate, s.ticket, s.err);
-    fricc_note_launch();
-    TRY(radix::sort_pairs(s.ckey, s.cidx, s.ktmp, s.vtmp, C, 64, true, s.rhist, st));
+    TRY(fricc_alloc_t(&s.rhist, radix::hist_words(n), st));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.hist, 0, NDIG * sizeof(unsigned), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.err, 0, sizeof(unsigned), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.tstate, 0, ntile * sizeof(unsigned long long), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.ticket, 0, sizeof(unsigned), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st), "memset"));
+    {
+      // the draw goes through a device word (a pageable-source copy completes
+      // before cudaMemcpyAsync returns, so a stack value is safe)
+      const double rn_h = rn;
+      TRY(fricc_cuda_check(cudaMemcpyAsync(&ctl->rn, &rn_h, sizeof(double), cudaMemcpyHostToDevice, st), "rn"));
+    }
+
+    // 1-2. select digit, candidates, sort (argsort, src/fri_utils.cpp:11-36)
+    k_hist12<<<grid_for(n, 256), 256, 0, st>>>(x, n, s.hist);
+    k_select_digit<<<1, 1, 0, st>>>(s.hist, m, ctl);
+    k_compact<<<(unsigned)ntile, 256, 0, st>>>(x, n, ctl, s.ckey, s.cidx, s.tstate, s.ticket, s.err);
+    fricc_note_launch(3);
+    TRY(radix::sort_pairs(s.ckey, s.cidx, s.ktmp, s.vtmp, n, 64, true, s.rhist, st, &ctl->ncand));
 
     if (mode == 1) {  // "largest": argsort(x, m) with unscaled values
-      k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, flat, vals);
+      k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, nullptr, flat, vals);
       fricc_note_launch();
       TRY(fricc_cuda_check(cudaGetLastError(), "largest"));
-      unsigned e = 0;
-      cudaMemcpyAsync(&e, s.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-      TRY(fricc_cuda_check(cudaStreamSynchronize(st), "compression"));
-      TRY(dev_status(e));
-      if (n_largest) *n_largest = m;
+      if (n_largest) {
+        unsigned e = 0;
+        TRY(fricc_cuda_check(cudaMemcpyAsync(&e, s.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "err"));
+        TRY(fricc_cuda_check(cudaStreamSynchronize(st), "compression"));
+        TRY(dev_status(e));
+        *n_largest = m;
+      }
       goto done;
     }
 
     // 3. one_norm
     TRY(fricc_alloc_t(&s.dzero, 1, st));
-    cudaMemsetAsync(s.dzero, 0, sizeof(double), st);
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.dzero, 0, sizeof(double), st), "memset"));
     TRY((exact::run_chain<GenAbs, exact::ConsNull, false, false>(GenAbs{x}, n, s.dzero, false, exact::ConsNull{},
                                                                  s.chain, s.err, st)));
     const int64_t nch_n = fricc_cdiv(n, exact::CH);
@@ -365,7 +421,7 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     TRY(fricc_alloc_t(&R0, 1, st));
     cudaMemcpyAsync(R0, s.chain.cstart + nch_n, sizeof(double), cudaMemcpyDeviceToDevice, st);
 
-    // 4. remaining-norm chain over the sorted top m
+    // 4. remaining-norm chain over the sorted top m, acceptance test
     TRY(fricc_alloc_t(&s.Rb, m + 1, st));
     TRY(fricc_alloc_t(&s.ffail, 1, st));
     k_set_u64<<<1, 1, 0, st>>>(s.ffail, (unsigned long long)m);
@@ -374,57 +430,39 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     rc = exact::run_chain<GenSorted, ConsAccept, false, true>(GenSorted{s.ckey}, m, R0, true, ca, s.chain, s.err, st);
     fricc_free(R0, st);
     if (rc) goto done;
-    unsigned long long nd_h = 0;
-    cudaMemcpyAsync(&nd_h, s.ffail, sizeof(nd_h), cudaMemcpyDeviceToHost, st);
-    unsigned long long dkey = 0;
-    unsigned didx_u = 0;
-    TRY(fricc_cuda_check(cudaStreamSynchronize(st), "compression"));
-    const int64_t nd = (int64_t)nd_h;
-    if (nd > 0) {
-      cudaMemcpyAsync(&dkey, s.ckey + (nd - 1), sizeof(dkey), cudaMemcpyDeviceToHost, st);
-      cudaMemcpyAsync(&didx_u, s.cidx + (nd - 1), sizeof(didx_u), cudaMemcpyDeviceToHost, st);
-    }
-    double R_h = 0.0;
-    cudaMemcpyAsync(&R_h, s.Rb + nd, sizeof(double), cudaMemcpyDeviceToHost, st);
-    TRY(fricc_cuda_check(cudaStreamSynchronize(st), "compression"));
-    const int64_t mp = m - nd;
-    GenP gp{x, s.Rb + nd, (double)(unsigned long long)mp, dkey, nd > 0 ? (int64_t)didx_u : -1};
+    k_finish_d<<<1, 1, 0, st>>>(s.ffail, s.Rb, s.ckey, s.cidx, m, ctl);
+    fricc_note_launch();
 
-    // 5. probabilities, p > 1 check, exact partial sums, systematic samples
-    TRY(fricc_alloc_t(&s.S, mp > 0 ? mp : 1, st));
-    if (mp > 0) {
-      k_zero_u32<<<grid_for(mp, 256), 256, 0, st>>>(s.S, mp);
-      fricc_note_launch();
-      if (R_h > 0.0 && std::isfinite(R_h)) {
-        ConsSample cs{rn, mp, s.S};
-        TRY((exact::run_chain<GenP, ConsSample, true, true>(gp, n, s.dzero, false, cs, s.chain, s.err, st)));
-      } else {
-        // R <= 0 or not finite: every p is 0, NaN or +-inf, no interval
-        // matches and all samples keep index 0; only the p > 1 check remains.
-        const int64_t nch = fricc_cdiv(n, exact::CH);
-        if (s.chain.cap < nch + 1) {
-          exact::free_chain(s.chain, st);
-          TRY(fricc_alloc_t(&s.chain.csum, nch + 1, st));
-        }
-        exact::k_chunk_sums<GenP, true><<<(unsigned)nch, 256, 0, st>>>(gp, n, s.chain.csum, s.err);
-        fricc_note_launch();
-      }
-    }
+    // 5. probabilities, the p > 1 check, exact partial sums, systematic samples
+    GenP gp{x, ctl};
+    TRY(fricc_alloc_t(&s.S, m, st));
+    k_zero_u32<<<grid_for(m, 256), 256, 0, st>>>(s.S, m);
+    fricc_note_launch();
+    // with m' = 0 every p is 0 (or NaN); with R <= 0 or not finite no
+    // interval matches (ConsSample checks ctl->sample): in both cases all
+    // samples keep index 0, as in the reference
+    ConsSample cs{ctl, s.S};
+    TRY((exact::run_chain<GenP, ConsSample, true, true>(gp, n, s.dzero, false, cs, s.chain, s.err, st)));
 
     // 6. output
-    if (nd > 0) k_out_d<<<grid_for(nd, 256), 256, 0, st>>>(x, s.cidx, nd, flat, vals);
-    if (mp > 0) k_out_s<<<grid_for(mp, 256), 256, 0, st>>>(gp, s.S, mp, nd, flat, vals);
-    fricc_note_launch((nd > 0) + (mp > 0));
+    k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, ctl, flat, vals);
+    k_out_s<<<grid_for(m, 256), 256, 0, st>>>(gp, s.S, flat, vals);
+    fricc_note_launch(2);
     TRY(fricc_cuda_check(cudaGetLastError(), "output"));
-    unsigned e = 0;
-    cudaMemcpyAsync(&e, s.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
-    TRY(fricc_cuda_check(cudaStreamSynchronize(st), "compression"));
-    TRY(dev_status(e));
-    if (n_largest) *n_largest = nd;
+    if (n_largest) {
+      unsigned e = 0;
+      int64_t nd = 0;
+      TRY(fricc_cuda_check(cudaMemcpyAsync(&e, s.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "err"));
+      TRY(fricc_cuda_check(cudaMemcpyAsync(&nd, &ctl->nd, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "nd"));
+      TRY(fricc_cuda_check(cudaStreamSynchronize(st), "compression"));
+      TRY(dev_status(e));
+      *n_largest = nd;
+    }
   }
 done:
 #undef TRY
   free_scratch(s, st);
+  fricc_free(ctl, st);
   return rc;
 }
 

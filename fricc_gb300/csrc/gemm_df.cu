@@ -15,7 +15,7 @@
 
 namespace {
 
-constexpr int BM = 64, BN = 64, BK = 16, NT = 256, TM = 4, TN = 4;
+constexpr int BK = 16, NT = 256;
 
 __device__ __forceinline__ float2 split(double d) {
   const float h = __double2float_rn(d);
@@ -34,7 +34,12 @@ struct GemmArgs {
   int64_t kchunk;  // K per split (multiple of BK)
 };
 
+// 256 threads as 16 x 16; each owns a TM x TN block of C (rows ty + 16 i,
+// columns tx + 16 j), so a CTA tile is (16 TM) x (16 TN): 64x64 for square
+// problems, 128x32 / 32x128 when one side is as small as nocc.
+template <int TM, int TN>
 __global__ void __launch_bounds__(NT) k_gemm_df(GemmArgs g) {
+  constexpr int BM = 16 * TM, BN = 16 * TN;
   __shared__ float2 As[BK][BM + 1];
   __shared__ float2 Bs[BK][BN + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
@@ -156,6 +161,18 @@ int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t ba
   g.sCm = sC[0]; g.sCn = sC[1]; g.sCb = sC[2];
   g.alpha = alpha;
   g.beta = beta;
+  // tile shape: the one of 64x64, 128x32, 32x128 that pads C least (a side
+  // as short as nocc would waste half of a 64-wide tile)
+  int tm = 4, tn = 4;
+  {
+    const int cand[3][2] = {{4, 4}, {8, 2}, {2, 8}};
+    int64_t best = -1;
+    for (const auto& c : cand) {
+      const int64_t pad = fricc_cdiv(M, 16 * c[0]) * 16 * c[0] * fricc_cdiv(N, 16 * c[1]) * 16 * c[1];
+      if (best < 0 || pad < best) { best = pad; tm = c[0]; tn = c[1]; }
+    }
+  }
+  const int64_t BM = 16 * tm, BN = 16 * tn;
   const int64_t tiles = fricc_cdiv(M, BM) * fricc_cdiv(N, BN) * batch;
   // split K until the grid covers the GPU about four times over
   int splits = 1;
@@ -173,7 +190,9 @@ int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t ba
     g.part = part;
   }
   dim3 grid((unsigned)fricc_cdiv(N, BN), (unsigned)fricc_cdiv(M, BM), (unsigned)(batch * splits));
-  k_gemm_df<<<grid, NT, 0, st>>>(g);
+  if (tm == 8) k_gemm_df<8, 2><<<grid, NT, 0, st>>>(g);
+  else if (tm == 2) k_gemm_df<2, 8><<<grid, NT, 0, st>>>(g);
+  else k_gemm_df<4, 4><<<grid, NT, 0, st>>>(g);
   fricc_note_launch();
   if (splits > 1) {
     int64_t n = batch * M * N;

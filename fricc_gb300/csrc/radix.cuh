@@ -19,8 +19,13 @@ __device__ __forceinline__ unsigned digit(unsigned long long k, int shift, int d
   return desc ? 255u - d : d;
 }
 
+// n_dev (optional): the element count in device memory, overriding n; tiles
+// past it count nothing (and scatter nothing), so a sort can be launched for
+// a worst-case size without the host knowing the real one.
 static __global__ void __launch_bounds__(NT) k_hist(const unsigned long long* __restrict__ keys, int64_t n, int shift,
-                                             int desc, unsigned* __restrict__ hist, int64_t ntiles) {
+                                             int desc, unsigned* __restrict__ hist, int64_t ntiles,
+                                             const int64_t* __restrict__ n_dev) {
+  if (n_dev) n = *n_dev;
   __shared__ unsigned h[256];
   h[threadIdx.x] = 0;
   __syncthreads();
@@ -65,7 +70,10 @@ static __global__ void __launch_bounds__(NT) k_scatter(const unsigned long long*
                                                 const unsigned* __restrict__ vin,
                                                 unsigned long long* __restrict__ kout, unsigned* __restrict__ vout,
                                                 int64_t n, int shift, int desc, const unsigned* __restrict__ offs,
-                                                int64_t ntiles, const unsigned* __restrict__ dbase) {
+                                                int64_t ntiles, const unsigned* __restrict__ dbase,
+                                                const int64_t* __restrict__ n_dev) {
+  if (n_dev) n = *n_dev;
+  if ((int64_t)blockIdx.x * TILE >= n) return;  // uniform per block
   constexpr int NW = NT / 32;
   __shared__ unsigned run[256];
   __shared__ unsigned wc[NW][256];
@@ -112,12 +120,14 @@ static __global__ void __launch_bounds__(NT) k_scatter(const unsigned long long*
   }
 }
 
-// Sorts n pairs on key bits [0, bits).  The result ends in (keys, vals); the
-// tmp buffers must hold n entries, hist hist_words(n) counts.
+// Sorts n pairs on key bits [0, bits) (or *n_dev <= n pairs, when given).
+// The result ends in (keys, vals); the tmp buffers must hold n entries, hist
+// hist_words(n) counts.
 inline int64_t hist_words(int64_t n) { return 256 * fricc_cdiv(n, TILE) + 512; }
 
 inline int sort_pairs(unsigned long long* keys, unsigned* vals, unsigned long long* ktmp, unsigned* vtmp,
-                      int64_t n, int bits, bool desc, unsigned* hist, cudaStream_t st) {
+                      int64_t n, int bits, bool desc, unsigned* hist, cudaStream_t st,
+                      const int64_t* n_dev = nullptr) {
   if (n <= 1) return FRICC_OK;
   if (n > 0xffffffffLL) return FRICC_ERR_ARG;
   const int64_t ntiles = fricc_cdiv(n, TILE);
@@ -127,10 +137,10 @@ inline int sort_pairs(unsigned long long* keys, unsigned* vals, unsigned long lo
   for (int shift = 0; shift < bits; shift += 8, ++passes) {
     unsigned* totals = hist + 256 * ntiles;
     unsigned* base = totals + 256;
-    k_hist<<<(unsigned)ntiles, NT, 0, st>>>(ka, n, shift, desc ? 1 : 0, hist, ntiles);
+    k_hist<<<(unsigned)ntiles, NT, 0, st>>>(ka, n, shift, desc ? 1 : 0, hist, ntiles, n_dev);
     k_scan_rows<<<256, 256, 0, st>>>(hist, ntiles, totals);
     k_scan_digits<<<1, 256, 0, st>>>(totals, base);
-    k_scatter<<<(unsigned)ntiles, NT, 0, st>>>(ka, va, kb, vb, n, shift, desc ? 1 : 0, hist, ntiles, base);
+    k_scatter<<<(unsigned)ntiles, NT, 0, st>>>(ka, va, kb, vb, n, shift, desc ? 1 : 0, hist, ntiles, base, n_dev);
     fricc_note_launch(4);
     unsigned long long* tk = ka;
     ka = kb;

@@ -174,6 +174,7 @@ class FRICCSDGPU:
         Tw = self._sp_w.compress(t2, m, s["compression"], rn[1], st) if need_w else None
 
         mm = D.gemm_df if self.precision == "df64" else D.gemm_torch
+        ein2 = D.einsum_df if self.precision == "df64" else torch.einsum   # two-operand O^3V^2 contractions
         f64, dev = t2.dtype, t2.device
         # cc_Foo / cc_Fvv share tt[p,q,r,s] = t2 + t1[p,r] t1[q,s]
         tt = t2 + ein("pr,qs->pqrs", t1, t1)
@@ -199,17 +200,18 @@ class FRICCSDGPU:
         t1new = t1new.contiguous()
         mm(t2.view(o, o * v * v), E.G_t1.view(o * v * v, v), t1new, 1.0, 1.0)  # O^2V^3, :165-166
         t1new += t1 @ (t1.reshape(1, ov) @ E.G_t1.permute(0, 2, 1, 3).reshape(ov, v * v)).view(v, v)  # :167-168
-        t1new += -2 * ein("lcki,klac->ia", E.ovoo, t2) + ein("kcli,klac->ia", E.ovoo, t2)
-        t1new += -2 * ein("lcki,lc,ka->ia", E.ovoo, t1, t1) + ein("kcli,lc,ka->ia", E.ovoo, t1, t1)
+        # -2 (lc|ki) + (kc|li) = -g_ovoo[l,c,k,i]
+        t1new -= ein2("lcki,klac->ia", E.g_ovoo, t2)
+        t1new -= ein("lcki,lc,ka->ia", E.g_ovoo, t1, t1)
 
         # T2 driver terms (:179-187)
-        Y1 = ein("kibc,jc->kibj", E.oovv, t1)
+        Y1 = ein2("kibc,jc->kibj", E.oovv, t1)
         R = torch.empty(o * v * v, o, dtype=f64, device=dev)   # R[(i,a,b), j] = sum_c (ia|cb) t_jc
         mm(E.ovvv_iabc.view(o * v * v, v), t1.T, R, 1.0, 0.0)
-        tmp = R.view(o, v, v, o).permute(0, 3, 1, 2) - ein("ka,kibj->ijab", t1, Y1)
+        tmp = R.view(o, v, v, o).permute(0, 3, 1, 2) - ein2("ka,kibj->ijab", t1, Y1)
         t2new = tmp + tmp.permute(1, 0, 3, 2)
-        tmp2 = ein("kcai,jc->akij", E.ovvo, t1) + E.ovoo.permute(1, 3, 0, 2)
-        tmp = ein("akij,kb->ijab", tmp2, t1)
+        tmp2 = ein2("kcai,jc->akij", E.ovvo, t1) + E.ovoo.permute(1, 3, 0, 2)
+        tmp = ein2("akij,kb->ijab", tmp2, t1)
         t2new -= tmp + tmp.permute(1, 0, 3, 2)
         t2new += E.ovov.permute(0, 2, 1, 3)
         t2new = t2new.contiguous()
@@ -220,11 +222,11 @@ class FRICCSDGPU:
         Lvv.diagonal().sub_(e_v)
 
         if "O^4V^2" in comp:  # sparse_cc_Woooo (:309-322)
-            Wo = (ein("lcki,jc->klij", E.ovoo, t1) + ein("kclj,ic->klij", E.ovoo, t1)).permute(2, 3, 0, 1)
+            Wo = (ein2("lcki,jc->klij", E.ovoo, t1) + ein2("kclj,ic->klij", E.ovoo, t1)).permute(2, 3, 0, 1)
             Wo = Wo.contiguous()                                                  # [i,j,k,l]
             self._spmm(Tw, 0, 1, 2, 3, 1.0, E.ovov_cdkl, o * o, Wo, st, const="ovov_cdkl")  # 1323
             Woooo = Wo.permute(2, 3, 0, 1)                                        # (k,l,i,j)
-            Woooo += ein("kcld,ic,jd->klij", E.ovov, t1, t1)
+            Woooo += ein2("kild,jd->klij", ein2("kcld,ic->kild", E.ovov, t1), t1)
             Woooo += E.oooo.permute(0, 2, 1, 3)
         else:
             Woooo = D.cc_Woooo(t1, t2, E)
@@ -232,26 +234,26 @@ class FRICCSDGPU:
         if "O^3V^3" in comp:  # sparse_cc_Wvoov / sparse_cc_Wvovo (:334-376)
             R = torch.empty(o * v * v, o, dtype=f64, device=dev)   # R[(k,c,a), i] = sum_d (kc|ad) t_id
             mm(E.ovvv.view(o * v * v, v), t1.T, R, 1.0, 0.0)
-            Wvoov = (R.view(o, v, v, o).permute(2, 0, 3, 1) - ein("kcli,la->akic", E.ovoo, t1)
+            Wvoov = (R.view(o, v, v, o).permute(2, 0, 3, 1) - ein2("kcli,la->akic", E.ovoo, t1)
                      + E.ovvo.permute(2, 0, 3, 1))
             Wp = Wvoov.permute(0, 2, 1, 3).contiguous()                         # [a,i,k,c]
             self._spmm(Tw, 3, 0, 1, 2, -0.5, E.ovov, ov, Wp, st, const="ovov")                     # 0112
             self._spmm(Tw, 2, 0, 1, 3, 1.0, E.ovov_0313_0113, ov, Wp, st, const="ovov_0313_0113")  # 0313+0113
             Wvoov = Wp.permute(0, 2, 1, 3)                                      # (a,k,i,c)
-            Wvoov -= ein("ldkc,id,la->akic", E.ovov, t1, t1)
+            Wvoov -= ein2("lkci,la->akic", ein2("ldkc,id->lkci", E.ovov, t1), t1)
             mm(E.ovvv_kacd.view(o * v * v, v), t1.T, R, 1.0, 0.0)   # R[(k,a,c), i] = sum_d (kd|ac) t_id
-            Wvovo = (R.view(o, v, v, o).permute(1, 0, 2, 3) - ein("lcki,la->akci", E.ovoo, t1)
+            Wvovo = (R.view(o, v, v, o).permute(1, 0, 2, 3) - ein2("lcki,la->akci", E.ovoo, t1)
                      + E.oovv.permute(2, 0, 3, 1))
             Wq = Wvovo.permute(0, 3, 1, 2).contiguous()                         # [a,i,k,c]
             self._spmm(Tw, 3, 0, 1, 2, -0.5, E.ovov_0312, ov, Wq, st, const="ovov_0312")          # 0312
             Wvovo = Wq.permute(0, 2, 3, 1)                                      # (a,k,c,i)
-            Wvovo -= ein("lckd,id,la->akci", E.ovov, t1, t1)
+            Wvovo -= ein2("lkci,la->akci", ein2("lckd,id->lkci", E.ovov, t1), t1)
         else:
             Wvoov = D.cc_Wvoov(t1, t2, E)
             Wvovo = D.cc_Wvovo(t1, t2, E)
 
         if "O^4V^2" in comp:
-            t2new += ein("klij,ka,lb->ijab", Woooo, t1, t1)
+            t2new += ein2("lija,lb->ijab", ein2("klij,ka->lija", Woooo, t1), t1)
             Tp = t2new.permute(2, 3, 0, 1).contiguous()                           # [a,b,i,j]
             self._spmm(T, 2, 3, 0, 1, 1.0, Woooo.contiguous(), o * o, Tp, st)     # 0101
             t2new.copy_(Tp.permute(2, 3, 0, 1))

@@ -15,6 +15,8 @@ only as vvvvT[c,d,a,b] = (ac|bd), the layout the O^2V^4 term streams.
 """
 from __future__ import annotations
 
+import math
+
 import numpy as np
 import torch
 
@@ -73,14 +75,32 @@ class DeviceERIs:
 
     SPLIT_BLOCKS = ("vvvvT", "ovvv_XY", "ovov", "ovov_0312", "ovov_0313_0113", "ovov_cdkl")
 
-    def prepare_splits(self):
-        """Build the (hi, lo) float-pair forms of the constant W' blocks once,
-        and wait for them: solvers on other streams read them afterwards."""
-        if len(self._splits) < len(self.SPLIT_BLOCKS):
-            for name in self.SPLIT_BLOCKS:
+    def prepare_splits(self, names=None):
+        """Build the (hi, lo) float-pair forms of constant W' blocks once (by
+        default those of FRI-CCSD), and wait for them: solvers on other
+        streams read them afterwards."""
+        names = self.SPLIT_BLOCKS if names is None else names
+        if any(n not in self._splits for n in names):
+            for name in names:
                 if name not in self._splits:
                     self._splits[name] = split_f2(getattr(self, name))
             torch.cuda.current_stream().synchronize()
+
+    LIN_BLOCKS = ("oooo_klij", "lin_WA", "lin_WB", "lin_W2AB")
+
+    def prepare_linear(self):
+        """The bare-integral W' layouts FRI-LCCSD contracts the compressed T2
+        with (fricc/frilccsd.py:172-175), built once and shared by solvers:
+        oooo_klij[k,l,i,j] = (ki|lj) (0101), lin_WA[k,c,i,a] = (kc|ai)
+        (1302, 1303), lin_WB[k,c,i,a] = (ki|ac) (1202, 1203) and
+        2 lin_WA - lin_WB (1302 and 1202 from one compression)."""
+        if not hasattr(self, "lin_WA"):
+            self.oooo_klij = self.oooo.permute(0, 2, 1, 3).contiguous()
+            self.lin_WA = self.ovvo.permute(0, 1, 3, 2).contiguous()
+            self.lin_WB = self.oovv.permute(0, 3, 1, 2).contiguous()
+            self.lin_W2AB = (2.0 * self.lin_WA - self.lin_WB).contiguous()
+            if self.device.type == "cuda":
+                torch.cuda.current_stream().synchronize()
 
     def split(self, name):
         """The float-pair form of a constant block (prepare_splits() built it)."""
@@ -154,6 +174,47 @@ def gemm_df(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
                                    L.i64arr(sC), float(alpha), float(beta),
                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return C
+
+
+def einsum_df(spec: str, A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+    """Two-operand einsum as one strided batched GEMM on the FP32-pair kernel.
+
+    Indices shared by both operands and the output form the batch, A-only
+    output indices the rows, B-only output indices the columns, shared
+    non-output indices the contraction; an index in one operand only and not
+    in the output is summed out first.  Operand groups merge into one stride
+    where the layout allows (``reshape`` copies otherwise); the result is a
+    view of a contiguous [batch, rows, cols] buffer in the output's order."""
+    lhs, out = spec.replace(" ", "").split("->")
+    a, b = lhs.split(",")
+    if len(set(a)) != len(a) or len(set(b)) != len(b):
+        raise ValueError(f"einsum_df: repeated index within an operand in {spec!r}")
+    lone = [c for c in a if c not in b and c not in out]
+    if lone:
+        A = A.sum(dim=[a.index(c) for c in lone])
+        a = "".join(c for c in a if c not in lone)
+    lone = [c for c in b if c not in a and c not in out]
+    if lone:
+        B = B.sum(dim=[b.index(c) for c in lone])
+        b = "".join(c for c in b if c not in lone)
+    size = {c: A.shape[a.index(c)] for c in a}
+    size.update({c: B.shape[b.index(c)] for c in b})
+    bt = [c for c in out if c in a and c in b]
+    mi = [c for c in out if c in a and c not in b]
+    ni = [c for c in out if c in b and c not in a]
+    ki = [c for c in a if c in b and c not in out]
+    prod = lambda idx: math.prod(size[c] for c in idx)
+    nb, M, N, K = prod(bt), prod(mi), prod(ni), prod(ki)
+    Ap = A.permute([a.index(c) for c in bt + mi + ki]).reshape(nb, M, K)
+    Bp = B.permute([b.index(c) for c in bt + ki + ni]).reshape(nb, K, N)
+    C = torch.empty(nb, M, N, dtype=torch.float64, device=A.device)
+    if C.numel():
+        if K == 0:
+            C.zero_()
+        else:
+            gemm_df(Ap, Bp, C)
+    order = bt + mi + ni
+    return C.view([size[c] for c in order]).permute([order.index(c) for c in out])
 
 
 def gemm_torch(A, B, C, alpha=1.0, beta=0.0):
@@ -253,6 +314,13 @@ def wvvvv_sum_cd(t1, E):
     """S[a,b] = sum_cd Wvvvv[a,b,c,d] without building Wvvvv:
     sum_cd (ac|bd) - sum_k t_kb sum_cd (kd|ac) - sum_k t_ka sum_cd (kc|bd)."""
     return E.S0 - E.U.T @ t1 - t1.T @ E.U
+
+
+def lin_cc_energy(t1, t2, E):
+    """2 sum f_ia t1_ia + sum t2_ijab (2 (ia|jb) - (ib|ja)) (fricc/frilccsd.py:504-522)."""
+    o = t1.shape[0]
+    fov = E.fock[:o, o:]
+    return float(2.0 * (fov * t1).sum() + ein("ijab,iajb->", t2, E.g_ovov))
 
 
 def ccsd_energy(t1, t2, E):
