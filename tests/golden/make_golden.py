@@ -12,7 +12,9 @@ records:
                    in place into a non-zero output, including strided W;
 * iteration.npz -- the reference's fricc/friccsd.py ``kernel`` run
                    unmodified (on the PySCF stand-in in oracle/) for a small
-                   synthetic system: every iterate, every energy, every draw.
+                   synthetic system: every iterate, every energy, every draw;
+* lccsd.npz     -- the same for fricc/frilccsd.py (FRI-LCCSD): one shared
+                   compression, six independent compressions, and LCCD.
 
 Usage:  OMP_NUM_THREADS=1 python tests/golden/make_golden.py
 """
@@ -178,12 +180,76 @@ def iteration_case(R):
     }
 
 
+def load_reference_frilccsd(F):
+    """fricc/frilccsd.py, with a stub for the emcee import it never calls here."""
+    if "emcee" not in sys.modules:
+        emcee = types.ModuleType("emcee")
+        emcee.autocorr = types.ModuleType("emcee.autocorr")
+
+        def integrated_time(*a, **k):
+            raise NotImplementedError("emcee is not installed")
+
+        emcee.autocorr.integrated_time = integrated_time
+        sys.modules["emcee"] = emcee
+        sys.modules["emcee.autocorr"] = emcee.autocorr
+    spec = importlib.util.spec_from_file_location("fricc.frilccsd",
+                                                  os.path.join(REF, "fricc", "frilccsd.py"))
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules["fricc.frilccsd"] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+LCCSD_VARIANTS = (("shared", False, False, 6), ("independent", True, False, 6), ("lccd", False, True, 4))
+
+
+def lccsd_cases(R):
+    """FRI-LCCSD trajectories of the reference's own fricc/frilccsd.py:
+    one shared compression, six independent compressions, and LCCD."""
+    F = load_reference_friccsd(R)
+    LF = load_reference_frilccsd(F)
+    s = SyntheticSystem(4, 12, 60, 0.05, 7)
+    eris = pyscf_standin.make_eris(s)
+    out = {"L": s.L, "mo_energy": s.mo_energy, "nocc": np.int64(4), "m": np.int64(800)}
+    for vi, (name, indep, lccd, n_iter) in enumerate(LCCSD_VARIANTS):
+        settings = {"m_keep": 800, "compression": "fri", "sampling_method": "systematic",
+                    "verbose": False, "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"],
+                    "LCCD": lccd, "Independent Compressions": indep}
+
+        class Driver(pyscf_standin.CCSD):
+            def energy(self, t1, t2, eris):
+                return LF.lin_cc_energy(self, t1, t2, eris)
+
+        cc = Driver(eris, settings)
+        cc.max_cycle = n_iter
+        t1, t2 = pyscf_standin.mp2_guess(eris)
+        iterates = [(t1, t2)]
+
+        def record(t1, t2, eris, cc=cc):
+            r = (LF.update_amps_independent_compressions if indep else LF.update_amps)(cc, t1, t2, eris)
+            iterates.append(r)
+            return r
+
+        cc.update_amps = record
+        seed = 21 + vi
+        libc.srand(seed)
+        F.kernel(cc, eris, t1, t2)
+        per = 6 if indep else 1
+        out[f"{name}_seed"] = np.int64(seed)
+        out[f"{name}_rn"] = np.array(draws(seed, per * (len(iterates) - 1)))
+        out[f"{name}_energies"] = np.array(cc.energies)
+        out[f"{name}_t1"] = np.stack([a for a, _ in iterates])
+        out[f"{name}_t2"] = np.stack([b for _, b in iterates])
+    return out
+
+
 def main():
     R = load_reference_module()
     np.savez_compressed(os.path.join(HERE, "compress.npz"), **compress_cases(R))
     np.savez_compressed(os.path.join(HERE, "contract.npz"), **contract_cases(R))
     np.savez_compressed(os.path.join(HERE, "iteration.npz"), **iteration_case(R))
-    for f in ("compress.npz", "contract.npz", "iteration.npz"):
+    np.savez_compressed(os.path.join(HERE, "lccsd.npz"), **lccsd_cases(R))
+    for f in ("compress.npz", "contract.npz", "iteration.npz", "lccsd.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

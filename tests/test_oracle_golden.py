@@ -90,3 +90,65 @@ def test_iteration_golden_free_running(oracle):
     conv, e, t1, t2, energies = CO.kernel(settings, eris, g["t1"][0], g["t2"][0], max_cycle=len(g["energies"]),
                                           rn_draw=lambda: next(draws))
     assert np.max(np.abs(np.array(energies) - g["energies"])) < 1e-10
+
+
+LCCSD_VARIANTS = (("shared", False, False), ("independent", True, False), ("lccd", False, True))
+
+
+def _lccsd_system():
+    g = golden("lccsd.npz")
+    from oracle import pyscf_standin as P
+    from fricc_gb300.synthetic import SyntheticSystem
+
+    class Sys:
+        pass
+
+    s = Sys()
+    s.nocc = int(g["nocc"])
+    s.L = g["L"]
+    s.mo_energy = g["mo_energy"]
+    s.nmo = s.mo_energy.size
+    s.nvir = s.nmo - s.nocc
+    s.fock = np.diag(s.mo_energy)
+    s.naux = s.L.shape[0]
+    s.eri = lambda b: SyntheticSystem.eri(s, b)
+    s._sl = lambda c: SyntheticSystem._sl(s, c)
+    return g, P.make_eris(s)
+
+
+def _lccsd_settings(g, lccd, indep):
+    return {"m_keep": int(g["m"]), "compression": "fri", "sampling_method": "systematic", "verbose": False,
+            "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"], "LCCD": lccd,
+            "Independent Compressions": indep}
+
+
+@pytest.mark.parametrize("name,indep,lccd", LCCSD_VARIANTS)
+def test_lccsd_golden_teacher_forced(oracle, name, indep, lccd):
+    """Each fricc/frilccsd.py iterate, fed to the oracle update with the same
+    draws, gives the next one; the linear energy matches."""
+    from oracle import lccsd_oracle as LO
+    g, eris = _lccsd_system()
+    settings = _lccsd_settings(g, lccd, indep)
+    rn = list(g[f"{name}_rn"])
+    per = 6 if indep else 1
+    t1s, t2s, E = g[f"{name}_t1"], g[f"{name}_t2"], g[f"{name}_energies"]
+    for it in range(len(E)):
+        draws = iter(rn[per * it: per * it + per])
+        t1n, t2n = LO.update_amps(settings, t1s[it], t2s[it], eris, rn_draw=lambda: next(draws),
+                                  independent=indep, lccd=lccd)
+        np.testing.assert_allclose(t2n, t2s[it + 1], rtol=0, atol=1e-13)
+        np.testing.assert_allclose(t1n, t1s[it + 1], rtol=0, atol=1e-13)
+        assert abs(LO.lin_cc_energy(t1n, t2n, eris) - E[it]) < 1e-12
+    if lccd:
+        assert not np.any(t1s[1:])
+
+
+@pytest.mark.parametrize("name,indep,lccd", LCCSD_VARIANTS)
+def test_lccsd_golden_free_running(oracle, name, indep, lccd):
+    from oracle import lccsd_oracle as LO
+    g, eris = _lccsd_system()
+    draws = iter(list(g[f"{name}_rn"]))
+    conv, e, t1, t2, energies = LO.kernel(_lccsd_settings(g, lccd, indep), eris, g[f"{name}_t1"][0],
+                                          g[f"{name}_t2"][0], max_cycle=len(g[f"{name}_energies"]),
+                                          rn_draw=lambda: next(draws), independent=indep, lccd=lccd)
+    assert np.max(np.abs(np.array(energies) - g[f"{name}_energies"])) < 1e-10
