@@ -40,7 +40,7 @@ SIGNATURES = [
                                   _dp, _i64, _dp, _vp]),
     ("fricc_spmm_f2", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_double, _dp, _i64, _dp, _vp]),
-    ("fricc_split_f2", ctypes.c_int, [_dp, _i64, _dp, _vp]),
+    ("fricc_split_f2", ctypes.c_int, [_dp, _i64, _i64, _dp, _vp]),
     ("fricc_gemm_df", ctypes.c_int, [_dp, _dp, _dp, _i64, _i64, _i64, _i64, _i64p, _i64p, _i64p, ctypes.c_double,
                                       ctypes.c_double, _vp]),
     ("fricc_contract_flops", ctypes.c_double, [ctypes.c_char_p, _vp]),
@@ -52,6 +52,7 @@ SIGNATURES = [
     ("fricc_prof_read", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_double)]),
     ("fricc_energy_update", ctypes.c_int, [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _i64, _dp, _dp, _dp, _vp]),
+    ("fricc_energy_update_lin", ctypes.c_int, [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _i64, _dp, _dp, _dp, _vp]),
 ]
 
 _lib = None

@@ -18,15 +18,15 @@ int fricc_contract_device(const char* term, const double* W, const int64_t Wd[4]
 double fricc_contract_flops_impl(const char* term, const FriccSparse* T);
 int fricc_spmm_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const double* Wp, int64_t QS,
                       double* Op, cudaStream_t st);
-int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float2* Wp, int64_t QS,
+int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float4* Wp, int64_t QS,
                          double* Op, cudaStream_t st);
-int fricc_split_f2_device(const double* x, int64_t n, float2* out, cudaStream_t st);
+int fricc_split_f2_device(const double* x, int64_t rows, int64_t qs, float4* out, cudaStream_t st);
 int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
                          const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
                          cudaStream_t st);
 int fricc_energy_update_device(const double* t1num, const double* t2num, const double* eia, const double* fov,
                                const double* ovov, const double* t1old, const double* t2old, int64_t o, int64_t v,
-                               double* t1out, double* t2out, double* res, cudaStream_t st);
+                               double* t1out, double* t2out, double* res, cudaStream_t st, bool linear);
 
 // ------------------------------------------------------------------ errors
 static thread_local char g_err[512] = "";
@@ -345,16 +345,16 @@ int fricc_spmm(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, con
   return rc;
 }
 
-int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* Wp2, int64_t QS,
+int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* Wp4, int64_t QS,
                   double* Op, void* stream) {
   cudaStream_t st = as_stream(stream);
-  int rc = fricc_spmm_f2_device(T, pa, pb, ka, kb, coef, reinterpret_cast<const float2*>(Wp2), QS, Op, st);
+  int rc = fricc_spmm_f2_device(T, pa, pb, ka, kb, coef, reinterpret_cast<const float4*>(Wp4), QS, Op, st);
   if (!rc && T) T->owner_stream = st;
   return rc;
 }
 
-int fricc_split_f2(const double* x, int64_t n, float* out2, void* stream) {
-  return fricc_split_f2_device(x, n, reinterpret_cast<float2*>(out2), as_stream(stream));
+int fricc_split_f2(const double* x, int64_t rows, int64_t qs, float* out4, void* stream) {
+  return fricc_split_f2_device(x, rows, qs, reinterpret_cast<float4*>(out4), as_stream(stream));
 }
 
 int fricc_gemm_df(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
@@ -385,15 +385,27 @@ int fricc_compress(const double* x, int64_t n, int64_t m, int compression, doubl
                                vals, n_largest);
 }
 
-int fricc_energy_update(const double* t1num, const double* t2num, const double* eia, const double* fov,
-                        const double* ovov, const double* t1old, const double* t2old, int64_t nocc, int64_t nvir,
-                        double* t1out, double* t2out, double* res, void* stream) {
+static int energy_update(const double* t1num, const double* t2num, const double* eia, const double* fov,
+                         const double* ovov, const double* t1old, const double* t2old, int64_t nocc, int64_t nvir,
+                         double* t1out, double* t2out, double* res, void* stream, bool linear) {
   if (!t1num || !t2num || !eia || !fov || !ovov || !t1old || !t2old || !t1out || !t2out || !res) {
     fricc_set_error("energy_update: null argument");
     return FRICC_ERR_ARG;
   }
   return fricc_energy_update_device(t1num, t2num, eia, fov, ovov, t1old, t2old, nocc, nvir, t1out, t2out, res,
-                                    as_stream(stream));
+                                    as_stream(stream), linear);
+}
+
+int fricc_energy_update(const double* t1num, const double* t2num, const double* eia, const double* fov,
+                        const double* ovov, const double* t1old, const double* t2old, int64_t nocc, int64_t nvir,
+                        double* t1out, double* t2out, double* res, void* stream) {
+  return energy_update(t1num, t2num, eia, fov, ovov, t1old, t2old, nocc, nvir, t1out, t2out, res, stream, false);
+}
+
+int fricc_energy_update_lin(const double* t1num, const double* t2num, const double* eia, const double* fov,
+                            const double* ovov, const double* t1old, const double* t2old, int64_t nocc, int64_t nvir,
+                            double* t1out, double* t2out, double* res, void* stream) {
+  return energy_update(t1num, t2num, eia, fov, ovov, t1old, t2old, nocc, nvir, t1out, t2out, res, stream, true);
 }
 
 int fricc_seq_cumsum(const double* x, int64_t n, double* out, void* stream) {

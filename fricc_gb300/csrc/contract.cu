@@ -149,37 +149,78 @@ __global__ void __launch_bounds__(SP_NT) k_spmm(const int* __restrict__ bptr, co
 //   p = Wh*vh exactly as ph + e (one FMA recovers the rounding error),
 //   pl = e + Wh*vl + Wl*vh (Wl*vl, ~2^-48 relative, is dropped),
 //   (ah, al) += (ph, pl) with an error-free two-sum on the high parts,
-// renormalised every 32 terms; the FP64 result is (double)ah + (double)al.
-// Relative error per output ~1e-14, against FP64's ~1e-16.
+// renormalised once per staged chunk of terms; the FP64 result is
+// (double)ah + (double)al.  Relative error per output ~1e-14, against
+// FP64's ~1e-16.
+//
+// Each thread owns pairs of adjacent outputs (q, q+1) and runs both through
+// the packed f32x2 instructions (add/sub/mul/fma.rn.f32x2): one issue slot
+// per two lanes of arithmetic.  W' is stored to match ("q-pair layout"):
+// row r, pair t holds the float4 (Wh[r][2t], Wh[r][2t+1], Wl[r][2t],
+// Wl[r][2t+1]); rows have ceil(QS/2) pairs, an odd QS padded with zero.
 __device__ __forceinline__ float2 split_f2(double d) {
   const float h = __double2float_rn(d);
   return make_float2(h, __double2float_rn(d - (double)h));
 }
 
-constexpr int DF_NT = 128;
-constexpr int DF_QPT = 4;
+typedef unsigned long long f32x2;  // two floats in one 64-bit register pair
 
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float2 upk2(f32x2 r) {
+  float2 f;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(r));
+  return f;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
+}
+
+constexpr int DF_NT = 128;  // threads per CTA
+constexpr int DF_PPT = 2;   // q-pairs per thread: a CTA covers 512 outputs of a row
+
+// one staged chunk of terms into the thread's DF_PPT accumulator pairs
 template <bool FULL>
-__device__ __forceinline__ void df_tile(const int* __restrict__ srow, const float2* __restrict__ sval, int cnt,
-                                        const float2* __restrict__ wq, int64_t QS, int64_t qrem, float* ah,
-                                        float* al) {
+__device__ __forceinline__ void df_tile(const int* __restrict__ srow, const ulonglong2* __restrict__ sv,
+                                        const f32x2* __restrict__ snv, int cnt, const ulonglong2* __restrict__ wq,
+                                        int64_t QS2, int64_t trem, f32x2* ah, f32x2* al) {
   for (int j = 0; j < cnt; ++j) {
-    const float2* w = wq + (int64_t)srow[j] * QS;
-    const float2 v = sval[j];
+    const ulonglong2* w = wq + (int64_t)srow[j] * QS2;
+    const ulonglong2 v = sv[j];  // (vh, vh), (vl, vl)
+    const f32x2 nvh = snv[j];    // (-vh, -vh)
 #pragma unroll
-    for (int k = 0; k < DF_QPT; ++k) {
-      if (FULL || k * DF_NT < qrem) {
-        // explicit _rn intrinsics: the error-free transforms must not be
-        // contracted into fused multiply-adds by the compiler
-        const float2 x = w[k * DF_NT];
-        const float ph = __fmul_rn(x.x, v.x);
-        float pl = __fmaf_rn(x.x, v.x, -ph);
-        pl = __fmaf_rn(x.x, v.y, pl);
-        pl = __fmaf_rn(x.y, v.x, pl);
-        const float s = __fadd_rn(ah[k], ph);
-        const float z = __fsub_rn(s, ah[k]);
-        const float err = __fadd_rn(__fsub_rn(ah[k], __fsub_rn(s, z)), __fsub_rn(ph, z));
-        al[k] = __fadd_rn(al[k], __fadd_rn(err, pl));
+    for (int k = 0; k < DF_PPT; ++k) {
+      if (FULL || k * DF_NT < trem) {
+        const ulonglong2 x = w[k * DF_NT];           // (Wh, Wh'), (Wl, Wl')
+        const f32x2 nph = mul2(x.x, nvh);            // -ph = -RN(Wh vh)
+        f32x2 pl = fma2(x.x, v.x, nph);              // Wh vh - ph, exact
+        pl = fma2(x.x, v.y, pl);
+        pl = fma2(x.y, v.x, pl);
+        // two-sum (ah, ph) -> (s, err), written with -ph
+        const f32x2 s = sub2(ah[k], nph);
+        const f32x2 z = sub2(s, ah[k]);
+        const f32x2 err = sub2(sub2(ah[k], sub2(s, z)), add2(nph, z));
+        al[k] = add2(al[k], add2(err, pl));
         ah[k] = s;
       }
     }
@@ -187,46 +228,56 @@ __device__ __forceinline__ void df_tile(const int* __restrict__ srow, const floa
 }
 
 __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr, const int* __restrict__ erow,
-                                                   const float2* __restrict__ eval, const float2* __restrict__ Wp,
+                                                   const float2* __restrict__ eval, const float4* __restrict__ Wp4,
                                                    double* __restrict__ Op, int64_t QS) {
   __shared__ int srow[DF_NT];
-  __shared__ float2 sval[DF_NT];
+  __shared__ ulonglong2 sv[DF_NT];
+  __shared__ f32x2 snv[DF_NT];
   const int64_t P = blockIdx.x;
   const int e0 = bptr[P], e1 = bptr[P + 1];
   if (e0 == e1) return;
-  const int64_t q0 = (int64_t)blockIdx.y * (DF_NT * DF_QPT) + threadIdx.x;
-  const int64_t qrem = QS - q0;  // this thread's q values are q0 + k*DF_NT < QS  <=>  k*DF_NT < qrem
-  const bool full = (int64_t)(blockIdx.y + 1) * (DF_NT * DF_QPT) <= QS;  // uniform per block
+  const int64_t QS2 = (QS + 1) >> 1;
+  const int64_t t0 = (int64_t)blockIdx.y * (DF_NT * DF_PPT) + threadIdx.x;
+  const int64_t trem = QS2 - t0;  // this thread's pairs are t0 + k*DF_NT < QS2  <=>  k*DF_NT < trem
+  const bool full = (int64_t)(blockIdx.y + 1) * (DF_NT * DF_PPT) <= QS2;  // uniform per block
   double* orow = Op + P * QS;
-  const float2* wq = Wp + q0;
-  float ah[DF_QPT], al[DF_QPT];
+  const ulonglong2* wq = reinterpret_cast<const ulonglong2*>(Wp4) + t0;
+  f32x2 ah[DF_PPT], al[DF_PPT];
 #pragma unroll
-  for (int k = 0; k < DF_QPT; ++k) {
-    const float2 a = split_f2(k * DF_NT < qrem ? orow[q0 + k * DF_NT] : 0.0);
-    ah[k] = a.x;
-    al[k] = a.y;
+  for (int k = 0; k < DF_PPT; ++k) {
+    const int64_t q = 2 * (t0 + k * DF_NT);
+    const float2 a = split_f2(q < QS ? orow[q] : 0.0);
+    const float2 b = split_f2(q + 1 < QS ? orow[q + 1] : 0.0);
+    ah[k] = pk2(a.x, b.x);
+    al[k] = pk2(a.y, b.y);
   }
   for (int eb = e0; eb < e1; eb += DF_NT) {
     const int cnt = e1 - eb < DF_NT ? e1 - eb : DF_NT;
     __syncthreads();
     if ((int)threadIdx.x < cnt) {
+      const float2 v = eval[eb + threadIdx.x];
       srow[threadIdx.x] = erow[eb + threadIdx.x];
-      sval[threadIdx.x] = eval[eb + threadIdx.x];
+      sv[threadIdx.x] = make_ulonglong2(pk2(v.x, v.x), pk2(v.y, v.y));
+      snv[threadIdx.x] = pk2(-v.x, -v.x);
     }
     __syncthreads();
-    if (full) df_tile<true>(srow, sval, cnt, wq, QS, qrem, ah, al);
-    else df_tile<false>(srow, sval, cnt, wq, QS, qrem, ah, al);
+    if (full) df_tile<true>(srow, sv, snv, cnt, wq, QS2, trem, ah, al);
+    else df_tile<false>(srow, sv, snv, cnt, wq, QS2, trem, ah, al);
     // renormalise once per staged chunk (<= DF_NT terms): keeps |al| ~ ulp(ah)
 #pragma unroll
-    for (int k = 0; k < DF_QPT; ++k) {
-      const float s = __fadd_rn(ah[k], al[k]);
-      al[k] = __fsub_rn(al[k], __fsub_rn(s, ah[k]));
+    for (int k = 0; k < DF_PPT; ++k) {
+      const f32x2 s = add2(ah[k], al[k]);
+      al[k] = sub2(al[k], sub2(s, ah[k]));
       ah[k] = s;
     }
   }
 #pragma unroll
-  for (int k = 0; k < DF_QPT; ++k)
-    if (k * DF_NT < qrem) orow[q0 + k * DF_NT] = (double)ah[k] + (double)al[k];
+  for (int k = 0; k < DF_PPT; ++k) {
+    const int64_t q = 2 * (t0 + k * DF_NT);
+    const float2 h = upk2(ah[k]), l = upk2(al[k]);
+    if (q < QS) orow[q] = (double)h.x + (double)l.x;
+    if (q + 1 < QS) orow[q + 1] = (double)h.y + (double)l.y;
+  }
 }
 
 __global__ void k_entries_df(const int* __restrict__ slots, const double* __restrict__ vals,
@@ -239,9 +290,15 @@ __global__ void k_entries_df(const int* __restrict__ slots, const double* __rest
   }
 }
 
-__global__ void k_split_f2(const double* __restrict__ x, int64_t n, float2* __restrict__ out) {
-  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x)
-    out[i] = split_f2(x[i]);
+// x [rows][QS] (FP64) -> the q-pair layout of k_spmm_df
+__global__ void k_split_f2(const double* __restrict__ x, int64_t rows, int64_t QS, float4* __restrict__ out) {
+  const int64_t QS2 = (QS + 1) >> 1, n = rows * QS2;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = i / QS2, q = 2 * (i - r * QS2);
+    const float2 a = split_f2(x[r * QS + q]);
+    const float2 b = split_f2(q + 1 < QS ? x[r * QS + q + 1] : 0.0);
+    out[i] = make_float4(a.x, b.x, a.y, b.y);
+  }
 }
 
 // dst (contiguous, extents e0..e3) = src viewed with strides s0..s3
@@ -469,11 +526,15 @@ int fricc_spmm_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coe
 
 // As fricc_spmm_device with W' pre-split into float pairs (fricc_split_f2);
 // the products and sums run on the FP32 pipe in pair arithmetic.
-int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float2* Wp, int64_t QS,
+int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float4* Wp, int64_t QS,
                          double* Op, cudaStream_t st) {
   if (!T || !Wp || !Op || QS <= 0 || pa < 0 || pa > 3 || pb < 0 || pb > 3 || ka < 0 || ka > 3 || kb < 0 || kb > 3 ||
       pa == pb || ka == kb) {
     fricc_set_error("spmm_f2: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  if (reinterpret_cast<uintptr_t>(Wp) % 16 != 0) {
+    fricc_set_error("spmm_f2: W' (q-pair layout) must be 16-byte aligned");
     return FRICC_ERR_ARG;
   }
   if (T->m == 0) return FRICC_OK;
@@ -484,7 +545,7 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
   float2* eval = nullptr;
   rc = fricc_alloc_t(&erow, T->m, st);
   if (!rc) rc = fricc_alloc_t(&eval, T->m, st);
-  const int64_t ntq = fricc_cdiv(QS, DF_NT * DF_QPT);
+  const int64_t ntq = fricc_cdiv((QS + 1) / 2, DF_NT * DF_PPT);
   if (!rc && (ntq > 65535 || bk->nbuckets > 0x7fffffffLL)) {
     fricc_set_error("spmm_f2: problem too large for one launch");
     rc = FRICC_ERR_ARG;
@@ -505,13 +566,18 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
   return rc;
 }
 
-int fricc_split_f2_device(const double* x, int64_t n, float2* out, cudaStream_t st) {
-  if (n < 0 || (n > 0 && (!x || !out))) {
+int fricc_split_f2_device(const double* x, int64_t rows, int64_t qs, float4* out, cudaStream_t st) {
+  if (rows < 0 || qs < 0 || (rows > 0 && qs > 0 && (!x || !out))) {
     fricc_set_error("split_f2: bad arguments");
     return FRICC_ERR_ARG;
   }
+  if (reinterpret_cast<uintptr_t>(out) % 16 != 0) {
+    fricc_set_error("split_f2: output must be 16-byte aligned");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t n = rows * ((qs + 1) / 2);
   if (n == 0) return FRICC_OK;
-  k_split_f2<<<grid_for(n, 256), 256, 0, st>>>(x, n, out);
+  k_split_f2<<<grid_for(n, 256), 256, 0, st>>>(x, rows, qs, out);
   fricc_note_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "split_f2", __FILE__, __LINE__);

@@ -114,16 +114,21 @@ int fricc_contract(const char* term, const double* W, const int64_t W_dims[4], c
 int fricc_spmm(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const double* Wp, int64_t QS,
                double* Op, void* stream);
 
-/* fricc_spmm in FP32-pair arithmetic (no reference counterpart): Wp2 is W'
- * split into (hi, lo) float pairs by fricc_split_f2 (2*n floats, 8-byte
- * aligned); every product and sum carries ~48 significand bits (relative
- * error per output ~1e-14) and runs on the FP32 pipe.  Op stays FP64. */
-int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* Wp2, int64_t QS,
+/* fricc_spmm in FP32-pair arithmetic (no reference counterpart): Wp4 is W'
+ * split by fricc_split_f2 into its q-pair layout (16-byte aligned); every
+ * product and sum carries ~48 significand bits (relative error per output
+ * ~1e-14) and runs on the FP32 pipe, two outputs per packed instruction.
+ * Op stays FP64. */
+int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* Wp4, int64_t QS,
                   double* Op, void* stream);
 
-/* out2[2i] + out2[2i+1] = x[i] to ~2^-48 relative: hi = (float)x,
- * lo = (float)(x - hi).  Stream-ordered. */
-int fricc_split_f2(const double* x, int64_t n, float* out2, void* stream);
+/* x [rows][qs] (FP64, contiguous) split into float pairs hi = (float)x,
+ * lo = (float)(x - hi) (hi + lo = x to ~2^-48 relative), in the q-pair
+ * layout fricc_spmm_f2 reads: for row r and pair t < ceil(qs/2), the four
+ * floats out4[4(r ceil(qs/2) + t) ..] = hi[r][2t], hi[r][2t+1], lo[r][2t],
+ * lo[r][2t+1] (an odd qs padded with zero).  out4 holds
+ * 4 rows ceil(qs/2) floats, 16-byte aligned.  Stream-ordered. */
+int fricc_split_f2(const double* x, int64_t rows, int64_t qs, float* out4, void* stream);
 
 /* Strided batched GEMM, FP64 in and out, products and sums in FP32 pairs
  * (no reference counterpart; it runs the dense O^2V^3 contractions of the
@@ -167,6 +172,13 @@ int fricc_seq_cumsum_noalloc(const double* x, int64_t n, double* out, void* stre
 int fricc_energy_update(const double* t1num, const double* t2num, const double* eia, const double* fov,
                         const double* ovov, const double* t1old, const double* t2old, int64_t nocc, int64_t nvir,
                         double* t1out, double* t2out, double* res, void* stream);
+
+/* The same update with the linearised energy of FRI-LCCSD,
+ * E = 2 sum f_ia t1_ia + sum t2_ijab (2 (ia|jb) - (ib|ja)): replaces the
+ * denominators of fricc/frilccsd.py:241-244 and lin_cc_energy :504-522. */
+int fricc_energy_update_lin(const double* t1num, const double* t2num, const double* eia, const double* fov,
+                            const double* ovov, const double* t1old, const double* t2old, int64_t nocc,
+                            int64_t nvir, double* t1out, double* t2out, double* res, void* stream);
 
 /* Instrumentation (no reference counterpart): the number of kernels this
  * library has launched so far; and CUDA-event timing of every sparse

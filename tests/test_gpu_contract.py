@@ -121,14 +121,16 @@ def test_spmm_f2_matches_fp64(gpulib):
     x = rng.standard_normal((o, o, v, v)) * np.exp(rng.standard_normal((o, o, v, v)))
     T = py_rccsd.SparseTensor4d(x, x.shape, 20000, "fri", "systematic", rn=0.6)
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
-    for (pa, pb, ka, kb, nkey, QS) in ((0, 1, 2, 3, v * v, v * v), (1, 3, 0, 2, o * v, o * v), (3, 0, 1, 2, o * v, o * v)):
+    cases = ((0, 1, 2, 3, v * v, v * v), (1, 3, 0, 2, o * v, o * v), (3, 0, 1, 2, o * v, o * v),
+             (0, 1, 2, 3, v * v, 777), (2, 3, 0, 1, o * o, 1), (2, 3, 0, 1, o * o, 2049))   # odd / tiny / ragged QS
+    for (pa, pb, ka, kb, nkey, QS) in cases:
         W = torch.from_numpy(rng.standard_normal((nkey, QS)) * 10.0 ** rng.integers(-6, 2, (nkey, 1))).cuda()
         nP = {0: o, 1: o, 2: v, 3: v}[pa] * {0: o, 1: o, 2: v, 3: v}[pb]
         out0 = torch.from_numpy(rng.standard_normal((nP, QS))).cuda()
         a, b = out0.clone(), out0.clone()
         _lib.check(gpulib.fricc_spmm(T.handle, pa, pb, ka, kb, -0.5, ctypes.c_void_p(W.data_ptr()), QS,
                                      ctypes.c_void_p(a.data_ptr()), st))
-        W2 = split_f2(W)
+        W2 = split_f2(W, QS)
         _lib.check(gpulib.fricc_spmm_f2(T.handle, pa, pb, ka, kb, -0.5, ctypes.c_void_p(W2.data_ptr()), QS,
                                         ctypes.c_void_p(b.data_ptr()), st))
         a, b = a.cpu().numpy(), b.cpu().numpy()
