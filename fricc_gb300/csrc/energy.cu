@@ -3,6 +3,7 @@
 //   t1 = t1num / eia,  t2 = t2num / (eia[i,a] + eia[j,b])   fri-cc fricc/friccsd.py:281-284
 //   E  = 2 sum f_ia t1_ia + sum tau_ijab (2 (ia|jb) - (ib|ja)),  tau = t2 + t1 t1
 //                                                             (CCSD energy, :427)
+//        or, linearised (FRI-LCCSD, fricc/frilccsd.py:504-522), tau = t2
 //   normt = || vec(t1,t2) - vec(t1old,t2old) ||, vec = t1 and the lower
 //           triangle of t2 seen as an (ia, jb) matrix          (:418-420)
 // One pass over t2num, ovov and t2old; (ib|ja) is read through a shared
@@ -14,6 +15,7 @@ namespace {
 
 constexpr int TB = 32;  // (a,b) tile edge
 
+template <bool LIN>
 __global__ void __launch_bounds__(256) k_t2_energy(const double* __restrict__ t2num, const double* __restrict__ t1,
                                                    const double* __restrict__ eia, const double* __restrict__ ovov,
                                                    const double* __restrict__ t2old, double* __restrict__ t2out,
@@ -39,7 +41,7 @@ __global__ void __launch_bounds__(256) k_t2_energy(const double* __restrict__ t2
       const int64_t idx = ((i * o + j) * v + a) * v + b;
       const double t2 = t2num[idx] / (eia[i * v + a] + eia[j * v + b]);
       t2out[idx] = t2;
-      const double tau = t2 + t1[i * v + a] * t1[j * v + b];
+      const double tau = LIN ? t2 : t2 + t1[i * v + a] * t1[j * v + b];
       const double iajb = ovov[((i * v + a) * o + j) * v + b];
       e_acc += tau * (2.0 * iajb - xt[tx][r]);
       if (i * v + a >= j * v + b) {
@@ -99,7 +101,7 @@ __global__ void __launch_bounds__(256) k_final(const double* __restrict__ part_e
 // may alias t1num/t2num.
 int fricc_energy_update_device(const double* t1num, const double* t2num, const double* eia, const double* fov,
                                const double* ovov, const double* t1old, const double* t2old, int64_t o, int64_t v,
-                               double* t1out, double* t2out, double* res, cudaStream_t st) {
+                               double* t1out, double* t2out, double* res, cudaStream_t st, bool linear) {
   if (o <= 0 || v <= 0) {
     fricc_set_error("energy_update: empty system");
     return FRICC_ERR_ARG;
@@ -114,8 +116,11 @@ int fricc_energy_update_device(const double* t1num, const double* t2num, const d
   int rc = fricc_alloc_t(&part, 2 * gx * gy, st);
   if (rc) return rc;
   k_t1<<<1, 256, 0, st>>>(t1num, eia, fov, t1old, t1out, o * v, res);
-  k_t2_energy<<<dim3((unsigned)gx, (unsigned)gy), 256, 0, st>>>(t2num, t1out, eia, ovov, t2old, t2out, o, v, part,
-                                                                part + gx * gy);
+  const dim3 grid((unsigned)gx, (unsigned)gy);
+  if (linear)
+    k_t2_energy<true><<<grid, 256, 0, st>>>(t2num, t1out, eia, ovov, t2old, t2out, o, v, part, part + gx * gy);
+  else
+    k_t2_energy<false><<<grid, 256, 0, st>>>(t2num, t1out, eia, ovov, t2old, t2out, o, v, part, part + gx * gy);
   k_final<<<1, 256, 0, st>>>(part, part + gx * gy, gx * gy, res);
   fricc_note_launch(3);
   cudaError_t e = cudaGetLastError();
