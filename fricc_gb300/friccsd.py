@@ -17,8 +17,12 @@ and ``kernel`` (:379-456) on the device:
 
 Settings are the reference's ``fri_settings`` keys.  The reference reads
 ``fri_settings["unbiased"]`` (:109), a key its defaults never set (they set
-"unbias"); a missing key is treated as False here.  The running-average
-("unbiased") mode is not implemented.
+"unbias"); a missing key is treated as False here.  With "unbiased" true,
+the W-intermediate compression takes, after ``burn_in`` iterations, the
+running average of the T2 inputs (:108-136, the formula as written, FP64
+and bit for bit); the iteration counter the reference reads there
+(``cc._iter``) is never defined by it, and is here the number of
+``update_amps`` calls this solver has run (``reset_average()`` zeroes it).
 
 ``update_amps_host`` is the end-to-end entry: host (numpy) amplitudes in,
 host amplitudes out, the copies included.
@@ -96,8 +100,6 @@ class FRICCSDGPU:
             raise ValueError(f"The compression method you chose ({s['compression']}) isn't supported")
         if s["compression"] == "fri" and s["sampling_method"] != "systematic":
             raise NotImplementedError("sampling_method 'pivotal' is not implemented on the GPU path")
-        if s.get("unbiased", False):
-            raise NotImplementedError("the running-average ('unbiased') mode is not implemented")
         self.settings = s
         self.eris = eris
         self.level_shift = float(level_shift)
@@ -113,6 +115,8 @@ class FRICCSDGPU:
         self._sp_w = _Handle()
         self._res = torch.zeros(4, dtype=torch.float64, device=eris.device)
         self._wT = None
+        self._iter = 0
+        self._t2_avg = None
         self.timings = {}
         self.last_energy = None
         self.last_normt = None
@@ -131,7 +135,8 @@ class FRICCSDGPU:
         form is cached on the DeviceERIs."""
         assert Wp.is_contiguous() and Op.is_contiguous()
         if self.precision == "df64":
-            W2 = self.eris.split(const) if const else D.split_f2(Wp)
+            W2 = self.eris.split(const) if const else D.split_f2(Wp, QS)
+            assert W2.numel() == (Wp.numel() // QS) * ((QS + 1) // 2) * 4, "float-pair W' split with another QS"
             L.check(self.lib.fricc_spmm_f2(T, pa, pb, ka, kb, float(coef), _ptr(W2), int(QS), _ptr(Op), stream))
         else:
             L.check(self.lib.fricc_spmm(T, pa, pb, ka, kb, float(coef), _ptr(Wp), int(QS), _ptr(Op), stream))
@@ -171,7 +176,8 @@ class FRICCSDGPU:
             kind = s["compression"]
             rn = [self.rn_draw() if kind == "fri" else 0.0 for _ in range(2 if need_w else 1)]
         T = self._sp.compress(t2, m, s["compression"], rn[0], st)
-        Tw = self._sp_w.compress(t2, m, s["compression"], rn[1], st) if need_w else None
+        Tw = self._sp_w.compress(self._w_source(t2), m, s["compression"], rn[1], st) if need_w else None
+        self._iter += 1
 
         mm = D.gemm_df if self.precision == "df64" else D.gemm_torch
         ein2 = D.einsum_df if self.precision == "df64" else torch.einsum   # two-operand O^3V^2 contractions
@@ -322,6 +328,28 @@ class FRICCSDGPU:
                                              _ptr(E.ovov), _ptr(t1o.contiguous()), _ptr(t2o.contiguous()), o, v,
                                              _ptr(t1new), _ptr(t2new), _ptr(self._res), st))
         return t1new, t2new
+
+    def _w_source(self, t2):
+        """T2, or after burn-in in the unbiased mode its running average
+        Y = X/it + (it-1)/it Y (it = iterations past burn-in; it = 0 and 1 both
+        restart from X), evaluated in the reference's operation order."""
+        s = self.settings
+        if not s.get("unbiased", False) or self._iter < s["burn_in"]:
+            return t2
+        it = self._iter - s["burn_in"]
+        if it == 0 or self._t2_avg is None:
+            self._t2_avg = t2.clone()
+        else:
+            # a tensor divisor: division by a host scalar may be done as a
+            # multiply by its reciprocal, which rounds differently from X/it
+            div = torch.full((1,), float(it), dtype=t2.dtype, device=t2.device)
+            self._t2_avg = t2 / div + ((it - 1) / it) * self._t2_avg
+        return self._t2_avg
+
+    def reset_average(self):
+        """Restart the iteration count (and so the burn-in) of the unbiased mode."""
+        self._iter = 0
+        self._t2_avg = None
 
     def read_energy(self):
         r = self._res[:2].cpu()

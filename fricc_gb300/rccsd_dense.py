@@ -229,14 +229,20 @@ def gemm_torch(A, B, C, alpha=1.0, beta=0.0):
     return C
 
 
-def split_f2(x: torch.Tensor) -> torch.Tensor:
-    """x (FP64, contiguous) as interleaved (hi, lo) floats, hi + lo = x to ~2^-48."""
+def split_f2(x: torch.Tensor, qs: int = None) -> torch.Tensor:
+    """W' [rows][qs] (FP64) as float pairs hi + lo = x (~2^-48), in the
+    q-pair layout of fricc_spmm_f2: per row, float4 (hi_q, hi_q+1, lo_q,
+    lo_q+1) for q = 0, 2, 4, ...  qs defaults to the product of the
+    dimensions after the first two (W' is always [key1, key2, q...])."""
     import ctypes
 
     from . import _lib as L
     x = x.contiguous()
-    out = torch.empty(x.numel() * 2, dtype=torch.float32, device=x.device)
-    L.check(L.load().fricc_split_f2(ctypes.c_void_p(x.data_ptr()), x.numel(), ctypes.c_void_p(out.data_ptr()),
+    if qs is None:
+        qs = math.prod(x.shape[2:]) if x.dim() > 2 else x.shape[-1]
+    rows = x.numel() // qs
+    out = torch.empty(rows * ((qs + 1) // 2) * 4, dtype=torch.float32, device=x.device)
+    L.check(L.load().fricc_split_f2(ctypes.c_void_p(x.data_ptr()), rows, qs, ctypes.c_void_p(out.data_ptr()),
                                     ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return out
 

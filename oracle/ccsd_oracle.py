@@ -10,6 +10,12 @@ and the denominators) on numpy, with the compressions and contractions taken
 from the C oracle (oracle/fri_oracle.c) and the dense CCSD algebra from
 oracle/pyscf_standin.py.  ``kernel`` restates the iteration loop :379-456.
 
+With ``settings["unbiased"]`` the W-intermediate compression takes, once
+``burn_in`` iterations have run, the running average of the T2 inputs
+instead of T2 (fricc/friccsd.py:108-136).  The reference reads an iteration
+counter ``cc._iter`` that nothing defines; here it is ``state["iter"]``, the
+number of updates run before this one, kept with the average in ``state``.
+
 The reference's T2 update adds ``einsum("abcd,ia,jb->ijab", Wvvvv, t1, t1)``
 (fricc/friccsd.py:222), which sums c and d inside Wvvvv instead of
 contracting them with t1 (CCSD has ``ic,jd``).  Parity means reproducing
@@ -42,7 +48,7 @@ def _sym(x):
 
 
 def update_amps(settings, t1, t2, eris, rn_draw=FO.libc_rand_uniform, sparse=FO,
-                level_shift=0.0, timings=None, wvvvv_t1t1="reference"):
+                level_shift=0.0, timings=None, wvvvv_t1t1="reference", state=None):
     """One FRI-CCSD amplitude update; returns (t1new, t2new).
 
     rn_draw() supplies the uniform draw of each systematic compression, in
@@ -60,15 +66,29 @@ def update_amps(settings, t1, t2, eris, rn_draw=FO.libc_rand_uniform, sparse=FO,
     fov = fock[:nocc, nocc:].copy()
     t2 = np.ascontiguousarray(t2)
 
-    def compress():
+    def compress(x=t2):
         kind = settings["compression"]
         rn = rn_draw() if kind == "fri" else None
-        return sparse.SparseTensor4d(t2, t2.shape, m, kind, settings["sampling_method"],
+        return sparse.SparseTensor4d(x, x.shape, m, kind, settings["sampling_method"],
                                      settings["verbose"], rn=rn)
+
+    state = {} if state is None else state
+    n_done = state.get("iter", 0)
 
     tc = time.perf_counter()
     t2_sp = compress()
-    t2_sp_w = compress() if ("O^3V^3" in comp or "O^4V^2" in comp) else None
+    t2_sp_w = None
+    if "O^3V^3" in comp or "O^4V^2" in comp:
+        if not settings.get("unbiased", False) or n_done < settings.get("burn_in", 100):
+            t2_sp_w = compress()
+        else:  # running average Y(t+1) = (1 - 1/t) Y(t) + X(t)/t, as written at :121-127
+            it = n_done - settings.get("burn_in", 100)
+            if it == 0:
+                state["t2_avg"] = t2
+            else:
+                state["t2_avg"] = t2 / it + (it - 1) / it * state["t2_avg"]
+            t2_sp_w = compress(state["t2_avg"])
+    state["iter"] = n_done + 1
     tim["compress"] = time.perf_counter() - tc
 
     Foo = PS.cc_Foo(t1, t2, eris)
@@ -201,12 +221,13 @@ def kernel(settings, eris, t1=None, t2=None, max_cycle=50, tol=1e-8, tolnormt=1e
     if t1 is None or t2 is None:
         t1, t2 = PS.mp2_guess(eris)
     eold = 0.0
+    state = {}
     ecc = PS.ccsd_energy(t1, t2, eris)
     energies = []
     conv = False
     for it in range(max_cycle):
         t1n, t2n = update_amps(settings, t1, t2, eris, rn_draw=rn_draw, sparse=sparse,
-                               wvvvv_t1t1=wvvvv_t1t1)
+                               wvvvv_t1t1=wvvvv_t1t1, state=state)
         normt = np.linalg.norm(PS.amplitudes_to_vector(t1n, t2n) - PS.amplitudes_to_vector(t1, t2))
         t1, t2 = t1n, t2n
         eold, ecc = ecc, PS.ccsd_energy(t1, t2, eris)

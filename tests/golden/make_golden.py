@@ -15,6 +15,9 @@ records:
                    synthetic system: every iterate, every energy, every draw;
 * lccsd.npz     -- the same for fricc/frilccsd.py (FRI-LCCSD): one shared
                    compression, six independent compressions, and LCCD.
+* unbiased.npz  -- fricc/friccsd.py with "unbiased": True (running-average
+                   W compression after burn-in), its missing iteration
+                   counter supplied by the driver.
 
 Usage:  OMP_NUM_THREADS=1 python tests/golden/make_golden.py
 """
@@ -243,13 +246,54 @@ def lccsd_cases(R):
     return out
 
 
+def unbiased_case(R):
+    """fricc/friccsd.py with "unbiased": True.  The reference reads an
+    iteration counter cc._iter that it never defines; the driver here sets it
+    to the number of updates already run before each call, so the
+    reference's own running-average code (:108-136) runs unmodified."""
+    F = load_reference_friccsd(R)
+    s = SyntheticSystem(4, 12, 60, 0.05, 7)
+    eris = pyscf_standin.make_eris(s)
+    settings = {"m_keep": 800, "compression": "fri", "sampling_method": "systematic",
+                "verbose": False, "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"],
+                "unbiased": True, "burn_in": 2}
+
+    class Driver(pyscf_standin.CCSD):
+        pass
+
+    cc = Driver(eris, settings)
+    n_iter = 7
+    cc.max_cycle = n_iter
+    cc._iter = 0
+    t1, t2 = pyscf_standin.mp2_guess(eris)
+    iterates = [(t1, t2)]
+
+    def record(t1, t2, eris):
+        r = F.update_amps(cc, t1, t2, eris)
+        cc._iter += 1
+        iterates.append(r)
+        return r
+
+    cc.update_amps = record
+    seed = 41
+    libc.srand(seed)
+    F.kernel(cc, eris, t1, t2)
+    return {
+        "L": s.L, "mo_energy": s.mo_energy, "nocc": np.int64(4), "m": np.int64(800), "burn_in": np.int64(2),
+        "seed": np.int64(seed), "rn": np.array(draws(seed, 2 * (len(iterates) - 1))),
+        "energies": np.array(cc.energies),
+        "t1": np.stack([a for a, _ in iterates]), "t2": np.stack([b for _, b in iterates]),
+    }
+
+
 def main():
     R = load_reference_module()
     np.savez_compressed(os.path.join(HERE, "compress.npz"), **compress_cases(R))
     np.savez_compressed(os.path.join(HERE, "contract.npz"), **contract_cases(R))
     np.savez_compressed(os.path.join(HERE, "iteration.npz"), **iteration_case(R))
     np.savez_compressed(os.path.join(HERE, "lccsd.npz"), **lccsd_cases(R))
-    for f in ("compress.npz", "contract.npz", "iteration.npz", "lccsd.npz"):
+    np.savez_compressed(os.path.join(HERE, "unbiased.npz"), **unbiased_case(R))
+    for f in ("compress.npz", "contract.npz", "iteration.npz", "lccsd.npz", "unbiased.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

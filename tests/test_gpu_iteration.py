@@ -122,3 +122,37 @@ def test_e2e_host_entry(gpulib):
     a1, a2 = gs.update_amps_host(t1h, t2h, rn=[0.1, 0.2])
     b1, b2 = gs.update_amps(torch.from_numpy(t1h).cuda(), torch.from_numpy(t2h).cuda(), rn=[0.1, 0.2])
     assert np.array_equal(a2, b2.cpu().numpy()) and np.array_equal(a1, b1.cpu().numpy())
+
+
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_unbiased_golden_teacher_forced(gpulib, precision):
+    """The running-average W compression after burn-in against the reference's
+    own trajectory (tests/golden/unbiased.npz): the average of the inputs is
+    bit for bit numpy's, so every compression matches and each step's energy
+    agrees to 1e-10 Eh."""
+    from fricc_gb300.friccsd import FRICCSDGPU
+    from fricc_gb300.rccsd_dense import DeviceERIs
+    from fricc_gb300.synthetic import SyntheticSystem
+    g = golden("unbiased.npz")
+    s = SyntheticSystem.__new__(SyntheticSystem)
+    s.nocc, s.L, s.mo_energy = int(g["nocc"]), g["L"], g["mo_energy"]
+    s.naux, s.nvir = s.L.shape[0], s.mo_energy.size - int(g["nocc"])
+    s.sigma, s.seed = 0.0, 0
+    b = int(g["burn_in"])
+    gs = FRICCSDGPU(DeviceERIs.from_system(s), dict(SETTINGS, m_keep=int(g["m"]), unbiased=True, burn_in=b),
+                    precision=precision)
+    rn = list(g["rn"])
+    y = None
+    for it in range(len(g["energies"])):
+        t1 = torch.from_numpy(g["t1"][it]).cuda()
+        t2 = torch.from_numpy(g["t2"][it]).cuda()
+        t1n, t2n = gs.update_amps(t1, t2, rn=rn[2 * it: 2 * it + 2])
+        e, _ = gs.read_energy()
+        assert abs(e - g["energies"][it]) < 1e-10, (it, e, g["energies"][it])
+        ref = g["t2"][it + 1]
+        assert np.abs(t2n.cpu().numpy() - ref).max() < 1e-10 * np.abs(ref).max()
+        if it >= b:
+            k = it - b
+            y = g["t2"][it] if k <= 1 else g["t2"][it] / k + (k - 1) / k * y
+            assert np.array_equal(gs._t2_avg.cpu().numpy(), y), it
+    assert y is not None

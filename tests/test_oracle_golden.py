@@ -152,3 +152,53 @@ def test_lccsd_golden_free_running(oracle, name, indep, lccd):
                                           g[f"{name}_t2"][0], max_cycle=len(g[f"{name}_energies"]),
                                           rn_draw=lambda: next(draws), independent=indep, lccd=lccd)
     assert np.max(np.abs(np.array(energies) - g[f"{name}_energies"])) < 1e-10
+
+
+def _unbiased_system():
+    g = golden("unbiased.npz")
+    from oracle import pyscf_standin as P
+    from fricc_gb300.synthetic import SyntheticSystem
+
+    class Sys:
+        pass
+
+    s = Sys()
+    s.nocc = int(g["nocc"])
+    s.L = g["L"]
+    s.mo_energy = g["mo_energy"]
+    s.nmo = s.mo_energy.size
+    s.nvir = s.nmo - s.nocc
+    s.fock = np.diag(s.mo_energy)
+    s.naux = s.L.shape[0]
+    s.eri = lambda b: SyntheticSystem.eri(s, b)
+    s._sl = lambda c: SyntheticSystem._sl(s, c)
+    return g, P.make_eris(s)
+
+
+def test_unbiased_golden(oracle):
+    """The running-average W compression after burn-in (fricc/friccsd.py:108-136):
+    the oracle's loop follows the reference's trajectory, and teacher-forced
+    steps (the average accumulating the reference's own inputs) match each iterate."""
+    from oracle import ccsd_oracle as CO
+    g, eris = _unbiased_system()
+    settings = {"m_keep": int(g["m"]), "compression": "fri", "sampling_method": "systematic", "verbose": False,
+                "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"], "unbiased": True,
+                "burn_in": int(g["burn_in"])}
+    draws = iter(list(g["rn"]))
+    conv, e, t1, t2, energies = CO.kernel(settings, eris, g["t1"][0], g["t2"][0], max_cycle=len(g["energies"]),
+                                          rn_draw=lambda: next(draws))
+    assert np.max(np.abs(np.array(energies) - g["energies"])) < 1e-10
+    state = {}
+    rn = list(g["rn"])
+    for it in range(len(g["energies"])):
+        d = iter(rn[2 * it: 2 * it + 2])
+        t1n, t2n = CO.update_amps(settings, g["t1"][it], g["t2"][it], eris, rn_draw=lambda: next(d), state=state)
+        np.testing.assert_allclose(t2n, g["t2"][it + 1], rtol=0, atol=1e-13)
+    assert state["iter"] == len(g["energies"])
+    # the average after burn-in: it=0 -> T2 input, it=1 -> reset to the input, then (1-1/it) Y + X/it
+    b = int(g["burn_in"])
+    y = g["t2"][b]
+    for k in range(b + 1, len(g["energies"])):
+        it = k - b
+        y = g["t2"][k] / it + (it - 1) / it * y
+    assert np.array_equal(state["t2_avg"], y)
