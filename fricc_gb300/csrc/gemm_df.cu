@@ -8,7 +8,8 @@
 // lanes).  Operands are split on the fly into (hi, lo) float pairs as they
 // are staged in shared memory; products are formed exactly to ~48 bits
 // (one FMA recovers the rounding error of hi*hi) and accumulated with an
-// error-free two-sum, renormalised every K tile.  Relative error of each
+// error-free two-sum, renormalised every K tile, two adjacent outputs per
+// packed f32x2 instruction.  Relative error of each
 // output ~1e-14.  A long K is split over blockIdx.z; the partial tiles are
 // summed afterwards in a fixed order, so results are deterministic.
 #include "common.cuh"
@@ -20,6 +21,40 @@ constexpr int BK = 16, NT = 256;
 __device__ __forceinline__ float2 split(double d) {
   const float h = __double2float_rn(d);
   return make_float2(h, __double2float_rn(d - (double)h));
+}
+
+// two floats in one 64-bit register pair, and the packed f32x2 arithmetic
+// (one issue slot per two lanes of FP32 work)
+typedef unsigned long long f32x2;
+__device__ __forceinline__ f32x2 pk2(float lo, float hi) {
+  f32x2 r;
+  asm("mov.b64 %0, {%1, %2};" : "=l"(r) : "f"(lo), "f"(hi));
+  return r;
+}
+__device__ __forceinline__ float2 upk2(f32x2 r) {
+  float2 f;
+  asm("mov.b64 {%0, %1}, %2;" : "=f"(f.x), "=f"(f.y) : "l"(r));
+  return f;
+}
+__device__ __forceinline__ f32x2 add2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("add.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 sub2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("sub.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 mul2(f32x2 a, f32x2 b) {
+  f32x2 d;
+  asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(d) : "l"(a), "l"(b));
+  return d;
+}
+__device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
+  f32x2 d;
+  asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(d) : "l"(a), "l"(b), "l"(c));
+  return d;
 }
 
 struct GemmArgs {
@@ -34,14 +69,20 @@ struct GemmArgs {
   int64_t kchunk;  // K per split (multiple of BK)
 };
 
-// 256 threads as 16 x 16; each owns a TM x TN block of C (rows ty + 16 i,
-// columns tx + 16 j), so a CTA tile is (16 TM) x (16 TN): 64x64 for square
-// problems, 128x32 / 32x128 when one side is as small as nocc.
+// 256 threads as 16 x 16.  Thread (tx, ty) owns rows ty + 16 i (i < TM) and
+// the column pairs 2 (tx + 16 j) + {0, 1} (j < TN / 2) of a (16 TM) x (16 TN)
+// tile of C; each pair is accumulated with packed f32x2 instructions.  The
+// shared tiles hold the operands already split: A as (h, h, l, l) per
+// element (broadcast to both lanes of a pair), B per column pair as
+// (h0, h1, l0, l1) plus (-h0, -h1) (the negated high part gives the exact
+// product error with one fma).  Rows are padded by one element so that the
+// staging stores do not conflict on banks.
 template <int TM, int TN>
 __global__ void __launch_bounds__(NT) k_gemm_df(GemmArgs g) {
-  constexpr int BM = 16 * TM, BN = 16 * TN;
-  __shared__ float2 As[BK][BM + 1];
-  __shared__ float2 Bs[BK][BN + 1];
+  constexpr int BM = 16 * TM, BN = 16 * TN, NP = BN / 2, JP = TN / 2;
+  __shared__ ulonglong2 As[BK][BM + 1];
+  __shared__ ulonglong2 Bs[BK][NP + 1];
+  __shared__ f32x2 Bn[BK][NP + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
   const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
   const int64_t bz = blockIdx.z / g.splits;
@@ -51,11 +92,11 @@ __global__ void __launch_bounds__(NT) k_gemm_df(GemmArgs g) {
   const double* A = g.A + bz * g.sAb;
   const double* B = g.B + bz * g.sBb;
 
-  float ah[TM][TN], al[TM][TN];
+  f32x2 ah[TM][JP], al[TM][JP];
 #pragma unroll
   for (int i = 0; i < TM; ++i)
 #pragma unroll
-    for (int j = 0; j < TN; ++j) ah[i][j] = al[i][j] = 0.f;
+    for (int j = 0; j < JP; ++j) ah[i][j] = al[i][j] = 0ull;  // +0.0f in both lanes
 
   const bool a_kfast = g.sAk == 1;
   const bool b_nfast = g.sBn == 1;
@@ -67,61 +108,75 @@ __global__ void __launch_bounds__(NT) k_gemm_df(GemmArgs g) {
       int mm, kk;
       if (a_kfast) { mm = idx / BK; kk = idx % BK; } else { kk = idx / BM; mm = idx % BM; }
       const int64_t m = m0 + mm, k = k0 + kk;
-      As[kk][mm] = split((m < g.M && k < k_end) ? A[m * g.sAm + k * g.sAk] : 0.0);
+      const float2 a = split((m < g.M && k < k_end) ? A[m * g.sAm + k * g.sAk] : 0.0);
+      As[kk][mm] = make_ulonglong2(pk2(a.x, a.x), pk2(a.y, a.y));
     }
 #pragma unroll
-    for (int r = 0; r < (BN * BK) / NT; ++r) {
+    for (int r = 0; r < (NP * BK + NT - 1) / NT; ++r) {
       const int idx = r * NT + threadIdx.x;
-      int nn, kk;
-      if (b_nfast) { kk = idx / BN; nn = idx % BN; } else { nn = idx / BK; kk = idx % BK; }
-      const int64_t n = n0 + nn, k = k0 + kk;
-      Bs[kk][nn] = split((n < g.N && k < k_end) ? B[k * g.sBk + n * g.sBn] : 0.0);
+      if ((NP * BK) % NT == 0 || idx < NP * BK) {
+        int pp, kk;
+        if (b_nfast) { kk = idx / NP; pp = idx % NP; } else { pp = idx / BK; kk = idx % BK; }
+        const int64_t n = n0 + 2 * pp, k = k0 + kk;
+        const bool kin = k < k_end;
+        const float2 b0 = split((n < g.N && kin) ? B[k * g.sBk + n * g.sBn] : 0.0);
+        const float2 b1 = split((n + 1 < g.N && kin) ? B[k * g.sBk + (n + 1) * g.sBn] : 0.0);
+        Bs[kk][pp] = make_ulonglong2(pk2(b0.x, b1.x), pk2(b0.y, b1.y));
+        Bn[kk][pp] = pk2(-b0.x, -b1.x);
+      }
     }
     __syncthreads();
-#pragma unroll 4
+#pragma unroll 2
     for (int kk = 0; kk < BK; ++kk) {
-      float2 a[TM], b[TN];
+      ulonglong2 a[TM], b[JP];
+      f32x2 nb[JP];
 #pragma unroll
       for (int i = 0; i < TM; ++i) a[i] = As[kk][ty + 16 * i];
 #pragma unroll
-      for (int j = 0; j < TN; ++j) b[j] = Bs[kk][tx + 16 * j];
+      for (int j = 0; j < JP; ++j) {
+        b[j] = Bs[kk][tx + 16 * j];
+        nb[j] = Bn[kk][tx + 16 * j];
+      }
 #pragma unroll
       for (int i = 0; i < TM; ++i)
 #pragma unroll
-        for (int j = 0; j < TN; ++j) {
-          // error-free transforms with explicit rounding (no compiler FMA contraction)
-          const float ph = __fmul_rn(a[i].x, b[j].x);
-          float pl = __fmaf_rn(a[i].x, b[j].x, -ph);
-          pl = __fmaf_rn(a[i].x, b[j].y, pl);
-          pl = __fmaf_rn(a[i].y, b[j].x, pl);
-          const float s = __fadd_rn(ah[i][j], ph);
-          const float z = __fsub_rn(s, ah[i][j]);
-          const float e = __fadd_rn(__fsub_rn(ah[i][j], __fsub_rn(s, z)), __fsub_rn(ph, z));
-          al[i][j] = __fadd_rn(al[i][j], __fadd_rn(e, pl));
+        for (int j = 0; j < JP; ++j) {
+          const f32x2 nph = mul2(a[i].x, nb[j]);      // -RN(ah bh)
+          f32x2 pl = fma2(a[i].x, b[j].x, nph);       // ah bh - ph, exact
+          pl = fma2(a[i].x, b[j].y, pl);
+          pl = fma2(a[i].y, b[j].x, pl);
+          const f32x2 s = sub2(ah[i][j], nph);        // two-sum (acc, ph), written with -ph
+          const f32x2 z = sub2(s, ah[i][j]);
+          const f32x2 e = sub2(sub2(ah[i][j], sub2(s, z)), add2(nph, z));
+          al[i][j] = add2(al[i][j], add2(e, pl));
           ah[i][j] = s;
         }
     }
 #pragma unroll
     for (int i = 0; i < TM; ++i)
 #pragma unroll
-      for (int j = 0; j < TN; ++j) {
-        const float s = __fadd_rn(ah[i][j], al[i][j]);
-        al[i][j] = __fsub_rn(al[i][j], __fsub_rn(s, ah[i][j]));
+      for (int j = 0; j < JP; ++j) {
+        const f32x2 s = add2(ah[i][j], al[i][j]);
+        al[i][j] = sub2(al[i][j], sub2(s, ah[i][j]));
         ah[i][j] = s;
       }
   }
 #pragma unroll
   for (int i = 0; i < TM; ++i)
 #pragma unroll
-    for (int j = 0; j < TN; ++j) {
-      const int64_t m = m0 + ty + 16 * i, n = n0 + tx + 16 * j;
-      if (m < g.M && n < g.N) {
-        const double acc = (double)ah[i][j] + (double)al[i][j];
-        if (g.splits == 1) {
-          double* c = g.C + bz * g.sCb + m * g.sCm + n * g.sCn;
-          *c = g.beta == 0.0 ? g.alpha * acc : fma(g.alpha, acc, g.beta * *c);
-        } else {
-          g.part[((bz * g.splits + sp) * g.M + m) * g.N + n] = acc;
+    for (int j = 0; j < JP; ++j) {
+      const int64_t m = m0 + ty + 16 * i, n = n0 + 2 * (tx + 16 * j);
+      const float2 h = upk2(ah[i][j]), l = upk2(al[i][j]);
+      const double acc[2] = {(double)h.x + (double)l.x, (double)h.y + (double)l.y};
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        if (m < g.M && n + c < g.N) {
+          if (g.splits == 1) {
+            double* cp = g.C + bz * g.sCb + m * g.sCm + (n + c) * g.sCn;
+            *cp = g.beta == 0.0 ? g.alpha * acc[c] : fma(g.alpha, acc[c], g.beta * *cp);
+          } else {
+            g.part[((bz * g.splits + sp) * g.M + m) * g.N + n + c] = acc[c];
+          }
         }
       }
     }
@@ -161,11 +216,11 @@ int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t ba
   g.sCm = sC[0]; g.sCn = sC[1]; g.sCb = sC[2];
   g.alpha = alpha;
   g.beta = beta;
-  // tile shape: the one of 64x64, 128x32, 32x128 that pads C least (a side
-  // as short as nocc would waste half of a 64-wide tile)
+  // tile shape: the one of 64x64, 128x32, 32x128, 32x160 that pads C least
+  // (a side as short as nocc would waste half of a 64-wide tile)
   int tm = 4, tn = 4;
   {
-    const int cand[3][2] = {{4, 4}, {8, 2}, {2, 8}};
+    const int cand[4][2] = {{4, 4}, {8, 2}, {2, 8}, {2, 10}};
     int64_t best = -1;
     for (const auto& c : cand) {
       const int64_t pad = fricc_cdiv(M, 16 * c[0]) * 16 * c[0] * fricc_cdiv(N, 16 * c[1]) * 16 * c[1];
@@ -191,7 +246,8 @@ int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t ba
   }
   dim3 grid((unsigned)fricc_cdiv(N, BN), (unsigned)fricc_cdiv(M, BM), (unsigned)(batch * splits));
   if (tm == 8) k_gemm_df<8, 2><<<grid, NT, 0, st>>>(g);
-  else if (tm == 2) k_gemm_df<2, 8><<<grid, NT, 0, st>>>(g);
+  else if (tn == 8) k_gemm_df<2, 8><<<grid, NT, 0, st>>>(g);
+  else if (tn == 10) k_gemm_df<2, 10><<<grid, NT, 0, st>>>(g);
   else k_gemm_df<4, 4><<<grid, NT, 0, st>>>(g);
   fricc_note_launch();
   if (splits > 1) {
