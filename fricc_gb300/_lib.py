@@ -14,7 +14,7 @@ LIB_PATH = os.path.join(_HERE, "_lib", "libfricc_gb300.so")
 
 FRICC_OK = 0
 STATUS_NAMES = {1: "FRICC_ERR_ARG", 2: "FRICC_ERR_TERM", 3: "FRICC_ERR_P_GT_ONE", 4: "FRICC_ERR_CUDA",
-                5: "FRICC_ERR_TIMEOUT", 6: "FRICC_ERR_INDEX", 7: "FRICC_ERR_UNSUPPORTED"}
+                5: "FRICC_ERR_TIMEOUT", 6: "FRICC_ERR_INDEX", 7: "FRICC_ERR_UNSUPPORTED", 8: "FRICC_ERR_PIVOTAL"}
 COMPRESSION = {"fri": 0, "largest": 1}
 SAMPLING = {"systematic": 0, "pivotal": 1}
 
@@ -23,12 +23,16 @@ _i64 = ctypes.c_int64
 _i64p = ctypes.POINTER(ctypes.c_int64)
 _dp = ctypes.c_void_p
 _vp = ctypes.c_void_p
+_u32p = ctypes.POINTER(ctypes.c_uint32)
 SIGNATURES = [
     ("fricc_version", ctypes.c_int, []),
     ("fricc_last_error", ctypes.c_char_p, []),
     ("fricc_sp_create", ctypes.c_int, [_dp, _i64p, _i64, ctypes.c_int, ctypes.c_int, ctypes.c_double, _vp,
                                        ctypes.POINTER(_vp)]),
     ("fricc_sp_recompress", ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, ctypes.c_double, _vp]),
+    ("fricc_sp_create_pivotal", ctypes.c_int, [_dp, _i64p, _i64, _u32p, _vp, ctypes.POINTER(_vp), _i64p]),
+    ("fricc_sp_recompress_pivotal", ctypes.c_int, [_vp, _dp, _u32p, _vp, _i64p]),
+    ("fricc_sp_status", ctypes.c_int, [_vp]),
     ("fricc_sp_create_empty", ctypes.c_int, [_i64p, _i64, _vp, ctypes.POINTER(_vp)]),
     ("fricc_sp_destroy", ctypes.c_int, [_vp]),
     ("fricc_sp_info", ctypes.c_int, [_vp, _i64p, _i64p, _i64p]),
@@ -45,6 +49,8 @@ SIGNATURES = [
                                       ctypes.c_double, _vp]),
     ("fricc_contract_flops", ctypes.c_double, [ctypes.c_char_p, _vp]),
     ("fricc_compress", ctypes.c_int, [_dp, _i64, _i64, ctypes.c_int, ctypes.c_double, _dp, _dp, _i64p, _vp]),
+    ("fricc_compress_pivotal", ctypes.c_int, [_dp, _i64, _i64, _u32p, _dp, _dp, _i64p, _i64p, _vp]),
+    ("fricc_glibc_uniforms", ctypes.c_int, [_u32p, _i64, _dp, _vp]),
     ("fricc_seq_cumsum", ctypes.c_int, [_dp, _i64, _dp, _vp]),
     ("fricc_seq_cumsum_noalloc", ctypes.c_int, [_dp, _i64, _dp, _vp]),
     ("fricc_launch_count", ctypes.c_longlong, []),
@@ -95,3 +101,17 @@ def check(status: int) -> None:
 
 def i64arr(vals):
     return (ctypes.c_int64 * len(vals))(*[int(v) for v in vals])
+
+
+def hist_arg(rng):
+    """(ctypes uint32[31] or None, writeback) for a draw source: a GlibcRand-like
+    object with history()/set_history() lends its history (the device draws
+    from it and hands it back); anything else (None, libc's rand) means the
+    process's own rand(), as the reference draws."""
+    if rng is not None and hasattr(rng, "history") and hasattr(rng, "set_history"):
+        h = (ctypes.c_uint32 * 31)(*[int(v) for v in rng.history()])
+
+        def writeback():
+            rng.set_history([h[i] for i in range(31)])
+        return h, writeback
+    return None, (lambda: None)

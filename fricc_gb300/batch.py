@@ -131,8 +131,9 @@ def request_stream(n: int, rate: float, seed: int = 0, nocc=(5, 30), ratio=(4.0,
 
 def footprint_bytes(o: int, v: int) -> int:
     """HBM a resident solve needs: integral blocks and the layouts derived from
-    them (vvvv twice, ovvv six times), amplitudes and work arrays (~16 o^2v^2)."""
-    return 8 * (2 * v**4 + 7 * o * v**3 + 16 * o * o * v * v + 4 * o**4 + 8 * o**3 * v)
+    them (vvvv and its float-pair form, ovvv in nine layouts or forms),
+    amplitudes and work arrays (~16 o^2v^2)."""
+    return 8 * (2 * v**4 + 9 * o * v**3 + 16 * o * o * v * v + 4 * o**4 + 8 * o**3 * v)
 
 
 class SolveServer:

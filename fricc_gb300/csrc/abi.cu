@@ -10,7 +10,12 @@
 #include "sparse.cuh"
 
 int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, double rn, cudaStream_t st, int64_t* flat,
-                          double* vals, int64_t* n_largest);
+                          double* vals, int64_t* n_largest, unsigned* glibc_hist, int64_t* n_draws,
+                          unsigned long long* meta = nullptr);
+int fricc_unpack_async(const int64_t* flat, int64_t m, const int64_t dims[4], int* slots, unsigned long long* meta,
+                       cudaStream_t st);
+int fricc_dev_status(unsigned e);
+int fricc_glibc_uniforms_device(unsigned* hist, int64_t k, double* out, cudaStream_t st);
 int fricc_seq_cumsum_device(const double* x, int64_t n, double* out, cudaStream_t st);
 int fricc_unpack_device(const int64_t* flat, int64_t m, const int64_t dims[4], int* slots, cudaStream_t st);
 int fricc_contract_device(const char* term, const double* W, const int64_t Wd[4], const int64_t Ws[4], FriccSparse* T,
@@ -108,6 +113,8 @@ void fricc_free(void* p, cudaStream_t s) {
 static cudaStream_t as_stream(void* s) { return reinterpret_cast<cudaStream_t>(s); }
 
 static void free_sparse_arrays(FriccSparse* T, cudaStream_t st) {
+  fricc_free(T->meta, st);
+  T->meta = nullptr;
   fricc_free(T->flat, st);
   fricc_free(T->vals, st);
   fricc_free(T->slots, st);
@@ -173,6 +180,53 @@ int fricc_prof_read(double* ms, long long* launches, double* flops) {
 
 const char* fricc_last_error(void) { return g_err; }
 
+// Read back the status block of an asynchronous compression (blocking).
+static int settle(const fricc_sparse* Tc) {
+  fricc_sparse* T = const_cast<fricc_sparse*>(Tc);
+  if (!T->pending) return T->status;
+  unsigned long long h[2] = {0, 0};
+  cudaError_t e = cudaMemcpyAsync(h, T->meta, sizeof(h), cudaMemcpyDeviceToHost, T->owner_stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(T->owner_stream);
+  if (e != cudaSuccess) return fricc_cuda_fail(e, "compression status", __FILE__, __LINE__);
+  T->pending = false;
+  T->n_largest = (int64_t)h[0];
+  T->status = fricc_dev_status((unsigned)h[1]);
+  return T->status;
+}
+
+// mode: 0 fri systematic (rn), 1 largest, 2 fri pivotal (hist / rand()).
+// Modes 0 and 1 only enqueue work: |D| and any error are read back by the
+// next blocking call on the handle (settle).
+static int recompress(fricc_sparse* T, const double* t2, int mode, double rn, unsigned* hist, int64_t* n_draws,
+                      void* stream) {
+  cudaStream_t st = as_stream(stream);
+  drop_bucketings(T, st);
+  const int64_t n = T->dims[0] * T->dims[1] * T->dims[2] * T->dims[3];
+  T->owner_stream = st;
+  T->pending = false;
+  T->status = FRICC_OK;
+  FRICC_CUDA(cudaMemsetAsync(T->meta, 0, 2 * sizeof(unsigned long long), st));
+  if (mode == 2) {
+    int64_t nd = 0;
+    int rc = fricc_compress_device(t2, n, T->m, mode, rn, st, T->flat, T->vals, &nd, hist, n_draws);
+    if (rc) return rc;
+    T->n_largest = nd;
+    return fricc_unpack_device(T->flat, T->m, T->dims, T->slots, st);
+  }
+  int rc = fricc_compress_device(t2, n, T->m, mode, rn, st, T->flat, T->vals, nullptr, hist, n_draws, T->meta);
+  if (!rc) rc = fricc_unpack_async(T->flat, T->m, T->dims, T->slots, T->meta, st);
+  if (!rc) T->pending = true;
+  return rc;
+}
+
+int fricc_sp_status(const fricc_sparse* T) {
+  if (!T) {
+    fricc_set_error("sp_status: null handle");
+    return FRICC_ERR_ARG;
+  }
+  return settle(T);
+}
+
 int fricc_sp_recompress(fricc_sparse* T, const double* t2, int compression, int sampling, double rn, void* stream) {
   if (!T || !t2) {
     fricc_set_error("sp_recompress: null argument");
@@ -182,24 +236,54 @@ int fricc_sp_recompress(fricc_sparse* T, const double* t2, int compression, int 
     fricc_set_error("The compression method you chose isn't supported: compression must be 'largest' or 'fri'");
     return FRICC_ERR_ARG;
   }
-  if (compression == FRICC_COMPRESSION_FRI && sampling != FRICC_SAMPLING_SYSTEMATIC) {
-    fricc_set_error("sampling_method 'pivotal' is not implemented on the GPU path (use 'systematic')");
-    return FRICC_ERR_UNSUPPORTED;
+  if (compression == FRICC_COMPRESSION_FRI && sampling == FRICC_SAMPLING_PIVOTAL) {
+    // pivotal draws one uniform per element: its entry points take the stream
+    fricc_set_error("pivotal sampling draws its uniforms itself: use fricc_sp_recompress_pivotal");
+    return FRICC_ERR_ARG;
   }
-  cudaStream_t st = as_stream(stream);
-  drop_bucketings(T, st);
-  const int64_t n = T->dims[0] * T->dims[1] * T->dims[2] * T->dims[3];
-  int64_t nd = 0;
-  int rc = fricc_compress_device(t2, n, T->m, compression == FRICC_COMPRESSION_LARGEST ? 1 : 0, rn, st, T->flat,
-                                 T->vals, &nd);
-  if (rc) return rc;
-  T->n_largest = nd;
-  T->owner_stream = st;
-  return fricc_unpack_device(T->flat, T->m, T->dims, T->slots, st);
+  if (compression == FRICC_COMPRESSION_FRI && sampling != FRICC_SAMPLING_SYSTEMATIC) {
+    fricc_set_error("sampling_method must be 'pivotal' or 'systematic'");
+    return FRICC_ERR_ARG;
+  }
+  return recompress(T, t2, compression == FRICC_COMPRESSION_LARGEST ? 1 : 0, rn, nullptr, nullptr, stream);
+}
+
+int fricc_sp_recompress_pivotal(fricc_sparse* T, const double* t2, uint32_t* glibc_hist, void* stream,
+                                int64_t* n_draws) {
+  if (!T || !t2) {
+    fricc_set_error("sp_recompress_pivotal: null argument");
+    return FRICC_ERR_ARG;
+  }
+  return recompress(T, t2, 2, 0.0, glibc_hist, n_draws, stream);
+}
+
+static int create(const double* t2, const int64_t dims[4], int64_t m, int mode, double rn, unsigned* hist,
+                  int64_t* n_draws, void* stream, fricc_sparse** out);
+
+int fricc_sp_create_pivotal(const double* t2, const int64_t dims[4], int64_t m, uint32_t* glibc_hist, void* stream,
+                            fricc_sparse** out, int64_t* n_draws) {
+  return create(t2, dims, m, 2, 0.0, glibc_hist, n_draws, stream, out);
 }
 
 int fricc_sp_create(const double* t2, const int64_t dims[4], int64_t m, int compression, int sampling, double rn,
                     void* stream, fricc_sparse** out) {
+  if (compression != FRICC_COMPRESSION_FRI && compression != FRICC_COMPRESSION_LARGEST) {
+    fricc_set_error("The compression method you chose isn't supported: compression must be 'largest' or 'fri'");
+    return FRICC_ERR_ARG;
+  }
+  if (compression == FRICC_COMPRESSION_FRI && sampling == FRICC_SAMPLING_PIVOTAL) {
+    fricc_set_error("pivotal sampling draws its uniforms itself: use fricc_sp_create_pivotal");
+    return FRICC_ERR_ARG;
+  }
+  if (compression == FRICC_COMPRESSION_FRI && sampling != FRICC_SAMPLING_SYSTEMATIC) {
+    fricc_set_error("sampling_method must be 'pivotal' or 'systematic'");
+    return FRICC_ERR_ARG;
+  }
+  return create(t2, dims, m, compression == FRICC_COMPRESSION_LARGEST ? 1 : 0, rn, nullptr, nullptr, stream, out);
+}
+
+static int create(const double* t2, const int64_t dims[4], int64_t m, int mode, double rn, unsigned* hist,
+                  int64_t* n_draws, void* stream, fricc_sparse** out) {
   if (!out || !t2 || bad_dims(dims)) {
     fricc_set_error("sp_create: null pointer or non-positive dims");
     return FRICC_ERR_ARG;
@@ -219,7 +303,8 @@ int fricc_sp_create(const double* t2, const int64_t dims[4], int64_t m, int comp
   int rc = fricc_alloc_t(&T->flat, m, st);
   if (!rc) rc = fricc_alloc_t(&T->vals, m, st);
   if (!rc) rc = fricc_alloc_t(&T->slots, 4 * m, st);
-  if (!rc) rc = fricc_sp_recompress(T, t2, compression, sampling, rn, stream);
+  if (!rc) rc = fricc_alloc_t(&T->meta, 2, st);
+  if (!rc) rc = recompress(T, t2, mode, rn, hist, n_draws, stream);
   if (rc) {
     free_sparse_arrays(T, st);
     cudaStreamSynchronize(st);
@@ -243,7 +328,9 @@ int fricc_sp_create_empty(const int64_t dims[4], int64_t nnz, void* stream, fric
   int rc = fricc_alloc_t(&T->flat, nnz, st);
   if (!rc) rc = fricc_alloc_t(&T->vals, nnz, st);
   if (!rc) rc = fricc_alloc_t(&T->slots, 4 * nnz, st);
+  if (!rc) rc = fricc_alloc_t(&T->meta, 2, st);
   if (!rc) {
+    cudaMemsetAsync(T->meta, 0, 2 * sizeof(unsigned long long), st);
     cudaMemsetAsync(T->flat, 0, nnz * sizeof(int64_t), st);
     cudaMemsetAsync(T->vals, 0, nnz * sizeof(double), st);
     cudaMemsetAsync(T->slots, 0, 4 * nnz * sizeof(int), st);
@@ -272,6 +359,8 @@ int fricc_sp_info(const fricc_sparse* T, int64_t dims[4], int64_t* m, int64_t* n
     fricc_set_error("sp_info: null handle");
     return FRICC_ERR_ARG;
   }
+  const int rc = settle(T);
+  if (rc) return rc;
   if (dims)
     for (int k = 0; k < 4; ++k) dims[k] = T->dims[k];
   if (m) *m = T->m;
@@ -284,6 +373,8 @@ int fricc_sp_get(const fricc_sparse* T, int64_t mi, int64_t idx[4], double* valu
     fricc_set_error("get_element: index %lld out of range", (long long)mi);
     return FRICC_ERR_ARG;
   }
+  const int rc = settle(T);
+  if (rc) return rc;
   int s[4];
   double v = 0.0;
   cudaError_t e = cudaStreamSynchronize(T->owner_stream);
@@ -301,6 +392,8 @@ int fricc_sp_export(const fricc_sparse* T, int64_t* flat_host, double* vals_host
     fricc_set_error("sp_export: null handle");
     return FRICC_ERR_ARG;
   }
+  const int rc = settle(T);  // also orders the copies after the compression
+  if (rc) return rc;
   cudaStream_t st = as_stream(stream);
   if (flat_host) FRICC_CUDA(cudaMemcpyAsync(flat_host, T->flat, T->m * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
   if (vals_host) FRICC_CUDA(cudaMemcpyAsync(vals_host, T->vals, T->m * sizeof(double), cudaMemcpyDeviceToHost, st));
@@ -382,7 +475,20 @@ int fricc_compress(const double* x, int64_t n, int64_t m, int compression, doubl
     return FRICC_ERR_ARG;
   }
   return fricc_compress_device(x, n, m, compression == FRICC_COMPRESSION_LARGEST ? 1 : 0, rn, as_stream(stream), flat,
-                               vals, n_largest);
+                               vals, n_largest, nullptr, nullptr);
+}
+
+int fricc_compress_pivotal(const double* x, int64_t n, int64_t m, uint32_t* glibc_hist, int64_t* flat, double* vals,
+                           int64_t* n_largest, int64_t* n_draws, void* stream) {
+  if (!x || !flat || !vals) {
+    fricc_set_error("compress_pivotal: null argument");
+    return FRICC_ERR_ARG;
+  }
+  return fricc_compress_device(x, n, m, 2, 0.0, as_stream(stream), flat, vals, n_largest, glibc_hist, n_draws);
+}
+
+int fricc_glibc_uniforms(uint32_t* hist, int64_t k, double* out, void* stream) {
+  return fricc_glibc_uniforms_device(hist, k, out, as_stream(stream));
 }
 
 static int energy_update(const double* t1num, const double* t2num, const double* eia, const double* fov,

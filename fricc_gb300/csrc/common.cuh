@@ -12,6 +12,63 @@
 #define FRICC_DEV_P_GT_ONE 1u
 #define FRICC_DEV_TIMEOUT 2u
 #define FRICC_DEV_INDEX 4u
+#define FRICC_DEV_PIVOTAL 8u
+
+// ---------------------------------------------------------------------------
+// Split an FP64 value into a float pair hi + lo (|d - hi - lo| < 2^-47 |d|)
+// with integer operations only.  GB300's FP64 unit (which also runs the
+// double<->float conversions) issues 1/64 as fast as the FP32 lanes, so a
+// conversion-based split (RN(d), RN(d - RN(d))) staged for every operand
+// tile can cost as much as the FP32-pair arithmetic it feeds.  For
+// 2^-74 <= |d| < 2^128 the pair is read off the bit pattern: hi keeps the
+// top 24 significand bits (truncated), lo is the remaining 29-bit field
+// rounded (half up) to 24 bits; both are then normal floats.  Zeros map to
+// (d, 0); anything else (tiny, huge, inf, NaN) takes the conversion path.
+__device__ __forceinline__ float2 split_f2_conv(double d) {
+  const float h = __double2float_rn(d);
+  return make_float2(h, __double2float_rn(d - (double)h));
+}
+
+__device__ __forceinline__ float2 split_f2_bits(double d) {
+  const unsigned long long u = (unsigned long long)__double_as_longlong(d);
+  const int E = (int)((u >> 52) & 0x7ffu);
+  const unsigned sgn = (unsigned)(u >> 32) & 0x80000000u;
+  if (E >= 1023 - 74 && E <= 1023 + 127) {
+    const unsigned long long M = u & 0xfffffffffffffull;
+    const unsigned hib = sgn | ((unsigned)(E - 1023 + 127) << 23) | (unsigned)(M >> 29);
+    const unsigned rest = (unsigned)(M & 0x1fffffffu);
+    unsigned lob = sgn;  // +-0 when the low field is empty
+    if (rest) {
+      const int p = 31 - __clz((int)rest);  // leading bit, 0..28
+      const int sh = p - 23;
+      unsigned m;                           // 24-bit significand incl. the leading 1, or 2^24 after a carry
+      if (sh <= 0) m = rest << (-sh);
+      else m = (rest >> sh) + ((rest >> (sh - 1)) & 1u);
+      const int ef = E - 1023 - 52 + p + 127;  // 1..230 on this path
+      lob = sgn | (((unsigned)(ef - 1) << 23) + m);
+    }
+    return make_float2(__uint_as_float(hib), __uint_as_float(lob));
+  }
+  if ((u << 1) == 0ull) return make_float2(__uint_as_float(sgn), 0.0f);
+  return split_f2_conv(d);
+}
+
+// float -> double, exactly, with integer operations (the conversion
+// instruction runs on the slow FP64 unit); zeros, subnormals, inf and NaN
+// take the conversion path.
+__device__ __forceinline__ double f2d_bits(float f) {
+  const unsigned b = __float_as_uint(f);
+  const unsigned e = (b >> 23) & 0xffu;
+  const unsigned long long sgn = (unsigned long long)(b & 0x80000000u) << 32;
+  if (e != 0u && e != 255u)
+    return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896u) << 52) |
+                                            ((unsigned long long)(b & 0x7fffffu) << 29)));
+  if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sgn);
+  return (double)f;
+}
+
+// hi + lo of a float pair, rounded once to FP64
+__device__ __forceinline__ double pair_to_f64(float hi, float lo) { return f2d_bits(hi) + f2d_bits(lo); }
 
 void fricc_set_error(const char* fmt, ...);
 int fricc_cuda_fail(cudaError_t e, const char* what, const char* file, int line);

@@ -20,6 +20,7 @@
 //      (:136, :147-157); unmatched samples keep index 0, as in the reference;
 //   6. output D in sorted order then S ascending, values x_D and x_S/p_S.
 #include <cmath>
+#include <cstdlib>
 #include <vector>
 
 #include "exactsum.cuh"
@@ -60,6 +61,11 @@ struct Ctl {
   double mprime;      // (double)(m - |D|)
   int sample;         // 1: R > 0 and finite, so samples can land in intervals
   double rn;          // the uniform draw
+  // pivotal sampling
+  int64_t jend;       // last element the sampler visits (it stops once m' indices are out)
+  int64_t npush;      // indices emitted up to jend (chain), then in total (final)
+  int64_t plast;      // the pivot after jend
+  int broke;          // 1: the sampler stopped early with m' indices
 };
 
 __device__ __forceinline__ unsigned long long ld_acquire(const unsigned long long* p) {
@@ -277,7 +283,264 @@ __global__ void k_unpack(const int64_t* __restrict__ flat, int64_t m, int64_t d0
   }
 }
 
+// ---------------------------------------------------------------------------
+// Pivotal sampling (src/fri_utils.cpp:63-127).  The sampler carries a weight
+// a = p_0; for j = 1, 2, ...: a += p_j and one uniform rn_j is drawn; below 1
+// the pivot i moves to j if rn_j < p_j / a; at or above 1, a -= 1 and one
+// index is emitted: the pivot (which then moves to j) if
+// rn_j < (1 - p_j) / (1 - a), else j; it stops once m' indices are out.
+//
+// Only the carried weight is a true recurrence (sequential FP64 with a
+// wrap), and it does not depend on the draws, nor does which elements emit.
+// So: (1) one warp walks the weight and records a_j and the wrap flag for
+// every element, which fixes where the sampler stops and how many draws it
+// consumes; (2) the draws arrive; (3) every decision is independent given
+// a_j, p_j and rn_j; (4) the pivot an element emits is the last "take"
+// before it, a max-scan; its slot in S is the count of emits before it, a
+// sum-scan.  Per-element codes: bit 0 the pivot moves here, bit 1 the
+// element emits, bit 2 it emits the pivot.
+constexpr unsigned char PV_TAKE = 1, PV_EMIT = 2, PV_PIVOT = 4;
+
+__global__ void k_pvec(GenP gp, int64_t n, double* __restrict__ P, unsigned* err) {
+  bool bad = false;
+  for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
+    const double p = gp.value(i);
+    P[i] = p;
+    bad |= p > 1.0;
+  }
+  if (bad) atomicOr(err, FRICC_DEV_P_GT_ONE);
+}
+
+// One warp.  Lane t of a batch of 32 elements keeps a_j and the wrap flag
+// of element j0 + t; every lane walks the same chain (the p_j come in by
+// shuffle, the next batch's are loaded while this one runs).
+__global__ void __launch_bounds__(32) k_piv_chain(const double* __restrict__ P, int64_t n, Ctl* c,
+                                                  double* __restrict__ A, unsigned char* __restrict__ code) {
+  const int lane = threadIdx.x;
+  const int64_t mp = c->mp;
+  double a = P[0];
+  if (lane == 0) {
+    A[0] = a;
+    code[0] = 0;
+  }
+  int64_t cnt = 0, jend = n - 1;
+  int broke = 0;
+  double pn = 1 + lane < n ? P[1 + lane] : 0.0;
+  for (int64_t j0 = 1; j0 < n; j0 += 32) {
+    const double pj = pn;
+    const int64_t jn = j0 + 32 + lane;
+    pn = jn < n ? P[jn] : 0.0;
+    double myA = 0.0;
+    bool myW = false;
+#pragma unroll
+    for (int t = 0; t < 32; ++t) {
+      const double pt = __shfl_sync(0xffffffffu, pj, t);
+      const double sum = __dadd_rn(a, pt);
+      const bool w = !(sum < 1.0);
+      a = w ? __dsub_rn(sum, 1.0) : sum;
+      if (lane == t) {
+        myA = a;
+        myW = w;
+      }
+    }
+    const int64_t j = j0 + lane;
+    const bool valid = j < n;
+    const unsigned wm = __ballot_sync(0xffffffffu, myW && valid);
+    // the first element of this batch after which exactly m' indices are out
+    int stop = -1;
+    if (mp == 0) {
+      if (j0 == 1 && !(wm & 1u)) stop = 0;
+    } else if (cnt < mp && cnt + __popc(wm) >= mp) {
+      int64_t r = mp - cnt;
+      for (int b = 0; b < 32; ++b)
+        if (((wm >> b) & 1u) && --r == 0) {
+          stop = b;
+          break;
+        }
+    }
+    if (valid && (stop < 0 || lane <= stop)) {
+      A[j] = myA;
+      code[j] = myW ? PV_EMIT : 0;
+    }
+    if (stop >= 0) {
+      jend = j0 + stop;
+      broke = 1;
+      cnt = mp;
+      break;
+    }
+    cnt += __popc(wm);
+  }
+  if (lane == 0) {
+    c->jend = jend;
+    c->npush = cnt;
+    c->broke = broke;
+  }
+}
+
+// decisions for j in [1, jend], with rn_j = R[j-1]
+__global__ void k_piv_decide(const double* __restrict__ P, const double* __restrict__ A,
+                             unsigned char* __restrict__ code, const double* __restrict__ R, const Ctl* c,
+                             unsigned* err) {
+  const int64_t jend = c->jend;
+  bool bad = false;
+  for (int64_t j = 1 + (int64_t)blockIdx.x * blockDim.x + threadIdx.x; j <= jend;
+       j += (int64_t)gridDim.x * blockDim.x) {
+    const double rn = R[j - 1], p = P[j], a = A[j];
+    unsigned char cd = code[j];
+    if (!(cd & PV_EMIT)) {
+      if (rn < __ddiv_rn(p, a)) cd |= PV_TAKE;
+    } else {
+      const double pa = __ddiv_rn(__dsub_rn(1.0, p), __dsub_rn(1.0, a));
+      bad |= pa > 1.0 || pa < 0.0;
+      if (rn < pa) cd |= PV_TAKE | PV_PIVOT;
+    }
+    code[j] = cd;
+  }
+  if (bad) atomicOr(err, FRICC_DEV_PIVOTAL);
+}
+
+constexpr int PV_NT = 256, PV_IT = 16, PV_TILE = PV_NT * PV_IT;
+
+// block-wide exclusive max of int64 (identity -1), thread order; smem >= 33
+__device__ __forceinline__ int64_t block_excl_max(int64_t v, int64_t* smem, int64_t* total) {
+  int64_t incl = v;
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int64_t w = __shfl_up_sync(0xffffffffu, incl, o);
+    if ((int)lane_id() >= o && w > incl) incl = w;
+  }
+  const int64_t excl_w = __shfl_up_sync(0xffffffffu, incl, 1);
+  const int nw = blockDim.x >> 5;
+  __syncthreads();
+  if (lane_id() == 31) smem[warp_id()] = incl;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    int64_t run = -1;
+    for (int w = 0; w < nw; ++w) {
+      const int64_t t = smem[w];
+      smem[w] = run;
+      run = t > run ? t : run;
+    }
+    smem[32] = run;
+  }
+  __syncthreads();
+  int64_t r = smem[warp_id()];
+  if (lane_id() > 0 && excl_w > r) r = excl_w;
+  *total = smem[32];
+  __syncthreads();
+  return r;
+}
+
+// per tile: the last take and the number of emits among j in [1, jend]
+__global__ void __launch_bounds__(PV_NT) k_piv_tiles(const unsigned char* __restrict__ code, const Ctl* c,
+                                                     int64_t* __restrict__ tlast, int64_t* __restrict__ tcnt) {
+  __shared__ int64_t sm[33];
+  const int64_t jend = c->jend;
+  const int64_t j0 = (int64_t)blockIdx.x * PV_TILE + (int64_t)threadIdx.x * PV_IT;
+  int64_t last = -1, cnt = 0;
+#pragma unroll
+  for (int k = 0; k < PV_IT; ++k) {
+    const int64_t j = j0 + k;
+    if (j >= 1 && j <= jend) {
+      const unsigned char cd = code[j];
+      if (cd & PV_TAKE) last = j;
+      cnt += (cd & PV_EMIT) ? 1 : 0;
+    }
+  }
+  int64_t tot_last, tot_cnt;
+  block_excl_max(last, sm, &tot_last);
+  block_excl_sum(cnt, sm, &tot_cnt);
+  if (threadIdx.x == 0) {
+    tlast[blockIdx.x] = tot_last;
+    tcnt[blockIdx.x] = tot_cnt;
+  }
+}
+
+// exclusive scans over tiles, in place; the pivot starts at index 0
+__global__ void __launch_bounds__(1024) k_piv_carry(int64_t* __restrict__ tlast, int64_t* __restrict__ tcnt,
+                                                    int64_t ntile, Ctl* c) {
+  __shared__ int64_t sm[33];
+  int64_t run_last = 0, run_cnt = 0;
+  for (int64_t b = 0; b < ntile; b += 1024) {
+    const int64_t t = b + threadIdx.x;
+    const int64_t l = t < ntile ? tlast[t] : -1, k = t < ntile ? tcnt[t] : 0;
+    int64_t tl, tk;
+    int64_t el = block_excl_max(l, sm, &tl);
+    const int64_t ek = block_excl_sum(k, sm, &tk);
+    el = el > run_last ? el : run_last;
+    if (t < ntile) {
+      tlast[t] = el;
+      tcnt[t] = run_cnt + ek;
+    }
+    run_last = tl > run_last ? tl : run_last;
+    run_cnt += tk;
+  }
+  if (threadIdx.x == 0) {
+    c->plast = run_last;
+    c->npush = run_cnt;
+  }
+}
+
+// S[slot] for every emit with slot < m'
+__global__ void __launch_bounds__(PV_NT) k_piv_emit(const unsigned char* __restrict__ code,
+                                                    const int64_t* __restrict__ clast,
+                                                    const int64_t* __restrict__ ccnt, const Ctl* c,
+                                                    unsigned* __restrict__ S) {
+  __shared__ int64_t sm[33];
+  const int64_t jend = c->jend, mp = c->mp;
+  const int64_t j0 = (int64_t)blockIdx.x * PV_TILE + (int64_t)threadIdx.x * PV_IT;
+  unsigned char cd[PV_IT];
+  int64_t last = -1, cnt = 0;
+#pragma unroll
+  for (int k = 0; k < PV_IT; ++k) {
+    const int64_t j = j0 + k;
+    cd[k] = (j >= 1 && j <= jend) ? code[j] : 0;
+    if (cd[k] & PV_TAKE) last = j;
+    cnt += (cd[k] & PV_EMIT) ? 1 : 0;
+  }
+  int64_t tl, tk;
+  int64_t piv = block_excl_max(last, sm, &tl);
+  int64_t slot = block_excl_sum(cnt, sm, &tk);
+  const int64_t cl = clast[blockIdx.x];
+  piv = piv > cl ? piv : cl;
+  slot += ccnt[blockIdx.x];
+#pragma unroll
+  for (int k = 0; k < PV_IT; ++k) {
+    const int64_t j = j0 + k;
+    if (cd[k] & PV_EMIT) {
+      if (slot < mp) S[slot] = (unsigned)((cd[k] & PV_PIVOT) ? piv : j);
+      ++slot;
+    }
+    if (cd[k] & PV_TAKE) piv = j;
+  }
+}
+
+// the end of the walk: a sampler that visited every element emits its pivot
+// when |a - 1| < 1e-5; the count must come out at m'
+__global__ void k_piv_final(const double* __restrict__ A, int64_t n, Ctl* c, unsigned* __restrict__ S,
+                            unsigned* err) {
+  int64_t np = c->npush;
+  bool bad = false;
+  if (!c->broke && n >= 2) {
+    if (fabs(__dsub_rn(A[n - 1], 1.0)) < 1e-5) {
+      if (np < c->mp) S[np] = (unsigned)c->plast;
+      ++np;
+    } else {
+      bad = true;
+    }
+  }
+  if (np != c->mp) bad = true;
+  c->npush = np;
+  if (bad) atomicOr(err, FRICC_DEV_PIVOTAL);
+}
+
 __global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v; }
+
+// |D| (m for "largest") and the error word into a handle's status block
+__global__ void k_put_meta(const Ctl* c, int64_t nd_fixed, const unsigned* err, unsigned long long* meta) {
+  meta[0] = (unsigned long long)(c ? c->nd : nd_fixed);
+  meta[1] |= (unsigned long long)*err;
+}
 __global__ void k_set_f64(double* p, double v) { *p = v; }
 
 inline unsigned grid_for(int64_t n, int nt) {
@@ -328,6 +591,11 @@ static int dev_status(unsigned e) {
     fricc_set_error("ERROR MAKING PROBABILITY VECTOR: a sampling probability exceeds 1");
     return FRICC_ERR_P_GT_ONE;
   }
+  if (e & FRICC_DEV_PIVOTAL) {
+    fricc_set_error("ERROR IN PIVOTAL SAMPLING: acceptance probability outside [0, 1], leftover weight "
+                    "|a - 1| >= 1e-5, or a wrong number of sampled elements");
+    return FRICC_ERR_PIVOTAL;
+  }
   if (e & FRICC_DEV_TIMEOUT) {
     fricc_set_error("a bounded device-side wait timed out");
     return FRICC_ERR_TIMEOUT;
@@ -346,8 +614,82 @@ static int dev_status(unsigned e) {
 // round trip is the final one: with n_largest != nullptr the call
 // synchronises the stream, reads |D| and the error word and reports them;
 // with n_largest == nullptr it returns at once (nothing read back).
+int fricc_glibc_uniforms_device(unsigned* hist, int64_t k, double* out, cudaStream_t st);
+
+// Steps of pivotal sampling after D, R and m' are on the device (ctl): the
+// weight walk, the draws, the decisions, the scans; leaves S (m' indices).
+static int pivotal(const double* x, int64_t n, int64_t m, const GenP& gp, Ctl* ctl, CompressScratch& s,
+                   unsigned* glibc_hist, int64_t* n_draws, cudaStream_t st) {
+  (void)x;
+  double *P = nullptr, *A = nullptr, *R = nullptr;
+  unsigned char* code = nullptr;
+  int64_t *tlast = nullptr, *tcnt = nullptr;
+  const int64_t ntile = fricc_cdiv(n, PV_TILE);
+  int rc = fricc_alloc_t(&P, n, st);
+  if (!rc) rc = fricc_alloc_t(&A, n, st);
+  if (!rc) rc = fricc_alloc_t(&code, n, st);
+  if (!rc) rc = fricc_alloc_t(&tlast, ntile, st);
+  if (!rc) rc = fricc_alloc_t(&tcnt, ntile, st);
+  if (!rc) rc = fricc_alloc_t(&s.S, m, st);
+  int64_t jend = 0;
+  unsigned e = 0;
+  if (!rc) {
+    k_zero_u32<<<grid_for(m, 256), 256, 0, st>>>(s.S, m);
+    k_pvec<<<grid_for(n, 256), 256, 0, st>>>(gp, n, P, s.err);
+    k_piv_chain<<<1, 32, 0, st>>>(P, n, ctl, A, code);
+    fricc_note_launch(3);
+    rc = fricc_cuda_check(cudaGetLastError(), "pivotal chain");
+  }
+  if (!rc) rc = fricc_cuda_check(cudaMemcpyAsync(&jend, &ctl->jend, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "jend");
+  if (!rc) rc = fricc_cuda_check(cudaMemcpyAsync(&e, s.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "err");
+  if (!rc) rc = fricc_cuda_check(cudaStreamSynchronize(st), "pivotal chain");
+  if (!rc) rc = dev_status(e);  // p > 1: the reference exits before drawing
+  const int64_t used = jend;   // one draw per visited element j = 1..jend
+  if (!rc && used > 0) {
+    rc = fricc_alloc_t(&R, used, st);
+    if (!rc && glibc_hist) {
+      rc = fricc_glibc_uniforms_device(glibc_hist, used, R, st);
+    } else if (!rc) {
+      std::vector<double> h((size_t)used);
+      for (int64_t k = 0; k < used; ++k) h[(size_t)k] = (double)rand() / RAND_MAX;
+      rc = fricc_cuda_check(cudaMemcpyAsync(R, h.data(), sizeof(double) * (size_t)used, cudaMemcpyHostToDevice, st),
+                            "draws");
+      if (!rc) rc = fricc_cuda_check(cudaStreamSynchronize(st), "draws");
+    }
+  }
+  if (!rc) {
+    if (n_draws) *n_draws = used;
+    if (used > 0) k_piv_decide<<<grid_for(used, 256), 256, 0, st>>>(P, A, code, R, ctl, s.err);
+    k_piv_tiles<<<(unsigned)ntile, PV_NT, 0, st>>>(code, ctl, tlast, tcnt);
+    k_piv_carry<<<1, 1024, 0, st>>>(tlast, tcnt, ntile, ctl);
+    k_piv_emit<<<(unsigned)ntile, PV_NT, 0, st>>>(code, tlast, tcnt, ctl, s.S);
+    k_piv_final<<<1, 1, 0, st>>>(A, n, ctl, s.S, s.err);
+    fricc_note_launch(used > 0 ? 5 : 4);
+    rc = fricc_cuda_check(cudaGetLastError(), "pivotal");
+  }
+  if (!rc) rc = fricc_cuda_check(cudaMemcpyAsync(&e, s.err, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "err");
+  if (!rc) rc = fricc_cuda_check(cudaStreamSynchronize(st), "pivotal");
+  if (!rc) rc = dev_status(e);
+  fricc_free(P, st);
+  fricc_free(A, st);
+  fricc_free(R, st);
+  fricc_free(code, st);
+  fricc_free(tlast, st);
+  fricc_free(tcnt, st);
+  return rc;
+}
+
+// mode 2: "fri" with pivotal sampling.  Its draws (one per visited element)
+// come from the glibc stream whose history is glibc_hist[31] (host, oldest
+// first; advanced past the draws on return), or with glibc_hist == nullptr
+// from this process's own rand(), as the reference draws them.  *n_draws
+// receives the number consumed.  Synchronises the stream twice (the number
+// of draws, then the result).
+// meta (device, 2 words, optional): receives |D| and ORs in the error bits,
+// in stream order, so a caller that passes n_largest == nullptr never waits.
 int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, double rn, cudaStream_t st,
-                          int64_t* flat, double* vals, int64_t* n_largest) {
+                          int64_t* flat, double* vals, int64_t* n_largest, unsigned* glibc_hist, int64_t* n_draws,
+                          unsigned long long* meta) {
   if (n < 0 || m <= 0 || m > n) {
     fricc_set_error("Bad m_keep value: need 0 < m <= tensor size (m=%lld, size=%lld)", (long long)m,
                     (long long)n);
@@ -400,6 +742,10 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     if (mode == 1) {  // "largest": argsort(x, m) with unscaled values
       k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, nullptr, flat, vals);
       fricc_note_launch();
+      if (meta) {
+        k_put_meta<<<1, 1, 0, st>>>(nullptr, m, s.err, meta);
+        fricc_note_launch();
+      }
       TRY(fricc_cuda_check(cudaGetLastError(), "largest"));
       if (n_largest) {
         unsigned e = 0;
@@ -433,8 +779,27 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     k_finish_d<<<1, 1, 0, st>>>(s.ffail, s.Rb, s.ckey, s.cidx, m, ctl);
     fricc_note_launch();
 
-    // 5. probabilities, the p > 1 check, exact partial sums, systematic samples
     GenP gp{x, ctl};
+    if (mode == 2) {
+      TRY(pivotal(x, n, m, gp, ctl, s, glibc_hist, n_draws, st));
+      k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, ctl, flat, vals);
+      k_out_s<<<grid_for(m, 256), 256, 0, st>>>(gp, s.S, flat, vals);
+      fricc_note_launch(2);
+      if (meta) {
+        k_put_meta<<<1, 1, 0, st>>>(ctl, 0, s.err, meta);
+        fricc_note_launch();
+      }
+      TRY(fricc_cuda_check(cudaGetLastError(), "output"));
+      if (n_largest) {
+        int64_t nd = 0;
+        TRY(fricc_cuda_check(cudaMemcpyAsync(&nd, &ctl->nd, sizeof(int64_t), cudaMemcpyDeviceToHost, st), "nd"));
+        TRY(fricc_cuda_check(cudaStreamSynchronize(st), "compression"));
+        *n_largest = nd;
+      }
+      goto done;
+    }
+
+    // 5. probabilities, the p > 1 check, exact partial sums, systematic samples
     TRY(fricc_alloc_t(&s.S, m, st));
     k_zero_u32<<<grid_for(m, 256), 256, 0, st>>>(s.S, m);
     fricc_note_launch();
@@ -448,6 +813,10 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, ctl, flat, vals);
     k_out_s<<<grid_for(m, 256), 256, 0, st>>>(gp, s.S, flat, vals);
     fricc_note_launch(2);
+    if (meta) {
+      k_put_meta<<<1, 1, 0, st>>>(ctl, 0, s.err, meta);
+      fricc_note_launch();
+    }
     TRY(fricc_cuda_check(cudaGetLastError(), "output"));
     if (n_largest) {
       unsigned e = 0;
@@ -464,6 +833,26 @@ done:
   free_scratch(s, st);
   fricc_free(ctl, st);
   return rc;
+}
+
+// The error bits of a deferred status word, as a status code (and message).
+int fricc_dev_status(unsigned e) { return dev_status(e); }
+
+__global__ void k_meta_or(const unsigned* err, unsigned long long* meta) { meta[1] |= (unsigned long long)*err; }
+
+// Unpack without waiting: an out-of-range index is ORed into meta[1].
+int fricc_unpack_async(const int64_t* flat, int64_t m, const int64_t dims[4], int* slots, unsigned long long* meta,
+                       cudaStream_t st) {
+  unsigned* err = nullptr;
+  int rc = fricc_alloc_t(&err, 1, st);
+  if (rc) return rc;
+  cudaMemsetAsync(err, 0, sizeof(unsigned), st);
+  k_unpack<<<grid_for(m, 256), 256, 0, st>>>(flat, m, dims[0], dims[1], dims[2], dims[3], slots, err);
+  k_meta_or<<<1, 1, 0, st>>>(err, meta);
+  fricc_note_launch(2);
+  cudaError_t ce = cudaGetLastError();
+  fricc_free(err, st);
+  return ce == cudaSuccess ? FRICC_OK : fricc_cuda_fail(ce, "unpack", __FILE__, __LINE__);
 }
 
 int fricc_unpack_device(const int64_t* flat, int64_t m, const int64_t dims[4], int* slots, cudaStream_t st) {

@@ -145,7 +145,8 @@ __global__ void __launch_bounds__(SP_NT) k_spmm(const int* __restrict__ bptr, co
 // FP32-pair ("double-float") variant.  GB300 issues 128 FP32 lanes per SM per
 // clock but only 2 FP64 FMAs, so each product-accumulate is done on pairs of
 // floats carrying ~48 significand bits:
-//   W = Wh + Wl, v = vh + vl (split once from FP64, |Wl| <= 2^-24 |Wh|),
+//   W = Wh + Wl, v = vh + vl (split once from FP64 by bit manipulation,
+//   split_f2_bits: |W - Wh - Wl| < 2^-47 |W|, |Wl| < 2^-23 |Wh|),
 //   p = Wh*vh exactly as ph + e (one FMA recovers the rounding error),
 //   pl = e + Wh*vl + Wl*vh (Wl*vl, ~2^-48 relative, is dropped),
 //   (ah, al) += (ph, pl) with an error-free two-sum on the high parts,
@@ -158,10 +159,7 @@ __global__ void __launch_bounds__(SP_NT) k_spmm(const int* __restrict__ bptr, co
 // per two lanes of arithmetic.  W' is stored to match ("q-pair layout"):
 // row r, pair t holds the float4 (Wh[r][2t], Wh[r][2t+1], Wl[r][2t],
 // Wl[r][2t+1]); rows have ceil(QS/2) pairs, an odd QS padded with zero.
-__device__ __forceinline__ float2 split_f2(double d) {
-  const float h = __double2float_rn(d);
-  return make_float2(h, __double2float_rn(d - (double)h));
-}
+__device__ __forceinline__ float2 split_f2(double d) { return split_f2_bits(d); }
 
 typedef unsigned long long f32x2;  // two floats in one 64-bit register pair
 
@@ -275,8 +273,8 @@ __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr,
   for (int k = 0; k < DF_PPT; ++k) {
     const int64_t q = 2 * (t0 + k * DF_NT);
     const float2 h = upk2(ah[k]), l = upk2(al[k]);
-    if (q < QS) orow[q] = (double)h.x + (double)l.x;
-    if (q + 1 < QS) orow[q + 1] = (double)h.y + (double)l.y;
+    if (q < QS) orow[q] = pair_to_f64(h.x, l.x);
+    if (q + 1 < QS) orow[q + 1] = pair_to_f64(h.y, l.y);
   }
 }
 

@@ -17,7 +17,12 @@ struct Bucketing {
 struct FriccSparse {
   int64_t dims[4] = {0, 0, 0, 0};
   int64_t m = 0;            // kept nonzeros
-  int64_t n_largest = 0;    // |D|: entries kept exactly (compression "fri")
+  int64_t n_largest = 0;    // |D|: entries kept exactly (compression "fri"), valid when !pending
+  // Written by the device at the end of an asynchronous compression and read
+  // back at the next blocking call on the handle: [0] |D|, [1] error bits.
+  unsigned long long* meta = nullptr;
+  bool pending = false;     // meta holds a result not yet read back
+  int status = 0;           // status of the last compression once read back
   int64_t* flat = nullptr;  // [m] flat C-order index into the dense tensor
   double* vals = nullptr;   // [m]
   int* slots = nullptr;     // [m][4] unpacked (i, j, a, b)

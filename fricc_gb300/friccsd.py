@@ -59,6 +59,24 @@ def _sym(x):
     return x + x.permute(1, 0, 3, 2)
 
 
+def _check_sampling(s, rn_draw):
+    if s["compression"] != "fri":
+        return
+    if s["sampling_method"] not in ("systematic", "pivotal"):
+        raise ValueError(f"sampling_method must be 'pivotal' or 'systematic', got {s['sampling_method']!r}")
+    if s["sampling_method"] == "pivotal" and not (rn_draw is libc_uniform or hasattr(rn_draw, "history")):
+        raise ValueError("pivotal sampling draws from the process's rand() (rn_draw=libc_uniform) or from a "
+                         "GlibcRand stream; a generic draw callable cannot supply them")
+
+
+def _compress(handle, t2, m, s, rn, rn_draw, stream):
+    """One compression as the settings ask: systematic/largest take the draw rn,
+    pivotal draws its own from rn_draw."""
+    if s["compression"] == "fri" and s["sampling_method"] == "pivotal":
+        return handle.compress_pivotal(t2, m, None if rn_draw is libc_uniform else rn_draw, stream)
+    return handle.compress(t2, m, s["compression"], rn, stream)
+
+
 class _Handle:
     """A reusable compressed-T2 handle (device SparseTensor4d)."""
 
@@ -77,6 +95,24 @@ class _Handle:
             L.check(lib.fricc_sp_create(_ptr(t2), L.i64arr(t2.shape), int(m), comp, 0, float(rn), stream,
                                         ctypes.byref(self.h)))
             self.key = key
+        return self.h
+
+    def compress_pivotal(self, t2, m, rng, stream):
+        """Pivotal FRI compression drawing from rng (GlibcRand: on the device;
+        the process's rand() otherwise)."""
+        lib = L.load()
+        key = (tuple(t2.shape), int(m))
+        hist, writeback = L.hist_arg(rng)
+        used = ctypes.c_int64(0)
+        if self.h.value and self.key == key:
+            L.check(lib.fricc_sp_recompress_pivotal(self.h, _ptr(t2), hist, stream, ctypes.byref(used)))
+        else:
+            self.free()
+            L.check(lib.fricc_sp_create_pivotal(_ptr(t2), L.i64arr(t2.shape), int(m), hist, stream,
+                                                ctypes.byref(self.h), ctypes.byref(used)))
+            self.key = key
+        writeback()
+        self.draws_used = used.value
         return self.h
 
     def free(self):
@@ -98,8 +134,7 @@ class FRICCSDGPU:
                 raise ValueError(f"Contraction ({c}) is not supported!")
         if s["compression"] not in L.COMPRESSION:
             raise ValueError(f"The compression method you chose ({s['compression']}) isn't supported")
-        if s["compression"] == "fri" and s["sampling_method"] != "systematic":
-            raise NotImplementedError("sampling_method 'pivotal' is not implemented on the GPU path")
+        _check_sampling(s, rn_draw)
         self.settings = s
         self.eris = eris
         self.level_shift = float(level_shift)
@@ -113,6 +148,7 @@ class FRICCSDGPU:
             eris.prepare_splits()
         self._sp = _Handle()
         self._sp_w = _Handle()
+        self._side = torch.cuda.Stream(device=eris.device)
         self._res = torch.zeros(4, dtype=torch.float64, device=eris.device)
         self._wT = None
         self._iter = 0
@@ -172,11 +208,23 @@ class FRICCSDGPU:
         fov = E.fock[:o, o:]
         ein = torch.einsum
         need_w = "O^3V^3" in comp or "O^4V^2" in comp
+        piv = s["compression"] == "fri" and s["sampling_method"] == "pivotal"
         if rn is None:
             kind = s["compression"]
-            rn = [self.rn_draw() if kind == "fri" else 0.0 for _ in range(2 if need_w else 1)]
-        T = self._sp.compress(t2, m, s["compression"], rn[0], st)
-        Tw = self._sp_w.compress(self._w_source(t2), m, s["compression"], rn[1], st) if need_w else None
+            rn = [self.rn_draw() if kind == "fri" and not piv else 0.0 for _ in range(2 if need_w else 1)]
+        # both compressions run on a side stream, overlapping the dense work
+        # below; the sparse terms wait for them
+        main, side = torch.cuda.current_stream(), self._side
+        ev_in = torch.cuda.Event()
+        ev_in.record(main)
+        side.wait_event(ev_in)
+        t2.record_stream(side)
+        with torch.cuda.stream(side):
+            sst = ctypes.c_void_p(side.cuda_stream)
+            T = _compress(self._sp, t2, m, s, rn[0], self.rn_draw, sst)
+            Tw = _compress(self._sp_w, self._w_source(t2), m, s, rn[1], self.rn_draw, sst) if need_w else None
+            ev_c = torch.cuda.Event()
+            ev_c.record(side)
         self._iter += 1
 
         mm = D.gemm_df if self.precision == "df64" else D.gemm_torch
@@ -205,7 +253,9 @@ class FRICCSDGPU:
         t1new += 2 * ein("kcai,kc->ia", E.ovvo, t1) - ein("kiac,kc->ia", E.oovv, t1)
         t1new = t1new.contiguous()
         mm(t2.view(o, o * v * v), E.G_t1.view(o * v * v, v), t1new, 1.0, 1.0)  # O^2V^3, :165-166
-        t1new += t1 @ (t1.reshape(1, ov) @ E.G_t1.permute(0, 2, 1, 3).reshape(ov, v * v)).view(v, v)  # :167-168
+        # X[c,a] = sum_kd t1[k,d] (2 (kd|ac) - (kc|ad)): the t1.t1 T1 term (:167-168) and Lvv's ovvv part
+        X = (t1.reshape(1, ov) @ E.G_t1_kdca.view(ov, v * v)).view(v, v)
+        t1new += t1 @ X
         # -2 (lc|ki) + (kc|li) = -g_ovoo[l,c,k,i]
         t1new -= ein2("lcki,klac->ia", E.g_ovoo, t2)
         t1new -= ein("lcki,lc,ka->ia", E.g_ovoo, t1, t1)
@@ -223,10 +273,11 @@ class FRICCSDGPU:
         t2new = t2new.contiguous()
 
         Loo = D.Loo(t1, t2, E, Foo=Foo0)
-        Lvv = D.Lvv(t1, t2, E, Fvv=Fvv0)
+        Lvv = Fvv0 - t1.T @ fov + X.T                      # Lvv with its ovvv part from X
         Loo.diagonal().sub_(e_o)
         Lvv.diagonal().sub_(e_v)
 
+        main.wait_event(ev_c)  # the compressed tensors from here on
         if "O^4V^2" in comp:  # sparse_cc_Woooo (:309-322)
             Wo = (ein2("lcki,jc->klij", E.ovoo, t1) + ein2("kclj,ic->klij", E.ovoo, t1)).permute(2, 3, 0, 1)
             Wo = Wo.contiguous()                                                  # [i,j,k,l]
@@ -351,8 +402,15 @@ class FRICCSDGPU:
         self._iter = 0
         self._t2_avg = None
 
+    def _handles_in_use(self):
+        return [h for h in (self._sp, self._sp_w) if h.h.value]
+
     def read_energy(self):
+        """E_corr and the step norm of the last update (waits for it); raises
+        if one of its compressions failed (a probability above 1)."""
         r = self._res[:2].cpu()
+        for h in self._handles_in_use():
+            L.check(self.lib.fricc_sp_status(h.h))
         self.last_energy, self.last_normt = float(r[0]), float(r[1])
         return self.last_energy, self.last_normt
 

@@ -28,7 +28,7 @@ import torch
 
 from . import _lib as L
 from . import rccsd_dense as D
-from .friccsd import ALLOWED_CONTRACTIONS, FRICCSDGPU, _Handle, _ptr, _sym
+from .friccsd import ALLOWED_CONTRACTIONS, FRICCSDGPU, _check_sampling, _compress, _Handle, _ptr, _sym
 from .py_rccsd import libc_uniform
 
 DEFAULT_SETTINGS = {
@@ -53,8 +53,7 @@ class FRILCCSDGPU(FRICCSDGPU):
                 raise ValueError(f"Contraction ({c}) is not supported!")
         if s["compression"] not in L.COMPRESSION:
             raise ValueError(f"The compression method you chose ({s['compression']}) isn't supported")
-        if s["compression"] == "fri" and s["sampling_method"] != "systematic":
-            raise NotImplementedError("sampling_method 'pivotal' is not implemented on the GPU path")
+        _check_sampling(s, rn_draw)
         if precision not in ("fp64", "df64"):
             raise ValueError("precision must be 'fp64' or 'df64'")
         self.settings = s
@@ -75,8 +74,10 @@ class FRILCCSDGPU(FRICCSDGPU):
 
     @property
     def n_draws(self):
-        """Uniform draws one iteration consumes (one per FRI compression)."""
-        return len(self._handles) if self.settings["compression"] == "fri" else 0
+        """Uniform draws one iteration takes as rn (one per systematic FRI
+        compression; pivotal sampling draws its own)."""
+        s = self.settings
+        return len(self._handles) if s["compression"] == "fri" and s["sampling_method"] == "systematic" else 0
 
     def update_amps(self, t1, t2, rn=None, t1_old=None, t2_old=None):
         """One FRI-LCCSD iteration on device tensors; returns (t1new, t2new).
@@ -103,10 +104,11 @@ class FRILCCSDGPU(FRICCSDGPU):
         ein2 = D.einsum_df if self.precision == "df64" else torch.einsum
         f64, dev = t2.dtype, t2.device
         if rn is None:
-            rn = [self.rn_draw() if s["compression"] == "fri" else 0.0 for _ in self._handles]
-        if len(rn) != len(self._handles):
+            rn = [self.rn_draw() for _ in range(self.n_draws)]
+        if self.n_draws and len(rn) != len(self._handles):
             raise ValueError(f"update_amps: {len(self._handles)} draws expected, got {len(rn)}")
-        Ts = [h.compress(t2, m, s["compression"], r, st) for h, r in zip(self._handles, rn)]
+        rn = list(rn) if self.n_draws else [0.0] * len(self._handles)
+        Ts = [_compress(h, t2, m, s, r, self.rn_draw, st) for h, r in zip(self._handles, rn)]
         T = dict(zip(SPARSE_ORDER, Ts if self.independent else Ts * len(SPARSE_ORDER)))
 
         Foo = E.fock[:o, :o].clone()
@@ -185,6 +187,9 @@ class FRILCCSDGPU(FRICCSDGPU):
                                                  _ptr(E.ovov), _ptr(t1o.contiguous()), _ptr(t2o.contiguous()), o, v,
                                                  _ptr(t1new), _ptr(t2new), _ptr(self._res), st))
         return t1new, t2new
+
+    def _handles_in_use(self):
+        return [h for h in self._handles if h.h.value]
 
     def energy(self, t1, t2):
         return D.lin_cc_energy(t1, t2, self.eris)

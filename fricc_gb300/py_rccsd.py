@@ -16,11 +16,19 @@ it unchanged (``from .py_rccsd import SparseTensor4d, contract_DTSpT``):
 Arrays may be numpy (host: copied to the device and, for ``ouput``, back) or
 torch CUDA tensors (used in place, on the current torch stream).
 
+Sampling: "systematic" consumes one libc ``rand()``; "pivotal" (the
+binding's default) one per element it visits, from this process's ``rand()``
+as the reference does, or, with ``rng=GlibcRand(...)``, from that stream
+(generated on the device, the object advanced past the draws).  Pivotal
+sampling emits S in the reference's order (not sorted).
+
 Differences, all raising instead of terminating the process:
-* sampling_method "pivotal" raises NotImplementedError (the reference's
-  FRI-CCSD path always passes "systematic");
 * a bad m, dims, term or compression raises ValueError where the reference
-  calls exit(EXIT_FAILURE); a probability above 1 raises FriccError.
+  calls exit(EXIT_FAILURE); a probability above 1 and the pivotal sampler's
+  own failures raise FriccError;
+* an unknown sampling_method raises ValueError (the reference's check of it
+  can never fire, src/fri_utils.cpp:443-455, and its sampled slots then keep
+  index 0).
 """
 from __future__ import annotations
 
@@ -60,7 +68,7 @@ class SparseTensor4d:
     """Device-resident compressed tensor (include/sparse_tensor.hpp:13-100)."""
 
     def __init__(self, tensor_arr, dims=None, m=None, compression="fri", sampling_method="pivotal",
-                 verbose=False, rn=None):
+                 verbose=False, rn=None, rng=None):
         lib = L.load()
         self._h = ctypes.c_void_p()
         if m is None and dims is not None and not isinstance(tensor_arr, (np.ndarray, torch.Tensor)):
@@ -84,17 +92,24 @@ class SparseTensor4d:
         m = int(m)
         t0 = time.perf_counter()
         x = _to_device(tensor_arr)
-        if rn is None:
-            rn = libc_uniform() if compression == "fri" else 0.0
         samp = L.SAMPLING.get(sampling_method, -1)
-        if compression == "fri" and samp != 0:
-            if sampling_method == "pivotal":
-                raise NotImplementedError("sampling_method 'pivotal' is not implemented on the GPU path "
-                                          "(fricc/friccsd.py uses 'systematic')")
+        self.draws_used = 0
+        if compression == "fri" and samp < 0:
             raise ValueError(f"sampling_method must be 'pivotal' or 'systematic', got {sampling_method!r}")
-        L.check(lib.fricc_sp_create(ctypes.c_void_p(x.data_ptr()), L.i64arr(self._dims), m,
-                                    L.COMPRESSION[compression], max(samp, 0), float(rn), _stream(),
-                                    ctypes.byref(self._h)))
+        if compression == "fri" and samp == L.SAMPLING["pivotal"]:
+            hist, writeback = L.hist_arg(rng)
+            used = ctypes.c_int64(0)
+            L.check(lib.fricc_sp_create_pivotal(ctypes.c_void_p(x.data_ptr()), L.i64arr(self._dims), m, hist,
+                                                _stream(), ctypes.byref(self._h), ctypes.byref(used)))
+            writeback()
+            self.draws_used = used.value
+        else:
+            if rn is None:
+                rn = (rng() if rng is not None else libc_uniform()) if compression == "fri" else 0.0
+            L.check(lib.fricc_sp_create(ctypes.c_void_p(x.data_ptr()), L.i64arr(self._dims), m,
+                                        L.COMPRESSION[compression], max(samp, 0), float(rn), _stream(),
+                                        ctypes.byref(self._h)))
+            L.check(lib.fricc_sp_status(self._h))  # the reference's constructor fails on the spot
         self._keep = x  # the device copy stays alive while the stream may still read it
         if verbose:
             t = time.perf_counter() - t0

@@ -55,6 +55,9 @@ class DeviceERIs:
         self.g_ovoo = 2.0 * ovoo - ovoo.permute(2, 1, 0, 3)               # [l,c,k,i]: 2(lc|ki) - (kc|li)
         # T1 O^2V^3 terms as one GEMM: G[k,c,d,a] = 2 (kd|ac) - (kc|ad)
         self.G_t1 = (2.0 * ovvv.permute(0, 3, 1, 2) - ovvv.permute(0, 1, 3, 2)).contiguous()
+        # the same integral as [k,d,c,a]: X[c,a] = sum_kd t1[k,d] G[k,c,d,a] is one GEMV
+        # (it serves the t1.t1 T1 term and the ovvv part of Lvv)
+        self.G_t1_kdca = self.G_t1.permute(0, 2, 1, 3).contiguous()
         # the t1 parts of Wvvvv, contracted with the compressed T2 instead of being
         # built densely: W'[c,d,(x,k,a)] = (kd|ac) for x=0 and (kc|ad) for x=1
         self.ovvv_XY = torch.stack([ovvv.permute(3, 1, 0, 2), ovvv.permute(1, 3, 0, 2)], dim=2).contiguous()
@@ -230,7 +233,7 @@ def gemm_torch(A, B, C, alpha=1.0, beta=0.0):
 
 
 def split_f2(x: torch.Tensor, qs: int = None) -> torch.Tensor:
-    """W' [rows][qs] (FP64) as float pairs hi + lo = x (~2^-48), in the
+    """W' [rows][qs] (FP64) as float pairs hi + lo = x (to 2^-47), in the
     q-pair layout of fricc_spmm_f2: per row, float4 (hi_q, hi_q+1, lo_q,
     lo_q+1) for q = 0, 2, 4, ...  qs defaults to the product of the
     dimensions after the first two (W' is always [key1, key2, q...])."""

@@ -46,6 +46,8 @@ extern "C" {
 #define FRICC_ERR_TIMEOUT 5      /* a bounded device-side wait gave up */
 #define FRICC_ERR_INDEX 6        /* an index fell outside dims */
 #define FRICC_ERR_UNSUPPORTED 7  /* mode not implemented on this path */
+#define FRICC_ERR_PIVOTAL 8      /* pivotal sampling failed as the reference's does (acceptance outside
+                                    [0,1], leftover weight, wrong sample count) */
 
 #define FRICC_COMPRESSION_FRI 0
 #define FRICC_COMPRESSION_LARGEST 1
@@ -66,12 +68,37 @@ const char* fricc_last_error(void);
  * rand()/RAND_MAX the reference consumes) or FRICC_COMPRESSION_LARGEST (rn
  * unused).  Entries come out in the reference's slot order: the exactly kept
  * largest entries in descending |t| (ties by ascending flat index), then the
- * sampled ones in ascending flat index.  Synchronises `stream`. */
+ * sampled ones in ascending flat index.  Stream-ordered and asynchronous:
+ * the call returns once the work is enqueued on `stream`; |D| and the
+ * compression's own failures (a probability above 1) are read back by the
+ * next blocking call on the handle (fricc_sp_status, fricc_sp_info,
+ * fricc_sp_get, fricc_sp_export), which then returns the error. */
 int fricc_sp_create(const double* t2, const int64_t dims[4], int64_t m, int compression, int sampling, double rn,
                     void* stream, fricc_sparse** out);
 
-/* Re-compress into an existing handle (same dims and m), reusing its memory. */
+/* Re-compress into an existing handle (same dims and m), reusing its memory;
+ * asynchronous like fricc_sp_create. */
 int fricc_sp_recompress(fricc_sparse* T, const double* t2, int compression, int sampling, double rn, void* stream);
+
+/* Wait for the handle's last compression and return its status (FRICC_OK,
+ * FRICC_ERR_P_GT_ONE, FRICC_ERR_TIMEOUT, FRICC_ERR_INDEX).  No reference
+ * counterpart: the reference exits inside the constructor. */
+int fricc_sp_status(const fricc_sparse* T);
+
+/* "fri" compression with pivotal sampling (src/fri_utils.cpp:63-127, the
+ * binding's default sampling_method), which draws one uniform
+ * rand()/RAND_MAX per element it visits.  glibc_hist: the state of the
+ * glibc rand() stream to draw from, as its 31-word history (the words
+ * r[k-31..k-1] of the recurrence r[k] = r[k-31] + r[k-3] mod 2^32, oldest
+ * first; host memory), advanced past the draws on return; NULL draws from
+ * this process's own rand(), exactly as the reference does.  *n_draws
+ * (optional) receives the number of draws consumed.  S keeps the order the
+ * sampler emits it.  Synchronises `stream`.  Failures of the reference's
+ * sampler (its exits) return FRICC_ERR_PIVOTAL. */
+int fricc_sp_create_pivotal(const double* t2, const int64_t dims[4], int64_t m, uint32_t* glibc_hist, void* stream,
+                            fricc_sparse** out, int64_t* n_draws);
+int fricc_sp_recompress_pivotal(fricc_sparse* T, const double* t2, uint32_t* glibc_hist, void* stream,
+                                int64_t* n_draws);
 
 /* An all-zero tensor of nnz entries (index 0, value 0). */
 int fricc_sp_create_empty(const int64_t dims[4], int64_t nnz, void* stream, fricc_sparse** out);
@@ -122,8 +149,10 @@ int fricc_spmm(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, con
 int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* Wp4, int64_t QS,
                   double* Op, void* stream);
 
-/* x [rows][qs] (FP64, contiguous) split into float pairs hi = (float)x,
- * lo = (float)(x - hi) (hi + lo = x to ~2^-48 relative), in the q-pair
+/* x [rows][qs] (FP64, contiguous) split into float pairs, hi the top 24
+ * significand bits of x and lo the rest rounded to 24 bits
+ * (|x - hi - lo| < 2^-47 |x|; outside 2^-74 <= |x| < 2^128, hi = (float)x,
+ * lo = (float)(x - hi)), in the q-pair
  * layout fricc_spmm_f2 reads: for row r and pair t < ceil(qs/2), the four
  * floats out4[4(r ceil(qs/2) + t) ..] = hi[r][2t], hi[r][2t+1], lo[r][2t],
  * lo[r][2t+1] (an odd qs padded with zero).  out4 holds
@@ -147,6 +176,17 @@ double fricc_contract_flops(const char* term, const fricc_sparse* T);
  * memory, |D| to *n_largest (host).  Synchronises `stream`. */
 int fricc_compress(const double* x, int64_t n, int64_t m, int compression, double rn, int64_t* flat, double* vals,
                    int64_t* n_largest, void* stream);
+
+/* fri_compression with pivotal sampling on flat device arrays (see
+ * fricc_sp_create_pivotal for glibc_hist and n_draws). */
+int fricc_compress_pivotal(const double* x, int64_t n, int64_t m, uint32_t* glibc_hist, int64_t* flat, double* vals,
+                           int64_t* n_largest, int64_t* n_draws, void* stream);
+
+/* k uniforms rand()/RAND_MAX of the glibc stream with history hist[31]
+ * (host, oldest first) into out (device); hist is advanced past them.  The
+ * device form of the draws the reference makes with rand() (no reference
+ * counterpart as a function).  Synchronises `stream`. */
+int fricc_glibc_uniforms(uint32_t* hist, int64_t k, double* out, void* stream);
 
 /* out[i] = fl(out[i-1] + |x[i]|) with out[-1] = 0 (device arrays of n
  * doubles): the exact bits a single CPU thread's left-to-right FP64 sum

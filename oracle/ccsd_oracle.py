@@ -42,6 +42,23 @@ DEFAULT_SETTINGS = {
 }
 
 
+def pivotal_tensor(sparse, x, m, rn_draw):
+    """A pivotal compression drawing from rn_draw: a GlibcRand-like stream
+    (history()/set_history()) is copied, the copy supplies up to one draw per
+    element, and the stream is then advanced by the draws consumed; anything
+    else means libc's own rand(), as the reference draws."""
+    if hasattr(rn_draw, "history"):
+        from fricc_gb300.rng import GlibcRand
+        probe = GlibcRand(1)
+        probe.set_history(rn_draw.history())
+        draws = np.array([probe.uniform() for _ in range(x.size)])
+        T = sparse.SparseTensor4d(x, x.shape, m, "fri", "pivotal", draws=draws)
+        for _ in range(T.draws_used):
+            rn_draw.rand()
+        return T
+    return sparse.SparseTensor4d(x, x.shape, m, "fri", "pivotal")
+
+
 def _sym(x):
     """x_ijab + x_jiba"""
     return x + x.transpose(1, 0, 3, 2)
@@ -68,6 +85,8 @@ def update_amps(settings, t1, t2, eris, rn_draw=FO.libc_rand_uniform, sparse=FO,
 
     def compress(x=t2):
         kind = settings["compression"]
+        if kind == "fri" and settings["sampling_method"] == "pivotal":
+            return pivotal_tensor(sparse, x, m, rn_draw)
         rn = rn_draw() if kind == "fri" else None
         return sparse.SparseTensor4d(x, x.shape, m, kind, settings["sampling_method"],
                                      settings["verbose"], rn=rn)

@@ -19,7 +19,8 @@
  *
  * Status codes: 0 ok, 1 bad argument, 3 probability > 1 (the reference
  * exits with "ERROR MAKING PROBABILITY VECTOR"), 6 unpacked index out of
- * range (the reference exits in SparseTensor4d::unpack_idx).
+ * range (the reference exits in SparseTensor4d::unpack_idx), 7 an exit of
+ * sample_pivotal ("ERROR IN PIVOTAL SAMPLING", "Wrong number of elements").
  */
 #include <math.h>
 #include <omp.h>
@@ -31,6 +32,8 @@
 #define FO_BAD_ARG 1
 #define FO_P_GT_ONE 3
 #define FO_INDEX_RANGE 6
+#define FO_PIVOTAL 7 /* sample_pivotal's own exits: acceptance outside [0,1],
+                        a leftover weight |a-1| >= 1e-5, or a wrong count */
 
 typedef struct {
   double key; /* |x_i| */
@@ -159,6 +162,74 @@ void fo_sample_systematic(int64_t n_sample, const double* p, int64_t n, double r
     }
   }
   free(I);
+}
+
+/* sample_pivotal, src/fri_utils.cpp:63-127.  One uniform per element
+ * j = 1, 2, ... (rand()/RAND_MAX): from draws[] when given (at most n_avail
+ * of them), else from libc rand() itself.  The carried weight a = p_0,
+ * a += p_j; below 1 the pivot i moves to j with probability p_j / a; at or
+ * above 1, a -= 1 and one index is emitted: the pivot (which then moves to
+ * j) with probability (1 - p_j) / (1 - a), else j.  Stops once n_sample
+ * indices are out; a run that reaches the last element with |a - 1| < 1e-5
+ * emits the pivot.  *n_used receives the draws consumed. */
+int fo_sample_pivotal(int64_t n_sample, const double* p, int64_t n, const double* draws, int64_t n_avail,
+                      int64_t* S, int64_t* n_used) {
+  int64_t ns = 0, i = 0, used = 0;
+  double a = n > 0 ? p[0] : 0.0;
+  for (int64_t j = 1; j < n; ++j) {
+    a += p[j];
+    double rn;
+    if (draws) {
+      if (used >= n_avail) return FO_BAD_ARG;
+      rn = draws[used];
+    } else {
+      rn = (double)rand() / RAND_MAX;
+    }
+    ++used;
+    if (a < 1.) {
+      if (rn < p[j] / a) i = j;
+    } else {
+      a -= 1.;
+      const double prob_accept = (1. - p[j]) / (1. - a);
+      if (prob_accept > 1 || prob_accept < 0) { *n_used = used; return FO_PIVOTAL; }
+      if (rn < prob_accept) { S[ns++] = i; i = j; }
+      else S[ns++] = j;
+    }
+    if (ns == n_sample) break;
+    if (j == n - 1) {
+      if (fabs(a - 1.) < 1e-5) S[ns++] = i;
+      else { *n_used = used; return FO_PIVOTAL; }
+    }
+  }
+  *n_used = used;
+  return ns == n_sample ? FO_OK : FO_PIVOTAL;
+}
+
+/* fri_compression, src/fri_utils.cpp:439-522, pivotal sampling (S in the
+ * order sample_pivotal emits it). */
+int fo_fri_compression_pivotal(const double* x, int64_t n, int64_t m, const double* draws, int64_t n_avail,
+                               int64_t* idx, double* val, int64_t* n_largest, int64_t* n_used) {
+  if (n < 0 || m < 0 || m > n) return FO_BAD_ARG;
+  int64_t* sorted = (int64_t*)malloc(sizeof(int64_t) * (size_t)(m > 0 ? m : 1));
+  fo_argsort(x, n, m, sorted);
+  double R;
+  int64_t nd = fo_get_d_largest(x, n, m, sorted, &R);
+  double* p = (double*)malloc(sizeof(double) * (size_t)(n > 0 ? n : 1));
+  int st = fo_make_probability_vector(x, n, m - nd, sorted, nd, R, p);
+  *n_used = 0;
+  if (st != FO_OK) { free(sorted); free(p); return st; }
+  int64_t* S = (int64_t*)malloc(sizeof(int64_t) * (size_t)(m - nd > 0 ? m - nd : 1));
+  st = fo_sample_pivotal(m - nd, p, n, draws, n_avail, S, n_used);
+  if (st == FO_OK) {
+    for (int64_t i = 0; i < nd; ++i) { idx[i] = sorted[i]; val[i] = x[sorted[i]]; }
+    for (int64_t k = 0; k < m - nd; ++k) {
+      idx[nd + k] = S[k];
+      val[nd + k] = x[S[k]] / p[S[k]];
+    }
+    if (n_largest) *n_largest = nd;
+  }
+  free(sorted); free(p); free(S);
+  return st;
 }
 
 /* fri_compression, src/fri_utils.cpp:439-522, systematic sampling.

@@ -52,6 +52,8 @@ def lib():
         L.fo_fri_compression.argtypes = [_f64p, ctypes.c_int64, ctypes.c_int64, ctypes.c_double,
                                          _i64p, _f64p, _i64p]
         L.fo_largest.argtypes = [_f64p, ctypes.c_int64, ctypes.c_int64, _i64p, _f64p]
+        L.fo_fri_compression_pivotal.argtypes = [_f64p, ctypes.c_int64, ctypes.c_int64, _f64p, ctypes.c_int64,
+                                                 _i64p, _f64p, _i64p, _i64p]
         L.fo_unpack.argtypes = [_i64p, ctypes.c_int64, _i64p, _i64p]
         L.fo_term_id.argtypes = [ctypes.c_char_p]
         L.fo_outer_size.restype = ctypes.c_int64
@@ -123,6 +125,31 @@ def fri_compression(x: np.ndarray, m: int, rn: float | None = None):
     return idx, val, nd.value
 
 
+def fri_compression_pivotal(x: np.ndarray, m: int, draws=None):
+    """Pivotal FRI compression; returns (flat_idx[m], vals[m], n_largest, draws_used).
+
+    draws: the uniforms rand()/RAND_MAX in order (an array); None draws from
+    libc rand() itself, like the reference."""
+    x = np.ascontiguousarray(x, dtype=np.float64).ravel()
+    idx = np.empty(m, dtype=np.int64)
+    val = np.empty(m, dtype=np.float64)
+    nd, used = ctypes.c_int64(0), ctypes.c_int64(0)
+    if draws is None:
+        dp, na = None, 0
+    else:
+        draws = np.ascontiguousarray(draws, dtype=np.float64)
+        dp, na = _p(draws, _f64p), draws.size
+    st = lib().fo_fri_compression_pivotal(_p(x, _f64p), x.size, m, dp, na, _p(idx, _i64p), _p(val, _f64p),
+                                          ctypes.byref(nd), ctypes.byref(used))
+    if st == 3:
+        raise RuntimeError("ERROR MAKING PROBABILITY VECTOR (p > 1)")
+    if st == 7:
+        raise RuntimeError("ERROR IN PIVOTAL SAMPLING")
+    if st:
+        raise ValueError(f"fri_compression_pivotal: status {st}")
+    return idx, val, nd.value, used.value
+
+
 def largest(x: np.ndarray, m: int):
     x = np.ascontiguousarray(x, dtype=np.float64).ravel()
     idx = np.empty(m, dtype=np.int64)
@@ -147,7 +174,7 @@ class SparseTensor4d:
     """Oracle mirror of the reference's SparseTensor4d (include/sparse_tensor.hpp:13-100)."""
 
     def __init__(self, tensor_arr, dims, m=None, compression="fri", sampling_method="pivotal",
-                 verbose=False, rn=None):
+                 verbose=False, rn=None, draws=None):
         if m is None:  # SparseTensor4d(dims, nnz): an empty tensor (src/py_rccsd.cpp:33)
             self.dims = tuple(int(d) for d in tensor_arr)
             nnz = int(dims)
@@ -165,9 +192,12 @@ class SparseTensor4d:
             self.flat, self.vals = largest(tensor_arr, m)
             self.n_largest = m
         elif compression == "fri":
-            if sampling_method != "systematic":
-                raise NotImplementedError(f"sampling_method {sampling_method!r}")
-            self.flat, self.vals, self.n_largest = fri_compression(tensor_arr, m, rn)
+            if sampling_method == "pivotal":
+                self.flat, self.vals, self.n_largest, self.draws_used = fri_compression_pivotal(tensor_arr, m, draws)
+            elif sampling_method == "systematic":
+                self.flat, self.vals, self.n_largest = fri_compression(tensor_arr, m, rn)
+            else:
+                raise ValueError(f"sampling_method {sampling_method!r}")
         else:
             raise ValueError(f"The compression method you chose ({compression}) isn't supported")
         self.idx4 = unpack(self.flat, self.dims)

@@ -56,6 +56,9 @@ def update_amps(settings, t1, t2, eris, rn_draw=FO.libc_rand_uniform, sparse=FO,
 
     def compress():
         kind = settings["compression"]
+        if kind == "fri" and settings["sampling_method"] == "pivotal":
+            from .ccsd_oracle import pivotal_tensor
+            return pivotal_tensor(sparse, t2, m, rn_draw)
         rn = rn_draw() if kind == "fri" else None
         return sparse.SparseTensor4d(t2, t2.shape, m, kind, settings["sampling_method"],
                                      settings["verbose"], rn=rn)

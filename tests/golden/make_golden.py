@@ -15,6 +15,10 @@ records:
                    synthetic system: every iterate, every energy, every draw;
 * lccsd.npz     -- the same for fricc/frilccsd.py (FRI-LCCSD): one shared
                    compression, six independent compressions, and LCCD.
+* pivotal.npz   -- SparseTensor4d("fri", "pivotal") outputs (pivotal is the
+                   binding's default) with the number of rand() draws each
+                   consumed, the reference run in a forked child because its
+                   sampler exits the process on its own errors;
 * unbiased.npz  -- fricc/friccsd.py with "unbiased": True (running-average
                    W compression after burn-in), its missing iteration
                    counter supplied by the driver.
@@ -117,6 +121,71 @@ def compress_cases(R):
             out[key + "_idx"] = idx
             out[key + "_val"] = val
     out["n_cases"] = np.int64(len(cases))
+    return out
+
+
+def _ref_pivotal_child(R, x, m, seed, wfd):
+    """In a forked child: the reference's pivotal SparseTensor4d (which may
+    exit the process on its own errors); the result goes back through wfd."""
+    import pickle
+    libc.srand(seed)
+    t = R.SparseTensor4d(x, x.shape, m, "fri", "pivotal", False)
+    tail = [libc.rand() for _ in range(4)]
+    idx = np.array([t.get_element(i)[0] for i in range(m)], dtype=np.int64).reshape(m, 4)
+    val = np.array([t.get_element(i)[1] for i in range(m)], dtype=np.float64)
+    os.write(wfd, pickle.dumps((idx, val, tail)))
+
+
+def ref_pivotal(R, x, m, seed):
+    """(idx, val, draws consumed) of the reference's pivotal compression, or
+    None when the reference exits (its own error paths)."""
+    import pickle
+    rfd, wfd = os.pipe()
+    pid = os.fork()
+    if pid == 0:
+        os.close(rfd)
+        try:
+            _ref_pivotal_child(R, x, m, seed, wfd)
+        finally:
+            os._exit(0)
+    os.close(wfd)
+    data = b""
+    while True:
+        chunk = os.read(rfd, 1 << 20)
+        if not chunk:
+            break
+        data += chunk
+    os.close(rfd)
+    _, status = os.waitpid(pid, 0)
+    if status != 0 or not data:
+        return None
+    idx, val, tail = pickle.loads(data)
+    libc.srand(seed)
+    stream = [libc.rand() for _ in range(x.size + 8)]
+    used = next(k for k in range(len(stream) - 3) if stream[k:k + 4] == tail)
+    return idx, val, used
+
+
+def pivotal_cases(R):
+    """Pivotal compressions by the reference (the binding's default sampling),
+    on the compress.npz inputs and on larger MP2 amplitudes."""
+    g = np.load(os.path.join(HERE, "compress.npz"))
+    xs = [(g[f"c{k}_x"], int(g[f"c{k}_m"])) for k in range(int(g["n_cases"]))]
+    for (o, v, seed, frac) in ((8, 32, 4, 0.05), (6, 30, 5, 0.2)):
+        sys_ = SyntheticSystem(o, v, 8 * (o + v), 0.05, seed)
+        x = sys_.mp2_amplitudes()[1]
+        xs.append((np.ascontiguousarray(x), int(frac * x.size)))
+    out = {"n_cases": np.int64(len(xs))}
+    for k, (x, m) in enumerate(xs):
+        seed = 500 + k
+        r = ref_pivotal(R, x, m, seed)
+        out[f"c{k}_x"] = x
+        out[f"c{k}_m"] = np.int64(m)
+        out[f"c{k}_seed"] = np.int64(seed)
+        out[f"c{k}_ok"] = np.int64(r is not None)
+        if r is not None:
+            idx, val, used = r
+            out[f"c{k}_idx"], out[f"c{k}_val"], out[f"c{k}_used"] = idx, val, np.int64(used)
     return out
 
 
@@ -293,7 +362,8 @@ def main():
     np.savez_compressed(os.path.join(HERE, "iteration.npz"), **iteration_case(R))
     np.savez_compressed(os.path.join(HERE, "lccsd.npz"), **lccsd_cases(R))
     np.savez_compressed(os.path.join(HERE, "unbiased.npz"), **unbiased_case(R))
-    for f in ("compress.npz", "contract.npz", "iteration.npz", "lccsd.npz", "unbiased.npz"):
+    np.savez_compressed(os.path.join(HERE, "pivotal.npz"), **pivotal_cases(R))
+    for f in ("compress.npz", "contract.npz", "iteration.npz", "lccsd.npz", "unbiased.npz", "pivotal.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

@@ -124,7 +124,9 @@ def test_errors_raise(gpulib):
         py_rccsd.SparseTensor4d(x, x.shape, 17, "fri", "systematic")
     with pytest.raises(ValueError):
         py_rccsd.SparseTensor4d(x, x.shape, 4, "bogus", "systematic")
-    with pytest.raises(NotImplementedError):
-        py_rccsd.SparseTensor4d(x, x.shape, 4, "fri", "pivotal")
+    with pytest.raises(ValueError):
+        py_rccsd.SparseTensor4d(x, x.shape, 4, "fri", "bogus")   # the reference would sample nothing
+    with pytest.raises(ValueError):
+        py_rccsd.SparseTensor4d(x, x.shape, 0, "fri", "pivotal")
     with pytest.raises(TypeError):
         py_rccsd.SparseTensor4d(x.astype(np.float32), x.shape, 4, "fri", "systematic")

@@ -136,3 +136,36 @@ def test_spmm_f2_matches_fp64(gpulib):
         a, b = a.cpu().numpy(), b.cpu().numpy()
         # per-element error relative to the sum of |terms| is ~1e-14; compare to the output scale
         assert np.abs(a - b).max() <= 1e-12 * np.abs(a).max(), np.abs(a - b).max() / np.abs(a).max()
+
+
+def test_split_f2_bits_bound_and_edges(gpulib):
+    """The integer float-pair split: |x - hi - lo| < 2^-47 |x| across the fast
+    range 2^-74 <= |x| < 2^128, exact-float inputs give lo = 0, and zeros,
+    tiny, huge, infinite and NaN inputs follow the conversion path."""
+    from fricc_gb300.rccsd_dense import split_f2
+    rng = np.random.default_rng(9)
+    e = rng.integers(-74, 128, 100000)
+    x = rng.choice([-1.0, 1.0], e.size) * rng.uniform(1.0, 2.0, e.size) * np.exp2(e.astype(np.float64))
+    x[::7] = x[::7].astype(np.float32).astype(np.float64)
+    edge = np.array([0.0, -0.0, 2.0**-74, -2.0**-74, 2.0**-75, 2.0**127 * 1.99, 2.0**128, 1e-300, 5e-324,
+                     np.inf, -np.inf, np.nan, 1.0, -1.0 - 2.0**-52])
+    xs = np.concatenate([x, edge])
+    xs = np.concatenate([xs, [0.0]]) if xs.size % 2 else xs
+    out = split_f2(torch.from_numpy(xs).cuda().view(1, 1, -1), qs=xs.size).cpu().numpy().reshape(-1, 4)
+    hi = np.stack([out[:, 0], out[:, 1]], 1).reshape(-1).astype(np.float64)
+    lo = np.stack([out[:, 2], out[:, 3]], 1).reshape(-1).astype(np.float64)
+    n = x.size
+    err = np.abs(hi[:n] + lo[:n] - x) / np.abs(x)
+    assert err.max() < 2.0**-47
+    assert np.all(lo[:n][::7] == 0.0)
+    with np.errstate(invalid="ignore", over="ignore"):
+        want_hi = edge.astype(np.float32).astype(np.float64)
+        want_lo = (edge - want_hi).astype(np.float32).astype(np.float64)
+    for k, v in enumerate(edge):
+        h, l = hi[n + k], lo[n + k]
+        if np.isnan(v):
+            assert np.isnan(h)
+        elif v == 0.0 or not np.isfinite(v) or abs(v) < 2.0**-74 or abs(v) >= 2.0**128:
+            assert h == want_hi[k] and (l == want_lo[k] or (np.isnan(l) and np.isnan(want_lo[k]))), (v, h, l)
+        else:
+            assert abs(h + l - v) <= 2.0**-47 * abs(v), v

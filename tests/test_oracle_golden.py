@@ -202,3 +202,23 @@ def test_unbiased_golden(oracle):
         it = k - b
         y = g["t2"][k] / it + (it - 1) / it * y
     assert np.array_equal(state["t2_avg"], y)
+
+
+def test_pivotal_golden_bitexact(oracle):
+    """Pivotal sampling (the binding's default, src/fri_utils.cpp:63-127): the
+    oracle, fed the reference's rand() stream, emits the reference's indices
+    and values bit for bit and consumes the same number of draws."""
+    from fricc_gb300.rng import GlibcRand
+    g = golden("pivotal.npz")
+    n = int(g["n_cases"])
+    assert n >= 19
+    for k in range(n):
+        if not int(g[f"c{k}_ok"]):
+            continue
+        x, m, used = g[f"c{k}_x"], int(g[f"c{k}_m"]), int(g[f"c{k}_used"])
+        r = GlibcRand(int(g[f"c{k}_seed"]))
+        draws = np.array([r.uniform() for _ in range(x.size)])
+        t = oracle.SparseTensor4d(x, x.shape, m, "fri", "pivotal", draws=draws)
+        np.testing.assert_array_equal(t.idx4, g[f"c{k}_idx"], err_msg=f"case {k}")
+        assert np.array_equal(t.vals.view(np.int64), g[f"c{k}_val"].view(np.int64)), f"case {k}"
+        assert t.draws_used == used, (k, t.draws_used, used)

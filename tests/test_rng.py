@@ -20,3 +20,21 @@ def test_independent_streams_and_first_draw():
     assert x[0] == 0.8401877171547095  # the first draw after srand(1)
     c = GlibcRand(2)
     assert c.uniform() != x[0]
+
+
+def test_glibc_seeds_edge_and_history_roundtrip():
+    """Seed 0 (glibc uses 1), seeds above 2^31 (stored as negative int32),
+    and a history handed out and back continues the same stream."""
+    libc = ctypes.CDLL(None)
+    for seed in (0, 2**31, 2**32 - 1, 3000000000):
+        g = GlibcRand(seed)
+        libc.srand(ctypes.c_uint(seed))
+        assert [g.rand() for _ in range(200)] == [libc.rand() for _ in range(200)]
+    a, b = GlibcRand(99), GlibcRand(99)
+    for _ in range(57):
+        a.rand()
+        b.rand()
+    h = a.history()
+    c = GlibcRand(1)
+    c.set_history(h)
+    assert [c.rand() for _ in range(100)] == [b.rand() for _ in range(100)]
