@@ -18,10 +18,7 @@ namespace {
 
 constexpr int BK = 16, NT = 256;
 
-__device__ __forceinline__ float2 split(double d) {
-  const float h = __double2float_rn(d);
-  return make_float2(h, __double2float_rn(d - (double)h));
-}
+__device__ __forceinline__ float2 split(double d) { return split_f2_bits(d); }
 
 // two floats in one 64-bit register pair, and the packed f32x2 arithmetic
 // (one issue slot per two lanes of FP32 work)
@@ -78,7 +75,7 @@ struct GemmArgs {
 // product error with one fma).  Rows are padded by one element so that the
 // staging stores do not conflict on banks.
 template <int TM, int TN>
-__global__ void __launch_bounds__(NT) k_gemm_df(GemmArgs g) {
+__global__ void __launch_bounds__(NT, 2) k_gemm_df(GemmArgs g) {
   constexpr int BM = 16 * TM, BN = 16 * TN, NP = BN / 2, JP = TN / 2;
   __shared__ ulonglong2 As[BK][BM + 1];
   __shared__ ulonglong2 Bs[BK][NP + 1];
@@ -100,32 +97,60 @@ __global__ void __launch_bounds__(NT) k_gemm_df(GemmArgs g) {
 
   const bool a_kfast = g.sAk == 1;
   const bool b_nfast = g.sBn == 1;
+  // Operand tiles go global -> registers (raw FP64) -> shared (split): the
+  // loads of tile k+1 are issued before tile k is computed, so their latency
+  // hides behind the arithmetic; the split happens once per element per CTA.
+  constexpr int RA = (BM * BK) / NT, RB = (NP * BK + NT - 1) / NT;
+  double ra[RA], rb0[RB], rb1[RB];
+  auto a_coord = [&](int r, int& mm, int& kk) {
+    const int idx = r * NT + threadIdx.x;
+    if (a_kfast) { mm = idx / BK; kk = idx % BK; } else { kk = idx / BM; mm = idx % BM; }
+  };
+  auto b_coord = [&](int r, int& pp, int& kk) {
+    const int idx = r * NT + threadIdx.x;
+    if (b_nfast) { kk = idx / NP; pp = idx % NP; } else { pp = idx / BK; kk = idx % BK; }
+    return (NP * BK) % NT == 0 || idx < NP * BK;
+  };
+  auto gload = [&](int64_t k0) {
+#pragma unroll
+    for (int r = 0; r < RA; ++r) {
+      int mm, kk;
+      a_coord(r, mm, kk);
+      const int64_t m = m0 + mm, k = k0 + kk;
+      ra[r] = (m < g.M && k < k_end) ? A[m * g.sAm + k * g.sAk] : 0.0;
+    }
+#pragma unroll
+    for (int r = 0; r < RB; ++r) {
+      int pp, kk;
+      const bool on = b_coord(r, pp, kk);
+      const int64_t n = n0 + 2 * pp, k = k0 + kk;
+      const bool kin = on && k < k_end;
+      rb0[r] = (n < g.N && kin) ? B[k * g.sBk + n * g.sBn] : 0.0;
+      rb1[r] = (n + 1 < g.N && kin) ? B[k * g.sBk + (n + 1) * g.sBn] : 0.0;
+    }
+  };
+  gload(k_begin);
   for (int64_t k0 = k_begin; k0 < k_end; k0 += BK) {
     __syncthreads();
 #pragma unroll
-    for (int r = 0; r < (BM * BK) / NT; ++r) {
-      const int idx = r * NT + threadIdx.x;
+    for (int r = 0; r < RA; ++r) {
       int mm, kk;
-      if (a_kfast) { mm = idx / BK; kk = idx % BK; } else { kk = idx / BM; mm = idx % BM; }
-      const int64_t m = m0 + mm, k = k0 + kk;
-      const float2 a = split((m < g.M && k < k_end) ? A[m * g.sAm + k * g.sAk] : 0.0);
+      a_coord(r, mm, kk);
+      const float2 a = split(ra[r]);
       As[kk][mm] = make_ulonglong2(pk2(a.x, a.x), pk2(a.y, a.y));
     }
 #pragma unroll
-    for (int r = 0; r < (NP * BK + NT - 1) / NT; ++r) {
-      const int idx = r * NT + threadIdx.x;
-      if ((NP * BK) % NT == 0 || idx < NP * BK) {
-        int pp, kk;
-        if (b_nfast) { kk = idx / NP; pp = idx % NP; } else { pp = idx / BK; kk = idx % BK; }
-        const int64_t n = n0 + 2 * pp, k = k0 + kk;
-        const bool kin = k < k_end;
-        const float2 b0 = split((n < g.N && kin) ? B[k * g.sBk + n * g.sBn] : 0.0);
-        const float2 b1 = split((n + 1 < g.N && kin) ? B[k * g.sBk + (n + 1) * g.sBn] : 0.0);
+    for (int r = 0; r < RB; ++r) {
+      int pp, kk;
+      if (b_coord(r, pp, kk)) {
+        const float2 b0 = split(rb0[r]);
+        const float2 b1 = split(rb1[r]);
         Bs[kk][pp] = make_ulonglong2(pk2(b0.x, b1.x), pk2(b0.y, b1.y));
         Bn[kk][pp] = pk2(-b0.x, -b1.x);
       }
     }
     __syncthreads();
+    if (k0 + BK < k_end) gload(k0 + BK);
 #pragma unroll 2
     for (int kk = 0; kk < BK; ++kk) {
       ulonglong2 a[TM], b[JP];
@@ -167,13 +192,17 @@ __global__ void __launch_bounds__(NT) k_gemm_df(GemmArgs g) {
     for (int j = 0; j < JP; ++j) {
       const int64_t m = m0 + ty + 16 * i, n = n0 + 2 * (tx + 16 * j);
       const float2 h = upk2(ah[i][j]), l = upk2(al[i][j]);
-      const double acc[2] = {(double)h.x + (double)l.x, (double)h.y + (double)l.y};
+      const double acc[2] = {pair_to_f64(h.x, l.x), pair_to_f64(h.y, l.y)};
 #pragma unroll
       for (int c = 0; c < 2; ++c) {
         if (m < g.M && n + c < g.N) {
           if (g.splits == 1) {
             double* cp = g.C + bz * g.sCb + m * g.sCm + (n + c) * g.sCn;
-            *cp = g.beta == 0.0 ? g.alpha * acc[c] : fma(g.alpha, acc[c], g.beta * *cp);
+            // FP64 work per output kept to one operation in the common cases
+            if (g.beta == 0.0) *cp = g.alpha == 1.0 ? acc[c] : (g.alpha == -1.0 ? -acc[c] : g.alpha * acc[c]);
+            else if (g.beta == 1.0 && g.alpha == 1.0) *cp = *cp + acc[c];
+            else if (g.beta == 1.0 && g.alpha == -1.0) *cp = *cp - acc[c];
+            else *cp = fma(g.alpha, acc[c], g.beta * *cp);
           } else {
             g.part[((bz * g.splits + sp) * g.M + m) * g.N + n + c] = acc[c];
           }
