@@ -24,7 +24,9 @@
 // top 24 significand bits (truncated), lo is the remaining 29-bit field
 // rounded (half up) to 24 bits; both are then normal floats.  Zeros map to
 // (d, 0); anything else (tiny, huge, inf, NaN) takes the conversion path.
-__device__ __forceinline__ float2 split_f2_conv(double d) {
+// kept out of line: if-converted into the fast path, its FP64 instructions
+// would issue (predicated off) for every element
+static __device__ __noinline__ float2 split_f2_conv(double d) {
   const float h = __double2float_rn(d);
   return make_float2(h, __double2float_rn(d - (double)h));
 }
@@ -56,6 +58,8 @@ __device__ __forceinline__ float2 split_f2_bits(double d) {
 // float -> double, exactly, with integer operations (the conversion
 // instruction runs on the slow FP64 unit); zeros, subnormals, inf and NaN
 // take the conversion path.
+static __device__ __noinline__ double f2d_conv(float f) { return (double)f; }
+
 __device__ __forceinline__ double f2d_bits(float f) {
   const unsigned b = __float_as_uint(f);
   const unsigned e = (b >> 23) & 0xffu;
@@ -64,7 +68,7 @@ __device__ __forceinline__ double f2d_bits(float f) {
     return __longlong_as_double((long long)(sgn | ((unsigned long long)(e + 896u) << 52) |
                                             ((unsigned long long)(b & 0x7fffffu) << 29)));
   if ((b & 0x7fffffffu) == 0u) return __longlong_as_double((long long)sgn);
-  return (double)f;
+  return f2d_conv(f);
 }
 
 // hi + lo of a float pair, rounded once to FP64

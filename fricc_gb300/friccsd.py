@@ -417,12 +417,30 @@ class FRICCSDGPU:
     def energy(self, t1, t2):
         return D.ccsd_energy(t1, t2, self.eris)
 
-    def update_amps_host(self, t1_host: np.ndarray, t2_host: np.ndarray, rn=None):
-        """End-to-end step: numpy amplitudes in (copied to HBM), numpy out."""
+    def update_amps_host(self, t1_host: np.ndarray, t2_host: np.ndarray, rn=None, out=None):
+        """End-to-end step: numpy amplitudes in (copied to HBM), numpy out.
+
+        The results are copied into ``out`` (a pair of float64 arrays) when
+        given; otherwise into one of two solver-owned page-locked buffer pairs
+        used in turn, so a result stays valid until the call after next (feed
+        it back as the next input, as the iteration loop does)."""
         t1 = torch.from_numpy(t1_host).to(self.eris.device, non_blocking=True)
         t2 = torch.from_numpy(t2_host).to(self.eris.device, non_blocking=True)
         t1n, t2n = self.update_amps(t1, t2, rn=rn)
-        return t1n.cpu().numpy(), t2n.cpu().numpy()
+        if out is None:
+            bufs = getattr(self, "_host_out", None)
+            if bufs is None or bufs[0][1].shape != t2n.shape:
+                bufs = [(torch.empty(t1n.shape, dtype=t1n.dtype, pin_memory=True),
+                         torch.empty(t2n.shape, dtype=t2n.dtype, pin_memory=True)) for _ in range(2)]
+                self._host_out, self._host_turn = bufs, 0
+            h1, h2 = bufs[self._host_turn]
+            self._host_turn ^= 1
+        else:
+            h1, h2 = torch.from_numpy(out[0]), torch.from_numpy(out[1])
+        h1.copy_(t1n, non_blocking=True)
+        h2.copy_(t2n, non_blocking=True)
+        torch.cuda.current_stream().synchronize()
+        return h1.numpy(), h2.numpy()
 
     def kernel(self, t1=None, t2=None, max_cycle=50, tol=1e-8, tolnormt=1e-6, callback=None):
         """The iteration loop of fricc/friccsd.py:379-456 (no DIIS).
