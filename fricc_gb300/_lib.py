@@ -33,6 +33,7 @@ SIGNATURES = [
     ("fricc_sp_create_pivotal", ctypes.c_int, [_dp, _i64p, _i64, _u32p, _vp, ctypes.POINTER(_vp), _i64p]),
     ("fricc_sp_recompress_pivotal", ctypes.c_int, [_vp, _dp, _u32p, _vp, _i64p]),
     ("fricc_sp_status", ctypes.c_int, [_vp]),
+    ("fricc_sp_recompress_dev", ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, _dp, _vp]),
     ("fricc_sp_create_empty", ctypes.c_int, [_i64p, _i64, _vp, ctypes.POINTER(_vp)]),
     ("fricc_sp_destroy", ctypes.c_int, [_vp]),
     ("fricc_sp_info", ctypes.c_int, [_vp, _i64p, _i64p, _i64p]),
@@ -53,6 +54,8 @@ SIGNATURES = [
     ("fricc_glibc_uniforms", ctypes.c_int, [_u32p, _i64, _dp, _vp]),
     ("fricc_seq_cumsum", ctypes.c_int, [_dp, _i64, _dp, _vp]),
     ("fricc_seq_cumsum_noalloc", ctypes.c_int, [_dp, _i64, _dp, _vp]),
+    ("fricc_stream_create", ctypes.c_int, [ctypes.POINTER(_vp)]),
+    ("fricc_stream_destroy", ctypes.c_int, [_vp]),
     ("fricc_launch_count", ctypes.c_longlong, []),
     ("fricc_prof_enable", None, [ctypes.c_int]),
     ("fricc_prof_read", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
@@ -115,3 +118,25 @@ def hist_arg(rng):
             rng.set_history([h[i] for i in range(31)])
         return h, writeback
     return None, (lambda: None)
+
+
+class OwnStream:
+    """A CUDA stream created for one owner (not taken from torch's shared
+    stream pool), usable as a torch stream; released with the object."""
+
+    def __init__(self, device):
+        import torch
+        self._lib = load()
+        h = ctypes.c_void_p()
+        with torch.cuda.device(device):
+            check(self._lib.fricc_stream_create(ctypes.byref(h)))
+        self.handle = h
+        self.stream = torch.cuda.ExternalStream(h.value, device=device)
+
+    def __del__(self):
+        if getattr(self, "handle", None) is not None and self.handle.value:
+            try:
+                self._lib.fricc_stream_destroy(self.handle)
+            except Exception:
+                pass
+            self.handle = None

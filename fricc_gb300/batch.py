@@ -43,11 +43,13 @@ def mp2_device(E: DeviceERIs):
 
 
 class ReplicaBatch:
-    def __init__(self, eris: DeviceERIs, settings: dict, seeds, n_streams: int = 8, precision: str = "df64"):
+    def __init__(self, eris: DeviceERIs, settings: dict, seeds, n_streams: int = 8, precision: str = "df64",
+                 graph: bool = False):
         self.eris = eris
         self.seeds = list(seeds)
         self.n = len(self.seeds)
-        self.solvers = [FRICCSDGPU(eris, settings, rn_draw=GlibcRand(s), precision=precision) for s in self.seeds]
+        self.solvers = [FRICCSDGPU(eris, settings, rn_draw=GlibcRand(s), precision=precision, graph=graph)
+                        for s in self.seeds]
         t1, t2 = mp2_device(eris)
         self.t1 = [t1.clone() for _ in range(self.n)]
         self.t2 = [t2.clone() for _ in range(self.n)]
@@ -138,7 +140,8 @@ def footprint_bytes(o: int, v: int) -> int:
 
 class SolveServer:
     def __init__(self, n_workers: int = 8, hbm_budget: float = 200e9, precision: str = "df64", max_cycle: int = 30,
-                 tol: float = 1e-7, device="cuda"):
+                 tol: float = 1e-7, device="cuda", graph: bool = False):
+        self.graph = graph
         self.k = n_workers
         self.budget = hbm_budget
         self.precision = precision
@@ -154,7 +157,8 @@ class SolveServer:
         with torch.cuda.stream(stream):
             system = SyntheticSystem(req.nocc, req.nvir, req.naux, req.sigma, req.seed)
             E = DeviceERIs.from_system(system, device=self.device)
-            solver = FRICCSDGPU(E, {"m_keep": req.m}, rn_draw=GlibcRand(req.seed), precision=self.precision)
+            solver = FRICCSDGPU(E, {"m_keep": req.m}, rn_draw=GlibcRand(req.seed), precision=self.precision,
+                                graph=self.graph)
             t1, t2 = mp2_device(E)
             req.started = time.perf_counter() - t0
             eold = solver.energy(t1, t2)

@@ -11,7 +11,7 @@
 
 int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, double rn, cudaStream_t st, int64_t* flat,
                           double* vals, int64_t* n_largest, unsigned* glibc_hist, int64_t* n_draws,
-                          unsigned long long* meta = nullptr);
+                          unsigned long long* meta = nullptr, const double* rn_dev = nullptr);
 int fricc_unpack_async(const int64_t* flat, int64_t m, const int64_t dims[4], int* slots, unsigned long long* meta,
                        cudaStream_t st);
 int fricc_dev_status(unsigned e);
@@ -128,12 +128,9 @@ static void free_sparse_arrays(FriccSparse* T, cudaStream_t st) {
   }
 }
 
-static void drop_bucketings(FriccSparse* T, cudaStream_t st) {
-  for (auto& b : T->buck) {
-    fricc_free(b.bptr, st);
-    fricc_free(b.order, st);
-    b = Bucketing{};
-  }
+// after a re-compression: keep the arrays, rebuild on next use
+static void stale_bucketings(FriccSparse* T) {
+  for (auto& b : T->buck) b.valid = false;
 }
 
 static bool bad_dims(const int64_t dims[4]) {
@@ -188,7 +185,8 @@ static int settle(const fricc_sparse* Tc) {
   cudaError_t e = cudaMemcpyAsync(h, T->meta, sizeof(h), cudaMemcpyDeviceToHost, T->owner_stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(T->owner_stream);
   if (e != cudaSuccess) return fricc_cuda_fail(e, "compression status", __FILE__, __LINE__);
-  T->pending = false;
+  // pending stays set: a re-compression replayed from a CUDA graph rewrites
+  // the block without passing through the host
   T->n_largest = (int64_t)h[0];
   T->status = fricc_dev_status((unsigned)h[1]);
   return T->status;
@@ -198,9 +196,9 @@ static int settle(const fricc_sparse* Tc) {
 // Modes 0 and 1 only enqueue work: |D| and any error are read back by the
 // next blocking call on the handle (settle).
 static int recompress(fricc_sparse* T, const double* t2, int mode, double rn, unsigned* hist, int64_t* n_draws,
-                      void* stream) {
+                      void* stream, const double* rn_dev = nullptr) {
   cudaStream_t st = as_stream(stream);
-  drop_bucketings(T, st);
+  stale_bucketings(T);
   const int64_t n = T->dims[0] * T->dims[1] * T->dims[2] * T->dims[3];
   T->owner_stream = st;
   T->pending = false;
@@ -213,7 +211,7 @@ static int recompress(fricc_sparse* T, const double* t2, int mode, double rn, un
     T->n_largest = nd;
     return fricc_unpack_device(T->flat, T->m, T->dims, T->slots, st);
   }
-  int rc = fricc_compress_device(t2, n, T->m, mode, rn, st, T->flat, T->vals, nullptr, hist, n_draws, T->meta);
+  int rc = fricc_compress_device(t2, n, T->m, mode, rn, st, T->flat, T->vals, nullptr, hist, n_draws, T->meta, rn_dev);
   if (!rc) rc = fricc_unpack_async(T->flat, T->m, T->dims, T->slots, T->meta, st);
   if (!rc) T->pending = true;
   return rc;
@@ -246,6 +244,24 @@ int fricc_sp_recompress(fricc_sparse* T, const double* t2, int compression, int 
     return FRICC_ERR_ARG;
   }
   return recompress(T, t2, compression == FRICC_COMPRESSION_LARGEST ? 1 : 0, rn, nullptr, nullptr, stream);
+}
+
+int fricc_sp_recompress_dev(fricc_sparse* T, const double* t2, int compression, int sampling, const double* rn_dev,
+                            void* stream) {
+  if (!T || !t2 || (compression == FRICC_COMPRESSION_FRI && !rn_dev)) {
+    fricc_set_error("sp_recompress_dev: null argument");
+    return FRICC_ERR_ARG;
+  }
+  if (compression != FRICC_COMPRESSION_FRI && compression != FRICC_COMPRESSION_LARGEST) {
+    fricc_set_error("The compression method you chose isn't supported: compression must be 'largest' or 'fri'");
+    return FRICC_ERR_ARG;
+  }
+  if (compression == FRICC_COMPRESSION_FRI && sampling != FRICC_SAMPLING_SYSTEMATIC) {
+    fricc_set_error("sp_recompress_dev: systematic sampling only (pivotal draws per element)");
+    return FRICC_ERR_ARG;
+  }
+  return recompress(T, t2, compression == FRICC_COMPRESSION_LARGEST ? 1 : 0, 0.0, nullptr, nullptr, stream,
+                    compression == FRICC_COMPRESSION_FRI ? rn_dev : nullptr);
 }
 
 int fricc_sp_recompress_pivotal(fricc_sparse* T, const double* t2, uint32_t* glibc_hist, void* stream,
@@ -485,6 +501,22 @@ int fricc_compress_pivotal(const double* x, int64_t n, int64_t m, uint32_t* glib
     return FRICC_ERR_ARG;
   }
   return fricc_compress_device(x, n, m, 2, 0.0, as_stream(stream), flat, vals, n_largest, glibc_hist, n_draws);
+}
+
+int fricc_stream_create(void** out) {
+  if (!out) {
+    fricc_set_error("stream_create: null argument");
+    return FRICC_ERR_ARG;
+  }
+  cudaStream_t s = nullptr;
+  FRICC_CUDA(cudaStreamCreateWithFlags(&s, cudaStreamNonBlocking));
+  *out = (void*)s;
+  return FRICC_OK;
+}
+
+int fricc_stream_destroy(void* stream) {
+  if (stream) FRICC_CUDA(cudaStreamDestroy(as_stream(stream)));
+  return FRICC_OK;
 }
 
 int fricc_glibc_uniforms(uint32_t* hist, int64_t k, double* out, void* stream) {

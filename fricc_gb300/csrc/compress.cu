@@ -689,7 +689,7 @@ static int pivotal(const double* x, int64_t n, int64_t m, const GenP& gp, Ctl* c
 // in stream order, so a caller that passes n_largest == nullptr never waits.
 int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, double rn, cudaStream_t st,
                           int64_t* flat, double* vals, int64_t* n_largest, unsigned* glibc_hist, int64_t* n_draws,
-                          unsigned long long* meta) {
+                          unsigned long long* meta, const double* rn_dev) {
   if (n < 0 || m <= 0 || m > n) {
     fricc_set_error("Bad m_keep value: need 0 < m <= tensor size (m=%lld, size=%lld)", (long long)m,
                     (long long)n);
@@ -725,7 +725,10 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     TRY(fricc_cuda_check(cudaMemsetAsync(s.tstate, 0, ntile * sizeof(unsigned long long), st), "memset"));
     TRY(fricc_cuda_check(cudaMemsetAsync(s.ticket, 0, sizeof(unsigned), st), "memset"));
     TRY(fricc_cuda_check(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st), "memset"));
-    {
+    if (rn_dev) {
+      // the draw already in device memory (stream-ordered; capturable)
+      TRY(fricc_cuda_check(cudaMemcpyAsync(&ctl->rn, rn_dev, sizeof(double), cudaMemcpyDeviceToDevice, st), "rn"));
+    } else {
       // the draw goes through a device word (a pageable-source copy completes
       // before cudaMemcpyAsync returns, so a stack value is safe)
       const double rn_h = rn;

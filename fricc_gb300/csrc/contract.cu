@@ -194,11 +194,10 @@ __device__ __forceinline__ f32x2 fma2(f32x2 a, f32x2 b, f32x2 c) {
   return d;
 }
 
-constexpr int DF_NT = 128;  // threads per CTA
-constexpr int DF_PPT = 2;   // q-pairs per thread: a CTA covers 512 outputs of a row
+constexpr int DF_NT = 128;  // threads per CTA; PPT q-pairs per thread, so a CTA covers 256 PPT outputs of a row
 
-// one staged chunk of terms into the thread's DF_PPT accumulator pairs
-template <bool FULL>
+// one staged chunk of terms into the thread's PPT accumulator pairs
+template <int DF_PPT, bool FULL>
 __device__ __forceinline__ void df_tile(const int* __restrict__ srow, const ulonglong2* __restrict__ sv,
                                         const f32x2* __restrict__ snv, int cnt, const ulonglong2* __restrict__ wq,
                                         int64_t QS2, int64_t trem, f32x2* ah, f32x2* al) {
@@ -225,6 +224,7 @@ __device__ __forceinline__ void df_tile(const int* __restrict__ srow, const ulon
   }
 }
 
+template <int DF_PPT>
 __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr, const int* __restrict__ erow,
                                                    const float2* __restrict__ eval, const float4* __restrict__ Wp4,
                                                    double* __restrict__ Op, int64_t QS) {
@@ -259,8 +259,8 @@ __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr,
       snv[threadIdx.x] = pk2(-v.x, -v.x);
     }
     __syncthreads();
-    if (full) df_tile<true>(srow, sv, snv, cnt, wq, QS2, trem, ah, al);
-    else df_tile<false>(srow, sv, snv, cnt, wq, QS2, trem, ah, al);
+    if (full) df_tile<DF_PPT, true>(srow, sv, snv, cnt, wq, QS2, trem, ah, al);
+    else df_tile<DF_PPT, false>(srow, sv, snv, cnt, wq, QS2, trem, ah, al);
     // renormalise once per staged chunk (<= DF_NT terms): keeps |al| ~ ulp(ah)
 #pragma unroll
     for (int k = 0; k < DF_PPT; ++k) {
@@ -345,19 +345,29 @@ bool is_contig_perm(const int64_t dims[4], const int64_t strides[4], const int p
 
 double fricc_contract_flops_impl(const char* term, const FriccSparse* T);
 
+// A re-compression keeps every bucketing's arrays (m and dims do not change)
+// and only marks it stale; it is rebuilt in place on first use, so a steady
+// iteration allocates nothing that outlives it (which also keeps it
+// capturable in a CUDA graph).
 int fricc_sparse_bucketing(FriccSparse* T, int pa, int pb, cudaStream_t st, Bucketing** out) {
-  for (auto& b : T->buck)
-    if (b.pa == pa && b.pb == pb && b.bptr) {
-      *out = &b;
-      return FRICC_OK;
-    }
   Bucketing* slot = nullptr;
   for (auto& b : T->buck)
-    if (!b.bptr) {
+    if (b.pa == pa && b.pb == pb && b.bptr) {
+      if (b.valid) {
+        *out = &b;
+        return FRICC_OK;
+      }
       slot = &b;
       break;
     }
+  if (!slot)
+    for (auto& b : T->buck)
+      if (!b.bptr) {
+        slot = &b;
+        break;
+      }
   if (!slot) return FRICC_ERR_ARG;
+  const bool fresh = slot->bptr == nullptr;
   const int64_t m = T->m;
   const int64_t nb = T->dims[pa] * T->dims[pb];
   int bits = 8;
@@ -368,8 +378,8 @@ int fricc_sparse_bucketing(FriccSparse* T, int pa, int pb, cudaStream_t st, Buck
   if (!rc) rc = fricc_alloc_t(&ktmp, m, st);
   if (!rc) rc = fricc_alloc_t(&vtmp, m, st);
   if (!rc) rc = fricc_alloc_t(&hist, radix::hist_words(m), st);
-  if (!rc) rc = fricc_alloc_t(&slot->order, m, st);
-  if (!rc) rc = fricc_alloc_t(&slot->bptr, nb + 1, st);
+  if (!rc && fresh) rc = fricc_alloc_t(&slot->order, m, st);
+  if (!rc && fresh) rc = fricc_alloc_t(&slot->bptr, nb + 1, st);
   if (!rc) {
     k_pair_keys<<<grid_for(m, 256), 256, 0, st>>>(T->slots, m, pa, pb, T->dims[pb], keys, slot->order);
     rc = radix::sort_pairs(keys, slot->order, ktmp, vtmp, m, bits, false, hist, st);
@@ -395,6 +405,7 @@ int fricc_sparse_bucketing(FriccSparse* T, int pa, int pb, cudaStream_t st, Buck
   slot->pa = pa;
   slot->pb = pb;
   slot->nbuckets = nb;
+  slot->valid = true;
   *out = slot;
   return FRICC_OK;
 }
@@ -543,7 +554,11 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
   float2* eval = nullptr;
   rc = fricc_alloc_t(&erow, T->m, st);
   if (!rc) rc = fricc_alloc_t(&eval, T->m, st);
-  const int64_t ntq = fricc_cdiv((QS + 1) / 2, DF_NT * DF_PPT);
+  // 2 q-pairs per thread: measured against 1 and 4 on the o30v150 terms
+  // (fewer leaves loads too few per thread, more costs occupancy)
+  const int64_t QS2 = (QS + 1) / 2;
+  constexpr int ppt = 2;
+  const int64_t ntq = fricc_cdiv(QS2, DF_NT * ppt);
   if (!rc && (ntq > 65535 || bk->nbuckets > 0x7fffffffLL)) {
     fricc_set_error("spmm_f2: problem too large for one launch");
     rc = FRICC_ERR_ARG;
@@ -553,7 +568,8 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
                                                       erow, eval);
     const bool prof = fricc_prof_on();
     if (prof) fricc_prof_record(st, true, 0.0);
-    k_spmm_df<<<dim3((unsigned)bk->nbuckets, (unsigned)ntq), DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS);
+    const dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq);
+    k_spmm_df<ppt><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS);
     if (prof) fricc_prof_record(st, false, 2.0 * (double)T->m * (double)QS);
     fricc_note_launch(2);
     cudaError_t e = cudaGetLastError();

@@ -12,6 +12,7 @@ struct Bucketing {
   int64_t nbuckets = 0;
   int* bptr = nullptr;       // [nbuckets + 1]
   unsigned* order = nullptr; // [m]
+  bool valid = false;        // false after a re-compression: rebuilt in place on next use
 };
 
 struct FriccSparse {
@@ -21,7 +22,7 @@ struct FriccSparse {
   // Written by the device at the end of an asynchronous compression and read
   // back at the next blocking call on the handle: [0] |D|, [1] error bits.
   unsigned long long* meta = nullptr;
-  bool pending = false;     // meta holds a result not yet read back
+  bool pending = false;     // the status lives in meta (asynchronous compressions)
   int status = 0;           // status of the last compression once read back
   int64_t* flat = nullptr;  // [m] flat C-order index into the dense tensor
   double* vals = nullptr;   // [m]

@@ -30,6 +30,7 @@ host amplitudes out, the copies included.
 from __future__ import annotations
 
 import ctypes
+import threading
 import time
 
 import numpy as np
@@ -40,6 +41,7 @@ from . import rccsd_dense as D
 from .py_rccsd import libc_uniform
 
 ALLOWED_CONTRACTIONS = ("O^2V^4", "O^3V^3", "O^4V^2")
+_CAPTURE_LOCK = threading.Lock()
 DEFAULT_SETTINGS = {
     "m_keep": 1000,
     "compression": "fri",
@@ -97,6 +99,14 @@ class _Handle:
             self.key = key
         return self.h
 
+    def compress_dev(self, t2, m, compression, rn_ptr, stream):
+        """Re-compress an existing handle with the draw read from device memory
+        (rn_ptr): stream-ordered work only, capturable in a CUDA graph."""
+        if not self.h.value or self.key != (tuple(t2.shape), int(m)):
+            raise RuntimeError("compress_dev needs a handle created for this shape")
+        L.check(L.load().fricc_sp_recompress_dev(self.h, _ptr(t2), L.COMPRESSION[compression], 0, rn_ptr, stream))
+        return self.h
+
     def compress_pivotal(self, t2, m, rng, stream):
         """Pivotal FRI compression drawing from rng (GlibcRand: on the device;
         the process's rand() otherwise)."""
@@ -126,7 +136,7 @@ class _Handle:
 
 class FRICCSDGPU:
     def __init__(self, eris: D.DeviceERIs, fri_settings=None, level_shift=0.0, rn_draw=libc_uniform,
-                 wvvvv_t1t1="reference", precision="fp64"):
+                 wvvvv_t1t1="reference", precision="fp64", graph=False):
         s = dict(DEFAULT_SETTINGS)
         s.update(fri_settings or {})
         for c in s["compressed_contractions"]:
@@ -148,7 +158,14 @@ class FRICCSDGPU:
             eris.prepare_splits()
         self._sp = _Handle()
         self._sp_w = _Handle()
-        self._side = torch.cuda.Stream(device=eris.device)
+        # streams of this solver alone (torch's pool hands the same few streams
+        # to everyone, which would tie solvers on different threads together)
+        self._side_owner = L.OwnStream(eris.device)
+        self._side = self._side_owner.stream
+        self.graph = bool(graph)
+        self._g = None
+        self._g_key = None
+        self._cap = None
         self._res = torch.zeros(4, dtype=torch.float64, device=eris.device)
         self._wT = None
         self._iter = 0
@@ -178,7 +195,60 @@ class FRICCSDGPU:
             L.check(self.lib.fricc_spmm(T, pa, pb, ka, kb, float(coef), _ptr(Wp), int(QS), _ptr(Op), stream))
 
     def update_amps(self, t1, t2, rn=None, t1_old=None, t2_old=None):
-        """One iteration on device tensors; returns (t1new, t2new).
+        """One iteration on device tensors; returns (t1new, t2new).  With
+        ``graph=True`` (and systematic or "largest" compression, no unbiased
+        averaging) the iteration after the first is captured once into a CUDA
+        graph and replayed: the host work per iteration drops to a few copies
+        and one launch, and the results are the same as eager execution."""
+        s = self.settings
+        if (self.graph and t1_old is None and t2_old is None and not s.get("unbiased", False)
+                and not (s["compression"] == "fri" and s["sampling_method"] == "pivotal")
+                and self._sp.h.value):
+            return self._update_graph(t1, t2, rn)
+        return self._update_eager(t1, t2, rn, t1_old, t2_old)
+
+    def _update_graph(self, t1, t2, rn):
+        s = self.settings
+        comp = s["compressed_contractions"]
+        need_w = "O^3V^3" in comp or "O^4V^2" in comp
+        if rn is None:
+            rn = [self.rn_draw() if s["compression"] == "fri" else 0.0 for _ in range(2 if need_w else 1)]
+        key = (tuple(t1.shape), tuple(t2.shape))
+        if self._g is None or self._g_key != key:
+            dev = t2.device
+            self._gs_t1 = t1.contiguous().clone()
+            self._gs_t2 = t2.contiguous().clone()
+            self._rn_dev = torch.zeros(2, dtype=torch.float64, device=dev)
+            # each solver captures on its own stream, without the device-wide
+            # synchronisation torch.cuda.graph() performs (other host threads
+            # may be replaying or capturing their own solvers meanwhile);
+            # captures themselves are serialised
+            cur = torch.cuda.current_stream()
+            if self._cap is None:
+                self._cap_owner = L.OwnStream(dev)
+                self._cap = self._cap_owner.stream
+            g = torch.cuda.CUDAGraph()
+            with _CAPTURE_LOCK:
+                self._cap.wait_stream(cur)
+                with torch.cuda.stream(self._cap):
+                    g.capture_begin(capture_error_mode="thread_local")
+                    try:
+                        out = self._update_eager(self._gs_t1, self._gs_t2, None, None, None, rn_dev=self._rn_dev)
+                    finally:
+                        g.capture_end()
+                cur.wait_stream(self._cap)
+            self._g, self._g_key, self._g_out = g, key, out
+        self._rn_dev.copy_(torch.tensor(list(rn) + [0.0] * (2 - len(rn)), dtype=torch.float64))
+        if t1.data_ptr() != self._gs_t1.data_ptr():
+            self._gs_t1.copy_(t1)
+        if t2.data_ptr() != self._gs_t2.data_ptr():
+            self._gs_t2.copy_(t2)
+        self._g.replay()
+        self._iter += 1
+        return self._g_out[0].clone(), self._g_out[1].clone()
+
+    def _update_eager(self, t1, t2, rn=None, t1_old=None, t2_old=None, rn_dev=None):
+        """One iteration, every kernel launched from the host.
 
         rn: the two uniform draws (compression #1, #2); default rn_draw().
         After the call, read_energy() gives E_corr(t1new, t2new) and the step
@@ -209,23 +279,27 @@ class FRICCSDGPU:
         ein = torch.einsum
         need_w = "O^3V^3" in comp or "O^4V^2" in comp
         piv = s["compression"] == "fri" and s["sampling_method"] == "pivotal"
-        if rn is None:
+        if rn is None and rn_dev is None:
             kind = s["compression"]
             rn = [self.rn_draw() if kind == "fri" and not piv else 0.0 for _ in range(2 if need_w else 1)]
         # both compressions run on a side stream, overlapping the dense work
         # below; the sparse terms wait for them
+        # (t2 needs no record_stream on the side stream: the main stream waits
+        # for the side stream below, before anything the caller can free
+        # or allocate after this call)
         main, side = torch.cuda.current_stream(), self._side
-        ev_in = torch.cuda.Event()
-        ev_in.record(main)
-        side.wait_event(ev_in)
-        t2.record_stream(side)
+        side.wait_stream(main)
         with torch.cuda.stream(side):
             sst = ctypes.c_void_p(side.cuda_stream)
-            T = _compress(self._sp, t2, m, s, rn[0], self.rn_draw, sst)
-            Tw = _compress(self._sp_w, self._w_source(t2), m, s, rn[1], self.rn_draw, sst) if need_w else None
-            ev_c = torch.cuda.Event()
-            ev_c.record(side)
-        self._iter += 1
+            if rn_dev is not None:  # captured: draws from device memory, handles exist
+                T = self._sp.compress_dev(t2, m, s["compression"], ctypes.c_void_p(rn_dev.data_ptr()), sst)
+                Tw = self._sp_w.compress_dev(t2, m, s["compression"], ctypes.c_void_p(rn_dev.data_ptr() + 8),
+                                             sst) if need_w else None
+            else:
+                T = _compress(self._sp, t2, m, s, rn[0], self.rn_draw, sst)
+                Tw = _compress(self._sp_w, self._w_source(t2), m, s, rn[1], self.rn_draw, sst) if need_w else None
+        if rn_dev is None:
+            self._iter += 1
 
         mm = D.gemm_df if self.precision == "df64" else D.gemm_torch
         ein2 = D.einsum_df if self.precision == "df64" else torch.einsum   # two-operand O^3V^2 contractions
@@ -277,7 +351,7 @@ class FRICCSDGPU:
         Loo.diagonal().sub_(e_o)
         Lvv.diagonal().sub_(e_v)
 
-        main.wait_event(ev_c)  # the compressed tensors from here on
+        main.wait_stream(side)  # the compressed tensors from here on
         if "O^4V^2" in comp:  # sparse_cc_Woooo (:309-322)
             Wo = (ein2("lcki,jc->klij", E.ovoo, t1) + ein2("kclj,ic->klij", E.ovoo, t1)).permute(2, 3, 0, 1)
             Wo = Wo.contiguous()                                                  # [i,j,k,l]

@@ -32,7 +32,7 @@ def run_replicas(args):
     E = DeviceERIs.from_system(system)
     settings = {"m_keep": w["m"]}
     seeds = [1000 + r for r in range(args.replicas)]
-    batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision)
+    batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision, graph=args.graph)
     for _ in range(args.warmup):
         batch.step()
     torch.cuda.synchronize()
@@ -43,18 +43,18 @@ def run_replicas(args):
     dt = time.perf_counter() - t
     mean, var = batch.stats()
     return {"mode": "replicas", "workload": "o20v100: nocc=20 nvir=100 naux=600 m=200000 per replica",
-            "replicas": args.replicas, "streams": args.streams, "precision": args.precision,
+            "replicas": args.replicas, "streams": args.streams, "precision": args.precision, "graph": args.graph,
             "iterations_per_s": args.replicas * args.steps / dt, "batch_steps_per_s": args.steps / dt,
             "e_corr_mean": mean, "e_corr_var": var, "iterations_each": args.warmup + args.steps}
 
 
 def run_serve(args):
     reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
-    server = SolveServer(n_workers=args.streams, precision=args.precision, max_cycle=args.max_cycle)
+    server = SolveServer(n_workers=args.streams, precision=args.precision, max_cycle=args.max_cycle, graph=args.graph)
     out = server.run(reqs, time_scale=1.0)
     served = latency_summary(out)
     line = {"mode": "serve", "requests": args.requests, "rate_per_s": args.rate, "workers": args.streams,
-            "precision": args.precision, "max_cycle": args.max_cycle, "served": served}
+            "precision": args.precision, "max_cycle": args.max_cycle, "graph": args.graph, "served": served}
     if args.plain:
         # the same requests, one at a time, FP64, arriving all at once
         plain_reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
@@ -84,6 +84,7 @@ def main():
     p.add_argument("--nocc-max", type=int, default=30)
     p.add_argument("--max-cycle", type=int, default=30)
     p.add_argument("--plain", action="store_true")
+    p.add_argument("--graph", action="store_true", help="replay each solver's iteration from a CUDA graph")
     args = p.parse_args()
     line = run_replicas(args) if args.mode == "replicas" else run_serve(args)
     print(json.dumps(line))

@@ -80,6 +80,14 @@ int fricc_sp_create(const double* t2, const int64_t dims[4], int64_t m, int comp
  * asynchronous like fricc_sp_create. */
 int fricc_sp_recompress(fricc_sparse* T, const double* t2, int compression, int sampling, double rn, void* stream);
 
+/* fricc_sp_recompress with the uniform draw read from device memory
+ * (rn_dev, one double; unused for "largest"), so that the whole call is
+ * stream-ordered device work: with the handle created (and its bucketings
+ * built) beforehand, it allocates only scratch that it frees again, and can
+ * be captured into a CUDA graph.  Systematic or "largest" only. */
+int fricc_sp_recompress_dev(fricc_sparse* T, const double* t2, int compression, int sampling, const double* rn_dev,
+                            void* stream);
+
 /* Wait for the handle's last compression and return its status (FRICC_OK,
  * FRICC_ERR_P_GT_ONE, FRICC_ERR_TIMEOUT, FRICC_ERR_INDEX).  No reference
  * counterpart: the reference exits inside the constructor. */
@@ -219,6 +227,13 @@ int fricc_energy_update(const double* t1num, const double* t2num, const double* 
 int fricc_energy_update_lin(const double* t1num, const double* t2num, const double* eia, const double* fov,
                             const double* ovov, const double* t1old, const double* t2old, int64_t nocc,
                             int64_t nvir, double* t1out, double* t2out, double* res, void* stream);
+
+/* A dedicated non-blocking stream of the current device, and its release
+ * (no reference counterpart).  Solvers that overlap or capture work need
+ * streams no other solver shares; torch's own streams come from a small
+ * shared pool. */
+int fricc_stream_create(void** out);
+int fricc_stream_destroy(void* stream);
 
 /* Instrumentation (no reference counterpart): the number of kernels this
  * library has launched so far; and CUDA-event timing of every sparse
