@@ -44,9 +44,10 @@ METRIC = "FRI-CCSD iter/s and solves/s at |ΔEcorr|≤1e-6 Eh vs plain GPU; p50/
 # and MEASURED_PEAKS.json has no FP64 figure.
 FP64_PEAK_TFLOPS = 1.2557
 FP32_PEAK_TFLOPS = 74.2
-# DRAM bytes per k_spmm launch from the ncu capture summarised in
-# profiles/k_spmm_o30v150.md (None until captured).
-SPMM_TRAFFIC = {}
+# DRAM bytes (read + write) per k_spmm_df launch, df64, from one ncu capture
+# of an o30v150 iteration's ten launches (profiles/k_spmm_df_traffic_o30v150.md):
+# 54.30 GB in total, of which 36.1 GB in the 2323 launch and 13.9 GB in X/Y.
+SPMM_TRAFFIC = {"o30v150": 5.43e9}
 
 
 def parse():
@@ -308,7 +309,7 @@ def run_gpu(args):
     roof = {"kernel": kname, "bound": bound,
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None,
-            "traffic": SPMM_TRAFFIC.get(args.workload),
+            "traffic": SPMM_TRAFFIC.get(args.workload) if args.precision != "fp64" else None,
             "launches": int(p_n.value), "kernel_ms": p_ms.value,
             "kernel_share_of_step": p_ms.value / ms if ms > 0 else None,
             "peak_source": psrc}
@@ -322,7 +323,8 @@ def run_gpu(args):
             "config": {"workload": f"{args.workload}: nocc={o} nvir={v} naux={w['naux']} sigma={w['sigma']} "
                                    f"m={m} FRI systematic, 2 compressions/iteration, FP64",
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": "working set > L2 ((ac|bd) 4.05 GB streamed by the O^2V^4 term every step)",
+                       "l2": f"working set > L2 ((ac|bd) {8 * v ** 4 / 1e9:.2f} GB and its float-pair copy "
+                             "streamed by the O^2V^4 term every step)",
                        "precision": args.precision},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
             "clocks": clk.summary(), "energy_last": energies[-1],

@@ -52,6 +52,7 @@ SIGNATURES = [
     ("fricc_compress", ctypes.c_int, [_dp, _i64, _i64, ctypes.c_int, ctypes.c_double, _dp, _dp, _i64p, _vp]),
     ("fricc_compress_pivotal", ctypes.c_int, [_dp, _i64, _i64, _u32p, _dp, _dp, _i64p, _i64p, _vp]),
     ("fricc_glibc_uniforms", ctypes.c_int, [_u32p, _i64, _dp, _vp]),
+    ("fricc_parallel_sample", ctypes.c_int, [_dp, _i64, _i64, ctypes.c_int, _u32p, _dp, _i64p, _vp]),
     ("fricc_seq_cumsum", ctypes.c_int, [_dp, _i64, _dp, _vp]),
     ("fricc_seq_cumsum_noalloc", ctypes.c_int, [_dp, _i64, _dp, _vp]),
     ("fricc_stream_create", ctypes.c_int, [ctypes.POINTER(_vp)]),

@@ -15,6 +15,8 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
 int fricc_unpack_async(const int64_t* flat, int64_t m, const int64_t dims[4], int* slots, unsigned long long* meta,
                        cudaStream_t st);
 int fricc_dev_status(unsigned e);
+int fricc_parallel_sample_device(const double* q, int64_t n, int64_t n_sample, int T, unsigned* glibc_hist,
+                                 int64_t* S_out, int64_t* n_draws, cudaStream_t st);
 int fricc_glibc_uniforms_device(unsigned* hist, int64_t k, double* out, cudaStream_t st);
 int fricc_seq_cumsum_device(const double* x, int64_t n, double* out, cudaStream_t st);
 int fricc_unpack_device(const int64_t* flat, int64_t m, const int64_t dims[4], int* slots, cudaStream_t st);
@@ -517,6 +519,11 @@ int fricc_stream_create(void** out) {
 int fricc_stream_destroy(void* stream) {
   if (stream) FRICC_CUDA(cudaStreamDestroy(as_stream(stream)));
   return FRICC_OK;
+}
+
+int fricc_parallel_sample(const double* q, int64_t n, int64_t n_sample, int chunks, uint32_t* glibc_hist,
+                          int64_t* S, int64_t* n_draws, void* stream) {
+  return fricc_parallel_sample_device(q, n, n_sample, chunks, glibc_hist, S, n_draws, as_stream(stream));
 }
 
 int fricc_glibc_uniforms(uint32_t* hist, int64_t k, double* out, void* stream) {

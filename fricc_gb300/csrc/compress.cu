@@ -21,6 +21,7 @@
 //   6. output D in sorted order then S ascending, values x_D and x_S/p_S.
 #include <cmath>
 #include <cstdlib>
+#include <cstring>
 #include <vector>
 
 #include "exactsum.cuh"
@@ -616,6 +617,173 @@ static int dev_status(unsigned e) {
 // with n_largest == nullptr it returns at once (nothing read back).
 int fricc_glibc_uniforms_device(unsigned* hist, int64_t k, double* out, cudaStream_t st);
 
+// ---------------------------------------------------------------------------
+// parallel_sample (src/fri_utils.cpp:176-362): T chunks sampled pivotally,
+// each walked by its own warp.  Per chunk (one block of 32): the reference's
+// adjustment of the chunk's probabilities towards its integer count g (a
+// running FP64 sum with a break; the per-element y is formed by every lane
+// in parallel, only the running sum is sequential), then the pivotal weight
+// walk of k_piv_chain on the adjusted probabilities.
+struct SegInfo {
+  int64_t lo, len;   // chunk position and length in q
+  double t, a, qn;   // frac(a), a, the chunk's norm
+  int64_t g;         // samples the chunk must give
+};
+
+__global__ void __launch_bounds__(32) k_seg_chain(const SegInfo* __restrict__ seg, double* __restrict__ P,
+                                                  double* __restrict__ A, unsigned char* __restrict__ code,
+                                                  Ctl* __restrict__ ctl) {
+  const SegInfo sg = seg[blockIdx.x];
+  Ctl* c = ctl + blockIdx.x;
+  double* p = P + sg.lo;
+  const int lane = threadIdx.x;
+  const double gd = (double)sg.g;
+  // 1. the adjustment (fri_utils.cpp:297-328): p_i <- y_i until the running sum
+  //    crosses g, the crossing element taking the remainder
+  const int mode = gd > sg.a ? 1 : (gd < sg.a ? -1 : 0);
+  if (mode != 0) {
+    double sj = sg.qn;
+    bool done = false;
+    for (int64_t i0 = 0; i0 < sg.len && !done; i0 += 32) {
+      const int64_t i = i0 + lane;
+      const double q = i < sg.len ? p[i] : 0.0;
+      double y;
+      if (mode > 0) {
+        const double r = __ddiv_rn(q, sg.t);
+        y = r < 1.0 ? r : 1.0;            // std::min(1., r): 1 unless r < 1 (NaN -> 1)
+      } else {
+        const double r = __ddiv_rn(__dsub_rn(q, sg.t), __dsub_rn(1.0, sg.t));
+        y = 0.0 < r ? r : 0.0;            // std::max(0., r): r if 0 < r (NaN -> 0)
+      }
+      const double d = __dsub_rn(y, q);
+      double myv = y;
+      int hit = 32;
+#pragma unroll
+      for (int t = 0; t < 32; ++t) {
+        const double dt = __shfl_sync(0xffffffffu, d, t);
+        const double yt = __shfl_sync(0xffffffffu, y, t);
+        if (i0 + t < sg.len && hit == 32) {
+          sj = __dadd_rn(sj, dt);
+          if (mode > 0 ? sj >= gd : sj <= gd) {
+            hit = t;
+            if (lane == t) myv = __dsub_rn(__dadd_rn(yt, gd), sj);
+          }
+        }
+      }
+      if (i < sg.len && lane <= hit) p[i] = myv;
+      if (hit < 32) done = true;
+    }
+  }
+  __syncwarp();
+  // 2. the pivotal weight walk over the adjusted chunk (as k_piv_chain)
+  const int64_t n = sg.len, mp = c->mp;
+  double a = n > 0 ? p[0] : 0.0;
+  if (lane == 0 && n > 0) {
+    A[sg.lo] = a;
+    code[sg.lo] = 0;
+  }
+  int64_t cnt = 0, jend = n - 1;
+  int broke = 0;
+  double pn = 1 + lane < n ? p[1 + lane] : 0.0;
+  for (int64_t j0 = 1; j0 < n; j0 += 32) {
+    const double pj = pn;
+    const int64_t jn = j0 + 32 + lane;
+    pn = jn < n ? p[jn] : 0.0;
+    double myA = 0.0;
+    bool myW = false;
+#pragma unroll
+    for (int t = 0; t < 32; ++t) {
+      const double pt = __shfl_sync(0xffffffffu, pj, t);
+      const double sum = __dadd_rn(a, pt);
+      const bool w = !(sum < 1.0);
+      a = w ? __dsub_rn(sum, 1.0) : sum;
+      if (lane == t) {
+        myA = a;
+        myW = w;
+      }
+    }
+    const int64_t j = j0 + lane;
+    const bool valid = j < n;
+    const unsigned wm = __ballot_sync(0xffffffffu, myW && valid);
+    int stop = -1;
+    if (mp == 0) {
+      if (j0 == 1 && !(wm & 1u)) stop = 0;
+    } else if (cnt < mp && cnt + __popc(wm) >= mp) {
+      int64_t r = mp - cnt;
+      for (int b = 0; b < 32; ++b)
+        if (((wm >> b) & 1u) && --r == 0) {
+          stop = b;
+          break;
+        }
+    }
+    if (valid && (stop < 0 || lane <= stop)) {
+      A[sg.lo + j] = myA;
+      code[sg.lo + j] = myW ? PV_EMIT : 0;
+    }
+    if (stop >= 0) {
+      jend = j0 + stop;
+      broke = 1;
+      cnt = mp;
+      break;
+    }
+    cnt += __popc(wm);
+  }
+  if (lane == 0) {
+    c->jend = jend < 0 ? 0 : jend;
+    c->npush = cnt;
+    c->broke = broke;
+  }
+}
+
+__global__ void k_s_to_flat(const unsigned* __restrict__ S, int64_t n, int64_t off, int64_t* __restrict__ out) {
+  for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < n; k += (int64_t)gridDim.x * blockDim.x)
+    out[k] = (int64_t)S[k] + off;
+}
+
+// the reference's sample_pivotal on the host, for the T chunk fractions
+template <class Draw>
+static int host_pivotal(int64_t n_sample, const std::vector<double>& probs, Draw draw, std::vector<int64_t>& S,
+                        int64_t* used) {
+  S.clear();
+  *used = 0;
+  const int64_t n = (int64_t)probs.size();
+  if (n == 0) return n_sample == 0 ? FRICC_OK : FRICC_ERR_PIVOTAL;
+  int64_t i = 0;
+  double a = probs[0];
+  for (int64_t j = 1; j < n; ++j) {
+    a += probs[(size_t)j];
+    const double r = draw();
+    ++*used;
+    if (a < 1.) {
+      if (r < probs[(size_t)j] / a) i = j;
+    } else {
+      a -= 1.;
+      const double pa = (1. - probs[(size_t)j]) / (1. - a);
+      if (pa > 1 || pa < 0) return FRICC_ERR_PIVOTAL;
+      if (r < pa) {
+        S.push_back(i);
+        i = j;
+      } else {
+        S.push_back(j);
+      }
+    }
+    if ((int64_t)S.size() == n_sample) break;
+    if (j == n - 1) {
+      if (std::fabs(a - 1.) < 1e-5) S.push_back(i);
+      else return FRICC_ERR_PIVOTAL;
+    }
+  }
+  return (int64_t)S.size() == n_sample ? FRICC_OK : FRICC_ERR_PIVOTAL;
+}
+
+// glibc's rand() recurrence on a 31-word history (oldest first), on the host
+static double host_glibc_uniform(unsigned* h) {
+  const unsigned w = h[0] + h[28];
+  for (int t = 0; t < 30; ++t) h[t] = h[t + 1];
+  h[30] = w;
+  return (double)(int)(w >> 1) / 2147483647.0;
+}
+
 // Steps of pivotal sampling after D, R and m' are on the device (ctl): the
 // weight walk, the draws, the decisions, the scans; leaves S (m' indices).
 static int pivotal(const double* x, int64_t n, int64_t m, const GenP& gp, Ctl* ctl, CompressScratch& s,
@@ -902,4 +1070,188 @@ int fricc_seq_cumsum_device(const double* x, int64_t n, double* out, cudaStream_
   fricc_free(dzero, st);
   fricc_free(err, st);
   return rc;
+}
+
+// The chunk walks, the chunk draws (in chunk order), the decisions and the
+// scans of each chunk, S assembled in the reference's order.
+static int fricc_parallel_sample_finish(const double* q, int64_t n, int64_t n_sample, std::vector<SegInfo>& seg,
+                                        unsigned* glibc_hist, int64_t* S_out, int64_t* n_draws, int64_t used,
+                                        unsigned* err, cudaStream_t st) {
+  const int T = (int)seg.size();
+  double *P = nullptr, *A = nullptr, *R = nullptr;
+  unsigned char* code = nullptr;
+  unsigned* Sseg = nullptr;
+  SegInfo* dseg = nullptr;
+  Ctl* ctl = nullptr;
+  int64_t *tlast = nullptr, *tcnt = nullptr;
+  std::vector<Ctl> hc((size_t)T);
+  std::vector<int64_t> dbase((size_t)T + 1, 0);
+  unsigned e = 0;
+  int64_t maxlen = 0;
+  for (auto& g : seg) maxlen = g.len > maxlen ? g.len : maxlen;
+  const int64_t ntile_max = fricc_cdiv(maxlen, PV_TILE);
+  int rc = fricc_alloc_t(&P, n, st);
+  if (!rc) rc = fricc_alloc_t(&A, n, st);
+  if (!rc) rc = fricc_alloc_t(&code, n, st);
+  if (!rc) rc = fricc_alloc_t(&Sseg, n_sample > 0 ? n_sample : 1, st);
+  if (!rc) rc = fricc_alloc_t(&dseg, T, st);
+  if (!rc) rc = fricc_alloc_t(&ctl, T, st);
+  if (!rc) rc = fricc_alloc_t(&tlast, ntile_max, st);
+  if (!rc) rc = fricc_alloc_t(&tcnt, ntile_max, st);
+  if (!rc) {
+    for (int j = 0; j < T; ++j) {
+      std::memset(&hc[(size_t)j], 0, sizeof(Ctl));
+      hc[(size_t)j].mp = seg[(size_t)j].g;
+    }
+    cudaError_t ce = cudaMemcpyAsync(P, q, sizeof(double) * n, cudaMemcpyDeviceToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(dseg, seg.data(), sizeof(SegInfo) * T, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(ctl, hc.data(), sizeof(Ctl) * T, cudaMemcpyHostToDevice, st);
+    if (ce == cudaSuccess) {
+      k_seg_chain<<<(unsigned)T, 32, 0, st>>>(dseg, P, A, code, ctl);
+      fricc_note_launch();
+      ce = cudaGetLastError();
+    }
+    if (ce == cudaSuccess) ce = cudaMemcpyAsync(hc.data(), ctl, sizeof(Ctl) * T, cudaMemcpyDeviceToHost, st);
+    if (ce == cudaSuccess) ce = cudaStreamSynchronize(st);
+    if (ce != cudaSuccess) rc = fricc_cuda_fail(ce, "parallel_sample walk", __FILE__, __LINE__);
+  }
+  if (!rc) {
+    // chunk j consumes one draw per element it visits after its first
+    for (int j = 0; j < T; ++j) dbase[(size_t)j + 1] = dbase[(size_t)j] + (seg[(size_t)j].len >= 2 ? hc[(size_t)j].jend : 0);
+    const int64_t total = dbase[(size_t)T];
+    if (total > 0) {
+      rc = fricc_alloc_t(&R, total, st);
+      if (!rc && glibc_hist) {
+        rc = fricc_glibc_uniforms_device(glibc_hist, total, R, st);
+      } else if (!rc) {
+        std::vector<double> h((size_t)total);
+        for (auto& r : h) r = (double)rand() / RAND_MAX;
+        rc = fricc_cuda_check(cudaMemcpyAsync(R, h.data(), sizeof(double) * total, cudaMemcpyHostToDevice, st),
+                              "draws");
+        if (!rc) rc = fricc_cuda_check(cudaStreamSynchronize(st), "draws");
+      }
+    }
+    used += total;
+  }
+  if (!rc) {
+    int64_t lb = 0;
+    for (int j = 0; j < T && !rc; ++j) {
+      const SegInfo& g = seg[(size_t)j];
+      Ctl* cj = ctl + j;
+      const int64_t nt = fricc_cdiv(g.len, PV_TILE);
+      if (hc[(size_t)j].jend > 0)
+        k_piv_decide<<<grid_for(hc[(size_t)j].jend, 256), 256, 0, st>>>(P + g.lo, A + g.lo, code + g.lo,
+                                                                        R + dbase[(size_t)j], cj, err);
+      k_piv_tiles<<<(unsigned)nt, PV_NT, 0, st>>>(code + g.lo, cj, tlast, tcnt);
+      k_piv_carry<<<1, 1024, 0, st>>>(tlast, tcnt, nt, cj);
+      k_piv_emit<<<(unsigned)nt, PV_NT, 0, st>>>(code + g.lo, tlast, tcnt, cj, Sseg + lb);
+      k_piv_final<<<1, 1, 0, st>>>(A + g.lo, g.len, cj, Sseg + lb, err);
+      if (g.g > 0) k_s_to_flat<<<grid_for(g.g, 256), 256, 0, st>>>(Sseg + lb, g.g, g.lo, S_out + lb);
+      fricc_note_launch(6);
+      lb += g.g;
+      rc = fricc_cuda_check(cudaGetLastError(), "parallel_sample");
+    }
+  }
+  if (!rc) rc = fricc_cuda_check(cudaMemcpyAsync(&e, err, sizeof(unsigned), cudaMemcpyDeviceToHost, st), "err");
+  if (!rc) rc = fricc_cuda_check(cudaStreamSynchronize(st), "parallel_sample");
+  if (!rc) rc = dev_status(e);
+  if (!rc && n_draws) *n_draws = used;
+  fricc_free(P, st);
+  fricc_free(A, st);
+  fricc_free(R, st);
+  fricc_free(code, st);
+  fricc_free(Sseg, st);
+  fricc_free(dseg, st);
+  fricc_free(ctl, st);
+  fricc_free(tlast, st);
+  fricc_free(tcnt, st);
+  fricc_free(err, st);
+  return rc;
+}
+
+// parallel_sample with T chunks over q (device, n doubles): S (device, n_sample
+// int64) in the reference's order; draws from glibc_hist (host, advanced) or
+// from this process's rand(), taken in chunk order.  *n_draws: draws used.
+int fricc_parallel_sample_device(const double* q, int64_t n, int64_t n_sample, int T, unsigned* glibc_hist,
+                                 int64_t* S_out, int64_t* n_draws, cudaStream_t st) {
+  if (!q || !S_out || n <= 0 || n_sample < 0 || T < 1 || n < T || n >= 0xffffffffLL) {
+    fricc_set_error("parallel_sample: bad arguments (need 1 <= chunks <= n, n < 2^32)");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t step = n / T;
+  std::vector<SegInfo> seg((size_t)T);
+  std::vector<double> frac((size_t)T);
+  int rc = FRICC_OK;
+  double *d_norm = nullptr, *dzero = nullptr;
+  unsigned* err = nullptr;
+  exact::ChainScratch sc;
+  int64_t used = 0;
+#define PTRY(x)           \
+  do {                    \
+    rc = (x);             \
+    if (rc) goto pdone;   \
+  } while (0)
+  {
+    // norms: exact sequential sums (the reference's one_norm at one thread)
+    PTRY(fricc_alloc_t(&d_norm, T + 1, st));
+    PTRY(fricc_alloc_t(&dzero, 1, st));
+    PTRY(fricc_alloc_t(&err, 1, st));
+    PTRY(fricc_cuda_check(cudaMemsetAsync(dzero, 0, sizeof(double), st), "memset"));
+    PTRY(fricc_cuda_check(cudaMemsetAsync(err, 0, sizeof(unsigned), st), "memset"));
+    for (int j = 0; j <= T; ++j) {
+      const int64_t lo = j < T ? j * step : 0, hi = j < T ? ((j + 1 == T) ? n : lo + step) : n;
+      PTRY((exact::run_chain<GenAbs, exact::ConsNull, false, false>(GenAbs{q + lo}, hi - lo, dzero, false,
+                                                                     exact::ConsNull{}, sc, err, st)));
+      PTRY(fricc_cuda_check(cudaMemcpyAsync(d_norm + j, sc.cstart + fricc_cdiv(hi - lo, exact::CH), sizeof(double),
+                                            cudaMemcpyDeviceToDevice, st), "norm"));
+    }
+    std::vector<double> hn((size_t)T + 1);
+    PTRY(fricc_cuda_check(cudaMemcpyAsync(hn.data(), d_norm, sizeof(double) * (T + 1), cudaMemcpyDeviceToHost, st),
+                          "norms"));
+    PTRY(fricc_cuda_check(cudaStreamSynchronize(st), "norms"));
+    const double q_norm = hn[(size_t)T];
+    uint64_t c = (uint64_t)n_sample;
+    for (int j = 0; j < T; ++j) {
+      SegInfo& g = seg[(size_t)j];
+      g.lo = j * step;
+      g.len = (j + 1 == T) ? n - g.lo : step;
+      g.qn = hn[(size_t)j];
+      g.a = (double)(uint64_t)n_sample * g.qn / q_norm;
+      g.t = g.a - std::floor(g.a);
+      g.g = (int)std::floor(g.a);
+      frac[(size_t)j] = g.t;
+      c -= (uint64_t)(int64_t)(int)g.g;
+    }
+    if (c > (uint64_t)T) {
+      fricc_set_error("ERROR IN PIVOTAL SAMPLING: chunk counts exceed n_sample");
+      PTRY(FRICC_ERR_PIVOTAL);
+    }
+    // the fraction sample decides which chunks give one more; its draws come
+    // first, one at a time, from the same stream
+    std::vector<int64_t> sp;
+    int64_t uf = 0;
+    auto draw = [&]() { return glibc_hist ? host_glibc_uniform(glibc_hist) : (double)rand() / RAND_MAX; };
+    rc = host_pivotal((int64_t)c, frac, draw, sp, &uf);
+    if (rc) {
+      fricc_set_error("ERROR IN PIVOTAL SAMPLING (chunk fractions)");
+      goto pdone;
+    }
+    used += uf;
+    for (int64_t k : sp) seg[(size_t)k].g += 1;
+    for (auto& g : seg)
+      if (g.g < 0 || g.g > g.len) {
+        fricc_set_error("ERROR IN PIVOTAL SAMPLING: a chunk cannot give its %lld samples", (long long)g.g);
+        PTRY(FRICC_ERR_PIVOTAL);
+      }
+  }
+pdone:
+#undef PTRY
+  exact::free_chain(sc, st);
+  fricc_free(d_norm, st);
+  fricc_free(dzero, st);
+  if (rc) {
+    fricc_free(err, st);
+    return rc;
+  }
+  return fricc_parallel_sample_finish(q, n, n_sample, seg, glibc_hist, S_out, n_draws, used, err, st);
 }

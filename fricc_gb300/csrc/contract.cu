@@ -227,7 +227,7 @@ __device__ __forceinline__ void df_tile(const int* __restrict__ srow, const ulon
 template <int DF_PPT>
 __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr, const int* __restrict__ erow,
                                                    const float2* __restrict__ eval, const float4* __restrict__ Wp4,
-                                                   double* __restrict__ Op, int64_t QS) {
+                                                   double* __restrict__ Op, int64_t QS, int qtile0) {
   __shared__ int srow[DF_NT];
   __shared__ ulonglong2 sv[DF_NT];
   __shared__ f32x2 snv[DF_NT];
@@ -235,9 +235,10 @@ __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr,
   const int e0 = bptr[P], e1 = bptr[P + 1];
   if (e0 == e1) return;
   const int64_t QS2 = (QS + 1) >> 1;
-  const int64_t t0 = (int64_t)blockIdx.y * (DF_NT * DF_PPT) + threadIdx.x;
+  const int64_t qt = (int64_t)blockIdx.y + qtile0;
+  const int64_t t0 = qt * (DF_NT * DF_PPT) + threadIdx.x;
   const int64_t trem = QS2 - t0;  // this thread's pairs are t0 + k*DF_NT < QS2  <=>  k*DF_NT < trem
-  const bool full = (int64_t)(blockIdx.y + 1) * (DF_NT * DF_PPT) <= QS2;  // uniform per block
+  const bool full = (qt + 1) * (DF_NT * DF_PPT) <= QS2;  // uniform per block
   double* orow = Op + P * QS;
   const ulonglong2* wq = reinterpret_cast<const ulonglong2*>(Wp4) + t0;
   f32x2 ah[DF_PPT], al[DF_PPT];
@@ -568,10 +569,16 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
                                                       erow, eval);
     const bool prof = fricc_prof_on();
     if (prof) fricc_prof_record(st, true, 0.0);
+    // One launch over all (bucket, q tile) pairs, buckets fastest.  For the
+    // wide-row terms (2323, X/Y) the W' rows of the ~1.4 q tiles resident at
+    // once exceed L2 and DRAM sees ~9x the W' bytes, yet only 1.6 TB/s;
+    // launching one q tile at a time cut that traffic 6x but ran 50% longer
+    // (900-CTA launches leave SMs idle at each tail), so it is not done.
     const dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq);
-    k_spmm_df<ppt><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS);
+    k_spmm_df<ppt><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
+    fricc_note_launch();
     if (prof) fricc_prof_record(st, false, 2.0 * (double)T->m * (double)QS);
-    fricc_note_launch(2);
+    fricc_note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = fricc_cuda_fail(e, "spmm_f2", __FILE__, __LINE__);
   }

@@ -52,6 +52,24 @@ def libc_uniform() -> float:
     return float(_libc.rand()) / float(RAND_MAX)
 
 
+def parallel_sample(n_sample: int, q, chunks: int = 1, rng=None) -> np.ndarray:
+    """parallel_sample(n_sample, q) of src/fri_utils.cpp:176-362 on the GPU:
+    pivotal sampling of q cut into `chunks` chunks (the reference's OpenMP
+    threads), each chunk walked by its own warp.  Draws from the process's
+    rand() (the reference's stream) or from rng (a GlibcRand), in chunk order.
+    Returns the n_sample indices (numpy int64)."""
+    lib = L.load()
+    qd = _to_device(np.ascontiguousarray(q, dtype=np.float64) if not isinstance(q, torch.Tensor) else q)
+    qd = qd.contiguous()
+    S = torch.empty(max(int(n_sample), 1), dtype=torch.int64, device=qd.device)
+    hist, writeback = L.hist_arg(rng)
+    used = ctypes.c_int64(0)
+    L.check(lib.fricc_parallel_sample(ctypes.c_void_p(qd.data_ptr()), qd.numel(), int(n_sample), int(chunks), hist,
+                                      ctypes.c_void_p(S.data_ptr()), ctypes.byref(used), _stream()))
+    writeback()
+    return S[:int(n_sample)].cpu().numpy()
+
+
 def _stream() -> ctypes.c_void_p:
     return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
 

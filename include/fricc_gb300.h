@@ -190,6 +190,18 @@ int fricc_compress(const double* x, int64_t n, int64_t m, int compression, doubl
 int fricc_compress_pivotal(const double* x, int64_t n, int64_t m, uint32_t* glibc_hist, int64_t* flat, double* vals,
                            int64_t* n_largest, int64_t* n_draws, void* stream);
 
+/* parallel_sample (src/fri_utils.cpp:176-362) over the probability vector q
+ * (device, n doubles) with `chunks` chunks (the reference uses one per
+ * OpenMP thread): S (device, n_sample int64) in the reference's order.  Each
+ * chunk's adjustment and pivotal walk runs on its own warp.  Draws come
+ * from glibc_hist (as for fricc_sp_create_pivotal) or from this process's
+ * rand(): first the chunk-fraction sample, then chunk 0, 1, ... (the
+ * reference's threads share rand() concurrently; this order is its outcome
+ * when they run one after another, and at one chunk the two coincide).
+ * *n_draws (optional) receives the draws consumed.  Synchronises `stream`. */
+int fricc_parallel_sample(const double* q, int64_t n, int64_t n_sample, int chunks, uint32_t* glibc_hist,
+                          int64_t* S, int64_t* n_draws, void* stream);
+
 /* k uniforms rand()/RAND_MAX of the glibc stream with history hist[31]
  * (host, oldest first) into out (device); hist is advanced past them.  The
  * device form of the draws the reference makes with rand() (no reference

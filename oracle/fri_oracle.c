@@ -205,6 +205,86 @@ int fo_sample_pivotal(int64_t n_sample, const double* p, int64_t n, const double
   return ns == n_sample ? FO_OK : FO_PIVOTAL;
 }
 
+/* parallel_sample, src/fri_utils.cpp:176-362, with T chunks (the reference
+ * uses T = omp_get_max_threads()).  q is cut into T contiguous chunks (the
+ * last takes the remainder); chunk j expects a_j = n * |q_j| / |q| samples,
+ * floor(a_j) surely and one more with probability frac(a_j), decided by a
+ * pivotal sample over the fractions; each chunk's probabilities are then
+ * pushed towards its integer count (the reference's two capped loops) and
+ * sampled pivotally, indices shifted by the chunk offset.  The reference
+ * runs the chunk samplers on concurrent threads sharing rand(); here the
+ * draws are taken in chunk order (the fraction sample, then chunk 0, 1, ...),
+ * which is the reference's outcome when its threads run one after another;
+ * at T = 1 the two coincide.  The norms are sequential sums (the reference's
+ * one_norm at one thread).  *n_used: draws consumed. */
+int fo_parallel_sample(int64_t n_sample, const double* q, int64_t n, int T, const double* draws,
+                       int64_t n_avail, int64_t* S, int64_t* n_used) {
+  if (T < 1 || n < T) return FO_BAD_ARG;
+  const int64_t step = n / T, rem = n % T;
+  double q_norm = 0.0;
+  for (int64_t i = 0; i < n; ++i) q_norm += fabs(q[i]);
+  double* t = (double*)malloc(sizeof(double) * T);
+  double* a = (double*)malloc(sizeof(double) * T);
+  double* qn = (double*)malloc(sizeof(double) * T);
+  int* g = (int*)malloc(sizeof(int) * T);
+  double* qj = (double*)malloc(sizeof(double) * (size_t)(step + rem));
+  int64_t* Sj = (int64_t*)malloc(sizeof(int64_t) * (size_t)(n_sample > 0 ? n_sample : 1));
+  uint64_t c = (uint64_t)n_sample;
+  for (int j = 0; j < T; ++j) {
+    const int64_t lo = j * step, hi = (j + 1 == T) ? n : lo + step;
+    double nj = 0.0;
+    for (int64_t i = lo; i < hi; ++i) nj += fabs(q[i]);
+    qn[j] = nj;
+    a[j] = (double)(uint64_t)n_sample * qn[j] / q_norm;
+    t[j] = a[j] - floor(a[j]);
+    g[j] = (int)floor(a[j]);
+    c -= (uint64_t)(int64_t)g[j];
+  }
+  int64_t used = 0, u = 0;
+  int st = FO_OK;
+  /* the fractions' pivotal sample picks which chunks get one more */
+  int64_t* sp = (int64_t*)malloc(sizeof(int64_t) * (size_t)(T > 0 ? T : 1));
+  if (c > (uint64_t)T) { st = FO_PIVOTAL; goto out; }
+  st = fo_sample_pivotal((int64_t)c, t, T, draws, n_avail, sp, &u);
+  used += u;
+  if (st) goto out;
+  for (uint64_t k = 0; k < c; ++k) g[sp[k]] += 1;
+  {
+    double chunk_lb = 0.0;
+    for (int j = 0; j < T; ++j) {
+      const int64_t lo = j * step, hi = (j + 1 == T) ? n : lo + step, len = hi - lo;
+      for (int64_t i = 0; i < len; ++i) qj[i] = q[lo + i];
+      double sj = qn[j];
+      if ((double)g[j] > a[j]) {
+        for (int64_t i = 0; i < len; ++i) {
+          const double y = fmin(1., qj[i] / t[j]);
+          sj += y - qj[i];
+          qj[i] = y;
+          if (sj >= (double)g[j]) { qj[i] = y + (double)g[j] - sj; break; }
+        }
+      } else if ((double)g[j] < a[j]) {
+        for (int64_t i = 0; i < len; ++i) {
+          const double y = fmax(0., (qj[i] - t[j]) / (1. - t[j]));
+          sj += y - qj[i];
+          qj[i] = y;
+          if (sj <= (double)g[j]) { qj[i] = y + (double)g[j] - sj; break; }
+        }
+      }
+      const int64_t lb = (int64_t)chunk_lb;
+      chunk_lb += (double)g[j];
+      if (g[j] < 0 || lb + g[j] > n_sample) { st = FO_PIVOTAL; goto out; }
+      st = fo_sample_pivotal(g[j], qj, len, draws ? draws + used : NULL, draws ? n_avail - used : 0, Sj, &u);
+      used += u;
+      if (st) goto out;
+      for (int64_t k = 0; k < g[j]; ++k) S[lb + k] = Sj[k] + lo;
+    }
+  }
+out:
+  *n_used = used;
+  free(t); free(a); free(qn); free(g); free(qj); free(Sj); free(sp);
+  return st;
+}
+
 /* fri_compression, src/fri_utils.cpp:439-522, pivotal sampling (S in the
  * order sample_pivotal emits it). */
 int fo_fri_compression_pivotal(const double* x, int64_t n, int64_t m, const double* draws, int64_t n_avail,

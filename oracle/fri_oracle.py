@@ -54,6 +54,8 @@ def lib():
         L.fo_largest.argtypes = [_f64p, ctypes.c_int64, ctypes.c_int64, _i64p, _f64p]
         L.fo_fri_compression_pivotal.argtypes = [_f64p, ctypes.c_int64, ctypes.c_int64, _f64p, ctypes.c_int64,
                                                  _i64p, _f64p, _i64p, _i64p]
+        L.fo_parallel_sample.argtypes = [ctypes.c_int64, _f64p, ctypes.c_int64, ctypes.c_int, _f64p,
+                                         ctypes.c_int64, _i64p, _i64p]
         L.fo_unpack.argtypes = [_i64p, ctypes.c_int64, _i64p, _i64p]
         L.fo_term_id.argtypes = [ctypes.c_char_p]
         L.fo_outer_size.restype = ctypes.c_int64
@@ -148,6 +150,22 @@ def fri_compression_pivotal(x: np.ndarray, m: int, draws=None):
     if st:
         raise ValueError(f"fri_compression_pivotal: status {st}")
     return idx, val, nd.value, used.value
+
+
+def parallel_sample(n_sample: int, q: np.ndarray, chunks: int, draws):
+    """parallel_sample with `chunks` chunks and the given draws (in chunk
+    order); returns (S[n_sample], draws_used)."""
+    q = np.ascontiguousarray(q, dtype=np.float64).ravel()
+    draws = np.ascontiguousarray(draws, dtype=np.float64)
+    S = np.zeros(max(n_sample, 1), dtype=np.int64)
+    used = ctypes.c_int64(0)
+    st = lib().fo_parallel_sample(n_sample, _p(q, _f64p), q.size, chunks, _p(draws, _f64p), draws.size,
+                                  _p(S, _i64p), ctypes.byref(used))
+    if st == 7:
+        raise RuntimeError("ERROR IN PIVOTAL SAMPLING")
+    if st:
+        raise ValueError(f"parallel_sample: status {st}")
+    return S[:n_sample], used.value
 
 
 def largest(x: np.ndarray, m: int):

@@ -19,6 +19,9 @@ records:
                    binding's default) with the number of rand() draws each
                    consumed, the reference run in a forked child because its
                    sampler exits the process on its own errors;
+* parallel_sample.npz -- the reference's parallel_sample (src/fri_utils.cpp:176-362)
+                   at one thread, through oracle/_ref/ref_parallel_sample, on FRI
+                   probability vectors, with the draws each call consumed;
 * unbiased.npz  -- fricc/friccsd.py with "unbiased": True (running-average
                    W compression after burn-in), its missing iteration
                    counter supplied by the driver.
@@ -186,6 +189,52 @@ def pivotal_cases(R):
         if r is not None:
             idx, val, used = r
             out[f"c{k}_idx"], out[f"c{k}_val"], out[f"c{k}_used"] = idx, val, np.int64(used)
+    return out
+
+
+def parallel_sample_cases():
+    """The reference's own parallel_sample (through oracle/_ref/ref_parallel_sample)
+    at one thread, on FRI probability vectors: p = |x| / R * m' with p_D = 0
+    (the oracle's get_d_largest, itself pinned above)."""
+    from oracle import fri_oracle as FO
+    import tempfile
+    exe = os.path.join(REPO, "oracle", "_ref", "ref_parallel_sample")
+    rng = np.random.default_rng(909)
+    xs = []
+    for c in range(8):
+        n = int(rng.integers(20, 3000))
+        x = rng.standard_normal(n) * np.exp(2 * rng.standard_normal(n))
+        xs.append((x, int(rng.integers(1, max(2, n // 3)))))
+    for (o, v, seed, frac) in ((6, 24, 1, 0.12), (8, 32, 4, 0.05)):
+        sys_ = SyntheticSystem(o, v, 8 * (o + v), 0.05, seed)
+        x = sys_.mp2_amplitudes()[1].ravel()
+        xs.append((x, int(frac * x.size)))
+    out = {"n_cases": np.int64(len(xs))}
+    for k, (x, m) in enumerate(xs):
+        D, R = FO.get_d_largest(x, m)
+        mp = m - D.size
+        p = np.abs(x) / R * float(mp)
+        p[D] = 0.0
+        seed = 700 + k
+        with tempfile.NamedTemporaryFile(suffix=".bin", delete=False) as f:
+            f.write(np.ascontiguousarray(p, dtype=np.float64).tobytes())
+            path = f.name
+        r = subprocess.run([exe, path, str(mp), "1", str(seed)], capture_output=True, text=True)
+        os.unlink(path)
+        out[f"c{k}_q"] = p
+        out[f"c{k}_n"] = np.int64(mp)
+        out[f"c{k}_seed"] = np.int64(seed)
+        out[f"c{k}_ok"] = np.int64(r.returncode == 0)
+        if r.returncode == 0:
+            # the reference logs its timings on stdout first; the driver's two lines come last
+            lines = r.stdout.split("\n")[:-1]
+            S = np.array([int(t) for t in lines[-2].split()], dtype=np.int64)
+            tail = [int(t) for t in lines[-1].split()]
+            libc.srand(seed)
+            stream = [libc.rand() for _ in range(p.size + 8)]
+            used = next(j for j in range(len(stream) - 3) if stream[j:j + 4] == tail)
+            out[f"c{k}_S"] = S
+            out[f"c{k}_used"] = np.int64(used)
     return out
 
 
@@ -363,7 +412,9 @@ def main():
     np.savez_compressed(os.path.join(HERE, "lccsd.npz"), **lccsd_cases(R))
     np.savez_compressed(os.path.join(HERE, "unbiased.npz"), **unbiased_case(R))
     np.savez_compressed(os.path.join(HERE, "pivotal.npz"), **pivotal_cases(R))
-    for f in ("compress.npz", "contract.npz", "iteration.npz", "lccsd.npz", "unbiased.npz", "pivotal.npz"):
+    np.savez_compressed(os.path.join(HERE, "parallel_sample.npz"), **parallel_sample_cases())
+    for f in ("compress.npz", "contract.npz", "iteration.npz", "lccsd.npz", "unbiased.npz", "pivotal.npz",
+              "parallel_sample.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

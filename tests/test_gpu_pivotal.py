@@ -129,3 +129,47 @@ def test_pivotal_iteration_vs_oracle(gpulib, oracle):
     o1, o2 = CO.update_amps(settings, t1, t2, eris, rn_draw=ro)
     assert abs(e - P.ccsd_energy(o1, o2, eris)) < 1e-10
     assert gs.rn_draw.rand() == ro.rand()   # both streams advanced by the same draws
+
+
+def test_parallel_sample_golden_one_chunk(gpulib):
+    """parallel_sample at one chunk against the reference's own outputs
+    (tests/golden/parallel_sample.npz), draws counted."""
+    from fricc_gb300 import py_rccsd
+    from fricc_gb300.rng import GlibcRand
+    g = golden("parallel_sample.npz")
+    for k in range(int(g["n_cases"])):
+        q, ns, seed, used = g[f"c{k}_q"], int(g[f"c{k}_n"]), int(g[f"c{k}_seed"]), int(g[f"c{k}_used"])
+        r = GlibcRand(seed)
+        S = py_rccsd.parallel_sample(ns, q, 1, rng=r)
+        np.testing.assert_array_equal(S, g[f"c{k}_S"], err_msg=f"case {k}")
+        ref = GlibcRand(seed)
+        for _ in range(used):
+            ref.rand()
+        assert r.rand() == ref.rand(), k
+
+
+@pytest.mark.parametrize("chunks", [2, 5, 16, 128])
+def test_parallel_sample_chunks_vs_oracle(gpulib, oracle, chunks):
+    """Several chunks (one warp each) against the oracle with the draws in
+    chunk order, on an FRI probability vector of 2.6M elements."""
+    from fricc_gb300 import py_rccsd
+    from fricc_gb300.rng import GlibcRand
+    from fricc_gb300.synthetic import SyntheticSystem
+    s = SyntheticSystem(18, 90, 864, 0.05, 6)
+    x = np.ascontiguousarray(s.mp2_amplitudes()[1]).ravel()
+    m = int(0.05 * x.size)
+    D, R = oracle.get_d_largest(x, m)
+    mp = m - D.size
+    q = np.abs(x) / R * float(mp)
+    q[D] = 0.0
+    r = GlibcRand(chunks)
+    S = py_rccsd.parallel_sample(mp, q, chunks, rng=r)
+    probe = GlibcRand(chunks)
+    draws = np.array([probe.uniform() for _ in range(q.size + chunks + 4)])
+    So, used = oracle.parallel_sample(mp, q, chunks, draws)
+    np.testing.assert_array_equal(S, So)
+    ref = GlibcRand(chunks)
+    for _ in range(used):
+        ref.rand()
+    assert r.rand() == ref.rand()
+    assert np.unique(S).size == S.size        # no index twice

@@ -222,3 +222,21 @@ def test_pivotal_golden_bitexact(oracle):
         np.testing.assert_array_equal(t.idx4, g[f"c{k}_idx"], err_msg=f"case {k}")
         assert np.array_equal(t.vals.view(np.int64), g[f"c{k}_val"].view(np.int64)), f"case {k}"
         assert t.draws_used == used, (k, t.draws_used, used)
+
+
+def test_parallel_sample_golden(oracle):
+    """parallel_sample (src/fri_utils.cpp:176-362) at one chunk: the oracle fed
+    the reference's rand() stream returns the reference's indices and consumes
+    the same number of draws."""
+    from fricc_gb300.rng import GlibcRand
+    g = golden("parallel_sample.npz")
+    n = int(g["n_cases"])
+    assert n >= 10
+    for k in range(n):
+        assert int(g[f"c{k}_ok"])
+        q, ns, seed = g[f"c{k}_q"], int(g[f"c{k}_n"]), int(g[f"c{k}_seed"])
+        r = GlibcRand(seed)
+        draws = np.array([r.uniform() for _ in range(q.size + 4)])
+        S, used = oracle.parallel_sample(ns, q, 1, draws)
+        np.testing.assert_array_equal(S, g[f"c{k}_S"], err_msg=f"case {k}")
+        assert used == int(g[f"c{k}_used"]), (k, used)
