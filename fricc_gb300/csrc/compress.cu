@@ -177,6 +177,16 @@ struct GenP {
   }
 };
 
+// The probabilities once computed into P (one division per element instead
+// of one per pass of the exact chain); the p > 1 check was made then.
+struct GenPv {
+  const double* P;
+  const double* x;
+  const Ctl* c;
+  __device__ __forceinline__ double operator()(int64_t i) const { return c->sample ? P[i] : 0.0; }
+  __device__ __forceinline__ double value(int64_t i) const { return P[i]; }
+};
+
 // get_d_largest's acceptance test for every position d of the sorted list.
 struct ConsAccept {
   int64_t m;
@@ -257,7 +267,8 @@ __global__ void k_out_d(const double* __restrict__ x, const unsigned* __restrict
 }
 
 // S part: flat = S_k, value = x / p (src/fri_utils.cpp:495,502-504)
-__global__ void k_out_s(GenP gp, const unsigned* __restrict__ S, int64_t* __restrict__ flat,
+template <class G>
+__global__ void k_out_s(G gp, const unsigned* __restrict__ S, int64_t* __restrict__ flat,
                         double* __restrict__ vals) {
   const int64_t mp = gp.c->mp, nd = gp.c->nd;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < mp; k += (int64_t)gridDim.x * blockDim.x) {
@@ -567,6 +578,7 @@ struct CompressScratch {
   double* Rb = nullptr;
   unsigned long long* ffail = nullptr;
   unsigned* S = nullptr;
+  double* P = nullptr;
   exact::ChainScratch chain;
 };
 
@@ -584,6 +596,7 @@ static void free_scratch(CompressScratch& s, cudaStream_t st) {
   fricc_free(s.Rb, st);
   fricc_free(s.ffail, st);
   fricc_free(s.S, st);
+  fricc_free(s.P, st);
   exact::free_chain(s.chain, st);
 }
 
@@ -970,19 +983,23 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
       goto done;
     }
 
-    // 5. probabilities, the p > 1 check, exact partial sums, systematic samples
+    // 5. probabilities (once, with the p > 1 check), exact partial sums,
+    //    systematic samples
     TRY(fricc_alloc_t(&s.S, m, st));
+    TRY(fricc_alloc_t(&s.P, n, st));
     k_zero_u32<<<grid_for(m, 256), 256, 0, st>>>(s.S, m);
-    fricc_note_launch();
+    k_pvec<<<grid_for(n, 256), 256, 0, st>>>(gp, n, s.P, s.err);
+    fricc_note_launch(2);
     // with m' = 0 every p is 0 (or NaN); with R <= 0 or not finite no
     // interval matches (ConsSample checks ctl->sample): in both cases all
     // samples keep index 0, as in the reference
+    const GenPv gpv{s.P, x, ctl};
     ConsSample cs{ctl, s.S};
-    TRY((exact::run_chain<GenP, ConsSample, true, true>(gp, n, s.dzero, false, cs, s.chain, s.err, st)));
+    TRY((exact::run_chain<GenPv, ConsSample, false, true>(gpv, n, s.dzero, false, cs, s.chain, s.err, st)));
 
     // 6. output
     k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, ctl, flat, vals);
-    k_out_s<<<grid_for(m, 256), 256, 0, st>>>(gp, s.S, flat, vals);
+    k_out_s<<<grid_for(m, 256), 256, 0, st>>>(gpv, s.S, flat, vals);
     fricc_note_launch(2);
     if (meta) {
       k_put_meta<<<1, 1, 0, st>>>(ctl, 0, s.err, meta);
