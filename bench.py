@@ -60,7 +60,7 @@ def parse():
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--precision", default="df64", choices=["fp64", "df64"],
-                   help="arithmetic of the sparse terms: FP64, or FP32 pairs (~48-bit) on the FP32 pipe")
+                   help="arithmetic of the sparse terms: FP64, or FP32 pairs (48-bit products, ~40-bit sums) on the FP32 pipe")
     return p.parse_args()
 
 
@@ -318,7 +318,7 @@ def run_gpu(args):
             "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f64 (sparse terms in f32 pairs, ~48-bit)",
+            "dtype": "f64" if args.precision == "fp64" else "f64 (sparse terms in f32 pairs: 48-bit products, ~40-bit sums)",
             "data": "synthetic",
             "config": {"workload": f"{args.workload}: nocc={o} nvir={v} naux={w['naux']} sigma={w['sigma']} "
                                    f"m={m} FRI systematic, 2 compressions/iteration, FP64",
