@@ -91,6 +91,22 @@ class ReplicaBatch:
         e = self.energies()
         return float(e.mean()), float(e.var(ddof=1)) if e.size > 1 else 0.0
 
+    def trace_stats(self, burn: int = 0):
+        """Error bars of the time-averaged energy of each replica's trace
+        after ``burn`` iterations, as fri-cc's ``mcmc_std`` gives them
+        (sqrt(tau / n var), tau the integrated autocorrelation time; a trace
+        too short for a reliable tau warns instead of raising).  Returns
+        (means, error bars, taus), one entry per replica."""
+        from .stats import mcmc_std
+        means, errs, taus = [], [], []
+        for h in self.history:
+            x = np.asarray(h[burn:], dtype=np.float64)
+            err, tau = mcmc_std(x, quiet=True)
+            means.append(float(x.mean()))
+            errs.append(float(err))
+            taus.append(float(tau))
+        return np.array(means), np.array(errs), np.array(taus)
+
 
 # ---------------------------------------------------------------------------
 @dataclass

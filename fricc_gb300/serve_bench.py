@@ -3,7 +3,8 @@
   --mode replicas : R independent FRI replicas (distinct seeds) of the
                     o20v100 system (naux=600, m = 5% of o^2 v^2), all resident,
                     iterated together on a pool of streams; prints iterations/s
-                    of the whole batch and the replica mean and variance of E_corr.
+                    of the whole batch, the replica mean and variance of E_corr and
+                    each replica's trace error bar (fri-cc's mcmc_std).
   --mode serve    : a Poisson stream of solve requests (nocc ~ U{5..30},
                     nvir = ceil(r nocc) with r ~ U[4,6], naux = 8(o+v), kept
                     fraction ~ U[5%,20%], converged at |dE| < 1e-7 Eh or
@@ -42,10 +43,14 @@ def run_replicas(args):
     torch.cuda.synchronize()
     dt = time.perf_counter() - t
     mean, var = batch.stats()
+    burn = min(args.warmup, len(batch.history[0]) - 2)
+    tmeans, terrs, taus = batch.trace_stats(burn=max(burn, 0))
     return {"mode": "replicas", "workload": "o20v100: nocc=20 nvir=100 naux=600 m=200000 per replica",
             "replicas": args.replicas, "streams": args.streams, "precision": args.precision, "graph": args.graph,
             "iterations_per_s": args.replicas * args.steps / dt, "batch_steps_per_s": args.steps / dt,
-            "e_corr_mean": mean, "e_corr_var": var, "iterations_each": args.warmup + args.steps}
+            "e_corr_mean": mean, "e_corr_var": var, "iterations_each": args.warmup + args.steps,
+            "trace_after_warmup": {"mean_of_means": float(tmeans.mean()), "mcmc_std_median": float(np.median(terrs)),
+                                   "tau_median": float(np.median(taus))}}
 
 
 def run_serve(args):

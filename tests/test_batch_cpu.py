@@ -27,3 +27,16 @@ def test_footprint_monotone_and_summary():
         r.iterations = 3
     s = latency_summary(reqs)
     assert s["n"] == 4 and s["iterations"] == 12 and s["p50_s"] >= 1.0
+
+
+def test_replica_trace_stats_is_mcmc_std():
+    from fricc_gb300.batch import ReplicaBatch
+    from fricc_gb300.stats import mcmc_std
+    rng = np.random.default_rng(4)
+    rb = ReplicaBatch.__new__(ReplicaBatch)  # only the recorded traces are needed
+    rb.history = [list(-0.1 + 1e-4 * rng.standard_normal(400)) for _ in range(3)]
+    means, errs, taus = rb.trace_stats(burn=50)
+    for r in range(3):
+        x = np.array(rb.history[r][50:])
+        e, t = mcmc_std(x)
+        assert means[r] == x.mean() and errs[r] == e and taus[r] == t
