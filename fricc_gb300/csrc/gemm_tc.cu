@@ -1,0 +1,449 @@
+// BF16 tensor-core GEMM on the 5th-generation tensor cores (tcgen05), and the
+// split-BF16x3 rebuild of integral blocks from a Cholesky factor.
+//
+// C[M][N] = A[M][K] B[N][K]^T, A and B BF16 and K-major, FP32 accumulation in
+// tensor memory (TMEM).  One CTA computes one 128 x 256 tile:
+//   warp 0, one lane  -- TMA producer: 128 x 64 and 256 x 64 operand boxes
+//                        (128-byte swizzle) into a 4-stage shared-memory ring,
+//                        each stage guarded by a "full" and an "empty" mbarrier;
+//   warp 1, one lane  -- MMA issuer: four tcgen05.mma (M=128, N=256, K=16) per
+//                        stage into one TMEM accumulator of 256 columns, then
+//                        tcgen05.commit to the stage's "empty" barrier;
+//   warp 2            -- allocates and frees the TMEM columns;
+//   all four warps    -- epilogue: tcgen05.ld of their 32 TMEM lanes (one
+//                        output row per thread, 16 columns per load) into the
+//                        epilogue functor.
+// Every mbarrier wait is bounded (2 s of global time); a wait that gives up
+// sets a device error word, the roles stop issuing, the producer waits
+// (bounded) for its copies in flight, and the CTA frees its TMEM and exits.
+//
+// Split-BF16x3: x = hi + lo with hi = bf16(x), lo = bf16(x - hi), and
+// A B^T ~ Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T (the lo*lo term is below FP32
+// accumulation error).  The three products are one GEMM over a K-concatenated
+// operand pair A' = [Ahi | Ahi | Alo], B' = [Bhi | Blo | Bhi] (K' = 3K).
+#include <cuda.h>
+#include <cudaTypedefs.h>
+#include <cuda_bf16.h>
+
+#include "common.cuh"
+
+namespace tc {
+
+constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
+constexpr int A_BYTES = BM * BK * 2;  // 16 KB
+constexpr int B_BYTES = BN * BK * 2;  // 32 KB
+constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024;  // + alignment slack
+constexpr int NT = 128;
+
+// Instruction descriptor (kind::f16): D = F32 (bits 4-5 = 1), A = B = BF16
+// (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
+// 17-22, M >> 4 at bits 24-28.
+constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
+                           ((uint32_t)(BM >> 4) << 24);
+
+// Shared-memory matrix descriptor of a K-major operand tile written by TMA
+// with the 128-byte swizzle: rows of 128 bytes, 8-row atoms 1024 bytes apart
+// (stride byte offset), start address >> 4 in bits 0-13, leading byte offset
+// (unused for this layout) 16 bytes, descriptor version 1 at bit 46, swizzle
+// mode 2 (128 B) at bits 61-63.  Stepping K by 16 elements inside the
+// 128-byte row adds 32 bytes to the start address.
+__device__ __forceinline__ uint64_t sw128_desc(uint32_t saddr) {
+  return (uint64_t)((saddr & 0x3FFFFu) >> 4) | ((uint64_t)1 << 16) | ((uint64_t)(1024 >> 4) << 32) |
+         ((uint64_t)1 << 46) | ((uint64_t)2 << 61);
+}
+
+__device__ __forceinline__ uint32_t smem_u32(const void* p) {
+  return (uint32_t)__cvta_generic_to_shared(p);
+}
+
+__device__ __forceinline__ uint64_t gtime() {
+  uint64_t t;
+  asm volatile("mov.u64 %0, %%globaltimer;" : "=l"(t));
+  return t;
+}
+
+__device__ __forceinline__ void mbar_init(uint32_t a, uint32_t count) {
+  asm volatile("mbarrier.init.shared::cta.b64 [%0], %1;" ::"r"(a), "r"(count) : "memory");
+}
+
+__device__ __forceinline__ void mbar_expect_tx(uint32_t a, uint32_t bytes) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.expect_tx.shared::cta.b64 st, [%0], %1;\n\t}" ::"r"(a),
+      "r"(bytes)
+      : "memory");
+}
+
+__device__ __forceinline__ bool mbar_try(uint32_t a, uint32_t parity) {
+  uint32_t ok;
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\t"
+      "selp.u32 %0, 1, 0, p;\n\t}"
+      : "=r"(ok)
+      : "r"(a), "r"(parity)
+      : "memory");
+  return ok != 0;
+}
+
+// Wait for the phase of parity `parity` to complete; false after ~2 s.
+__device__ __forceinline__ bool mbar_wait(uint32_t a, uint32_t parity) {
+  if (mbar_try(a, parity)) return true;
+  const uint64_t t0 = gtime();
+  for (;;) {
+    for (int i = 0; i < 256; ++i)
+      if (mbar_try(a, parity)) return true;
+    if (gtime() - t0 > 2000000000ull) return false;
+  }
+}
+
+__device__ __forceinline__ void tma_load_2d(uint32_t dst, const CUtensorMap* map, int x, int y, uint32_t bar) {
+  asm volatile(
+      "cp.async.bulk.tensor.2d.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(
+          dst),
+      "l"(reinterpret_cast<uint64_t>(map)), "r"(x), "r"(y), "r"(bar)
+      : "memory");
+}
+
+__device__ __forceinline__ void tc_fence_before() {
+  asm volatile("tcgen05.fence::before_thread_sync;" ::: "memory");
+}
+__device__ __forceinline__ void tc_fence_after() {
+  asm volatile("tcgen05.fence::after_thread_sync;" ::: "memory");
+}
+
+__device__ __forceinline__ void tc_mma(uint32_t d, uint64_t a, uint64_t b, uint32_t idesc, uint32_t acc) {
+  asm volatile(
+      "{\n\t.reg .pred p;\n\t"
+      "setp.ne.b32 p, %4, 0;\n\t"
+      "tcgen05.mma.cta_group::1.kind::f16 [%0], %1, %2, %3, p;\n\t}" ::"r"(d),
+      "l"(a), "l"(b), "r"(idesc), "r"(acc)
+      : "memory");
+}
+
+// arrive on the mbarrier once every tcgen05 op issued so far by this thread completes
+__device__ __forceinline__ void tc_commit(uint32_t bar) {
+  asm volatile("tcgen05.commit.cta_group::1.mbarrier::arrive::one.shared::cluster.b64 [%0];" ::"r"(bar) : "memory");
+}
+
+__device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
+  uint32_t r[16];
+  asm volatile(
+      "tcgen05.ld.sync.aligned.32x32b.x16.b32 {%0, %1, %2, %3, %4, %5, %6, %7, %8, %9, %10, %11, %12, %13, %14, "
+      "%15}, [%16];"
+      : "=r"(r[0]), "=r"(r[1]), "=r"(r[2]), "=r"(r[3]), "=r"(r[4]), "=r"(r[5]), "=r"(r[6]), "=r"(r[7]), "=r"(r[8]),
+        "=r"(r[9]), "=r"(r[10]), "=r"(r[11]), "=r"(r[12]), "=r"(r[13]), "=r"(r[14]), "=r"(r[15])
+      : "r"(taddr));
+  asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
+#pragma unroll
+  for (int i = 0; i < 16; ++i) v[i] = __uint_as_float(r[i]);
+}
+
+// C row-major FP32 [M][ldc]
+struct EpiRowMajor {
+  float* C;
+  int64_t M, N, ldc;
+  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v) const {
+    if (row >= M) return;
+    float* c = C + row * ldc + col0;
+    if (col0 + 16 <= N && (ldc & 3) == 0) {
+#pragma unroll
+      for (int i = 0; i < 16; i += 4) *reinterpret_cast<float4*>(c + i) = make_float4(v[i], v[i + 1], v[i + 2], v[i + 3]);
+    } else {
+#pragma unroll
+      for (int i = 0; i < 16; ++i)
+        if (col0 + i < N) c[i] = v[i];
+    }
+  }
+};
+
+// C row-major FP64 [M][ldc] (the FP32 accumulators widened exactly)
+struct EpiRowMajorF64 {
+  double* C;
+  int64_t M, N, ldc;
+  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v) const {
+    if (row >= M) return;
+    double* c = C + row * ldc + col0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      if (col0 + i < N) c[i] = f2d_bits(v[i]);
+  }
+};
+
+// The (vv|vv) block for the O^2V^4 contraction: GEMM row r1 = c v + a, column
+// r2 = d v + b, value (ac|bd), stored at W[(c v + d) * ldw + a v + b] (rows
+// (c,d), columns (a,b): the layout the FP32 sparse kernel streams).
+struct EpiVvvv {
+  float* W;
+  int64_t v, ldw;
+  __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x) const {
+    const int64_t vv = v * v;
+    if (r1 >= vv) return;
+    const int64_t c = r1 / v, a = r1 - c * v;
+    int64_t d = r2 / v, b = r2 - d * v;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      if (d < v) W[(c * v + d) * ldw + a * v + b] = x[i];
+      if (++b == v) {
+        b = 0;
+        ++d;
+      }
+    }
+  }
+};
+
+template <class Epi>
+__global__ void __launch_bounds__(NT, 1)
+    k_gemm_tc(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb, int K, int tiles_m,
+              int tiles_n, Epi epi, unsigned* err) {
+  extern __shared__ uint8_t dsm[];
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], done;
+  __shared__ uint32_t tbase;
+  __shared__ int failed;
+  const uint32_t base = (smem_u32(dsm) + 1023u) & ~1023u;
+  const uint32_t sA = base, sB = base + STAGES * A_BYTES;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+
+  // tile order: groups of 16 M tiles sweep all N tiles, so the CTAs resident
+  // at once share a few operand panels in L2
+  constexpr int GROUP = 16;
+  const int id = blockIdx.x;
+  const int per_group = GROUP * tiles_n;
+  const int g = id / per_group, rem = id - g * per_group;
+  const int gm = min(GROUP, tiles_m - g * GROUP);
+  const int mt = g * GROUP + rem % gm, nt = rem / gm;
+  const int m0 = mt * BM, n0 = nt * BN;
+  const int nk = (K + BK - 1) / BK;
+
+  if (threadIdx.x == 0) {
+    for (int s = 0; s < STAGES; ++s) {
+      mbar_init(smem_u32(&full[s]), 1);
+      mbar_init(smem_u32(&empty[s]), 1);
+    }
+    mbar_init(smem_u32(&done), 1);
+    failed = 0;
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+  }
+  if (warp == 2) {
+    asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tbase)),
+                 "r"((uint32_t)BN)
+                 : "memory");
+    asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
+  }
+  tc_fence_before();
+  __syncthreads();
+  tc_fence_after();
+  const uint32_t tmem = tbase;
+
+  if (warp == 0 && lane == 0) {
+    int issued = 0;
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+      if (kb >= STAGES && !mbar_wait(smem_u32(&empty[s]), ph ^ 1u)) {
+        atomicOr(err, FRICC_DEV_TIMEOUT);
+        failed = 1;
+        break;
+      }
+      if (*(volatile int*)&failed) break;
+      mbar_expect_tx(smem_u32(&full[s]), A_BYTES + B_BYTES);
+      tma_load_2d(sA + s * A_BYTES, &tma, kb * BK, m0, smem_u32(&full[s]));
+      tma_load_2d(sB + s * B_BYTES, &tmb, kb * BK, n0, smem_u32(&full[s]));
+      ++issued;
+    }
+    if (*(volatile int*)&failed) {
+      // let the copies in flight land before the CTA's shared memory goes away
+      for (int kb = issued - STAGES < 0 ? 0 : issued - STAGES; kb < issued; ++kb)
+        mbar_wait(smem_u32(&full[kb % STAGES]), (uint32_t)(kb / STAGES) & 1u);
+    }
+  } else if (warp == 1 && lane == 0) {
+    for (int kb = 0; kb < nk; ++kb) {
+      const int s = kb % STAGES;
+      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
+      if (!mbar_wait(smem_u32(&full[s]), ph)) {
+        atomicOr(err, FRICC_DEV_TIMEOUT);
+        failed = 1;
+        break;
+      }
+      tc_fence_after();
+      const uint32_t a0 = sA + s * A_BYTES, b0 = sB + s * B_BYTES;
+#pragma unroll
+      for (int k = 0; k < BK / 16; ++k)
+        tc_mma(tmem, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), IDESC, (kb | k) != 0);
+      tc_commit(smem_u32(&empty[s]));
+    }
+    tc_commit(smem_u32(&done));  // arrives when every MMA above has completed
+  }
+  __syncwarp();
+
+  bool ok = mbar_wait(smem_u32(&done), 0);
+  ok = __all_sync(0xffffffffu, ok && !*(volatile int*)&failed) && nk > 0;
+  tc_fence_after();
+  if (ok) {
+    const int64_t row = (int64_t)m0 + warp * 32 + lane;
+    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
+#pragma unroll 1
+    for (int c = 0; c < BN / 16; ++c) {
+      float v[16];
+      tc_ld16(lane_base + (uint32_t)(c * 16), v);
+      epi(row, (int64_t)n0 + c * 16, v);
+    }
+  } else if (lane == 0 && warp == 0) {
+    atomicOr(err, FRICC_DEV_TIMEOUT);
+  }
+  tc_fence_before();
+  __syncthreads();
+  if (warp == 2)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
+}
+
+// x [rows][ld] FP64 (the first k columns used) -> A' [rows][kp] = [hi | hi | lo]
+// and B' [rows][kp] = [hi | lo | hi], kp >= 3k, padding columns zero.
+__global__ void k_split_bf16x3(const double* __restrict__ x, int64_t rows, int64_t k, int64_t ld, int64_t kp,
+                               __nv_bfloat16* __restrict__ Ap, __nv_bfloat16* __restrict__ Bp) {
+  const int64_t n = rows * kp;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / kp, j = t - r * kp;
+    const int64_t part = j / k, col = j - part * k;
+    __nv_bfloat16 a = __float2bfloat16(0.0f), b = a;
+    if (part < 3) {
+      const double xv = x[r * ld + col];
+      const __nv_bfloat16 hi = __double2bfloat16(xv);
+      const __nv_bfloat16 lo = __double2bfloat16(xv - (double)__bfloat162float(hi));
+      a = part < 2 ? hi : lo;
+      b = part == 1 ? lo : hi;
+    }
+    Ap[t] = a;
+    Bp[t] = b;
+  }
+}
+
+PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
+  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
+  static bool tried = false;
+  if (!tried) {
+    tried = true;
+    void* p = nullptr;
+    cudaDriverEntryPointQueryResult q;
+    if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
+        q == cudaDriverEntryPointSuccess)
+      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+  }
+  return fn;
+}
+
+// 2-D map of a K-major BF16 matrix [rows][ld] (K = k columns used), box
+// (64 K elements = 128 bytes) x box_rows, 128-byte swizzle, zero fill.
+int make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t k, int64_t ld, int box_rows) {
+  auto fn = encode_fn();
+  if (!fn) {
+    fricc_set_error("gemm_tc: cuTensorMapEncodeTiled is unavailable");
+    return FRICC_ERR_CUDA;
+  }
+  cuuint64_t gdim[2] = {(cuuint64_t)k, (cuuint64_t)rows};
+  cuuint64_t gstride[1] = {(cuuint64_t)ld * 2};
+  cuuint32_t box[2] = {(cuuint32_t)BK, (cuuint32_t)box_rows};
+  cuuint32_t estr[2] = {1, 1};
+  const CUresult r = fn(map, CU_TENSOR_MAP_DATA_TYPE_BFLOAT16, 2, const_cast<void*>(ptr), gdim, gstride, box, estr,
+                        CU_TENSOR_MAP_INTERLEAVE_NONE, CU_TENSOR_MAP_SWIZZLE_128B, CU_TENSOR_MAP_L2_PROMOTION_L2_256B,
+                        CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE);
+  if (r != CUDA_SUCCESS) {
+    fricc_set_error("gemm_tc: cuTensorMapEncodeTiled failed (%d)", (int)r);
+    return FRICC_ERR_ARG;
+  }
+  return FRICC_OK;
+}
+
+template <class Epi>
+int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K, const Epi& epi,
+           cudaStream_t st) {
+  if (!A || !B || M <= 0 || N <= 0 || K <= 0 || lda < K || ldb < K || (lda % 8) || (ldb % 8) ||
+      (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16)) {
+    fricc_set_error("gemm_tc: bad arguments (K-major BF16 operands: 16-byte aligned, ld >= K, ld %% 8 == 0)");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t tm = fricc_cdiv(M, BM), tn = fricc_cdiv(N, BN);
+  if (tm * tn > 0x7fffffffLL || K > 0x7fffffffLL) {
+    fricc_set_error("gemm_tc: problem too large for one launch");
+    return FRICC_ERR_ARG;
+  }
+  CUtensorMap ma, mb;
+  int rc = make_map(&ma, A, M, K, lda, BM);
+  if (!rc) rc = make_map(&mb, B, N, K, ldb, BN);
+  if (rc) return rc;
+  unsigned* err = nullptr;
+  rc = fricc_alloc_t(&err, 1, st);
+  if (rc) return rc;
+  static bool attr = false;  // per instantiation
+  cudaError_t e = cudaSuccess;
+  if (!attr) {
+    e = cudaFuncSetAttribute(k_gemm_tc<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    attr = e == cudaSuccess;
+  }
+  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(unsigned), st);
+  if (e == cudaSuccess) {
+    k_gemm_tc<Epi><<<(unsigned)(tm * tn), NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, epi, err);
+    fricc_note_launch();
+    e = cudaGetLastError();
+  }
+  unsigned herr = 0;
+  if (e == cudaSuccess) e = cudaMemcpyAsync(&herr, err, sizeof(unsigned), cudaMemcpyDeviceToHost, st);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+  fricc_free(err, st);
+  if (e != cudaSuccess) return fricc_cuda_fail(e, "gemm_tc", __FILE__, __LINE__);
+  if (herr) {
+    fricc_set_error("gemm_tc: a bounded pipeline wait gave up (device error 0x%x)", herr);
+    return FRICC_ERR_TIMEOUT;
+  }
+  return FRICC_OK;
+}
+
+}  // namespace tc
+
+extern "C" {
+
+int fricc_gemm_bf16_tn(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                       float* C, int64_t ldc, void* stream) {
+  if (!C || ldc < N) {
+    fricc_set_error("gemm_bf16_tn: bad output");
+    return FRICC_ERR_ARG;
+  }
+  return tc::launch(A, lda, B, ldb, M, N, K, tc::EpiRowMajor{C, M, N, ldc}, (cudaStream_t)stream);
+}
+
+int fricc_gemm_bf16_tn_f64(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                           double* C, int64_t ldc, void* stream) {
+  if (!C || ldc < N) {
+    fricc_set_error("gemm_bf16_tn_f64: bad output");
+    return FRICC_ERR_ARG;
+  }
+  return tc::launch(A, lda, B, ldb, M, N, K, tc::EpiRowMajorF64{C, M, N, ldc}, (cudaStream_t)stream);
+}
+
+int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int64_t kp, void* Ap, void* Bp,
+                       void* stream) {
+  if (rows < 0 || k <= 0 || ld < k || kp < 3 * k || (rows > 0 && (!x || !Ap || !Bp))) {
+    fricc_set_error("split_bf16x3: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t n = rows * kp;
+  if (n == 0) return FRICC_OK;
+  int64_t g = fricc_cdiv(n, 256);
+  if (g > 152 * 32) g = 152 * 32;
+  tc::k_split_bf16x3<<<(unsigned)g, 256, 0, (cudaStream_t)stream>>>(
+      x, rows, k, ld, kp, static_cast<__nv_bfloat16*>(Ap), static_cast<__nv_bfloat16*>(Bp));
+  fricc_note_launch();
+  cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "split_bf16x3", __FILE__, __LINE__);
+}
+
+int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t kp, float* W, int64_t ldw,
+                              void* stream) {
+  if (!W || v <= 0 || ldw < v * v) {
+    fricc_set_error("vvvv_rebuild_bf16x3: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  return tc::launch(Ap, kp, Bp, kp, v * v, v * v, kp, tc::EpiVvvv{W, v, ldw}, (cudaStream_t)stream);
+}
+
+}  // extern "C"

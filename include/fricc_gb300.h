@@ -240,6 +240,34 @@ int fricc_energy_update_lin(const double* t1num, const double* t2num, const doub
                             const double* ovov, const double* t1old, const double* t2old, int64_t nocc,
                             int64_t nvir, double* t1out, double* t2out, double* res, void* stream);
 
+/* Split-precision integral rebuilds on the tcgen05 tensor cores (the
+ * reference builds its dense integral blocks in FP64 through PySCF,
+ * fricc/friccsd.py:325-331 for Wvvvv; the split-BF16x3 rebuild from a
+ * Cholesky factor has no reference counterpart).
+ *
+ * fricc_gemm_bf16_tn: C[M][N] = A[M][K] B[N][K]^T with BF16 operands, both
+ * K-major (row strides lda, ldb in elements: multiples of 8, base 16-byte
+ * aligned), FP32 accumulation; C FP32 (or FP64 for the _f64 form, the FP32
+ * sums widened exactly), row stride ldc.  Synchronises the stream and
+ * returns FRICC_ERR_TIMEOUT if a bounded pipeline wait gave up.
+ *
+ * fricc_split_bf16x3: x [rows][ld] FP64 (first k columns) ->
+ * A' = [hi | hi | lo], B' = [hi | lo | hi] ([rows][kp] BF16, kp >= 3k, the
+ * columns past 3k zero), hi = bf16(x), lo = bf16(x - hi); A'_r . B'_s is
+ * then the split-BF16x3 product of rows r and s.
+ *
+ * fricc_vvvv_rebuild_bf16x3: from the split operands of L_vv^T
+ * ([v*v][kp], row c*v + a = L[:, a, c]), W[(c*v + d)*ldw + a*v + b] = (ac|bd)
+ * in FP32 -- the O^2V^4 operand of fricc_spmm_f1. */
+int fricc_gemm_bf16_tn(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                       float* C, int64_t ldc, void* stream);
+int fricc_gemm_bf16_tn_f64(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                           double* C, int64_t ldc, void* stream);
+int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int64_t kp, void* Ap, void* Bp,
+                       void* stream);
+int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t kp, float* W, int64_t ldw,
+                              void* stream);
+
 /* A dedicated non-blocking stream of the current device, and its release
  * (no reference counterpart).  Solvers that overlap or capture work need
  * streams no other solver shares; torch's own streams come from a small

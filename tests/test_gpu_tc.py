@@ -1,0 +1,86 @@
+"""The tcgen05 BF16 GEMM and the split-BF16x3 rebuilds (fricc_gb300/csrc/gemm_tc.cu).
+
+* integer-valued BF16 operands make every FP32 sum exact, so the tensor-core
+  result must equal the FP64 product bit for bit: this pins the operand
+  layouts (TMA boxes, 128-byte swizzle, MMA descriptors), the K tail, the M
+  and N edge tiles and the tile order;
+* random operands: within FP32 accumulation error of the FP64 product;
+* split-BF16x3 products and the (vv|vv) rebuild: within 2^-14 of
+  sum |x||y| of the FP64 product (the BF16 hi + lo pair keeps ~16 bits).
+"""
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+def _ints(shape, lo, hi, seed):
+    g = torch.Generator().manual_seed(seed)
+    return torch.randint(lo, hi + 1, shape, generator=g).to(torch.bfloat16).cuda()
+
+
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (300, 520, 200), (2100, 300, 72), (77, 19, 8)])
+def test_gemm_integer_exact(gpulib, M, N, K):
+    from fricc_gb300.cholesky import gemm_bf16_tn
+    A = _ints((M, K), -8, 8, 1)
+    B = _ints((N, K), -8, 8, 2)
+    C = gemm_bf16_tn(A, B)
+    ref = (A.double() @ B.double().T).float()
+    assert torch.equal(C, ref)
+    C64 = gemm_bf16_tn(A, B, f64=True)
+    assert torch.equal(C64, A.double() @ B.double().T)
+
+
+def test_gemm_strided_operands(gpulib):
+    from fricc_gb300.cholesky import gemm_bf16_tn
+    Abig = _ints((260, 136), -4, 4, 3)
+    Bbig = _ints((140, 136), -4, 4, 4)
+    A, B = Abig[:, :120], Bbig[3:, :120]  # row strides 136, K = 120
+    out = torch.full((260, 140), -1.0, dtype=torch.float32, device="cuda")
+    C = gemm_bf16_tn(A, B, out=out[:, :137])  # output row stride 140
+    assert torch.equal(C, (A.double() @ B.double().T).float())
+    assert bool((out[:, 137:] == -1.0).all())
+
+
+def test_gemm_random_fp32_accuracy(gpulib):
+    from fricc_gb300.cholesky import gemm_bf16_tn
+    g = torch.Generator().manual_seed(5)
+    A = torch.randn(520, 1000, generator=g).to(torch.bfloat16).cuda()
+    B = torch.randn(390, 1000, generator=g).to(torch.bfloat16).cuda()
+    C = gemm_bf16_tn(A, B, f64=True)
+    ref = A.double() @ B.double().T
+    scale = A.double().abs() @ B.double().abs().T
+    assert bool(((C - ref).abs() <= 1e-6 * scale).all())
+
+
+def test_split_bf16x3_product(gpulib):
+    from fricc_gb300.cholesky import gemm_bf16_tn, split_bf16x3
+    g = torch.Generator().manual_seed(6)
+    x = torch.randn(300, 150, generator=g, dtype=torch.float64).cuda()
+    y = torch.randn(260, 150, generator=g, dtype=torch.float64).cuda() * 1e-3
+    Ax, _ = split_bf16x3(x)
+    _, By = split_bf16x3(y)
+    assert Ax.shape == (300, 456) and bool((Ax[:, 450:] == 0).all())
+    C = gemm_bf16_tn(Ax, By, f64=True)
+    ref = x @ y.T
+    scale = x.abs() @ y.abs().T
+    err = float(((C - ref).abs() / scale).max())
+    assert err < 2.0 ** -14, err
+    # the split itself: hi + lo within 2^-16 of x
+    hi, lo = Ax[:, :150].double(), Ax[:, 300:450].double()
+    assert float(((hi + lo - x).abs() / x.abs().clamp_min(1e-300)).max()) < 2.0 ** -15
+
+
+def test_vvvv_rebuild_matches_fp64(gpulib):
+    from fricc_gb300.cholesky import VvvvRebuild
+    from fricc_gb300.synthetic import make_system
+    s = make_system("o10v40", seed=0)
+    Lf = torch.from_numpy(s.L).cuda()
+    o, v = s.nocc, s.nvir
+    R = VvvvRebuild(Lf, o)
+    W = R.rebuild()
+    Lv = Lf[:, o:, o:]
+    ref = torch.einsum("Pac,Pbd->cdab", Lv, Lv).reshape(v * v, v * v)
+    scale = torch.einsum("Pac,Pbd->cdab", Lv.abs(), Lv.abs()).reshape(v * v, v * v)
+    err = float(((W.double() - ref).abs() / scale).max())
+    assert err < 2.0 ** -14, err
