@@ -59,12 +59,26 @@ def parse():
     p.add_argument("--workload", default="o30v150")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--precision", default="df64", choices=["fp64", "df64"],
-                   help="arithmetic of the sparse terms: FP64, or FP32 pairs (48-bit products, ~40-bit sums) on the FP32 pipe")
+    p.add_argument("--precision", default="df64", choices=["fp64", "df64", "split"],
+                   help="arithmetic of the sparse terms: FP64, or FP32 pairs (48-bit products, ~40-bit sums) on the "
+                        "FP32 pipe; 'split' also rebuilds (vv|vv) every iteration from the BF16 hi+lo Cholesky "
+                        "factor on the tcgen05 tensor cores (split-BF16x3, FP32) and builds (ov|vv), (oo|vv) "
+                        "the same way")
     return p.parse_args()
 
 
 # --------------------------------------------------------------------- helpers
+def measured_peaks() -> dict:
+    """The machine's measured HBM and BF16 peaks (MEASURED_PEAKS.json beside
+    this file), or the earlier GB300 measurement when the file is absent."""
+    path = os.path.join(os.path.dirname(os.path.abspath(__file__)), "MEASURED_PEAKS.json")
+    try:
+        with open(path) as f:
+            return json.load(f)
+    except (OSError, ValueError):
+        return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0, "bf16_tflops_sustained": 1700.0, "fallback": True}
+
+
 def dist_setup():
     world = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -223,7 +237,12 @@ def run_gpu(args):
     eia = e[:o, None] - e[None, o:]
     t2 = (E.ovov.permute(0, 2, 1, 3) / (eia[:, None, :, None] + eia[None, :, None, :])).contiguous()
     t1 = torch.zeros(o, v, dtype=torch.float64, device=dev)
-    solver = FRICCSDGPU(E, {"m_keep": m}, rn_draw=seeded_draws(1000 + rank), precision=args.precision)
+    Es = None
+    if args.precision == "split":
+        from fricc_gb300.cholesky import split_eris
+        Es = split_eris(system, device=dev)
+    solver = FRICCSDGPU(Es if Es is not None else E, {"m_keep": m}, rn_draw=seeded_draws(1000 + rank),
+                        precision=args.precision)
     stream = torch.cuda.current_stream()
 
     for _ in range(args.warmup):
@@ -246,6 +265,28 @@ def run_gpu(args):
         if world > 1:
             dist.barrier()
         torch.cuda.synchronize()
+
+    # the tensor-core rebuild of (vv|vv) alone (split precision): CUDA events
+    # around 3 rebuilds into the solver's own buffer, outside the timed region
+    tc_roof = None
+    if Es is not None:
+        R = Es.vvvv_rebuild
+        buf = solver._vvvv_buf
+        ra, rb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        R.rebuild(buf)
+        ra.record(stream)
+        for _ in range(3):
+            R.rebuild(buf)
+        rb.record(stream)
+        torch.cuda.synchronize()
+        R.check()
+        r_ms = ra.elapsed_time(rb) / 3
+        pk = measured_peaks().get("bf16_tflops")
+        ach = R.flops() / (r_ms / 1000.0) / 1e12
+        tc_roof = {"kernel": "k_gemm_tc<EpiVvvv> ((vv|vv) rebuild, tcgen05 BF16, split-BF16x3, FP32 accumulation)",
+                   "bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s",
+                   "frac": ach / pk if pk else None, "ms": r_ms,
+                   "flops": R.flops(), "peak_source": "bf16_tflops (burst) of MEASURED_PEAKS.json"}
 
     lib.fricc_prof_enable(1)
     launches0 = lib.fricc_launch_count()
@@ -330,6 +371,12 @@ def run_gpu(args):
             "clocks": clk.summary(), "energy_last": energies[-1],
             "delta_e_vs_fp64_per_step": delta_e,
         }
+        if tc_roof is not None:
+            line["tensor_core_rebuild"] = tc_roof
+            line["dtype"] = ("f64 (compression, denominators, energy); (vv|vv), (ov|vv), (oo|vv) split-BF16x3 on "
+                             "tcgen05 with FP32 accumulation; sparse terms in f32 pairs")
+            line["config"]["l2"] = (f"working set > L2 ((ac|bd) rebuilt in FP32, {4 * v ** 4 / 1e9:.2f} GB, "
+                                    "streamed by the O^2V^4 term every step)")
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

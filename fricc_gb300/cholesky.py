@@ -78,21 +78,80 @@ def lvv_t(Lf: torch.Tensor, nocc: int) -> torch.Tensor:
 
 class VvvvRebuild:
     """The (vv|vv) block rebuilt from the split factor: W[(c,d), (a,b)] =
-    (ac|bd) in FP32 (rows of ``ldw`` = v*v floats), on demand."""
+    (ac|bd) in FP32 (rows of ``ldw`` = v*v floats, rounded up to even), on
+    demand.  ``rebuild()`` is stream-ordered and capturable: a pipeline wait
+    that gave up is recorded in a device status word that ``check()`` reads."""
 
     def __init__(self, Lf: torch.Tensor, nocc: int):
         nmo = Lf.shape[1]
         self.v = nmo - nocc
         self.Ap, self.Bp = split_bf16x3(lvv_t(Lf, nocc))
         self.kp = self.Ap.shape[1]
-        self.ldw = self.v * self.v
+        self.ldw = self.v * self.v + (self.v * self.v) % 2
+        self.status = torch.zeros(1, dtype=torch.int32, device=Lf.device)
         self.W = None
+        self.rebuilds = 0
+
+    def flops(self) -> float:
+        """Tensor-core flops of one rebuild (the three BF16 products)."""
+        return 2.0 * (self.v ** 4) * self.kp
 
     def rebuild(self, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Rebuild into ``out`` (v*v rows of ldw floats), or into the block
+        kept on this object (``W``), on the current stream."""
         v = self.v
+        if out is not None and (out.dtype != torch.float32 or out.shape != (v * v, self.ldw)
+                                or not out.is_contiguous()):
+            raise ValueError("out: a contiguous float32 (v*v, ldw) buffer")
         if out is None:
             if self.W is None:
                 self.W = torch.empty(v * v, self.ldw, dtype=torch.float32, device=self.Ap.device)
             out = self.W
-        L.check(L.load().fricc_vvvv_rebuild_bf16x3(_p(self.Ap), _p(self.Bp), v, self.kp, _p(out), self.ldw, _st()))
+        L.check(L.load().fricc_vvvv_rebuild_bf16x3(_p(self.Ap), _p(self.Bp), v, self.kp, _p(out), self.ldw,
+                                                   _p(self.status), _st()))
+        self.rebuilds += 1
         return out
+
+    def check(self):
+        if int(self.status.item()):
+            raise L.FriccError(5, "vvvv rebuild: a bounded tensor-core pipeline wait gave up")
+
+
+def split_eris(system, device="cuda"):
+    """DeviceERIs of a synthetic system for the split-precision form: the
+    (ov|vv) and (oo|vv) blocks rebuilt from the BF16 hi + lo factor on the
+    tensor cores (split-BF16x3, FP32 accumulation, widened to FP64 for the
+    dense algebra), the (vv|vv) block never stored in FP64 but rebuilt by
+    ``VvvvRebuild`` for the O^2V^4 contraction; the small blocks (oo|oo),
+    (ov|oo), (ov|ov), (ov|vo) and sum_cd (ac|bd) in FP64 from the factor."""
+    from .rccsd_dense import DeviceERIs
+    dev = torch.device(device)
+    Lf = torch.from_numpy(system.L).to(dev, torch.float64)
+    o, nmo = system.nocc, system.nmo
+    naux = Lf.shape[0]
+    sl = {"o": slice(0, o), "v": slice(o, nmo)}
+
+    def fac(p, q):
+        return Lf[:, sl[p], sl[q]].reshape(naux, -1).t().contiguous()  # [(p,q), P]
+
+    def fp64_blk(name):
+        p, q, r, t = name
+        n1 = (Lf[:, sl[p], sl[q]]).shape[1:]
+        n2 = (Lf[:, sl[r], sl[t]]).shape[1:]
+        return (fac(p, q) @ fac(r, t).t()).reshape(*n1, *n2)
+
+    def tc_blk(name):
+        p, q, r, t = name
+        A, _ = split_bf16x3(fac(p, q))
+        _, B = split_bf16x3(fac(r, t))
+        n1 = (Lf[:, sl[p], sl[q]]).shape[1:]
+        n2 = (Lf[:, sl[r], sl[t]]).shape[1:]
+        return gemm_bf16_tn(A, B, f64=True).reshape(*n1, *n2)
+
+    blocks = {k: fp64_blk(k) for k in ("oooo", "ovoo", "ovov", "ovvo")}
+    blocks["ovvv"] = tc_blk("ovvv")
+    blocks["oovv"] = tc_blk("oovv")
+    s = Lf[:, o:, o:].sum(dim=2)                      # [P, a] = sum_c L[P,a,c]
+    blocks["S0"] = s.t() @ s                          # sum_cd (ac|bd)
+    blocks["vvvv_rebuild"] = VvvvRebuild(Lf, o)
+    return DeviceERIs(torch.from_numpy(system.fock), torch.from_numpy(system.mo_energy), o, blocks, device)

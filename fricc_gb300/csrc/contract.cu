@@ -279,6 +279,90 @@ __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr,
   }
 }
 
+// The same contraction against an FP32 W (the split-precision (vv|vv) block
+// rebuilt on the tensor cores): row r of W holds ldw floats, read as pairs
+// (W[r][2t], W[r][2t+1]); the compressed T values stay float pairs, so
+//   ph + e = W vh exactly, pl = e + W vl, and the same two-sum accumulation.
+// Half the bytes of the q-pair layout per term and one FMA fewer.
+template <int PPT, bool FULL>
+__device__ __forceinline__ void f1_tile(const int* __restrict__ srow, const ulonglong2* __restrict__ sv,
+                                        const f32x2* __restrict__ snv, int cnt, const f32x2* __restrict__ wq,
+                                        int64_t ldw2, int64_t trem, f32x2* ah, f32x2* al) {
+  for (int j = 0; j < cnt; ++j) {
+    const f32x2* w = wq + (int64_t)srow[j] * ldw2;
+    const ulonglong2 v = sv[j];  // (vh, vh), (vl, vl)
+    const f32x2 nvh = snv[j];    // (-vh, -vh)
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      if (FULL || k * DF_NT < trem) {
+        const f32x2 x = w[k * DF_NT];       // (W, W')
+        const f32x2 nph = mul2(x, nvh);     // -ph
+        f32x2 pl = fma2(x, v.x, nph);       // W vh - ph, exact
+        pl = fma2(x, v.y, pl);
+        const f32x2 s = sub2(ah[k], nph);
+        const f32x2 z = sub2(s, ah[k]);
+        const f32x2 err = sub2(sub2(ah[k], sub2(s, z)), add2(nph, z));
+        al[k] = add2(al[k], add2(err, pl));
+        ah[k] = s;
+      }
+    }
+  }
+}
+
+template <int PPT>
+__global__ void __launch_bounds__(DF_NT) k_spmm_f1(const int* __restrict__ bptr, const int* __restrict__ erow,
+                                                   const float2* __restrict__ eval, const float2* __restrict__ W2,
+                                                   int64_t ldw2, double* __restrict__ Op, int64_t QS) {
+  __shared__ int srow[DF_NT];
+  __shared__ ulonglong2 sv[DF_NT];
+  __shared__ f32x2 snv[DF_NT];
+  const int64_t P = blockIdx.x;
+  const int e0 = bptr[P], e1 = bptr[P + 1];
+  if (e0 == e1) return;
+  const int64_t QS2 = (QS + 1) >> 1;
+  const int64_t qt = blockIdx.y;
+  const int64_t t0 = qt * (DF_NT * PPT) + threadIdx.x;
+  const int64_t trem = QS2 - t0;
+  const bool full = (qt + 1) * (DF_NT * PPT) <= QS2;
+  double* orow = Op + P * QS;
+  const f32x2* wq = reinterpret_cast<const f32x2*>(W2) + t0;
+  f32x2 ah[PPT], al[PPT];
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int64_t q = 2 * (t0 + k * DF_NT);
+    const float2 a = split_f2(q < QS ? orow[q] : 0.0);
+    const float2 b = split_f2(q + 1 < QS ? orow[q + 1] : 0.0);
+    ah[k] = pk2(a.x, b.x);
+    al[k] = pk2(a.y, b.y);
+  }
+  for (int eb = e0; eb < e1; eb += DF_NT) {
+    const int cnt = e1 - eb < DF_NT ? e1 - eb : DF_NT;
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      const float2 v = eval[eb + threadIdx.x];
+      srow[threadIdx.x] = erow[eb + threadIdx.x];
+      sv[threadIdx.x] = make_ulonglong2(pk2(v.x, v.x), pk2(v.y, v.y));
+      snv[threadIdx.x] = pk2(-v.x, -v.x);
+    }
+    __syncthreads();
+    if (full) f1_tile<PPT, true>(srow, sv, snv, cnt, wq, ldw2, trem, ah, al);
+    else f1_tile<PPT, false>(srow, sv, snv, cnt, wq, ldw2, trem, ah, al);
+#pragma unroll
+    for (int k = 0; k < PPT; ++k) {
+      const f32x2 s = add2(ah[k], al[k]);
+      al[k] = sub2(al[k], sub2(s, ah[k]));
+      ah[k] = s;
+    }
+  }
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int64_t q = 2 * (t0 + k * DF_NT);
+    const float2 h = upk2(ah[k]), l = upk2(al[k]);
+    if (q < QS) orow[q] = pair_to_f64(h.x, l.x);
+    if (q + 1 < QS) orow[q + 1] = pair_to_f64(h.y, l.y);
+  }
+}
+
 __global__ void k_entries_df(const int* __restrict__ slots, const double* __restrict__ vals,
                              const unsigned* __restrict__ order, int64_t m, int ka, int kb, int64_t dkb, double coef,
                              int* __restrict__ erow, float2* __restrict__ eval) {
@@ -581,6 +665,49 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
     fricc_note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = fricc_cuda_fail(e, "spmm_f2", __FILE__, __LINE__);
+  }
+  fricc_free(erow, st);
+  fricc_free(eval, st);
+  return rc;
+}
+
+int fricc_spmm_f1_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float* W, int64_t QS,
+                         int64_t ldw, double* Op, cudaStream_t st) {
+  if (!T || !W || !Op || QS <= 0 || ldw < QS || (ldw & 1) || pa < 0 || pa > 3 || pb < 0 || pb > 3 || ka < 0 ||
+      ka > 3 || kb < 0 || kb > 3 || pa == pb || ka == kb) {
+    fricc_set_error("spmm_f1: bad arguments (W rows of ldw >= QS floats, ldw even)");
+    return FRICC_ERR_ARG;
+  }
+  if (reinterpret_cast<uintptr_t>(W) % 8 != 0) {
+    fricc_set_error("spmm_f1: W must be 8-byte aligned");
+    return FRICC_ERR_ARG;
+  }
+  if (T->m == 0) return FRICC_OK;
+  Bucketing* bk = nullptr;
+  int rc = fricc_sparse_bucketing(T, pa, pb, st, &bk);
+  if (rc) return rc;
+  int* erow = nullptr;
+  float2* eval = nullptr;
+  rc = fricc_alloc_t(&erow, T->m, st);
+  if (!rc) rc = fricc_alloc_t(&eval, T->m, st);
+  constexpr int ppt = 2;
+  const int64_t QS2 = (QS + 1) / 2;
+  const int64_t ntq = fricc_cdiv(QS2, DF_NT * ppt);
+  if (!rc && (ntq > 65535 || bk->nbuckets > 0x7fffffffLL)) {
+    fricc_set_error("spmm_f1: problem too large for one launch");
+    rc = FRICC_ERR_ARG;
+  }
+  if (!rc) {
+    k_entries_df<<<grid_for(T->m, 256), 256, 0, st>>>(T->slots, T->vals, bk->order, T->m, ka, kb, T->dims[kb], coef,
+                                                      erow, eval);
+    const bool prof = fricc_prof_on();
+    if (prof) fricc_prof_record(st, true, 0.0);
+    const dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq);
+    k_spmm_f1<ppt><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, reinterpret_cast<const float2*>(W), ldw / 2, Op, QS);
+    if (prof) fricc_prof_record(st, false, 2.0 * (double)T->m * (double)QS);
+    fricc_note_launch(2);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fricc_cuda_fail(e, "spmm_f1", __FILE__, __LINE__);
   }
   fricc_free(erow, st);
   fricc_free(eval, st);

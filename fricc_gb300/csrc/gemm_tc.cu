@@ -354,9 +354,12 @@ int make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t k, int64_t
   return FRICC_OK;
 }
 
+// status == nullptr: synchronous, a gave-up wait returns FRICC_ERR_TIMEOUT;
+// otherwise stream-ordered (capturable): the kernel ORs FRICC_DEV_TIMEOUT into
+// *status and the caller reads it later.
 template <class Epi>
 int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K, const Epi& epi,
-           cudaStream_t st) {
+           cudaStream_t st, unsigned* status = nullptr) {
   if (!A || !B || M <= 0 || N <= 0 || K <= 0 || lda < K || ldb < K || (lda % 8) || (ldb % 8) ||
       (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16)) {
     fricc_set_error("gemm_tc: bad arguments (K-major BF16 operands: 16-byte aligned, ld >= K, ld %% 8 == 0)");
@@ -371,16 +374,23 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
   int rc = make_map(&ma, A, M, K, lda, BM);
   if (!rc) rc = make_map(&mb, B, N, K, ldb, BN);
   if (rc) return rc;
-  unsigned* err = nullptr;
-  rc = fricc_alloc_t(&err, 1, st);
-  if (rc) return rc;
   static bool attr = false;  // per instantiation
   cudaError_t e = cudaSuccess;
   if (!attr) {
     e = cudaFuncSetAttribute(k_gemm_tc<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
-    attr = e == cudaSuccess;
+    if (e != cudaSuccess) return fricc_cuda_fail(e, "gemm_tc attribute", __FILE__, __LINE__);
+    attr = true;
   }
-  if (e == cudaSuccess) e = cudaMemsetAsync(err, 0, sizeof(unsigned), st);
+  if (status) {
+    k_gemm_tc<Epi><<<(unsigned)(tm * tn), NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, epi, status);
+    fricc_note_launch();
+    e = cudaGetLastError();
+    return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "gemm_tc", __FILE__, __LINE__);
+  }
+  unsigned* err = nullptr;
+  rc = fricc_alloc_t(&err, 1, st);
+  if (rc) return rc;
+  e = cudaMemsetAsync(err, 0, sizeof(unsigned), st);
   if (e == cudaSuccess) {
     k_gemm_tc<Epi><<<(unsigned)(tm * tn), NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, epi, err);
     fricc_note_launch();
@@ -438,12 +448,12 @@ int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int
 }
 
 int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t kp, float* W, int64_t ldw,
-                              void* stream) {
+                              unsigned* status, void* stream) {
   if (!W || v <= 0 || ldw < v * v) {
     fricc_set_error("vvvv_rebuild_bf16x3: bad arguments");
     return FRICC_ERR_ARG;
   }
-  return tc::launch(Ap, kp, Bp, kp, v * v, v * v, kp, tc::EpiVvvv{W, v, ldw}, (cudaStream_t)stream);
+  return tc::launch(Ap, kp, Bp, kp, v * v, v * v, kp, tc::EpiVvvv{W, v, ldw}, (cudaStream_t)stream, status);
 }
 
 }  // extern "C"

@@ -136,7 +136,7 @@ class _Handle:
 
 class FRICCSDGPU:
     def __init__(self, eris: D.DeviceERIs, fri_settings=None, level_shift=0.0, rn_draw=libc_uniform,
-                 wvvvv_t1t1="reference", precision="fp64", graph=False):
+                 wvvvv_t1t1="reference", precision="fp64", graph=False, rebuild_vvvv=True):
         s = dict(DEFAULT_SETTINGS)
         s.update(fri_settings or {})
         for c in s["compressed_contractions"]:
@@ -150,11 +150,23 @@ class FRICCSDGPU:
         self.level_shift = float(level_shift)
         self.rn_draw = rn_draw
         self.wvvvv_t1t1 = wvvvv_t1t1
-        if precision not in ("fp64", "df64"):
-            raise ValueError("precision must be 'fp64' or 'df64'")
+        if precision not in ("fp64", "df64", "split"):
+            raise ValueError("precision must be 'fp64', 'df64' or 'split'")
+        if precision == "split":
+            if getattr(eris, "vvvv_rebuild", None) is None:
+                raise ValueError("precision 'split' needs the integrals of fricc_gb300.cholesky.split_eris")
+            if wvvvv_t1t1 != "reference" or "O^2V^4" not in s["compressed_contractions"]:
+                raise ValueError("precision 'split' contracts (vv|vv) only through the compressed O^2V^4 term")
+        elif eris.vvvvT is None:
+            raise ValueError("these integrals keep no FP64 (vv|vv) block: use precision 'split'")
         self.precision = precision
+        self._df = precision in ("df64", "split")   # FP32-pair sparse terms and dense GEMMs
+        # split precision: rebuild (vv|vv) from the factor every iteration (it
+        # is never resident), or once and keep the FP32 block
+        self.rebuild_vvvv = bool(rebuild_vvvv)
+        self._vvvv_buf = None
         self.lib = L.load()
-        if precision == "df64":
+        if self._df:
             eris.prepare_splits()
         self._sp = _Handle()
         self._sp_w = _Handle()
@@ -187,7 +199,7 @@ class FRICCSDGPU:
         arithmetic; ``const`` names a constant integral block whose split
         form is cached on the DeviceERIs."""
         assert Wp.is_contiguous() and Op.is_contiguous()
-        if self.precision == "df64":
+        if self._df:
             W2 = self.eris.split(const) if const else D.split_f2(Wp, QS)
             assert W2.numel() == (Wp.numel() // QS) * ((QS + 1) // 2) * 4, "float-pair W' split with another QS"
             L.check(self.lib.fricc_spmm_f2(T, pa, pb, ka, kb, float(coef), _ptr(W2), int(QS), _ptr(Op), stream))
@@ -301,8 +313,8 @@ class FRICCSDGPU:
         if rn_dev is None:
             self._iter += 1
 
-        mm = D.gemm_df if self.precision == "df64" else D.gemm_torch
-        ein2 = D.einsum_df if self.precision == "df64" else torch.einsum   # two-operand O^3V^2 contractions
+        mm = D.gemm_df if self._df else D.gemm_torch
+        ein2 = D.einsum_df if self._df else torch.einsum   # two-operand O^3V^2 contractions
         f64, dev = t2.dtype, t2.device
         # cc_Foo / cc_Fvv share tt[p,q,r,s] = t2 + t1[p,r] t1[q,s]
         tt = t2 + ein("pr,qs->pqrs", t1, t1)
@@ -399,7 +411,20 @@ class FRICCSDGPU:
             S = D.wvvvv_sum_cd(t1, E)
             t2new += S[None, None, :, :] * t1[:, None, :, None] * t1[None, :, None, :]
             if "O^2V^4" in comp:
-                self._spmm(T, 0, 1, 2, 3, 1.0, E.vvvvT, v * v, t2new, st, const="vvvvT")  # (ac|bd) of 2323
+                if self.precision == "split":
+                    # (ac|bd) rebuilt from the split factor on the tensor cores, FP32
+                    # (every iteration into this solver's own buffer, or once
+                    # into the block the solvers of these integrals share)
+                    R = E.vvvv_rebuild
+                    if self.rebuild_vvvv:
+                        if self._vvvv_buf is None:
+                            self._vvvv_buf = torch.empty(v * v, R.ldw, dtype=torch.float32, device=t2.device)
+                        W = R.rebuild(self._vvvv_buf)
+                    else:
+                        W = R.W if R.W is not None else R.rebuild()
+                    L.check(self.lib.fricc_spmm_f1(T, 0, 1, 2, 3, 1.0, _ptr(W), v * v, R.ldw, _ptr(t2new), st))
+                else:
+                    self._spmm(T, 0, 1, 2, 3, 1.0, E.vvvvT, v * v, t2new, st, const="vvvvT")  # (ac|bd) of 2323
                 XY = torch.zeros(o, o, 2, o, v, dtype=t2.dtype, device=t2.device)
                 self._spmm(T, 0, 1, 2, 3, 1.0, E.ovvv_XY, 2 * ov, XY, st, const="ovvv_XY")  # t1 parts
                 XYv = XY.view(o * o, 2, o, v)
@@ -485,6 +510,8 @@ class FRICCSDGPU:
         r = self._res[:2].cpu()
         for h in self._handles_in_use():
             L.check(self.lib.fricc_sp_status(h.h))
+        if self.precision == "split":
+            self.eris.vvvv_rebuild.check()
         self.last_energy, self.last_normt = float(r[0]), float(r[1])
         return self.last_energy, self.last_normt
 

@@ -43,9 +43,15 @@ class DeviceERIs:
         vvvv = put(blocks["vvvv"]) if "vvvv" in blocks else None
         if "vvvvT" in blocks:
             self.vvvvT = put(blocks["vvvvT"])
-        else:
+        elif vvvv is not None:
             self.vvvvT = vvvv.permute(1, 3, 0, 2).contiguous()  # [c,d,a,b] = (ac|bd)
+        else:
+            # split precision: (vv|vv) is rebuilt from the factor when needed
+            # (fricc_gb300.cholesky); only sum_cd (ac|bd) is kept
+            self.vvvvT = None
         del vvvv
+        self._S0 = put(blocks["S0"]) if "S0" in blocks else None
+        self.vvvv_rebuild = blocks.get("vvvv_rebuild")
         self._derive()
 
     def _derive(self):
@@ -62,7 +68,7 @@ class DeviceERIs:
         # built densely: W'[c,d,(x,k,a)] = (kd|ac) for x=0 and (kc|ad) for x=1
         self.ovvv_XY = torch.stack([ovvv.permute(3, 1, 0, 2), ovvv.permute(1, 3, 0, 2)], dim=2).contiguous()
         # sum_cd of the three Wvvvv pieces (for the reference's Wvvvv.t1.t1 term)
-        self.S0 = self.vvvvT.sum(dim=(0, 1))                              # [a,b] = sum_cd (ac|bd)
+        self.S0 = self._S0 if self._S0 is not None else self.vvvvT.sum(dim=(0, 1))  # [a,b] = sum_cd (ac|bd)
         self.U = ovvv.sum(dim=(1, 3))                                     # [k,a] = sum_cd (kd|ac) = sum_cd (kc|ad)
         # W' of the sparse W-intermediate terms, [l,d,k,c]
         self.ovov_0312 = ovov.permute(0, 3, 2, 1).contiguous()            # (lc|kd)
@@ -85,7 +91,7 @@ class DeviceERIs:
         names = self.SPLIT_BLOCKS if names is None else names
         if any(n not in self._splits for n in names):
             for name in names:
-                if name not in self._splits:
+                if name not in self._splits and getattr(self, name) is not None:
                     self._splits[name] = split_f2(getattr(self, name))
             torch.cuda.current_stream().synchronize()
 

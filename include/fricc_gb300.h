@@ -167,6 +167,13 @@ int fricc_spmm_f2(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, 
  * 4 rows ceil(qs/2) floats, 16-byte aligned.  Stream-ordered. */
 int fricc_split_f2(const double* x, int64_t rows, int64_t qs, float* out4, void* stream);
 
+/* fricc_spmm against an FP32 W (rows of ldw floats, ldw even, 8-byte
+ * aligned base): the O^2V^4 term of the split-precision form, whose (vv|vv)
+ * block is rebuilt in FP32 by fricc_vvvv_rebuild_bf16x3.  T's values enter
+ * as float pairs and the sums are float-pair sums, as in fricc_spmm_f2. */
+int fricc_spmm_f1(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* W, int64_t QS,
+                  int64_t ldw, double* Op, void* stream);
+
 /* Strided batched GEMM, FP64 in and out, products and sums in FP32 pairs
  * (no reference counterpart; it runs the dense O^2V^3 contractions of the
  * iteration):  C[b] = alpha * A[b] @ B[b] + beta * C[b], b < batch.
@@ -258,7 +265,10 @@ int fricc_energy_update_lin(const double* t1num, const double* t2num, const doub
  *
  * fricc_vvvv_rebuild_bf16x3: from the split operands of L_vv^T
  * ([v*v][kp], row c*v + a = L[:, a, c]), W[(c*v + d)*ldw + a*v + b] = (ac|bd)
- * in FP32 -- the O^2V^4 operand of fricc_spmm_f1. */
+ * in FP32 -- the O^2V^4 operand of fricc_spmm_f1.  With status == NULL it
+ * synchronises like fricc_gemm_bf16_tn; otherwise it is stream-ordered (and
+ * capturable into a CUDA graph) and a gave-up wait ORs FRICC_DEV_TIMEOUT (2)
+ * into the device word *status. */
 int fricc_gemm_bf16_tn(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K,
                        float* C, int64_t ldc, void* stream);
 int fricc_gemm_bf16_tn_f64(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K,
@@ -266,7 +276,7 @@ int fricc_gemm_bf16_tn_f64(const void* A, int64_t lda, const void* B, int64_t ld
 int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int64_t kp, void* Ap, void* Bp,
                        void* stream);
 int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t kp, float* W, int64_t ldw,
-                              void* stream);
+                              unsigned* status, void* stream);
 
 /* A dedicated non-blocking stream of the current device, and its release
  * (no reference counterpart).  Solvers that overlap or capture work need

@@ -1,0 +1,123 @@
+"""The split-precision form: integral blocks rebuilt from the BF16 hi + lo
+Cholesky factor on the tcgen05 tensor cores (fricc_gb300.cholesky), the
+O^2V^4 term against the FP32 (vv|vv) block (fricc_spmm_f1), and the
+iteration's |dE_corr| against the plain FP64 GPU path (bound 1e-6 Eh)."""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+
+@pytest.fixture(scope="module")
+def systems():
+    from fricc_gb300.cholesky import split_eris
+    from fricc_gb300.rccsd_dense import DeviceERIs
+    from fricc_gb300.synthetic import make_system
+    s = make_system("o10v40", seed=0)
+    return s, DeviceERIs.from_system(s), split_eris(s)
+
+
+def test_split_blocks(gpulib, systems):
+    s, E, Es = systems
+    Lf = torch.from_numpy(s.L).cuda()
+    o = s.nocc
+    La = Lf.abs()
+    for name in ("ovvv", "oovv"):
+        sl = {"o": slice(0, o), "v": slice(o, s.nmo)}
+        p, q, r, t = (sl[c] for c in name)
+        scale = torch.einsum("Ppq,Prs->pqrs", La[:, p, q], La[:, r, t])
+        err = float(((getattr(Es, name) - getattr(E, name)).abs() / scale).max())
+        assert err < 2.0 ** -14, (name, err)
+    for name in ("oooo", "ovoo", "ovov", "ovvo"):
+        torch.testing.assert_close(getattr(Es, name), getattr(E, name), rtol=1e-13, atol=1e-16)
+    torch.testing.assert_close(Es.S0, E.S0, rtol=1e-12, atol=1e-15)
+    assert Es.vvvvT is None
+
+
+def test_spmm_f1_matches_fp64_kernel(gpulib, systems):
+    from fricc_gb300 import _lib as L
+    from fricc_gb300 import py_rccsd
+    s, E, Es = systems
+    o, v = s.nocc, s.nvir
+    R = Es.vvvv_rebuild
+    W = R.rebuild()
+    R.check()
+    t2 = torch.from_numpy(np.ascontiguousarray(s.mp2_amplitudes()[1])).cuda()
+    T = py_rccsd.SparseTensor4d(t2, t2.shape, 20000, "fri", "systematic", rn=0.5)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    W64 = W[:, : v * v].double().contiguous()
+    a = torch.randn(o * o, v * v, dtype=torch.float64, device="cuda") * 1e-3
+    b = a.clone()
+    L.check(gpulib.fricc_spmm(T.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(W64.data_ptr()), v * v,
+                              ctypes.c_void_p(a.data_ptr()), st))
+    L.check(gpulib.fricc_spmm_f1(T.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(W.data_ptr()), v * v, R.ldw,
+                                 ctypes.c_void_p(b.data_ptr()), st))
+    Ta = py_rccsd.SparseTensor4d(t2.abs(), t2.shape, 20000, "fri", "systematic", rn=0.5)
+    c = torch.zeros_like(a)
+    Wa = W64.abs()
+    L.check(gpulib.fricc_spmm(Ta.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(Wa.data_ptr()), v * v,
+                              ctypes.c_void_p(c.data_ptr()), st))
+    torch.cuda.synchronize()
+    bound = 1e-11 * (c + 1e-3 * 4)  # sum |W||T| plus the initial output's scale
+    assert bool(((a - b).abs() <= bound).all())
+
+
+def test_split_iteration_delta_e(gpulib, systems):
+    from fricc_gb300.friccsd import FRICCSDGPU
+    s, E, Es = systems
+    t1, t2 = [torch.from_numpy(x).cuda() for x in s.mp2_amplitudes()]
+    m = 20000
+    fp = FRICCSDGPU(E, {"m_keep": m}, precision="fp64")
+    sp = FRICCSDGPU(Es, {"m_keep": m}, precision="split")
+    a1, a2 = t1, t2
+    b1, b2 = t1, t2
+    worst = 0.0
+    for it in range(6):
+        rn = [0.1 + 0.13 * it, 0.77 - 0.09 * it]
+        a1, a2 = fp.update_amps(a1, a2, rn=rn)
+        b1, b2 = sp.update_amps(b1, b2, rn=rn)
+        ea, eb = fp.read_energy()[0], sp.read_energy()[0]
+        worst = max(worst, abs(ea - eb))
+    assert worst < 1e-6, worst
+    assert Es.vvvv_rebuild.rebuilds >= 6
+
+
+def test_split_rebuild_once_same_as_every_iteration(gpulib, systems):
+    from fricc_gb300.friccsd import FRICCSDGPU
+    s, E, Es = systems
+    t1, t2 = [torch.from_numpy(x).cuda() for x in s.mp2_amplitudes()]
+    a = FRICCSDGPU(Es, {"m_keep": 20000}, precision="split")
+    b = FRICCSDGPU(Es, {"m_keep": 20000}, precision="split", rebuild_vvvv=False)
+    for it in range(3):
+        rn = [0.2 + 0.1 * it, 0.6]
+        a1, a2 = a.update_amps(t1, t2, rn=rn)
+        b1, b2 = b.update_amps(t1, t2, rn=rn)
+        assert torch.equal(a2, b2) and torch.equal(a1, b1)  # the rebuild is deterministic
+        t1, t2 = a1, a2
+
+
+def test_split_graph_replay_matches_eager(gpulib, systems):
+    from fricc_gb300.friccsd import FRICCSDGPU
+    s, E, Es = systems
+    t1, t2 = [torch.from_numpy(x).cuda() for x in s.mp2_amplitudes()]
+    g = FRICCSDGPU(Es, {"m_keep": 20000}, precision="split", graph=True)
+    e = FRICCSDGPU(Es, {"m_keep": 20000}, precision="split")
+    a1, a2, b1, b2 = t1, t2, t1, t2
+    for it in range(4):
+        rn = [0.15 + 0.2 * it, 0.5]
+        a1, a2 = g.update_amps(a1, a2, rn=rn)
+        b1, b2 = e.update_amps(b1, b2, rn=rn)
+        assert abs(g.read_energy()[0] - e.read_energy()[0]) < 1e-14
+    torch.testing.assert_close(a2, b2, rtol=1e-13, atol=1e-18)
+
+
+def test_split_requires_split_eris(gpulib, systems):
+    from fricc_gb300.friccsd import FRICCSDGPU
+    s, E, Es = systems
+    with pytest.raises(ValueError):
+        FRICCSDGPU(E, {"m_keep": 100}, precision="split")
+    with pytest.raises(ValueError):
+        FRICCSDGPU(Es, {"m_keep": 100}, precision="df64")
