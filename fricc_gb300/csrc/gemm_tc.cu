@@ -2,17 +2,22 @@
 // split-BF16x3 rebuild of integral blocks from a Cholesky factor.
 //
 // C[M][N] = A[M][K] B[N][K]^T, A and B BF16 and K-major, FP32 accumulation in
-// tensor memory (TMEM).  One CTA computes one 128 x 256 tile:
+// tensor memory (TMEM).  A persistent kernel: one CTA per SM walks 128 x 256
+// output tiles, with warp-specialised roles:
 //   warp 0, one lane  -- TMA producer: 128 x 64 and 256 x 64 operand boxes
 //                        (128-byte swizzle) into a 4-stage shared-memory ring,
 //                        each stage guarded by a "full" and an "empty" mbarrier;
 //   warp 1, one lane  -- MMA issuer: four tcgen05.mma (M=128, N=256, K=16) per
-//                        stage into one TMEM accumulator of 256 columns, then
-//                        tcgen05.commit to the stage's "empty" barrier;
-//   warp 2            -- allocates and frees the TMEM columns;
-//   all four warps    -- epilogue: tcgen05.ld of their 32 TMEM lanes (one
+//                        stage into one of two TMEM accumulators of 256
+//                        columns, tcgen05.commit to the stage's "empty"
+//                        barrier, and at the end of a tile to the
+//                        accumulator's "full" barrier (warp 1 also allocates
+//                        and frees the 512 TMEM columns);
+//   warps 2-5         -- epilogue: tcgen05.ld of their 32 TMEM lanes (one
 //                        output row per thread, 16 columns per load) into the
-//                        epilogue functor.
+//                        epilogue functor, then an arrive on the
+//                        accumulator's "empty" barrier -- overlapping the
+//                        MMAs of the next tile in the other accumulator.
 // Every mbarrier wait is bounded (2 s of global time); a wait that gives up
 // sets a device error word, the roles stop issuing, the producer waits
 // (bounded) for its copies in flight, and the CTA frees its TMEM and exits.
@@ -33,7 +38,8 @@ constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
 constexpr int A_BYTES = BM * BK * 2;  // 16 KB
 constexpr int B_BYTES = BN * BK * 2;  // 32 KB
 constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024;  // + alignment slack
-constexpr int NT = 128;
+constexpr int EPI_WARPS = 4;
+constexpr int NT = 32 * (2 + EPI_WARPS);  // producer warp, MMA warp, epilogue warps
 
 // Instruction descriptor (kind::f16): D = F32 (bits 4-5 = 1), A = B = BF16
 // (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
@@ -170,49 +176,64 @@ struct EpiRowMajorF64 {
   }
 };
 
-// The (vv|vv) block for the O^2V^4 contraction: GEMM row r1 = c v + a, column
-// r2 = d v + b, value (ac|bd), stored at W[(c v + d) * ldw + a v + b] (rows
-// (c,d), columns (a,b): the layout the FP32 sparse kernel streams).
+// The (vv|vv) block for the O^2V^4 contraction.  The factor is symmetric
+// (L[P,a,c] = L[P,c,a]), so row r of L_vv^T serves both operands and the
+// GEMM value at (r1, r2) = (d v + b, c v + a) is (bd|ac) = (ac|bd); it is
+// stored at W[(c v + d) * ldw + a v + b] (rows (c,d), columns (a,b): the
+// layout the FP32 sparse kernel streams).  A warp's 32 lanes are 32
+// consecutive r1, i.e. consecutive b: each of its stores writes one
+// contiguous 128-byte run (two where the warp crosses a d boundary).
 struct EpiVvvv {
   float* W;
   int64_t v, ldw;
   __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x) const {
-    const int64_t vv = v * v;
-    if (r1 >= vv) return;
-    const int64_t c = r1 / v, a = r1 - c * v;
-    int64_t d = r2 / v, b = r2 - d * v;
+    if (r1 >= v * v) return;
+    const int64_t d = r1 / v, b = r1 - d * v;
+    int64_t c = r2 / v, a = r2 - c * v;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-      if (d < v) W[(c * v + d) * ldw + a * v + b] = x[i];
-      if (++b == v) {
-        b = 0;
-        ++d;
+      if (c < v) W[(c * v + d) * ldw + a * v + b] = x[i];
+      if (++a == v) {
+        a = 0;
+        ++c;
       }
     }
   }
 };
 
+__device__ __forceinline__ void mbar_arrive(uint32_t a) {
+  asm volatile(
+      "{\n\t.reg .b64 st;\n\t"
+      "mbarrier.arrive.shared::cta.b64 st, [%0];\n\t}" ::"r"(a)
+      : "memory");
+}
+
+// linear tile index -> (m tile, n tile): groups of 16 M tiles sweep all N
+// tiles, so the CTAs working at once share a few operand panels in L2
+__device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, int& mt, int& nt) {
+  constexpr int GROUP = 16;
+  const int per_group = GROUP * tiles_n;
+  const int g = id / per_group, rem = id - g * per_group;
+  const int gm = min(GROUP, tiles_m - g * GROUP);
+  mt = g * GROUP + rem % gm;
+  nt = rem / gm;
+}
+
+// Persistent: each CTA walks tiles blockIdx.x, +gridDim.x, ...  The TMEM
+// accumulator is double-buffered (2 x 256 columns), so the epilogue warps
+// drain tile i while the MMA warp accumulates tile i+1.
 template <class Epi>
 __global__ void __launch_bounds__(NT, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb, int K, int tiles_m,
               int tiles_n, Epi epi, unsigned* err) {
   extern __shared__ uint8_t dsm[];
-  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], done;
+  __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2];
   __shared__ uint32_t tbase;
   __shared__ int failed;
   const uint32_t base = (smem_u32(dsm) + 1023u) & ~1023u;
   const uint32_t sA = base, sB = base + STAGES * A_BYTES;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-
-  // tile order: groups of 16 M tiles sweep all N tiles, so the CTAs resident
-  // at once share a few operand panels in L2
-  constexpr int GROUP = 16;
-  const int id = blockIdx.x;
-  const int per_group = GROUP * tiles_n;
-  const int g = id / per_group, rem = id - g * per_group;
-  const int gm = min(GROUP, tiles_m - g * GROUP);
-  const int mt = g * GROUP + rem % gm, nt = rem / gm;
-  const int m0 = mt * BM, n0 = nt * BN;
+  const int ntiles = tiles_m * tiles_n;
   const int nk = (K + BK - 1) / BK;
 
   if (threadIdx.x == 0) {
@@ -220,13 +241,16 @@ __global__ void __launch_bounds__(NT, 1)
       mbar_init(smem_u32(&full[s]), 1);
       mbar_init(smem_u32(&empty[s]), 1);
     }
-    mbar_init(smem_u32(&done), 1);
+    for (int b = 0; b < 2; ++b) {
+      mbar_init(smem_u32(&tfull[b]), 1);
+      mbar_init(smem_u32(&tempty[b]), EPI_WARPS);
+    }
     failed = 0;
     asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
   }
-  if (warp == 2) {
+  if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tbase)),
-                 "r"((uint32_t)BN)
+                 "r"((uint32_t)(2 * BN))
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -235,66 +259,102 @@ __global__ void __launch_bounds__(NT, 1)
   tc_fence_after();
   const uint32_t tmem = tbase;
 
-  if (warp == 0 && lane == 0) {
-    int issued = 0;
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-      if (kb >= STAGES && !mbar_wait(smem_u32(&empty[s]), ph ^ 1u)) {
-        atomicOr(err, FRICC_DEV_TIMEOUT);
-        failed = 1;
-        break;
+  if (warp == 0) {
+    if (lane == 0) {  // TMA producer
+      int g = 0;      // k blocks issued over all tiles
+      for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&failed; tile += gridDim.x) {
+        int mt, nt;
+        tile_coords(tile, tiles_m, tiles_n, mt, nt);
+        for (int kb = 0; kb < nk; ++kb, ++g) {
+          const int s = g % STAGES;
+          const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
+          if (g >= STAGES && !mbar_wait(smem_u32(&empty[s]), ph ^ 1u)) {
+            atomicOr(err, FRICC_DEV_TIMEOUT);
+            failed = 1;
+            break;
+          }
+          mbar_expect_tx(smem_u32(&full[s]), A_BYTES + B_BYTES);
+          tma_load_2d(sA + s * A_BYTES, &tma, kb * BK, mt * BM, smem_u32(&full[s]));
+          tma_load_2d(sB + s * B_BYTES, &tmb, kb * BK, nt * BN, smem_u32(&full[s]));
+        }
       }
-      if (*(volatile int*)&failed) break;
-      mbar_expect_tx(smem_u32(&full[s]), A_BYTES + B_BYTES);
-      tma_load_2d(sA + s * A_BYTES, &tma, kb * BK, m0, smem_u32(&full[s]));
-      tma_load_2d(sB + s * B_BYTES, &tmb, kb * BK, n0, smem_u32(&full[s]));
-      ++issued;
+      if (*(volatile int*)&failed) {
+        // let the copies in flight land before the CTA's shared memory goes away
+        for (int q = g - STAGES < 0 ? 0 : g - STAGES; q < g; ++q)
+          mbar_wait(smem_u32(&full[q % STAGES]), (uint32_t)(q / STAGES) & 1u);
+      }
     }
-    if (*(volatile int*)&failed) {
-      // let the copies in flight land before the CTA's shared memory goes away
-      for (int kb = issued - STAGES < 0 ? 0 : issued - STAGES; kb < issued; ++kb)
-        mbar_wait(smem_u32(&full[kb % STAGES]), (uint32_t)(kb / STAGES) & 1u);
+  } else if (warp == 1) {
+    if (lane == 0) {  // MMA issuer
+      int g = 0, i = 0;
+      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+        const int b = i & 1;
+        const uint32_t u = (uint32_t)(i >> 1);
+        // the epilogue must have drained this accumulator's previous tile
+        if (i >= 2 && !mbar_wait(smem_u32(&tempty[b]), (u & 1u) ^ 1u)) {
+          atomicOr(err, FRICC_DEV_TIMEOUT);
+          failed = 1;
+        }
+        if (*(volatile int*)&failed) break;
+        tc_fence_after();
+        const uint32_t acc = tmem + (uint32_t)(b * BN);
+        for (int kb = 0; kb < nk; ++kb, ++g) {
+          const int s = g % STAGES;
+          const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
+          if (!mbar_wait(smem_u32(&full[s]), ph)) {
+            atomicOr(err, FRICC_DEV_TIMEOUT);
+            failed = 1;
+            break;
+          }
+          tc_fence_after();
+          const uint32_t a0 = sA + s * A_BYTES, b0 = sB + s * B_BYTES;
+#pragma unroll
+          for (int k = 0; k < BK / 16; ++k)
+            tc_mma(acc, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), IDESC, (kb | k) != 0);
+          tc_commit(smem_u32(&empty[s]));
+        }
+        tc_commit(smem_u32(&tfull[b]));  // arrives when this tile's MMAs have completed
+        if (*(volatile int*)&failed) break;
+      }
     }
-  } else if (warp == 1 && lane == 0) {
-    for (int kb = 0; kb < nk; ++kb) {
-      const int s = kb % STAGES;
-      const uint32_t ph = (uint32_t)(kb / STAGES) & 1u;
-      if (!mbar_wait(smem_u32(&full[s]), ph)) {
-        atomicOr(err, FRICC_DEV_TIMEOUT);
-        failed = 1;
+  } else {  // epilogue warps 2..5: TMEM lanes 32 (warp % 4) ...
+    const int quad = warp & 3;
+    int i = 0;
+    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      const int b = i & 1;
+      const uint32_t u = (uint32_t)(i >> 1);
+      bool ok = mbar_wait(smem_u32(&tfull[b]), u & 1u);
+      ok = __all_sync(0xffffffffu, ok && !*(volatile int*)&failed);
+      if (!ok) {
+        if (lane == 0) {
+          atomicOr(err, FRICC_DEV_TIMEOUT);
+          failed = 1;
+        }
         break;
       }
       tc_fence_after();
-      const uint32_t a0 = sA + s * A_BYTES, b0 = sB + s * B_BYTES;
-#pragma unroll
-      for (int k = 0; k < BK / 16; ++k)
-        tc_mma(tmem, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), IDESC, (kb | k) != 0);
-      tc_commit(smem_u32(&empty[s]));
+      int mt, nt;
+      tile_coords(tile, tiles_m, tiles_n, mt, nt);
+      const int64_t row = (int64_t)mt * BM + quad * 32 + lane;
+      const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * BN);
+#pragma unroll 1
+      for (int c = 0; c < BN / 16; ++c) {
+        float v[16];
+        tc_ld16(lane_base + (uint32_t)(c * 16), v);
+        epi(row, (int64_t)nt * BN + c * 16, v);
+      }
+      tc_fence_before();
+      __syncwarp();
+      if (lane == 0) mbar_arrive(smem_u32(&tempty[b]));
     }
-    tc_commit(smem_u32(&done));  // arrives when every MMA above has completed
   }
   __syncwarp();
-
-  bool ok = mbar_wait(smem_u32(&done), 0);
-  ok = __all_sync(0xffffffffu, ok && !*(volatile int*)&failed) && nk > 0;
-  tc_fence_after();
-  if (ok) {
-    const int64_t row = (int64_t)m0 + warp * 32 + lane;
-    const uint32_t lane_base = tmem + ((uint32_t)(warp * 32) << 16);
-#pragma unroll 1
-    for (int c = 0; c < BN / 16; ++c) {
-      float v[16];
-      tc_ld16(lane_base + (uint32_t)(c * 16), v);
-      epi(row, (int64_t)n0 + c * 16, v);
-    }
-  } else if (lane == 0 && warp == 0) {
-    atomicOr(err, FRICC_DEV_TIMEOUT);
-  }
   tc_fence_before();
   __syncthreads();
-  if (warp == 2)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)BN) : "memory");
+  tc_fence_after();
+  if (warp == 1)
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * BN))
+                 : "memory");
 }
 
 // x [rows][ld] FP64 (the first k columns used) -> A' [rows][kp] = [hi | hi | lo]
@@ -381,8 +441,19 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
     if (e != cudaSuccess) return fricc_cuda_fail(e, "gemm_tc attribute", __FILE__, __LINE__);
     attr = true;
   }
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess || nsm <= 0) {
+      nsm = 0;
+      return fricc_cuda_fail(e != cudaSuccess ? e : cudaErrorUnknown, "gemm_tc SM count", __FILE__, __LINE__);
+    }
+  }
+  const unsigned grid = (unsigned)(tm * tn < nsm ? tm * tn : nsm);  // persistent: one CTA per SM
   if (status) {
-    k_gemm_tc<Epi><<<(unsigned)(tm * tn), NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, epi, status);
+    k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, epi, status);
     fricc_note_launch();
     e = cudaGetLastError();
     return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "gemm_tc", __FILE__, __LINE__);
@@ -392,7 +463,7 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
   if (rc) return rc;
   e = cudaMemsetAsync(err, 0, sizeof(unsigned), st);
   if (e == cudaSuccess) {
-    k_gemm_tc<Epi><<<(unsigned)(tm * tn), NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, epi, err);
+    k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, epi, err);
     fricc_note_launch();
     e = cudaGetLastError();
   }
