@@ -70,6 +70,68 @@ def split_bf16x3(x: torch.Tensor, kp: int | None = None):
     return Ap, Bp
 
 
+def _kp(k: int) -> int:
+    return -(-3 * k // 8) * 8
+
+
+def _split_view(x, rows, k, ri, sro, sri, sk, want_a, want_b):
+    kp = _kp(k)
+    Ap = torch.empty(rows, kp, dtype=torch.bfloat16, device=x.device) if want_a else None
+    Bp = torch.empty(rows, kp, dtype=torch.bfloat16, device=x.device) if want_b else None
+    L.check(L.load().fricc_split_bf16x3_strided(_p(x), rows, k, ri, sro, sri, sk, kp,
+                                                _p(Ap) if want_a else None, _p(Bp) if want_b else None, _st()))
+    return Ap if want_a else Bp
+
+
+# the tensor-core path needs enough output tiles to spread over the SMs; a
+# GEMM with a long K and a tiny output (the O^2V^3 T1 term, cc_Foo, cc_Fvv)
+# stays on the split-K FP32-pair GEMM
+_MIN_TILES = 38
+
+
+def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.0, beta: float = 0.0,
+            status: torch.Tensor | None = None):
+    """C = alpha A @ B + beta C with split-BF16x3 operands on the tcgen05
+    tensor cores (FP32 accumulation, FP64 epilogue): the contract of
+    ``rccsd_dense.gemm_df`` -- FP64 tensors with any strides, 2-D or batched
+    3-D with one operand shared (batch stride 0), flattened into one GEMM.
+    Shapes with too few output tiles, or both operands batched, go to
+    ``gemm_df``.  ``status`` (a device int32) makes the launch
+    stream-ordered; a gave-up pipeline wait is recorded there."""
+    from . import rccsd_dense as D
+    sA, bA = D._strides3(A)
+    sB, bB = D._strides3(B)
+    sC, batch = D._strides3(C)
+    M, N, K = C.shape[-2], C.shape[-1], A.shape[-1]
+    assert A.shape[-2] == M and B.shape[-2] == K and B.shape[-1] == N and bA in (1, batch) and bB in (1, batch)
+    a_b = batch > 1 and bA > 1 and sA[2] != 0   # batched (an expanded view has batch stride 0)
+    b_b = batch > 1 and bB > 1 and sB[2] != 0
+    if batch > 1 and a_b == b_b:
+        return D.gemm_df(A, B, C, alpha, beta)
+    Mf = M * (batch if a_b else 1)
+    Nf = N * (batch if b_b else 1)
+    if -(-Mf // 128) * -(-Nf // 256) < _MIN_TILES or K == 0:
+        return D.gemm_df(A, B, C, alpha, beta)
+    # rows of A' are (b, m) or m; rows of B' are (b, n) or n; both K-major
+    if Mf > M:
+        Ap = _split_view(A, Mf, K, M, sA[2], sA[0], sA[1], True, False)
+        mi, sro, sri = M, sC[2], sC[0]
+    else:
+        Ap = _split_view(A, M, K, 1, sA[0], 0, sA[1], True, False)
+        mi, sro, sri = M, 0, sC[0]
+    if Nf > N:
+        Bp = _split_view(B, Nf, K, N, sB[2], sB[1], sB[0], False, True)
+        ni, sco, sci = N, sC[2], sC[1]
+    else:
+        Bp = _split_view(B, N, K, 1, sB[1], 0, sB[0], False, True)
+        ni, sco, sci = N, 0, sC[1]
+    kp = Ap.shape[1]
+    L.check(L.load().fricc_gemm_bf16_tn_strided(_p(Ap), kp, _p(Bp), kp, Mf, Nf, kp, _p(C), mi, ni, sro, sri, sco,
+                                                sci, float(alpha), float(beta),
+                                                _p(status) if status is not None else None, _st()))
+    return C
+
+
 def lvv_t(Lf: torch.Tensor, nocc: int) -> torch.Tensor:
     """L_vv^T [v*v, naux] (row c*v + a = L[:, a, c]) of a factor L [naux, nmo, nmo]."""
     naux = Lf.shape[0]

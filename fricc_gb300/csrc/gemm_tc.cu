@@ -176,6 +176,33 @@ struct EpiRowMajorF64 {
   }
 };
 
+// C (FP64, strided) = alpha acc + beta C, for GEMMs whose rows or columns
+// flatten a (batch, index) pair: element (r, c) sits at
+// (r / mi) sro + (r % mi) sri + (c / ni) sco + (c % ni) sci.
+struct EpiStridedF64 {
+  double* C;
+  int64_t M, N, mi, ni, sro, sri, sco, sci;
+  double alpha, beta;
+  __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v) const {
+    if (r >= M) return;
+    const int64_t ro = r / mi;
+    const int64_t rbase = ro * sro + (r - ro * mi) * sri;
+    int64_t co = c0 / ni, ci = c0 - co * ni;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      if (c0 + i < N) {
+        double* p = C + rbase + co * sco + ci * sci;
+        const double x = alpha * f2d_bits(v[i]);
+        *p = beta == 0.0 ? x : x + beta * *p;
+      }
+      if (++ci == ni) {
+        ci = 0;
+        ++co;
+      }
+    }
+  }
+};
+
 // The (vv|vv) block for the O^2V^4 contraction.  The factor is symmetric
 // (L[P,a,c] = L[P,c,a]), so row r of L_vv^T serves both operands and the
 // GEMM value at (r1, r2) = (d v + b, c v + a) is (bd|ac) = (ac|bd); it is
@@ -357,24 +384,29 @@ __global__ void __launch_bounds__(NT, 1)
                  : "memory");
 }
 
-// x [rows][ld] FP64 (the first k columns used) -> A' [rows][kp] = [hi | hi | lo]
-// and B' [rows][kp] = [hi | lo | hi], kp >= 3k, padding columns zero.
-__global__ void k_split_bf16x3(const double* __restrict__ x, int64_t rows, int64_t k, int64_t ld, int64_t kp,
-                               __nv_bfloat16* __restrict__ Ap, __nv_bfloat16* __restrict__ Bp) {
+// x (FP64, strided) -> A' [rows][kp] = [hi | hi | lo] and B' [rows][kp] =
+// [hi | lo | hi] (either may be null), kp >= 3k, padding columns zero.
+// Row r = (r / ri, r % ri) and column j < k of x sit at
+// (r / ri) sro + (r % ri) sri + j sk: a transposed or batch-flattened view
+// becomes a K-major operand in the same pass.
+__global__ void k_split_bf16x3(const double* __restrict__ x, int64_t rows, int64_t k, int64_t ri, int64_t sro,
+                               int64_t sri, int64_t sk, int64_t kp, __nv_bfloat16* __restrict__ Ap,
+                               __nv_bfloat16* __restrict__ Bp) {
   const int64_t n = rows * kp;
   for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
     const int64_t r = t / kp, j = t - r * kp;
     const int64_t part = j / k, col = j - part * k;
     __nv_bfloat16 a = __float2bfloat16(0.0f), b = a;
     if (part < 3) {
-      const double xv = x[r * ld + col];
+      const int64_t ro = r / ri;
+      const double xv = x[ro * sro + (r - ro * ri) * sri + col * sk];
       const __nv_bfloat16 hi = __double2bfloat16(xv);
       const __nv_bfloat16 lo = __double2bfloat16(xv - (double)__bfloat162float(hi));
       a = part < 2 ? hi : lo;
       b = part == 1 ? lo : hi;
     }
-    Ap[t] = a;
-    Bp[t] = b;
+    if (Ap) Ap[t] = a;
+    if (Bp) Bp[t] = b;
   }
 }
 
@@ -501,9 +533,9 @@ int fricc_gemm_bf16_tn_f64(const void* A, int64_t lda, const void* B, int64_t ld
   return tc::launch(A, lda, B, ldb, M, N, K, tc::EpiRowMajorF64{C, M, N, ldc}, (cudaStream_t)stream);
 }
 
-int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int64_t kp, void* Ap, void* Bp,
-                       void* stream) {
-  if (rows < 0 || k <= 0 || ld < k || kp < 3 * k || (rows > 0 && (!x || !Ap || !Bp))) {
+int fricc_split_bf16x3_strided(const double* x, int64_t rows, int64_t k, int64_t ri, int64_t sro, int64_t sri,
+                               int64_t sk, int64_t kp, void* Ap, void* Bp, void* stream) {
+  if (rows < 0 || k <= 0 || ri <= 0 || kp < 3 * k || (kp % 8) || (rows > 0 && (!x || (!Ap && !Bp)))) {
     fricc_set_error("split_bf16x3: bad arguments");
     return FRICC_ERR_ARG;
   }
@@ -512,10 +544,30 @@ int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int
   int64_t g = fricc_cdiv(n, 256);
   if (g > 152 * 32) g = 152 * 32;
   tc::k_split_bf16x3<<<(unsigned)g, 256, 0, (cudaStream_t)stream>>>(
-      x, rows, k, ld, kp, static_cast<__nv_bfloat16*>(Ap), static_cast<__nv_bfloat16*>(Bp));
+      x, rows, k, ri, sro, sri, sk, kp, static_cast<__nv_bfloat16*>(Ap), static_cast<__nv_bfloat16*>(Bp));
   fricc_note_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "split_bf16x3", __FILE__, __LINE__);
+}
+
+int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int64_t kp, void* Ap, void* Bp,
+                       void* stream) {
+  if (ld < k || !Ap || !Bp) {
+    fricc_set_error("split_bf16x3: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  return fricc_split_bf16x3_strided(x, rows, k, 1, ld, ld, 1, kp, Ap, Bp, stream);
+}
+
+int fricc_gemm_bf16_tn_strided(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N,
+                               int64_t K, double* C, int64_t mi, int64_t ni, int64_t sro, int64_t sri, int64_t sco,
+                               int64_t sci, double alpha, double beta, unsigned* status, void* stream) {
+  if (!C || mi <= 0 || ni <= 0) {
+    fricc_set_error("gemm_bf16_tn_strided: bad output");
+    return FRICC_ERR_ARG;
+  }
+  return tc::launch(A, lda, B, ldb, M, N, K, tc::EpiStridedF64{C, M, N, mi, ni, sro, sri, sco, sci, alpha, beta},
+                    (cudaStream_t)stream, status);
 }
 
 int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t kp, float* W, int64_t ldw,

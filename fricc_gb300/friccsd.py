@@ -165,6 +165,7 @@ class FRICCSDGPU:
         # is never resident), or once and keep the FP32 block
         self.rebuild_vvvv = bool(rebuild_vvvv)
         self._vvvv_buf = None
+        self._tc_status = torch.zeros(1, dtype=torch.int32, device=eris.device)
         self.lib = L.load()
         if self._df:
             eris.prepare_splits()
@@ -313,8 +314,18 @@ class FRICCSDGPU:
         if rn_dev is None:
             self._iter += 1
 
-        mm = D.gemm_df if self._df else D.gemm_torch
-        ein2 = D.einsum_df if self._df else torch.einsum   # two-operand O^3V^2 contractions
+        if self.precision == "split":   # split-BF16x3 on the tensor cores (FP32-pair where the grid is too small)
+            from .cholesky import gemm_tc
+            tcs = self._tc_status
+
+            def mm(A_, B_, C_, alpha=1.0, beta=0.0):
+                return gemm_tc(A_, B_, C_, alpha, beta, status=tcs)
+
+            def ein2(spec, A_, B_):
+                return D.einsum_df(spec, A_, B_, gemm=mm)
+        else:
+            mm = D.gemm_df if self._df else D.gemm_torch
+            ein2 = D.einsum_df if self._df else torch.einsum   # two-operand O^3V^2 contractions
         f64, dev = t2.dtype, t2.device
         # cc_Foo / cc_Fvv share tt[p,q,r,s] = t2 + t1[p,r] t1[q,s]
         tt = t2 + ein("pr,qs->pqrs", t1, t1)
@@ -512,6 +523,8 @@ class FRICCSDGPU:
             L.check(self.lib.fricc_sp_status(h.h))
         if self.precision == "split":
             self.eris.vvvv_rebuild.check()
+            if int(self._tc_status.item()):
+                raise L.FriccError(5, "split-precision GEMM: a bounded tensor-core pipeline wait gave up")
         self.last_energy, self.last_normt = float(r[0]), float(r[1])
         return self.last_energy, self.last_normt
 

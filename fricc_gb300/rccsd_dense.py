@@ -185,13 +185,14 @@ def gemm_df(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
     return C
 
 
-def einsum_df(spec: str, A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
+def einsum_df(spec: str, A: torch.Tensor, B: torch.Tensor, gemm=None) -> torch.Tensor:
     """Two-operand einsum as one strided batched GEMM on the FP32-pair kernel.
 
     Indices shared by both operands and the output form the batch, A-only
     output indices the rows, B-only output indices the columns, shared
     non-output indices the contraction; an index in one operand only and not
-    in the output is summed out first.  Operand groups merge into one stride
+    in the output is summed out first.  ``gemm`` replaces the FP32-pair GEMM
+    (the split-precision form passes the tensor-core one).  Operand groups merge into one stride
     where the layout allows (``reshape`` copies otherwise); the result is a
     view of a contiguous [batch, rows, cols] buffer in the output's order."""
     lhs, out = spec.replace(" ", "").split("->")
@@ -221,7 +222,7 @@ def einsum_df(spec: str, A: torch.Tensor, B: torch.Tensor) -> torch.Tensor:
         if K == 0:
             C.zero_()
         else:
-            gemm_df(Ap, Bp, C)
+            (gemm or gemm_df)(Ap, Bp, C)
     order = bt + mi + ni
     return C.view([size[c] for c in order]).permute([order.index(c) for c in out])
 

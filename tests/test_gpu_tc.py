@@ -84,3 +84,46 @@ def test_vvvv_rebuild_matches_fp64(gpulib):
     scale = torch.einsum("Pac,Pbd->cdab", Lv.abs(), Lv.abs()).reshape(v * v, v * v)
     err = float(((W.double() - ref).abs() / scale).max())
     assert err < 2.0 ** -14, err
+
+
+def _bound_ok(C, ref, scale, tol=2.0 ** -14):
+    return bool(((C - ref).abs() <= tol * scale + 1e-300).all())
+
+
+@pytest.mark.parametrize("case", ["2d", "2d_transposed", "a_shared", "b_shared", "beta", "fallback_small"])
+def test_gemm_tc_contract(gpulib, case):
+    """gemm_tc follows gemm_df's contract (strided, batched with a shared
+    operand, alpha/beta) within the split-BF16x3 error."""
+    from fricc_gb300.cholesky import gemm_tc
+    g = torch.Generator().manual_seed(11)
+    r = lambda *s: torch.randn(*s, generator=g, dtype=torch.float64).cuda()
+    alpha, beta = 1.0, 0.0
+    if case == "2d":
+        A, B = r(3000, 70), r(70, 300)
+        C = torch.empty(3000, 300, dtype=torch.float64, device="cuda")
+    elif case == "2d_transposed":   # A and B as transposed views
+        A = r(45, 2900).T
+        B = r(310, 45).T
+        C = torch.empty(2900, 310, dtype=torch.float64, device="cuda")
+    elif case == "a_shared":   # Lvv t2: A (v x v) shared over o^2 batches
+        A = r(60, 60).unsqueeze(0).expand(400, 60, 60)
+        B = r(400, 60, 60)
+        C = torch.empty(400, 60, 60, dtype=torch.float64, device="cuda")
+    elif case == "b_shared":   # X t1: B shared over batches, A a transposed batched view
+        A = r(400, 20, 60).transpose(1, 2)
+        B = r(20, 60).unsqueeze(0).expand(400, 20, 60)
+        C = torch.empty(400, 60, 60, dtype=torch.float64, device="cuda")
+    elif case == "beta":
+        A, B = r(6000, 40), r(40, 200)
+        C = r(6000, 200)
+        alpha, beta = -1.0, 1.0
+    else:                      # too few output tiles: the FP32-pair GEMM
+        A, B = r(30, 20000), r(20000, 150)
+        C = torch.empty(30, 150, dtype=torch.float64, device="cuda")
+    C0 = C.clone()
+    ref = alpha * torch.matmul(A, B) + beta * C0
+    scale = abs(alpha) * torch.matmul(A.abs(), B.abs()) + abs(beta) * C0.abs()
+    gemm_tc(A, B, C, alpha, beta)
+    assert _bound_ok(C, ref, scale)
+    if case == "fallback_small":
+        assert float(((C - ref).abs() / scale).max()) < 1e-12  # FP32 pairs, not BF16
