@@ -167,8 +167,12 @@ class FRICCSDGPU:
         self._vvvv_buf = None
         self._tc_status = torch.zeros(1, dtype=torch.int32, device=eris.device)
         self.lib = L.load()
-        if self._df:
+        if precision == "df64":
             eris.prepare_splits()
+        elif precision == "split":
+            o_, v_ = eris.nocc, eris.mo_energy.numel() - eris.nocc
+            eris.prepare_f32({"ovvv_XY": 2 * o_ * v_, "ovov": o_ * v_, "ovov_0313_0113": o_ * v_,
+                              "ovov_0312": o_ * v_, "ovov_cdkl": o_ * o_})
         self._sp = _Handle()
         self._sp_w = _Handle()
         # streams of this solver alone (torch's pool hands the same few streams
@@ -200,7 +204,14 @@ class FRICCSDGPU:
         arithmetic; ``const`` names a constant integral block whose split
         form is cached on the DeviceERIs."""
         assert Wp.is_contiguous() and Op.is_contiguous()
-        if self._df:
+        if self.precision == "split":
+            # the integrals carry split-BF16x3 error (~2^-16): W' in FP32
+            # (half the bytes of the float-pair layout), T values and sums
+            # still float pairs
+            W32 = self.eris.f32(const, QS) if const else D.to_f32_rows(Wp, QS)
+            L.check(self.lib.fricc_spmm_f1(T, pa, pb, ka, kb, float(coef), _ptr(W32), int(QS), W32.shape[1],
+                                           _ptr(Op), stream))
+        elif self._df:
             W2 = self.eris.split(const) if const else D.split_f2(Wp, QS)
             assert W2.numel() == (Wp.numel() // QS) * ((QS + 1) // 2) * 4, "float-pair W' split with another QS"
             L.check(self.lib.fricc_spmm_f2(T, pa, pb, ka, kb, float(coef), _ptr(W2), int(QS), _ptr(Op), stream))

@@ -111,6 +111,22 @@ class DeviceERIs:
             if self.device.type == "cuda":
                 torch.cuda.current_stream().synchronize()
 
+    def prepare_f32(self, blocks: dict):
+        """Build the FP32 forms {name: qs} once, and wait for them (solvers
+        on other streams read them afterwards)."""
+        if any(("f32", n, q) not in self._splits for n, q in blocks.items()):
+            for n, q in blocks.items():
+                self.f32(n, q)
+            torch.cuda.current_stream().synchronize()
+
+    def f32(self, name, qs):
+        """FP32 rows (qs columns, padded to even) of a constant block, built
+        once: the W' operands of the split-precision form."""
+        key = ("f32", name, qs)
+        if key not in self._splits:
+            self._splits[key] = to_f32_rows(getattr(self, name), qs)
+        return self._splits[key]
+
     def split(self, name):
         """The float-pair form of a constant block (prepare_splits() built it)."""
         if name not in self._splits:
@@ -237,6 +253,18 @@ def gemm_torch(A, B, C, alpha=1.0, beta=0.0):
             C.mul_(beta)
         C.add_(R, alpha=alpha)
     return C
+
+
+def to_f32_rows(x: torch.Tensor, qs: int) -> torch.Tensor:
+    """x viewed as [rows][qs] in FP32, rows padded to an even length (the
+    layout fricc_spmm_f1 reads as float pairs)."""
+    rows = x.numel() // qs
+    x2 = x.reshape(rows, qs)
+    if qs % 2 == 0:
+        return x2.to(torch.float32).contiguous()
+    out = torch.zeros(rows, qs + 1, dtype=torch.float32, device=x.device)
+    out[:, :qs] = x2
+    return out
 
 
 def split_f2(x: torch.Tensor, qs: int = None) -> torch.Tensor:
