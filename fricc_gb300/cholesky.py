@@ -89,15 +89,22 @@ def _split_view(x, rows, k, ri, sro, sri, sk, want_a, want_b):
 _MIN_TILES = 38
 
 
+def split_a(A: torch.Tensor) -> torch.Tensor:
+    """A' ([hi|hi|lo], K-major) of a 2-D FP64 operand, for reuse through
+    ``gemm_tc(..., a_split=)`` when A is a constant integral block."""
+    return _split_view(A, A.shape[0], A.shape[1], A.shape[0], 0, A.stride(0), A.stride(1), True, False)
+
+
 def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.0, beta: float = 0.0,
-            status: torch.Tensor | None = None):
+            status: torch.Tensor | None = None, a_split: torch.Tensor | None = None):
     """C = alpha A @ B + beta C with split-BF16x3 operands on the tcgen05
     tensor cores (FP32 accumulation, FP64 epilogue): the contract of
     ``rccsd_dense.gemm_df`` -- FP64 tensors with any strides, 2-D or batched
     3-D with one operand shared (batch stride 0), flattened into one GEMM.
     Shapes with too few output tiles, or both operands batched, go to
     ``gemm_df``.  ``status`` (a device int32) makes the launch
-    stream-ordered; a gave-up pipeline wait is recorded there."""
+    stream-ordered; a gave-up pipeline wait is recorded there.
+    ``a_split``: A' of a 2-D A made once by ``split_a``."""
     from . import rccsd_dense as D
     sA, bA = D._strides3(A)
     sB, bB = D._strides3(B)
@@ -113,17 +120,21 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
     if -(-Mf // 128) * -(-Nf // 256) < _MIN_TILES or K == 0:
         return D.gemm_df(A, B, C, alpha, beta)
     # rows of A' are (b, m) or m; rows of B' are (b, n) or n; both K-major
-    if Mf > M:
+    if a_split is not None:
+        assert Mf == M and a_split.shape == (M, _kp(K))
+        Ap = a_split
+        mi, sro, sri = M, 0, sC[0]
+    elif Mf > M:
         Ap = _split_view(A, Mf, K, M, sA[2], sA[0], sA[1], True, False)
         mi, sro, sri = M, sC[2], sC[0]
     else:
-        Ap = _split_view(A, M, K, 1, sA[0], 0, sA[1], True, False)
+        Ap = _split_view(A, M, K, M, 0, sA[0], sA[1], True, False)
         mi, sro, sri = M, 0, sC[0]
     if Nf > N:
         Bp = _split_view(B, Nf, K, N, sB[2], sB[1], sB[0], False, True)
         ni, sco, sci = N, sC[2], sC[1]
     else:
-        Bp = _split_view(B, N, K, 1, sB[1], 0, sB[0], False, True)
+        Bp = _split_view(B, N, K, N, 0, sB[1], sB[0], False, True)
         ni, sco, sci = N, 0, sC[1]
     kp = Ap.shape[1]
     L.check(L.load().fricc_gemm_bf16_tn_strided(_p(Ap), kp, _p(Bp), kp, Mf, Nf, kp, _p(C), mi, ni, sro, sri, sco,

@@ -389,24 +389,71 @@ __global__ void __launch_bounds__(NT, 1)
 // Row r = (r / ri, r % ri) and column j < k of x sit at
 // (r / ri) sro + (r % ri) sri + j sk: a transposed or batch-flattened view
 // becomes a K-major operand in the same pass.
-__global__ void k_split_bf16x3(const double* __restrict__ x, int64_t rows, int64_t k, int64_t ri, int64_t sro,
-                               int64_t sri, int64_t sk, int64_t kp, __nv_bfloat16* __restrict__ Ap,
-                               __nv_bfloat16* __restrict__ Bp) {
-  const int64_t n = rows * kp;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < n; t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t r = t / kp, j = t - r * kp;
-    const int64_t part = j / k, col = j - part * k;
-    __nv_bfloat16 a = __float2bfloat16(0.0f), b = a;
-    if (part < 3) {
-      const int64_t ro = r / ri;
-      const double xv = x[ro * sro + (r - ro * ri) * sri + col * sk];
-      const __nv_bfloat16 hi = __double2bfloat16(xv);
-      const __nv_bfloat16 lo = __double2bfloat16(xv - (double)__bfloat162float(hi));
-      a = part < 2 ? hi : lo;
-      b = part == 1 ? lo : hi;
+__device__ __forceinline__ void split_put(double xv, int64_t k, __nv_bfloat16* ar, __nv_bfloat16* br) {
+  const __nv_bfloat16 hi = __double2bfloat16(xv);
+  const __nv_bfloat16 lo = __double2bfloat16(xv - (double)__bfloat162float(hi));
+  if (ar) {
+    ar[0] = hi;
+    ar[k] = hi;
+    ar[2 * k] = lo;
+  }
+  if (br) {
+    br[0] = hi;
+    br[k] = lo;
+    br[2 * k] = hi;
+  }
+}
+
+// columns contiguous (or any layout): one row per block pass, threads over j
+__global__ void k_split_rows(const double* __restrict__ x, int64_t rows, int64_t k, int64_t ri, int64_t sro,
+                             int64_t sri, int64_t sk, int64_t kp, __nv_bfloat16* __restrict__ Ap,
+                             __nv_bfloat16* __restrict__ Bp) {
+  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+    const int64_t ro = r / ri;
+    const double* xr = x + ro * sro + (r - ro * ri) * sri;
+    __nv_bfloat16* ar = Ap ? Ap + r * kp : nullptr;
+    __nv_bfloat16* br = Bp ? Bp + r * kp : nullptr;
+    for (int64_t j = threadIdx.x; j < k; j += blockDim.x) split_put(xr[j * sk], k, ar ? ar + j : nullptr,
+                                                                    br ? br + j : nullptr);
+    for (int64_t j = 3 * k + threadIdx.x; j < kp; j += blockDim.x) {
+      if (ar) ar[j] = __float2bfloat16(0.0f);
+      if (br) br[j] = __float2bfloat16(0.0f);
     }
-    if (Ap) Ap[t] = a;
-    if (Bp) Bp[t] = b;
+  }
+}
+
+// rows contiguous (sri == 1, within runs of ri rows): 32 x 32 tiles read
+// along r and written along j through shared memory
+__global__ void k_split_tr(const double* __restrict__ x, int64_t rows, int64_t k, int64_t ri, int64_t sro, int64_t sk,
+                           int64_t kp, __nv_bfloat16* __restrict__ Ap, __nv_bfloat16* __restrict__ Bp) {
+  __shared__ double tile[32][33];
+  const int64_t tiles_r = fricc_cdiv(rows, 32), tiles_k = fricc_cdiv(k, 32);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;  // 32 x 8 threads
+  for (int64_t t = blockIdx.x; t < tiles_r * tiles_k; t += gridDim.x) {
+    const int64_t r0 = (t / tiles_k) * 32, j0 = (t % tiles_k) * 32;
+    __syncthreads();
+    for (int yy = ty; yy < 32; yy += 8) {  // tile[j][r]: read x(r0 + tx, j0 + yy)
+      const int64_t r = r0 + tx, j = j0 + yy;
+      double v = 0.0;
+      if (r < rows && j < k) {
+        const int64_t ro = r / ri;
+        v = x[ro * sro + (r - ro * ri) + j * sk];
+      }
+      tile[yy][tx] = v;
+    }
+    __syncthreads();
+    for (int yy = ty; yy < 32; yy += 8) {  // write row r0 + yy, columns j0 + tx
+      const int64_t r = r0 + yy, j = j0 + tx;
+      if (r < rows && j < k)
+        split_put(tile[tx][yy], k, Ap ? Ap + r * kp + j : nullptr, Bp ? Bp + r * kp + j : nullptr);
+    }
+  }
+  // padding columns
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < rows * (kp - 3 * k);
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t r = t / (kp - 3 * k), j = 3 * k + (t - r * (kp - 3 * k));
+    if (Ap) Ap[r * kp + j] = __float2bfloat16(0.0f);
+    if (Bp) Bp[r * kp + j] = __float2bfloat16(0.0f);
   }
 }
 
@@ -541,10 +588,16 @@ int fricc_split_bf16x3_strided(const double* x, int64_t rows, int64_t k, int64_t
   }
   const int64_t n = rows * kp;
   if (n == 0) return FRICC_OK;
-  int64_t g = fricc_cdiv(n, 256);
-  if (g > 152 * 32) g = 152 * 32;
-  tc::k_split_bf16x3<<<(unsigned)g, 256, 0, (cudaStream_t)stream>>>(
-      x, rows, k, ri, sro, sri, sk, kp, static_cast<__nv_bfloat16*>(Ap), static_cast<__nv_bfloat16*>(Bp));
+  auto* a = static_cast<__nv_bfloat16*>(Ap);
+  auto* b = static_cast<__nv_bfloat16*>(Bp);
+  if (sri == 1 && sk != 1 && ri >= 32) {
+    int64_t g = fricc_cdiv(rows, 32) * fricc_cdiv(k, 32);
+    if (g > 152 * 16) g = 152 * 16;
+    tc::k_split_tr<<<(unsigned)g, 256, 0, (cudaStream_t)stream>>>(x, rows, k, ri, sro, sk, kp, a, b);
+  } else {
+    const int64_t g = rows < 152 * 16 ? rows : 152 * 16;
+    tc::k_split_rows<<<(unsigned)g, 128, 0, (cudaStream_t)stream>>>(x, rows, k, ri, sro, sri, sk, kp, a, b);
+  }
   fricc_note_launch();
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "split_bf16x3", __FILE__, __LINE__);

@@ -173,6 +173,7 @@ class FRICCSDGPU:
             o_, v_ = eris.nocc, eris.mo_energy.numel() - eris.nocc
             eris.prepare_f32({"ovvv_XY": 2 * o_ * v_, "ovov": o_ * v_, "ovov_0313_0113": o_ * v_,
                               "ovov_0312": o_ * v_, "ovov_cdkl": o_ * o_})
+            eris.prepare_tc_a(("ovvv_iabc", "ovvv", "ovvv_kacd"))
         self._sp = _Handle()
         self._sp_w = _Handle()
         # streams of this solver alone (torch's pool hands the same few streams
@@ -329,13 +330,18 @@ class FRICCSDGPU:
             from .cholesky import gemm_tc
             tcs = self._tc_status
 
-            def mm(A_, B_, C_, alpha=1.0, beta=0.0):
-                return gemm_tc(A_, B_, C_, alpha, beta, status=tcs)
+            def mm(A_, B_, C_, alpha=1.0, beta=0.0, const=None):
+                return gemm_tc(A_, B_, C_, alpha, beta, status=tcs,
+                               a_split=E.tc_a(const) if const else None)
 
             def ein2(spec, A_, B_):
                 return D.einsum_df(spec, A_, B_, gemm=mm)
         else:
-            mm = D.gemm_df if self._df else D.gemm_torch
+            mm0 = D.gemm_df if self._df else D.gemm_torch
+
+            def mm(A_, B_, C_, alpha=1.0, beta=0.0, const=None):
+                return mm0(A_, B_, C_, alpha, beta)
+
             ein2 = D.einsum_df if self._df else torch.einsum   # two-operand O^3V^2 contractions
         f64, dev = t2.dtype, t2.device
         # cc_Foo / cc_Fvv share tt[p,q,r,s] = t2 + t1[p,r] t1[q,s]
@@ -371,7 +377,7 @@ class FRICCSDGPU:
         # T2 driver terms (:179-187)
         Y1 = ein2("kibc,jc->kibj", E.oovv, t1)
         R = torch.empty(o * v * v, o, dtype=f64, device=dev)   # R[(i,a,b), j] = sum_c (ia|cb) t_jc
-        mm(E.ovvv_iabc.view(o * v * v, v), t1.T, R, 1.0, 0.0)
+        mm(E.ovvv_iabc.view(o * v * v, v), t1.T, R, 1.0, 0.0, const="ovvv_iabc")
         tmp = R.view(o, v, v, o).permute(0, 3, 1, 2) - ein2("ka,kibj->ijab", t1, Y1)
         t2new = tmp + tmp.permute(1, 0, 3, 2)
         tmp2 = ein2("kcai,jc->akij", E.ovvo, t1) + E.ovoo.permute(1, 3, 0, 2)
@@ -398,7 +404,7 @@ class FRICCSDGPU:
 
         if "O^3V^3" in comp:  # sparse_cc_Wvoov / sparse_cc_Wvovo (:334-376)
             R = torch.empty(o * v * v, o, dtype=f64, device=dev)   # R[(k,c,a), i] = sum_d (kc|ad) t_id
-            mm(E.ovvv.view(o * v * v, v), t1.T, R, 1.0, 0.0)
+            mm(E.ovvv.view(o * v * v, v), t1.T, R, 1.0, 0.0, const="ovvv")
             Wvoov = (R.view(o, v, v, o).permute(2, 0, 3, 1) - ein2("kcli,la->akic", E.ovoo, t1)
                      + E.ovvo.permute(2, 0, 3, 1))
             Wp = Wvoov.permute(0, 2, 1, 3).contiguous()                         # [a,i,k,c]
@@ -406,7 +412,7 @@ class FRICCSDGPU:
             self._spmm(Tw, 2, 0, 1, 3, 1.0, E.ovov_0313_0113, ov, Wp, st, const="ovov_0313_0113")  # 0313+0113
             Wvoov = Wp.permute(0, 2, 1, 3)                                      # (a,k,i,c)
             Wvoov -= ein2("lkci,la->akic", ein2("ldkc,id->lkci", E.ovov, t1), t1)
-            mm(E.ovvv_kacd.view(o * v * v, v), t1.T, R, 1.0, 0.0)   # R[(k,a,c), i] = sum_d (kd|ac) t_id
+            mm(E.ovvv_kacd.view(o * v * v, v), t1.T, R, 1.0, 0.0, const="ovvv_kacd")   # R[(k,a,c), i] = sum_d (kd|ac) t_id
             Wvovo = (R.view(o, v, v, o).permute(1, 0, 2, 3) - ein2("lcki,la->akci", E.ovoo, t1)
                      + E.oovv.permute(2, 0, 3, 1))
             Wq = Wvovo.permute(0, 3, 1, 2).contiguous()                         # [a,i,k,c]

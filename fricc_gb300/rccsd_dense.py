@@ -119,6 +119,21 @@ class DeviceERIs:
                 self.f32(n, q)
             torch.cuda.current_stream().synchronize()
 
+    def prepare_tc_a(self, names):
+        """The split-BF16x3 A' of constant [o v v, v] blocks (the A operands
+        of the split-precision form's t1 GEMMs), made once and waited for."""
+        from .cholesky import split_a
+        if any(("tcA", n) not in self._splits for n in names):
+            for n in names:
+                x = getattr(self, n)
+                self._splits[("tcA", n)] = split_a(x.reshape(-1, x.shape[-1]))
+            torch.cuda.current_stream().synchronize()
+
+    def tc_a(self, name):
+        if ("tcA", name) not in self._splits:
+            raise RuntimeError(f"split A' of {name} missing: call prepare_tc_a() first")
+        return self._splits[("tcA", name)]
+
     def f32(self, name, qs):
         """FP32 rows (qs columns, padded to even) of a constant block, built
         once: the W' operands of the split-precision form."""
