@@ -54,7 +54,8 @@ SIGNATURES = [
     ("fricc_vvvv_rebuild_bf16x3", ctypes.c_int, [_vp, _vp, _i64, _i64, _dp, _i64, _vp, _vp]),
     ("fricc_split_bf16x3_strided", ctypes.c_int, [_dp, _i64, _i64, _i64, _i64, _i64, _i64, _i64, _vp, _vp, _vp]),
     ("fricc_gemm_bf16_tn_strided", ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _dp, _i64, _i64, _i64,
-                                                  _i64, _i64, _i64, ctypes.c_double, ctypes.c_double, _vp, _vp]),
+                                                  _i64, _i64, _i64, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                  _vp, _vp]),
     ("fricc_gemm_df", ctypes.c_int, [_dp, _dp, _dp, _i64, _i64, _i64, _i64, _i64p, _i64p, _i64p, ctypes.c_double,
                                       ctypes.c_double, _vp]),
     ("fricc_contract_flops", ctypes.c_double, [ctypes.c_char_p, _vp]),

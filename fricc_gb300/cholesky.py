@@ -83,10 +83,22 @@ def _split_view(x, rows, k, ri, sro, sri, sk, want_a, want_b):
     return Ap if want_a else Bp
 
 
-# the tensor-core path needs enough output tiles to spread over the SMs; a
-# GEMM with a long K and a tiny output (the O^2V^3 T1 term, cc_Foo, cc_Fvv)
-# stays on the split-K FP32-pair GEMM
+# the tensor-core path needs enough work units to spread over the SMs: a
+# GEMM with few output tiles and a long K (the O^2V^3 T1 term, cc_Foo,
+# cc_Fvv) splits K; one with few tiles and a short K stays on the FP32-pair
+# GEMM
 _MIN_TILES = 38
+_SMS = 152
+
+
+def _ksplit(tiles: int, kp: int) -> int:
+    """1, a K split for few tiles and a long K, or 0 (use the FP32-pair GEMM)."""
+    if tiles >= _MIN_TILES:
+        return 1
+    nk = -(-kp // 64)
+    if nk < 16:
+        return 0
+    return max(2, min(nk // 4, -(-_SMS // tiles)))
 
 
 def split_a(A: torch.Tensor) -> torch.Tensor:
@@ -101,8 +113,8 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
     tensor cores (FP32 accumulation, FP64 epilogue): the contract of
     ``rccsd_dense.gemm_df`` -- FP64 tensors with any strides, 2-D or batched
     3-D with one operand shared (batch stride 0), flattened into one GEMM.
-    Shapes with too few output tiles, or both operands batched, go to
-    ``gemm_df``.  ``status`` (a device int32) makes the launch
+    Few output tiles with a long K split K; few tiles with a short K, or both
+    operands batched, go to ``gemm_df``.  ``status`` (a device int32) makes the launch
     stream-ordered; a gave-up pipeline wait is recorded there.
     ``a_split``: A' of a 2-D A made once by ``split_a``."""
     from . import rccsd_dense as D
@@ -117,7 +129,8 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
         return D.gemm_df(A, B, C, alpha, beta)
     Mf = M * (batch if a_b else 1)
     Nf = N * (batch if b_b else 1)
-    if -(-Mf // 128) * -(-Nf // 256) < _MIN_TILES or K == 0:
+    ks = _ksplit(-(-Mf // 128) * -(-Nf // 256), _kp(K)) if K > 0 else 0
+    if ks == 0:
         return D.gemm_df(A, B, C, alpha, beta)
     # rows of A' are (b, m) or m; rows of B' are (b, n) or n; both K-major
     if a_split is not None:
@@ -138,7 +151,7 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
         ni, sco, sci = N, 0, sC[1]
     kp = Ap.shape[1]
     L.check(L.load().fricc_gemm_bf16_tn_strided(_p(Ap), kp, _p(Bp), kp, Mf, Nf, kp, _p(C), mi, ni, sro, sri, sco,
-                                                sci, float(alpha), float(beta),
+                                                sci, float(alpha), float(beta), ks,
                                                 _p(status) if status is not None else None, _st()))
     return C
 

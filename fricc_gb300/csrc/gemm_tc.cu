@@ -149,7 +149,7 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 struct EpiRowMajor {
   float* C;
   int64_t M, N, ldc;
-  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v) const {
+  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v, int) const {
     if (row >= M) return;
     float* c = C + row * ldc + col0;
     if (col0 + 16 <= N && (ldc & 3) == 0) {
@@ -167,7 +167,7 @@ struct EpiRowMajor {
 struct EpiRowMajorF64 {
   double* C;
   int64_t M, N, ldc;
-  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v) const {
+  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v, int) const {
     if (row >= M) return;
     double* c = C + row * ldc + col0;
 #pragma unroll
@@ -183,7 +183,7 @@ struct EpiStridedF64 {
   double* C;
   int64_t M, N, mi, ni, sro, sri, sco, sci;
   double alpha, beta;
-  __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v) const {
+  __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v, int) const {
     if (r >= M) return;
     const int64_t ro = r / mi;
     const int64_t rbase = ro * sro + (r - ro * mi) * sri;
@@ -203,6 +203,33 @@ struct EpiStridedF64 {
   }
 };
 
+// split K: slice s of the sum into the FP32 partial P[s][M][N]
+struct EpiPartial {
+  float* P;
+  int64_t M, N;
+  __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v, int s) const {
+    if (r >= M) return;
+    float* p = P + ((int64_t)s * M + r) * N + c0;
+#pragma unroll
+    for (int i = 0; i < 16; ++i)
+      if (c0 + i < N) p[i] = v[i];
+  }
+};
+
+// C (the EpiStridedF64 mapping) = alpha sum_s P[s] + beta C, slices summed
+// in order (deterministic)
+__global__ void k_reduce_partials(const float* __restrict__ P, int ks, int64_t M, int64_t N, EpiStridedF64 o) {
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < M * N; t += (int64_t)gridDim.x * blockDim.x) {
+    double acc = 0.0;
+    for (int s = 0; s < ks; ++s) acc += f2d_bits(P[(int64_t)s * M * N + t]);
+    const int64_t r = t / N, c = t - r * N;
+    const int64_t ro = r / o.mi, co = c / o.ni;
+    double* p = o.C + ro * o.sro + (r - ro * o.mi) * o.sri + co * o.sco + (c - co * o.ni) * o.sci;
+    const double x = o.alpha * acc;
+    *p = o.beta == 0.0 ? x : x + o.beta * *p;
+  }
+}
+
 // The (vv|vv) block for the O^2V^4 contraction.  The factor is symmetric
 // (L[P,a,c] = L[P,c,a]), so row r of L_vv^T serves both operands and the
 // GEMM value at (r1, r2) = (d v + b, c v + a) is (bd|ac) = (ac|bd); it is
@@ -213,7 +240,7 @@ struct EpiStridedF64 {
 struct EpiVvvv {
   float* W;
   int64_t v, ldw;
-  __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x) const {
+  __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x, int) const {
     if (r1 >= v * v) return;
     const int64_t d = r1 / v, b = r1 - d * v;
     int64_t c = r2 / v, a = r2 - c * v;
@@ -252,7 +279,7 @@ __device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, in
 template <class Epi>
 __global__ void __launch_bounds__(NT, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb, int K, int tiles_m,
-              int tiles_n, Epi epi, unsigned* err) {
+              int tiles_n, int ksplit, Epi epi, unsigned* err) {
   extern __shared__ uint8_t dsm[];
   __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2];
   __shared__ uint32_t tbase;
@@ -262,6 +289,10 @@ __global__ void __launch_bounds__(NT, 1)
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int ntiles = tiles_m * tiles_n;
   const int nk = (K + BK - 1) / BK;
+  // split K: work unit u = (tile u % ntiles, K slice u / ntiles), each slice
+  // nkc k blocks (the last one shorter, never empty)
+  const int nkc = (nk + ksplit - 1) / ksplit;
+  const int nunits = ntiles * ksplit;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -289,10 +320,11 @@ __global__ void __launch_bounds__(NT, 1)
   if (warp == 0) {
     if (lane == 0) {  // TMA producer
       int g = 0;      // k blocks issued over all tiles
-      for (int tile = blockIdx.x; tile < ntiles && !*(volatile int*)&failed; tile += gridDim.x) {
+      for (int u = blockIdx.x; u < nunits && !*(volatile int*)&failed; u += gridDim.x) {
         int mt, nt;
-        tile_coords(tile, tiles_m, tiles_n, mt, nt);
-        for (int kb = 0; kb < nk; ++kb, ++g) {
+        tile_coords(u % ntiles, tiles_m, tiles_n, mt, nt);
+        const int kb1 = min(nk, (u / ntiles + 1) * nkc);
+        for (int kb = (u / ntiles) * nkc; kb < kb1; ++kb, ++g) {
           const int s = g % STAGES;
           const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
           if (g >= STAGES && !mbar_wait(smem_u32(&empty[s]), ph ^ 1u)) {
@@ -314,9 +346,10 @@ __global__ void __launch_bounds__(NT, 1)
   } else if (warp == 1) {
     if (lane == 0) {  // MMA issuer
       int g = 0, i = 0;
-      for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+      for (int w = blockIdx.x; w < nunits; w += gridDim.x, ++i) {
         const int b = i & 1;
         const uint32_t u = (uint32_t)(i >> 1);
+        const int kb0 = (w / ntiles) * nkc, kb1 = min(nk, kb0 + nkc);
         // the epilogue must have drained this accumulator's previous tile
         if (i >= 2 && !mbar_wait(smem_u32(&tempty[b]), (u & 1u) ^ 1u)) {
           atomicOr(err, FRICC_DEV_TIMEOUT);
@@ -325,7 +358,7 @@ __global__ void __launch_bounds__(NT, 1)
         if (*(volatile int*)&failed) break;
         tc_fence_after();
         const uint32_t acc = tmem + (uint32_t)(b * BN);
-        for (int kb = 0; kb < nk; ++kb, ++g) {
+        for (int kb = kb0; kb < kb1; ++kb, ++g) {
           const int s = g % STAGES;
           const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
           if (!mbar_wait(smem_u32(&full[s]), ph)) {
@@ -337,7 +370,7 @@ __global__ void __launch_bounds__(NT, 1)
           const uint32_t a0 = sA + s * A_BYTES, b0 = sB + s * B_BYTES;
 #pragma unroll
           for (int k = 0; k < BK / 16; ++k)
-            tc_mma(acc, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), IDESC, (kb | k) != 0);
+            tc_mma(acc, sw128_desc(a0 + k * 32), sw128_desc(b0 + k * 32), IDESC, ((kb - kb0) | k) != 0);
           tc_commit(smem_u32(&empty[s]));
         }
         tc_commit(smem_u32(&tfull[b]));  // arrives when this tile's MMAs have completed
@@ -347,7 +380,7 @@ __global__ void __launch_bounds__(NT, 1)
   } else {  // epilogue warps 2..5: TMEM lanes 32 (warp % 4) ...
     const int quad = warp & 3;
     int i = 0;
-    for (int tile = blockIdx.x; tile < ntiles; tile += gridDim.x, ++i) {
+    for (int w = blockIdx.x; w < nunits; w += gridDim.x, ++i) {
       const int b = i & 1;
       const uint32_t u = (uint32_t)(i >> 1);
       bool ok = mbar_wait(smem_u32(&tfull[b]), u & 1u);
@@ -361,14 +394,14 @@ __global__ void __launch_bounds__(NT, 1)
       }
       tc_fence_after();
       int mt, nt;
-      tile_coords(tile, tiles_m, tiles_n, mt, nt);
+      tile_coords(w % ntiles, tiles_m, tiles_n, mt, nt);
       const int64_t row = (int64_t)mt * BM + quad * 32 + lane;
       const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * BN);
 #pragma unroll 1
       for (int c = 0; c < BN / 16; ++c) {
         float v[16];
         tc_ld16(lane_base + (uint32_t)(c * 16), v);
-        epi(row, (int64_t)nt * BN + c * 16, v);
+        epi(row, (int64_t)nt * BN + c * 16, v, w / ntiles);
       }
       tc_fence_before();
       __syncwarp();
@@ -496,16 +529,31 @@ int make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t k, int64_t
 // status == nullptr: synchronous, a gave-up wait returns FRICC_ERR_TIMEOUT;
 // otherwise stream-ordered (capturable): the kernel ORs FRICC_DEV_TIMEOUT into
 // *status and the caller reads it later.
+int sm_count(int* out) {
+  static int nsm = 0;
+  if (!nsm) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+    if (e != cudaSuccess || nsm <= 0) {
+      nsm = 0;
+      return fricc_cuda_fail(e != cudaSuccess ? e : cudaErrorUnknown, "gemm_tc SM count", __FILE__, __LINE__);
+    }
+  }
+  *out = nsm;
+  return FRICC_OK;
+}
+
 template <class Epi>
 int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K, const Epi& epi,
-           cudaStream_t st, unsigned* status = nullptr) {
+           cudaStream_t st, unsigned* status = nullptr, int ksplit = 1) {
   if (!A || !B || M <= 0 || N <= 0 || K <= 0 || lda < K || ldb < K || (lda % 8) || (ldb % 8) ||
       (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16)) {
     fricc_set_error("gemm_tc: bad arguments (K-major BF16 operands: 16-byte aligned, ld >= K, ld %% 8 == 0)");
     return FRICC_ERR_ARG;
   }
   const int64_t tm = fricc_cdiv(M, BM), tn = fricc_cdiv(N, BN);
-  if (tm * tn > 0x7fffffffLL || K > 0x7fffffffLL) {
+  if (tm * tn * ksplit > 0x7fffffffLL || K > 0x7fffffffLL) {
     fricc_set_error("gemm_tc: problem too large for one launch");
     return FRICC_ERR_ARG;
   }
@@ -520,19 +568,20 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
     if (e != cudaSuccess) return fricc_cuda_fail(e, "gemm_tc attribute", __FILE__, __LINE__);
     attr = true;
   }
-  static int nsm = 0;
-  if (!nsm) {
-    int dev = 0;
-    e = cudaGetDevice(&dev);
-    if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess || nsm <= 0) {
-      nsm = 0;
-      return fricc_cuda_fail(e != cudaSuccess ? e : cudaErrorUnknown, "gemm_tc SM count", __FILE__, __LINE__);
-    }
+  int nsm = 0;
+  rc = sm_count(&nsm);
+  if (rc) return rc;
+  const int64_t nk = fricc_cdiv(K, BK);
+  if (ksplit < 1 || ksplit > nk) {
+    fricc_set_error("gemm_tc: split K must be between 1 and the number of 64-wide K blocks");
+    return FRICC_ERR_ARG;
   }
-  const unsigned grid = (unsigned)(tm * tn < nsm ? tm * tn : nsm);  // persistent: one CTA per SM
+  const int64_t nkc = fricc_cdiv(nk, ksplit);
+  ksplit = (int)fricc_cdiv(nk, nkc);  // every slice non-empty
+  const int64_t units = tm * tn * ksplit;
+  const unsigned grid = (unsigned)(units < nsm ? units : nsm);  // persistent: one CTA per SM
   if (status) {
-    k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, epi, status);
+    k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, status);
     fricc_note_launch();
     e = cudaGetLastError();
     return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "gemm_tc", __FILE__, __LINE__);
@@ -542,7 +591,7 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
   if (rc) return rc;
   e = cudaMemsetAsync(err, 0, sizeof(unsigned), st);
   if (e == cudaSuccess) {
-    k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, epi, err);
+    k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, err);
     fricc_note_launch();
     e = cudaGetLastError();
   }
@@ -614,13 +663,32 @@ int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int
 
 int fricc_gemm_bf16_tn_strided(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N,
                                int64_t K, double* C, int64_t mi, int64_t ni, int64_t sro, int64_t sri, int64_t sco,
-                               int64_t sci, double alpha, double beta, unsigned* status, void* stream) {
-  if (!C || mi <= 0 || ni <= 0) {
-    fricc_set_error("gemm_bf16_tn_strided: bad output");
+                               int64_t sci, double alpha, double beta, int ksplit, unsigned* status, void* stream) {
+  if (!C || mi <= 0 || ni <= 0 || ksplit < 1) {
+    fricc_set_error("gemm_bf16_tn_strided: bad output or split");
     return FRICC_ERR_ARG;
   }
-  return tc::launch(A, lda, B, ldb, M, N, K, tc::EpiStridedF64{C, M, N, mi, ni, sro, sri, sco, sci, alpha, beta},
-                    (cudaStream_t)stream, status);
+  const tc::EpiStridedF64 out{C, M, N, mi, ni, sro, sri, sco, sci, alpha, beta};
+  cudaStream_t st = (cudaStream_t)stream;
+  if (ksplit == 1) return tc::launch(A, lda, B, ldb, M, N, K, out, st, status);
+  // split K: FP32 partials per slice, then one ordered reduction into C
+  const int64_t nk = fricc_cdiv(K, tc::BK);
+  if (ksplit > nk) ksplit = (int)nk;
+  const int ks = (int)fricc_cdiv(nk, fricc_cdiv(nk, ksplit));
+  float* P = nullptr;
+  int rc = fricc_alloc_t(&P, (size_t)ks * M * N, st);
+  if (rc) return rc;
+  rc = tc::launch(A, lda, B, ldb, M, N, K, tc::EpiPartial{P, M, N}, st, status, ks);
+  if (!rc) {
+    int64_t g = fricc_cdiv(M * N, 256);
+    if (g > 152 * 16) g = 152 * 16;
+    tc::k_reduce_partials<<<(unsigned)g, 256, 0, st>>>(P, ks, M, N, out);
+    fricc_note_launch();
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fricc_cuda_fail(e, "gemm_tc reduce", __FILE__, __LINE__);
+  }
+  fricc_free(P, st);
+  return rc;
 }
 
 int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t kp, float* W, int64_t ldw,

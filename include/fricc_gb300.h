@@ -285,12 +285,15 @@ int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t
  * operand); either output may be NULL.
  * fricc_gemm_bf16_tn_strided: C = alpha (A B^T) + beta C, C FP64 with
  * element (r, c) at (r / mi)*sro + (r % mi)*sri + (c / ni)*sco + (c % ni)*sci
- * (beta == 0 does not read C); status as for fricc_vvvv_rebuild_bf16x3. */
+ * (beta == 0 does not read C); status as for fricc_vvvv_rebuild_bf16x3.
+ * ksplit > 1 splits K into that many slices (for a long K and few output
+ * tiles): FP32 partial sums per slice, then one reduction in slice order
+ * (deterministic). */
 int fricc_split_bf16x3_strided(const double* x, int64_t rows, int64_t k, int64_t ri, int64_t sro, int64_t sri,
                                int64_t sk, int64_t kp, void* Ap, void* Bp, void* stream);
 int fricc_gemm_bf16_tn_strided(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N,
                                int64_t K, double* C, int64_t mi, int64_t ni, int64_t sro, int64_t sri, int64_t sco,
-                               int64_t sci, double alpha, double beta, unsigned* status, void* stream);
+                               int64_t sci, double alpha, double beta, int ksplit, unsigned* status, void* stream);
 
 /* A dedicated non-blocking stream of the current device, and its release
  * (no reference counterpart).  Solvers that overlap or capture work need

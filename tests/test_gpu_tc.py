@@ -90,7 +90,7 @@ def _bound_ok(C, ref, scale, tol=2.0 ** -14):
     return bool(((C - ref).abs() <= tol * scale + 1e-300).all())
 
 
-@pytest.mark.parametrize("case", ["2d", "2d_transposed", "a_shared", "b_shared", "beta", "fallback_small"])
+@pytest.mark.parametrize("case", ["2d", "2d_transposed", "a_shared", "b_shared", "beta", "splitk", "fallback_small"])
 def test_gemm_tc_contract(gpulib, case):
     """gemm_tc follows gemm_df's contract (strided, batched with a shared
     operand, alpha/beta) within the split-BF16x3 error."""
@@ -117,8 +117,12 @@ def test_gemm_tc_contract(gpulib, case):
         A, B = r(6000, 40), r(40, 200)
         C = r(6000, 200)
         alpha, beta = -1.0, 1.0
-    else:                      # too few output tiles: the FP32-pair GEMM
+    elif case == "splitk":     # one output tile, long K: split K, ordered reduction
         A, B = r(30, 20000), r(20000, 150)
+        C = r(30, 150)
+        alpha, beta = 0.5, 2.0
+    else:                      # few tiles, short K: the FP32-pair GEMM
+        A, B = r(30, 300), r(300, 150)
         C = torch.empty(30, 150, dtype=torch.float64, device="cuda")
     C0 = C.clone()
     ref = alpha * torch.matmul(A, B) + beta * C0
@@ -127,3 +131,17 @@ def test_gemm_tc_contract(gpulib, case):
     assert _bound_ok(C, ref, scale)
     if case == "fallback_small":
         assert float(((C - ref).abs() / scale).max()) < 1e-12  # FP32 pairs, not BF16
+
+
+def test_gemm_tc_splitk_deterministic(gpulib):
+    from fricc_gb300.cholesky import gemm_tc
+    g = torch.Generator().manual_seed(12)
+    A = torch.randn(200, 30000, generator=g, dtype=torch.float64).cuda()
+    B = torch.randn(30000, 200, generator=g, dtype=torch.float64).cuda()
+    C1 = torch.empty(200, 200, dtype=torch.float64, device="cuda")
+    C2 = torch.empty_like(C1)
+    gemm_tc(A, B, C1)
+    gemm_tc(A, B, C2)
+    assert torch.equal(C1, C2)
+    ref, scale = A @ B, A.abs() @ B.abs()
+    assert _bound_ok(C1, ref, scale)
