@@ -61,6 +61,7 @@ class FRILCCSDGPU(FRICCSDGPU):
         self.level_shift = float(level_shift)
         self.rn_draw = rn_draw
         self.precision = precision
+        self._df = precision == "df64"
         self.lib = L.load()
         eris.prepare_linear()
         if precision == "df64":
