@@ -48,6 +48,8 @@ SIGNATURES = [
     ("fricc_split_f2", ctypes.c_int, [_dp, _i64, _i64, _dp, _vp]),
     ("fricc_spmm_f1", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                      ctypes.c_double, _dp, _i64, _i64, _dp, _vp]),
+    ("fricc_spmm_f32", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_double, _dp, _i64, _i64, _dp, _vp]),
     ("fricc_gemm_bf16_tn", ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _dp, _i64, _vp]),
     ("fricc_gemm_bf16_tn_f64", ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _dp, _i64, _vp]),
     ("fricc_split_bf16x3", ctypes.c_int, [_dp, _i64, _i64, _i64, _i64, _vp, _vp, _vp]),

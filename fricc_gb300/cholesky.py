@@ -107,8 +107,15 @@ def split_a(A: torch.Tensor) -> torch.Tensor:
     return _split_view(A, A.shape[0], A.shape[1], A.shape[0], 0, A.stride(0), A.stride(1), True, False)
 
 
+def split_b(B: torch.Tensor) -> torch.Tensor:
+    """B' ([hi|lo|hi], rows n, K-major) of a 2-D FP64 operand [K, N], for
+    reuse through ``gemm_tc(..., b_split=)``."""
+    return _split_view(B, B.shape[1], B.shape[0], B.shape[1], 0, B.stride(1), B.stride(0), False, True)
+
+
 def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.0, beta: float = 0.0,
-            status: torch.Tensor | None = None, a_split: torch.Tensor | None = None):
+            status: torch.Tensor | None = None, a_split: torch.Tensor | None = None,
+            b_split: torch.Tensor | None = None):
     """C = alpha A @ B + beta C with split-BF16x3 operands on the tcgen05
     tensor cores (FP32 accumulation, FP64 epilogue): the contract of
     ``rccsd_dense.gemm_df`` -- FP64 tensors with any strides, 2-D or batched
@@ -116,7 +123,8 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
     Few output tiles with a long K split K; few tiles with a short K, or both
     operands batched, go to ``gemm_df``.  ``status`` (a device int32) makes the launch
     stream-ordered; a gave-up pipeline wait is recorded there.
-    ``a_split``: A' of a 2-D A made once by ``split_a``."""
+    ``a_split`` / ``b_split``: the split of a constant 2-D operand made once
+    by ``split_a`` / ``split_b``."""
     from . import rccsd_dense as D
     sA, bA = D._strides3(A)
     sB, bB = D._strides3(B)
@@ -143,7 +151,11 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
     else:
         Ap = _split_view(A, M, K, M, 0, sA[0], sA[1], True, False)
         mi, sro, sri = M, 0, sC[0]
-    if Nf > N:
+    if b_split is not None:
+        assert Nf == N and b_split.shape == (N, _kp(K))
+        Bp = b_split
+        ni, sco, sci = N, 0, sC[1]
+    elif Nf > N:
         Bp = _split_view(B, Nf, K, N, sB[2], sB[1], sB[0], False, True)
         ni, sco, sci = N, sC[2], sC[1]
     else:

@@ -363,6 +363,64 @@ __global__ void __launch_bounds__(DF_NT) k_spmm_f1(const int* __restrict__ bptr,
   }
 }
 
+// FP32 throughout (the split-precision form, whose integrals carry ~2^-16
+// relative error anyway): W rows of ldw floats read as pairs, T values as
+// floats, one packed FMA per output pair per term, the FP32 sum added to the
+// FP64 output once at the end.  PPT q-pairs per thread.
+template <int PPT, bool FULL>
+__device__ __forceinline__ void f32_tile(const int* __restrict__ srow, const f32x2* __restrict__ sv, int cnt,
+                                         const f32x2* __restrict__ wq, int64_t ldw2, int64_t trem, f32x2* acc) {
+#pragma unroll 4
+  for (int j = 0; j < cnt; ++j) {
+    const f32x2* w = wq + (int64_t)srow[j] * ldw2;
+    const f32x2 v = sv[j];  // (t, t)
+#pragma unroll
+    for (int k = 0; k < PPT; ++k)
+      if (FULL || k * DF_NT < trem) acc[k] = fma2(w[k * DF_NT], v, acc[k]);
+  }
+}
+
+template <int PPT>
+__global__ void __launch_bounds__(DF_NT) k_spmm_f32(const int* __restrict__ bptr, const int* __restrict__ erow,
+                                                    const float2* __restrict__ eval, const float2* __restrict__ W2,
+                                                    int64_t ldw2, double* __restrict__ Op, int64_t QS) {
+  __shared__ int srow[DF_NT];
+  __shared__ f32x2 sv[DF_NT];
+  const int64_t P = blockIdx.x;
+  const int e0 = bptr[P], e1 = bptr[P + 1];
+  if (e0 == e1) return;
+  const int64_t QS2 = (QS + 1) >> 1;
+  const int64_t qt = blockIdx.y;
+  const int64_t t0 = qt * (DF_NT * PPT) + threadIdx.x;
+  const int64_t trem = QS2 - t0;
+  const bool full = (qt + 1) * (DF_NT * PPT) <= QS2;
+  const f32x2* wq = reinterpret_cast<const f32x2*>(W2) + t0;
+  f32x2 acc[PPT];
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) acc[k] = 0ull;
+  for (int eb = e0; eb < e1; eb += DF_NT) {
+    const int cnt = e1 - eb < DF_NT ? e1 - eb : DF_NT;
+    __syncthreads();
+    if ((int)threadIdx.x < cnt) {
+      const float2 v = eval[eb + threadIdx.x];
+      const float t = v.x + v.y;
+      srow[threadIdx.x] = erow[eb + threadIdx.x];
+      sv[threadIdx.x] = pk2(t, t);
+    }
+    __syncthreads();
+    if (full) f32_tile<PPT, true>(srow, sv, cnt, wq, ldw2, trem, acc);
+    else f32_tile<PPT, false>(srow, sv, cnt, wq, ldw2, trem, acc);
+  }
+  double* orow = Op + P * QS;
+#pragma unroll
+  for (int k = 0; k < PPT; ++k) {
+    const int64_t q = 2 * (t0 + k * DF_NT);
+    const float2 a = upk2(acc[k]);
+    if (q < QS) orow[q] += f2d_bits(a.x);
+    if (q + 1 < QS) orow[q + 1] += f2d_bits(a.y);
+  }
+}
+
 __global__ void k_entries_df(const int* __restrict__ slots, const double* __restrict__ vals,
                              const unsigned* __restrict__ order, int64_t m, int ka, int kb, int64_t dkb, double coef,
                              int* __restrict__ erow, float2* __restrict__ eval) {
@@ -672,7 +730,7 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
 }
 
 int fricc_spmm_f1_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float* W, int64_t QS,
-                         int64_t ldw, double* Op, cudaStream_t st) {
+                         int64_t ldw, double* Op, cudaStream_t st, bool fp32) {
   if (!T || !W || !Op || QS <= 0 || ldw < QS || (ldw & 1) || pa < 0 || pa > 3 || pb < 0 || pb > 3 || ka < 0 ||
       ka > 3 || kb < 0 || kb > 3 || pa == pb || ka == kb) {
     fricc_set_error("spmm_f1: bad arguments (W rows of ldw >= QS floats, ldw even)");
@@ -703,7 +761,12 @@ int fricc_spmm_f1_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
     const bool prof = fricc_prof_on();
     if (prof) fricc_prof_record(st, true, 0.0);
     const dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq);
-    k_spmm_f1<ppt><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, reinterpret_cast<const float2*>(W), ldw / 2, Op, QS);
+    if (fp32)
+      k_spmm_f32<ppt><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, reinterpret_cast<const float2*>(W), ldw / 2, Op,
+                                             QS);
+    else
+      k_spmm_f1<ppt><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, reinterpret_cast<const float2*>(W), ldw / 2, Op,
+                                            QS);
     if (prof) fricc_prof_record(st, false, 2.0 * (double)T->m * (double)QS);
     fricc_note_launch(2);
     cudaError_t e = cudaGetLastError();

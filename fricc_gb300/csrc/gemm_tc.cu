@@ -437,21 +437,28 @@ __device__ __forceinline__ void split_put(double xv, int64_t k, __nv_bfloat16* a
   }
 }
 
-// columns contiguous (or any layout): one row per block pass, threads over j
+// columns contiguous (or any layout): work items of (row, 1024 columns), a
+// block's threads over the columns, so a few very long rows spread as well
 __global__ void k_split_rows(const double* __restrict__ x, int64_t rows, int64_t k, int64_t ri, int64_t sro,
                              int64_t sri, int64_t sk, int64_t kp, __nv_bfloat16* __restrict__ Ap,
                              __nv_bfloat16* __restrict__ Bp) {
-  for (int64_t r = blockIdx.x; r < rows; r += gridDim.x) {
+  constexpr int64_t CH = 1024;
+  const int64_t nch = fricc_cdiv(kp - 2 * k, CH);  // chunks over j < k, then the padding j >= 3k
+  for (int64_t w = blockIdx.x; w < rows * nch; w += gridDim.x) {
+    const int64_t r = w / nch, c = w - r * nch;
     const int64_t ro = r / ri;
     const double* xr = x + ro * sro + (r - ro * ri) * sri;
     __nv_bfloat16* ar = Ap ? Ap + r * kp : nullptr;
     __nv_bfloat16* br = Bp ? Bp + r * kp : nullptr;
-    for (int64_t j = threadIdx.x; j < k; j += blockDim.x) split_put(xr[j * sk], k, ar ? ar + j : nullptr,
-                                                                    br ? br + j : nullptr);
-    for (int64_t j = 3 * k + threadIdx.x; j < kp; j += blockDim.x) {
-      if (ar) ar[j] = __float2bfloat16(0.0f);
-      if (br) br[j] = __float2bfloat16(0.0f);
-    }
+    const int64_t j1 = (c + 1) * CH < k ? (c + 1) * CH : k;
+    for (int64_t j = c * CH + threadIdx.x; j < j1; j += blockDim.x)
+      split_put(xr[j * sk], k, ar ? ar + j : nullptr, br ? br + j : nullptr);
+    // padding: chunk c also zeroes columns 3k + [c*CH - k, ...) that fall in [3k, kp)
+    for (int64_t j = 3 * k + c * CH - k + threadIdx.x; j < kp && j < 3 * k + (c + 1) * CH - k; j += blockDim.x)
+      if (j >= 3 * k) {
+        if (ar) ar[j] = __float2bfloat16(0.0f);
+        if (br) br[j] = __float2bfloat16(0.0f);
+      }
   }
 }
 
@@ -644,7 +651,8 @@ int fricc_split_bf16x3_strided(const double* x, int64_t rows, int64_t k, int64_t
     if (g > 152 * 16) g = 152 * 16;
     tc::k_split_tr<<<(unsigned)g, 256, 0, (cudaStream_t)stream>>>(x, rows, k, ri, sro, sk, kp, a, b);
   } else {
-    const int64_t g = rows < 152 * 16 ? rows : 152 * 16;
+    const int64_t items = rows * fricc_cdiv(kp - 2 * k, 1024);
+    const int64_t g = items < 152 * 16 ? items : 152 * 16;
     tc::k_split_rows<<<(unsigned)g, 128, 0, (cudaStream_t)stream>>>(x, rows, k, ri, sro, sri, sk, kp, a, b);
   }
   fricc_note_launch();

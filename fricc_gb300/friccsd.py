@@ -136,7 +136,7 @@ class _Handle:
 
 class FRICCSDGPU:
     def __init__(self, eris: D.DeviceERIs, fri_settings=None, level_shift=0.0, rn_draw=libc_uniform,
-                 wvvvv_t1t1="reference", precision="fp64", graph=False, rebuild_vvvv=True):
+                 wvvvv_t1t1="reference", precision="fp64", graph=False, rebuild_vvvv=True, split_sparse="fp32"):
         s = dict(DEFAULT_SETTINGS)
         s.update(fri_settings or {})
         for c in s["compressed_contractions"]:
@@ -164,6 +164,11 @@ class FRICCSDGPU:
         # split precision: rebuild (vv|vv) from the factor every iteration (it
         # is never resident), or once and keep the FP32 block
         self.rebuild_vvvv = bool(rebuild_vvvv)
+        # split precision, sparse terms: plain FP32 sums ("fp32"), or T values
+        # and sums in float pairs ("pairs"); W is FP32 either way
+        if split_sparse not in ("fp32", "pairs"):
+            raise ValueError("split_sparse must be 'fp32' or 'pairs'")
+        self._spmm32 = L.load().fricc_spmm_f32 if split_sparse == "fp32" else L.load().fricc_spmm_f1
         self._vvvv_buf = None
         self._tc_status = torch.zeros(1, dtype=torch.int32, device=eris.device)
         self.lib = L.load()
@@ -173,7 +178,10 @@ class FRICCSDGPU:
             o_, v_ = eris.nocc, eris.mo_energy.numel() - eris.nocc
             eris.prepare_f32({"ovvv_XY": 2 * o_ * v_, "ovov": o_ * v_, "ovov_0313_0113": o_ * v_,
                               "ovov_0312": o_ * v_, "ovov_cdkl": o_ * o_})
-            eris.prepare_tc_a(("ovvv_iabc", "ovvv", "ovvv_kacd"))
+            ovv = o_ * v_ * v_
+            eris.prepare_tc({"ovvv_iabc": ("A", ovv, v_), "ovvv": ("A", ovv, v_), "ovvv_kacd": ("A", ovv, v_),
+                             "g_klcd": ("A", o_, ovv), "g_kldc": ("B", o_ * o_ * v_, v_),
+                             "G_t1": ("B", ovv, v_)})
         self._sp = _Handle()
         self._sp_w = _Handle()
         # streams of this solver alone (torch's pool hands the same few streams
@@ -210,8 +218,7 @@ class FRICCSDGPU:
             # (half the bytes of the float-pair layout), T values and sums
             # still float pairs
             W32 = self.eris.f32(const, QS) if const else D.to_f32_rows(Wp, QS)
-            L.check(self.lib.fricc_spmm_f1(T, pa, pb, ka, kb, float(coef), _ptr(W32), int(QS), W32.shape[1],
-                                           _ptr(Op), stream))
+            L.check(self._spmm32(T, pa, pb, ka, kb, float(coef), _ptr(W32), int(QS), W32.shape[1], _ptr(Op), stream))
         elif self._df:
             W2 = self.eris.split(const) if const else D.split_f2(Wp, QS)
             assert W2.numel() == (Wp.numel() // QS) * ((QS + 1) // 2) * 4, "float-pair W' split with another QS"
@@ -330,16 +337,17 @@ class FRICCSDGPU:
             from .cholesky import gemm_tc
             tcs = self._tc_status
 
-            def mm(A_, B_, C_, alpha=1.0, beta=0.0, const=None):
+            def mm(A_, B_, C_, alpha=1.0, beta=0.0, const=None, const_b=None):
                 return gemm_tc(A_, B_, C_, alpha, beta, status=tcs,
-                               a_split=E.tc_a(const) if const else None)
+                               a_split=E.tc(const, "A") if const else None,
+                               b_split=E.tc(const_b, "B") if const_b else None)
 
             def ein2(spec, A_, B_):
                 return D.einsum_df(spec, A_, B_, gemm=mm)
         else:
             mm0 = D.gemm_df if self._df else D.gemm_torch
 
-            def mm(A_, B_, C_, alpha=1.0, beta=0.0, const=None):
+            def mm(A_, B_, C_, alpha=1.0, beta=0.0, const=None, const_b=None):
                 return mm0(A_, B_, C_, alpha, beta)
 
             ein2 = D.einsum_df if self._df else torch.einsum   # two-operand O^3V^2 contractions
@@ -347,9 +355,10 @@ class FRICCSDGPU:
         # cc_Foo / cc_Fvv share tt[p,q,r,s] = t2 + t1[p,r] t1[q,s]
         tt = t2 + ein("pr,qs->pqrs", t1, t1)
         Foo0 = E.fock[:o, :o].clone()                     # f_ki + sum_lcd g[k,c,l,d] tt[i,l,c,d]
-        mm(E.g_klcd.view(o, o * v * v), tt.view(o, o * v * v).T, Foo0, 1.0, 1.0)
+        mm(E.g_klcd.view(o, o * v * v), tt.view(o, o * v * v).T, Foo0, 1.0, 1.0, const="g_klcd")
         Fvv0 = E.fock[o:, o:].clone()                     # f_ac - sum_kld g[k,c,l,d] tt[k,l,a,d]
-        mm(tt.permute(2, 0, 1, 3).contiguous().view(v, o * o * v), E.g_kldc.view(o * o * v, v), Fvv0, -1.0, 1.0)
+        mm(tt.permute(2, 0, 1, 3).contiguous().view(v, o * o * v), E.g_kldc.view(o * o * v, v), Fvv0, -1.0, 1.0,
+           const_b="g_kldc")
         del tt
         Fov = D.cc_Fov(t1, t2, E)
         Foo = Foo0.clone()
@@ -366,7 +375,7 @@ class FRICCSDGPU:
         t1new += fov
         t1new += 2 * ein("kcai,kc->ia", E.ovvo, t1) - ein("kiac,kc->ia", E.oovv, t1)
         t1new = t1new.contiguous()
-        mm(t2.view(o, o * v * v), E.G_t1.view(o * v * v, v), t1new, 1.0, 1.0)  # O^2V^3, :165-166
+        mm(t2.view(o, o * v * v), E.G_t1.view(o * v * v, v), t1new, 1.0, 1.0, const_b="G_t1")  # O^2V^3, :165-166
         # X[c,a] = sum_kd t1[k,d] (2 (kd|ac) - (kc|ad)): the t1.t1 T1 term (:167-168) and Lvv's ovvv part
         X = (t1.reshape(1, ov) @ E.G_t1_kdca.view(ov, v * v)).view(v, v)
         t1new += t1 @ X
@@ -450,7 +459,7 @@ class FRICCSDGPU:
                         W = R.rebuild(self._vvvv_buf)
                     else:
                         W = R.W if R.W is not None else R.rebuild()
-                    L.check(self.lib.fricc_spmm_f1(T, 0, 1, 2, 3, 1.0, _ptr(W), v * v, R.ldw, _ptr(t2new), st))
+                    L.check(self._spmm32(T, 0, 1, 2, 3, 1.0, _ptr(W), v * v, R.ldw, _ptr(t2new), st))
                 else:
                     self._spmm(T, 0, 1, 2, 3, 1.0, E.vvvvT, v * v, t2new, st, const="vvvvT")  # (ac|bd) of 2323
                 XY = torch.zeros(o, o, 2, o, v, dtype=t2.dtype, device=t2.device)

@@ -119,20 +119,23 @@ class DeviceERIs:
                 self.f32(n, q)
             torch.cuda.current_stream().synchronize()
 
-    def prepare_tc_a(self, names):
-        """The split-BF16x3 A' of constant [o v v, v] blocks (the A operands
-        of the split-precision form's t1 GEMMs), made once and waited for."""
-        from .cholesky import split_a
-        if any(("tcA", n) not in self._splits for n in names):
-            for n in names:
-                x = getattr(self, n)
-                self._splits[("tcA", n)] = split_a(x.reshape(-1, x.shape[-1]))
+    def prepare_tc(self, operands: dict):
+        """The split-BF16x3 operands of constant blocks for the split-precision
+        form's tensor-core GEMMs, made once and waited for:
+        {name: ("A" or "B", rows, cols)} with the block viewed as [rows, cols]."""
+        from .cholesky import split_a, split_b
+        todo = {n: spec for n, spec in operands.items() if ("tc", n) not in self._splits}
+        if todo:
+            for n, (role, r, c) in todo.items():
+                x = getattr(self, n).reshape(r, c)
+                self._splits[("tc", n)] = (role, split_a(x) if role == "A" else split_b(x))
             torch.cuda.current_stream().synchronize()
 
-    def tc_a(self, name):
-        if ("tcA", name) not in self._splits:
-            raise RuntimeError(f"split A' of {name} missing: call prepare_tc_a() first")
-        return self._splits[("tcA", name)]
+    def tc(self, name, role):
+        got = self._splits.get(("tc", name))
+        if got is None or got[0] != role:
+            raise RuntimeError(f"split operand {role} of {name} missing: call prepare_tc() first")
+        return got[1]
 
     def f32(self, name, qs):
         """FP32 rows (qs columns, padded to even) of a constant block, built

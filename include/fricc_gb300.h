@@ -174,6 +174,13 @@ int fricc_split_f2(const double* x, int64_t rows, int64_t qs, float* out4, void*
 int fricc_spmm_f1(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* W, int64_t QS,
                   int64_t ldw, double* Op, void* stream);
 
+/* fricc_spmm_f1 in plain FP32: T values rounded to FP32, one FP32 sum per
+ * output added to the FP64 output at the end (~2^-24 per product, the sum's
+ * rounding on top).  For the split-precision form only, whose integrals
+ * carry ~2^-16 relative error from the BF16x3 rebuild. */
+int fricc_spmm_f32(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* W, int64_t QS,
+                   int64_t ldw, double* Op, void* stream);
+
 /* Strided batched GEMM, FP64 in and out, products and sums in FP32 pairs
  * (no reference counterpart; it runs the dense O^2V^3 contractions of the
  * iteration):  C[b] = alpha * A[b] @ B[b] + beta * C[b], b < batch.

@@ -65,6 +65,48 @@ def test_spmm_f1_matches_fp64_kernel(gpulib, systems):
     assert bool(((a - b).abs() <= bound).all())
 
 
+def test_spmm_f32_within_fp32_error(gpulib, systems):
+    """The plain-FP32 sparse kernel: each output within 2^-16 of sum |W||T|
+    of the FP64 kernel's (FP32 products and an FP32 sum over a bucket)."""
+    from fricc_gb300 import _lib as L
+    from fricc_gb300 import py_rccsd
+    s, E, Es = systems
+    o, v = s.nocc, s.nvir
+    R = Es.vvvv_rebuild
+    W = R.rebuild()
+    t2 = torch.from_numpy(np.ascontiguousarray(s.mp2_amplitudes()[1])).cuda()
+    T = py_rccsd.SparseTensor4d(t2, t2.shape, 20000, "fri", "systematic", rn=0.5)
+    Ta = py_rccsd.SparseTensor4d(t2.abs(), t2.shape, 20000, "fri", "systematic", rn=0.5)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    W64 = W[:, : v * v].double().contiguous()
+    Wa = W64.abs()
+    a = torch.randn(o * o, v * v, dtype=torch.float64, device="cuda") * 1e-3
+    b, c = a.clone(), torch.zeros_like(a)
+    L.check(gpulib.fricc_spmm(T.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(W64.data_ptr()), v * v,
+                              ctypes.c_void_p(a.data_ptr()), st))
+    L.check(gpulib.fricc_spmm_f32(T.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(W.data_ptr()), v * v, R.ldw,
+                                  ctypes.c_void_p(b.data_ptr()), st))
+    L.check(gpulib.fricc_spmm(Ta.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(Wa.data_ptr()), v * v,
+                              ctypes.c_void_p(c.data_ptr()), st))
+    torch.cuda.synchronize()
+    assert bool(((a - b).abs() <= 2.0 ** -16 * c + 1e-18).all())
+
+
+@pytest.mark.parametrize("sums", ["fp32", "pairs"])
+def test_split_iteration_delta_e_sums(gpulib, systems, sums):
+    from fricc_gb300.friccsd import FRICCSDGPU
+    s, E, Es = systems
+    t1, t2 = [torch.from_numpy(x).cuda() for x in s.mp2_amplitudes()]
+    fp = FRICCSDGPU(E, {"m_keep": 20000}, precision="fp64")
+    sp = FRICCSDGPU(Es, {"m_keep": 20000}, precision="split", split_sparse=sums)
+    for it in range(3):
+        rn = [0.3 + 0.1 * it, 0.4]
+        a1, a2 = fp.update_amps(t1, t2, rn=rn)
+        sp.update_amps(t1, t2, rn=rn)
+        assert abs(fp.read_energy()[0] - sp.read_energy()[0]) < 1e-6
+        t1, t2 = a1, a2
+
+
 def test_split_iteration_delta_e(gpulib, systems):
     from fricc_gb300.friccsd import FRICCSDGPU
     s, E, Es = systems
