@@ -30,7 +30,7 @@ import torch
 from .friccsd import FRICCSDGPU
 from .rccsd_dense import DeviceERIs
 from .rng import GlibcRand
-from .synthetic import SyntheticSystem
+from .synthetic import DeviceSystem, SyntheticSystem
 
 
 def mp2_device(E: DeviceERIs):
@@ -147,17 +147,24 @@ def request_stream(n: int, rate: float, seed: int = 0, nocc=(5, 30), ratio=(4.0,
     return out
 
 
-def footprint_bytes(o: int, v: int) -> int:
+def footprint_bytes(o: int, v: int, precision: str = "df64") -> int:
     """HBM a resident solve needs: integral blocks and the layouts derived from
     them (vvvv and its float-pair form, ovvv in nine layouts or forms),
-    amplitudes and work arrays (~16 o^2v^2)."""
-    return 8 * (2 * v**4 + 9 * o * v**3 + 16 * o * o * v * v + 4 * o**4 + 8 * o**3 * v)
+    amplitudes and work arrays (~16 o^2v^2).  Split precision keeps (vv|vv)
+    only as the FP32 block it rebuilds (v^4 / 2 doubles) and adds the
+    BF16x3 operand splits (~4.5 o v^3 doubles)."""
+    vvvv = 0.5 * v**4 if precision == "split" else 2 * v**4
+    ovvv = 13.5 * o * v**3 if precision == "split" else 9 * o * v**3
+    return int(8 * (vvvv + ovvv + 16 * o * o * v * v + 4 * o**4 + 8 * o**3 * v))
 
 
 class SolveServer:
     def __init__(self, n_workers: int = 8, hbm_budget: float = 200e9, precision: str = "df64", max_cycle: int = 30,
-                 tol: float = 1e-7, device="cuda", graph: bool = False):
+                 tol: float = 1e-7, device="cuda", graph: bool = False, device_inputs: bool = True):
         self.graph = graph
+        # draw each request's synthetic system on the GPU (DeviceSystem) or
+        # on the host (SyntheticSystem, numpy)
+        self.device_inputs = device_inputs
         self.k = n_workers
         self.budget = hbm_budget
         self.precision = precision
@@ -171,8 +178,15 @@ class SolveServer:
 
     def _solve(self, req: Request, t0: float, stream):
         with torch.cuda.stream(stream):
-            system = SyntheticSystem(req.nocc, req.nvir, req.naux, req.sigma, req.seed)
-            E = DeviceERIs.from_system(system, device=self.device)
+            if self.device_inputs:
+                system = DeviceSystem(req.nocc, req.nvir, req.naux, req.sigma, req.seed, device=self.device)
+            else:
+                system = SyntheticSystem(req.nocc, req.nvir, req.naux, req.sigma, req.seed)
+            if self.precision == "split":  # integrals rebuilt from the BF16 hi+lo factor on the tensor cores
+                from .cholesky import split_eris
+                E = split_eris(system, device=self.device)
+            else:
+                E = DeviceERIs.from_system(system, device=self.device)
             solver = FRICCSDGPU(E, {"m_keep": req.m}, rn_draw=GlibcRand(req.seed), precision=self.precision,
                                 graph=self.graph)
             t1, t2 = mp2_device(E)
@@ -205,7 +219,7 @@ class SolveServer:
                 delay = r.arrival * time_scale - (time.perf_counter() - t0)
                 if delay > 0:
                     time.sleep(delay)
-                need = footprint_bytes(r.nocc, r.nvir)
+                need = footprint_bytes(r.nocc, r.nvir, self.precision)
                 with self._cv:
                     while self._in_use + need > self.budget and self._in_use > 0:
                         self._cv.wait()
@@ -228,7 +242,7 @@ class SolveServer:
                     errors.append(e)
                 r.finished = time.perf_counter() - t0
                 with self._cv:
-                    self._in_use -= footprint_bytes(r.nocc, r.nvir)
+                    self._in_use -= footprint_bytes(r.nocc, r.nvir, self.precision)
                     self._cv.notify_all()
 
         th = [threading.Thread(target=dispatcher)] + [threading.Thread(target=worker, args=(w,)) for w in range(self.k)]

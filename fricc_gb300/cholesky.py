@@ -222,9 +222,9 @@ def split_eris(system, device="cuda"):
     dense algebra), the (vv|vv) block never stored in FP64 but rebuilt by
     ``VvvvRebuild`` for the O^2V^4 contraction; the small blocks (oo|oo),
     (ov|oo), (ov|ov), (ov|vo) and sum_cd (ac|bd) in FP64 from the factor."""
-    from .rccsd_dense import DeviceERIs
+    from .rccsd_dense import DeviceERIs, _dev_tensor
     dev = torch.device(device)
-    Lf = torch.from_numpy(system.L).to(dev, torch.float64)
+    Lf = _dev_tensor(system.L, dev)
     o, nmo = system.nocc, system.nmo
     naux = Lf.shape[0]
     sl = {"o": slice(0, o), "v": slice(o, nmo)}
@@ -252,4 +252,4 @@ def split_eris(system, device="cuda"):
     s = Lf[:, o:, o:].sum(dim=2)                      # [P, a] = sum_c L[P,a,c]
     blocks["S0"] = s.t() @ s                          # sum_cd (ac|bd)
     blocks["vvvv_rebuild"] = VvvvRebuild(Lf, o)
-    return DeviceERIs(torch.from_numpy(system.fock), torch.from_numpy(system.mo_energy), o, blocks, device)
+    return DeviceERIs(_dev_tensor(system.fock, dev), _dev_tensor(system.mo_energy, dev), o, blocks, device)

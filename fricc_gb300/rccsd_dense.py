@@ -163,7 +163,7 @@ class DeviceERIs:
     def from_system(cls, system, device="cuda"):
         """Build every block on the device from the Cholesky factor of a SyntheticSystem."""
         dev = torch.device(device)
-        L = torch.from_numpy(system.L).to(dev, torch.float64)
+        L = _dev_tensor(system.L, dev)
         o = system.nocc
         naux = L.shape[0]
         sl = {"o": slice(0, o), "v": slice(o, system.nmo)}
@@ -185,13 +185,19 @@ class DeviceERIs:
         X = (Lca.T @ Ldb).reshape(v, v, v, v)            # [c,a,d,b]
         blocks["vvvvT"] = X.permute(0, 2, 1, 3).contiguous()
         del X
-        return cls(torch.from_numpy(system.fock), torch.from_numpy(system.mo_energy), o, blocks, device)
+        return cls(_dev_tensor(system.fock, dev), _dev_tensor(system.mo_energy, dev), o, blocks, device)
 
     def to_numpy_blocks(self):
         """Host copies in the stand-in layout (for checking against the oracle)."""
         out = {k: getattr(self, k).cpu().numpy() for k in ("oooo", "ovoo", "ovov", "oovv", "ovvo", "ovvv")}
         out["vvvv"] = self.vvvvT.permute(2, 0, 3, 1).contiguous().cpu().numpy()  # (ab|cd)
         return out
+
+
+def _dev_tensor(a, dev):
+    """FP64 copy of a numpy array, or the tensor itself moved to ``dev``."""
+    t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
+    return t.to(dev, torch.float64)
 
 
 def _strides3(t: torch.Tensor):

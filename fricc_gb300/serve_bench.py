@@ -55,17 +55,20 @@ def run_replicas(args):
 
 def run_serve(args):
     reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
-    server = SolveServer(n_workers=args.streams, precision=args.precision, max_cycle=args.max_cycle, graph=args.graph)
+    server = SolveServer(n_workers=args.streams, precision=args.precision, max_cycle=args.max_cycle, graph=args.graph,
+                         device_inputs=not args.host_inputs)
     out = server.run(reqs, time_scale=1.0)
     served = latency_summary(out)
     line = {"mode": "serve", "requests": args.requests, "rate_per_s": args.rate, "workers": args.streams,
+            "inputs": "host (numpy)" if args.host_inputs else "device (torch Philox)",
             "precision": args.precision, "max_cycle": args.max_cycle, "graph": args.graph, "served": served}
     if args.plain:
         # the same requests, one at a time, FP64, arriving all at once
         plain_reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
         for r in plain_reqs:
             r.arrival = 0.0
-        plain = SolveServer(n_workers=1, precision="fp64", max_cycle=args.max_cycle).run(plain_reqs)
+        plain = SolveServer(n_workers=1, precision="fp64", max_cycle=args.max_cycle,
+                            device_inputs=not args.host_inputs).run(plain_reqs)
         line["plain"] = latency_summary(plain)
         diffs = [abs(a.e_corr - b.e_corr) for a, b in zip(sorted(out, key=lambda r: r.rid),
                                                           sorted(plain_reqs, key=lambda r: r.rid))]
@@ -81,7 +84,7 @@ def main():
     p.add_argument("--streams", type=int, default=8)
     p.add_argument("--steps", type=int, default=3)
     p.add_argument("--warmup", type=int, default=1)
-    p.add_argument("--precision", default="df64", choices=["fp64", "df64"])
+    p.add_argument("--precision", default="df64", choices=["fp64", "df64", "split"])
     p.add_argument("--requests", type=int, default=40)
     p.add_argument("--rate", type=float, default=50.0)
     p.add_argument("--seed", type=int, default=0)
@@ -89,6 +92,8 @@ def main():
     p.add_argument("--nocc-max", type=int, default=30)
     p.add_argument("--max-cycle", type=int, default=30)
     p.add_argument("--plain", action="store_true")
+    p.add_argument("--host-inputs", action="store_true",
+                   help="draw each request's synthetic system with numpy on the host (default: on the GPU)")
     p.add_argument("--graph", action="store_true", help="replay each solver's iteration from a CUDA graph")
     args = p.parse_args()
     line = run_replicas(args) if args.mode == "replicas" else run_serve(args)

@@ -88,6 +88,37 @@ class SyntheticSystem:
         return t1, np.ascontiguousarray(t2)
 
 
+class DeviceSystem:
+    """The same recipe drawn on the GPU (torch's Philox generator seeded with
+    ``seed``): the same distributions and sizes as ``SyntheticSystem``, but
+    not the same numbers.  A request server uses it for every arm it
+    compares, so that drawing a few hundred million normals on the host does
+    not stand in front of every solve."""
+
+    def __init__(self, nocc, nvir, naux, sigma, seed=0, device="cuda"):
+        import torch
+        self.nocc, self.nvir, self.naux, self.sigma, self.seed = int(nocc), int(nvir), int(naux), sigma, seed
+        dev = torch.device(device)
+        g = torch.Generator(device=dev)
+        g.manual_seed(int(seed))
+        f64 = torch.float64
+        eo = torch.sort(torch.rand(self.nocc, generator=g, device=dev, dtype=f64) * 1.2 - 1.5).values
+        ev = torch.sort(torch.rand(self.nvir, generator=g, device=dev, dtype=f64) * 2.8 + 0.2).values
+        self.mo_energy = torch.cat([eo, ev])
+        nmo = self.nmo
+        A = torch.randn(self.naux, nmo, nmo, generator=g, device=dev, dtype=f64) * (sigma / self.naux ** 0.5)
+        self.L = torch.triu(A) + torch.triu(A, 1).transpose(1, 2)
+
+    @property
+    def nmo(self) -> int:
+        return self.nocc + self.nvir
+
+    @property
+    def fock(self):
+        import torch
+        return torch.diag(self.mo_energy)
+
+
 def make_system(name: str, seed: int = 0) -> SyntheticSystem:
     w = WORKLOADS[name]
     return SyntheticSystem(w["nocc"], w["nvir"], w["naux"], w["sigma"], seed)

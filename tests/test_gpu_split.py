@@ -163,3 +163,23 @@ def test_split_requires_split_eris(gpulib, systems):
         FRICCSDGPU(E, {"m_keep": 100}, precision="split")
     with pytest.raises(ValueError):
         FRICCSDGPU(Es, {"m_keep": 100}, precision="df64")
+
+
+def test_device_system_recipe(gpulib):
+    """DeviceSystem draws the synthetic recipe on the GPU: sorted orbital
+    energies in their ranges, L symmetric with the normalised spread,
+    reproducible per seed, and integral blocks the solvers accept."""
+    from fricc_gb300.cholesky import split_eris
+    from fricc_gb300.rccsd_dense import DeviceERIs
+    from fricc_gb300.synthetic import DeviceSystem
+    a = DeviceSystem(6, 30, 288, 0.05, seed=7)
+    b = DeviceSystem(6, 30, 288, 0.05, seed=7)
+    assert torch.equal(a.L, b.L) and torch.equal(a.mo_energy, b.mo_energy)
+    e = a.mo_energy
+    assert bool((e[:6] >= -1.5).all() and (e[:6] <= -0.3).all() and (e[6:] >= 0.2).all() and (e[6:] <= 3.0).all())
+    assert bool((e[:6].diff() >= 0).all() and (e[6:].diff() >= 0).all())
+    assert torch.equal(a.L, a.L.transpose(1, 2))
+    assert abs(float(a.L.std()) * 288 ** 0.5 / 0.05 - 1.0) < 0.05
+    E = DeviceERIs.from_system(a)
+    Es = split_eris(a)
+    torch.testing.assert_close(Es.ovov, E.ovov, rtol=1e-13, atol=1e-16)
