@@ -343,6 +343,10 @@ def run_gpu(args):
     if args.precision == "fp64":
         kname, bound, peak = "k_spmm (bucketed sparse-T2 x dense-W, FP64)", "fp64", FP64_PEAK_TFLOPS
         psrc = "measured FP64 FMA rate of this GB300 pool (DFMA probe); FP64 is not in MEASURED_PEAKS.json"
+    elif args.precision == "split":
+        kname, bound, peak = "k_spmm_f32 (bucketed sparse-T2 x dense-W, FP32)", "fp32-pipe", FP32_PEAK_TFLOPS
+        psrc = ("FP32 FMA rate of this GB300 pool (74.2 TF/s, FFMA probe): one packed FMA per two outputs, "
+                "2 flops per multiply-add")
     else:
         kname, bound, peak = "k_spmm_df (bucketed sparse-T2 x dense-W, FP32 pairs)", "fp32-pipe", FP32_PEAK_TFLOPS / 12
         psrc = ("FP32 FMA rate of this GB300 pool (74.2 TF/s = 37.1 T instructions/s, FFMA probe) / 12 FP32 "
@@ -350,7 +354,7 @@ def run_gpu(args):
     roof = {"kernel": kname, "bound": bound,
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None,
-            "traffic": SPMM_TRAFFIC.get(args.workload) if args.precision != "fp64" else None,
+            "traffic": SPMM_TRAFFIC.get(args.workload) if args.precision == "df64" else None,
             "launches": int(p_n.value), "kernel_ms": p_ms.value,
             "kernel_share_of_step": p_ms.value / ms if ms > 0 else None,
             "peak_source": psrc}

@@ -50,6 +50,9 @@ SIGNATURES = [
                                      ctypes.c_double, _dp, _i64, _i64, _dp, _vp]),
     ("fricc_spmm_f32", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                       ctypes.c_double, _dp, _i64, _i64, _dp, _vp]),
+    ("fricc_densify_bf16x3", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                            ctypes.c_double, _vp, _i64, _vp]),
+    ("fricc_vvvv_rebuild_split_b", ctypes.c_int, [_vp, _vp, _i64, _i64, _vp, _i64, _vp, _vp]),
     ("fricc_gemm_bf16_tn", ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _dp, _i64, _vp]),
     ("fricc_gemm_bf16_tn_f64", ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _dp, _i64, _vp]),
     ("fricc_split_bf16x3", ctypes.c_int, [_dp, _i64, _i64, _i64, _i64, _vp, _vp, _vp]),

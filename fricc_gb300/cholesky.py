@@ -168,6 +168,34 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
     return C
 
 
+def dense_spmm_ok(dims, pa, pb, ka, kb, QS: int) -> bool:
+    """Whether ``dense_spmm`` takes this term (enough tiles, or a K long
+    enough to split)."""
+    nP, R = dims[pa] * dims[pb], dims[ka] * dims[kb]
+    return _ksplit(-(-nP // 128) * -(-QS // 256), _kp(R)) > 0
+
+
+def dense_spmm(T, dims, pa, pb, ka, kb, coef, Bt: torch.Tensor, QS: int, Op: torch.Tensor,
+               status: torch.Tensor | None = None) -> bool:
+    """Op[P][q] += coef * sum_r T[P][r] W[r][q] as a dense tensor-core GEMM:
+    the compressed T scattered into a zero-filled split-BF16x3 A' (rows
+    P = (pa,pb), K = (ka,kb)), Bt = the split W^T ([hi|lo|hi], rows q).
+    Returns False (and does nothing) when the GEMM would have too few tiles
+    and too short a K for the tensor cores."""
+    nP, R = dims[pa] * dims[pb], dims[ka] * dims[kb]
+    kp = _kp(R)
+    assert Bt.shape == (QS, kp) and Op.is_contiguous() and Op.numel() == nP * QS
+    ks = _ksplit(-(-nP // 128) * -(-QS // 256), kp)
+    if ks == 0:
+        return False
+    Ap = torch.empty(nP, kp, dtype=torch.bfloat16, device=Op.device)
+    lib = L.load()
+    L.check(lib.fricc_densify_bf16x3(T, pa, pb, ka, kb, float(coef), _p(Ap), kp, _st()))
+    L.check(lib.fricc_gemm_bf16_tn_strided(_p(Ap), kp, _p(Bt), kp, nP, QS, kp, _p(Op), nP, QS, 0, QS, 0, 1,
+                                           1.0, 1.0, ks, _p(status) if status is not None else None, _st()))
+    return True
+
+
 def lvv_t(Lf: torch.Tensor, nocc: int) -> torch.Tensor:
     """L_vv^T [v*v, naux] (row c*v + a = L[:, a, c]) of a factor L [naux, nmo, nmo]."""
     naux = Lf.shape[0]
@@ -207,6 +235,20 @@ class VvvvRebuild:
             out = self.W
         L.check(L.load().fricc_vvvv_rebuild_bf16x3(_p(self.Ap), _p(self.Bp), v, self.kp, _p(out), self.ldw,
                                                    _p(self.status), _st()))
+        self.rebuilds += 1
+        return out
+
+    def rebuild_split_b(self, out: torch.Tensor | None = None) -> torch.Tensor:
+        """Rebuild straight into the B operand of the dense O^2V^4 GEMM
+        (rows q = (a,b), K = (c,d), [hi | lo | hi]) on the current stream."""
+        v = self.v
+        kpo = _kp(v * v)
+        if out is None:
+            out = torch.empty(v * v, kpo, dtype=torch.bfloat16, device=self.Ap.device)
+        if out.dtype != torch.bfloat16 or out.shape != (v * v, kpo) or not out.is_contiguous():
+            raise ValueError("out: a contiguous bfloat16 (v*v, kp) buffer")
+        L.check(L.load().fricc_vvvv_rebuild_split_b(_p(self.Ap), _p(self.Bp), v, self.kp, _p(out), kpo,
+                                                    _p(self.status), _st()))
         self.rebuilds += 1
         return out
 

@@ -30,6 +30,8 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
 int fricc_split_f2_device(const double* x, int64_t rows, int64_t qs, float4* out, cudaStream_t st);
 int fricc_spmm_f1_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, const float* W, int64_t QS,
                          int64_t ldw, double* Op, cudaStream_t st, bool fp32);
+int fricc_densify_bf16x3_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, void* Ap, int64_t kp,
+                                cudaStream_t st);
 int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
                          const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
                          cudaStream_t st);
@@ -470,6 +472,14 @@ int fricc_spmm_f1(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, 
                   int64_t ldw, double* Op, void* stream) {
   cudaStream_t st = as_stream(stream);
   int rc = fricc_spmm_f1_device(T, pa, pb, ka, kb, coef, W, QS, ldw, Op, st, false);
+  if (!rc && T) T->owner_stream = st;
+  return rc;
+}
+
+int fricc_densify_bf16x3(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, void* Ap, int64_t kp,
+                         void* stream) {
+  cudaStream_t st = as_stream(stream);
+  int rc = fricc_densify_bf16x3_device(T, pa, pb, ka, kb, coef, Ap, kp, st);
   if (!rc && T) T->owner_stream = st;
   return rc;
 }

@@ -18,6 +18,8 @@
 #include <cmath>
 #include <cstring>
 
+#include <cuda_bf16.h>
+
 #include "radix.cuh"
 #include "sparse.cuh"
 
@@ -276,6 +278,28 @@ __global__ void __launch_bounds__(DF_NT) k_spmm_df(const int* __restrict__ bptr,
     const float2 h = upk2(ah[k]), l = upk2(al[k]);
     if (q < QS) orow[q] = pair_to_f64(h.x, l.x);
     if (q + 1 < QS) orow[q + 1] = pair_to_f64(h.y, l.y);
+  }
+}
+
+// The compressed T viewed as a dense [nP][R] matrix (rows P = (pa,pb) pair,
+// columns r = (ka,kb) pair), coef * value split into BF16 hi + lo and
+// scattered into the K-concatenated tensor-core operand A' = [hi | hi | lo]
+// (rows of kp elements, zeroed beforehand): the split-precision form runs
+// every sparse term as a dense GEMM on the tensor cores.  (P, r) is unique
+// per nonzero, so the scatter has no collisions.
+__global__ void k_densify_bf16x3(const int* __restrict__ slots, const double* __restrict__ vals, int64_t m, int pa,
+                                 int pb, int64_t dpb, int ka, int kb, int64_t dkb, double coef, int64_t R, int64_t kp,
+                                 __nv_bfloat16* __restrict__ Ap) {
+  for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m; s += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t P = (int64_t)slots[4 * s + pa] * dpb + slots[4 * s + pb];
+    const int64_t r = (int64_t)slots[4 * s + ka] * dkb + slots[4 * s + kb];
+    const double x = coef * vals[s];
+    const __nv_bfloat16 hi = __double2bfloat16(x);
+    const __nv_bfloat16 lo = __double2bfloat16(x - (double)__bfloat162float(hi));
+    __nv_bfloat16* row = Ap + P * kp;
+    row[r] = hi;
+    row[R + r] = hi;
+    row[2 * R + r] = lo;
   }
 }
 
@@ -775,6 +799,29 @@ int fricc_spmm_f1_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
   fricc_free(erow, st);
   fricc_free(eval, st);
   return rc;
+}
+
+int fricc_densify_bf16x3_device(FriccSparse* T, int pa, int pb, int ka, int kb, double coef, void* Ap, int64_t kp,
+                                cudaStream_t st) {
+  if (!T || !Ap || pa < 0 || pa > 3 || pb < 0 || pb > 3 || ka < 0 || ka > 3 || kb < 0 || kb > 3 || pa == pb ||
+      ka == kb) {
+    fricc_set_error("densify_bf16x3: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t nP = T->dims[pa] * T->dims[pb], R = T->dims[ka] * T->dims[kb];
+  if (kp < 3 * R) {
+    fricc_set_error("densify_bf16x3: kp must be >= 3 * dims[ka] * dims[kb]");
+    return FRICC_ERR_ARG;
+  }
+  cudaError_t e = cudaMemsetAsync(Ap, 0, sizeof(__nv_bfloat16) * (size_t)(nP * kp), st);
+  if (e == cudaSuccess && T->m > 0) {
+    k_densify_bf16x3<<<grid_for(T->m, 256), 256, 0, st>>>(T->slots, T->vals, T->m, pa, pb, T->dims[pb], ka, kb,
+                                                          T->dims[kb], coef, R, kp,
+                                                          static_cast<__nv_bfloat16*>(Ap));
+    fricc_note_launch();
+    e = cudaGetLastError();
+  }
+  return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "densify_bf16x3", __FILE__, __LINE__);
 }
 
 int fricc_split_f2_device(const double* x, int64_t rows, int64_t qs, float4* out, cudaStream_t st) {

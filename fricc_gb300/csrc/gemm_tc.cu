@@ -276,6 +276,37 @@ __device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, in
 // Persistent: each CTA walks tiles blockIdx.x, +gridDim.x, ...  The TMEM
 // accumulator is double-buffered (2 x 256 columns), so the epilogue warps
 // drain tile i while the MMA warp accumulates tile i+1.
+// The (vv|vv) block straight into the B' operand of the dense O^2V^4 GEMM:
+// B'[q][k] for q = (a,b), k = (c,d) holds (ac|bd) as [hi | lo | hi] at
+// k, R + k, 2R + k (R = v^2, rows of kpo elements).  GEMM row r1 = b v + d
+// (L[:, b, d]) and column r2 = a v + c give (bd|ac) = (ac|bd); a warp's 32
+// lanes are 32 consecutive d, so each store is one contiguous run.
+struct EpiVvvvSplitB {
+  __nv_bfloat16* B;
+  int64_t v, kpo;
+  __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x, int) const {
+    const int64_t R = v * v;
+    if (r1 >= R) return;
+    const int64_t b = r1 / v, d = r1 - b * v;
+    int64_t a = r2 / v, c = r2 - a * v;
+#pragma unroll
+    for (int i = 0; i < 16; ++i) {
+      if (a < v) {
+        const __nv_bfloat16 hi = __float2bfloat16(x[i]);
+        const __nv_bfloat16 lo = __float2bfloat16(x[i] - __bfloat162float(hi));
+        __nv_bfloat16* row = B + (a * v + b) * kpo + c * v + d;
+        row[0] = hi;
+        row[R] = lo;
+        row[2 * R] = hi;
+      }
+      if (++c == v) {
+        c = 0;
+        ++a;
+      }
+    }
+  }
+};
+
 template <class Epi>
 __global__ void __launch_bounds__(NT, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb, int K, int tiles_m,
@@ -706,6 +737,23 @@ int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t
     return FRICC_ERR_ARG;
   }
   return tc::launch(Ap, kp, Bp, kp, v * v, v * v, kp, tc::EpiVvvv{W, v, ldw}, (cudaStream_t)stream, status);
+}
+
+int fricc_vvvv_rebuild_split_b(const void* Ap, const void* Bp, int64_t v, int64_t kp, void* Bout, int64_t kpo,
+                               unsigned* status, void* stream) {
+  if (!Bout || v <= 0 || kpo < 3 * v * v || (kpo % 8)) {
+    fricc_set_error("vvvv_rebuild_split_b: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  // the padding columns past 3 v^2 must be zero
+  if (kpo > 3 * v * v) {
+    cudaError_t e = cudaMemset2DAsync(static_cast<__nv_bfloat16*>(Bout) + 3 * v * v, sizeof(__nv_bfloat16) * kpo, 0,
+                                      sizeof(__nv_bfloat16) * (kpo - 3 * v * v), v * v, st);
+    if (e != cudaSuccess) return fricc_cuda_fail(e, "vvvv_rebuild_split_b padding", __FILE__, __LINE__);
+  }
+  return tc::launch(Ap, kp, Bp, kp, v * v, v * v, kp,
+                    tc::EpiVvvvSplitB{static_cast<__nv_bfloat16*>(Bout), v, kpo}, st, status);
 }
 
 }  // extern "C"

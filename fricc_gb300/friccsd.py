@@ -136,7 +136,7 @@ class _Handle:
 
 class FRICCSDGPU:
     def __init__(self, eris: D.DeviceERIs, fri_settings=None, level_shift=0.0, rn_draw=libc_uniform,
-                 wvvvv_t1t1="reference", precision="fp64", graph=False, rebuild_vvvv=True, split_sparse="fp32"):
+                 wvvvv_t1t1="reference", precision="fp64", graph=False, rebuild_vvvv=True, split_sparse="dense"):
         s = dict(DEFAULT_SETTINGS)
         s.update(fri_settings or {})
         for c in s["compressed_contractions"]:
@@ -164,11 +164,17 @@ class FRICCSDGPU:
         # split precision: rebuild (vv|vv) from the factor every iteration (it
         # is never resident), or once and keep the FP32 block
         self.rebuild_vvvv = bool(rebuild_vvvv)
-        # split precision, sparse terms: plain FP32 sums ("fp32"), or T values
-        # and sums in float pairs ("pairs"); W is FP32 either way
-        if split_sparse not in ("fp32", "pairs"):
-            raise ValueError("split_sparse must be 'fp32' or 'pairs'")
-        self._spmm32 = L.load().fricc_spmm_f32 if split_sparse == "fp32" else L.load().fricc_spmm_f1
+        # split precision, sparse terms: the compressed T zero-filled into a
+        # dense split-BF16x3 GEMM on the tensor cores ("dense"), or the sparse
+        # kernels against FP32 W with plain FP32 sums ("fp32", also the
+        # fallback for GEMMs too small for the tensor cores) or with T values
+        # and sums in float pairs ("pairs")
+        if split_sparse not in ("dense", "fp32", "pairs"):
+            raise ValueError("split_sparse must be 'dense', 'fp32' or 'pairs'")
+        self.split_sparse = split_sparse
+        self._spmm32 = L.load().fricc_spmm_f1 if split_sparse == "pairs" else L.load().fricc_spmm_f32
+        self._dims = None
+        self._vvvv_bt = None
         self._vvvv_buf = None
         self._tc_status = torch.zeros(1, dtype=torch.int32, device=eris.device)
         self.lib = L.load()
@@ -214,9 +220,16 @@ class FRICCSDGPU:
         form is cached on the DeviceERIs."""
         assert Wp.is_contiguous() and Op.is_contiguous()
         if self.precision == "split":
+            if self.split_sparse == "dense":
+                # the compressed T zero-filled into a split-BF16x3 operand and
+                # contracted on the tensor cores
+                from .cholesky import dense_spmm, dense_spmm_ok, split_b
+                if dense_spmm_ok(self._dims, pa, pb, ka, kb, QS):
+                    Bt = self.eris.tc_w(const, QS) if const else split_b(Wp.reshape(-1, QS))
+                    dense_spmm(T, self._dims, pa, pb, ka, kb, coef, Bt, QS, Op, self._tc_status)
+                    return
             # the integrals carry split-BF16x3 error (~2^-16): W' in FP32
-            # (half the bytes of the float-pair layout), T values and sums
-            # still float pairs
+            # (half the bytes of the float-pair layout)
             W32 = self.eris.f32(const, QS) if const else D.to_f32_rows(Wp, QS)
             L.check(self._spmm32(T, pa, pb, ka, kb, float(coef), _ptr(W32), int(QS), W32.shape[1], _ptr(Op), stream))
         elif self._df:
@@ -295,6 +308,7 @@ class FRICCSDGPU:
           each pair runs as one pass over a combined W.
         Each rearrangement changes results only at the level of FP64 rounding.
         """
+        self._dims = tuple(t2.shape)
         E = self.eris
         s = self.settings
         m = int(s["m_keep"])
@@ -453,13 +467,20 @@ class FRICCSDGPU:
                     # (every iteration into this solver's own buffer, or once
                     # into the block the solvers of these integrals share)
                     R = E.vvvv_rebuild
-                    if self.rebuild_vvvv:
+                    from .cholesky import dense_spmm, dense_spmm_ok
+                    if self.split_sparse == "dense" and dense_spmm_ok(self._dims, 0, 1, 2, 3, v * v):
+                        if self.rebuild_vvvv or self._vvvv_bt is None:
+                            self._vvvv_bt = R.rebuild_split_b(self._vvvv_bt)
+                        dense_spmm(T, self._dims, 0, 1, 2, 3, 1.0, self._vvvv_bt, v * v, t2new, self._tc_status)
+                        W = None
+                    elif self.rebuild_vvvv:
                         if self._vvvv_buf is None:
                             self._vvvv_buf = torch.empty(v * v, R.ldw, dtype=torch.float32, device=t2.device)
                         W = R.rebuild(self._vvvv_buf)
                     else:
                         W = R.W if R.W is not None else R.rebuild()
-                    L.check(self._spmm32(T, 0, 1, 2, 3, 1.0, _ptr(W), v * v, R.ldw, _ptr(t2new), st))
+                    if W is not None:
+                        L.check(self._spmm32(T, 0, 1, 2, 3, 1.0, _ptr(W), v * v, R.ldw, _ptr(t2new), st))
                 else:
                     self._spmm(T, 0, 1, 2, 3, 1.0, E.vvvvT, v * v, t2new, st, const="vvvvT")  # (ac|bd) of 2323
                 XY = torch.zeros(o, o, 2, o, v, dtype=t2.dtype, device=t2.device)

@@ -131,6 +131,17 @@ class DeviceERIs:
                 self._splits[("tc", n)] = (role, split_a(x) if role == "A" else split_b(x))
             torch.cuda.current_stream().synchronize()
 
+    def tc_w(self, name, qs):
+        """The split W^T ([hi|lo|hi], rows q) of a constant W' block viewed as
+        [rows][qs]: the B operand of the split-precision dense sparse terms.
+        Built on first use (the first, eager iteration)."""
+        from .cholesky import split_b
+        key = ("tcW", name, qs)
+        if key not in self._splits:
+            x = getattr(self, name)
+            self._splits[key] = split_b(x.reshape(-1, qs))
+        return self._splits[key]
+
     def tc(self, name, role):
         got = self._splits.get(("tc", name))
         if got is None or got[0] != role:

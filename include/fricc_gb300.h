@@ -181,6 +181,15 @@ int fricc_spmm_f1(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, 
 int fricc_spmm_f32(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const float* W, int64_t QS,
                    int64_t ldw, double* Op, void* stream);
 
+/* The compressed T as a dense [dims[pa]*dims[pb]][R] matrix (R =
+ * dims[ka]*dims[kb]; row P = (pa,pb) pair, column r = (ka,kb) pair) of
+ * coef * value, split into BF16 hi + lo and written as the tensor-core A
+ * operand [hi | hi | lo] (rows of kp >= 3R elements; everything else zero):
+ * the split-precision form contracts it with fricc_gemm_bf16_tn_strided
+ * against the split W^T.  Stream-ordered. */
+int fricc_densify_bf16x3(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, void* Ap, int64_t kp,
+                         void* stream);
+
 /* Strided batched GEMM, FP64 in and out, products and sums in FP32 pairs
  * (no reference counterpart; it runs the dense O^2V^3 contractions of the
  * iteration):  C[b] = alpha * A[b] @ B[b] + beta * C[b], b < batch.
@@ -284,6 +293,13 @@ int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int
                        void* stream);
 int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t kp, float* W, int64_t ldw,
                               unsigned* status, void* stream);
+
+/* fricc_vvvv_rebuild_split_b: the same rebuild written as the B operand of
+ * the dense O^2V^4 GEMM: row q = a*v + b, K index k = c*v + d, (ac|bd) as
+ * [hi | lo | hi] at k, v^2 + k, 2 v^2 + k (rows of kpo >= 3 v^2 elements, a
+ * multiple of 8; the padding is zeroed).  status as above. */
+int fricc_vvvv_rebuild_split_b(const void* Ap, const void* Bp, int64_t v, int64_t kp, void* Bout, int64_t kpo,
+                               unsigned* status, void* stream);
 
 /* The general forms behind the split-precision dense algebra.
  * fricc_split_bf16x3_strided: as fricc_split_bf16x3 for a strided view:

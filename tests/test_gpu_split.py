@@ -92,7 +92,44 @@ def test_spmm_f32_within_fp32_error(gpulib, systems):
     assert bool(((a - b).abs() <= 2.0 ** -16 * c + 1e-18).all())
 
 
-@pytest.mark.parametrize("sums", ["fp32", "pairs"])
+def test_dense_spmm_and_split_b_rebuild(gpulib, systems):
+    """The split form's dense path: the (vv|vv) rebuild written as the B'
+    operand (hi + lo within 2^-16 of (ac|bd)), and the compressed T densified
+    and contracted on the tensor cores against it, within 2^-14 of
+    sum |W||T| of the FP64 sparse kernel."""
+    from fricc_gb300 import _lib as L
+    from fricc_gb300 import py_rccsd
+    from fricc_gb300.cholesky import dense_spmm
+    s, E, Es = systems
+    o, v = s.nocc, s.nvir
+    R = Es.vvvv_rebuild
+    Bt = R.rebuild_split_b()
+    R.check()
+    vv = v * v
+    hi, lo = Bt[:, :vv].double(), Bt[:, vv:2 * vv].double()
+    assert torch.equal(Bt[:, :vv], Bt[:, 2 * vv:3 * vv]) and bool((Bt[:, 3 * vv:] == 0).all())
+    ref = E.vvvvT.reshape(vv, vv).T  # [q=(a,b)][k=(c,d)] = (ac|bd)
+    Lv = torch.from_numpy(s.L).cuda()[:, o:, o:].abs()
+    scale = torch.einsum("Pac,Pbd->abcd", Lv, Lv).reshape(vv, vv)
+    assert float(((hi + lo - ref).abs() / scale).max()) < 2.0 ** -14
+    t2 = torch.from_numpy(np.ascontiguousarray(s.mp2_amplitudes()[1])).cuda()
+    T = py_rccsd.SparseTensor4d(t2, t2.shape, 20000, "fri", "systematic", rn=0.5)
+    Ta = py_rccsd.SparseTensor4d(t2.abs(), t2.shape, 20000, "fri", "systematic", rn=0.5)
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    a = torch.randn(o * o, vv, dtype=torch.float64, device="cuda") * 1e-3
+    b, c = a.clone(), torch.zeros_like(a)
+    W = E.vvvvT.reshape(vv, vv).contiguous()
+    L.check(gpulib.fricc_spmm(T.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(W.data_ptr()), vv,
+                              ctypes.c_void_p(a.data_ptr()), st))
+    assert dense_spmm(T.handle, t2.shape, 0, 1, 2, 3, 1.0, Bt, vv, b)
+    Wa = scale.T.contiguous()  # [k][q] bound of |W|
+    L.check(gpulib.fricc_spmm(Ta.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(Wa.data_ptr()), vv,
+                              ctypes.c_void_p(c.data_ptr()), st))
+    torch.cuda.synchronize()
+    assert bool(((a - b).abs() <= 2.0 ** -14 * c + 1e-18).all())
+
+
+@pytest.mark.parametrize("sums", ["dense", "fp32", "pairs"])
 def test_split_iteration_delta_e_sums(gpulib, systems, sums):
     from fricc_gb300.friccsd import FRICCSDGPU
     s, E, Es = systems
