@@ -271,19 +271,21 @@ def run_gpu(args):
     tc_roof = None
     if Es is not None:
         R = Es.vvvv_rebuild
-        buf = solver._vvvv_buf
+        dense = solver._vvvv_bt is not None  # the rebuild the solver uses
+        rebuild = (lambda: R.rebuild_split_b(solver._vvvv_bt)) if dense else (lambda: R.rebuild(solver._vvvv_buf))
         ra, rb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        R.rebuild(buf)
+        rebuild()
         ra.record(stream)
         for _ in range(3):
-            R.rebuild(buf)
+            rebuild()
         rb.record(stream)
         torch.cuda.synchronize()
         R.check()
         r_ms = ra.elapsed_time(rb) / 3
         pk = measured_peaks().get("bf16_tflops")
         ach = R.flops() / (r_ms / 1000.0) / 1e12
-        tc_roof = {"kernel": "k_gemm_tc<EpiVvvv> ((vv|vv) rebuild, tcgen05 BF16, split-BF16x3, FP32 accumulation)",
+        tc_roof = {"kernel": ("k_gemm_tc<EpiVvvvSplitB>" if dense else "k_gemm_tc<EpiVvvv>")
+                   + " ((vv|vv) rebuild, tcgen05 BF16, split-BF16x3, FP32 accumulation)",
                    "bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s",
                    "frac": ach / pk if pk else None, "ms": r_ms,
                    "flops": R.flops(), "peak_source": "bf16_tflops (burst) of MEASURED_PEAKS.json"}
@@ -303,6 +305,8 @@ def run_gpu(args):
     launches = lib.fricc_launch_count() - launches0
     p_ms, p_n, p_fl = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
     _lib.check(lib.fricc_prof_read(ctypes.byref(p_ms), ctypes.byref(p_n), ctypes.byref(p_fl)))
+    t_ms, t_n, t_fl = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
+    _lib.check(lib.fricc_prof_read_tc(ctypes.byref(t_ms), ctypes.byref(t_n), ctypes.byref(t_fl)))
     lib.fricc_prof_enable(0)
     energies.append(solver.read_energy()[0])
 
@@ -344,7 +348,8 @@ def run_gpu(args):
         kname, bound, peak = "k_spmm (bucketed sparse-T2 x dense-W, FP64)", "fp64", FP64_PEAK_TFLOPS
         psrc = "measured FP64 FMA rate of this GB300 pool (DFMA probe); FP64 is not in MEASURED_PEAKS.json"
     elif args.precision == "split":
-        kname, bound, peak = "k_spmm_f32 (bucketed sparse-T2 x dense-W, FP32)", "fp32-pipe", FP32_PEAK_TFLOPS
+        kname, bound, peak = "k_spmm_f32 (bucketed sparse-T2 x dense-W, FP32; terms too small for the tensor cores)", \
+            "fp32-pipe", FP32_PEAK_TFLOPS
         psrc = ("FP32 FMA rate of this GB300 pool (74.2 TF/s, FFMA probe): one packed FMA per two outputs, "
                 "2 flops per multiply-add")
     else:
@@ -358,6 +363,22 @@ def run_gpu(args):
             "launches": int(p_n.value), "kernel_ms": p_ms.value,
             "kernel_share_of_step": p_ms.value / ms if ms > 0 else None,
             "peak_source": psrc}
+    if args.precision == "split":
+        # the dominant kernel of the split form: the tensor-core GEMMs
+        # (dense sparse terms, dense algebra, (vv|vv) rebuild), timed live
+        sus = measured_peaks().get("bf16_tflops_sustained")
+        tc_ach = (t_fl.value / (t_ms.value / 1000.0)) / 1e12 if t_ms.value > 0 else None
+        sparse_roof = roof
+        roof = {"kernel": "k_gemm_tc (tcgen05 split-BF16x3 GEMMs: the sparse terms on the zero-filled compressed "
+                          "T2, the dense algebra, the (vv|vv) rebuild)",
+                "bound": "tensor", "achieved": tc_ach, "peak": sus, "unit": "TFLOP/s",
+                "frac": (tc_ach / sus) if (tc_ach and sus) else None, "traffic": None,
+                "launches": int(t_n.value), "kernel_ms": t_ms.value,
+                "kernel_share_of_step": t_ms.value / ms if ms > 0 else None,
+                "flops_counted": "2 M N K' per launch (K' = 3 K, the three BF16 products; zero padding and the "
+                                 "zeros of the compressed T2 included)",
+                "peak_source": "bf16_tflops_sustained of MEASURED_PEAKS.json (kernels timed inside the step)",
+                "sparse_kernel": sparse_roof if sparse_roof.get("launches") else None}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,

@@ -76,6 +76,8 @@ SIGNATURES = [
     ("fricc_prof_enable", None, [ctypes.c_int]),
     ("fricc_prof_read", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_double)]),
+    ("fricc_prof_read_tc", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
+                                          ctypes.POINTER(ctypes.c_double)]),
     ("fricc_energy_update", ctypes.c_int, [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _i64, _dp, _dp, _dp, _vp]),
     ("fricc_energy_update_lin", ctypes.c_int, [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _i64, _dp, _dp, _dp, _vp]),
 ]

@@ -66,24 +66,27 @@ int fricc_cuda_fail(cudaError_t e, const char* what, const char* file, int line)
 static std::atomic<long long> g_launches{0};
 static std::atomic<bool> g_prof{false};
 static std::mutex g_prof_mu;
-static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_prof_ev;
-static std::vector<double> g_prof_flops;
-static cudaEvent_t g_prof_pending = nullptr;
+// channel 0: the sparse contraction kernels; channel 1: the tensor-core GEMMs
+static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_prof_ev[2];
+static std::vector<double> g_prof_flops[2];
+static cudaEvent_t g_prof_pending[2] = {nullptr, nullptr};
 
 void fricc_note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 bool fricc_prof_on() { return g_prof.load(std::memory_order_relaxed); }
 
-void fricc_prof_record(cudaStream_t st, bool start, double flops) {
+void fricc_prof_record(cudaStream_t st, bool start, double flops, int ch) {
+  if (ch < 0 || ch > 1) return;
   std::lock_guard<std::mutex> lk(g_prof_mu);
   cudaEvent_t e;
   if (cudaEventCreate(&e) != cudaSuccess) return;
   cudaEventRecord(e, st);
   if (start) {
-    g_prof_pending = e;
-  } else if (g_prof_pending) {
-    g_prof_ev.emplace_back(g_prof_pending, e);
-    g_prof_flops.push_back(flops);
-    g_prof_pending = nullptr;
+    if (g_prof_pending[ch]) cudaEventDestroy(g_prof_pending[ch]);
+    g_prof_pending[ch] = e;
+  } else if (g_prof_pending[ch]) {
+    g_prof_ev[ch].emplace_back(g_prof_pending[ch], e);
+    g_prof_flops[ch].push_back(flops);
+    g_prof_pending[ch] = nullptr;
   } else {
     cudaEventDestroy(e);
   }
@@ -156,30 +159,38 @@ long long fricc_launch_count(void) { return g_launches.load(); }
 void fricc_prof_enable(int on) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   g_prof.store(on != 0);
-  for (auto& pr : g_prof_ev) {
-    cudaEventDestroy(pr.first);
-    cudaEventDestroy(pr.second);
+  for (int ch = 0; ch < 2; ++ch) {
+    for (auto& pr : g_prof_ev[ch]) {
+      cudaEventDestroy(pr.first);
+      cudaEventDestroy(pr.second);
+    }
+    g_prof_ev[ch].clear();
+    g_prof_flops[ch].clear();
+    if (g_prof_pending[ch]) cudaEventDestroy(g_prof_pending[ch]);
+    g_prof_pending[ch] = nullptr;
   }
-  g_prof_ev.clear();
-  g_prof_flops.clear();
 }
 
-int fricc_prof_read(double* ms, long long* launches, double* flops) {
+static int prof_read(int ch, double* ms, long long* launches, double* flops) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   double t = 0.0, f = 0.0;
-  for (size_t k = 0; k < g_prof_ev.size(); ++k) {
+  for (size_t k = 0; k < g_prof_ev[ch].size(); ++k) {
     float x = 0.f;
-    cudaError_t e = cudaEventSynchronize(g_prof_ev[k].second);
-    if (e == cudaSuccess) e = cudaEventElapsedTime(&x, g_prof_ev[k].first, g_prof_ev[k].second);
+    cudaError_t e = cudaEventSynchronize(g_prof_ev[ch][k].second);
+    if (e == cudaSuccess) e = cudaEventElapsedTime(&x, g_prof_ev[ch][k].first, g_prof_ev[ch][k].second);
     if (e != cudaSuccess) return fricc_cuda_fail(e, "prof_read", __FILE__, __LINE__);
     t += x;
-    f += g_prof_flops[k];
+    f += g_prof_flops[ch][k];
   }
   if (ms) *ms = t;
-  if (launches) *launches = (long long)g_prof_ev.size();
+  if (launches) *launches = (long long)g_prof_ev[ch].size();
   if (flops) *flops = f;
   return FRICC_OK;
 }
+
+int fricc_prof_read(double* ms, long long* launches, double* flops) { return prof_read(0, ms, launches, flops); }
+
+int fricc_prof_read_tc(double* ms, long long* launches, double* flops) { return prof_read(1, ms, launches, flops); }
 
 const char* fricc_last_error(void) { return g_err; }
 

@@ -95,7 +95,7 @@ void fricc_free(void* p, cudaStream_t s);
 // event timing of the sparse contraction kernel (off unless enabled).
 void fricc_note_launch(int n = 1);
 bool fricc_prof_on();
-void fricc_prof_record(cudaStream_t st, bool start, double flops);
+void fricc_prof_record(cudaStream_t st, bool start, double flops, int channel = 0);
 
 template <class T>
 inline int fricc_alloc_t(T** p, size_t n, cudaStream_t s) {

@@ -618,8 +618,11 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
   ksplit = (int)fricc_cdiv(nk, nkc);  // every slice non-empty
   const int64_t units = tm * tn * ksplit;
   const unsigned grid = (unsigned)(units < nsm ? units : nsm);  // persistent: one CTA per SM
+  const bool prof = fricc_prof_on();
   if (status) {
+    if (prof) fricc_prof_record(st, true, 0.0, 1);
     k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, status);
+    if (prof) fricc_prof_record(st, false, 2.0 * (double)M * (double)N * (double)K, 1);
     fricc_note_launch();
     e = cudaGetLastError();
     return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "gemm_tc", __FILE__, __LINE__);
@@ -629,7 +632,9 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
   if (rc) return rc;
   e = cudaMemsetAsync(err, 0, sizeof(unsigned), st);
   if (e == cudaSuccess) {
+    if (prof) fricc_prof_record(st, true, 0.0, 1);
     k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, err);
+    if (prof) fricc_prof_record(st, false, 2.0 * (double)M * (double)N * (double)K, 1);
     fricc_note_launch();
     e = cudaGetLastError();
   }

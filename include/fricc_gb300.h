@@ -333,6 +333,9 @@ int fricc_stream_destroy(void* stream);
 long long fricc_launch_count(void);
 void fricc_prof_enable(int on);
 int fricc_prof_read(double* ms, long long* launches, double* flops);
+/* The same record for the tensor-core GEMM launches (fricc_gemm_bf16_*,
+ * the rebuilds; flops = 2 M N K' of the BF16 products). */
+int fricc_prof_read_tc(double* ms, long long* launches, double* flops);
 
 #ifdef __cplusplus
 }
