@@ -160,8 +160,11 @@ def footprint_bytes(o: int, v: int, precision: str = "df64") -> int:
 
 class SolveServer:
     def __init__(self, n_workers: int = 8, hbm_budget: float = 200e9, precision: str = "df64", max_cycle: int = 30,
-                 tol: float = 1e-7, device="cuda", graph: bool = False, device_inputs: bool = True):
+                 tol: float = 1e-7, device="cuda", graph: bool = False, device_inputs: bool = True,
+                 rebuild_vvvv: bool = True):
         self.graph = graph
+        # split precision: rebuild (vv|vv) every iteration, or once per solve
+        self.rebuild_vvvv = rebuild_vvvv
         # draw each request's synthetic system on the GPU (DeviceSystem) or
         # on the host (SyntheticSystem, numpy)
         self.device_inputs = device_inputs
@@ -188,7 +191,7 @@ class SolveServer:
             else:
                 E = DeviceERIs.from_system(system, device=self.device)
             solver = FRICCSDGPU(E, {"m_keep": req.m}, rn_draw=GlibcRand(req.seed), precision=self.precision,
-                                graph=self.graph)
+                                graph=self.graph, rebuild_vvvv=self.rebuild_vvvv)
             t1, t2 = mp2_device(E)
             req.started = time.perf_counter() - t0
             eold = solver.energy(t1, t2)

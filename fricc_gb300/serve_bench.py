@@ -53,22 +53,35 @@ def run_replicas(args):
                                    "tau_median": float(np.median(taus))}}
 
 
+def _warm(server, args):
+    """One untimed pass of a few requests through the same server: the
+    first requests of a process pay one-time set-up (kernel modules loaded
+    on first launch, per-thread library handles, allocator growth)."""
+    warm = request_stream(max(2, min(args.streams, 8)), 1e6, seed=args.seed + 7919,
+                          nocc=(args.nocc_min, args.nocc_max))
+    server.run(warm, time_scale=0.0)
+
+
 def run_serve(args):
     reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
     server = SolveServer(n_workers=args.streams, precision=args.precision, max_cycle=args.max_cycle, graph=args.graph,
-                         device_inputs=not args.host_inputs)
+                         device_inputs=not args.host_inputs, rebuild_vvvv=not args.rebuild_once)
+    _warm(server, args)
     out = server.run(reqs, time_scale=1.0)
     served = latency_summary(out)
     line = {"mode": "serve", "requests": args.requests, "rate_per_s": args.rate, "workers": args.streams,
             "inputs": "host (numpy)" if args.host_inputs else "device (torch Philox)",
+            "vvvv_rebuild": "once per solve" if args.rebuild_once else "every iteration",
             "precision": args.precision, "max_cycle": args.max_cycle, "graph": args.graph, "served": served}
     if args.plain:
         # the same requests, one at a time, FP64, arriving all at once
         plain_reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
         for r in plain_reqs:
             r.arrival = 0.0
-        plain = SolveServer(n_workers=1, precision="fp64", max_cycle=args.max_cycle,
-                            device_inputs=not args.host_inputs).run(plain_reqs)
+        plain_server = SolveServer(n_workers=1, precision="fp64", max_cycle=args.max_cycle,
+                                   device_inputs=not args.host_inputs)
+        _warm(plain_server, args)
+        plain = plain_server.run(plain_reqs)
         line["plain"] = latency_summary(plain)
         diffs = [abs(a.e_corr - b.e_corr) for a, b in zip(sorted(out, key=lambda r: r.rid),
                                                           sorted(plain_reqs, key=lambda r: r.rid))]
@@ -92,6 +105,8 @@ def main():
     p.add_argument("--nocc-max", type=int, default=30)
     p.add_argument("--max-cycle", type=int, default=30)
     p.add_argument("--plain", action="store_true")
+    p.add_argument("--rebuild-once", action="store_true",
+                   help="split precision: rebuild (vv|vv) once per solve instead of every iteration")
     p.add_argument("--host-inputs", action="store_true",
                    help="draw each request's synthetic system with numpy on the host (default: on the GPU)")
     p.add_argument("--graph", action="store_true", help="replay each solver's iteration from a CUDA graph")
