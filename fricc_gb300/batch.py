@@ -48,7 +48,9 @@ class ReplicaBatch:
         self.eris = eris
         self.seeds = list(seeds)
         self.n = len(self.seeds)
-        self.solvers = [FRICCSDGPU(eris, settings, rn_draw=GlibcRand(s), precision=precision, graph=graph)
+        # split precision: the replicas share one (vv|vv) operand, rebuilt once
+        self.solvers = [FRICCSDGPU(eris, settings, rn_draw=GlibcRand(s), precision=precision, graph=graph,
+                                   rebuild_vvvv=precision != "split")
                         for s in self.seeds]
         t1, t2 = mp2_device(eris)
         self.t1 = [t1.clone() for _ in range(self.n)]

@@ -13,6 +13,7 @@ contraction (rows (c,d), columns (a,b)), so it never exists in FP64.
 from __future__ import annotations
 
 import ctypes
+import threading
 
 import torch
 
@@ -216,6 +217,8 @@ class VvvvRebuild:
         self.ldw = self.v * self.v + (self.v * self.v) % 2
         self.status = torch.zeros(1, dtype=torch.int32, device=Lf.device)
         self.W = None
+        self.Bt = None
+        self._lock = threading.Lock()
         self.rebuilds = 0
 
     def flops(self) -> float:
@@ -251,6 +254,18 @@ class VvvvRebuild:
                                                     _p(self.status), _st()))
         self.rebuilds += 1
         return out
+
+    def shared_split_b(self) -> torch.Tensor:
+        """The B operand rebuilt once and kept on this object for every
+        solver of these integrals (built under a lock, then waited for, so
+        solvers on other streams and threads read a finished block)."""
+        if self.Bt is None:
+            with self._lock:
+                if self.Bt is None:
+                    bt = self.rebuild_split_b()
+                    torch.cuda.current_stream().synchronize()
+                    self.Bt = bt
+        return self.Bt
 
     def check(self):
         if int(self.status.item()):

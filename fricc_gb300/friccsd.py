@@ -469,9 +469,12 @@ class FRICCSDGPU:
                     R = E.vvvv_rebuild
                     from .cholesky import dense_spmm, dense_spmm_ok
                     if self.split_sparse == "dense" and dense_spmm_ok(self._dims, 0, 1, 2, 3, v * v):
-                        if self.rebuild_vvvv or self._vvvv_bt is None:
+                        if self.rebuild_vvvv:  # into this solver's own buffer, every iteration
                             self._vvvv_bt = R.rebuild_split_b(self._vvvv_bt)
-                        dense_spmm(T, self._dims, 0, 1, 2, 3, 1.0, self._vvvv_bt, v * v, t2new, self._tc_status)
+                            Bt = self._vvvv_bt
+                        else:                  # once, shared by the solvers of these integrals
+                            Bt = R.shared_split_b()
+                        dense_spmm(T, self._dims, 0, 1, 2, 3, 1.0, Bt, v * v, t2new, self._tc_status)
                         W = None
                     elif self.rebuild_vvvv:
                         if self._vvvv_buf is None:

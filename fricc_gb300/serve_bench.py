@@ -30,7 +30,11 @@ from .synthetic import WORKLOADS, make_system
 def run_replicas(args):
     w = WORKLOADS["o20v100x64"]
     system = make_system("o20v100x64", seed=0)
-    E = DeviceERIs.from_system(system)
+    if args.precision == "split":
+        from .cholesky import split_eris
+        E = split_eris(system)
+    else:
+        E = DeviceERIs.from_system(system)
     settings = {"m_keep": w["m"]}
     seeds = [1000 + r for r in range(args.replicas)]
     batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision, graph=args.graph)
