@@ -278,7 +278,8 @@ def split_eris(system, device="cuda"):
     tensor cores (split-BF16x3, FP32 accumulation, widened to FP64 for the
     dense algebra), the (vv|vv) block never stored in FP64 but rebuilt by
     ``VvvvRebuild`` for the O^2V^4 contraction; the small blocks (oo|oo),
-    (ov|oo), (ov|ov), (ov|vo) and sum_cd (ac|bd) in FP64 from the factor."""
+    (ov|oo), (ov|ov), (ov|vo) from the FP64 factor on the FP32-pair GEMM
+    (~2^-40), sum_cd (ac|bd) in FP64."""
     from .rccsd_dense import DeviceERIs, _dev_tensor
     dev = torch.device(device)
     Lf = _dev_tensor(system.L, dev)
@@ -290,10 +291,16 @@ def split_eris(system, device="cuda"):
         return Lf[:, sl[p], sl[q]].reshape(naux, -1).t().contiguous()  # [(p,q), P]
 
     def fp64_blk(name):
+        # FP64-accurate (~2^-40) on the FP32-pair GEMM: GB300's FP64 unit
+        # would spend ~0.1 s per (ov|ov)-sized block of a large request
+        from .rccsd_dense import gemm_df
         p, q, r, t = name
         n1 = (Lf[:, sl[p], sl[q]]).shape[1:]
         n2 = (Lf[:, sl[r], sl[t]]).shape[1:]
-        return (fac(p, q) @ fac(r, t).t()).reshape(*n1, *n2)
+        A, B = fac(p, q), fac(r, t)
+        C = torch.empty(A.shape[0], B.shape[0], dtype=torch.float64, device=dev)
+        gemm_df(A, B.t(), C)
+        return C.reshape(*n1, *n2)
 
     def tc_blk(name):
         p, q, r, t = name
