@@ -59,6 +59,9 @@ def parse():
     p.add_argument("--workload", default="o30v150")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--autotune", action="store_true",
+                   help="df64: time the launch configurations of every sparse term and GEMM shape during the "
+                        "warm-up and keep the fastest")
     p.add_argument("--precision", default="df64", choices=["fp64", "df64", "split"],
                    help="arithmetic of the sparse terms: FP64, or FP32 pairs (48-bit products, ~40-bit sums) on the "
                         "FP32 pipe; 'split' also rebuilds (vv|vv) every iteration from the BF16 hi+lo Cholesky "
@@ -242,7 +245,7 @@ def run_gpu(args):
         from fricc_gb300.cholesky import split_eris
         Es = split_eris(system, device=dev)
     solver = FRICCSDGPU(Es if Es is not None else E, {"m_keep": m}, rn_draw=seeded_draws(1000 + rank),
-                        precision=args.precision)
+                        precision=args.precision, autotune=args.autotune)
     stream = torch.cuda.current_stream()
 
     for _ in range(args.warmup):
@@ -391,7 +394,7 @@ def run_gpu(args):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": f"working set > L2 ((ac|bd) {8 * v ** 4 / 1e9:.2f} GB and its float-pair copy "
                              "streamed by the O^2V^4 term every step)",
-                       "precision": args.precision},
+                       "precision": args.precision, "autotune": bool(args.autotune)},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
             "clocks": clk.summary(), "energy_last": energies[-1],
             "delta_e_vs_fp64_per_step": delta_e,

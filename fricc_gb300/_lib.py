@@ -73,6 +73,7 @@ SIGNATURES = [
     ("fricc_stream_create", ctypes.c_int, [ctypes.POINTER(_vp)]),
     ("fricc_stream_destroy", ctypes.c_int, [_vp]),
     ("fricc_launch_count", ctypes.c_longlong, []),
+    ("fricc_tune_set", ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     ("fricc_prof_enable", None, [ctypes.c_int]),
     ("fricc_prof_read", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_double)]),

@@ -72,6 +72,9 @@ static std::vector<double> g_prof_flops[2];
 static cudaEvent_t g_prof_pending[2] = {nullptr, nullptr};
 
 void fricc_note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
+
+static thread_local int g_tune[FRICC_TUNE_KNOBS] = {-1, -1, -1};
+int fricc_tune_get(int knob) { return knob >= 0 && knob < FRICC_TUNE_KNOBS ? g_tune[knob] : -1; }
 bool fricc_prof_on() { return g_prof.load(std::memory_order_relaxed); }
 
 void fricc_prof_record(cudaStream_t st, bool start, double flops, int ch) {
@@ -155,6 +158,20 @@ extern "C" {
 int fricc_version(void) { return 100; }
 
 long long fricc_launch_count(void) { return g_launches.load(); }
+
+int fricc_tune_set(int knob, int value) {
+  static const int lo[FRICC_TUNE_KNOBS] = {1, 0, 1}, hi[FRICC_TUNE_KNOBS] = {4, 3, 16};
+  if (knob < 0 || knob >= FRICC_TUNE_KNOBS || (value != -1 && (value < lo[knob] || value > hi[knob]))) {
+    fricc_set_error("tune_set: bad knob or value");
+    return FRICC_ERR_ARG;
+  }
+  if (knob == FRICC_TUNE_SPMM_PPT && value == 3) {
+    fricc_set_error("tune_set: pairs per thread is 1, 2 or 4");
+    return FRICC_ERR_ARG;
+  }
+  g_tune[knob] = value;
+  return FRICC_OK;
+}
 
 void fricc_prof_enable(int on) {
   std::lock_guard<std::mutex> lk(g_prof_mu);

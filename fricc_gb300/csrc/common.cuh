@@ -94,6 +94,18 @@ void fricc_free(void* p, cudaStream_t s);
 // Instrumentation: a count of every kernel this library launches, and CUDA
 // event timing of the sparse contraction kernel (off unless enabled).
 void fricc_note_launch(int n = 1);
+
+// Launch-configuration overrides set by an autotuner (thread-local, so a
+// tuning solver does not change other threads' launches); -1 = the built-in
+// choice.  Knobs: FRICC_TUNE_SPMM_PPT (output pairs per thread of the
+// float-pair sparse kernel: 1, 2 or 4), FRICC_TUNE_GEMM_TILE (the FP32-pair
+// GEMM's tile: 0 = 64x64, 1 = 128x32, 2 = 32x128, 3 = 32x160),
+// FRICC_TUNE_GEMM_COVER (CTAs per SM the GEMM's split K aims for, 1..16).
+#define FRICC_TUNE_SPMM_PPT 0
+#define FRICC_TUNE_GEMM_TILE 1
+#define FRICC_TUNE_GEMM_COVER 2
+#define FRICC_TUNE_KNOBS 3
+int fricc_tune_get(int knob);
 bool fricc_prof_on();
 void fricc_prof_record(cudaStream_t st, bool start, double flops, int channel = 0);
 

@@ -721,10 +721,11 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
   float2* eval = nullptr;
   rc = fricc_alloc_t(&erow, T->m, st);
   if (!rc) rc = fricc_alloc_t(&eval, T->m, st);
-  // 2 q-pairs per thread: measured against 1 and 4 on the o30v150 terms
-  // (fewer leaves loads too few per thread, more costs occupancy)
+  // 2 q-pairs per thread unless tuned: measured against 1 and 4 over the
+  // o30v150 terms (fewer leaves loads too few per thread, more costs
+  // occupancy); a term's best can differ (an autotuner sets the knob)
   const int64_t QS2 = (QS + 1) / 2;
-  constexpr int ppt = 2;
+  const int ppt = fricc_tune_get(FRICC_TUNE_SPMM_PPT) > 0 ? fricc_tune_get(FRICC_TUNE_SPMM_PPT) : 2;
   const int64_t ntq = fricc_cdiv(QS2, DF_NT * ppt);
   if (!rc && (ntq > 65535 || bk->nbuckets > 0x7fffffffLL)) {
     fricc_set_error("spmm_f2: problem too large for one launch");
@@ -741,7 +742,9 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
     // launching one q tile at a time cut that traffic 6x but ran 50% longer
     // (900-CTA launches leave SMs idle at each tail), so it is not done.
     const dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq);
-    k_spmm_df<ppt><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
+    if (ppt == 1) k_spmm_df<1><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
+    else if (ppt == 4) k_spmm_df<4><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
+    else k_spmm_df<2><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
     fricc_note_launch();
     if (prof) fricc_prof_record(st, false, 2.0 * (double)T->m * (double)QS);
     fricc_note_launch();

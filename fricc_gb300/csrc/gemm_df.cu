@@ -250,17 +250,25 @@ int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t ba
   int tm = 4, tn = 4;
   {
     const int cand[4][2] = {{4, 4}, {8, 2}, {2, 8}, {2, 10}};
-    int64_t best = -1;
-    for (const auto& c : cand) {
-      const int64_t pad = fricc_cdiv(M, 16 * c[0]) * 16 * c[0] * fricc_cdiv(N, 16 * c[1]) * 16 * c[1];
-      if (best < 0 || pad < best) { best = pad; tm = c[0]; tn = c[1]; }
+    const int forced = fricc_tune_get(FRICC_TUNE_GEMM_TILE);
+    if (forced >= 0) {
+      tm = cand[forced][0];
+      tn = cand[forced][1];
+    } else {
+      int64_t best = -1;
+      for (const auto& c : cand) {
+        const int64_t pad = fricc_cdiv(M, 16 * c[0]) * 16 * c[0] * fricc_cdiv(N, 16 * c[1]) * 16 * c[1];
+        if (best < 0 || pad < best) { best = pad; tm = c[0]; tn = c[1]; }
+      }
     }
   }
   const int64_t BM = 16 * tm, BN = 16 * tn;
   const int64_t tiles = fricc_cdiv(M, BM) * fricc_cdiv(N, BN) * batch;
-  // split K until the grid covers the GPU about four times over
+  // split K until the grid covers the GPU about four (or the tuned number
+  // of) times over
+  const int cover = fricc_tune_get(FRICC_TUNE_GEMM_COVER) > 0 ? fricc_tune_get(FRICC_TUNE_GEMM_COVER) : 4;
   int splits = 1;
-  while (splits < 1024 && tiles * splits < 152 * 4 && K / (2 * splits) >= 8 * BK) splits *= 2;
+  while (splits < 1024 && tiles * splits < 152 * cover && K / (2 * splits) >= 8 * BK) splits *= 2;
   g.splits = splits;
   g.kchunk = fricc_cdiv(fricc_cdiv(K, splits), BK) * BK;
   if (fricc_cdiv(M, BM) > 65535 || batch * splits > 65535) {

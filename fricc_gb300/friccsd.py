@@ -136,7 +136,8 @@ class _Handle:
 
 class FRICCSDGPU:
     def __init__(self, eris: D.DeviceERIs, fri_settings=None, level_shift=0.0, rn_draw=libc_uniform,
-                 wvvvv_t1t1="reference", precision="fp64", graph=False, rebuild_vvvv=True, split_sparse="dense"):
+                 wvvvv_t1t1="reference", precision="fp64", graph=False, rebuild_vvvv=True, split_sparse="dense",
+                 autotune=False):
         s = dict(DEFAULT_SETTINGS)
         s.update(fri_settings or {})
         for c in s["compressed_contractions"]:
@@ -172,6 +173,10 @@ class FRICCSDGPU:
         if split_sparse not in ("dense", "fp32", "pairs"):
             raise ValueError("split_sparse must be 'dense', 'fp32' or 'pairs'")
         self.split_sparse = split_sparse
+        # df64: time the launch configurations of every sparse term and
+        # FP32-pair GEMM shape on first use and keep the fastest
+        from .autotune import Autotuner
+        self._tuner = Autotuner() if (autotune and precision == "df64") else None
         self._spmm32 = L.load().fricc_spmm_f1 if split_sparse == "pairs" else L.load().fricc_spmm_f32
         self._dims = None
         self._vvvv_bt = None
@@ -235,7 +240,15 @@ class FRICCSDGPU:
         elif self._df:
             W2 = self.eris.split(const) if const else D.split_f2(Wp, QS)
             assert W2.numel() == (Wp.numel() // QS) * ((QS + 1) // 2) * 4, "float-pair W' split with another QS"
-            L.check(self.lib.fricc_spmm_f2(T, pa, pb, ka, kb, float(coef), _ptr(W2), int(QS), _ptr(Op), stream))
+
+            def launch(outs):
+                L.check(self.lib.fricc_spmm_f2(T, pa, pb, ka, kb, float(coef), _ptr(W2), int(QS), _ptr(outs[0]),
+                                               stream))
+            if self._tuner is not None:
+                from .autotune import SPMM_CANDIDATES
+                self._tuner.run(("spmm", pa, pb, ka, kb, int(QS), self._dims), SPMM_CANDIDATES, launch, [Op])
+            else:
+                launch([Op])
         else:
             L.check(self.lib.fricc_spmm(T, pa, pb, ka, kb, float(coef), _ptr(Wp), int(QS), _ptr(Op), stream))
 
@@ -360,11 +373,22 @@ class FRICCSDGPU:
                 return D.einsum_df(spec, A_, B_, gemm=mm)
         else:
             mm0 = D.gemm_df if self._df else D.gemm_torch
+            tuner = self._tuner
 
             def mm(A_, B_, C_, alpha=1.0, beta=0.0, const=None, const_b=None):
-                return mm0(A_, B_, C_, alpha, beta)
+                if tuner is None:
+                    return mm0(A_, B_, C_, alpha, beta)
+                from .autotune import GEMM_CANDIDATES
+                key = ("gemm", tuple(A_.shape), A_.stride(), tuple(B_.shape), B_.stride(), tuple(C_.shape),
+                       C_.stride(), beta != 0.0)
+                tuner.run(key, GEMM_CANDIDATES, lambda outs: mm0(A_, B_, outs[0], alpha, beta), [C_])
+                return C_
 
-            ein2 = D.einsum_df if self._df else torch.einsum   # two-operand O^3V^2 contractions
+            if self._df:
+                def ein2(spec, A_, B_):   # two-operand O^3V^2 contractions
+                    return D.einsum_df(spec, A_, B_, gemm=mm)
+            else:
+                ein2 = torch.einsum
         f64, dev = t2.dtype, t2.device
         # cc_Foo / cc_Fvv share tt[p,q,r,s] = t2 + t1[p,r] t1[q,s]
         tt = t2 + ein("pr,qs->pqrs", t1, t1)

@@ -325,6 +325,15 @@ int fricc_gemm_bf16_tn_strided(const void* A, int64_t lda, const void* B, int64_
 int fricc_stream_create(void** out);
 int fricc_stream_destroy(void* stream);
 
+/* Launch-configuration overrides for an autotuner (no reference
+ * counterpart), thread-local; value -1 restores the built-in choice.
+ * knob 0: output pairs per thread of the float-pair sparse kernel (1, 2, 4);
+ * knob 1: tile of the FP32-pair GEMM (0 = 64x64, 1 = 128x32, 2 = 32x128,
+ * 3 = 32x160); knob 2: CTAs per SM the FP32-pair GEMM's split K aims for
+ * (1..16).  No knob changes a result's arithmetic except the GEMM's tile
+ * and split, which reorder its sums. */
+int fricc_tune_set(int knob, int value);
+
 /* Instrumentation (no reference counterpart): the number of kernels this
  * library has launched so far; and CUDA-event timing of every sparse
  * contraction kernel launched while enabled (fricc_prof_enable(1) clears
