@@ -71,6 +71,57 @@ class ReplicaBatch:
         except BaseException as e:  # surfaced by step()
             self._errors.append(e)
 
+    def _capture_batch(self):
+        """One CUDA graph for an iteration of every replica: each replica's
+        iteration is captured on a stream of its own (forked from the capture
+        stream and joined back), reading static amplitudes and device-resident
+        draws and writing the new amplitudes back into the static inputs, so
+        each replay advances the whole batch by one iteration."""
+        from . import _lib as L
+        from .friccsd import _CAPTURE_LOCK
+        dev = self.eris.device
+        self._bt1 = [t.contiguous().clone() for t in self.t1]
+        self._bt2 = [t.contiguous().clone() for t in self.t2]
+        self._brn = torch.zeros(self.n, 2, dtype=torch.float64, device=dev)
+        self._bstreams = [L.OwnStream(dev) for _ in range(self.n)]
+        self._bcap = L.OwnStream(dev)
+        cs, cur = self._bcap.stream, torch.cuda.current_stream()
+        g = torch.cuda.CUDAGraph()
+        with _CAPTURE_LOCK:
+            cs.wait_stream(cur)
+            with torch.cuda.stream(cs):
+                g.capture_begin(capture_error_mode="thread_local")
+                try:
+                    for r, sol in enumerate(self.solvers):
+                        sr = self._bstreams[r].stream
+                        sr.wait_stream(cs)
+                        with torch.cuda.stream(sr):
+                            o1, o2 = sol._update_eager(self._bt1[r], self._bt2[r], rn_dev=self._brn[r])
+                            self._bt1[r].copy_(o1)
+                            self._bt2[r].copy_(o2)
+                        cs.wait_stream(sr)
+                finally:
+                    g.capture_end()
+            cur.wait_stream(cs)
+        self._bgraph = g
+
+    def step_graph(self, record: bool = True):
+        """One iteration of every replica as one replay of the batch graph
+        (captured at the first call; the replicas' handles must exist, i.e.
+        one eager ``step()`` first)."""
+        if getattr(self, "_bgraph", None) is None:
+            self._capture_batch()
+        draws = [[sol.rn_draw(), sol.rn_draw()] for sol in self.solvers]  # the reference's order per replica
+        self._brn.copy_(torch.tensor(draws, dtype=torch.float64))
+        self._bgraph.replay()
+        for sol in self.solvers:
+            sol._iter += 1
+        self.t1, self.t2 = self._bt1, self._bt2
+        torch.cuda.current_stream().synchronize()
+        if record:
+            for r in range(self.n):
+                self.history[r].append(self.solvers[r].read_energy()[0])
+
     def step(self, record: bool = True):
         """One iteration of every replica (all streams joined on return)."""
         threads = [threading.Thread(target=self._work, args=(w,)) for w in range(self.k)]

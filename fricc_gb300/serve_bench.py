@@ -37,20 +37,25 @@ def run_replicas(args):
         E = DeviceERIs.from_system(system)
     settings = {"m_keep": w["m"]}
     seeds = [1000 + r for r in range(args.replicas)]
-    batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision, graph=args.graph)
-    for _ in range(args.warmup):
-        batch.step()
+    batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision,
+                         graph=args.graph and not args.batch_graph)
+    step = batch.step
+    for i in range(args.warmup):
+        step()
+        if args.batch_graph:  # the first step is eager (it creates the handles), then one graph per batch step
+            step = batch.step_graph
     torch.cuda.synchronize()
     t = time.perf_counter()
     for _ in range(args.steps):
-        batch.step()
+        step()
     torch.cuda.synchronize()
     dt = time.perf_counter() - t
     mean, var = batch.stats()
     burn = min(args.warmup, len(batch.history[0]) - 2)
     tmeans, terrs, taus = batch.trace_stats(burn=max(burn, 0))
     return {"mode": "replicas", "workload": "o20v100: nocc=20 nvir=100 naux=600 m=200000 per replica",
-            "replicas": args.replicas, "streams": args.streams, "precision": args.precision, "graph": args.graph,
+            "replicas": args.replicas, "streams": args.streams, "precision": args.precision,
+            "graph": "one graph per batch step" if args.batch_graph else args.graph,
             "iterations_per_s": args.replicas * args.steps / dt, "batch_steps_per_s": args.steps / dt,
             "e_corr_mean": mean, "e_corr_var": var, "iterations_each": args.warmup + args.steps,
             "trace_after_warmup": {"mean_of_means": float(tmeans.mean()), "mcmc_std_median": float(np.median(terrs)),
@@ -114,6 +119,8 @@ def main():
     p.add_argument("--host-inputs", action="store_true",
                    help="draw each request's synthetic system with numpy on the host (default: on the GPU)")
     p.add_argument("--graph", action="store_true", help="replay each solver's iteration from a CUDA graph")
+    p.add_argument("--batch-graph", action="store_true",
+                   help="replicas: capture every replica's iteration into one CUDA graph per batch step")
     args = p.parse_args()
     line = run_replicas(args) if args.mode == "replicas" else run_serve(args)
     print(json.dumps(line))

@@ -33,6 +33,30 @@ def test_replicas_alone_and_in_the_mix(gpulib):
     assert np.isfinite(mean) and var > 0.0  # distinct seeds give distinct samples
 
 
+@pytest.mark.parametrize("precision", ["df64", "split"])
+def test_batch_graph_matches_eager(gpulib, precision):
+    """One CUDA graph per batch step (every replica's iteration captured on
+    its own stream) gives the trajectories of the eager batch."""
+    from fricc_gb300.batch import ReplicaBatch
+    from fricc_gb300.cholesky import split_eris
+    from fricc_gb300.rccsd_dense import DeviceERIs
+    from fricc_gb300.synthetic import SyntheticSystem
+    s = SyntheticSystem(6, 24, 120, 0.05, 3)
+    E = split_eris(s) if precision == "split" else DeviceERIs.from_system(s)
+    settings = {"m_keep": 4000}
+    seeds = [31, 32, 33, 34, 35]
+    g = ReplicaBatch(E, settings, seeds, n_streams=3, precision=precision)
+    e = ReplicaBatch(E, settings, seeds, n_streams=3, precision=precision)
+    g.step()
+    e.step()
+    for _ in range(4):
+        g.step_graph()
+        e.step()
+    for r in range(len(seeds)):
+        assert np.max(np.abs(np.array(g.history[r]) - np.array(e.history[r]))) < 1e-13, r
+    torch.testing.assert_close(g.t2[0], e.t2[0], rtol=1e-12, atol=1e-18)
+
+
 def test_served_requests_match_lone_solves(gpulib):
     from fricc_gb300.batch import SolveServer, request_stream
     reqs = request_stream(6, rate=200.0, seed=5, nocc=(4, 7))
