@@ -59,6 +59,8 @@ def parse():
     p.add_argument("--workload", default="o30v150")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--no-split-form", action="store_true",
+                   help="skip the secondary measurement of the split-precision form")
     p.add_argument("--autotune", action="store_true",
                    help="df64: time the launch configurations of every sparse term and GEMM shape during the "
                         "warm-up and keep the fastest")
@@ -215,6 +217,52 @@ def cpu_baseline_line(eris_np, t1, t2, m, workload, seed):
             "sample": _sample_text(workload, cores, pairs, wall) + f" ({secs:.1f} s/iteration extrapolated)"}
 
 
+def split_form_line(args, system, E, t1, t2, m, stream):
+    """Iterations/s of the split-precision form on the bench's workload
+    (CUDA events over args.steps steps after 2 warm-up steps), its |dE|
+    against the FP64 GPU path, and its tensor-core roofline."""
+    import torch
+
+    from fricc_gb300 import _lib
+    from fricc_gb300.cholesky import split_eris
+    from fricc_gb300.friccsd import FRICCSDGPU
+    from fricc_gb300.rng import GlibcRand
+    lib = _lib.load()
+    Es = split_eris(system, device=t2.device)
+    sol = FRICCSDGPU(Es, {"m_keep": m}, rn_draw=GlibcRand(4242), precision="split")
+    a1, a2 = t1, t2
+    for _ in range(2):
+        a1, a2 = sol.update_amps(a1, a2)
+    rn = [0.3141592653589793, 0.2718281828459045]
+    sol.update_amps(a1, a2, rn=rn)
+    e_split = sol.read_energy()[0]
+    ref = FRICCSDGPU(E, {"m_keep": m}, precision="fp64")
+    ref.update_amps(a1, a2, rn=rn)
+    d_e = abs(ref.read_energy()[0] - e_split)
+    del ref
+    torch.cuda.synchronize()
+    lib.fricc_prof_enable(1)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for _ in range(args.steps):
+        a1, a2 = sol.update_amps(a1, a2)
+    ev1.record(stream)
+    torch.cuda.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    t_ms, t_n, t_fl = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
+    _lib.check(lib.fricc_prof_read_tc(ctypes.byref(t_ms), ctypes.byref(t_n), ctypes.byref(t_fl)))
+    lib.fricc_prof_enable(0)
+    sol.read_energy()
+    sus = measured_peaks().get("bf16_tflops_sustained")
+    ach = t_fl.value / (t_ms.value / 1000.0) / 1e12 if t_ms.value > 0 else None
+    return {"value": args.steps / (ms / 1000.0), "unit": "iter/s", "ms_per_step": ms / args.steps,
+            "delta_e_vs_fp64_per_step": d_e,
+            "dtype": "split-BF16x3 on tcgen05 (FP32 accumulation); FP64 compression, denominators, energy",
+            "tensor_core": {"kernel": "k_gemm_tc (all tcgen05 GEMMs of the step)", "achieved": ach, "peak": sus,
+                            "unit": "TFLOP/s", "frac": (ach / sus) if (ach and sus) else None,
+                            "share_of_step": t_ms.value / ms if ms > 0 else None, "launches": int(t_n.value)}}
+
+
 # ------------------------------------------------------------------ GPU arm
 def run_gpu(args):
     import torch
@@ -340,6 +388,19 @@ def run_gpu(args):
         e2e = {"value": world * args.steps / float(te.item()), "unit": "iter/s", "h2d_bytes_per_step": nb,
                "d2h_bytes_per_step": nb}
 
+    # the split-precision form on the same workload, as a secondary figure:
+    # integrals rebuilt from the BF16 hi+lo factor and every large
+    # contraction on the tcgen05 tensor cores (a different arithmetic, so not
+    # the headline); |dE| against the FP64 path for one step from the same
+    # state and draws
+    split_form = None
+    if args.precision == "df64" and world == 1 and not args.no_split_form:
+        try:
+            split_form = split_form_line(args, system, E, t1, t2, m, stream)
+        except Exception as ex:  # reported, never fatal to the headline
+            split_form = {"error": f"{type(ex).__name__}: {str(ex)[:300]}"}
+        torch.cuda.empty_cache()
+
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
         eris_np = host_eris_from_device(E)
@@ -399,6 +460,8 @@ def run_gpu(args):
             "clocks": clk.summary(), "energy_last": energies[-1],
             "delta_e_vs_fp64_per_step": delta_e,
         }
+        if split_form is not None:
+            line["split_form"] = split_form
         if tc_roof is not None:
             line["tensor_core_rebuild"] = tc_roof
             line["dtype"] = ("f64 (compression, denominators, energy); (vv|vv), (ov|vv), (oo|vv) split-BF16x3 on "

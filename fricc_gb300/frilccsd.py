@@ -62,6 +62,7 @@ class FRILCCSDGPU(FRICCSDGPU):
         self.rn_draw = rn_draw
         self.precision = precision
         self._df = precision == "df64"
+        self._tuner = None  # the shared sparse-term dispatcher's autotuner (not used here)
         self.lib = L.load()
         eris.prepare_linear()
         if precision == "df64":
