@@ -92,6 +92,11 @@ _MIN_TILES = 38
 _SMS = 152
 
 
+def _tiles(M: int, N: int) -> int:
+    """Output tiles of the tensor-core GEMM (128 x 64 when N <= 64, else 128 x 256)."""
+    return -(-M // 128) * -(-N // (64 if N <= 64 else 256))
+
+
 def _ksplit(tiles: int, kp: int) -> int:
     """1, a K split for few tiles and a long K, or 0 (use the FP32-pair GEMM)."""
     if tiles >= _MIN_TILES:
@@ -138,7 +143,9 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
         return D.gemm_df(A, B, C, alpha, beta)
     Mf = M * (batch if a_b else 1)
     Nf = N * (batch if b_b else 1)
-    ks = _ksplit(-(-Mf // 128) * -(-Nf // 256), _kp(K)) if K > 0 else 0
+    # a narrow side goes to N (64-wide tiles): C^T = B^T A^T when M is small
+    swap = Mf <= 64 < Nf
+    ks = _ksplit(_tiles(Nf, Mf) if swap else _tiles(Mf, Nf), _kp(K)) if K > 0 else 0
     if ks == 0:
         return D.gemm_df(A, B, C, alpha, beta)
     # rows of A' are (b, m) or m; rows of B' are (b, n) or n; both K-major
@@ -163,6 +170,9 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
         Bp = _split_view(B, N, K, N, 0, sB[1], sB[0], False, True)
         ni, sco, sci = N, 0, sC[1]
     kp = Ap.shape[1]
+    if swap:  # the operands' split patterns are complementary, so either may sit in the A slot
+        Ap, Bp, Mf, Nf = Bp, Ap, Nf, Mf
+        mi, sro, sri, ni, sco, sci = ni, sco, sci, mi, sro, sri
     L.check(L.load().fricc_gemm_bf16_tn_strided(_p(Ap), kp, _p(Bp), kp, Mf, Nf, kp, _p(C), mi, ni, sro, sri, sco,
                                                 sci, float(alpha), float(beta), ks,
                                                 _p(status) if status is not None else None, _st()))
@@ -173,7 +183,7 @@ def dense_spmm_ok(dims, pa, pb, ka, kb, QS: int) -> bool:
     """Whether ``dense_spmm`` takes this term (enough tiles, or a K long
     enough to split)."""
     nP, R = dims[pa] * dims[pb], dims[ka] * dims[kb]
-    return _ksplit(-(-nP // 128) * -(-QS // 256), _kp(R)) > 0
+    return _ksplit(_tiles(nP, QS), _kp(R)) > 0
 
 
 def dense_spmm(T, dims, pa, pb, ka, kb, coef, Bt: torch.Tensor, QS: int, Op: torch.Tensor,
@@ -186,7 +196,7 @@ def dense_spmm(T, dims, pa, pb, ka, kb, coef, Bt: torch.Tensor, QS: int, Op: tor
     nP, R = dims[pa] * dims[pb], dims[ka] * dims[kb]
     kp = _kp(R)
     assert Bt.shape == (QS, kp) and Op.is_contiguous() and Op.numel() == nP * QS
-    ks = _ksplit(-(-nP // 128) * -(-QS // 256), kp)
+    ks = _ksplit(_tiles(nP, QS), kp)
     if ks == 0:
         return False
     Ap = torch.empty(nP, kp, dtype=torch.bfloat16, device=Op.device)

@@ -34,18 +34,29 @@
 
 namespace tc {
 
-constexpr int BM = 128, BN = 256, BK = 64, STAGES = 4;
+constexpr int BM = 128, BK = 64;
 constexpr int A_BYTES = BM * BK * 2;  // 16 KB
-constexpr int B_BYTES = BN * BK * 2;  // 32 KB
-constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024;  // + alignment slack
 constexpr int EPI_WARPS = 4;
 constexpr int NT = 32 * (2 + EPI_WARPS);  // producer warp, MMA warp, epilogue warps
 
+// Tile width BN (the MMA's N: 256 for wide outputs, 64 for outputs as
+// narrow as nocc, whose 256-wide tiles would be mostly padding), with the
+// stage count that fills ~192 KB of shared memory.
 // Instruction descriptor (kind::f16): D = F32 (bits 4-5 = 1), A = B = BF16
 // (bits 7-9, 10-12 = 1), both K-major (bits 15, 16 = 0), N >> 3 at bits
 // 17-22, M >> 4 at bits 24-28.
-constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN >> 3) << 17) |
-                           ((uint32_t)(BM >> 4) << 24);
+template <int BN_>
+struct Tile {
+  static constexpr int BN = BN_;
+  static constexpr int STAGES = BN_ >= 256 ? 4 : 8;
+  static constexpr int B_BYTES = BN_ * BK * 2;
+  static constexpr int SMEM_BYTES = STAGES * (A_BYTES + B_BYTES) + 1024;  // + alignment slack
+  static constexpr uint32_t TMEM_COLS = 2 * BN_;                          // two accumulators, a power of 2
+  static constexpr uint32_t IDESC = (1u << 4) | (1u << 7) | (1u << 10) | ((uint32_t)(BN_ >> 3) << 17) |
+                                    ((uint32_t)(BM >> 4) << 24);
+  static_assert(BN_ % 16 == 0 && BN_ >= 16 && BN_ <= 256, "MMA N for M = 128");
+  static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
+};
 
 // Shared-memory matrix descriptor of a K-major operand tile written by TMA
 // with the 128-byte swizzle: rows of 128 bytes, 8-row atoms 1024 bytes apart
@@ -307,10 +318,12 @@ struct EpiVvvvSplitB {
   }
 };
 
-template <class Epi>
+template <class TC, class Epi>
 __global__ void __launch_bounds__(NT, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb, int K, int tiles_m,
               int tiles_n, int ksplit, Epi epi, unsigned* err) {
+  constexpr int BN = TC::BN, STAGES = TC::STAGES, B_BYTES = TC::B_BYTES;
+  constexpr uint32_t IDESC = TC::IDESC;
   extern __shared__ uint8_t dsm[];
   __shared__ __align__(8) uint64_t full[STAGES], empty[STAGES], tfull[2], tempty[2];
   __shared__ uint32_t tbase;
@@ -339,7 +352,7 @@ __global__ void __launch_bounds__(NT, 1)
   }
   if (warp == 1) {
     asm volatile("tcgen05.alloc.cta_group::1.sync.aligned.shared::cta.b32 [%0], %1;" ::"r"(smem_u32(&tbase)),
-                 "r"((uint32_t)(2 * BN))
+                 "r"(TC::TMEM_COLS)
                  : "memory");
     asm volatile("tcgen05.relinquish_alloc_permit.cta_group::1.sync.aligned;" ::: "memory");
   }
@@ -444,7 +457,7 @@ __global__ void __launch_bounds__(NT, 1)
   __syncthreads();
   tc_fence_after();
   if (warp == 1)
-    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"((uint32_t)(2 * BN))
+    asm volatile("tcgen05.dealloc.cta_group::1.sync.aligned.b32 %0, %1;" ::"r"(tmem), "r"(TC::TMEM_COLS)
                  : "memory");
 }
 
@@ -582,9 +595,10 @@ int sm_count(int* out) {
   return FRICC_OK;
 }
 
-template <class Epi>
-int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K, const Epi& epi,
-           cudaStream_t st, unsigned* status = nullptr, int ksplit = 1) {
+template <class TC, class Epi>
+int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K,
+                const Epi& epi, cudaStream_t st, unsigned* status, int ksplit) {
+  constexpr int BN = TC::BN, SMEM_BYTES = TC::SMEM_BYTES;
   if (!A || !B || M <= 0 || N <= 0 || K <= 0 || lda < K || ldb < K || (lda % 8) || (ldb % 8) ||
       (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16)) {
     fricc_set_error("gemm_tc: bad arguments (K-major BF16 operands: 16-byte aligned, ld >= K, ld %% 8 == 0)");
@@ -602,7 +616,7 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
   static bool attr = false;  // per instantiation
   cudaError_t e = cudaSuccess;
   if (!attr) {
-    e = cudaFuncSetAttribute(k_gemm_tc<Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
+    e = cudaFuncSetAttribute(k_gemm_tc<TC, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return fricc_cuda_fail(e, "gemm_tc attribute", __FILE__, __LINE__);
     attr = true;
   }
@@ -621,7 +635,7 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
   const bool prof = fricc_prof_on();
   if (status) {
     if (prof) fricc_prof_record(st, true, 0.0, 1);
-    k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, status);
+    k_gemm_tc<TC, Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, status);
     if (prof) fricc_prof_record(st, false, 2.0 * (double)M * (double)N * (double)K, 1);
     fricc_note_launch();
     e = cudaGetLastError();
@@ -633,7 +647,7 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
   e = cudaMemsetAsync(err, 0, sizeof(unsigned), st);
   if (e == cudaSuccess) {
     if (prof) fricc_prof_record(st, true, 0.0, 1);
-    k_gemm_tc<Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, err);
+    k_gemm_tc<TC, Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, err);
     if (prof) fricc_prof_record(st, false, 2.0 * (double)M * (double)N * (double)K, 1);
     fricc_note_launch();
     e = cudaGetLastError();
@@ -648,6 +662,14 @@ int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, in
     return FRICC_ERR_TIMEOUT;
   }
   return FRICC_OK;
+}
+
+// tile width by the output's N: 64 when N <= 64 (nocc-wide outputs), else 256
+template <class Epi>
+int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K, const Epi& epi,
+           cudaStream_t st, unsigned* status = nullptr, int ksplit = 1) {
+  if (N <= 64) return launch_tile<Tile<64>>(A, lda, B, ldb, M, N, K, epi, st, status, ksplit);
+  return launch_tile<Tile<256>>(A, lda, B, ldb, M, N, K, epi, st, status, ksplit);
 }
 
 }  // namespace tc

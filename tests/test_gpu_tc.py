@@ -19,7 +19,7 @@ def _ints(shape, lo, hi, seed):
     return torch.randint(lo, hi + 1, shape, generator=g).to(torch.bfloat16).cuda()
 
 
-@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (300, 520, 200), (2100, 300, 72), (77, 19, 8)])
+@pytest.mark.parametrize("M,N,K", [(128, 256, 64), (300, 520, 200), (2100, 300, 72), (77, 19, 8), (2100, 64, 200), (300, 33, 1000)])
 def test_gemm_integer_exact(gpulib, M, N, K):
     from fricc_gb300.cholesky import gemm_bf16_tn
     A = _ints((M, K), -8, 8, 1)
@@ -90,7 +90,8 @@ def _bound_ok(C, ref, scale, tol=2.0 ** -14):
     return bool(((C - ref).abs() <= tol * scale + 1e-300).all())
 
 
-@pytest.mark.parametrize("case", ["2d", "2d_transposed", "a_shared", "b_shared", "beta", "splitk", "fallback_small"])
+@pytest.mark.parametrize("case", ["2d", "2d_transposed", "a_shared", "b_shared", "beta", "splitk", "narrow_n",
+                                  "narrow_m", "fallback_small"])
 def test_gemm_tc_contract(gpulib, case):
     """gemm_tc follows gemm_df's contract (strided, batched with a shared
     operand, alpha/beta) within the split-BF16x3 error."""
@@ -117,6 +118,13 @@ def test_gemm_tc_contract(gpulib, case):
         A, B = r(6000, 40), r(40, 200)
         C = r(6000, 200)
         alpha, beta = -1.0, 1.0
+    elif case == "narrow_n":   # N = nocc: 64-wide tiles (the [o v v, v] x t1^T GEMMs)
+        A, B = r(30 * 150 * 150 // 10, 150), r(150, 30)
+        C = torch.empty(A.shape[0], 30, dtype=torch.float64, device="cuda")
+    elif case == "narrow_m":   # M = nocc: operands swapped so the narrow side is N
+        A, B = r(30, 3000), r(3000, 7000)
+        C = r(30, 7000)
+        alpha, beta = 1.0, -1.0
     elif case == "splitk":     # one output tile, long K: split K, ordered reduction
         A, B = r(30, 20000), r(20000, 150)
         C = r(30, 150)
