@@ -34,6 +34,8 @@ SIGNATURES = [
     ("fricc_sp_recompress_pivotal", ctypes.c_int, [_vp, _dp, _u32p, _vp, _i64p]),
     ("fricc_sp_status", ctypes.c_int, [_vp]),
     ("fricc_sp_recompress_dev", ctypes.c_int, [_vp, _dp, ctypes.c_int, ctypes.c_int, _dp, _vp]),
+    ("fricc_sp_recompress_pair", ctypes.c_int, [_vp, _vp, _dp, ctypes.c_double, ctypes.c_double, _vp]),
+    ("fricc_sp_recompress_pair_dev", ctypes.c_int, [_vp, _vp, _dp, _dp, _vp]),
     ("fricc_sp_create_empty", ctypes.c_int, [_i64p, _i64, _vp, ctypes.POINTER(_vp)]),
     ("fricc_sp_destroy", ctypes.c_int, [_vp]),
     ("fricc_sp_info", ctypes.c_int, [_vp, _i64p, _i64p, _i64p]),

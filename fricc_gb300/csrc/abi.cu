@@ -11,7 +11,8 @@
 
 int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, double rn, cudaStream_t st, int64_t* flat,
                           double* vals, int64_t* n_largest, unsigned* glibc_hist, int64_t* n_draws,
-                          unsigned long long* meta = nullptr, const double* rn_dev = nullptr);
+                          unsigned long long* meta = nullptr, const double* rn_dev = nullptr,
+                          const CompressPairOut* pair = nullptr);
 int fricc_unpack_async(const int64_t* flat, int64_t m, const int64_t dims[4], int* slots, unsigned long long* meta,
                        cudaStream_t st);
 int fricc_dev_status(unsigned e);
@@ -249,6 +250,54 @@ static int recompress(fricc_sparse* T, const double* t2, int mode, double rn, un
   if (!rc) rc = fricc_unpack_async(T->flat, T->m, T->dims, T->slots, T->meta, st);
   if (!rc) T->pending = true;
   return rc;
+}
+
+// Both handles from the same tensor with draws rn_a, rn_b (host values, or the
+// two doubles at rn_dev): the shared phases run once and one sampling chain
+// serves both (systematic FRI only; the handles must have t2's dims and
+// equal m).  Stream-ordered like recompress.
+static int recompress_pair(fricc_sparse* A, fricc_sparse* B, const double* t2, double rn_a, double rn_b,
+                           const double* rn_dev, void* stream) {
+  if (!A || !B || !t2 || A == B || A->m != B->m) {
+    fricc_set_error("sp_recompress_pair: two distinct handles with the same m");
+    return FRICC_ERR_ARG;
+  }
+  for (int k = 0; k < 4; ++k)
+    if (A->dims[k] != B->dims[k]) {
+      fricc_set_error("sp_recompress_pair: the handles' dims differ");
+      return FRICC_ERR_ARG;
+    }
+  cudaStream_t st = as_stream(stream);
+  stale_bucketings(A);
+  stale_bucketings(B);
+  const int64_t n = A->dims[0] * A->dims[1] * A->dims[2] * A->dims[3];
+  for (fricc_sparse* T : {A, B}) {
+    T->owner_stream = st;
+    T->pending = false;
+    T->status = FRICC_OK;
+    FRICC_CUDA(cudaMemsetAsync(T->meta, 0, 2 * sizeof(unsigned long long), st));
+  }
+  const CompressPairOut pb{B->flat, B->vals, B->meta, rn_b, rn_dev ? rn_dev + 1 : nullptr};
+  int rc = fricc_compress_device(t2, n, A->m, 0, rn_a, st, A->flat, A->vals, nullptr, nullptr, nullptr, A->meta,
+                                 rn_dev, &pb);
+  if (!rc) rc = fricc_unpack_async(A->flat, A->m, A->dims, A->slots, A->meta, st);
+  if (!rc) rc = fricc_unpack_async(B->flat, B->m, B->dims, B->slots, B->meta, st);
+  if (!rc) A->pending = B->pending = true;
+  return rc;
+}
+
+int fricc_sp_recompress_pair(fricc_sparse* A, fricc_sparse* B, const double* t2, double rn_a, double rn_b,
+                             void* stream) {
+  return recompress_pair(A, B, t2, rn_a, rn_b, nullptr, stream);
+}
+
+int fricc_sp_recompress_pair_dev(fricc_sparse* A, fricc_sparse* B, const double* t2, const double* rn_dev,
+                                 void* stream) {
+  if (!rn_dev) {
+    fricc_set_error("sp_recompress_pair_dev: null draws");
+    return FRICC_ERR_ARG;
+  }
+  return recompress_pair(A, B, t2, 0.0, 0.0, rn_dev, stream);
 }
 
 int fricc_sp_status(const fricc_sparse* T) {

@@ -74,6 +74,16 @@ __device__ __forceinline__ double f2d_bits(float f) {
 // hi + lo of a float pair, rounded once to FP64
 __device__ __forceinline__ double pair_to_f64(float hi, float lo) { return f2d_bits(hi) + f2d_bits(lo); }
 
+// The second output of a paired systematic compression: the same tensor
+// compressed with another draw (host value rn, or the double at rn_dev).
+struct CompressPairOut {
+  int64_t* flat;
+  double* vals;
+  unsigned long long* meta;
+  double rn;
+  const double* rn_dev;
+};
+
 void fricc_set_error(const char* fmt, ...);
 int fricc_cuda_fail(cudaError_t e, const char* what, const char* file, int line);
 int fricc_cuda_check(cudaError_t e, const char* what);  // FRICC_OK on success

@@ -224,6 +224,17 @@ struct ConsSample {
   }
 };
 
+// Two systematic samplers over one chain: the two compressions of the same
+// tensor an iteration makes (different draws) share every phase up to the
+// probabilities, and the partial sums too.
+struct ConsSample2 {
+  ConsSample a, b;
+  __device__ __forceinline__ void operator()(int64_t j, double lo, double hi, double p) const {
+    a(j, lo, hi, p);
+    b(j, lo, hi, p);
+  }
+};
+
 // The select digit: the largest d with count(digit >= d) >= m (one thread).
 __global__ void k_select_digit(const unsigned* __restrict__ hist, int64_t m, Ctl* c) {
   int64_t cum = 0;
@@ -870,7 +881,11 @@ static int pivotal(const double* x, int64_t n, int64_t m, const GenP& gp, Ctl* c
 // in stream order, so a caller that passes n_largest == nullptr never waits.
 int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, double rn, cudaStream_t st,
                           int64_t* flat, double* vals, int64_t* n_largest, unsigned* glibc_hist, int64_t* n_draws,
-                          unsigned long long* meta, const double* rn_dev) {
+                          unsigned long long* meta, const double* rn_dev, const CompressPairOut* pair) {
+  if (pair && (mode != 0 || !meta || !pair->flat || !pair->vals || !pair->meta)) {
+    fricc_set_error("compress: a paired compression is systematic FRI with status blocks");
+    return FRICC_ERR_ARG;
+  }
   if (n < 0 || m <= 0 || m > n) {
     fricc_set_error("Bad m_keep value: need 0 < m <= tensor size (m=%lld, size=%lld)", (long long)m,
                     (long long)n);
@@ -882,6 +897,8 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
   }
   CompressScratch s;
   Ctl* ctl = nullptr;
+  Ctl* ctl2 = nullptr;  // a paired compression's second state
+  unsigned* S2 = nullptr;
   int rc = FRICC_OK;
 #define TRY(x)                  \
   do {                          \
@@ -962,6 +979,17 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     if (rc) goto done;
     k_finish_d<<<1, 1, 0, st>>>(s.ffail, s.Rb, s.ckey, s.cidx, m, ctl);
     fricc_note_launch();
+    if (pair) {  // the second compression: the same state, its own draw
+      TRY(fricc_alloc_t(&ctl2, 1, st));
+      TRY(fricc_cuda_check(cudaMemcpyAsync(ctl2, ctl, sizeof(Ctl), cudaMemcpyDeviceToDevice, st), "ctl"));
+      if (pair->rn_dev) {
+        TRY(fricc_cuda_check(cudaMemcpyAsync(&ctl2->rn, pair->rn_dev, sizeof(double), cudaMemcpyDeviceToDevice, st),
+                             "rn"));
+      } else {
+        const double rn_h = pair->rn;
+        TRY(fricc_cuda_check(cudaMemcpyAsync(&ctl2->rn, &rn_h, sizeof(double), cudaMemcpyHostToDevice, st), "rn"));
+      }
+    }
 
     GenP gp{x, ctl};
     if (mode == 2) {
@@ -995,7 +1023,15 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     // samples keep index 0, as in the reference
     const GenPv gpv{s.P, x, ctl};
     ConsSample cs{ctl, s.S};
-    TRY((exact::run_chain<GenPv, ConsSample, false, true>(gpv, n, s.dzero, false, cs, s.chain, s.err, st)));
+    if (pair) {
+      TRY(fricc_alloc_t(&S2, m, st));
+      k_zero_u32<<<grid_for(m, 256), 256, 0, st>>>(S2, m);
+      fricc_note_launch();
+      ConsSample2 cs2{cs, ConsSample{ctl2, S2}};
+      TRY((exact::run_chain<GenPv, ConsSample2, false, true>(gpv, n, s.dzero, false, cs2, s.chain, s.err, st)));
+    } else {
+      TRY((exact::run_chain<GenPv, ConsSample, false, true>(gpv, n, s.dzero, false, cs, s.chain, s.err, st)));
+    }
 
     // 6. output
     k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, ctl, flat, vals);
@@ -1004,6 +1040,13 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     if (meta) {
       k_put_meta<<<1, 1, 0, st>>>(ctl, 0, s.err, meta);
       fricc_note_launch();
+    }
+    if (pair) {
+      const GenPv gpv2{s.P, x, ctl2};
+      k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, ctl2, pair->flat, pair->vals);
+      k_out_s<<<grid_for(m, 256), 256, 0, st>>>(gpv2, S2, pair->flat, pair->vals);
+      k_put_meta<<<1, 1, 0, st>>>(ctl2, 0, s.err, pair->meta);
+      fricc_note_launch(3);
     }
     TRY(fricc_cuda_check(cudaGetLastError(), "output"));
     if (n_largest) {
@@ -1020,6 +1063,8 @@ done:
 #undef TRY
   free_scratch(s, st);
   fricc_free(ctl, st);
+  fricc_free(ctl2, st);
+  fricc_free(S2, st);
   return rc;
 }
 

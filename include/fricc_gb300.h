@@ -88,6 +88,19 @@ int fricc_sp_recompress(fricc_sparse* T, const double* t2, int compression, int 
 int fricc_sp_recompress_dev(fricc_sparse* T, const double* t2, int compression, int sampling, const double* rn_dev,
                             void* stream);
 
+/* The two compressions one iteration makes of the same T2 (fricc/friccsd.py:
+ * 100-117: the T2-term and W-intermediate compressions, draws rn_a then
+ * rn_b), into handles A and B at once: the norm, the top-m select, the
+ * largest-set walk and the probabilities run once and one partial-sum chain
+ * serves both samplers.  Each handle ends bit-identical to
+ * fricc_sp_recompress(A, t2, FRI, SYSTEMATIC, rn_a) and (B, ..., rn_b).
+ * Systematic FRI only; A and B distinct, with t2's dims and equal m.  The
+ * _dev form reads the two draws from device memory (rn_dev[0], rn_dev[1]). */
+int fricc_sp_recompress_pair(fricc_sparse* A, fricc_sparse* B, const double* t2, double rn_a, double rn_b,
+                             void* stream);
+int fricc_sp_recompress_pair_dev(fricc_sparse* A, fricc_sparse* B, const double* t2, const double* rn_dev,
+                                 void* stream);
+
 /* Wait for the handle's last compression and return its status (FRICC_OK,
  * FRICC_ERR_P_GT_ONE, FRICC_ERR_TIMEOUT, FRICC_ERR_INDEX).  No reference
  * counterpart: the reference exits inside the constructor. */

@@ -130,3 +130,55 @@ def test_errors_raise(gpulib):
         py_rccsd.SparseTensor4d(x, x.shape, 0, "fri", "pivotal")
     with pytest.raises(TypeError):
         py_rccsd.SparseTensor4d(x.astype(np.float32), x.shape, 4, "fri", "systematic")
+
+
+def test_paired_recompress_bit_identical(gpulib):
+    """fricc_sp_recompress_pair gives each handle exactly what two separate
+    systematic compressions with the same draws give (o20v100: N = 4M)."""
+    import ctypes
+    import numpy as np
+    import torch
+    from fricc_gb300 import _lib as L
+    from fricc_gb300.synthetic import make_system
+    s = make_system("o20v100x64", seed=3)
+    t2 = torch.from_numpy(np.ascontiguousarray(s.mp2_amplitudes()[1])).cuda()
+    m = 200_000
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    dims = L.i64arr(t2.shape)
+
+    def make(rn):
+        h = ctypes.c_void_p()
+        L.check(gpulib.fricc_sp_create(ctypes.c_void_p(t2.data_ptr()), dims, m, 0, 0, rn, st, ctypes.byref(h)))
+        return h
+
+    def export(h):  # host arrays
+        f = np.empty(m, dtype=np.int64)
+        v = np.empty(m, dtype=np.float64)
+        L.check(gpulib.fricc_sp_export(h, f.ctypes.data_as(ctypes.c_void_p), v.ctypes.data_as(ctypes.c_void_p), st))
+        return torch.from_numpy(f), torch.from_numpy(v)
+
+    a, b, c, d = make(0.5), make(0.5), make(0.5), make(0.5)
+    L.check(gpulib.fricc_sp_recompress_pair(a, b, ctypes.c_void_p(t2.data_ptr()), 0.123, 0.877, st))
+    L.check(gpulib.fricc_sp_recompress(c, ctypes.c_void_p(t2.data_ptr()), 0, 0, 0.123, st))
+    L.check(gpulib.fricc_sp_recompress(d, ctypes.c_void_p(t2.data_ptr()), 0, 0, 0.877, st))
+    for x, y in ((a, c), (b, d)):
+        L.check(gpulib.fricc_sp_status(x))
+        fx, vx = export(x)
+        fy, vy = export(y)
+        assert torch.equal(fx, fy) and torch.equal(vx.view(torch.int64), vy.view(torch.int64))
+    fa, _ = export(a)
+    fb, _ = export(b)
+    assert not torch.equal(fa, fb)  # the draws differ
+    rn = torch.tensor([0.31, 0.62], dtype=torch.float64, device="cuda")
+    L.check(gpulib.fricc_sp_recompress_pair_dev(a, b, ctypes.c_void_p(t2.data_ptr()), ctypes.c_void_p(rn.data_ptr()),
+                                                st))
+    L.check(gpulib.fricc_sp_recompress(c, ctypes.c_void_p(t2.data_ptr()), 0, 0, 0.31, st))
+    L.check(gpulib.fricc_sp_recompress(d, ctypes.c_void_p(t2.data_ptr()), 0, 0, 0.62, st))
+    for x, y in ((a, c), (b, d)):
+        fx, vx = export(x)
+        fy, vy = export(y)
+        assert torch.equal(fx, fy) and torch.equal(vx.view(torch.int64), vy.view(torch.int64))
+    for h in (a, b, c, d):
+        gpulib.fricc_sp_destroy(h)
+    with pytest.raises(ValueError):
+        L.check(gpulib.fricc_sp_recompress_pair(a, a, ctypes.c_void_p(t2.data_ptr()), 0.1, 0.2, st))
