@@ -97,14 +97,31 @@ def _tiles(M: int, N: int) -> int:
     return -(-M // 128) * -(-N // (64 if N <= 64 else 256))
 
 
+def _wave_eff(units: int) -> float:
+    """Busy fraction of the SMs over the rounds a persistent launch of
+    ``units`` work units takes (one unit per SM at a time)."""
+    return units / (-(-units // _SMS) * _SMS)
+
+
 def _ksplit(tiles: int, kp: int) -> int:
-    """1, a K split for few tiles and a long K, or 0 (use the FP32-pair GEMM)."""
-    if tiles >= _MIN_TILES:
-        return 1
+    """The K split for a GEMM of ``tiles`` output tiles and K' = kp: none
+    from two rounds of tiles up; below that the smallest split that fills
+    the SMs' rounds to 90% (each slice at least 8 K blocks; a split must
+    gain 5 points of occupancy to be taken); 0 (use the FP32-pair GEMM)
+    when there are few tiles and K is short."""
     nk = -(-kp // 64)
-    if nk < 16:
+    if tiles < _MIN_TILES and nk < 16:
         return 0
-    return max(2, min(nk // 4, -(-_SMS // tiles)))
+    if tiles >= 2 * _SMS:  # two or more rounds already: a split's partials cost more than the tail
+        return 1
+    best, best_eff = 1, (_wave_eff(tiles) if tiles >= _MIN_TILES else 0.0)
+    for ks in (2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 152):
+        if best_eff >= 0.9 or nk // ks < 8:
+            break
+        e = _wave_eff(tiles * ks)
+        if e > best_eff + 0.05:
+            best, best_eff = ks, e
+    return best
 
 
 def split_a(A: torch.Tensor) -> torch.Tensor:

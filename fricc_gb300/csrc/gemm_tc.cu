@@ -13,11 +13,12 @@
 //                        barrier, and at the end of a tile to the
 //                        accumulator's "full" barrier (warp 1 also allocates
 //                        and frees the 512 TMEM columns);
-//   warps 2-5         -- epilogue: tcgen05.ld of their 32 TMEM lanes (one
-//                        output row per thread, 16 columns per load) into the
-//                        epilogue functor, then an arrive on the
-//                        accumulator's "empty" barrier -- overlapping the
-//                        MMAs of the next tile in the other accumulator.
+//   warps 2-9         -- epilogue: tcgen05.ld of their 32 TMEM lanes (one
+//                        output row per thread, 16 columns per load; two
+//                        warps per lane quadrant, each with half the
+//                        columns) into the epilogue functor, then an arrive
+//                        on the accumulator's "empty" barrier -- overlapping
+//                        the MMAs of the next tile in the other accumulator.
 // Every mbarrier wait is bounded (2 s of global time); a wait that gives up
 // sets a device error word, the roles stop issuing, the producer waits
 // (bounded) for its copies in flight, and the CTA frees its TMEM and exits.
@@ -36,7 +37,7 @@ namespace tc {
 
 constexpr int BM = 128, BK = 64;
 constexpr int A_BYTES = BM * BK * 2;  // 16 KB
-constexpr int EPI_WARPS = 4;
+constexpr int EPI_WARPS = 8;  // two per TMEM lane quadrant, each draining half the columns
 constexpr int NT = 32 * (2 + EPI_WARPS);  // producer warp, MMA warp, epilogue warps
 
 // Tile width BN (the MMA's N: 256 for wide outputs, 64 for outputs as
@@ -421,8 +422,9 @@ __global__ void __launch_bounds__(NT, 1)
         if (*(volatile int*)&failed) break;
       }
     }
-  } else {  // epilogue warps 2..5: TMEM lanes 32 (warp % 4) ...
+  } else {  // epilogue warps 2..9: TMEM lanes 32 (warp % 4) ..., column half (warp - 2) / 4
     const int quad = warp & 3;
+    const int half = (warp - 2) >> 2;
     int i = 0;
     for (int w = blockIdx.x; w < nunits; w += gridDim.x, ++i) {
       const int b = i & 1;
@@ -442,7 +444,7 @@ __global__ void __launch_bounds__(NT, 1)
       const int64_t row = (int64_t)mt * BM + quad * 32 + lane;
       const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * BN);
 #pragma unroll 1
-      for (int c = 0; c < BN / 16; ++c) {
+      for (int c = half * (BN / 32); c < (half + 1) * (BN / 32); ++c) {
         float v[16];
         tc_ld16(lane_base + (uint32_t)(c * 16), v);
         epi(row, (int64_t)nt * BN + c * 16, v, w / ntiles);
