@@ -2,17 +2,19 @@
 // split-BF16x3 rebuild of integral blocks from a Cholesky factor.
 //
 // C[M][N] = A[M][K] B[N][K]^T, A and B BF16 and K-major, FP32 accumulation in
-// tensor memory (TMEM).  A persistent kernel: one CTA per SM walks 128 x 256
-// output tiles, with warp-specialised roles:
-//   warp 0, one lane  -- TMA producer: 128 x 64 and 256 x 64 operand boxes
-//                        (128-byte swizzle) into a 4-stage shared-memory ring,
-//                        each stage guarded by a "full" and an "empty" mbarrier;
-//   warp 1, one lane  -- MMA issuer: four tcgen05.mma (M=128, N=256, K=16) per
-//                        stage into one of two TMEM accumulators of 256
+// tensor memory (TMEM).  A persistent kernel: one CTA per SM walks 128 x BN
+// output tiles (BN = 256, or 64 for outputs as narrow as nocc), or split-K
+// slices of them, with warp-specialised roles:
+//   warp 0, one lane  -- TMA producer: 128 x 64 and BN x 64 operand boxes
+//                        (128-byte swizzle) into a 4-stage (BN = 256) or
+//                        8-stage (BN = 64) shared-memory ring, each stage
+//                        guarded by a "full" and an "empty" mbarrier;
+//   warp 1, one lane  -- MMA issuer: four tcgen05.mma (M=128, N=BN, K=16) per
+//                        stage into one of two TMEM accumulators of BN
 //                        columns, tcgen05.commit to the stage's "empty"
 //                        barrier, and at the end of a tile to the
 //                        accumulator's "full" barrier (warp 1 also allocates
-//                        and frees the 512 TMEM columns);
+//                        and frees the 2 BN TMEM columns);
 //   warps 2-9         -- epilogue: tcgen05.ld of their 32 TMEM lanes (one
 //                        output row per thread, 16 columns per load; two
 //                        warps per lane quadrant, each with half the
