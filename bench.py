@@ -61,6 +61,8 @@ def parse():
     p.add_argument("--no-e2e", action="store_true")
     p.add_argument("--no-split-form", action="store_true",
                    help="skip the secondary measurement of the split-precision form")
+    p.add_argument("--graph", action="store_true",
+                   help="replay each iteration from one captured CUDA graph (after the first, eager one)")
     p.add_argument("--autotune", action="store_true",
                    help="df64: time the launch configurations of every sparse term and GEMM shape during the "
                         "warm-up and keep the fastest")
@@ -293,7 +295,7 @@ def run_gpu(args):
         from fricc_gb300.cholesky import split_eris
         Es = split_eris(system, device=dev)
     solver = FRICCSDGPU(Es if Es is not None else E, {"m_keep": m}, rn_draw=seeded_draws(1000 + rank),
-                        precision=args.precision, autotune=args.autotune)
+                        precision=args.precision, autotune=args.autotune, graph=args.graph)
     stream = torch.cuda.current_stream()
 
     for _ in range(args.warmup):
@@ -455,7 +457,8 @@ def run_gpu(args):
                        "parallelism": "replicas" if world > 1 else "single GPU",
                        "l2": f"working set > L2 ((ac|bd) {8 * v ** 4 / 1e9:.2f} GB and its float-pair copy "
                              "streamed by the O^2V^4 term every step)",
-                       "precision": args.precision, "autotune": bool(args.autotune)},
+                       "precision": args.precision, "autotune": bool(args.autotune),
+                       "cuda_graph": bool(args.graph)},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
             "clocks": clk.summary(), "energy_last": energies[-1],
             "delta_e_vs_fp64_per_step": delta_e,
