@@ -225,3 +225,20 @@ def test_device_system_recipe(gpulib):
     La = a.L[:, :6, 6:].abs().reshape(288, -1)
     scale = (La.T @ La).reshape(6, 30, 6, 30)
     assert float(((Es.ovov - E.ovov).abs() / scale).max()) < 1e-11
+
+
+def test_split_kernel_loop(gpulib, systems):
+    """FRICCSDGPU.kernel (the reference's loop) in the split form, against
+    the FP64 form's loop with the same draws."""
+    from fricc_gb300.batch import mp2_device
+    from fricc_gb300.friccsd import FRICCSDGPU
+    from fricc_gb300.rng import GlibcRand
+    s, E, Es = systems
+    runs = []
+    for eris, prec in ((Es, "split"), (E, "fp64")):
+        cc = FRICCSDGPU(eris, {"m_keep": 20000}, rn_draw=GlibcRand(77), precision=prec)
+        conv, e, t1, t2, energies = cc.kernel(*mp2_device(eris), max_cycle=6)
+        runs.append(np.array(energies))
+    assert len(runs[0]) == len(runs[1]) or abs(len(runs[0]) - len(runs[1])) <= 1
+    n = min(len(runs[0]), len(runs[1]))
+    assert np.max(np.abs(runs[0][:n] - runs[1][:n])) < 1e-6
