@@ -24,7 +24,7 @@ records:
                    probability vectors, with the draws each call consumed;
 * unbiased.npz  -- fricc/friccsd.py with "unbiased": True (running-average
                    W compression after burn-in), its missing iteration
-                   counter supplied by the driver.
+                   counter supplied by the loop in this script.
 
 Usage:  OMP_NUM_THREADS=1 python tests/golden/make_golden.py
 """
@@ -226,7 +226,7 @@ def parallel_sample_cases():
         out[f"c{k}_seed"] = np.int64(seed)
         out[f"c{k}_ok"] = np.int64(r.returncode == 0)
         if r.returncode == 0:
-            # the reference logs its timings on stdout first; the driver's two lines come last
+            # the reference logs its timings on stdout first; ref_parallel_sample's own two lines come last
             lines = r.stdout.split("\n")[:-1]
             S = np.array([int(t) for t in lines[-2].split()], dtype=np.int64)
             tail = [int(t) for t in lines[-1].split()]
@@ -366,7 +366,7 @@ def lccsd_cases(R):
 
 def unbiased_case(R):
     """fricc/friccsd.py with "unbiased": True.  The reference reads an
-    iteration counter cc._iter that it never defines; the driver here sets it
+    iteration counter cc._iter that it never defines; the loop here sets it
     to the number of updates already run before each call, so the
     reference's own running-average code (:108-136) runs unmodified."""
     F = load_reference_friccsd(R)
