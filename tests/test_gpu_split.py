@@ -242,3 +242,26 @@ def test_split_kernel_loop(gpulib, systems):
     assert len(runs[0]) == len(runs[1]) or abs(len(runs[0]) - len(runs[1])) <= 1
     n = min(len(runs[0]), len(runs[1]))
     assert np.max(np.abs(runs[0][:n] - runs[1][:n])) < 1e-6
+
+
+@pytest.mark.parametrize("o,v", [(5, 21), (7, 33)])
+def test_split_odd_sizes(gpulib, o, v):
+    """Odd nocc and nvir (odd row lengths everywhere, partial tiles, the
+    FP32 fallback's padded rows) in the split form, against FP64."""
+    from fricc_gb300.batch import mp2_device
+    from fricc_gb300.cholesky import split_eris
+    from fricc_gb300.friccsd import FRICCSDGPU
+    from fricc_gb300.rccsd_dense import DeviceERIs
+    from fricc_gb300.synthetic import SyntheticSystem
+    s = SyntheticSystem(o, v, 6 * (o + v), 0.05, 11)
+    E, Es = DeviceERIs.from_system(s), split_eris(s)
+    m = (o * o * v * v) // 8
+    fp = FRICCSDGPU(E, {"m_keep": m}, precision="fp64")
+    sp = FRICCSDGPU(Es, {"m_keep": m}, precision="split")
+    t1, t2 = mp2_device(E)
+    for it in range(3):
+        rn = [0.11 + 0.2 * it, 0.7]
+        a1, a2 = fp.update_amps(t1, t2, rn=rn)
+        sp.update_amps(t1, t2, rn=rn)
+        assert abs(fp.read_energy()[0] - sp.read_energy()[0]) < 1e-6
+        t1, t2 = a1, a2
