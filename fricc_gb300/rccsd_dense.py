@@ -17,6 +17,8 @@ from __future__ import annotations
 
 import math
 
+import threading
+
 import numpy as np
 import torch
 
@@ -81,6 +83,7 @@ class DeviceERIs:
         self.ovvv_kacd = ovvv.permute(0, 2, 3, 1).contiguous()           # Wvovo t1 term
         self._dense_wvvvv = None
         self._splits = {}
+        self._lock = threading.Lock()
 
     SPLIT_BLOCKS = ("vvvvT", "ovvv_XY", "ovov", "ovov_0312", "ovov_0313_0113", "ovov_cdkl")
 
@@ -134,13 +137,20 @@ class DeviceERIs:
     def tc_w(self, name, qs):
         """The split W^T ([hi|lo|hi], rows q) of a constant W' block viewed as
         [rows][qs]: the B operand of the split-precision dense sparse terms.
-        Built on first use (the first, eager iteration)."""
+        Built on first use (the first, eager iteration) under a lock and
+        waited for, so solvers on other threads and streams never read a
+        block whose split is still in flight."""
         from .cholesky import split_b
         key = ("tcW", name, qs)
-        if key not in self._splits:
-            x = getattr(self, name)
-            self._splits[key] = split_b(x.reshape(-1, qs))
-        return self._splits[key]
+        got = self._splits.get(key)
+        if got is None:
+            with self._lock:
+                got = self._splits.get(key)
+                if got is None:
+                    got = split_b(getattr(self, name).reshape(-1, qs))
+                    torch.cuda.current_stream().synchronize()
+                    self._splits[key] = got
+        return got
 
     def tc(self, name, role):
         got = self._splits.get(("tc", name))
