@@ -76,6 +76,7 @@ SIGNATURES = [
     ("fricc_stream_destroy", ctypes.c_int, [_vp]),
     ("fricc_launch_count", ctypes.c_longlong, []),
     ("fricc_tune_set", ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
+    ("fricc_symadd", ctypes.c_int, [_dp, _dp, _i64, _i64, _i64p, ctypes.c_double, _vp]),
     ("fricc_prof_enable", None, [ctypes.c_int]),
     ("fricc_prof_read", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                                        ctypes.POINTER(ctypes.c_double)]),

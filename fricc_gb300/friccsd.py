@@ -442,12 +442,11 @@ class FRICCSDGPU:
         R = torch.empty(o * v * v, o, dtype=f64, device=dev)   # R[(i,a,b), j] = sum_c (ia|cb) t_jc
         mm(E.ovvv_iabc.view(o * v * v, v), t1.T, R, 1.0, 0.0, const="ovvv_iabc")
         tmp = R.view(o, v, v, o).permute(0, 3, 1, 2) - ein2("ka,kibj->ijab", t1, Y1)
-        t2new = tmp + tmp.permute(1, 0, 3, 2)
+        t2new = E.ovov.permute(0, 2, 1, 3).contiguous()
+        D.sym_add(t2new, tmp, 1.0)
         tmp2 = ein2("kcai,jc->akij", E.ovvo, t1) + E.ovoo.permute(1, 3, 0, 2)
         tmp = ein2("akij,kb->ijab", tmp2, t1)
-        t2new -= tmp + tmp.permute(1, 0, 3, 2)
-        t2new += E.ovov.permute(0, 2, 1, 3)
-        t2new = t2new.contiguous()
+        D.sym_add(t2new, tmp, -1.0)
 
         Loo = D.Loo(t1, t2, E, Foo=Foo0)
         Lvv = Fvv0 - t1.T @ fov + X.T                      # Lvv with its ovvv part from X
@@ -546,9 +545,9 @@ class FRICCSDGPU:
 
         tmpL = torch.empty_like(t2)
         mm(Lvv.unsqueeze(0).expand(o * o, v, v), t2.view(o * o, v, v), tmpL.view(o * o, v, v), 1.0, 0.0)
-        t2new += _sym(tmpL)                                 # Lvv t2, :238-239
+        D.sym_add(t2new, tmpL, 1.0)                         # Lvv t2, :238-239
         mm(Loo.T, t2.view(o, o * v * v), tmpL.view(o, o * v * v), 1.0, 0.0)
-        t2new -= _sym(tmpL)                                 # Loo t2, :240-241
+        D.sym_add(t2new, tmpL, -1.0)                        # Loo t2, :240-241
         del tmpL
 
         if "O^3V^3" in comp:
@@ -556,13 +555,13 @@ class FRICCSDGPU:
             WB = Wvovo.permute(1, 2, 3, 0).contiguous()      # [k,c,i,a] = Wvovo(a,k,c,i)
             tmp = torch.zeros(o, v, o, v, dtype=t2.dtype, device=t2.device)   # [j,b,i,a]
             self._spmm(T, 1, 3, 0, 2, 1.0, 2.0 * WA - WB, ov, tmp, st)        # 1302 + 1202
-            t2new += _sym(tmp.permute(2, 0, 3, 1))
+            D.sym_add(t2new, tmp.permute(2, 0, 3, 1), 1.0)
             tmp.zero_()
             self._spmm(T, 1, 2, 0, 3, 1.0, WA, ov, tmp, st)                   # 1303, [j,b,i,a]
-            t2new -= _sym(tmp.permute(2, 0, 3, 1))
+            D.sym_add(t2new, tmp.permute(2, 0, 3, 1), -1.0)
             tmp.zero_()
             self._spmm(T, 1, 2, 0, 3, 1.0, WB, ov, tmp, st)                   # 1203, [j,a,i,b]
-            t2new -= _sym(tmp.permute(2, 0, 1, 3))
+            D.sym_add(t2new, tmp.permute(2, 0, 1, 3), -1.0)
         else:
             tmp = 2 * ein("akic,kjcb->ijab", Wvoov, t2) - ein("akci,kjcb->ijab", Wvovo, t2)
             t2new += _sym(tmp)

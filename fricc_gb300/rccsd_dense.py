@@ -215,6 +215,23 @@ class DeviceERIs:
         return out
 
 
+def sym_add(out: torch.Tensor, X: torch.Tensor, coef: float = 1.0) -> torch.Tensor:
+    """out += coef * (X + X.permute(1, 0, 3, 2)) in one fused pass (the
+    symmetrised T2 residual terms); out contiguous [o,o,v,v] FP64 on the
+    device, X any [o,o,v,v] FP64 view not overlapping out."""
+    import ctypes
+
+    from . import _lib as L
+    o, v = out.shape[0], out.shape[2]
+    if (not out.is_contiguous() or out.dtype != torch.float64 or X.dtype != torch.float64
+            or tuple(X.shape) != tuple(out.shape) or out.shape != (o, o, v, v)):
+        raise ValueError("sym_add: out contiguous [o,o,v,v] float64 and X a float64 view of the same shape")
+    L.check(L.load().fricc_symadd(ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(X.data_ptr()), o, v,
+                                  L.i64arr(X.stride()), float(coef),
+                                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return out
+
+
 def _dev_tensor(a, dev):
     """FP64 copy of a numpy array, or the tensor itself moved to ``dev``."""
     t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))

@@ -276,6 +276,14 @@ int fricc_energy_update_lin(const double* t1num, const double* t2num, const doub
                             const double* ovov, const double* t1old, const double* t2old, int64_t nocc,
                             int64_t nvir, double* t1out, double* t2out, double* res, void* stream);
 
+/* out[i,j,a,b] += coef * (X[i,j,a,b] + X[j,i,b,a]) in one pass: the
+ * symmetrised additions of the T2 residual (fricc/friccsd.py:245-267,
+ * "tmp + tmp.transpose(1,0,3,2)").  out: contiguous [nocc][nocc][nvir][nvir];
+ * X: any [nocc][nocc][nvir][nvir] view given by its element strides, not
+ * overlapping out.  Stream-ordered. */
+int fricc_symadd(double* out, const double* X, int64_t nocc, int64_t nvir, const int64_t strides[4], double coef,
+                 void* stream);
+
 /* Split-precision integral rebuilds on the tcgen05 tensor cores (the
  * reference builds its dense integral blocks in FP64 through PySCF,
  * fricc/friccsd.py:325-331 for Wvvvv; the split-BF16x3 rebuild from a

@@ -169,3 +169,23 @@ def test_split_f2_bits_bound_and_edges(gpulib):
             assert h == want_hi[k] and (l == want_lo[k] or (np.isnan(l) and np.isnan(want_lo[k]))), (v, h, l)
         else:
             assert abs(h + l - v) <= 2.0**-47 * abs(v), v
+
+
+@pytest.mark.parametrize("perm", [(0, 1, 2, 3), (2, 0, 3, 1), (2, 0, 1, 3), (1, 0, 2, 3)])
+@pytest.mark.parametrize("o,v", [(4, 37), (6, 64)])
+def test_sym_add_matches_torch(gpulib, perm, o, v):
+    """out += c (X + X^T(0,1,3,2)) in one pass, for the strided views the
+    iteration passes (and odd nvir: partial 32 x 32 tiles)."""
+    import torch
+    from fricc_gb300.rccsd_dense import sym_add
+    g = torch.Generator().manual_seed(9)
+    # base laid out so that base.permute(perm) has shape (o, o, v, v)
+    shape = [0, 0, 0, 0]
+    for k, p in enumerate(perm):
+        shape[p] = (o, o, v, v)[k]
+    base = torch.randn(*shape, generator=g, dtype=torch.float64).cuda()
+    X = base.permute(*perm)
+    out = torch.randn(o, o, v, v, generator=g, dtype=torch.float64).cuda()
+    ref = out + -0.5 * (X + X.permute(1, 0, 3, 2))
+    sym_add(out, X, -0.5)
+    torch.testing.assert_close(out, ref, rtol=0, atol=0)
