@@ -305,8 +305,8 @@ def split_eris(system, device="cuda"):
     tensor cores (split-BF16x3, FP32 accumulation, widened to FP64 for the
     dense algebra), the (vv|vv) block never stored in FP64 but rebuilt by
     ``VvvvRebuild`` for the O^2V^4 contraction; the small blocks (oo|oo),
-    (ov|oo), (ov|ov), (ov|vo) from the FP64 factor on the FP32-pair GEMM
-    (~2^-40), sum_cd (ac|bd) in FP64."""
+    (ov|oo), (ov|ov) from the FP64 factor on the FP32-pair GEMM (~2^-40),
+    (ov|vo) = (ov|ov) permuted (L is symmetric), sum_cd (ac|bd) in FP64."""
     from .rccsd_dense import DeviceERIs, _dev_tensor
     dev = torch.device(device)
     Lf = _dev_tensor(system.L, dev)
@@ -337,7 +337,8 @@ def split_eris(system, device="cuda"):
         n2 = (Lf[:, sl[r], sl[t]]).shape[1:]
         return gemm_bf16_tn(A, B, f64=True).reshape(*n1, *n2)
 
-    blocks = {k: fp64_blk(k) for k in ("oooo", "ovoo", "ovov", "ovvo")}
+    blocks = {k: fp64_blk(k) for k in ("oooo", "ovoo", "ovov")}
+    blocks["ovvo"] = blocks["ovov"].permute(0, 1, 3, 2).contiguous()  # (ia|bj) = (ia|jb), L symmetric
     blocks["ovvv"] = tc_blk("ovvv")
     blocks["oovv"] = tc_blk("oovv")
     s = Lf[:, o:, o:].sum(dim=2)                      # [P, a] = sum_c L[P,a,c]

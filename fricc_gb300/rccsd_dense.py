@@ -197,7 +197,9 @@ class DeviceERIs:
             n2 = L[:, r, s].shape[1:]
             return (A.T @ B).reshape(*n1, *n2)
 
-        blocks = {k: blk(k) for k in ("oooo", "ovoo", "ovov", "oovv", "ovvo", "ovvv")}
+        blocks = {k: blk(k) for k in ("oooo", "ovoo", "ovov", "oovv", "ovvv")}
+        # (ia|bj) = (ia|jb): L is symmetric in its two orbital indices
+        blocks["ovvo"] = blocks["ovov"].permute(0, 1, 3, 2).contiguous()
         Lvv = L[:, sl["v"], sl["v"]]
         v = system.nvir
         # vvvvT[c,d,a,b] = (ac|bd) = sum_P L[P,a,c] L[P,b,d]
