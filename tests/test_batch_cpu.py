@@ -40,3 +40,40 @@ def test_replica_trace_stats_is_mcmc_std():
         x = np.array(rb.history[r][50:])
         e, t = mcmc_std(x)
         assert means[r] == x.mean() and errs[r] == e and taus[r] == t
+
+
+def test_server_admission_respects_hbm_budget(monkeypatch):
+    """The request server's dispatcher admits a request only while the
+    estimated footprints in flight fit the budget (a request larger than the
+    budget runs alone), and every request finishes (solves faked on CPU)."""
+    import threading
+    import time
+
+    from fricc_gb300 import batch as B
+    monkeypatch.setattr(B.torch.cuda, "set_device", lambda d: None)
+    monkeypatch.setattr(B.torch.cuda, "Stream", lambda device=None: object())
+    lock = threading.Lock()
+    state = {"in_use": 0, "max": 0, "n": 0}
+
+    def fake_solve(self, req, t0, stream):
+        need = B.footprint_bytes(req.nocc, req.nvir, self.precision)
+        with lock:
+            state["in_use"] += need
+            state["max"] = max(state["max"], state["in_use"])
+            state["n"] += 1
+        req.started = time.perf_counter() - t0
+        time.sleep(0.005 * (1 + req.rid % 3))
+        req.energies, req.iterations, req.converged, req.e_corr = [-1.0], 1, True, -1.0
+        with lock:
+            state["in_use"] -= need
+
+    monkeypatch.setattr(B.SolveServer, "_solve", fake_solve)
+    reqs = request_stream(16, rate=1000.0, seed=3, nocc=(5, 12))
+    sizes = sorted(B.footprint_bytes(r.nocc, r.nvir, "split") for r in reqs)
+    budget = sizes[-1] + sizes[-2] // 2   # the two largest never run together
+    srv = B.SolveServer(n_workers=4, hbm_budget=budget, precision="split", device="cuda:0")
+    out = srv.run(reqs, time_scale=0.0)
+    assert state["n"] == 16 and all(r.finished >= r.admitted >= 0 for r in out)
+    assert state["max"] <= budget
+    s = latency_summary(out)
+    assert s["n"] == 16 and s["converged"] == 16 and s["solves_per_s"] > 0
