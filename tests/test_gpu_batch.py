@@ -69,3 +69,27 @@ def test_served_requests_match_lone_solves(gpulib):
         SolveServer(n_workers=1, precision="df64", max_cycle=4).run([r])
     for a, b in zip(sorted(out, key=lambda r: r.rid), sorted(lone, key=lambda r: r.rid)):
         assert abs(a.e_corr - b.e_corr) < 1e-10, (a.rid, a.e_corr, b.e_corr)
+
+
+def test_served_split_requests_alone_in_the_mix_and_against_fp64(gpulib):
+    """The served split-precision form: each request's energies are the same
+    served among others (3 workers, overlapping solves) as solved alone, and
+    every iteration's energy is within 1e-6 Eh of the plain FP64 GPU form's
+    (same synthetic system, same draws)."""
+    from fricc_gb300.batch import SolveServer, request_stream
+
+    def stream():
+        return request_stream(6, rate=200.0, seed=11, nocc=(5, 8))
+
+    served = SolveServer(n_workers=3, precision="split", max_cycle=4).run(stream())
+    lone, plain = stream(), stream()
+    for r in lone:
+        SolveServer(n_workers=1, precision="split", max_cycle=4).run([r])
+    for r in plain:
+        SolveServer(n_workers=1, precision="fp64", max_cycle=4).run([r])
+    key = lambda r: r.rid  # noqa: E731
+    for a, b, c in zip(sorted(served, key=key), sorted(lone, key=key), sorted(plain, key=key)):
+        assert a.iterations == b.iterations >= 1 and np.isfinite(a.e_corr)
+        assert np.max(np.abs(np.array(a.energies) - np.array(b.energies))) < 1e-10, a.rid
+        n = min(len(a.energies), len(c.energies))
+        assert np.max(np.abs(np.array(a.energies[:n]) - np.array(c.energies[:n]))) <= 1e-6, (a.rid, a.energies, c.energies)
