@@ -240,3 +240,48 @@ def test_parallel_sample_golden(oracle):
         S, used = oracle.parallel_sample(ns, q, 1, draws)
         np.testing.assert_array_equal(S, g[f"c{k}_S"], err_msg=f"case {k}")
         assert used == int(g[f"c{k}_used"]), (k, used)
+
+
+EINSUM = {"0101": ("klij,klab->ijab", 1.0, "oooo"), "2323": ("abcd,ijcd->ijab", 1.0, "vvvv"),
+          "1302": ("akic,kjcb->ijab", 2.0, "voov"), "1202": ("akci,kjcb->ijab", -1.0, "vovo"),
+          "1303": ("akic,kjbc->ijab", 1.0, "voov"), "1203": ("bkci,kjac->ijab", 1.0, "vovo"),
+          "1323": ("kcld,ijcd->klij", 1.0, "ovov"), "0112": ("ldkc,ilda->akic", -0.5, "ovov"),
+          "0113": ("ldkc,ilad->akic", 1.0, "ovov"), "0313": ("lckd,ilad->akic", -0.5, "ovov"),
+          "0312": ("lckd,ilda->akci", -0.5, "ovov")}
+
+
+@pytest.mark.parametrize("no,nv,frac", [(4, 8, 0.1), (5, 10, 0.01), (10, 20, 0.001), (20, 40, 0.001)])
+def test_oracle_terms_equal_einsum(oracle, no, nv, frac):
+    """The reference's fricc/tests/test_sparse_tensors.py pattern on the
+    oracle: every term on a "largest"-compressed T2 that keeps all nonzeros
+    equals np.einsum of the dense T2 (:48-269; seed 20 as there)."""
+    rng = np.random.default_rng(20)
+    d = {"o": no, "v": nv}
+    t2 = np.zeros(no * no * nv * nv)
+    nnz = max(1, int(t2.size * frac))
+    t2[rng.choice(t2.size, nnz, replace=False)] = rng.random(nnz)
+    t2 = t2.reshape(no, no, nv, nv)
+    T = oracle.SparseTensor4d(t2, t2.shape, nnz, "largest")
+    for term in TERMS:
+        spec, coef, wshape = EINSUM[term]
+        W = rng.random(tuple(d[c] for c in wshape))
+        ref = coef * np.einsum(spec, W, t2)
+        out = np.zeros(ref.shape)
+        oracle.contract_DTSpT(W, T, out, term)
+        np.testing.assert_allclose(out, ref, rtol=1e-12, atol=1e-13 * max(1.0, np.abs(ref).max()), err_msg=term)
+
+
+@pytest.mark.parametrize("no,nv,frac", [(4, 8, 0.1), (10, 15, 0.001), (100, 2, 0.001)])
+def test_oracle_largest_elements_exact(oracle, no, nv, frac):
+    """test_sparse_tensors.py:18-45: every kept (index, value) of a "largest"
+    compression is the dense tensor's element at that index, and they are the
+    m largest magnitudes."""
+    rng = np.random.default_rng(20)
+    a = rng.random((no, no, nv, nv))
+    m = max(1, int(a.size * frac))
+    T = oracle.SparseTensor4d(a, a.shape, m, "largest")
+    for mi in range(m):
+        idx, value = T.get_element(mi)
+        assert value == a[tuple(idx)]
+    kept = np.sort(np.abs(T.vals))
+    assert np.array_equal(kept, np.sort(np.abs(a.ravel()))[-m:])
