@@ -52,14 +52,15 @@ def libc_uniform() -> float:
     return float(_libc.rand()) / float(RAND_MAX)
 
 
-def parallel_sample(n_sample: int, q, chunks: int = 1, rng=None) -> np.ndarray:
-    """parallel_sample(n_sample, q) of src/fri_utils.cpp:176-362 on the GPU:
-    pivotal sampling of q cut into `chunks` chunks (the reference's OpenMP
+def parallel_sample(n_sample: int, probs, chunks: int = 1, rng=None) -> np.ndarray:
+    """parallel_sample(n_sample, probs) of src/fri_utils.cpp:176-362 (argument
+    names of the binding, src/py_rccsd.cpp:22-23) on the GPU: pivotal
+    sampling of probs cut into `chunks` chunks (the reference's OpenMP
     threads), each chunk walked by its own warp.  Draws from the process's
     rand() (the reference's stream) or from rng (a GlibcRand), in chunk order.
     Returns the n_sample indices (numpy int64)."""
     lib = L.load()
-    qd = _to_device(np.ascontiguousarray(q, dtype=np.float64) if not isinstance(q, torch.Tensor) else q)
+    qd = _to_device(np.ascontiguousarray(probs, dtype=np.float64) if not isinstance(probs, torch.Tensor) else probs)
     qd = qd.contiguous()
     S = torch.empty(max(int(n_sample), 1), dtype=torch.int64, device=qd.device)
     hist, writeback = L.hist_arg(rng)

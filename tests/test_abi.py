@@ -39,3 +39,26 @@ def test_version_and_error_paths(gpulib):
     assert st == 1  # FRICC_ERR_ARG
     with pytest.raises(ValueError):
         _lib.check(st)
+
+
+def test_python_binding_surface():
+    """fricc_gb300.py_rccsd carries the reference binding's names, argument
+    names and defaults for the FRI-CCSD path (src/py_rccsd.cpp:22-23,29-30,
+    32-54), so keyword calls written for fricc.py_rccsd work unchanged."""
+    import inspect
+
+    from fricc_gb300 import py_rccsd as m
+
+    def names(f):
+        return list(inspect.signature(f).parameters)
+
+    assert names(m.contract_DTSpT) == ["W", "T", "ouput", "term"]
+    assert names(m.contract_DTSpT_experimental) == ["W", "T", "ouput", "term"]
+    p = inspect.signature(m.fri_compression).parameters
+    assert list(p)[:4] == ["x", "n_sample", "sampling_method", "verbose"]
+    assert p["sampling_method"].default == "pivotal" and p["verbose"].default is False
+    p = inspect.signature(m.SparseTensor4d.__init__).parameters
+    assert list(p)[1:7] == ["tensor_arr", "dims", "m", "compression", "sampling_method", "verbose"]
+    assert (p["compression"].default, p["sampling_method"].default, p["verbose"].default) == ("fri", "pivotal", False)
+    assert names(m.parallel_sample)[:2] == ["n_sample", "probs"]
+    assert callable(m.SparseTensor4d.get_element) and callable(m.SparseTensor4d.print)
