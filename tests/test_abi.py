@@ -62,3 +62,25 @@ def test_python_binding_surface():
     assert (p["compression"].default, p["sampling_method"].default, p["verbose"].default) == ("fri", "pivotal", False)
     assert names(m.parallel_sample)[:2] == ["n_sample", "probs"]
     assert callable(m.SparseTensor4d.get_element) and callable(m.SparseTensor4d.print)
+
+
+def test_binding_argument_checks_before_device_work(gpulib):
+    """The binding's own argument errors (src/py_rccsd.cpp:34-39 noconvert,
+    include/sparse_tensor.hpp:70-76 unknown compression,
+    src/sparse_tensor.cpp:378-381 unknown term) raise before any device work."""
+    import numpy as np
+
+    from fricc_gb300 import py_rccsd as m
+    a = np.zeros((2, 2, 3, 3))
+    with pytest.raises(TypeError):
+        m.SparseTensor4d(a.astype(np.float32), a.shape, 4, "fri", "systematic")
+    with pytest.raises(TypeError):
+        m.SparseTensor4d(np.asfortranarray(a), a.shape, 4, "fri", "systematic")
+    with pytest.raises(TypeError):
+        m.SparseTensor4d(a.tolist(), a.shape, 4, "fri", "systematic")
+    with pytest.raises(ValueError, match="compression"):
+        m.SparseTensor4d(a, a.shape, 4, "random")
+    with pytest.raises(ValueError, match="CASE NOT IMPLEMENTED"):
+        m.contract_DTSpT(a, None, a.copy(), "2332")
+    with pytest.raises(ValueError, match="CASE NOT IMPLEMENTED"):
+        m.contract_DTSpT_experimental(a, None, a.copy(), "2323")
