@@ -84,3 +84,31 @@ def test_binding_argument_checks_before_device_work(gpulib):
         m.contract_DTSpT(a, None, a.copy(), "2332")
     with pytest.raises(ValueError, match="CASE NOT IMPLEMENTED"):
         m.contract_DTSpT_experimental(a, None, a.copy(), "2323")
+
+
+@pytest.mark.parametrize("compiler,ext", [("gcc", "c"), ("g++", "cpp")])
+def test_header_compiles_and_links(gpulib, tmp_path, compiler, ext):
+    """A C and a C++ program that include include/fricc_gb300.h, take the
+    address of every function it declares and link against the built
+    library (the integration a C or C++ host makes) compile, link and run
+    fricc_version() without a GPU."""
+    import shutil
+    import subprocess
+
+    if shutil.which(compiler) is None:
+        pytest.skip(f"{compiler} not found")
+    names = _declared()
+    src = tmp_path / f"probe.{ext}"
+    src.write_text(
+        '#include "fricc_gb300.h"\n#include <stdio.h>\n'
+        "typedef void (*fp)(void);\n"
+        "int main(void) {\n  volatile fp f[] = {\n"
+        + "".join(f"    (fp){n},\n" for n in names)
+        + "  };\n  (void)f;\n  printf(\"%d\\n\", fricc_version());\n  return 0;\n}\n")
+    libdir = os.path.join(REPO, "fricc_gb300", "_lib")
+    exe = tmp_path / "probe"
+    r = subprocess.run([compiler, "-Wall", "-Werror", "-I", os.path.join(REPO, "include"), str(src), "-o", str(exe),
+                        "-L", libdir, "-lfricc_gb300", f"-Wl,-rpath,{libdir}"], capture_output=True, text=True)
+    assert r.returncode == 0, r.stderr
+    r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
+    assert r.returncode == 0 and r.stdout.strip() == "100", (r.stdout, r.stderr)
