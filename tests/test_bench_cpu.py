@@ -24,3 +24,37 @@ def test_reference_arm_json_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     assert d["config"]["workload"].startswith("o10v40")
+
+
+def test_clock_sampler_reads_a_fake_nvidia_smi(tmp_path, monkeypatch):
+    """The clocks record of the JSON line: the median SM clock under load,
+    the maximum clock, and every throttle reason seen active, read from
+    nvidia-smi's CSV stream (a fake nvidia-smi on PATH; no GPU involved)."""
+    import time
+    sys.path.insert(0, REPO)
+    import bench
+    fake = tmp_path / "nvidia-smi"
+    fake.write_text("#!/bin/sh\n"
+                    "echo '2070, 2070, 900.5, Not Active, Not Active, Not Active, Not Active'\n"
+                    "echo '1980, 2070, 1350.0, Not Active, Not Active, Not Active, Active'\n"
+                    "echo '2055, 2070, 1200.0, Not Active, Not Active, Not Active, Not Active'\n"
+                    "echo 'garbage line'\n"
+                    "exec sleep 30\n")
+    fake.chmod(0o755)
+    monkeypatch.setenv("PATH", f"{tmp_path}{os.pathsep}{os.environ['PATH']}")
+    with bench.ClockSampler(0) as cs:
+        t0 = time.time()
+        while len(cs.rows) < 3 and time.time() - t0 < 20:
+            time.sleep(0.05)
+    s = cs.summary()
+    assert s == {"sm_mhz": 2055.0, "sm_max_mhz": 2070.0, "reasons": ["sw_power_cap"], "samples": 3}
+    assert bench.ClockSampler(0).summary()["reasons"] == ["unsampled"]
+
+
+def test_measured_peaks_file_or_fallback():
+    sys.path.insert(0, REPO)
+    import bench
+    p = bench.measured_peaks()
+    assert p["hbm_gbs"] > 1000 and p["bf16_tflops"] > 100
+    if not os.path.exists(os.path.join(REPO, "MEASURED_PEAKS.json")):
+        assert p.get("fallback") is True
