@@ -39,9 +39,10 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 METRIC = "FRI-CCSD iter/s and solves/s at |ΔEcorr|≤1e-6 Eh vs plain GPU; p50/p99 latency"
-# FP64 FMA throughput of this GB300 pool, measured with a 16-chain DFMA probe
-# (profiles/fp64_peak_gb300.md): the contraction kernel is FP64-pipe bound
-# and MEASURED_PEAKS.json has no FP64 figure.
+# FP64 and FP32 FMA throughput of this GB300 pool, measured with the
+# independent-chain FMA probe of fricc_gb300/peaks.cu (python -m
+# fricc_gb300.peaks; profiles/fp64_peak_gb300.md): the contraction kernels are
+# FP64- or FP32-pipe bound and MEASURED_PEAKS.json has no figure for either.
 FP64_PEAK_TFLOPS = 1.2557
 FP32_PEAK_TFLOPS = 74.2
 # DRAM bytes (read + write) per k_spmm_df launch, df64, from one ncu capture

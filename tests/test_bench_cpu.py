@@ -58,3 +58,17 @@ def test_measured_peaks_file_or_fallback():
     assert p["hbm_gbs"] > 1000 and p["bf16_tflops"] > 100
     if not os.path.exists(os.path.join(REPO, "MEASURED_PEAKS.json")):
         assert p.get("fallback") is True
+
+
+def test_peaks_probe_builds():
+    """The probe that measures the FP64 and FP32 FMA rates bench.py's roofline
+    divides by (python -m fricc_gb300.peaks) cross-compiles for sm_103a."""
+    import shutil
+
+    import pytest
+    if shutil.which("nvcc") is None and not os.path.exists("/usr/local/cuda/bin/nvcc"):
+        pytest.skip("nvcc not found")
+    sys.path.insert(0, REPO)
+    from fricc_gb300 import peaks
+    exe = peaks.build()
+    assert os.path.exists(exe) and os.access(exe, os.X_OK)
