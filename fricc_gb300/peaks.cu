@@ -4,8 +4,8 @@
 // (the FP32-pair kernels' bound: 12 FP32 instructions per pair multiply-add)
 // and, for scale, FP64 mma.sync and a plain copy.  Each kernel runs
 // independent FMA chains (no data dependence between them) so the pipe, not
-// latency, bounds it; times are CUDA events around one launch after a
-// warm-up launch.  One JSON object per line on stdout.
+// latency, bounds it; times are CUDA events around one launch (five for the
+// copy) after a warm-up launch.  One JSON object per line on stdout.
 //
 // Build and run: python -m fricc_gb300.peaks
 #include <cstdio>
