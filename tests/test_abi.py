@@ -112,3 +112,12 @@ def test_header_compiles_and_links(gpulib, tmp_path, compiler, ext):
     assert r.returncode == 0, r.stderr
     r = subprocess.run([str(exe)], capture_output=True, text=True, timeout=60)
     assert r.returncode == 0 and r.stdout.strip() == "100", (r.stdout, r.stderr)
+
+
+def test_missing_library_fails_loudly(tmp_path, monkeypatch):
+    """Without the built library the GPU path raises at load time; nothing
+    falls back to a CPU implementation."""
+    from fricc_gb300 import _lib
+    monkeypatch.setattr(_lib, "_lib", None)
+    with pytest.raises(ImportError, match="no CPU fallback"):
+        _lib.load(str(tmp_path / "libfricc_gb300.so"))
