@@ -24,6 +24,7 @@ _i64p = ctypes.POINTER(ctypes.c_int64)
 _dp = ctypes.c_void_p
 _vp = ctypes.c_void_p
 _u32p = ctypes.POINTER(ctypes.c_uint32)
+_vpp = ctypes.POINTER(ctypes.c_void_p)  # an array of pointers
 SIGNATURES = [
     ("fricc_version", ctypes.c_int, []),
     ("fricc_last_error", ctypes.c_char_p, []),
@@ -43,6 +44,10 @@ SIGNATURES = [
     ("fricc_sp_export", ctypes.c_int, [_vp, _vp, _vp, _vp]),
     ("fricc_sp_device_arrays", ctypes.c_int, [_vp, ctypes.POINTER(_vp), ctypes.POINTER(_vp), ctypes.POINTER(_vp)]),
     ("fricc_contract", ctypes.c_int, [ctypes.c_char_p, _dp, _i64p, _i64p, _vp, _dp, _i64p, _i64p, _vp]),
+    ("fricc_contract_batch", ctypes.c_int, [ctypes.c_char_p, _i64, _vpp, _i64p, _i64p, _vpp, _vpp, _i64p, _i64p,
+                                            _vp]),
+    ("fricc_sp_recompress_batch", ctypes.c_int, [_i64, _vpp, _vpp, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.POINTER(ctypes.c_double), _vp]),
     ("fricc_spmm", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_double,
                                   _dp, _i64, _dp, _vp]),
     ("fricc_spmm_f2", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,

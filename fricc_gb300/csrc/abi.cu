@@ -529,6 +529,42 @@ int fricc_contract(const char* term, const double* W, const int64_t W_dims[4], c
   return rc;
 }
 
+// the failing item's index in front of its own message
+static int batch_item_error(const char* what, int64_t r, int rc) {
+  char msg[sizeof(g_err)];
+  snprintf(msg, sizeof(msg), "%s", g_err);
+  fricc_set_error("%s item %lld: %s", what, (long long)r, msg);
+  return rc;
+}
+
+int fricc_contract_batch(const char* term, int64_t count, const double* const* W, const int64_t* W_dims,
+                         const int64_t* W_strides, fricc_sparse* const* T, double* const* out,
+                         const int64_t* out_dims, const int64_t* out_strides, void* stream) {
+  if (count < 0 || (count > 0 && (!W || !W_dims || !W_strides || !T || !out || !out_dims || !out_strides))) {
+    fricc_set_error("contract_batch: negative count or null array");
+    return FRICC_ERR_ARG;
+  }
+  for (int64_t r = 0; r < count; ++r) {
+    const int rc = fricc_contract(term, W[r], W_dims + 4 * r, W_strides + 4 * r, T[r], out[r], out_dims + 4 * r,
+                                  out_strides + 4 * r, stream);
+    if (rc) return batch_item_error("contract_batch", r, rc);
+  }
+  return FRICC_OK;
+}
+
+int fricc_sp_recompress_batch(int64_t count, fricc_sparse* const* T, const double* const* t2, int compression,
+                              int sampling, const double* rn, void* stream) {
+  if (count < 0 || (count > 0 && (!T || !t2 || !rn))) {
+    fricc_set_error("sp_recompress_batch: negative count or null array");
+    return FRICC_ERR_ARG;
+  }
+  for (int64_t r = 0; r < count; ++r) {
+    const int rc = fricc_sp_recompress(T[r], t2[r], compression, sampling, rn[r], stream);
+    if (rc) return batch_item_error("sp_recompress_batch", r, rc);
+  }
+  return FRICC_OK;
+}
+
 int fricc_spmm(fricc_sparse* T, int pa, int pb, int ka, int kb, double coef, const double* Wp, int64_t QS,
                double* Op, void* stream) {
   cudaStream_t st = as_stream(stream);

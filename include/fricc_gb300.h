@@ -151,6 +151,19 @@ int fricc_contract(const char* term, const double* W, const int64_t W_dims[4], c
                    fricc_sparse* T, double* out, const int64_t out_dims[4], const int64_t out_strides[4],
                    void* stream);
 
+/* Batched forms for R independent replicas or solves (no reference
+ * counterpart: the reference runs one solve per process).  Item r is exactly
+ * fricc_contract(term, W[r], W_dims + 4r, W_strides + 4r, T[r], out[r],
+ * out_dims + 4r, out_strides + 4r, stream), respectively
+ * fricc_sp_recompress(T[r], t2[r], compression, sampling, rn[r], stream),
+ * issued in order on `stream`; the first failing item stops the batch and its
+ * index leads the message.  count = 0 does nothing. */
+int fricc_contract_batch(const char* term, int64_t count, const double* const* W, const int64_t* W_dims,
+                         const int64_t* W_strides, fricc_sparse* const* T, double* const* out,
+                         const int64_t* out_dims, const int64_t* out_strides, void* stream);
+int fricc_sp_recompress_batch(int64_t count, fricc_sparse* const* T, const double* const* t2, int compression,
+                              int sampling, const double* rn, void* stream);
+
 /* The kernel behind every term, in general form (no reference counterpart;
  * each contract_DTSpT term is one instance of it):
  *   Op[P][q] += coef * sum over nonzeros e with P_e == P of Wp[key_e][q] * value_e

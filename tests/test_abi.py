@@ -121,3 +121,25 @@ def test_missing_library_fails_loudly(tmp_path, monkeypatch):
     monkeypatch.setattr(_lib, "_lib", None)
     with pytest.raises(ImportError, match="no CPU fallback"):
         _lib.load(str(tmp_path / "libfricc_gb300.so"))
+
+
+def test_batch_entry_points_check_arguments(gpulib):
+    """fricc_contract_batch / fricc_sp_recompress_batch: bad counts and null
+    arrays are rejected, count 0 does nothing, and an item's own error (here
+    raised before any device work) comes back with its index in front."""
+    import ctypes
+
+    from fricc_gb300 import _lib
+    d = _lib.i64arr([1] * 8)
+    nulls = (ctypes.c_void_p * 2)()
+    assert gpulib.fricc_contract_batch(b"2323", -1, nulls, d, d, nulls, nulls, d, d, None) == 1
+    assert gpulib.fricc_contract_batch(b"2323", 2, None, d, d, nulls, nulls, d, d, None) == 1
+    assert gpulib.fricc_contract_batch(b"2323", 0, None, None, None, None, None, None, None, None) == 0
+    assert gpulib.fricc_contract_batch(b"9999", 2, nulls, d, d, nulls, nulls, d, d, None) == 2
+    assert gpulib.fricc_last_error().startswith(b"contract_batch item 0: CASE NOT IMPLEMENTED")
+    rn = (ctypes.c_double * 2)(0.5, 0.5)
+    assert gpulib.fricc_sp_recompress_batch(-1, nulls, nulls, 0, 0, rn, None) == 1
+    assert gpulib.fricc_sp_recompress_batch(2, nulls, nulls, 0, 0, None, None) == 1
+    assert gpulib.fricc_sp_recompress_batch(0, None, None, 0, 0, None, None) == 0
+    assert gpulib.fricc_sp_recompress_batch(2, nulls, nulls, 0, 0, rn, None) == 1
+    assert gpulib.fricc_last_error() == b"sp_recompress_batch item 0: sp_recompress: null argument"

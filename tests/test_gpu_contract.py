@@ -189,3 +189,36 @@ def test_sym_add_matches_torch(gpulib, perm, o, v):
     ref = out + -0.5 * (X + X.permute(1, 0, 3, 2))
     sym_add(out, X, -0.5)
     torch.testing.assert_close(out, ref, rtol=0, atol=0)
+
+
+def test_batch_entry_points_match_single_calls(gpulib):
+    """fricc_sp_recompress_batch and fricc_contract_batch: every item is bit
+    for bit its single-handle call (same kernels, issued in order)."""
+    import ctypes
+
+    from fricc_gb300 import _lib, py_rccsd
+    rng = np.random.default_rng(5)
+    o, v, m, R = 4, 9, 300, 2
+    dims = (o, o, v, v)
+    Ts = [py_rccsd.SparseTensor4d(rng.standard_normal(dims), dims, m, "fri", "systematic", rn=0.3) for _ in range(R)]
+    new = [torch.from_numpy(rng.standard_normal(dims)).cuda() for _ in range(R)]
+    rns = (ctypes.c_double * R)(0.11, 0.77)
+    hs = (ctypes.c_void_p * R)(*[T.handle.value for T in Ts])
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    _lib.check(gpulib.fricc_sp_recompress_batch(R, hs, (ctypes.c_void_p * R)(*[x.data_ptr() for x in new]), 0, 0,
+                                                rns, st))
+    for r in range(R):
+        ref = py_rccsd.SparseTensor4d(new[r], dims, m, "fri", "systematic", rn=rns[r])
+        (fa, va), (fb, vb) = Ts[r].export(), ref.export()
+        assert np.array_equal(fa, fb) and np.array_equal(va.view(np.int64), vb.view(np.int64)), r
+    Ws = [torch.from_numpy(rng.standard_normal((v, v, v, v))).cuda() for _ in range(R)]
+    outs = [torch.from_numpy(rng.standard_normal(dims)).cuda() for _ in range(R)]
+    refs = [x.clone() for x in outs]
+    cat = lambda ts, f: _lib.i64arr([k for t in ts for k in f(t)])  # noqa: E731
+    _lib.check(gpulib.fricc_contract_batch(
+        b"2323", R, (ctypes.c_void_p * R)(*[w.data_ptr() for w in Ws]), cat(Ws, lambda t: t.shape),
+        cat(Ws, lambda t: t.stride()), hs, (ctypes.c_void_p * R)(*[x.data_ptr() for x in outs]),
+        cat(outs, lambda t: t.shape), cat(outs, lambda t: t.stride()), st))
+    for r in range(R):
+        py_rccsd.contract_DTSpT(Ws[r], Ts[r], refs[r], "2323")
+        assert torch.equal(outs[r], refs[r]), r
