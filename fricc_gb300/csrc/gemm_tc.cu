@@ -29,6 +29,7 @@
 // A B^T ~ Ahi Bhi^T + Ahi Blo^T + Alo Bhi^T (the lo*lo term is below FP32
 // accumulation error).  The three products are one GEMM over a K-concatenated
 // operand pair A' = [Ahi | Ahi | Alo], B' = [Bhi | Blo | Bhi] (K' = 3K).
+#include <atomic>
 #include <cuda.h>
 #include <cudaTypedefs.h>
 #include <cuda_bf16.h>
@@ -545,17 +546,17 @@ __global__ void k_split_tr(const double* __restrict__ x, int64_t rows, int64_t k
   }
 }
 
+// looked up once; a function-local static is initialised exactly once even
+// when several host threads (a request server's workers) arrive together
 PFN_cuTensorMapEncodeTiled_v12000 encode_fn() {
-  static PFN_cuTensorMapEncodeTiled_v12000 fn = nullptr;
-  static bool tried = false;
-  if (!tried) {
-    tried = true;
+  static const PFN_cuTensorMapEncodeTiled_v12000 fn = []() -> PFN_cuTensorMapEncodeTiled_v12000 {
     void* p = nullptr;
     cudaDriverEntryPointQueryResult q;
     if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &p, 12000, cudaEnableDefault, &q) == cudaSuccess &&
         q == cudaDriverEntryPointSuccess)
-      fn = reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
-  }
+      return reinterpret_cast<PFN_cuTensorMapEncodeTiled_v12000>(p);
+    return nullptr;
+  }();
   return fn;
 }
 
@@ -585,15 +586,15 @@ int make_map(CUtensorMap* map, const void* ptr, int64_t rows, int64_t k, int64_t
 // otherwise stream-ordered (capturable): the kernel ORs FRICC_DEV_TIMEOUT into
 // *status and the caller reads it later.
 int sm_count(int* out) {
-  static int nsm = 0;
+  static std::atomic<int> cached{0};  // shared by the host threads; every writer stores the same value
+  int nsm = cached.load(std::memory_order_relaxed);
   if (!nsm) {
     int dev = 0;
     cudaError_t e = cudaGetDevice(&dev);
     if (e == cudaSuccess) e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-    if (e != cudaSuccess || nsm <= 0) {
-      nsm = 0;
+    if (e != cudaSuccess || nsm <= 0)
       return fricc_cuda_fail(e != cudaSuccess ? e : cudaErrorUnknown, "gemm_tc SM count", __FILE__, __LINE__);
-    }
+    cached.store(nsm, std::memory_order_relaxed);
   }
   *out = nsm;
   return FRICC_OK;
@@ -617,12 +618,13 @@ int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t 
   int rc = make_map(&ma, A, M, K, lda, BM);
   if (!rc) rc = make_map(&mb, B, N, K, ldb, BN);
   if (rc) return rc;
-  static bool attr = false;  // per instantiation
+  // per instantiation; threads that race here all set the same attribute
+  static std::atomic<bool> attr{false};
   cudaError_t e = cudaSuccess;
-  if (!attr) {
+  if (!attr.load(std::memory_order_acquire)) {
     e = cudaFuncSetAttribute(k_gemm_tc<TC, Epi>, cudaFuncAttributeMaxDynamicSharedMemorySize, SMEM_BYTES);
     if (e != cudaSuccess) return fricc_cuda_fail(e, "gemm_tc attribute", __FILE__, __LINE__);
-    attr = true;
+    attr.store(true, std::memory_order_release);
   }
   int nsm = 0;
   rc = sm_count(&nsm);
