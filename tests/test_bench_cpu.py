@@ -72,3 +72,23 @@ def test_peaks_probe_builds():
     from fricc_gb300 import peaks
     exe = peaks.build()
     assert os.path.exists(exe) and os.access(exe, os.X_OK)
+
+
+def test_reference_arm_under_torchrun_two_ranks():
+    """Launched the way the multi-GPU runs launch bench.py (torchrun, two
+    ranks): rank 0 alone runs the reference arm and prints one line; the
+    other rank exits 0 without work."""
+    import socket
+    s = socket.socket()
+    s.bind(("127.0.0.1", 0))
+    port = s.getsockname()[1]
+    s.close()
+    r = subprocess.run([sys.executable, "-m", "torch.distributed.run", "--nnodes=1", "--nproc-per-node", "2",
+                        "--master-addr", "127.0.0.1", "--master-port", str(port), "bench.py", "--impl", "reference",
+                        "--workload", "o10v40", "--gpus", "2", "--steps", "1", "--warmup", "1"],
+                       cwd=REPO, capture_output=True, text=True, timeout=900)
+    assert r.returncode == 0, r.stderr[-2000:]
+    lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+    assert len(lines) == 1
+    d = json.loads(lines[0])
+    assert d["impl"] == "reference" and d["value"] > 0
