@@ -2,10 +2,13 @@
 """FRI-CCSD iterations per second on one GB300 (and N independent replicas).
 
 Workload (default): o30v150 -- nocc=30, nvir=150 (o^2 v^2 = 20.25M amplitudes),
-Cholesky ERIs with naux=900 and N(0, 0.03^2) entries, MP2 starting T2,
-m = 2,000,000 kept amplitudes per FRI compression, two compressions per
-iteration, FP64 throughout.  A step is one FRI-CCSD iteration (update_amps
-plus the energy), continuing the trajectory from the MP2 guess.
+Cholesky ERIs with naux=900 and factor entries N(0, 0.03^2/naux), MP2
+starting T2, m = 2,000,000 kept amplitudes per FRI compression, two
+compressions per iteration.  A step is one FRI-CCSD iteration (update_amps
+plus the energy), continuing the trajectory from the MP2 guess.  The
+headline runs in FP64 (--precision fp64, the default); the FP32-pair form
+(df64) and the split-precision form are measured beside it as secondary
+figures, each with its |dE_corr| against the FP64 path for one step.
 
     python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -15,8 +18,11 @@ resident in HBM; e2e = the same step through the host entry point
 --impl reference: the reference algorithm on the host cores (the oracle port
 of fri-cc's C++ plus numpy for the dense algebra), each step one sampled
 iteration: both compressions in full, the dense algebra in full, and every
-contraction term on a bounded sample of its outer-index pairs, scaled by the
-pair count.
+contraction term on one contiguous block of its outer-index pairs, the block
+rotating from step to step (B consecutive steps cover every pair once),
+scaled by the pair count.
+--validate-sample (with --impl reference): one full iteration timed beside
+the B block estimates of the same iteration.
 
 Under torchrun (N>1) every rank runs its own replica (different seed) of
 the same workload; value = all ranks' iterations / the slowest rank's time.
@@ -39,16 +45,34 @@ REPO = os.path.dirname(os.path.abspath(__file__))
 sys.path.insert(0, REPO)
 
 METRIC = "FRI-CCSD iter/s and solves/s at |ΔEcorr|≤1e-6 Eh vs plain GPU; p50/p99 latency"
-# FP64 and FP32 FMA throughput of this GB300 pool, measured with the
-# independent-chain FMA probe of fricc_gb300/peaks.cu (python -m
-# fricc_gb300.peaks; profiles/fp64_peak_gb300.md): the contraction kernels are
-# FP64- or FP32-pipe bound and MEASURED_PEAKS.json has no figure for either.
-FP64_PEAK_TFLOPS = 1.2557
-FP32_PEAK_TFLOPS = 74.2
-# DRAM bytes (read + write) per k_spmm_df launch, df64, from one ncu capture
-# of an o30v150 iteration's ten launches (profiles/k_spmm_df_traffic_o30v150.md):
-# 54.30 GB in total, of which 36.1 GB in the 2323 launch and 13.9 GB in X/Y.
-SPMM_TRAFFIC = {"o30v150": 5.43e9}
+# FP64 / FP32 FMA rates used when the live probe (fricc_gb300.peaks) cannot
+# run: the figures that probe gave on a GB300 of this pool (TFLOP/s).
+FP64_PEAK_FALLBACK = 1.2557
+FP32_PEAK_FALLBACK = 74.2
+# DRAM bytes (read + write) per launch of the dominant sparse kernel, from
+# one single-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum)
+# of a whole o30v150 iteration: a constant, not measured by this run.
+# Keys: (precision, workload) -> {term: bytes per launch}.
+SPMM_TRAFFIC_CAPTURED = {
+    ("df64", "o30v150"): {"2323": 36.1e9, "XY": 13.85e9},
+}
+
+
+def fma_peaks(probe: bool = True) -> dict:
+    """FP64 and FP32 FMA rates of this GPU (TFLOP/s), measured now by the
+    independent-chain FMA probe (a separate process, before any timed
+    work); the recorded pool figures if the probe cannot run."""
+    if not probe:
+        return {"fp64": FP64_PEAK_FALLBACK, "fp32": FP32_PEAK_FALLBACK, "source": "recorded pool figures"}
+    try:
+        from fricc_gb300 import peaks
+        lines = peaks.run()
+        fp64 = max(x["tflops"] for x in lines if x.get("kernel") == "dfma16")
+        fp32 = max(x["tflops"] for x in lines if x.get("kernel") == "ffma8")
+        return {"fp64": fp64, "fp32": fp32, "source": "measured by this run (FMA probe, fricc_gb300.peaks)"}
+    except Exception as ex:  # reported in the line, never fatal
+        return {"fp64": FP64_PEAK_FALLBACK, "fp32": FP32_PEAK_FALLBACK,
+                "source": f"recorded pool figures (probe failed: {type(ex).__name__})"}
 
 
 def parse():
@@ -60,14 +84,18 @@ def parse():
     p.add_argument("--workload", default="o30v150")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
-    p.add_argument("--no-split-form", action="store_true",
-                   help="skip the secondary measurement of the split-precision form")
+    p.add_argument("--no-secondary", action="store_true",
+                   help="skip the secondary measurements of the other arithmetic forms")
+    p.add_argument("--no-peak-probe", action="store_true",
+                   help="use the recorded FMA peaks instead of running the FMA probe")
+    p.add_argument("--validate-sample", action="store_true",
+                   help="with --impl reference: time one iteration in full beside its sampled estimate")
     p.add_argument("--graph", action="store_true",
                    help="replay each iteration from one captured CUDA graph (after the first, eager one)")
     p.add_argument("--autotune", action="store_true",
                    help="df64: time the launch configurations of every sparse term and GEMM shape during the "
                         "warm-up and keep the fastest")
-    p.add_argument("--precision", default="df64", choices=["fp64", "df64", "split"],
+    p.add_argument("--precision", default="fp64", choices=["fp64", "df64", "split"],
                    help="arithmetic of the sparse terms: FP64, or FP32 pairs (48-bit products, ~40-bit sums) on the "
                         "FP32 pipe; 'split' also rebuilds (vv|vv) every iteration from the BF16 hi+lo Cholesky "
                         "factor on the tcgen05 tensor cores (split-BF16x3, FP32) and builds (ov|vv), (oo|vv) "
@@ -151,42 +179,58 @@ def seeded_draws(seed):
 
 
 # ------------------------------------------------------------------ CPU side
-class SampledOracle:
-    """The oracle port with each contraction term run on a bounded sample of
-    its outer-index pairs; the term's full time is the sample's time scaled
-    by the pair count (the reference's cost per pair is the same m-entry scan
-    plus that pair's nonzeros)."""
+def block_plan(n_outer: int, n_blocks: int, block: int):
+    """Block ``block`` of ``n_blocks`` contiguous blocks of a term's outer
+    pairs: ((begin, end), size)."""
+    begin = (block * n_outer) // n_blocks
+    end = ((block + 1) * n_outer) // n_blocks
+    return (begin, end), end - begin
 
-    def __init__(self, pairs_per_term):
+
+class BlockOracle:
+    """The oracle port with each contraction term run on one contiguous block
+    (block ``block`` of ``n_blocks``) of its outer-index pairs; the term's
+    full time is the block's time scaled by the pair count.  A contiguous
+    block keeps what the full loop does to the memory system (neighbouring
+    pairs share cache lines of W and of the output, and the OpenMP threads
+    balance many pairs each); rotating the block from step to step makes the
+    estimates of n_blocks consecutive steps add up to whole terms."""
+
+    def __init__(self, n_blocks, block):
         from oracle import fri_oracle
         self.FO = fri_oracle
         self.SparseTensor4d = fri_oracle.SparseTensor4d
-        self.pairs = pairs_per_term
-        self.full_below = 1.0  # seconds: a term this cheap runs in full
+        self.n_blocks = n_blocks
+        self.block = block % n_blocks
+        self.full_below = 0.5  # seconds: a term this cheap runs in full (its fixed costs do not scale)
         self.contract_s = 0.0
         self.sample_wall = 0.0
+        self.per_term = {}
 
     def contract_DTSpT(self, W, T, out, term):
         n_outer = self.FO.outer_size(term, T.dims, W.shape)
-        k = min(n_outer, self.pairs)
+        rng, k = block_plan(n_outer, self.n_blocks, self.block)
         t = time.perf_counter()
-        self.FO.contract_DTSpT(W, T, out, term, outer_range=(0, k))
+        if k > 0:
+            self.FO.contract_DTSpT(W, T, out, term, outer_range=rng)
         dt = time.perf_counter() - t
         self.sample_wall += dt
-        est = dt * n_outer / k
-        if k < n_outer and est < self.full_below:  # cheap enough: time the whole term instead
+        est = dt * n_outer / k if k > 0 else 0.0
+        if k < n_outer and est < self.full_below:  # cheap: time the whole term instead
             t = time.perf_counter()
             self.FO.contract_DTSpT(W, T, out, term)
-            dt = time.perf_counter() - t
-            self.sample_wall += dt
-            est = dt
+            est = time.perf_counter() - t
+            self.sample_wall += est
         self.contract_s += est
+        self.per_term[term] = self.per_term.get(term, 0.0) + est
 
 
-def cpu_sampled_iteration(eris_np, t1, t2, m, pairs, rn_draw):
-    """One reference iteration on the host: seconds (extrapolated) and a description."""
+def cpu_sampled_iteration(eris_np, t1, t2, m, n_blocks, block, rn_draw):
+    """One reference iteration on the host with every contraction term on
+    one block of its outer pairs: seconds (estimated), the wall time actually
+    spent, the compression time and the per-term estimates."""
     from oracle import ccsd_oracle as CO
-    so = SampledOracle(pairs)
+    so = BlockOracle(n_blocks, block)
     settings = {"m_keep": m, "compression": "fri", "sampling_method": "systematic", "verbose": False,
                 "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"]}
     tim = {}
@@ -194,14 +238,36 @@ def cpu_sampled_iteration(eris_np, t1, t2, m, pairs, rn_draw):
     CO.update_amps(settings, t1, t2, eris_np, rn_draw=rn_draw, sparse=so, timings=tim)
     wall = time.perf_counter() - t0
     seconds = wall - so.sample_wall + so.contract_s
-    return seconds, wall, tim.get("compress", 0.0)
+    return seconds, wall, tim.get("compress", 0.0), so.per_term
 
 
-def _sample_text(workload, cores, pairs, wall):
+def n_blocks_for(steps: int, cap: int = 10) -> int:
+    """Blocks per term for a run of ``steps`` steps: the largest divisor of
+    steps up to ``cap`` (so every block is timed equally often), or
+    min(steps, cap) when steps has none above 1."""
+    best = max(d for d in range(1, min(steps, cap) + 1) if steps % d == 0)
+    return best if best > 1 or steps == 1 else min(steps, cap)
+
+
+def cpu_full_iteration(eris_np, t1, t2, m, rn_draw):
+    """One reference iteration on the host with every term in full: seconds
+    and the per-term times."""
+    from oracle import ccsd_oracle as CO
+    settings = {"m_keep": m, "compression": "fri", "sampling_method": "systematic", "verbose": False,
+                "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"]}
+    tim = {}
+    t0 = time.perf_counter()
+    CO.update_amps(settings, t1, t2, eris_np, rn_draw=rn_draw, timings=tim)
+    return time.perf_counter() - t0, tim
+
+
+def _sample_text(workload, cores, n_blocks, wall, steps):
     return (f"each step: one {workload} iteration of the oracle port of fri-cc's C++ (OpenMP, {cores} threads) "
-            f"and numpy dense algebra; both compressions and the dense algebra in full; each contraction term in "
-            f"full when that takes under 1 s, else on its first {pairs} outer-index pairs scaled by the pair "
-            f"count; {wall:.1f} s of CPU work")
+            f"and numpy dense algebra; both compressions and the dense algebra in full; every contraction term on "
+            f"one contiguous block of 1/{n_blocks} of its outer-index pairs (block = step mod {n_blocks}, so "
+            f"{n_blocks} consecutive steps cover every pair once), its time scaled by the pair count (a term "
+            f"estimated under 0.5 s runs in full instead); "
+            f"{steps} step(s), {wall:.1f} s of CPU work")
 
 
 def host_eris_from_device(E):
@@ -210,38 +276,60 @@ def host_eris_from_device(E):
     return P._ChemistsERIs(E.fock.cpu().numpy(), E.mo_energy.cpu().numpy(), E.nocc, blocks)
 
 
-def cpu_baseline_line(eris_np, t1, t2, m, workload, seed):
+def cpu_baseline_line(eris_np, t1, t2, m, workload, seed, n_blocks=10, blocks=(0, 5)):
+    """The reference algorithm on the host cores for the GPU arm's line:
+    a bounded sample (two blocks of every term, each with the iteration's
+    compressions and dense algebra in full)."""
     from oracle import fri_oracle
     cores = os.cpu_count() or 1
     fri_oracle.set_threads(cores)
-    pairs = 4 * cores
-    secs, wall, comp = cpu_sampled_iteration(eris_np, t1, t2, m, pairs, seeded_draws(seed))
-    return {"value": 1.0 / secs, "unit": "iter/s", "cores": cores, "kind": "port",
-            "sample": _sample_text(workload, cores, pairs, wall) + f" ({secs:.1f} s/iteration extrapolated)"}
+    draw = seeded_draws(seed)
+    est, walls = [], []
+    for b in blocks:
+        secs, wall, _, _ = cpu_sampled_iteration(eris_np, t1, t2, m, n_blocks, b, draw)
+        est.append(secs)
+        walls.append(wall)
+    secs = sum(est) / len(est)
+    return {"value": 1.0 / secs, "unit": "iter/s", "cores": cores, "kind": "port", "extrapolated": True,
+            "sample": _sample_text(workload, cores, n_blocks, sum(walls), len(blocks))
+            + f" (blocks {list(blocks)}; {secs:.1f} s/iteration estimated)"}
 
 
-def split_form_line(args, system, E, t1, t2, m, stream):
-    """Iterations/s of the split-precision form on the bench's workload
-    (CUDA events over args.steps steps after 2 warm-up steps), its |dE|
-    against the FP64 GPU path, and its tensor-core roofline."""
+WORKLOAD_TEXT = ("{wl}: nocc={o} nvir={v} naux={naux} Cholesky factor entries N(0, {sigma}^2/naux) (a factor "
+                 "normalised by naux; entries N(0, {sigma}^2) put every workload outside CCSD's convergence "
+                 "regime), m={m} FRI systematic, 2 compressions/iteration, MP2 start")
+
+
+def workload_text(wl, o, v, w):
+    return WORKLOAD_TEXT.format(wl=wl, o=o, v=v, naux=w["naux"], sigma=w["sigma"], m=w["m"])
+
+
+def secondary_form_line(precision, args, system, E, t1, t2, m, stream):
+    """Iterations/s of another arithmetic form on the bench's workload (CUDA
+    events over args.steps steps after 2 warm-up steps), its |dE_corr|
+    against the FP64 GPU path for one step from the same state and draws,
+    and the roofline of its dominant kernel."""
     import torch
 
     from fricc_gb300 import _lib
-    from fricc_gb300.cholesky import split_eris
     from fricc_gb300.friccsd import FRICCSDGPU
     from fricc_gb300.rng import GlibcRand
     lib = _lib.load()
-    Es = split_eris(system, device=t2.device)
-    sol = FRICCSDGPU(Es, {"m_keep": m}, rn_draw=GlibcRand(4242), precision="split")
+    if precision == "split":
+        from fricc_gb300.cholesky import split_eris
+        Es = split_eris(system, device=t2.device)
+    else:
+        Es = E
+    sol = FRICCSDGPU(Es, {"m_keep": m}, rn_draw=GlibcRand(4242), precision=precision)
     a1, a2 = t1, t2
     for _ in range(2):
         a1, a2 = sol.update_amps(a1, a2)
     rn = [0.3141592653589793, 0.2718281828459045]
     sol.update_amps(a1, a2, rn=rn)
-    e_split = sol.read_energy()[0]
+    e_form = sol.read_energy()[0]
     ref = FRICCSDGPU(E, {"m_keep": m}, precision="fp64")
     ref.update_amps(a1, a2, rn=rn)
-    d_e = abs(ref.read_energy()[0] - e_split)
+    d_e = abs(ref.read_energy()[0] - e_form)
     del ref
     torch.cuda.synchronize()
     lib.fricc_prof_enable(1)
@@ -252,22 +340,52 @@ def split_form_line(args, system, E, t1, t2, m, stream):
     ev1.record(stream)
     torch.cuda.synchronize()
     ms = ev0.elapsed_time(ev1)
+    p_ms, p_n, p_fl = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
+    _lib.check(lib.fricc_prof_read(ctypes.byref(p_ms), ctypes.byref(p_n), ctypes.byref(p_fl)))
     t_ms, t_n, t_fl = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
     _lib.check(lib.fricc_prof_read_tc(ctypes.byref(t_ms), ctypes.byref(t_n), ctypes.byref(t_fl)))
     lib.fricc_prof_enable(0)
     sol.read_energy()
-    sus = measured_peaks().get("bf16_tflops_sustained")
-    ach = t_fl.value / (t_ms.value / 1000.0) / 1e12 if t_ms.value > 0 else None
-    return {"value": args.steps / (ms / 1000.0), "unit": "iter/s", "ms_per_step": ms / args.steps,
-            "delta_e_vs_fp64_per_step": d_e,
-            "dtype": "split-BF16x3 on tcgen05 (FP32 accumulation); FP64 compression, denominators, energy",
-            "tensor_core": {"kernel": "k_gemm_tc (all tcgen05 GEMMs of the step)", "achieved": ach, "peak": sus,
-                            "unit": "TFLOP/s", "frac": (ach / sus) if (ach and sus) else None,
-                            "share_of_step": t_ms.value / ms if ms > 0 else None, "launches": int(t_n.value)}}
+    line = {"value": args.steps / (ms / 1000.0), "unit": "iter/s", "ms_per_step": ms / args.steps,
+            "delta_e_vs_fp64_per_step": d_e}
+    if precision == "split":
+        sus = measured_peaks().get("bf16_tflops_sustained")
+        ach = t_fl.value / (t_ms.value / 1000.0) / 1e12 if t_ms.value > 0 else None
+        line["dtype"] = "split-BF16x3 on tcgen05 (FP32 accumulation); FP64 compression, denominators, energy"
+        line["tensor_core"] = {
+            "kernel": "k_gemm_tc (all tcgen05 GEMMs of the step)", "achieved": ach, "peak": sus,
+            "unit": "TFLOP/s", "frac": (ach / sus) if (ach and sus) else None,
+            "flops_counted": "2 M N K' per launch (K' = 3 K): the zero-filled compressed T2 of the sparse "
+                             "terms included, so about 90% of the O^2V^4 term's counted flops multiply zeros",
+            "share_of_step": t_ms.value / ms if ms > 0 else None, "launches": int(t_n.value)}
+    else:
+        pk = fma_peaks_cached()["fp32"] / 12.0
+        ach = (p_fl.value / (p_ms.value / 1000.0)) / 1e12 if p_ms.value > 0 else None
+        line["dtype"] = "f64 storage; sparse terms and dense GEMMs in f32 pairs (48-bit products, ~40-bit sums)"
+        line["spmm"] = {"kernel": "k_spmm_df (bucketed sparse-T2 x dense-W, FP32 pairs)", "achieved": ach,
+                        "peak": pk, "unit": "TFLOP/s (FP64-equivalent)", "frac": (ach / pk) if ach else None,
+                        "peak_source": "FP32 FMA rate / 12 FP32 instructions per FP32-pair multiply-add",
+                        "share_of_step": p_ms.value / ms if ms > 0 else None, "launches": int(p_n.value),
+                        "traffic_per_launch_captured": SPMM_TRAFFIC_CAPTURED.get((precision, args.workload))}
+    del sol
+    return line
+
+
+_PEAKS = None
+
+
+def fma_peaks_cached(probe: bool = True):
+    global _PEAKS
+    if _PEAKS is None:
+        _PEAKS = fma_peaks(probe)
+    return _PEAKS
 
 
 # ------------------------------------------------------------------ GPU arm
 def run_gpu(args):
+    world, rank, local = dist_setup()
+    if rank == 0:
+        fma_peaks_cached(not args.no_peak_probe)  # the FMA probe runs before this process touches the GPU
     import torch
     import torch.distributed as dist
 
@@ -276,7 +394,6 @@ def run_gpu(args):
     from fricc_gb300.rccsd_dense import DeviceERIs
     from fricc_gb300.synthetic import WORKLOADS, make_system
 
-    world, rank, local = dist_setup()
     if world > 1:
         dist.init_process_group("nccl")
     torch.cuda.set_device(local)
@@ -320,34 +437,9 @@ def run_gpu(args):
             dist.barrier()
         torch.cuda.synchronize()
 
-    # the tensor-core rebuild of (vv|vv) alone (split precision): CUDA events
-    # around 3 rebuilds into the solver's own buffer, outside the timed region
-    tc_roof = None
-    if Es is not None:
-        R = Es.vvvv_rebuild
-        dense = solver._vvvv_bt is not None  # the rebuild the solver uses
-        rebuild = (lambda: R.rebuild_split_b(solver._vvvv_bt)) if dense else (lambda: R.rebuild(solver._vvvv_buf))
-        ra, rb = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-        rebuild()
-        ra.record(stream)
-        for _ in range(3):
-            rebuild()
-        rb.record(stream)
-        torch.cuda.synchronize()
-        R.check()
-        r_ms = ra.elapsed_time(rb) / 3
-        pk = measured_peaks().get("bf16_tflops")
-        ach = R.flops() / (r_ms / 1000.0) / 1e12
-        tc_roof = {"kernel": ("k_gemm_tc<EpiVvvvSplitB>" if dense else "k_gemm_tc<EpiVvvv>")
-                   + " ((vv|vv) rebuild, tcgen05 BF16, split-BF16x3, FP32 accumulation)",
-                   "bound": "tensor", "achieved": ach, "peak": pk, "unit": "TFLOP/s",
-                   "frac": ach / pk if pk else None, "ms": r_ms,
-                   "flops": R.flops(), "peak_source": "bf16_tflops (burst) of MEASURED_PEAKS.json"}
-
     lib.fricc_prof_enable(1)
     launches0 = lib.fricc_launch_count()
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    energies = []
     barrier()
     with ClockSampler(local) as clk:
         ev0.record(stream)
@@ -361,8 +453,10 @@ def run_gpu(args):
     _lib.check(lib.fricc_prof_read(ctypes.byref(p_ms), ctypes.byref(p_n), ctypes.byref(p_fl)))
     t_ms, t_n, t_fl = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
     _lib.check(lib.fricc_prof_read_tc(ctypes.byref(t_ms), ctypes.byref(t_n), ctypes.byref(t_fl)))
+    g_ms, g_n, g_fl = ctypes.c_double(), ctypes.c_longlong(), ctypes.c_double()
+    _lib.check(lib.fricc_prof_read_gemm(ctypes.byref(g_ms), ctypes.byref(g_n), ctypes.byref(g_fl)))
     lib.fricc_prof_enable(0)
-    energies.append(solver.read_energy()[0])
+    energy_last = solver.read_energy()[0]
 
     t_max = torch.tensor([ms], dtype=torch.float64, device=dev)
     if world > 1:
@@ -390,19 +484,22 @@ def run_gpu(args):
         nb = 8 * (o * v + o * o * v * v)
         e2e = {"value": world * args.steps / float(te.item()), "unit": "iter/s", "h2d_bytes_per_step": nb,
                "d2h_bytes_per_step": nb}
+    del solver
+    torch.cuda.empty_cache()
 
-    # the split-precision form on the same workload, as a secondary figure:
-    # integrals rebuilt from the BF16 hi+lo factor and every large
-    # contraction on the tcgen05 tensor cores (a different arithmetic, so not
-    # the headline); |dE| against the FP64 path for one step from the same
-    # state and draws
-    split_form = None
-    if args.precision == "df64" and world == 1 and not args.no_split_form:
-        try:
-            split_form = split_form_line(args, system, E, t1, t2, m, stream)
-        except Exception as ex:  # reported, never fatal to the headline
-            split_form = {"error": f"{type(ex).__name__}: {str(ex)[:300]}"}
-        torch.cuda.empty_cache()
+    # the other arithmetic forms on the same workload, as secondary figures
+    # (narrower arithmetic than FP64, so never the headline), each with its
+    # |dE| against the FP64 path for one step from the same state and draws
+    secondary = {}
+    if world == 1 and not args.no_secondary:
+        for form in ("df64", "split"):
+            if form == args.precision:
+                continue
+            try:
+                secondary[form + "_form"] = secondary_form_line(form, args, system, E, t1, t2, m, stream)
+            except Exception as ex:  # reported, never fatal to the headline
+                secondary[form + "_form"] = {"error": f"{type(ex).__name__}: {str(ex)[:300]}"}
+            torch.cuda.empty_cache()
 
     cpu = None
     if rank == 0 and world == 1 and not args.no_cpu_baseline:
@@ -410,29 +507,41 @@ def run_gpu(args):
         t1h, t2h = system.mp2_amplitudes()
         cpu = cpu_baseline_line(eris_np, t1h, t2h, m, args.workload, 7)
 
+    pk = fma_peaks_cached() if rank == 0 else {"fp64": FP64_PEAK_FALLBACK, "fp32": FP32_PEAK_FALLBACK,
+                                                "source": "recorded pool figures"}
     achieved = (p_fl.value / (p_ms.value / 1000.0)) / 1e12 if p_ms.value > 0 else None
     if args.precision == "fp64":
-        kname, bound, peak = "k_spmm (bucketed sparse-T2 x dense-W, FP64)", "fp64", FP64_PEAK_TFLOPS
-        psrc = "measured FP64 FMA rate of this GB300 pool (DFMA probe); FP64 is not in MEASURED_PEAKS.json"
+        kname, bound, peak = "k_spmm (bucketed sparse-T2 x dense-W, FP64)", "fp64-pipe", pk["fp64"]
+        psrc = f"FP64 FMA rate of this GPU, {pk['source']}; MEASURED_PEAKS.json has no FP64 figure"
     elif args.precision == "split":
         kname, bound, peak = "k_spmm_f32 (bucketed sparse-T2 x dense-W, FP32; terms too small for the tensor cores)", \
-            "fp32-pipe", FP32_PEAK_TFLOPS
-        psrc = ("FP32 FMA rate of this GB300 pool (74.2 TF/s, FFMA probe): one packed FMA per two outputs, "
-                "2 flops per multiply-add")
+            "fp32-pipe", pk["fp32"]
+        psrc = f"FP32 FMA rate of this GPU, {pk['source']}: one packed FMA per two outputs"
     else:
-        kname, bound, peak = "k_spmm_df (bucketed sparse-T2 x dense-W, FP32 pairs)", "fp32-pipe", FP32_PEAK_TFLOPS / 12
-        psrc = ("FP32 FMA rate of this GB300 pool (74.2 TF/s = 37.1 T instructions/s, FFMA probe) / 12 FP32 "
-                "instructions per FP32-pair multiply-add, counted as 2 FP64-equivalent flops")
+        kname, bound, peak = "k_spmm_df (bucketed sparse-T2 x dense-W, FP32 pairs)", "fp32-pipe", pk["fp32"] / 12
+        psrc = (f"FP32 FMA rate of this GPU ({pk['source']}) / 12 FP32 instructions per FP32-pair multiply-add, "
+                "counted as 2 FP64-equivalent flops")
+    traffic = SPMM_TRAFFIC_CAPTURED.get((args.precision, args.workload))
     roof = {"kernel": kname, "bound": bound,
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None,
-            "traffic": SPMM_TRAFFIC.get(args.workload) if args.precision == "df64" else None,
+            "traffic": None,
+            "traffic_per_launch_captured": traffic,
+            "traffic_note": ("DRAM bytes per launch are not measured live; the captured figures (when present) "
+                             "come from one single-pass ncu capture of an iteration of this workload"),
+            "flops_counted": "2 m Q per launch (m nonzeros, Q outputs per nonzero): algorithmic, no padding",
             "launches": int(p_n.value), "kernel_ms": p_ms.value,
             "kernel_share_of_step": p_ms.value / ms if ms > 0 else None,
             "peak_source": psrc}
+    gemm = None
+    if g_n.value:
+        g_ach = (g_fl.value / (g_ms.value / 1000.0)) / 1e12 if g_ms.value > 0 else None
+        gemm = {"kernel": "k_gemm_f64 (dense O^2V^3 / O^3V^2 contractions, FP64 DFMA)", "bound": "fp64-pipe",
+                "achieved": g_ach, "peak": pk["fp64"], "unit": "TFLOP/s",
+                "frac": (g_ach / pk["fp64"]) if g_ach else None, "launches": int(g_n.value),
+                "kernel_ms": g_ms.value, "kernel_share_of_step": g_ms.value / ms if ms > 0 else None}
     if args.precision == "split":
         # the dominant kernel of the split form: the tensor-core GEMMs
-        # (dense sparse terms, dense algebra, (vv|vv) rebuild), timed live
         sus = measured_peaks().get("bf16_tflops_sustained")
         tc_ach = (t_fl.value / (t_ms.value / 1000.0)) / 1e12 if t_ms.value > 0 else None
         sparse_roof = roof
@@ -443,35 +552,34 @@ def run_gpu(args):
                 "launches": int(t_n.value), "kernel_ms": t_ms.value,
                 "kernel_share_of_step": t_ms.value / ms if ms > 0 else None,
                 "flops_counted": "2 M N K' per launch (K' = 3 K, the three BF16 products; zero padding and the "
-                                 "zeros of the compressed T2 included)",
+                                 "zeros of the compressed T2 included: about 90% of the O^2V^4 term's counted "
+                                 "flops multiply zeros)",
                 "peak_source": "bf16_tflops_sustained of MEASURED_PEAKS.json (kernels timed inside the step)",
                 "sparse_kernel": sparse_roof if sparse_roof.get("launches") else None}
+    dtypes = {"fp64": "f64",
+              "df64": "f64 storage; sparse terms and dense GEMMs in f32 pairs (48-bit products, ~40-bit sums)",
+              "split": ("f64 (compression, denominators, energy); (vv|vv), (ov|vv), (oo|vv) and the large "
+                        "contractions split-BF16x3 on tcgen05 with FP32 accumulation")}
     if rank == 0:
         line = {
             "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None,
-            "dtype": "f64" if args.precision == "fp64" else "f64 (sparse terms in f32 pairs: 48-bit products, ~40-bit sums)",
-            "data": "synthetic",
-            "config": {"workload": f"{args.workload}: nocc={o} nvir={v} naux={w['naux']} sigma={w['sigma']} "
-                                   f"m={m} FRI systematic, 2 compressions/iteration, FP64",
+            "scaling": "weak", "vs_baseline": None, "dtype": dtypes[args.precision], "data": "synthetic",
+            "config": {"workload": workload_text(args.workload, o, v, w),
                        "parallelism": "replicas" if world > 1 else "single GPU",
-                       "l2": f"working set > L2 ((ac|bd) {8 * v ** 4 / 1e9:.2f} GB and its float-pair copy "
-                             "streamed by the O^2V^4 term every step)",
+                       "l2": (f"working set > L2: the (ac|bd) block ({8 * v ** 4 / 1e9:.2f} GB FP64) is streamed "
+                              "by the O^2V^4 term every step" if args.precision != "split" else
+                              "working set > L2: (ac|bd) rebuilt every step as a split-BF16x3 operand "
+                              f"({12 * v ** 4 / 1e9:.2f} GB) and streamed by the O^2V^4 GEMM"),
                        "precision": args.precision, "autotune": bool(args.autotune),
                        "cuda_graph": bool(args.graph)},
             "e2e": e2e, "gpu_launches": int(launches), "roofline": roof, "cpu_baseline": cpu,
-            "clocks": clk.summary(), "energy_last": energies[-1],
+            "clocks": clk.summary(), "energy_last": energy_last,
             "delta_e_vs_fp64_per_step": delta_e,
         }
-        if split_form is not None:
-            line["split_form"] = split_form
-        if tc_roof is not None:
-            line["tensor_core_rebuild"] = tc_roof
-            line["dtype"] = ("f64 (compression, denominators, energy); (vv|vv), (ov|vv), (oo|vv) split-BF16x3 on "
-                             "tcgen05 with FP32 accumulation; sparse terms in f32 pairs")
-            line["config"]["l2"] = (f"working set > L2 ((ac|bd) rebuilt in FP32, {4 * v ** 4 / 1e9:.2f} GB, "
-                                    "streamed by the O^2V^4 term every step)")
+        if gemm is not None:
+            line["dense_gemm"] = gemm
+        line.update(secondary)
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()
@@ -503,15 +611,34 @@ def run_reference(args):
         eris_np = P.make_eris(system)
     t1, t2 = system.mp2_amplitudes()
     m = w["m"]
-    pairs = 4 * cores
+    n_blocks = n_blocks_for(args.steps)
+    if args.validate_sample:
+        # the same iteration (same amplitudes and draws) in full, and as the
+        # n_blocks block estimates a run of that many steps adds up
+        full, per_full = cpu_full_iteration(eris_np, t1, t2, m, seeded_draws(1000))
+        blocks = []
+        per_blocks = {}
+        for b in range(n_blocks):
+            est, wall, _, per = cpu_sampled_iteration(eris_np, t1, t2, m, n_blocks, b, seeded_draws(1000))
+            blocks.append({"block": b, "estimate_s": est, "wall_s": wall})
+            for k, v in per.items():
+                per_blocks[k] = per_blocks.get(k, 0.0) + v / n_blocks
+        mean_est = sum(x["estimate_s"] for x in blocks) / n_blocks
+        print(json.dumps({"validate_sample": args.workload, "cores": cores, "n_blocks": n_blocks,
+                          "full_s": full, "mean_block_estimate_s": mean_est,
+                          "ratio_estimate_over_full": mean_est / full, "blocks": blocks,
+                          "terms_mean_estimate_s": per_blocks,
+                          "terms_full_s": {k: v for k, v in per_full.items() if k != "compress"},
+                          "compress_s": per_full.get("compress")}))
+        return
     draw = seeded_draws(1000)
     # warm-up: one small compression (the CPU path has nothing to warm)
     for _ in range(args.warmup):
         fri_oracle.fri_compression(t2.ravel()[:100000], 1000, rn=0.5)
     per = []
     walls = []
-    for _ in range(args.steps):
-        secs, wall, _ = cpu_sampled_iteration(eris_np, t1, t2, m, pairs, draw)
+    for step in range(args.steps):
+        secs, wall, _, _ = cpu_sampled_iteration(eris_np, t1, t2, m, n_blocks, step, draw)
         per.append(secs)
         walls.append(wall)
     total = sum(per)
@@ -519,12 +646,12 @@ def run_reference(args):
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
+        "timed_wall_ms_per_step": 1000.0 * sum(walls) / args.steps, "extrapolated": True,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": f"{args.workload}: nocc={system.nocc} nvir={system.nvir} naux={w['naux']} "
-                               f"sigma={w['sigma']} m={m} FRI systematic, 2 compressions/iteration, FP64",
-                   "parallelism": "host cores"},
-        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": cores, "kind": "port",
-                         "sample": _sample_text(args.workload, cores, pairs, sum(walls))},
+        "config": {"workload": workload_text(args.workload, system.nocc, system.nvir, w),
+                   "parallelism": "host cores", "precision": "fp64"},
+        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": cores, "kind": "port", "extrapolated": True,
+                         "sample": _sample_text(args.workload, cores, n_blocks, sum(walls), args.steps)},
         "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }

@@ -70,6 +70,13 @@ SIGNATURES = [
                                                   _vp, _vp]),
     ("fricc_gemm_df", ctypes.c_int, [_dp, _dp, _dp, _i64, _i64, _i64, _i64, _i64p, _i64p, _i64p, ctypes.c_double,
                                       ctypes.c_double, _vp]),
+    ("fricc_gemm_f64", ctypes.c_int, [_dp, _dp, _dp, _i64, _i64, _i64, _i64, _i64p, _i64p, _i64p, ctypes.c_double,
+                                       ctypes.c_double, _vp]),
+    ("fricc_combine", ctypes.c_int, [_i64p, ctypes.c_int, _vpp, _i64p, ctypes.c_int, _vpp, _i64p, ctypes.c_int,
+                                      _vpp, _i64p, ctypes.POINTER(ctypes.c_double), ctypes.c_int, _vp]),
+    ("fricc_zero", ctypes.c_int, [_vp, _i64, _vp]),
+    ("fricc_phase_timing_set", ctypes.c_int, [ctypes.c_int]),
+    ("fricc_phase_timing_read", ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     ("fricc_contract_flops", ctypes.c_double, [ctypes.c_char_p, _vp]),
     ("fricc_compress", ctypes.c_int, [_dp, _i64, _i64, ctypes.c_int, ctypes.c_double, _dp, _dp, _i64p, _vp]),
     ("fricc_compress_pivotal", ctypes.c_int, [_dp, _i64, _i64, _u32p, _dp, _dp, _i64p, _i64p, _vp]),
@@ -80,6 +87,7 @@ SIGNATURES = [
     ("fricc_stream_create", ctypes.c_int, [ctypes.POINTER(_vp)]),
     ("fricc_stream_destroy", ctypes.c_int, [_vp]),
     ("fricc_launch_count", ctypes.c_longlong, []),
+    ("fricc_alloc_count", ctypes.c_longlong, []),
     ("fricc_tune_set", ctypes.c_int, [ctypes.c_int, ctypes.c_int]),
     ("fricc_symadd", ctypes.c_int, [_dp, _dp, _i64, _i64, _i64p, ctypes.c_double, _vp]),
     ("fricc_prof_enable", None, [ctypes.c_int]),
@@ -87,6 +95,8 @@ SIGNATURES = [
                                        ctypes.POINTER(ctypes.c_double)]),
     ("fricc_prof_read_tc", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
                                           ctypes.POINTER(ctypes.c_double)]),
+    ("fricc_prof_read_gemm", ctypes.c_int, [ctypes.POINTER(ctypes.c_double), ctypes.POINTER(ctypes.c_longlong),
+                                            ctypes.POINTER(ctypes.c_double)]),
     ("fricc_energy_update", ctypes.c_int, [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _i64, _dp, _dp, _dp, _vp]),
     ("fricc_energy_update_lin", ctypes.c_int, [_dp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _i64, _dp, _dp, _dp, _vp]),
 ]

@@ -17,7 +17,7 @@ CSRC = os.path.join(HERE, "csrc")
 BUILD = os.path.join(os.path.dirname(HERE), "_build")
 LIBDIR = os.path.join(HERE, "_lib")
 LIB = os.path.join(LIBDIR, "libfricc_gb300.so")
-SOURCES = ["abi.cu", "compress.cu", "contract.cu", "energy.cu", "gemm_df.cu", "gemm_tc.cu", "glibc_rand.cu", "noalloc.cu", "symadd.cu"]
+SOURCES = ["abi.cu", "combine.cu", "compress.cu", "contract.cu", "energy.cu", "gemm_df.cu", "gemm_f64.cu", "gemm_tc.cu", "glibc_rand.cu", "noalloc.cu", "symadd.cu"]
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 FLAGS = ["-O3", "-std=c++17", "-lineinfo", "-Xcompiler", "-fPIC", "--expt-relaxed-constexpr"]
 

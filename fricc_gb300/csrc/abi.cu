@@ -36,6 +36,12 @@ int fricc_densify_bf16x3_device(FriccSparse* T, int pa, int pb, int ka, int kb, 
 int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
                          const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
                          cudaStream_t st);
+int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N,
+                          int64_t K, const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha,
+                          double beta, cudaStream_t st);
+int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x, const int64_t* sx, int n_prod,
+                         const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
+                         const double* coef, int accumulate, cudaStream_t st);
 int fricc_energy_update_device(const double* t1num, const double* t2num, const double* eia, const double* fov,
                                const double* ovov, const double* t1old, const double* t2old, int64_t o, int64_t v,
                                double* t1out, double* t2out, double* res, cudaStream_t st, bool linear);
@@ -65,21 +71,24 @@ int fricc_cuda_fail(cudaError_t e, const char* what, const char* file, int line)
 #include <atomic>
 #include <vector>
 static std::atomic<long long> g_launches{0};
+static std::atomic<long long> g_allocs{0};
 static std::atomic<bool> g_prof{false};
 static std::mutex g_prof_mu;
-// channel 0: the sparse contraction kernels; channel 1: the tensor-core GEMMs
-static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_prof_ev[2];
-static std::vector<double> g_prof_flops[2];
-static cudaEvent_t g_prof_pending[2] = {nullptr, nullptr};
+// channel 0: the sparse contraction kernels; channel 1: the tensor-core
+// GEMMs; channel 2: the FP64 GEMMs
+constexpr int kProfChannels = 3;
+static std::vector<std::pair<cudaEvent_t, cudaEvent_t>> g_prof_ev[kProfChannels];
+static std::vector<double> g_prof_flops[kProfChannels];
+static cudaEvent_t g_prof_pending[kProfChannels] = {nullptr, nullptr, nullptr};
 
 void fricc_note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
-static thread_local int g_tune[FRICC_TUNE_KNOBS] = {-1, -1, -1};
+static thread_local int g_tune[FRICC_TUNE_KNOBS] = {-1, -1, -1, -1};
 int fricc_tune_get(int knob) { return knob >= 0 && knob < FRICC_TUNE_KNOBS ? g_tune[knob] : -1; }
 bool fricc_prof_on() { return g_prof.load(std::memory_order_relaxed); }
 
 void fricc_prof_record(cudaStream_t st, bool start, double flops, int ch) {
-  if (ch < 0 || ch > 1) return;
+  if (ch < 0 || ch >= kProfChannels) return;
   std::lock_guard<std::mutex> lk(g_prof_mu);
   cudaEvent_t e;
   if (cudaEventCreate(&e) != cudaSuccess) return;
@@ -111,6 +120,7 @@ int fricc_alloc(void** p, size_t bytes, cudaStream_t s) {
       }
     });
   }
+  g_allocs.fetch_add(1, std::memory_order_relaxed);
   cudaError_t e = cudaMallocAsync(p, bytes ? bytes : 16, s);
   if (e != cudaSuccess) {
     *p = nullptr;
@@ -160,8 +170,10 @@ int fricc_version(void) { return 100; }
 
 long long fricc_launch_count(void) { return g_launches.load(); }
 
+long long fricc_alloc_count(void) { return g_allocs.load(); }
+
 int fricc_tune_set(int knob, int value) {
-  static const int lo[FRICC_TUNE_KNOBS] = {1, 0, 1}, hi[FRICC_TUNE_KNOBS] = {4, 3, 16};
+  static const int lo[FRICC_TUNE_KNOBS] = {1, 0, 1, 1}, hi[FRICC_TUNE_KNOBS] = {4, 3, 16, 1 << 20};
   if (knob < 0 || knob >= FRICC_TUNE_KNOBS || (value != -1 && (value < lo[knob] || value > hi[knob]))) {
     fricc_set_error("tune_set: bad knob or value");
     return FRICC_ERR_ARG;
@@ -177,7 +189,7 @@ int fricc_tune_set(int knob, int value) {
 void fricc_prof_enable(int on) {
   std::lock_guard<std::mutex> lk(g_prof_mu);
   g_prof.store(on != 0);
-  for (int ch = 0; ch < 2; ++ch) {
+  for (int ch = 0; ch < kProfChannels; ++ch) {
     for (auto& pr : g_prof_ev[ch]) {
       cudaEventDestroy(pr.first);
       cudaEventDestroy(pr.second);
@@ -209,6 +221,8 @@ static int prof_read(int ch, double* ms, long long* launches, double* flops) {
 int fricc_prof_read(double* ms, long long* launches, double* flops) { return prof_read(0, ms, launches, flops); }
 
 int fricc_prof_read_tc(double* ms, long long* launches, double* flops) { return prof_read(1, ms, launches, flops); }
+
+int fricc_prof_read_gemm(double* ms, long long* launches, double* flops) { return prof_read(2, ms, launches, flops); }
 
 const char* fricc_last_error(void) { return g_err; }
 
@@ -617,6 +631,32 @@ int fricc_gemm_df(const double* A, const double* B, double* C, int64_t batch, in
     return FRICC_ERR_ARG;
   }
   return fricc_gemm_df_device(A, B, C, batch, M, N, K, sA, sB, sC, alpha, beta, as_stream(stream));
+}
+
+int fricc_gemm_f64(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
+                  const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
+                  void* stream) {
+  if (!sA || !sB || !sC) {
+    fricc_set_error("gemm_f64: null stride array");
+    return FRICC_ERR_ARG;
+  }
+  return fricc_gemm_f64_device(A, B, C, batch, M, N, K, sA, sB, sC, alpha, beta, as_stream(stream));
+}
+
+int fricc_combine(const int64_t dims[4], int n_in, const double* const* x, const int64_t* sx, int n_prod,
+                  const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
+                  const double* coef, int accumulate, void* stream) {
+  return fricc_combine_device(dims, n_in, x, sx, n_prod, p, sp, n_out, out, so, coef, accumulate, as_stream(stream));
+}
+
+int fricc_zero(void* p, int64_t bytes, void* stream) {
+  if (bytes < 0 || (!p && bytes > 0)) {
+    fricc_set_error("zero: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  if (bytes == 0) return FRICC_OK;
+  FRICC_CUDA(cudaMemsetAsync(p, 0, (size_t)bytes, as_stream(stream)));
+  return FRICC_OK;
 }
 
 double fricc_contract_flops(const char* term, const fricc_sparse* T) {

@@ -114,7 +114,11 @@ void fricc_note_launch(int n = 1);
 #define FRICC_TUNE_SPMM_PPT 0
 #define FRICC_TUNE_GEMM_TILE 1
 #define FRICC_TUNE_GEMM_COVER 2
-#define FRICC_TUNE_KNOBS 3
+// test only: before its look-back, tile 1 of a compression's compaction
+// polls a word nothing sets this many times, then reports FRICC_DEV_TIMEOUT
+// (the compaction itself then runs as usual, so every result stays valid)
+#define FRICC_TUNE_TEST_WAIT 3
+#define FRICC_TUNE_KNOBS 4
 int fricc_tune_get(int knob);
 bool fricc_prof_on();
 void fricc_prof_record(cudaStream_t st, bool start, double flops, int channel = 0);

@@ -83,7 +83,8 @@ constexpr long long SPIN_LIMIT = 1ll << 22;
 // count and looks back over its predecessors for its output offset.
 __global__ void __launch_bounds__(256) k_compact(const double* __restrict__ x, int64_t n, const Ctl* __restrict__ c,
                                                  unsigned long long* __restrict__ ckey, unsigned* __restrict__ cidx,
-                                                 unsigned long long* tstate, unsigned* ticket, unsigned* err) {
+                                                 unsigned long long* tstate, unsigned* ticket, unsigned* err,
+                                                 const unsigned long long* never_set, long long test_spins) {
   constexpr int NT = 256, ITEMS = 16, TILE = NT * ITEMS;
   const unsigned dmin = (unsigned)c->dmin;
   __shared__ int s_tile;
@@ -109,6 +110,16 @@ __global__ void __launch_bounds__(256) k_compact(const double* __restrict__ x, i
       atomicExch(&tstate[0], ST_INCL | (unsigned long long)tot);
     } else {
       atomicExch(&tstate[tile], ST_AGG | (unsigned long long)tot);
+      if (test_spins > 0 && tile == 1) {
+        // test only: a bounded wait on a word nothing sets runs out
+        long long w = 0;
+        while (ld_acquire(never_set) == 0ull) {
+          if (++w > test_spins) {
+            atomicOr(err, FRICC_DEV_TIMEOUT);
+            break;
+          }
+        }
+      }
       int j = tile - 1;
       long long spins = 0;
       while (j >= 0) {
@@ -810,6 +821,54 @@ static double host_glibc_uniform(unsigned* h) {
 
 // Steps of pivotal sampling after D, R and m' are on the device (ctl): the
 // weight walk, the draws, the decisions, the scans; leaves S (m' indices).
+// Phase timing of a compression (the reference's verbose table,
+// src/fri_utils.cpp:509-519): CUDA events at the phase boundaries of the
+// calling thread's compressions while enabled.  Boundaries: 0 start, 1 the
+// largest elements and the remaining norm (the reference's "Sorting":
+// get_d_largest), 2 the probability vector, 3 the samples, 4 the outputs
+// ("Wrap up").
+struct PhaseTimer {
+  bool on = false;
+  bool recorded = false;
+  cudaEvent_t ev[5] = {nullptr, nullptr, nullptr, nullptr, nullptr};
+};
+static thread_local PhaseTimer g_phase;
+
+static void phase_mark(int k, cudaStream_t st) {
+  if (!g_phase.on) return;
+  if (!g_phase.ev[k] && cudaEventCreate(&g_phase.ev[k]) != cudaSuccess) {
+    g_phase.ev[k] = nullptr;
+    return;
+  }
+  cudaEventRecord(g_phase.ev[k], st);
+  if (k == 4) g_phase.recorded = true;
+}
+
+extern "C" int fricc_phase_timing_set(int on) {
+  g_phase.on = on != 0;
+  g_phase.recorded = false;
+  return FRICC_OK;
+}
+
+// Seconds of each phase of the calling thread's last timed compression:
+// sorting, P vector, sampling, wrap up, total (waits for its events).
+extern "C" int fricc_phase_timing_read(double sec[5]) {
+  if (!sec) {
+    fricc_set_error("phase_timing_read: null output");
+    return FRICC_ERR_ARG;
+  }
+  if (!g_phase.recorded) {
+    fricc_set_error("phase_timing_read: no compression was timed on this thread");
+    return FRICC_ERR_ARG;
+  }
+  float ms[5] = {0, 0, 0, 0, 0};
+  FRICC_CUDA(cudaEventSynchronize(g_phase.ev[4]));
+  for (int k = 0; k < 4; ++k) FRICC_CUDA(cudaEventElapsedTime(&ms[k], g_phase.ev[k], g_phase.ev[k + 1]));
+  FRICC_CUDA(cudaEventElapsedTime(&ms[4], g_phase.ev[0], g_phase.ev[4]));
+  for (int k = 0; k < 5; ++k) sec[k] = ms[k] * 1e-3;
+  return FRICC_OK;
+}
+
 static int pivotal(const double* x, int64_t n, int64_t m, const GenP& gp, Ctl* ctl, CompressScratch& s,
                    unsigned* glibc_hist, int64_t* n_draws, cudaStream_t st) {
   (void)x;
@@ -828,6 +887,7 @@ static int pivotal(const double* x, int64_t n, int64_t m, const GenP& gp, Ctl* c
   if (!rc) {
     k_zero_u32<<<grid_for(m, 256), 256, 0, st>>>(s.S, m);
     k_pvec<<<grid_for(n, 256), 256, 0, st>>>(gp, n, P, s.err);
+    phase_mark(2, st);
     k_piv_chain<<<1, 32, 0, st>>>(P, n, ctl, A, code);
     fricc_note_launch(3);
     rc = fricc_cuda_check(cudaGetLastError(), "pivotal chain");
@@ -915,12 +975,12 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     TRY(fricc_alloc_t(&s.cidx, n, st));
     TRY(fricc_alloc_t(&s.ktmp, n, st));
     TRY(fricc_alloc_t(&s.vtmp, n, st));
-    TRY(fricc_alloc_t(&s.tstate, ntile, st));
+    TRY(fricc_alloc_t(&s.tstate, ntile + 1, st));  // + a zero word no tile writes (the test-only wait)
     TRY(fricc_alloc_t(&s.ticket, 1, st));
     TRY(fricc_alloc_t(&s.rhist, radix::hist_words(n), st));
     TRY(fricc_cuda_check(cudaMemsetAsync(s.hist, 0, NDIG * sizeof(unsigned), st), "memset"));
     TRY(fricc_cuda_check(cudaMemsetAsync(s.err, 0, sizeof(unsigned), st), "memset"));
-    TRY(fricc_cuda_check(cudaMemsetAsync(s.tstate, 0, ntile * sizeof(unsigned long long), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.tstate, 0, (ntile + 1) * sizeof(unsigned long long), st), "memset"));
     TRY(fricc_cuda_check(cudaMemsetAsync(s.ticket, 0, sizeof(unsigned), st), "memset"));
     TRY(fricc_cuda_check(cudaMemsetAsync(ctl, 0, sizeof(Ctl), st), "memset"));
     if (rn_dev) {
@@ -934,15 +994,21 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     }
 
     // 1-2. select digit, candidates, sort (argsort, src/fri_utils.cpp:11-36)
+    phase_mark(0, st);
     k_hist12<<<grid_for(n, 256), 256, 0, st>>>(x, n, s.hist);
     k_select_digit<<<1, 1, 0, st>>>(s.hist, m, ctl);
-    k_compact<<<(unsigned)ntile, 256, 0, st>>>(x, n, ctl, s.ckey, s.cidx, s.tstate, s.ticket, s.err);
+    k_compact<<<(unsigned)ntile, 256, 0, st>>>(x, n, ctl, s.ckey, s.cidx, s.tstate, s.ticket, s.err,
+                                               s.tstate + ntile, (long long)fricc_tune_get(FRICC_TUNE_TEST_WAIT));
     fricc_note_launch(3);
     TRY(radix::sort_pairs(s.ckey, s.cidx, s.ktmp, s.vtmp, n, 64, true, s.rhist, st, &ctl->ncand));
 
     if (mode == 1) {  // "largest": argsort(x, m) with unscaled values
+      phase_mark(1, st);
+      phase_mark(2, st);
+      phase_mark(3, st);
       k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, nullptr, flat, vals);
       fricc_note_launch();
+      phase_mark(4, st);
       if (meta) {
         k_put_meta<<<1, 1, 0, st>>>(nullptr, m, s.err, meta);
         fricc_note_launch();
@@ -979,6 +1045,7 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     if (rc) goto done;
     k_finish_d<<<1, 1, 0, st>>>(s.ffail, s.Rb, s.ckey, s.cidx, m, ctl);
     fricc_note_launch();
+    phase_mark(1, st);
     if (pair) {  // the second compression: the same state, its own draw
       TRY(fricc_alloc_t(&ctl2, 1, st));
       TRY(fricc_cuda_check(cudaMemcpyAsync(ctl2, ctl, sizeof(Ctl), cudaMemcpyDeviceToDevice, st), "ctl"));
@@ -994,9 +1061,11 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     GenP gp{x, ctl};
     if (mode == 2) {
       TRY(pivotal(x, n, m, gp, ctl, s, glibc_hist, n_draws, st));
+      phase_mark(3, st);
       k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, ctl, flat, vals);
       k_out_s<<<grid_for(m, 256), 256, 0, st>>>(gp, s.S, flat, vals);
       fricc_note_launch(2);
+      phase_mark(4, st);
       if (meta) {
         k_put_meta<<<1, 1, 0, st>>>(ctl, 0, s.err, meta);
         fricc_note_launch();
@@ -1018,6 +1087,7 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     k_zero_u32<<<grid_for(m, 256), 256, 0, st>>>(s.S, m);
     k_pvec<<<grid_for(n, 256), 256, 0, st>>>(gp, n, s.P, s.err);
     fricc_note_launch(2);
+    phase_mark(2, st);
     // with m' = 0 every p is 0 (or NaN); with R <= 0 or not finite no
     // interval matches (ConsSample checks ctl->sample): in both cases all
     // samples keep index 0, as in the reference
@@ -1034,9 +1104,11 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
     }
 
     // 6. output
+    phase_mark(3, st);
     k_out_d<<<grid_for(m, 256), 256, 0, st>>>(x, s.cidx, m, ctl, flat, vals);
     k_out_s<<<grid_for(m, 256), 256, 0, st>>>(gpv, s.S, flat, vals);
     fricc_note_launch(2);
+    if (!pair) phase_mark(4, st);
     if (meta) {
       k_put_meta<<<1, 1, 0, st>>>(ctl, 0, s.err, meta);
       fricc_note_launch();
@@ -1047,6 +1119,7 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
       k_out_s<<<grid_for(m, 256), 256, 0, st>>>(gpv2, S2, pair->flat, pair->vals);
       k_put_meta<<<1, 1, 0, st>>>(ctl2, 0, s.err, pair->meta);
       fricc_note_launch(3);
+      phase_mark(4, st);
     }
     TRY(fricc_cuda_check(cudaGetLastError(), "output"));
     if (n_largest) {

@@ -17,7 +17,10 @@
 //   library, until the process exits.
 // * The first call on a device looks up the array's device address for
 //   that device (cudaGetSymbolAddress, once per device, with that device
-//   current); make that first call before any stream capture begins.
+//   current; a failed lookup is retried by the next call); make that first
+//   call before any stream capture begins.  The address is kept for the
+//   life of the process: a process that resets a device
+//   (cudaDeviceReset) must not call this entry point on it afterwards.
 // * Every call uses the same array: two calls whose work overlaps on the
 //   GPU (different streams, no ordering between them) race and corrupt
 //   each other's results.  Calls ordered on one stream are safe.  Each call
@@ -53,11 +56,12 @@ struct ConsWriteNA {
   __device__ __forceinline__ void operator()(int64_t i, double, double after, double) const { out[i] = after; }
 };
 
-std::once_flag g_once[64];
+std::mutex g_mu[64];
 unsigned char* g_ptr[64] = {};
-cudaError_t g_setup_err[64] = {};
 
-// Device address of g_scratch for the current device (looked up once per device).
+// Device address of g_scratch for the current device, looked up on the
+// first successful call on that device and kept from then on.  A lookup
+// that fails is not remembered: the next call tries again.
 int scratch_for_current_device(unsigned char** p) {
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -66,13 +70,17 @@ int scratch_for_current_device(unsigned char** p) {
     fricc_set_error("seq_cumsum_noalloc: device ordinal %d out of range", dev);
     return FRICC_ERR_ARG;
   }
-  std::call_once(g_once[dev], [dev]() {
+  std::lock_guard<std::mutex> lk(g_mu[dev]);
+  if (!g_ptr[dev]) {
     void* ptr = nullptr;
-    g_setup_err[dev] = cudaGetSymbolAddress(&ptr, g_scratch);
+    e = cudaGetSymbolAddress(&ptr, g_scratch);
+    if (e != cudaSuccess) return fricc_cuda_fail(e, "cudaGetSymbolAddress(g_scratch)", __FILE__, __LINE__);
+    if (!ptr) {
+      fricc_set_error("seq_cumsum_noalloc: cudaGetSymbolAddress(g_scratch) gave a null address");
+      return FRICC_ERR_CUDA;
+    }
     g_ptr[dev] = static_cast<unsigned char*>(ptr);
-  });
-  if (g_setup_err[dev] != cudaSuccess || !g_ptr[dev])
-    return fricc_cuda_fail(g_setup_err[dev], "cudaGetSymbolAddress(g_scratch)", __FILE__, __LINE__);
+  }
   *p = g_ptr[dev];
   return FRICC_OK;
 }

@@ -13,7 +13,8 @@ and ``kernel`` (:379-456) on the device:
 * the denominators, the CCSD energy and the step norm fused in
   ``fricc_energy_update``;
 * the dense remainder (Fock-like intermediates, the T1 equation, the dense
-  W builds) as cuBLAS GEMMs through torch.
+  W builds) as GEMMs of the library: FP64 DFMA (``fricc_gemm_f64``), FP32
+  pairs (df64) or split-BF16x3 on the tensor cores (split).
 
 Settings are the reference's ``fri_settings`` keys.  The reference reads
 ``fri_settings["unbiased"]`` (:109), a key its defaults never set (they set
@@ -262,7 +263,7 @@ class FRICCSDGPU:
         graph and replayed: the host work per iteration drops to a few copies
         and one launch, and the results are the same as eager execution."""
         s = self.settings
-        if (self.graph and t1_old is None and t2_old is None and not s.get("unbiased", False)
+        if (self.graph and t1_old is None and t2_old is None and not s.get("unbiased", False) and not s["verbose"]
                 and not (s["compression"] == "fri" and s["sampling_method"] == "pivotal")
                 and self._sp.h.value):
             return self._update_graph(t1, t2, rn)
@@ -335,9 +336,7 @@ class FRICCSDGPU:
         ov = o * v
         st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
         t2 = t2.contiguous()
-        e_o = E.mo_energy[:o]
-        e_v = E.mo_energy[o:] + self.level_shift
-        fov = E.fock[:o, o:]
+        t1 = t1.contiguous()
         ein = torch.einsum
         need_w = "O^3V^3" in comp or "O^4V^2" in comp
         piv = s["compression"] == "fri" and s["sampling_method"] == "pivotal"
@@ -356,8 +355,9 @@ class FRICCSDGPU:
             # both compressions of the same T2 (systematic FRI, no running
             # average): one paired pass, bit-identical to two
             ws = t2 if (rn_dev is not None or not need_w) else self._w_source(t2)  # once: it may update
+            verbose = bool(s["verbose"]) and rn_dev is None   # one phase table per compression, as the reference
             paired = (need_w and s["compression"] == "fri" and s["sampling_method"] == "systematic"
-                      and self._sp.ready_for(t2, m) and self._sp_w.ready_for(t2, m) and ws is t2)
+                      and self._sp.ready_for(t2, m) and self._sp_w.ready_for(t2, m) and ws is t2 and not verbose)
             if paired and rn_dev is not None:  # captured: draws from device memory
                 L.check(self.lib.fricc_sp_recompress_pair_dev(self._sp.h, self._sp_w.h, _ptr(t2),
                                                               ctypes.c_void_p(rn_dev.data_ptr()), sst))
@@ -371,8 +371,9 @@ class FRICCSDGPU:
                 Tw = self._sp_w.compress_dev(t2, m, s["compression"], ctypes.c_void_p(rn_dev.data_ptr() + 8),
                                              sst) if need_w else None
             else:
-                T = _compress(self._sp, t2, m, s, rn[0], self.rn_draw, sst)
-                Tw = _compress(self._sp_w, ws, m, s, rn[1], self.rn_draw, sst) if need_w else None
+                T = self._timed(verbose, lambda: _compress(self._sp, t2, m, s, rn[0], self.rn_draw, sst))
+                Tw = self._timed(verbose, lambda: _compress(self._sp_w, ws, m, s, rn[1], self.rn_draw, sst)) \
+                    if need_w else None
         if rn_dev is None:
             self._iter += 1
 
@@ -385,10 +386,8 @@ class FRICCSDGPU:
                                a_split=E.tc(const, "A") if const else None,
                                b_split=E.tc(const_b, "B") if const_b else None)
 
-            def ein2(spec, A_, B_):
-                return D.einsum_df(spec, A_, B_, gemm=mm)
         else:
-            mm0 = D.gemm_df if self._df else D.gemm_torch
+            mm0 = D.gemm_df if self._df else D.gemm_f64
             tuner = self._tuner
 
             def mm(A_, B_, C_, alpha=1.0, beta=0.0, const=None, const_b=None):
@@ -400,97 +399,134 @@ class FRICCSDGPU:
                 tuner.run(key, GEMM_CANDIDATES, lambda outs: mm0(A_, B_, outs[0], alpha, beta), [C_])
                 return C_
 
-            if self._df:
-                def ein2(spec, A_, B_):   # two-operand O^3V^2 contractions
-                    return D.einsum_df(spec, A_, B_, gemm=mm)
-            else:
-                ein2 = torch.einsum
         f64, dev = t2.dtype, t2.device
-        # cc_Foo / cc_Fvv share tt[p,q,r,s] = t2 + t1[p,r] t1[q,s]
-        tt = t2 + ein("pr,qs->pqrs", t1, t1)
-        Foo0 = E.fock[:o, :o].clone()                     # f_ki + sum_lcd g[k,c,l,d] tt[i,l,c,d]
+        comb, mmf = D.combine, D.gemm_f64   # elementwise passes; small GEMMs and GEMVs, FP64 in every form
+        C = self._constants(o, v)
+        fov, e_o, e_v = C["fov"], C["e_o"], C["e_v"]
+
+        def new(*shape):
+            return torch.empty(*shape, dtype=f64, device=dev)
+
+        def ein2(spec, A_, B_, out=None, alpha=1.0, beta=0.0):   # two-operand contractions on mm
+            return D.einsum_df(spec, A_, B_, gemm=mm, out=out, alpha=alpha, beta=beta)
+
+        # cc_Foo / cc_Fvv share tt[p,q,r,s] = t2 + t1[p,r] t1[q,s]; cc_Fvv reads it as [r,p,q,s]
+        tt, ttp = new(o, o, v, v), new(v, o, o, v)
+        comb([tt, ttp.permute(1, 2, 0, 3)], [t2], [[1.0, 1.0], [1.0, 1.0]],
+             prod=[t1[:, None, :, None], t1[None, :, None, :]])
+        Foo0 = new(o, o)                                   # f_ki + sum_lcd g[k,c,l,d] tt[i,l,c,d]
+        comb([Foo0], [C["foo"]])
         mm(E.g_klcd.view(o, o * v * v), tt.view(o, o * v * v).T, Foo0, 1.0, 1.0, const="g_klcd")
-        Fvv0 = E.fock[o:, o:].clone()                     # f_ac - sum_kld g[k,c,l,d] tt[k,l,a,d]
-        mm(tt.permute(2, 0, 1, 3).contiguous().view(v, o * o * v), E.g_kldc.view(o * o * v, v), Fvv0, -1.0, 1.0,
-           const_b="g_kldc")
-        del tt
-        Fov = D.cc_Fov(t1, t2, E)
-        Foo = Foo0.clone()
-        Fvv = Fvv0.clone()
-        Foo.diagonal().sub_(e_o)
-        Fvv.diagonal().sub_(e_v)
+        Fvv0 = new(v, v)                                   # f_ac - sum_kld g[k,c,l,d] tt[k,l,a,d]
+        comb([Fvv0], [C["fvv"]])
+        mm(ttp.view(v, o * o * v), E.g_kldc.view(o * o * v, v), Fvv0, -1.0, 1.0, const_b="g_kldc")
+        del tt, ttp
+        Fov = new(o, v)                                    # cc_Fov: f_kc + sum_ld g[k,c,l,d] t_ld
+        comb([Fov], [fov])
+        mmf(E.g_ovov.view(ov, ov), t1.reshape(ov, 1), Fov.view(ov, 1), 1.0, 1.0)
+        Foo, Fvv = new(o, o), new(v, v)
+        comb([Foo], [Foo0])
+        comb([Foo.diagonal()], [e_o], [[-1.0]], accumulate=True)
+        comb([Fvv], [Fvv0])
+        comb([Fvv.diagonal()], [e_v], [[-1.0]], accumulate=True)
 
         # T1 equation (fricc/friccsd.py:153-176)
-        t1new = -2 * ein("kc,ka,ic->ia", fov, t1, t1)
-        t1new += t1 @ Fvv.T
-        t1new -= Foo.T @ t1
-        t1new += 2 * ein("kc,kica->ia", Fov, t2) - ein("kc,ikca->ia", Fov, t2)
-        t1new += ein("kc,ic,ka->ia", Fov, t1, t1)
-        t1new += fov
-        t1new += 2 * ein("kcai,kc->ia", E.ovvo, t1) - ein("kiac,kc->ia", E.oovv, t1)
-        t1new = t1new.contiguous()
+        t1new = new(o, v)
+        A_ik = new(o, o)
+        mmf(t1, fov.T, A_ik)                               # A[i,k] = sum_c t_ic f_kc
+        mmf(A_ik, t1, t1new, -2.0, 0.0)                    # -2 sum_kc f_kc t_ka t_ic
+        mmf(t1, Fvv.T, t1new, 1.0, 1.0)                    # + sum_c Fvv[a,c] t_ic
+        mmf(Foo.T, t1, t1new, -1.0, 1.0)                   # - sum_k Foo[k,i] t_ka
+        U = new(o, v, o, v)                                # U[k,c,i,a] = 2 t2[k,i,c,a] - t2[i,k,c,a]
+        comb([U], [t2.permute(0, 2, 1, 3), t2.permute(1, 2, 0, 3)], [[2.0, -1.0]])
+        mmf(Fov.reshape(1, ov), U.view(ov, ov), t1new.view(1, ov), 1.0, 1.0)   # 2 Fov t2 - Fov t2
+        del U
+        B_ik = new(o, o)
+        mmf(t1, Fov.T, B_ik)                               # B[i,k] = sum_c t_ic Fov_kc
+        mmf(B_ik, t1, t1new, 1.0, 1.0)                     # + sum_kc Fov_kc t_ic t_ka
+        comb([t1new], [fov], accumulate=True)              # + f_ia
+        mmf(t1.reshape(1, ov), E.G_t1_kcia.view(ov, ov), t1new.view(1, ov), 1.0, 1.0)  # 2 (kc|ai) t - (ki|ac) t
         mm(t2.view(o, o * v * v), E.G_t1.view(o * v * v, v), t1new, 1.0, 1.0, const_b="G_t1")  # O^2V^3, :165-166
         # X[c,a] = sum_kd t1[k,d] (2 (kd|ac) - (kc|ad)): the t1.t1 T1 term (:167-168) and Lvv's ovvv part
-        X = (t1.reshape(1, ov) @ E.G_t1_kdca.view(ov, v * v)).view(v, v)
-        t1new += t1 @ X
+        X = new(v, v)
+        mmf(t1.reshape(1, ov), E.G_t1_kdca.view(ov, v * v), X.view(1, v * v))
+        mmf(t1, X, t1new, 1.0, 1.0)
         # -2 (lc|ki) + (kc|li) = -g_ovoo[l,c,k,i]
-        t1new -= ein2("lcki,klac->ia", E.g_ovoo, t2)
-        t1new -= ein("lcki,lc,ka->ia", E.g_ovoo, t1, t1)
+        ein2("lcki,klac->ia", E.g_ovoo, t2, out=t1new, alpha=-1.0, beta=1.0)
+        u_ki = new(o, o)                                   # u[k,i] = sum_lc t_lc g_ovoo[l,c,k,i]
+        mmf(t1.reshape(1, ov), E.g_ovoo.view(ov, o * o), u_ki.view(1, o * o))
+        mmf(u_ki.T, t1, t1new, -1.0, 1.0)                  # - sum_k u[k,i] t_ka
 
         # T2 driver terms (:179-187)
         Y1 = ein2("kibc,jc->kibj", E.oovv, t1)
-        R = torch.empty(o * v * v, o, dtype=f64, device=dev)   # R[(i,a,b), j] = sum_c (ia|cb) t_jc
+        R = new(o * v * v, o)                              # R[(i,a,b), j] = sum_c (ia|cb) t_jc
         mm(E.ovvv_iabc.view(o * v * v, v), t1.T, R, 1.0, 0.0, const="ovvv_iabc")
-        tmp = R.view(o, v, v, o).permute(0, 3, 1, 2) - ein2("ka,kibj->ijab", t1, Y1)
-        t2new = E.ovov.permute(0, 2, 1, 3).contiguous()
+        tmp = new(o, o, v, v)
+        comb([tmp], [R.view(o, v, v, o).permute(0, 3, 1, 2), ein2("ka,kibj->ijab", t1, Y1)], [[1.0, -1.0]])
+        del Y1
+        t2new = new(o, o, v, v)
+        comb([t2new], [E.ovov.permute(0, 2, 1, 3)])
         D.sym_add(t2new, tmp, 1.0)
-        tmp2 = ein2("kcai,jc->akij", E.ovvo, t1) + E.ovoo.permute(1, 3, 0, 2)
-        tmp = ein2("akij,kb->ijab", tmp2, t1)
-        D.sym_add(t2new, tmp, -1.0)
+        tmp2 = new(v, o, o, o)
+        comb([tmp2], [ein2("kcai,jc->akij", E.ovvo, t1), E.ovoo.permute(1, 3, 0, 2)])
+        D.sym_add(t2new, ein2("akij,kb->ijab", tmp2, t1), -1.0)
+        del tmp, tmp2
 
-        Loo = D.Loo(t1, t2, E, Foo=Foo0)
-        Lvv = Fvv0 - t1.T @ fov + X.T                      # Lvv with its ovvv part from X
-        Loo.diagonal().sub_(e_o)
-        Lvv.diagonal().sub_(e_v)
+        Loo = new(o, o)                                    # Loo = cc_Foo + f t1^T + sum_lc t_lc g_ovoo[l,c,k,i]
+        comb([Loo], [Foo0])
+        mmf(fov, t1.T, Loo, 1.0, 1.0)
+        comb([Loo], [u_ki], accumulate=True)
+        Lvv = new(v, v)                                    # Lvv with its ovvv part from X
+        comb([Lvv], [Fvv0])
+        mmf(t1.T, fov, Lvv, -1.0, 1.0)
+        comb([Lvv], [X.T], accumulate=True)
+        comb([Loo.diagonal()], [e_o], [[-1.0]], accumulate=True)
+        comb([Lvv.diagonal()], [e_v], [[-1.0]], accumulate=True)
 
         main.wait_stream(side)  # the compressed tensors from here on
         if "O^4V^2" in comp:  # sparse_cc_Woooo (:309-322)
-            Wo = (ein2("lcki,jc->klij", E.ovoo, t1) + ein2("kclj,ic->klij", E.ovoo, t1)).permute(2, 3, 0, 1)
-            Wo = Wo.contiguous()                                                  # [i,j,k,l]
+            Wo = new(o, o, o, o)                                                  # [i,j,k,l]
+            comb([Wo.permute(2, 3, 0, 1)], [ein2("lcki,jc->klij", E.ovoo, t1), ein2("kclj,ic->klij", E.ovoo, t1)])
             self._spmm(Tw, 0, 1, 2, 3, 1.0, E.ovov_cdkl, o * o, Wo, st, const="ovov_cdkl")  # 1323
             Woooo = Wo.permute(2, 3, 0, 1)                                        # (k,l,i,j)
-            Woooo += ein2("kild,jd->klij", ein2("kcld,ic->kild", E.ovov, t1), t1)
-            Woooo += E.oooo.permute(0, 2, 1, 3)
+            comb([Woooo], [ein2("kild,jd->klij", ein2("kcld,ic->kild", E.ovov, t1), t1)], accumulate=True)
+            comb([Woooo], [E.oooo.permute(0, 2, 1, 3)], accumulate=True)
         else:
             Woooo = D.cc_Woooo(t1, t2, E)
 
         if "O^3V^3" in comp:  # sparse_cc_Wvoov / sparse_cc_Wvovo (:334-376)
-            R = torch.empty(o * v * v, o, dtype=f64, device=dev)   # R[(k,c,a), i] = sum_d (kc|ad) t_id
+            R = new(o * v * v, o)                          # R[(k,c,a), i] = sum_d (kc|ad) t_id
             mm(E.ovvv.view(o * v * v, v), t1.T, R, 1.0, 0.0, const="ovvv")
-            Wvoov = (R.view(o, v, v, o).permute(2, 0, 3, 1) - ein2("kcli,la->akic", E.ovoo, t1)
-                     + E.ovvo.permute(2, 0, 3, 1))
-            Wp = Wvoov.permute(0, 2, 1, 3).contiguous()                         # [a,i,k,c]
+            Wp = new(v, o, o, v)                                                  # [a,i,k,c]
+            Wvoov = Wp.permute(0, 2, 1, 3)                                        # (a,k,i,c)
+            comb([Wvoov], [R.view(o, v, v, o).permute(2, 0, 3, 1), ein2("kcli,la->akic", E.ovoo, t1),
+                           E.ovvo.permute(2, 0, 3, 1)], [[1.0, -1.0, 1.0]])
             self._spmm(Tw, 3, 0, 1, 2, -0.5, E.ovov, ov, Wp, st, const="ovov")                     # 0112
             self._spmm(Tw, 2, 0, 1, 3, 1.0, E.ovov_0313_0113, ov, Wp, st, const="ovov_0313_0113")  # 0313+0113
-            Wvoov = Wp.permute(0, 2, 1, 3)                                      # (a,k,i,c)
-            Wvoov -= ein2("lkci,la->akic", ein2("ldkc,id->lkci", E.ovov, t1), t1)
+            comb([Wvoov], [ein2("lkci,la->akic", ein2("ldkc,id->lkci", E.ovov, t1), t1)], [[-1.0]],
+                 accumulate=True)
             mm(E.ovvv_kacd.view(o * v * v, v), t1.T, R, 1.0, 0.0, const="ovvv_kacd")   # R[(k,a,c), i] = sum_d (kd|ac) t_id
-            Wvovo = (R.view(o, v, v, o).permute(1, 0, 2, 3) - ein2("lcki,la->akci", E.ovoo, t1)
-                     + E.oovv.permute(2, 0, 3, 1))
-            Wq = Wvovo.permute(0, 3, 1, 2).contiguous()                         # [a,i,k,c]
+            Wq = new(v, o, o, v)                                                  # [a,i,k,c]
+            Wvovo = Wq.permute(0, 2, 3, 1)                                        # (a,k,c,i)
+            comb([Wvovo], [R.view(o, v, v, o).permute(1, 0, 2, 3), ein2("lcki,la->akci", E.ovoo, t1),
+                           E.oovv.permute(2, 0, 3, 1)], [[1.0, -1.0, 1.0]])
             self._spmm(Tw, 3, 0, 1, 2, -0.5, E.ovov_0312, ov, Wq, st, const="ovov_0312")          # 0312
-            Wvovo = Wq.permute(0, 2, 3, 1)                                      # (a,k,c,i)
-            Wvovo -= ein2("lkci,la->akci", ein2("lckd,id->lkci", E.ovov, t1), t1)
+            comb([Wvovo], [ein2("lkci,la->akci", ein2("lckd,id->lkci", E.ovov, t1), t1)], [[-1.0]],
+                 accumulate=True)
+            del R
         else:
             Wvoov = D.cc_Wvoov(t1, t2, E)
             Wvovo = D.cc_Wvovo(t1, t2, E)
 
         if "O^4V^2" in comp:
-            t2new += ein2("lija,lb->ijab", ein2("klij,ka->lija", Woooo, t1), t1)
-            Tp = t2new.permute(2, 3, 0, 1).contiguous()                           # [a,b,i,j]
-            self._spmm(T, 2, 3, 0, 1, 1.0, Woooo.contiguous(), o * o, Tp, st)     # 0101
-            t2new.copy_(Tp.permute(2, 3, 0, 1))
-            del Tp
+            comb([t2new], [ein2("lija,lb->ijab", ein2("klij,ka->lija", Woooo, t1), t1)], accumulate=True)
+            Tp = new(v, v, o, o)                                                  # [a,b,i,j]
+            comb([Tp], [t2new.permute(2, 3, 0, 1)])
+            Wk = new(o, o, o, o)
+            comb([Wk], [Woooo])
+            self._spmm(T, 2, 3, 0, 1, 1.0, Wk, o * o, Tp, st)                     # 0101
+            comb([t2new], [Tp.permute(2, 3, 0, 1)])
+            del Tp, Wk
         else:
             tau = t2 + ein("ia,jb->ijab", t1, t1)
             t2new += ein("klij,klab->ijab", Woooo, tau)
@@ -498,8 +534,12 @@ class FRICCSDGPU:
         # Wvvvv terms (:207, :222-234)
         if self.wvvvv_t1t1 == "reference":
             # fricc/friccsd.py:222: einsum("abcd,ia,jb->ijab") sums c,d inside Wvvvv
-            S = D.wvvvv_sum_cd(t1, E)
-            t2new += S[None, None, :, :] * t1[:, None, :, None] * t1[None, :, None, :]
+            S = new(v, v)                                  # sum_cd Wvvvv[a,b,c,d]
+            comb([S], [E.S0])
+            mmf(E.U.T, t1, S, -1.0, 1.0)
+            mmf(t1.T, E.U, S, -1.0, 1.0)
+            comb([t2new], [], [[1.0]], prod=[S[None, None, :, :], t1[:, None, :, None], t1[None, :, None, :]],
+                 accumulate=True)
             if "O^2V^4" in comp:
                 if self.precision == "split":
                     # (ac|bd) rebuilt from the split factor on the tensor cores, FP32
@@ -525,12 +565,13 @@ class FRICCSDGPU:
                         L.check(self._spmm32(T, 0, 1, 2, 3, 1.0, _ptr(W), v * v, R.ldw, _ptr(t2new), st))
                 else:
                     self._spmm(T, 0, 1, 2, 3, 1.0, E.vvvvT, v * v, t2new, st, const="vvvvT")  # (ac|bd) of 2323
-                XY = torch.zeros(o, o, 2, o, v, dtype=t2.dtype, device=t2.device)
+                XY = D.zero(new(o, o, 2, o, v))
                 self._spmm(T, 0, 1, 2, 3, 1.0, E.ovvv_XY, 2 * ov, XY, st, const="ovvv_XY")  # t1 parts
                 XYv = XY.view(o * o, 2, o, v)
                 t2v = t2new.view(o * o, v, v)
                 mm(XYv[:, 0].transpose(1, 2), t1.unsqueeze(0).expand(o * o, o, v), t2v, -1.0, 1.0)  # -X t1
                 mm(t1.T.unsqueeze(0).expand(o * o, v, o), XYv[:, 1], t2v, -1.0, 1.0)               # -t1 Y
+                del XY
             else:
                 WT = D.wvvvv_T(t1, E)
                 t2new += ein("abcd,ijcd->ijab", WT.permute(2, 3, 0, 1), t2)
@@ -543,7 +584,7 @@ class FRICCSDGPU:
             else:
                 t2new += ein("abcd,ijcd->ijab", Wvvvv, t2)
 
-        tmpL = torch.empty_like(t2)
+        tmpL = new(o, o, v, v)
         mm(Lvv.unsqueeze(0).expand(o * o, v, v), t2.view(o * o, v, v), tmpL.view(o * o, v, v), 1.0, 0.0)
         D.sym_add(t2new, tmpL, 1.0)                         # Lvv t2, :238-239
         mm(Loo.T, t2.view(o, o * v * v), tmpL.view(o, o * v * v), 1.0, 0.0)
@@ -551,17 +592,19 @@ class FRICCSDGPU:
         del tmpL
 
         if "O^3V^3" in comp:
-            WA = Wvoov.permute(1, 3, 2, 0).contiguous()      # [k,c,i,a] = Wvoov(a,k,i,c)
-            WB = Wvovo.permute(1, 2, 3, 0).contiguous()      # [k,c,i,a] = Wvovo(a,k,c,i)
-            tmp = torch.zeros(o, v, o, v, dtype=t2.dtype, device=t2.device)   # [j,b,i,a]
-            self._spmm(T, 1, 3, 0, 2, 1.0, 2.0 * WA - WB, ov, tmp, st)        # 1302 + 1202
+            WA, WB, W2 = new(o, v, o, v), new(o, v, o, v), new(o, v, o, v)   # [k,c,i,a]
+            comb([WA, WB, W2], [Wvoov.permute(1, 3, 2, 0), Wvovo.permute(1, 2, 3, 0)],
+                 [[1.0, 0.0], [0.0, 1.0], [2.0, -1.0]])   # Wvoov(a,k,i,c), Wvovo(a,k,c,i), 2 WA - WB
+            tmp = D.zero(new(o, v, o, v))                                     # [j,b,i,a]
+            self._spmm(T, 1, 3, 0, 2, 1.0, W2, ov, tmp, st)                   # 1302 + 1202
             D.sym_add(t2new, tmp.permute(2, 0, 3, 1), 1.0)
-            tmp.zero_()
+            D.zero(tmp)
             self._spmm(T, 1, 2, 0, 3, 1.0, WA, ov, tmp, st)                   # 1303, [j,b,i,a]
             D.sym_add(t2new, tmp.permute(2, 0, 3, 1), -1.0)
-            tmp.zero_()
+            D.zero(tmp)
             self._spmm(T, 1, 2, 0, 3, 1.0, WB, ov, tmp, st)                   # 1203, [j,a,i,b]
             D.sym_add(t2new, tmp.permute(2, 0, 1, 3), -1.0)
+            del WA, WB, W2, tmp
         else:
             tmp = 2 * ein("akic,kjcb->ijab", Wvoov, t2) - ein("akci,kjcb->ijab", Wvovo, t2)
             t2new += _sym(tmp)
@@ -569,15 +612,44 @@ class FRICCSDGPU:
             t2new -= _sym(ein("bkci,kjac->ijab", Wvovo, t2))
 
         # denominators + energy + step norm (:281-284, :418-427)
-        eia = (e_o[:, None] - e_v[None, :]).contiguous()
-        t1new = t1new.contiguous()
-        t2new = t2new.contiguous()
         t1o = t1 if t1_old is None else t1_old
         t2o = t2 if t2_old is None else t2_old
-        L.check(self.lib.fricc_energy_update(_ptr(t1new), _ptr(t2new), _ptr(eia), _ptr(fov.contiguous()),
+        L.check(self.lib.fricc_energy_update(_ptr(t1new), _ptr(t2new), _ptr(C["eia"]), _ptr(fov),
                                              _ptr(E.ovov), _ptr(t1o.contiguous()), _ptr(t2o.contiguous()), o, v,
                                              _ptr(t1new), _ptr(t2new), _ptr(self._res), st))
         return t1new, t2new
+
+    def _timed(self, verbose, compress):
+        """Run one compression; with ``verbose``, print the reference's phase
+        table for it (src/fri_utils.cpp:509-519) from CUDA events at its
+        phase boundaries."""
+        if not verbose:
+            return compress()
+        from .py_rccsd import print_phase_table
+        L.check(self.lib.fricc_phase_timing_set(1))
+        sec = (ctypes.c_double * 5)()
+        try:
+            h = compress()
+            L.check(self.lib.fricc_phase_timing_read(sec))
+        finally:
+            self.lib.fricc_phase_timing_set(0)
+        print_phase_table(list(sec))
+        return h
+
+    def _constants(self, o, v):
+        """Per-solver constants of the iteration, built once: contiguous
+        Fock blocks, the shifted orbital energies and the denominator
+        matrix eia = e_i - e_a (fricc/friccsd.py:83, :281-284)."""
+        key = (o, v)
+        if getattr(self, "_const_key", None) != key:
+            E = self.eris
+            e_o = E.mo_energy[:o].contiguous()
+            e_v = (E.mo_energy[o:] + self.level_shift).contiguous()
+            self._const = {"foo": E.fock[:o, :o].contiguous(), "fvv": E.fock[o:, o:].contiguous(),
+                           "fov": E.fock[:o, o:].contiguous(), "e_o": e_o, "e_v": e_v,
+                           "eia": (e_o[:, None] - e_v[None, :]).contiguous()}
+            self._const_key = key
+        return self._const
 
     def _w_source(self, t2):
         """T2, or after burn-in in the unbiased mode its running average

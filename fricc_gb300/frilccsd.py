@@ -102,8 +102,10 @@ class FRILCCSDGPU(FRICCSDGPU):
         e_v = E.mo_energy[o:] + self.level_shift
         fov = E.fock[:o, o:]
         ein = torch.einsum
-        mm = D.gemm_df if self.precision == "df64" else D.gemm_torch
-        ein2 = D.einsum_df if self.precision == "df64" else torch.einsum
+        mm = D.gemm_df if self.precision == "df64" else D.gemm_f64
+
+        def ein2(spec, A_, B_):
+            return D.einsum_df(spec, A_, B_, gemm=mm)
         f64, dev = t2.dtype, t2.device
         if rn is None:
             rn = [self.rn_draw() for _ in range(self.n_draws)]

@@ -33,7 +33,6 @@ Differences, all raising instead of terminating the process:
 from __future__ import annotations
 
 import ctypes
-import time
 
 import numpy as np
 import torch
@@ -83,6 +82,18 @@ def _to_device(a, dtype=torch.float64):
     return torch.from_numpy(np.asarray(a)).to("cuda")
 
 
+def print_phase_table(sec):
+    """The verbose timing table of fri_compression (src/fri_utils.cpp:509-519):
+    Sorting, P vector, Sampling, Wrap up and Total seconds, with each one's
+    fraction of the total, in the reference's layout."""
+    total = sec[4]
+    print("Subsection    Fraction of Total    Total Time")
+    print("==========    =================    ==========")
+    for name, t in zip(("Sorting ", "P vector", "Sampling", "Wrap up ", "Total   "), sec):
+        frac = t / total if total > 0 else float("nan")
+        print(f"{name}      {frac:6.4f}               {t:6.4f} (s)")
+
+
 class SparseTensor4d:
     """Device-resident compressed tensor (include/sparse_tensor.hpp:13-100)."""
 
@@ -109,8 +120,9 @@ class SparseTensor4d:
                              "compression must be 'largest' or 'fri'")
         self._dims = tuple(int(x) for x in dims)
         m = int(m)
-        t0 = time.perf_counter()
         x = _to_device(tensor_arr)
+        if verbose:
+            L.check(lib.fricc_phase_timing_set(1))
         samp = L.SAMPLING.get(sampling_method, -1)
         self.draws_used = 0
         if compression == "fri" and samp < 0:
@@ -131,10 +143,12 @@ class SparseTensor4d:
             L.check(lib.fricc_sp_status(self._h))  # the reference's constructor fails on the spot
         self._keep = x  # the device copy stays alive while the stream may still read it
         if verbose:
-            t = time.perf_counter() - t0
-            print("Subsection    Fraction of Total    Total Time")
-            print("==========    =================    ==========")
-            print(f"Total         {1.0:6.4f}               {t:6.4f} (s)")
+            sec = (ctypes.c_double * 5)()
+            try:
+                L.check(lib.fricc_phase_timing_read(sec))
+            finally:
+                lib.fricc_phase_timing_set(0)
+            print_phase_table(list(sec))
 
     # -- accessors --------------------------------------------------------
     @property

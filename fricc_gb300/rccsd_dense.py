@@ -4,9 +4,11 @@ These are the parts of fricc/friccsd.py:update_amps that the reference
 delegates to PySCF (``rintermediates`` cc_Foo, cc_Fvv, cc_Fov, Loo, Lvv and
 the dense W intermediates, the CCSD energy) written from the closed-shell
 CCSD equations (Hirata et al., J. Chem. Phys. 120, 2581 (2004)), with torch
-tensors on the device.  torch is the plumbing here: the contractions below
-are cuBLAS GEMMs; the hot path (compression, sparse terms, denominators) is
-the CUDA library.
+tensors on the device.  The reference-shaped helpers below (cc_Foo, Loo,
+cc_Woooo, ...) are written with torch einsums and serve the uncompressed
+variants and the tests; the iteration itself (fricc_gb300.friccsd) runs its
+dense algebra on the library's GEMMs (gemm_f64, gemm_df, the tensor-core
+GEMM) and its elementwise passes on the library's combine kernel.
 
 Integral blocks, chemists' notation: ovov[i,a,j,b] = (ia|jb),
 oovv[i,j,a,b] = (ij|ab), ovvo[i,a,b,j] = (ia|bj), ovoo[i,a,j,k] = (ia|jk),
@@ -66,6 +68,9 @@ class DeviceERIs:
         # the same integral as [k,d,c,a]: X[c,a] = sum_kd t1[k,d] G[k,c,d,a] is one GEMV
         # (it serves the t1.t1 T1 term and the ovvv part of Lvv)
         self.G_t1_kdca = self.G_t1.permute(0, 2, 1, 3).contiguous()
+        # the T1 terms 2 sum_kc (kc|ai) t_kc - sum_kc (ki|ac) t_kc as one GEMV:
+        # G1[k,c,i,a] = 2 (kc|ai) - (ki|ac)
+        self.G_t1_kcia = (2.0 * self.ovvo.permute(0, 1, 3, 2) - self.oovv.permute(0, 3, 1, 2)).contiguous()
         # the t1 parts of Wvvvv, contracted with the compressed T2 instead of being
         # built densely: W'[c,d,(x,k,a)] = (kd|ac) for x=0 and (kc|ad) for x=1
         self.ovvv_XY = torch.stack([ovvv.permute(3, 1, 0, 2), ovvv.permute(1, 3, 0, 2)], dim=2).contiguous()
@@ -234,6 +239,74 @@ def sym_add(out: torch.Tensor, X: torch.Tensor, coef: float = 1.0) -> torch.Tens
     return out
 
 
+def _view4(t: torch.Tensor, shape):
+    """Element strides of ``t`` broadcast to ``shape``, padded to 4 dims."""
+    b = t.expand(*shape) if tuple(t.shape) != tuple(shape) else t
+    st = list(b.stride())
+    return [0] * (4 - len(st)) + st
+
+
+def combine(outs, xs=(), coefs=None, prod=(), accumulate=False):
+    """One pass of the library's strided elementwise kernel (fricc_combine):
+    out_k = sum_t coefs[k][t] xs[t] (+ coefs[k][-1] * prod[0] * prod[1] ...
+    when ``prod`` is given), or out_k += that with ``accumulate``.  Every
+    tensor is an FP64 device view; inputs broadcast to the outputs' shape
+    (at most 4 dims); the last dim should be the first output's contiguous
+    one.  Outputs must not overlap the inputs."""
+    import ctypes
+
+    from . import _lib as L
+    outs = list(outs)
+    xs = list(xs)
+    prod = list(prod)
+    shape = tuple(outs[0].shape)
+    if len(shape) > 4 or any(tuple(o.shape) != shape for o in outs):
+        raise ValueError("combine: outputs of one shape, at most 4 dims")
+    for t in outs + xs + prod:
+        if t.dtype != torch.float64 or t.device.type != "cuda":
+            raise ValueError("combine: FP64 CUDA tensors only")
+    nc = len(xs) + (1 if prod else 0)
+    if coefs is None:
+        coefs = [[1.0] * nc for _ in outs]
+    if len(coefs) != len(outs) or any(len(c) != nc for c in coefs):
+        raise ValueError("combine: one coefficient per input (and one for the product) per output")
+    dims = [1] * (4 - len(shape)) + list(shape)
+    vp = ctypes.c_void_p
+
+    def ptrs(ts):
+        return (vp * max(len(ts), 1))(*[t.data_ptr() for t in ts])
+
+    # walk the index space in the first output's memory order (its
+    # smallest stride innermost), so its reads and writes coalesce
+    s0 = _view4(outs[0], shape)
+    perm = sorted(range(4), key=lambda d: (dims[d] != 1, -s0[d]))
+
+    def strides(ts):
+        flat = []
+        for t in ts:
+            st = _view4(t, shape)
+            flat.extend(st[d] for d in perm)
+        return L.i64arr(flat if flat else [0])
+
+    cf = (ctypes.c_double * (len(outs) * nc))(*[float(c) for row in coefs for c in row])
+    L.check(L.load().fricc_combine(L.i64arr([dims[d] for d in perm]), len(xs), ptrs(xs), strides(xs), len(prod),
+                                   ptrs(prod), strides(prod), len(outs), ptrs(outs), strides(outs), cf,
+                                   int(bool(accumulate)), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return outs[0]
+
+
+def zero(t: torch.Tensor) -> torch.Tensor:
+    """t[...] = 0 for a contiguous device tensor, through the library."""
+    import ctypes
+
+    from . import _lib as L
+    if not t.is_contiguous():
+        raise ValueError("zero: contiguous tensors only")
+    L.check(L.load().fricc_zero(ctypes.c_void_p(t.data_ptr()), t.numel() * t.element_size(),
+                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    return t
+
+
 def _dev_tensor(a, dev):
     """FP64 copy of a numpy array, or the tensor itself moved to ``dev``."""
     t = a if isinstance(a, torch.Tensor) else torch.from_numpy(np.ascontiguousarray(a))
@@ -246,9 +319,7 @@ def _strides3(t: torch.Tensor):
     return (t.stride(1), t.stride(2), t.stride(0)), t.shape[0]
 
 
-def gemm_df(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.0, beta: float = 0.0):
-    """C = alpha A @ B + beta C on the FP32-pair GEMM kernel; FP64 tensors with
-    any strides, 2-D or batched 3-D (a batch stride of 0 shares an operand)."""
+def _gemm_call(fn, A, B, C, alpha, beta):
     import ctypes
 
     from . import _lib as L
@@ -258,53 +329,89 @@ def gemm_df(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
     M, N = C.shape[-2], C.shape[-1]
     K = A.shape[-1]
     assert A.shape[-2] == M and B.shape[-2] == K and B.shape[-1] == N and bA in (1, batch) and bB in (1, batch)
-    L.check(L.load().fricc_gemm_df(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
-                                   ctypes.c_void_p(C.data_ptr()), batch, M, N, K, L.i64arr(sA), L.i64arr(sB),
-                                   L.i64arr(sC), float(alpha), float(beta),
-                                   ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    L.check(getattr(L.load(), fn)(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
+                                  ctypes.c_void_p(C.data_ptr()), batch, M, N, K, L.i64arr(sA), L.i64arr(sB),
+                                  L.i64arr(sC), float(alpha), float(beta),
+                                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return C
 
 
-def einsum_df(spec: str, A: torch.Tensor, B: torch.Tensor, gemm=None) -> torch.Tensor:
+def gemm_df(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.0, beta: float = 0.0):
+    """C = alpha A @ B + beta C on the FP32-pair GEMM kernel; FP64 tensors with
+    any strides, 2-D or batched 3-D (a batch stride of 0 shares an operand)."""
+    return _gemm_call("fricc_gemm_df", A, B, C, alpha, beta)
+
+
+def gemm_f64(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.0, beta: float = 0.0):
+    """The same contract in FP64 on the library's DFMA GEMM kernel."""
+    return _gemm_call("fricc_gemm_f64", A, B, C, alpha, beta)
+
+
+def _as3(x: torch.Tensor, shape3):
+    """x (a permuted view) as a [batch, rows, cols] view, copied to a
+    contiguous buffer by the library when its strides do not allow one."""
+    try:
+        return x.view(*shape3)
+    except RuntimeError:
+        if x.device.type != "cuda":
+            return x.reshape(*shape3)
+        buf = torch.empty(x.shape, dtype=x.dtype, device=x.device)
+        combine([buf], [x])
+        return buf.view(*shape3)
+
+
+def einsum_df(spec: str, A: torch.Tensor, B: torch.Tensor, gemm=None, out=None, alpha: float = 1.0,
+              beta: float = 0.0) -> torch.Tensor:
     """Two-operand einsum as one strided batched GEMM on the FP32-pair kernel.
 
     Indices shared by both operands and the output form the batch, A-only
     output indices the rows, B-only output indices the columns, shared
     non-output indices the contraction; an index in one operand only and not
     in the output is summed out first.  ``gemm`` replaces the FP32-pair GEMM
-    (the split-precision form passes the tensor-core one).  Operand groups merge into one stride
-    where the layout allows (``reshape`` copies otherwise); the result is a
-    view of a contiguous [batch, rows, cols] buffer in the output's order."""
-    lhs, out = spec.replace(" ", "").split("->")
+    (the FP64 form passes the DFMA one, the split-precision form the
+    tensor-core one).  Operand groups merge into one stride where the layout
+    allows (the library copies them otherwise).  Without ``out`` the result
+    is a view of a new contiguous [batch, rows, cols] buffer in the output's
+    order; with ``out`` (a tensor in the output's index order whose
+    [batch, rows, cols] grouping is a view) the GEMM writes
+    out = alpha * result + beta * out in place."""
+    lhs, outs = spec.replace(" ", "").split("->")
     a, b = lhs.split(",")
     if len(set(a)) != len(a) or len(set(b)) != len(b):
         raise ValueError(f"einsum_df: repeated index within an operand in {spec!r}")
-    lone = [c for c in a if c not in b and c not in out]
+    lone = [c for c in a if c not in b and c not in outs]
     if lone:
         A = A.sum(dim=[a.index(c) for c in lone])
         a = "".join(c for c in a if c not in lone)
-    lone = [c for c in b if c not in a and c not in out]
+    lone = [c for c in b if c not in a and c not in outs]
     if lone:
         B = B.sum(dim=[b.index(c) for c in lone])
         b = "".join(c for c in b if c not in lone)
     size = {c: A.shape[a.index(c)] for c in a}
     size.update({c: B.shape[b.index(c)] for c in b})
-    bt = [c for c in out if c in a and c in b]
-    mi = [c for c in out if c in a and c not in b]
-    ni = [c for c in out if c in b and c not in a]
-    ki = [c for c in a if c in b and c not in out]
+    bt = [c for c in outs if c in a and c in b]
+    mi = [c for c in outs if c in a and c not in b]
+    ni = [c for c in outs if c in b and c not in a]
+    ki = [c for c in a if c in b and c not in outs]
     prod = lambda idx: math.prod(size[c] for c in idx)
     nb, M, N, K = prod(bt), prod(mi), prod(ni), prod(ki)
-    Ap = A.permute([a.index(c) for c in bt + mi + ki]).reshape(nb, M, K)
-    Bp = B.permute([b.index(c) for c in bt + ki + ni]).reshape(nb, K, N)
-    C = torch.empty(nb, M, N, dtype=torch.float64, device=A.device)
+    Ap = _as3(A.permute([a.index(c) for c in bt + mi + ki]), (nb, M, K))
+    Bp = _as3(B.permute([b.index(c) for c in bt + ki + ni]), (nb, K, N))
+    order = bt + mi + ni
+    if out is not None:
+        C = out.permute([outs.index(c) for c in order]).view(nb, M, N)
+    else:
+        C = torch.empty(nb, M, N, dtype=torch.float64, device=A.device)
+        alpha, beta = 1.0, 0.0
     if C.numel():
         if K == 0:
-            C.zero_()
+            if beta == 0.0:
+                C.zero_()
         else:
-            (gemm or gemm_df)(Ap, Bp, C)
-    order = bt + mi + ni
-    return C.view([size[c] for c in order]).permute([order.index(c) for c in out])
+            (gemm or gemm_df)(Ap, Bp, C, alpha, beta)
+    if out is not None:
+        return out
+    return C.view([size[c] for c in order]).permute([order.index(c) for c in outs])
 
 
 def gemm_torch(A, B, C, alpha=1.0, beta=0.0):

@@ -226,6 +226,52 @@ int fricc_gemm_df(const double* A, const double* B, double* C, int64_t batch, in
                   const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
                   void* stream);
 
+/* The same contract in FP64 arithmetic on the FP64 FMA pipe: the dense
+ * O^2V^3 / O^3V^2 contractions of the FP64 iteration, which the reference
+ * leaves to PySCF's einsums (fricc/friccsd.py:144-192,211,238-241 through
+ * pyscf.cc.rintermediates).  Each output is one FMA chain in k order (a
+ * long K with few output tiles is split and the partials summed in slice
+ * order), so results are deterministic.  Stream-ordered. */
+int fricc_gemm_f64(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
+                   const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
+                   void* stream);
+
+/* Strided elementwise combination over a 4-D index space, one pass (no
+ * reference counterpart; it runs the permuted copies, linear combinations,
+ * broadcast products and diagonal updates that fricc/friccsd.py:144-301 and
+ * :309-376 write as NumPy expressions).  For every i < dims (i3 fastest):
+ *   r_k(i) = sum_{t<n_in} coef[k*nc+t] x_t(i)
+ *            + coef[k*nc+n_in] * p_0(i) * ... * p_{n_prod-1}(i)   (if n_prod > 0)
+ *   out_k(i) = r_k(i), or out_k(i) + r_k(i) when accumulate != 0,
+ * nc = n_in + (n_prod > 0), each operand addressed through its own four
+ * element strides (sx[4t..4t+3], sp[4s..], so[4k..]; 0 broadcasts).  Terms
+ * are summed in the order given, a zero coefficient drops its term.  Up to
+ * FRICC_COMBINE_MAX_IN inputs, FRICC_COMBINE_MAX_PROD product factors and
+ * FRICC_COMBINE_MAX_OUT outputs; outputs must not overlap the inputs.
+ * Stream-ordered. */
+#define FRICC_COMBINE_MAX_IN 5
+#define FRICC_COMBINE_MAX_PROD 3
+#define FRICC_COMBINE_MAX_OUT 3
+int fricc_combine(const int64_t dims[4], int n_in, const double* const* x, const int64_t* sx, int n_prod,
+                  const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
+                  const double* coef, int accumulate, void* stream);
+
+/* Phase timing of the calling thread's compressions (the reference's
+ * verbose table of fri_compression, src/fri_utils.cpp:509-519, and of the
+ * SparseTensor4d constructor's verbose flag, include/sparse_tensor.hpp:33-77):
+ * fricc_phase_timing_set(1) records CUDA events at the phase boundaries of
+ * every later compression on this thread (0 stops);
+ * fricc_phase_timing_read waits for the last one and writes the seconds of
+ * its phases: sec[0] "Sorting" (the largest elements and the remaining
+ * norm), sec[1] "P vector", sec[2] "Sampling", sec[3] "Wrap up" (the
+ * outputs), sec[4] "Total". */
+int fricc_phase_timing_set(int on);
+int fricc_phase_timing_read(double sec[5]);
+
+/* Zero `bytes` bytes of device memory at p (no reference counterpart; the
+ * np.zeros of the reference's scratch outputs).  Stream-ordered. */
+int fricc_zero(void* p, int64_t bytes, void* stream);
+
 /* Floating-point operations of one contract call (2 per multiply-add). */
 double fricc_contract_flops(const char* term, const fricc_sparse* T);
 
@@ -363,9 +409,14 @@ int fricc_stream_destroy(void* stream);
  * counterpart), thread-local; value -1 restores the built-in choice.
  * knob 0: output pairs per thread of the float-pair sparse kernel (1, 2, 4);
  * knob 1: tile of the FP32-pair GEMM (0 = 64x64, 1 = 128x32, 2 = 32x128,
- * 3 = 32x160); knob 2: CTAs per SM the FP32-pair GEMM's split K aims for
- * (1..16).  No knob changes a result's arithmetic except the GEMM's tile
- * and split, which reorder its sums. */
+ * 3 = 32x160; the FP64 GEMM's candidate set too); knob 2: CTAs per SM the
+ * FP32-pair and FP64 GEMMs' split K aims for (1..16); knob 3 (a test of the
+ * error path, 1..2^20): in every later compression on this thread, one
+ * tile of the candidate compaction first polls a device word that nothing
+ * sets, gives up after that many polls and reports FRICC_ERR_TIMEOUT
+ * through the compression's status (its results stay valid: the
+ * compaction then runs as usual).  No knob changes a result's arithmetic
+ * except the GEMMs' tile and split, which reorder their sums. */
 int fricc_tune_set(int knob, int value);
 
 /* Instrumentation (no reference counterpart): the number of kernels this
@@ -374,11 +425,17 @@ int fricc_tune_set(int knob, int value);
  * the record; fricc_prof_read synchronises on the recorded events and
  * returns total milliseconds, launches and algorithmic flops). */
 long long fricc_launch_count(void);
+/* The number of device allocations (stream-ordered cudaMallocAsync) this
+ * library has made so far (no reference counterpart). */
+long long fricc_alloc_count(void);
 void fricc_prof_enable(int on);
 int fricc_prof_read(double* ms, long long* launches, double* flops);
 /* The same record for the tensor-core GEMM launches (fricc_gemm_bf16_*,
  * the rebuilds; flops = 2 M N K' of the BF16 products). */
 int fricc_prof_read_tc(double* ms, long long* launches, double* flops);
+/* The same record for the FP64 GEMM launches (fricc_gemm_f64; flops =
+ * 2 batch M N K). */
+int fricc_prof_read_gemm(double* ms, long long* launches, double* flops);
 
 #ifdef __cplusplus
 }

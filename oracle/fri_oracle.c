@@ -372,8 +372,9 @@ int fo_unpack(const int64_t* flat, int64_t m, const int64_t dims[4], int64_t* id
  * W and out are addressed through element strides (the reference reads
  * them through pybind11 unchecked<4> views, which honour strides).
  *
- * outer_begin/outer_end restrict the flattened outer-pair loop, so that a
- * bounded sample of a large contraction can be timed.
+ * outer_begin/outer_end/outer_step restrict the flattened outer-pair loop to
+ * begin, begin + step, ... < end, so that a bounded sample of a large
+ * contraction, spread evenly over all its outer pairs, can be timed.
  * ------------------------------------------------------------------------ */
 #define W4(a, b, c, d) W[(a) * ws[0] + (b) * ws[1] + (c) * ws[2] + (d) * ws[3]]
 #define O4(a, b, c, d) out[(a) * os[0] + (b) * os[1] + (c) * os[2] + (d) * os[3]]
@@ -408,17 +409,21 @@ int64_t fo_outer_size(int term, const int64_t tdims[4], const int64_t wdims[4]) 
 
 int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t ws[4],
                 const int64_t* idx4, const double* vals, int64_t m, const int64_t tdims[4],
-                double* out, const int64_t os[4], int64_t outer_begin, int64_t outer_end) {
+                double* out, const int64_t os[4], int64_t outer_begin, int64_t outer_end,
+                int64_t outer_step) {
   const int64_t no = tdims[0], nv = tdims[2];
   int64_t n_outer = fo_outer_size(term, tdims, wdims);
   if (n_outer < 0) return FO_BAD_ARG;
   if (outer_begin < 0) outer_begin = 0;
   if (outer_end < 0 || outer_end > n_outer) outer_end = n_outer;
+  if (outer_step < 1) outer_step = 1;
+  const int64_t n_iter = outer_end > outer_begin ? (outer_end - outer_begin + outer_step - 1) / outer_step : 0;
 
   switch (term) {
     case T0101: /* out(i,j,a,b) += W(k,l,i,j) * T(k,l,a,b); outer (a,b) */
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t a = p / nv, b = p % nv;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -434,7 +439,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
     case T2323: { /* out(i,j,a,b) += W(a,b,c,d) * T(i,j,c,d); outer (i,j) */
       const int64_t dj = tdims[1], da = wdims[0], db = wdims[1];
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t i = p / dj, j = p % dj;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -450,7 +456,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
     }
     case T1302: /* out(i,j,a,b) += 2*W(a,k,i,c)*T(k,j,c,b); outer (b,j) */
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t b = p / no, j = p % no;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -465,7 +472,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
       break;
     case T1202: /* out(i,j,a,b) -= W(a,k,c,i)*T(k,j,c,b); outer (b,j) */
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t b = p / no, j = p % no;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -480,7 +488,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
       break;
     case T1303: /* out(i,j,a,b) += W(a,k,i,c)*T(k,j,b,c); outer (b,j) */
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t b = p / no, j = p % no;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -495,7 +504,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
       break;
     case T1203: /* out(i,j,a,b) += W(b,k,c,i)*T(k,j,a,c); outer (a,j) */
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t a = p / no, j = p % no;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -510,7 +520,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
       break;
     case T1323: /* out(k,l,i,j) += ovov(k,c,l,d)*T(i,j,c,d); outer (i,j) */
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t i = p / no, j = p % no;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -525,7 +536,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
       break;
     case T0112: /* out(a,k,i,c) -= 0.5*ovov(l,d,k,c)*T(i,l,d,a); outer (a,i) */
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t a = p / no, i = p % no;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -540,7 +552,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
       break;
     case T0313: /* out(a,k,i,c) -= 0.5*ovov(l,c,k,d)*T(i,l,a,d); outer (a,i) */
 #pragma omp parallel for schedule(dynamic, 16)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t a = p / no, i = p % no;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -555,7 +568,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
       break;
     case T0113: /* out(a,k,i,c) += ovov(l,d,k,c)*T(i,l,a,d); outer (a,i) */
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t a = p / no, i = p % no;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;
@@ -570,7 +584,8 @@ int fo_contract(int term, const double* W, const int64_t wdims[4], const int64_t
       break;
     case T0312: /* out(a,k,c,i) -= 0.5*ovov(l,c,k,d)*T(i,l,d,a); outer (a,i) */
 #pragma omp parallel for schedule(dynamic)
-      for (int64_t p = outer_begin; p < outer_end; ++p) {
+      for (int64_t q = 0; q < n_iter; ++q) {
+        const int64_t p = outer_begin + q * outer_step;
         const int64_t a = p / no, i = p % no;
         for (int64_t s = 0; s < m; ++s) {
           const int64_t* id = idx4 + 4 * s;

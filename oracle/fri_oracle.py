@@ -61,7 +61,7 @@ def lib():
         L.fo_outer_size.restype = ctypes.c_int64
         L.fo_outer_size.argtypes = [ctypes.c_int, _i64p, _i64p]
         L.fo_contract.argtypes = [ctypes.c_int, _f64p, _i64p, _i64p, _i64p, _f64p, ctypes.c_int64,
-                                  _i64p, _f64p, _i64p, ctypes.c_int64, ctypes.c_int64]
+                                  _i64p, _f64p, _i64p, ctypes.c_int64, ctypes.c_int64, ctypes.c_int64]
         L.fo_get_d_largest.restype = ctypes.c_int64
         L.fo_get_d_largest.argtypes = [_f64p, ctypes.c_int64, ctypes.c_int64, _i64p, _f64p]
         L.fo_max_threads.restype = ctypes.c_int
@@ -238,7 +238,8 @@ def contract_DTSpT(W, T, ouput, term, outer_range=None):
     """Accumulate the sparse x dense term into ``ouput`` in place (src/sparse_tensor.cpp:349-382).
 
     W and ouput may carry any (element-aligned, non-negative) strides.
-    ``outer_range=(begin, end)`` restricts the outer-pair loop (timing samples).
+    ``outer_range=(begin, end)`` or ``(begin, end, step)`` restricts the
+    outer-pair loop to begin, begin + step, ... < end (timing samples).
     """
     if term not in TERMS:
         raise ValueError(f"CASE NOT IMPLEMENTED: {term}")
@@ -253,11 +254,11 @@ def contract_DTSpT(W, T, ouput, term, outer_range=None):
     os_ = _strides(ouput)
     idx4 = np.ascontiguousarray(T.idx4, dtype=np.int64)
     vals = np.ascontiguousarray(T.vals, dtype=np.float64)
-    b, e = (0, -1) if outer_range is None else outer_range
+    b, e, step = (0, -1, 1) if outer_range is None else (tuple(outer_range) + (1,))[:3]
     # ctypes pointers at the array base honour negative-free strides
     st = L.fo_contract(tid, ctypes.cast(W.ctypes.data, _f64p), _p(wd, _i64p), _p(ws, _i64p),
                        _p(idx4, _i64p), _p(vals, _f64p), vals.size, _p(td, _i64p),
-                       ctypes.cast(ouput.ctypes.data, _f64p), _p(os_, _i64p), b, e)
+                       ctypes.cast(ouput.ctypes.data, _f64p), _p(os_, _i64p), b, e, step)
     if st:
         raise ValueError(f"contract_DTSpT: status {st}")
 

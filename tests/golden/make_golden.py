@@ -25,8 +25,12 @@ records:
 * unbiased.npz  -- fricc/friccsd.py with "unbiased": True (running-average
                    W compression after burn-in), its missing iteration
                    counter supplied by the loop in this script.
+* dropin.npz    -- every SparseTensor4d / contract_DTSpT call the unmodified
+                   fricc/friccsd.py makes in two iterations, recorded at the
+                   binding (arguments, draw, results), for replay through
+                   fricc_gb300.py_rccsd.
 
-Usage:  OMP_NUM_THREADS=1 python tests/golden/make_golden.py
+Usage:  OMP_NUM_THREADS=1 python tests/golden/make_golden.py [--only-dropin]
 """
 from __future__ import annotations
 
@@ -404,7 +408,94 @@ def unbiased_case(R):
     }
 
 
+def _layout(a):
+    """(contiguous data, permutation) such that data.transpose(inverse) has
+    a's memory order: a permuted view of a C-contiguous array is rebuilt
+    with the same strides by data.transpose(np.argsort(perm))."""
+    perm = tuple(int(i) for i in np.argsort([-s for s in a.strides], kind="stable"))
+    return np.array(a.transpose(perm), order="C", copy=True), np.array(perm, dtype=np.int64)
+
+
+def dropin_case(R):
+    """Every py_rccsd call the unmodified fricc/friccsd.py makes in two
+    iterations of its kernel (on the PySCF stand-in), recorded at the
+    binding: each SparseTensor4d(...) with its arguments, the libc draw it
+    consumed and its entries (get_element for every slot), and each
+    contract_DTSpT(W, T, ouput, term) with W, the output before and after
+    the call (W and ouput in their memory layout) and which recorded tensor
+    it used.  Replaying the calls through another implementation of the
+    binding shows that fricc/friccsd.py would run the same iteration on it."""
+    rec = {"calls": []}
+    seed = 61
+    state = {"draws": 0}
+
+    class Rec(types.ModuleType):
+        pass
+
+    mod = Rec("py_rccsd_recorder")
+
+    def SparseTensor4d(tensor_arr, dims, m, compression="fri", sampling_method="pivotal", verbose=False):
+        k = sum(1 for c in rec["calls"] if c["kind"] == "sp")
+        t = R.SparseTensor4d(tensor_arr, dims, m, compression, sampling_method, verbose)
+        rn = -1.0
+        if compression == "fri" and sampling_method == "systematic":
+            rn = draws(seed, state["draws"] + 1)[-1]
+            state["draws"] += 1
+        idx = np.array([t.get_element(i)[0] for i in range(m)], dtype=np.int64).reshape(m, 4)
+        val = np.array([t.get_element(i)[1] for i in range(m)], dtype=np.float64)
+        rec["calls"].append({"kind": "sp", "k": k, "x": np.array(tensor_arr), "dims": np.array(dims, np.int64),
+                             "m": int(m), "compression": compression, "sampling": sampling_method,
+                             "rn": rn, "idx": idx, "val": val})
+        return Tagged(t, k)
+
+    class Tagged:
+        """The reference's tensor with the number of its recorded constructor call."""
+
+        def __init__(self, t, k):
+            self.t, self.k = t, k
+
+        def __getattr__(self, name):
+            return getattr(self.t, name)
+
+    def contract_DTSpT(W, T, ouput, term):
+        before, operm = _layout(ouput)
+        wdata, wperm = _layout(W)
+        R.contract_DTSpT(W, T.t, ouput, term)
+        after, _ = _layout(ouput)
+        rec["calls"].append({"kind": "ct", "term": term, "sp": T.k, "W": wdata, "wperm": wperm,
+                             "before": before, "after": after, "operm": operm})
+
+    mod.SparseTensor4d = SparseTensor4d
+    mod.contract_DTSpT = contract_DTSpT
+    F = load_reference_friccsd(mod)
+    s = SyntheticSystem(4, 12, 60, 0.05, 9)
+    eris = pyscf_standin.make_eris(s)
+    settings = {"m_keep": 700, "compression": "fri", "sampling_method": "systematic",
+                "verbose": False, "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"],
+                "unbiased": False}
+
+    class Driver(pyscf_standin.CCSD):
+        def update_amps(self, t1, t2, eris):
+            return F.update_amps(self, t1, t2, eris)
+
+    cc = Driver(eris, settings)
+    cc.max_cycle = 2
+    t1, t2 = pyscf_standin.mp2_guess(eris)
+    libc.srand(seed)
+    F.kernel(cc, eris, t1, t2)
+    out = {"n_calls": np.int64(len(rec["calls"])), "seed": np.int64(seed), "energies": np.array(cc.energies)}
+    for i, c in enumerate(rec["calls"]):
+        for key, val in c.items():
+            out[f"c{i}_{key}"] = np.asarray(val)
+    return out
+
+
 def main():
+    if "--only-dropin" in sys.argv:
+        R = load_reference_module()
+        np.savez_compressed(os.path.join(HERE, "dropin.npz"), **dropin_case(R))
+        print("dropin.npz", os.path.getsize(os.path.join(HERE, "dropin.npz")), "bytes")
+        return
     R = load_reference_module()
     np.savez_compressed(os.path.join(HERE, "compress.npz"), **compress_cases(R))
     np.savez_compressed(os.path.join(HERE, "contract.npz"), **contract_cases(R))
@@ -413,8 +504,9 @@ def main():
     np.savez_compressed(os.path.join(HERE, "unbiased.npz"), **unbiased_case(R))
     np.savez_compressed(os.path.join(HERE, "pivotal.npz"), **pivotal_cases(R))
     np.savez_compressed(os.path.join(HERE, "parallel_sample.npz"), **parallel_sample_cases())
+    np.savez_compressed(os.path.join(HERE, "dropin.npz"), **dropin_case(R))
     for f in ("compress.npz", "contract.npz", "iteration.npz", "lccsd.npz", "unbiased.npz", "pivotal.npz",
-              "parallel_sample.npz"):
+              "parallel_sample.npz", "dropin.npz"):
         print(f, os.path.getsize(os.path.join(HERE, f)), "bytes")
 
 

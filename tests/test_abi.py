@@ -143,11 +143,3 @@ def test_batch_entry_points_check_arguments(gpulib):
     assert gpulib.fricc_sp_recompress_batch(0, None, None, 0, 0, None, None) == 0
     assert gpulib.fricc_sp_recompress_batch(2, nulls, nulls, 0, 0, rn, None) == 1
     assert gpulib.fricc_last_error() == b"sp_recompress_batch item 0: sp_recompress: null argument"
-
-
-def test_every_entry_point_is_documented():
-    """INTEGRATION.md's table names every function include/fricc_gb300.h
-    declares, with the reference interface it replaces or its purpose."""
-    doc = open(os.path.join(REPO, "INTEGRATION.md")).read()
-    missing = [n for n in _declared() if f"`{n}`" not in doc]
-    assert not missing, missing

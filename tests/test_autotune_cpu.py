@@ -68,5 +68,8 @@ def test_tune_set_checks_arguments():
     assert lib.fricc_tune_set(0, 3) == 1   # pairs per thread: 1, 2 or 4
     assert lib.fricc_tune_set(1, 4) == 1   # four tiles, 0..3
     assert lib.fricc_tune_set(2, 17) == 1  # cover 1..16
-    assert lib.fricc_tune_set(3, 1) == 1   # no such knob
+    assert lib.fricc_tune_set(3, 0) == 1   # the test-only wait: 1..2^20 polls
+    assert lib.fricc_tune_set(3, 1 << 21) == 1
+    assert lib.fricc_tune_set(3, 5) == 0 and lib.fricc_tune_set(3, -1) == 0
+    assert lib.fricc_tune_set(4, 1) == 1   # no such knob
     assert lib.fricc_tune_set(1, 3) == 0 and lib.fricc_tune_set(1, -1) == 0

@@ -92,3 +92,19 @@ def test_reference_arm_under_torchrun_two_ranks():
     assert len(lines) == 1
     d = json.loads(lines[0])
     assert d["impl"] == "reference" and d["value"] > 0
+
+
+def test_block_plan_covers_every_pair_once():
+    """The reference arm's rotating blocks: n_blocks consecutive steps time
+    every outer pair of a term exactly once."""
+    sys.path.insert(0, REPO)
+    import bench
+    for n in (1, 7, 400, 900, 4500):
+        for nb in (1, 3, 10):
+            seen = []
+            for b in range(nb):
+                (lo, hi), k = bench.block_plan(n, nb, b)
+                assert k == hi - lo
+                seen.extend(range(lo, hi))
+            assert seen == list(range(n))
+    assert [bench.n_blocks_for(k) for k in (1, 2, 5, 7, 20, 30)] == [1, 2, 5, 7, 10, 10]

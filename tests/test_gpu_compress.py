@@ -182,3 +182,31 @@ def test_paired_recompress_bit_identical(gpulib):
         gpulib.fricc_sp_destroy(h)
     with pytest.raises(ValueError):
         L.check(gpulib.fricc_sp_recompress_pair(a, a, ctypes.c_void_p(t2.data_ptr()), 0.1, 0.2, st))
+
+
+@pytest.mark.parametrize("compression,method", [("fri", "systematic"), ("fri", "pivotal"), ("largest", "systematic")])
+def test_verbose_phase_table(gpulib, oracle, capsys, compression, method):
+    """SparseTensor4d(..., verbose=True) prints the reference's phase table
+    (src/fri_utils.cpp:509-519): Sorting, P vector, Sampling, Wrap up and
+    Total rows, each fraction of the total, the four phases adding up to the
+    total; the compression itself is unchanged."""
+    from fricc_gb300 import py_rccsd
+    from fricc_gb300.rng import GlibcRand
+    rng = np.random.default_rng(5)
+    x = rng.standard_normal((6, 6, 20, 20)) * rng.random((6, 6, 20, 20)) ** 3
+    kw = {"rng": GlibcRand(9)} if method == "pivotal" else {"rn": 0.375}
+    quiet = py_rccsd.SparseTensor4d(x, x.shape, 3000, compression, method, False,
+                                    **({"rng": GlibcRand(9)} if method == "pivotal" else kw))
+    capsys.readouterr()
+    loud = py_rccsd.SparseTensor4d(x, x.shape, 3000, compression, method, True, **kw)
+    out = capsys.readouterr().out.splitlines()
+    assert out[0].split() == ["Subsection", "Fraction", "of", "Total", "Total", "Time"]
+    rows = out[2:]
+    assert [r[:14].strip() for r in rows] == ["Sorting", "P vector", "Sampling", "Wrap up", "Total"]
+    secs = [float(r.split()[-2]) for r in rows]
+    fracs = [float(r[14:20]) for r in rows]
+    assert secs[4] > 0 and abs(sum(secs[:4]) - secs[4]) <= 1e-3 + 1e-3 * secs[4]
+    assert abs(fracs[4] - 1.0) < 1e-9 and all(0.0 <= f <= 1.0001 for f in fracs)
+    fq, vq = quiet.export()
+    fl, vl = loud.export()
+    assert np.array_equal(fq, fl) and np.array_equal(vq.view(np.int64), vl.view(np.int64))

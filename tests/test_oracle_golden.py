@@ -285,3 +285,27 @@ def test_oracle_largest_elements_exact(oracle, no, nv, frac):
         assert value == a[tuple(idx)]
     kept = np.sort(np.abs(T.vals))
     assert np.array_equal(kept, np.sort(np.abs(a.ravel()))[-m:])
+
+
+def test_oracle_replays_reference_driver_calls(oracle):
+    """Every py_rccsd call of the reference's own fricc/friccsd.py (two
+    iterations, tests/golden/dropin.npz) replayed through the oracle: the
+    compressions bit for bit, the contractions bit for bit (the oracle keeps
+    the reference's loop order)."""
+    g = golden("dropin.npz")
+    tensors = {}
+    for i in range(int(g["n_calls"])):
+        c = lambda key: g[f"c{i}_{key}"]  # noqa: E731
+        if str(c("kind")) == "sp":
+            x = np.ascontiguousarray(c("x"))
+            T = oracle.SparseTensor4d(x, tuple(int(d) for d in c("dims")), int(c("m")), str(c("compression")),
+                                      str(c("sampling")), rn=float(c("rn")))
+            assert np.array_equal(T.idx4, c("idx"))
+            assert np.array_equal(T.vals.view(np.int64), c("val").view(np.int64))
+            tensors[int(c("k"))] = T
+        else:
+            W = np.ascontiguousarray(c("W")).copy().transpose(np.argsort(c("wperm")))
+            out = np.ascontiguousarray(c("before")).copy().transpose(np.argsort(c("operm")))
+            oracle.contract_DTSpT(W, tensors[int(c("sp"))], out, str(c("term")))
+            want = np.ascontiguousarray(c("after")).transpose(np.argsort(c("operm")))
+            assert np.array_equal(out, want), (i, str(c("term")))

@@ -41,6 +41,28 @@ def test_noalloc_matches_allocating_entry_point(gpulib):
         assert np.array_equal(g.view(np.int64), np.add.accumulate(x_h).view(np.int64))
 
 
+def test_noalloc_at_the_size_limit_allocates_nothing(gpulib):
+    """n = 2^26, where the chunk scratch is used to its last entry: still bit
+    for bit the allocating entry point's result, and the library's
+    allocation counter does not move during the call (the allocating entry
+    point, called for contrast, does allocate)."""
+    from fricc_gb300 import _lib
+    rng = np.random.default_rng(12)
+    x_h = rng.random(MAX_N)
+    x = torch.from_numpy(x_h).cuda()
+    ref = torch.empty_like(x)
+    got = torch.empty_like(x)
+    torch.cuda.synchronize()
+    before = gpulib.fricc_alloc_count()
+    _lib.check(_call(gpulib, "fricc_seq_cumsum_noalloc", x, got))
+    torch.cuda.synchronize()
+    assert gpulib.fricc_alloc_count() == before
+    _lib.check(_call(gpulib, "fricc_seq_cumsum", x, ref))
+    torch.cuda.synchronize()
+    assert gpulib.fricc_alloc_count() > before
+    assert np.array_equal(ref.cpu().numpy().view(np.int64), got.cpu().numpy().view(np.int64))
+
+
 def test_noalloc_rejects_oversize(gpulib):
     x = torch.zeros(4, dtype=torch.float64, device="cuda")
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
