@@ -75,6 +75,24 @@ SIGNATURES = [
     ("fricc_combine", ctypes.c_int, [_i64p, ctypes.c_int, _vpp, _i64p, ctypes.c_int, _vpp, _i64p, ctypes.c_int,
                                       _vpp, _i64p, ctypes.POINTER(ctypes.c_double), ctypes.c_int, _vp]),
     ("fricc_zero", ctypes.c_int, [_vp, _i64, _vp]),
+    ("fricc_gemm_f64_b2", ctypes.c_int, [_dp, _dp, _dp, _i64, _i64, _i64, _i64, _i64, _i64p, _i64p, _i64p,
+                                          ctypes.c_double, ctypes.c_double, _vp]),
+    ("fricc_gemm_df_b2", ctypes.c_int, [_dp, _dp, _dp, _i64, _i64, _i64, _i64, _i64, _i64p, _i64p, _i64p,
+                                         ctypes.c_double, ctypes.c_double, _vp]),
+    ("fricc_combine5", ctypes.c_int, [_i64p, ctypes.c_int, _vpp, _i64p, ctypes.c_int, _vpp, _i64p, ctypes.c_int,
+                                       _vpp, _i64p, ctypes.POINTER(ctypes.c_double), ctypes.c_int, _vp]),
+    ("fricc_spb_create", ctypes.c_int, [ctypes.c_int, _i64p, _i64, _vp, ctypes.POINTER(_vp)]),
+    ("fricc_spb_destroy", ctypes.c_int, [_vp]),
+    ("fricc_spb_recompress_pair", ctypes.c_int, [_vp, _dp, _dp, _vp]),
+    ("fricc_spb_status", ctypes.c_int, [_vp, ctypes.POINTER(ctypes.c_int)]),
+    ("fricc_spb_export", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, _vp, _vp, _vp]),
+    ("fricc_spb_spmm", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                      ctypes.c_double, _dp, _i64, _i64, _dp, _i64, _vp]),
+    ("fricc_spb_spmm_f2", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                         ctypes.c_double, _vp, _i64, _i64, _dp, _i64, _vp]),
+    ("fricc_symadd_b", ctypes.c_int, [_dp, _dp, _i64, _i64, _i64, _i64p, ctypes.c_double, _vp]),
+    ("fricc_energy_update_batch", ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _i64, _dp,
+                                                 _dp, _dp, _vp]),
     ("fricc_phase_timing_set", ctypes.c_int, [ctypes.c_int]),
     ("fricc_phase_timing_read", ctypes.c_int, [ctypes.POINTER(ctypes.c_double)]),
     ("fricc_contract_flops", ctypes.c_double, [ctypes.c_char_p, _vp]),

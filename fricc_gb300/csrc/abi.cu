@@ -35,13 +35,28 @@ int fricc_densify_bf16x3_device(FriccSparse* T, int pa, int pb, int ka, int kb, 
                                 cudaStream_t st);
 int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
                          const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
-                         cudaStream_t st);
+                         cudaStream_t st, int64_t batch2, const int64_t* s2);
 int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N,
                           int64_t K, const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha,
-                          double beta, cudaStream_t st);
-int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x, const int64_t* sx, int n_prod,
+                          double beta, cudaStream_t st, int64_t batch2, const int64_t* s2);
+int fricc_combine_device(const int64_t dims[5], int n_in, const double* const* x, const int64_t* sx, int n_prod,
                          const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
                          const double* coef, int accumulate, cudaStream_t st);
+int fricc_combine4_device(const int64_t dims[4], int n_in, const double* const* x, const int64_t* sx, int n_prod,
+                          const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
+                          const double* coef, int accumulate, cudaStream_t st);
+int fricc_compress_pair_batch_device(const double* x, int64_t n, int64_t m, int R, const double* rn_dev,
+                                     int64_t* flatA, double* valsA, unsigned long long* metaA, int64_t* flatB,
+                                     double* valsB, unsigned long long* metaB, cudaStream_t st);
+int fricc_unpack_batch_async(const int64_t* flat, int64_t m, int R, const int64_t dims[4], int* slots,
+                             unsigned long long* meta, cudaStream_t st);
+int fricc_batch_spmm_device(FriccSparseBatch* B, int which, int pa, int pb, int ka, int kb, double coef,
+                            const void* Wp, int64_t w_stride, int64_t QS, double* Op, int64_t o_stride, bool f2,
+                            cudaStream_t st);
+int fricc_energy_update_batch_device(int R, const double* t1num, const double* t2num, const double* eia,
+                                     const double* fov, const double* ovov, const double* t1old, const double* t2old,
+                                     int64_t o, int64_t v, double* t1out, double* t2out, double* res,
+                                     cudaStream_t st);
 int fricc_energy_update_device(const double* t1num, const double* t2num, const double* eia, const double* fov,
                                const double* ovov, const double* t1old, const double* t2old, int64_t o, int64_t v,
                                double* t1out, double* t2out, double* res, cudaStream_t st, bool linear);
@@ -630,7 +645,7 @@ int fricc_gemm_df(const double* A, const double* B, double* C, int64_t batch, in
     fricc_set_error("gemm_df: null stride array");
     return FRICC_ERR_ARG;
   }
-  return fricc_gemm_df_device(A, B, C, batch, M, N, K, sA, sB, sC, alpha, beta, as_stream(stream));
+  return fricc_gemm_df_device(A, B, C, batch, M, N, K, sA, sB, sC, alpha, beta, as_stream(stream), 1, nullptr);
 }
 
 int fricc_gemm_f64(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
@@ -640,13 +655,176 @@ int fricc_gemm_f64(const double* A, const double* B, double* C, int64_t batch, i
     fricc_set_error("gemm_f64: null stride array");
     return FRICC_ERR_ARG;
   }
-  return fricc_gemm_f64_device(A, B, C, batch, M, N, K, sA, sB, sC, alpha, beta, as_stream(stream));
+  return fricc_gemm_f64_device(A, B, C, batch, M, N, K, sA, sB, sC, alpha, beta, as_stream(stream), 1, nullptr);
 }
 
 int fricc_combine(const int64_t dims[4], int n_in, const double* const* x, const int64_t* sx, int n_prod,
                   const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
                   const double* coef, int accumulate, void* stream) {
+  return fricc_combine4_device(dims, n_in, x, sx, n_prod, p, sp, n_out, out, so, coef, accumulate, as_stream(stream));
+}
+
+int fricc_gemm_f64_b2(const double* A, const double* B, double* C, int64_t batch, int64_t batch2, int64_t M,
+                      int64_t N, int64_t K, const int64_t sA[4], const int64_t sB[4], const int64_t sC[4], double alpha,
+                      double beta, void* stream) {
+  if (!sA || !sB || !sC) {
+    fricc_set_error("gemm_f64_b2: null stride array");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t s2[3] = {sA[3], sB[3], sC[3]};
+  return fricc_gemm_f64_device(A, B, C, batch, M, N, K, sA, sB, sC, alpha, beta, as_stream(stream), batch2, s2);
+}
+
+int fricc_gemm_df_b2(const double* A, const double* B, double* C, int64_t batch, int64_t batch2, int64_t M, int64_t N,
+                     int64_t K, const int64_t sA[4], const int64_t sB[4], const int64_t sC[4], double alpha,
+                     double beta, void* stream) {
+  if (!sA || !sB || !sC) {
+    fricc_set_error("gemm_df_b2: null stride array");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t s2[3] = {sA[3], sB[3], sC[3]};
+  return fricc_gemm_df_device(A, B, C, batch, M, N, K, sA, sB, sC, alpha, beta, as_stream(stream), batch2, s2);
+}
+
+int fricc_combine5(const int64_t dims[5], int n_in, const double* const* x, const int64_t* sx, int n_prod,
+                   const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
+                   const double* coef, int accumulate, void* stream) {
   return fricc_combine_device(dims, n_in, x, sx, n_prod, p, sp, n_out, out, so, coef, accumulate, as_stream(stream));
+}
+
+int fricc_spb_create(int R, const int64_t dims[4], int64_t m, void* stream, fricc_spbatch** out) {
+  if (!out || R < 1 || R > 65535 || bad_dims(dims) || m <= 0) {
+    fricc_set_error("spb_create: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  *out = nullptr;
+  const int64_t n = dims[0] * dims[1] * dims[2] * dims[3];
+  if (m > n || n >= 0xffffffffLL) {
+    fricc_set_error("Bad m_keep value: need 0 < m <= tensor size < 2^32 (m=%lld, size=%lld)", (long long)m,
+                    (long long)n);
+    return FRICC_ERR_ARG;
+  }
+  cudaStream_t st = as_stream(stream);
+  auto* B = new FriccSparseBatch();
+  B->R = R;
+  for (int k = 0; k < 4; ++k) B->dims[k] = dims[k];
+  B->m = m;
+  B->owner_stream = st;
+  cudaGetDevice(&B->device);
+  int rc = FRICC_OK;
+  for (int w = 0; w < 2 && !rc; ++w) {
+    rc = fricc_alloc_t(&B->flat[w], (size_t)R * m, st);
+    if (!rc) rc = fricc_alloc_t(&B->vals[w], (size_t)R * m, st);
+    if (!rc) rc = fricc_alloc_t(&B->slots[w], (size_t)R * m * 4, st);
+    if (!rc) rc = fricc_alloc_t(&B->meta[w], (size_t)R * 2, st);
+    if (!rc) rc = fricc_cuda_check(cudaMemsetAsync(B->meta[w], 0, (size_t)R * 2 * sizeof(unsigned long long), st),
+                                   "memset");
+  }
+  if (rc) {
+    fricc_spb_destroy(B);
+    return rc;
+  }
+  *out = B;
+  return FRICC_OK;
+}
+
+int fricc_spb_destroy(fricc_spbatch* B) {
+  if (!B) return FRICC_OK;
+  cudaStream_t st = B->owner_stream;
+  for (int w = 0; w < 2; ++w) {
+    fricc_free(B->flat[w], st);
+    fricc_free(B->vals[w], st);
+    fricc_free(B->slots[w], st);
+    fricc_free(B->meta[w], st);
+    for (auto& b : B->buck[w]) {
+      fricc_free(b.bptr, st);
+      fricc_free(b.order, st);
+    }
+  }
+  cudaStreamSynchronize(st);
+  delete B;
+  return FRICC_OK;
+}
+
+int fricc_spb_recompress_pair(fricc_spbatch* B, const double* t2, const double* rn_dev, void* stream) {
+  if (!B || !t2 || !rn_dev) {
+    fricc_set_error("spb_recompress_pair: null argument");
+    return FRICC_ERR_ARG;
+  }
+  cudaStream_t st = as_stream(stream);
+  const int64_t n = B->dims[0] * B->dims[1] * B->dims[2] * B->dims[3];
+  // the status words start clean: each compression ORs its error bits in
+  int rc = fricc_cuda_check(cudaMemsetAsync(B->meta[0], 0, (size_t)B->R * 2 * sizeof(unsigned long long), st), "meta");
+  if (!rc) rc = fricc_cuda_check(cudaMemsetAsync(B->meta[1], 0, (size_t)B->R * 2 * sizeof(unsigned long long), st),
+                                 "meta");
+  if (!rc) rc = fricc_compress_pair_batch_device(t2, n, B->m, B->R, rn_dev, B->flat[0], B->vals[0], B->meta[0],
+                                                 B->flat[1], B->vals[1], B->meta[1], st);
+  for (int w = 0; w < 2 && !rc; ++w)
+    rc = fricc_unpack_batch_async(B->flat[w], B->m, B->R, B->dims, B->slots[w], B->meta[w], st);
+  for (auto& bw : B->buck)
+    for (auto& b : bw) b.valid = false;
+  if (!rc) B->compressed = true;
+  return rc;
+}
+
+int fricc_spb_status(fricc_spbatch* B, int* replica) {
+  if (!B) {
+    fricc_set_error("spb_status: null batch");
+    return FRICC_ERR_ARG;
+  }
+  if (replica) *replica = -1;
+  std::vector<unsigned long long> h((size_t)B->R * 4);
+  FRICC_CUDA(cudaMemcpyAsync(h.data(), B->meta[0], (size_t)B->R * 2 * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, B->owner_stream));
+  FRICC_CUDA(cudaMemcpyAsync(h.data() + 2 * B->R, B->meta[1], (size_t)B->R * 2 * sizeof(unsigned long long),
+                             cudaMemcpyDeviceToHost, B->owner_stream));
+  FRICC_CUDA(cudaStreamSynchronize(B->owner_stream));
+  for (int k = 0; k < 2 * B->R; ++k) {
+    const unsigned e = (unsigned)h[2 * (size_t)k + 1];
+    if (e) {
+      if (replica) *replica = k % B->R;
+      return fricc_dev_status(e);
+    }
+  }
+  return FRICC_OK;
+}
+
+int fricc_spb_export(fricc_spbatch* B, int which, int r, int64_t* flat_host, double* vals_host, void* stream) {
+  if (!B || which < 0 || which > 1 || r < 0 || r >= B->R || !B->compressed) {
+    fricc_set_error("spb_export: bad arguments (or nothing compressed yet)");
+    return FRICC_ERR_ARG;
+  }
+  cudaStream_t st = as_stream(stream);
+  const size_t off = (size_t)r * B->m;
+  if (flat_host)
+    FRICC_CUDA(cudaMemcpyAsync(flat_host, B->flat[which] + off, B->m * sizeof(int64_t), cudaMemcpyDeviceToHost, st));
+  if (vals_host)
+    FRICC_CUDA(cudaMemcpyAsync(vals_host, B->vals[which] + off, B->m * sizeof(double), cudaMemcpyDeviceToHost, st));
+  FRICC_CUDA(cudaStreamSynchronize(st));
+  return FRICC_OK;
+}
+
+int fricc_spb_spmm(fricc_spbatch* B, int which, int pa, int pb, int ka, int kb, double coef, const double* Wp,
+                   int64_t w_stride, int64_t QS, double* Op, int64_t o_stride, void* stream) {
+  return fricc_batch_spmm_device(B, which, pa, pb, ka, kb, coef, Wp, w_stride, QS, Op, o_stride, false,
+                                 as_stream(stream));
+}
+
+int fricc_spb_spmm_f2(fricc_spbatch* B, int which, int pa, int pb, int ka, int kb, double coef, const void* W2,
+                      int64_t w2_stride, int64_t QS, double* Op, int64_t o_stride, void* stream) {
+  return fricc_batch_spmm_device(B, which, pa, pb, ka, kb, coef, W2, w2_stride, QS, Op, o_stride, true,
+                                 as_stream(stream));
+}
+
+int fricc_energy_update_batch(int R, const double* t1num, const double* t2num, const double* eia, const double* fov,
+                              const double* ovov, const double* t1old, const double* t2old, int64_t o, int64_t v,
+                              double* t1out, double* t2out, double* res, void* stream) {
+  if (!t1num || !t2num || !eia || !fov || !ovov || !t1old || !t2old || !t1out || !t2out || !res) {
+    fricc_set_error("energy_update_batch: null argument");
+    return FRICC_ERR_ARG;
+  }
+  return fricc_energy_update_batch_device(R, t1num, t2num, eia, fov, ovov, t1old, t2old, o, v, t1out, t2out, res,
+                                          as_stream(stream));
 }
 
 int fricc_zero(void* p, int64_t bytes, void* stream) {

@@ -1,21 +1,23 @@
-// Strided elementwise combinations over a 4-D index space:
+// Strided elementwise combinations over a 5-D index space (the 4-D entry
+// point is the 5-D one with a leading extent 1; the fifth dimension is the
+// replica of a replica batch):
 //
 //   r_k(i) = sum_t c[k][t] x_t(i) + c[k][n_in] p_0(i) p_1(i) ... (product term)
 //   out_k(i) = r_k(i)               (accumulate = 0)
 //   out_k(i) = out_k(i) + r_k(i)    (accumulate = 1)
 //
-// for every i = (i0, i1, i2, i3) < dims, where every operand is a view
-// x_t(i) = x_t[i0 s0 + i1 s1 + i2 s2 + i3 s3] with its own element strides
+// for every i = (i0, .., i4) < dims, where every operand is a view
+// x_t(i) = x_t[i0 s0 + .. + i4 s4] with its own element strides
 // (0 broadcasts).  The permuted copies, linear combinations, broadcast
 // products and diagonal updates of an FRI-CCSD iteration's intermediates
 // (fricc/friccsd.py:144-301 and the W builds :309-376) run here, so every
 // elementwise pass of the iteration is a launch of this library.
 //
-// The index space runs i3 fastest; callers order it so that the first
-// output is contiguous along i3.  Inputs contiguous along i3 (or
+// The index space runs i4 fastest; callers order it so that the first
+// output is contiguous along i4.  Inputs contiguous along i4 (or
 // broadcast, or scattered) are read directly; an input contiguous along
 // another dimension d (a transposed view) is read through 32 x 32 shared-
-// memory tiles of the plane (d, 3), so that its reads and the outputs'
+// memory tiles of the plane (d, 4), so that its reads and the outputs'
 // accesses both coalesce.  Inputs are grouped by that layout and each group
 // is one pass (the first writes or accumulates as asked, later ones
 // accumulate), so a result is r_k summed group by group: deterministic for
@@ -51,23 +53,25 @@ struct FastDiv {
   __device__ __forceinline__ unsigned div(unsigned n) const { return m ? (__umulhi(n, m) >> s) : n; }
 };
 
+constexpr int D = 5;
+
 struct CombineArgs {
-  int64_t d[4];
+  int64_t d[D];
   int64_t n;                // product of the dims
-  FastDiv f1, f2, f3;       // dims[1..3] (32-bit path)
+  FastDiv f1, f2, f3, f4;   // dims[1..4] (32-bit path)
   const double* x[kMaxIn];
-  int64_t sx[kMaxIn][4];
+  int64_t sx[kMaxIn][D];
   const double* p[kMaxProd];
-  int64_t sp[kMaxProd][4];
+  int64_t sp[kMaxProd][D];
   double* out[kMaxOut];
-  int64_t so[kMaxOut][4];
+  int64_t so[kMaxOut][D];
   double c[kMaxOut][kMaxIn + 1];
   int acc[kMaxOut];  // per output: add to its current value (1) or overwrite it (0)
 };
 
 template <typename I>
-__device__ __forceinline__ I off4(const int64_t s[4], I i0, I i1, I i2, I i3) {
-  return i0 * (I)s[0] + i1 * (I)s[1] + i2 * (I)s[2] + i3 * (I)s[3];
+__device__ __forceinline__ I off5(const int64_t s[D], I i0, I i1, I i2, I i3, I i4) {
+  return i0 * (I)s[0] + i1 * (I)s[1] + i2 * (I)s[2] + i3 * (I)s[3] + i4 * (I)s[4];
 }
 
 // r_k from the loaded values; old[k] is out_k's value before the call
@@ -114,17 +118,22 @@ __global__ void __launch_bounds__(256) k_combine(const CombineArgs a) {
       const I t = base + (I)e * stride;
       pv[e] = 0.0;
       if (t >= n) continue;
-      I r, i3, i2, i1;
+      I r, i4, i3, i2, i1;
       if constexpr (sizeof(I) == 4) {
-        r = a.f3.div(t);
-        i3 = t - r * (I)a.d[3];
-        const I r2 = a.f2.div(r);
-        i2 = r - r2 * (I)a.d[2];
-        r = a.f1.div(r2);
-        i1 = r2 - r * (I)a.d[1];
+        r = a.f4.div(t);
+        i4 = t - r * (I)a.d[4];
+        I r2 = a.f3.div(r);
+        i3 = r - r2 * (I)a.d[3];
+        r = a.f2.div(r2);
+        i2 = r2 - r * (I)a.d[2];
+        r2 = a.f1.div(r);
+        i1 = r - r2 * (I)a.d[1];
+        r = r2;
       } else {
-        i3 = t % a.d[3];
-        r = t / a.d[3];
+        i4 = t % a.d[4];
+        r = t / a.d[4];
+        i3 = r % a.d[3];
+        r /= a.d[3];
         i2 = r % a.d[2];
         r /= a.d[2];
         i1 = r % a.d[1];
@@ -132,15 +141,15 @@ __global__ void __launch_bounds__(256) k_combine(const CombineArgs a) {
       }
 #pragma unroll
       for (int k = 0; k < NOUT; ++k) {
-        op[e][k] = a.out[k] + off4<I>(a.so[k], r, i1, i2, i3);
+        op[e][k] = a.out[k] + off5<I>(a.so[k], r, i1, i2, i3, i4);
         old[e][k] = a.acc[k] ? *op[e][k] : 0.0;
       }
 #pragma unroll
-      for (int s = 0; s < NIN; ++s) xv[e][s] = __ldg(a.x[s] + off4<I>(a.sx[s], r, i1, i2, i3));
+      for (int s = 0; s < NIN; ++s) xv[e][s] = __ldg(a.x[s] + off5<I>(a.sx[s], r, i1, i2, i3, i4));
       if (NPROD > 0) {
-        double q = __ldg(a.p[0] + off4<I>(a.sp[0], r, i1, i2, i3));
+        double q = __ldg(a.p[0] + off5<I>(a.sp[0], r, i1, i2, i3, i4));
 #pragma unroll
-        for (int s = 1; s < NPROD; ++s) q = q * __ldg(a.p[s] + off4<I>(a.sp[s], r, i1, i2, i3));
+        for (int s = 1; s < NPROD; ++s) q = q * __ldg(a.p[s] + off5<I>(a.sp[s], r, i1, i2, i3, i4));
         pv[e] = q;
       }
     }
@@ -152,33 +161,35 @@ __global__ void __launch_bounds__(256) k_combine(const CombineArgs a) {
   }
 }
 
-// Inputs contiguous along dimension 2 (the host moves the transposed
-// dimension there): 32 x 32 tiles of the plane (2, 3).  Thread (x, y) of
-// 32 x 8 stages element (i2 = x, i3 = y + 8 r) of every input and computes
-// element (i3 = x, i2 = y + 8 r), r < 4.  Dimensions 0 and 1 run over
+// Inputs contiguous along dimension 3 (the host moves the transposed
+// dimension there): 32 x 32 tiles of the plane (3, 4).  Thread (x, y) of
+// 32 x 8 stages element (i3 = x, i4 = y + 8 r) of every input and computes
+// element (i4 = x, i3 = y + 8 r), r < 4.  Dimensions 0..2 run over
 // blockIdx.y.
 struct TileArgs {
-  int64_t nt3;        // tiles along dimension 3
-  int64_t ntiles;     // tiles in the (2, 3) plane
-  int64_t nrest;      // dims[0] * dims[1]
+  int64_t nt4;        // tiles along dimension 4
+  int64_t ntiles;     // tiles in the (3, 4) plane
+  int64_t nrest;      // dims[0] * dims[1] * dims[2]
 };
 
 template <int NIN, int NOUT, typename I>
 __global__ void __launch_bounds__(256) k_combine_t(const CombineArgs a, const TileArgs ta) {
   extern __shared__ double sm[];  // [NIN][32][33]
   const int x = threadIdx.x & 31, y = threadIdx.x >> 5;
-  const I t3 = (I)(blockIdx.x % ta.nt3), t2 = (I)(blockIdx.x / ta.nt3);
-  const I d2 = (I)a.d[2], d3 = (I)a.d[3];
+  const I t4 = (I)(blockIdx.x % ta.nt4), t3 = (I)(blockIdx.x / ta.nt4);
+  const I d3 = (I)a.d[3], d4 = (I)a.d[4];
   for (int64_t rest = blockIdx.y; rest < ta.nrest; rest += gridDim.y) {
-    const I i0 = (I)(rest / a.d[1]), i1 = (I)(rest % a.d[1]);
+    const I i2 = (I)(rest % a.d[2]);
+    const int64_t r01 = rest / a.d[2];
+    const I i1 = (I)(r01 % a.d[1]), i0 = (I)(r01 / a.d[1]);
     __syncthreads();  // the previous tile's reads of shared memory are done
     double v[NIN][4];
 #pragma unroll
     for (int s = 0; s < NIN; ++s)
 #pragma unroll
       for (int r = 0; r < 4; ++r) {
-        const I i2 = t2 * 32 + x, i3 = t3 * 32 + y + 8 * r;
-        v[s][r] = (i2 < d2 && i3 < d3) ? __ldg(a.x[s] + off4<I>(a.sx[s], i0, i1, i2, i3)) : 0.0;
+        const I i3 = t3 * 32 + x, i4 = t4 * 32 + y + 8 * r;
+        v[s][r] = (i3 < d3 && i4 < d4) ? __ldg(a.x[s] + off5<I>(a.sx[s], i0, i1, i2, i3, i4)) : 0.0;
       }
 #pragma unroll
     for (int s = 0; s < NIN; ++s)
@@ -189,19 +200,19 @@ __global__ void __launch_bounds__(256) k_combine_t(const CombineArgs a, const Ti
     double* op[4][NOUT];
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      const I i3 = t3 * 32 + x, i2 = t2 * 32 + y + 8 * r;
-      const bool in = i3 < d3 && i2 < d2;
+      const I i4 = t4 * 32 + x, i3 = t3 * 32 + y + 8 * r;
+      const bool in = i4 < d4 && i3 < d3;
 #pragma unroll
       for (int k = 0; k < NOUT; ++k) {
-        op[r][k] = a.out[k] + (in ? off4<I>(a.so[k], i0, i1, i2, i3) : (I)0);
+        op[r][k] = a.out[k] + (in ? off5<I>(a.so[k], i0, i1, i2, i3, i4) : (I)0);
         old[r][k] = (a.acc[k] && in) ? *op[r][k] : 0.0;
       }
     }
     __syncthreads();
 #pragma unroll
     for (int r = 0; r < 4; ++r) {
-      const I i3 = t3 * 32 + x, i2 = t2 * 32 + y + 8 * r;
-      if (i3 >= d3 || i2 >= d2) continue;
+      const I i4 = t4 * 32 + x, i3 = t3 * 32 + y + 8 * r;
+      if (i4 >= d4 || i3 >= d3) continue;
       double xv[NIN];
 #pragma unroll
       for (int s = 0; s < NIN; ++s) xv[s] = sm[(s * 32 + y + 8 * r) * 33 + x];
@@ -265,9 +276,9 @@ void launch_tiled(const CombineArgs& a, int n_in, int n_out, const TileArgs& ta,
 
 // the largest element offset a view reaches (INT64_MAX for a negative
 // stride, which the 32-bit path cannot take)
-int64_t reach(const int64_t d[4], const int64_t s[4]) {
+int64_t reach(const int64_t d[D], const int64_t s[D]) {
   int64_t r = 0;
-  for (int k = 0; k < 4; ++k) {
+  for (int k = 0; k < D; ++k) {
     if (s[k] < 0) return INT64_MAX;
     r += (d[k] - 1) * s[k];
   }
@@ -276,7 +287,7 @@ int64_t reach(const int64_t d[4], const int64_t s[4]) {
 
 }  // namespace
 
-int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x, const int64_t* sx, int n_prod,
+int fricc_combine_device(const int64_t dims[5], int n_in, const double* const* x, const int64_t* sx, int n_prod,
                          const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
                          const double* coef, int accumulate, cudaStream_t st) {
   if (!dims || n_in < 0 || n_in > kMaxIn || n_prod < 0 || n_prod > kMaxProd || n_out < 1 || n_out > kMaxOut ||
@@ -286,7 +297,7 @@ int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x
     return FRICC_ERR_ARG;
   }
   int64_t n = 1;
-  for (int d = 0; d < 4; ++d) {
+  for (int d = 0; d < D; ++d) {
     if (dims[d] < 0) {
       fricc_set_error("combine: negative dimension");
       return FRICC_ERR_ARG;
@@ -311,15 +322,15 @@ int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x
     }
   const int nc = n_in + (n_prod > 0 ? 1 : 0);
 
-  // group the inputs by layout: -1 read directly (contiguous along 3,
-  // broadcast or scattered), d in 0..2 contiguous along d (tiled)
+  // group the inputs by layout: -1 read directly (contiguous along 4,
+  // broadcast or scattered), d in 0..3 contiguous along d (tiled)
   int group[kMaxIn];
   for (int s = 0; s < n_in; ++s) {
     group[s] = -1;
-    const int64_t* st4 = sx + 4 * s;
-    if (st4[3] == 1 || st4[3] == 0 || dims[3] < 8) continue;
-    for (int d = 0; d < 3; ++d)
-      if (st4[d] == 1 && dims[d] >= 8) {
+    const int64_t* st5 = sx + D * s;
+    if (st5[4] == 1 || st5[4] == 0 || dims[4] < 8) continue;
+    for (int d = 0; d < 4; ++d)
+      if (st5[d] == 1 && dims[d] >= 8) {
         group[s] = d;
         break;
       }
@@ -336,7 +347,7 @@ int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x
     for (int t = 0; t < nc; ++t) reached[k] = reached[k] || coef[k * nc + t] != 0.0;
   }
   bool first_pass = true;
-  for (int gsel = -1; gsel < 3; ++gsel) {
+  for (int gsel = -1; gsel < 4; ++gsel) {
     int members[kMaxIn], nm = 0;
     for (int s = 0; s < n_in; ++s)
       if (group[s] == gsel) members[nm++] = s;
@@ -350,29 +361,29 @@ int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x
     }
     if (no == 0) continue;
     CombineArgs a{};
-    // dimension order: the tiled dimension moves to position 2
-    int order[4] = {0, 1, 2, 3};
+    // dimension order: the tiled dimension moves to position 3
+    int order[D] = {0, 1, 2, 3, 4};
     if (gsel >= 0) {
       int nr = 0;
-      for (int d = 0; d < 3; ++d)
+      for (int d = 0; d < 4; ++d)
         if (d != gsel) order[nr++] = d;
-      order[2] = gsel;
+      order[3] = gsel;
     }
-    for (int d = 0; d < 4; ++d) a.d[d] = dims[order[d]];
+    for (int d = 0; d < D; ++d) a.d[d] = dims[order[d]];
     a.n = n;
     for (int j = 0; j < nm; ++j) {
       a.x[j] = x[members[j]];
-      for (int d = 0; d < 4; ++d) a.sx[j][d] = sx[4 * members[j] + order[d]];
+      for (int d = 0; d < D; ++d) a.sx[j][d] = sx[D * members[j] + order[d]];
     }
     if (with_prod)
       for (int s = 0; s < n_prod; ++s) {
         a.p[s] = p[s];
-        for (int d = 0; d < 4; ++d) a.sp[s][d] = sp[4 * s + order[d]];
+        for (int d = 0; d < D; ++d) a.sp[s][d] = sp[D * s + order[d]];
       }
     for (int q = 0; q < no; ++q) {
       const int k = outs[q];
       a.out[q] = out[k];
-      for (int d = 0; d < 4; ++d) a.so[q][d] = so[4 * k + order[d]];
+      for (int d = 0; d < D; ++d) a.so[q][d] = so[D * k + order[d]];
       for (int j = 0; j < nm; ++j) a.c[q][j] = coef[k * nc + members[j]];
       if (with_prod) a.c[q][nm] = coef[k * nc + n_in];
       a.acc[q] = touched[k] ? 1 : 0;
@@ -388,6 +399,7 @@ int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x
       a.f1.set((unsigned)a.d[1]);
       a.f2.set((unsigned)a.d[2]);
       a.f3.set((unsigned)a.d[3]);
+      a.f4.set((unsigned)a.d[4]);
     }
     if (gsel < 0) {
       int64_t g = fricc_cdiv(n, 256 * 4);
@@ -396,9 +408,9 @@ int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x
       else launch_direct_all<int64_t>(a, nm, with_prod ? n_prod : 0, n_out_pass, (unsigned)g, st);
     } else {
       TileArgs ta{};
-      ta.nt3 = fricc_cdiv(a.d[3], 32);
-      ta.ntiles = ta.nt3 * fricc_cdiv(a.d[2], 32);
-      ta.nrest = a.d[0] * a.d[1];
+      ta.nt4 = fricc_cdiv(a.d[4], 32);
+      ta.ntiles = ta.nt4 * fricc_cdiv(a.d[3], 32);
+      ta.nrest = a.d[0] * a.d[1] * a.d[2];
       if (ta.ntiles > 0x7fffffff) {
         fricc_set_error("combine: tile grid too large");
         return FRICC_ERR_ARG;
@@ -411,4 +423,27 @@ int fricc_combine_device(const int64_t dims[4], int n_in, const double* const* x
   }
   cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "combine", __FILE__, __LINE__);
+}
+
+// The 4-D form: a leading extent 1 and strides 0.
+int fricc_combine4_device(const int64_t dims[4], int n_in, const double* const* x, const int64_t* sx, int n_prod,
+                          const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
+                          const double* coef, int accumulate, cudaStream_t st) {
+  if (!dims || n_in < 0 || n_in > kMaxIn || n_prod < 0 || n_prod > kMaxProd || n_out < 1 || n_out > kMaxOut ||
+      (n_in > 0 && !sx) || (n_prod > 0 && !sp) || !so) {
+    fricc_set_error("combine: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  int64_t d5[D] = {1, dims[0], dims[1], dims[2], dims[3]};
+  int64_t sx5[kMaxIn * D], sp5[kMaxProd * D], so5[kMaxOut * D];
+  auto widen = [](const int64_t* s4, int64_t* s5, int cnt) {
+    for (int t = 0; t < cnt; ++t) {
+      s5[D * t] = 0;
+      for (int d = 0; d < 4; ++d) s5[D * t + 1 + d] = s4[4 * t + d];
+    }
+  };
+  widen(sx, sx5, n_in);
+  widen(sp, sp5, n_prod);
+  widen(so, so5, n_out);
+  return fricc_combine_device(d5, n_in, x, sx5, n_prod, p, sp5, n_out, out, so5, coef, accumulate, st);
 }

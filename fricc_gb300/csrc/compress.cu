@@ -38,7 +38,19 @@ __device__ __forceinline__ unsigned long long abs_key(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
 }
 
-__global__ void __launch_bounds__(256) k_hist12(const double* __restrict__ x, int64_t n, unsigned* __restrict__ hist) {
+// Replica batches (R compressions of R equal-sized tensors in one set of
+// launches): per-replica strides, in elements, of the n-sized arrays, the
+// m-sized arrays and the tile-state words; `one` is 1 for single words and
+// structs (0, with every stride 0, outside a batch).  The replica is
+// blockIdx.y, or blockIdx.x for the one-block kernels.
+struct Rep {
+  int64_t n = 0, m = 0, tile = 0, one = 0;
+};
+
+__global__ void __launch_bounds__(256) k_hist12(const double* __restrict__ x, int64_t n, unsigned* __restrict__ hist,
+                                                Rep rp = Rep{}) {
+  x += blockIdx.y * rp.n;
+  hist += blockIdx.y * rp.one * NDIG;
   __shared__ unsigned h[NDIG];
   for (int i = threadIdx.x; i < NDIG; i += 256) h[i] = 0;
   __syncthreads();
@@ -84,8 +96,20 @@ constexpr long long SPIN_LIMIT = 1ll << 22;
 __global__ void __launch_bounds__(256) k_compact(const double* __restrict__ x, int64_t n, const Ctl* __restrict__ c,
                                                  unsigned long long* __restrict__ ckey, unsigned* __restrict__ cidx,
                                                  unsigned long long* tstate, unsigned* ticket, unsigned* err,
-                                                 const unsigned long long* never_set, long long test_spins) {
+                                                 const unsigned long long* never_set, long long test_spins,
+                                                 Rep rp = Rep{}) {
   constexpr int NT = 256, ITEMS = 16, TILE = NT * ITEMS;
+  {
+    const int64_t r = blockIdx.y;
+    x += r * rp.n;
+    c += r * rp.one;
+    ckey += r * rp.n;
+    cidx += r * rp.n;
+    tstate += r * rp.tile;
+    never_set += r * rp.tile;
+    ticket += r * rp.one;
+    err += r * rp.one;
+  }
   const unsigned dmin = (unsigned)c->dmin;
   __shared__ int s_tile;
   __shared__ int64_t s_pre;
@@ -155,12 +179,16 @@ __global__ void __launch_bounds__(256) k_compact(const double* __restrict__ x, i
 
 struct GenAbs {
   const double* x;
+  int64_t rs = 0;  // replica stride of x
   __device__ __forceinline__ double operator()(int64_t i) const { return fabs(x[i]); }
+  __device__ __forceinline__ GenAbs at(int r) const { return GenAbs{x + r * rs, rs}; }
 };
 
 struct GenSorted {
   const unsigned long long* keys;
+  int64_t rs = 0;
   __device__ __forceinline__ double operator()(int64_t i) const { return __longlong_as_double((long long)keys[i]); }
+  __device__ __forceinline__ GenSorted at(int r) const { return GenSorted{keys + r * rs, rs}; }
 };
 
 // p_i of make_probability_vector (src/fri_utils.cpp:375,378-381); D membership
@@ -168,6 +196,8 @@ struct GenSorted {
 struct GenP {
   const double* x;
   const Ctl* c;
+  int64_t rs = 0, cs = 0;  // replica strides of x and c
+  __device__ __forceinline__ GenP at(int r) const { return GenP{x + r * rs, c + r * cs, rs, cs}; }
   __device__ __forceinline__ double operator()(int64_t i) const {
     const double a = fabs(x[i]);
     const unsigned long long k = abs_key(a);
@@ -194,6 +224,8 @@ struct GenPv {
   const double* P;
   const double* x;
   const Ctl* c;
+  int64_t rs = 0, cs = 0;  // replica strides of P and x, and of c
+  __device__ __forceinline__ GenPv at(int r) const { return GenPv{P + r * rs, x + r * rs, c + r * cs, rs, cs}; }
   __device__ __forceinline__ double operator()(int64_t i) const { return c->sample ? P[i] : 0.0; }
   __device__ __forceinline__ double value(int64_t i) const { return P[i]; }
 };
@@ -203,6 +235,10 @@ struct ConsAccept {
   int64_t m;
   double* Rb;                    // [m+1]: R before element d (Rb[m]: after the last)
   unsigned long long* first_fail;
+  int64_t one = 0;               // 1 in a replica batch
+  __device__ __forceinline__ ConsAccept at(int r) const {
+    return ConsAccept{m, Rb + r * one * (m + 1), first_fail + r * one, one};
+  }
   __device__ __forceinline__ void operator()(int64_t d, double before, double after, double a) const {
     Rb[d] = before;
     if (d == m - 1) Rb[m] = after;
@@ -225,6 +261,8 @@ __device__ __forceinline__ int64_t count_below(double I, double rn, int64_t mp) 
 struct ConsSample {
   const Ctl* c;
   unsigned* S;
+  int64_t cs = 0, ss = 0;  // replica strides of c and S
+  __device__ __forceinline__ ConsSample at(int r) const { return ConsSample{c + r * cs, S + r * ss, cs, ss}; }
   __device__ __forceinline__ void operator()(int64_t j, double lo, double hi, double p) const {
     if (!c->sample || !(p > 0.0)) return;
     const double rn = c->rn;
@@ -240,6 +278,7 @@ struct ConsSample {
 // probabilities, and the partial sums too.
 struct ConsSample2 {
   ConsSample a, b;
+  __device__ __forceinline__ ConsSample2 at(int r) const { return ConsSample2{a.at(r), b.at(r)}; }
   __device__ __forceinline__ void operator()(int64_t j, double lo, double hi, double p) const {
     a(j, lo, hi, p);
     b(j, lo, hi, p);
@@ -247,7 +286,9 @@ struct ConsSample2 {
 };
 
 // The select digit: the largest d with count(digit >= d) >= m (one thread).
-__global__ void k_select_digit(const unsigned* __restrict__ hist, int64_t m, Ctl* c) {
+__global__ void k_select_digit(const unsigned* __restrict__ hist, int64_t m, Ctl* c, Rep rp = Rep{}) {
+  hist += blockIdx.x * rp.one * NDIG;
+  c += blockIdx.x * rp.one;
   int64_t cum = 0;
   int d = NDIG - 1;
   for (; d >= 0; --d) {
@@ -261,7 +302,15 @@ __global__ void k_select_digit(const unsigned* __restrict__ hist, int64_t m, Ctl
 // After the remaining-norm chain: |D|, R, the D threshold, m' (one thread).
 __global__ void k_finish_d(const unsigned long long* __restrict__ ffail, const double* __restrict__ Rb,
                            const unsigned long long* __restrict__ ckey, const unsigned* __restrict__ cidx, int64_t m,
-                           Ctl* c) {
+                           Ctl* c, Rep rp = Rep{}) {
+  {
+    const int64_t r = blockIdx.x;
+    ffail += r * rp.one;
+    Rb += r * rp.one * (m + 1);
+    ckey += r * rp.n;
+    cidx += r * rp.n;
+    c += r * rp.one;
+  }
   const int64_t nd = (int64_t)*ffail;
   c->nd = nd;
   c->mp = m - nd;
@@ -279,7 +328,16 @@ __global__ void k_zero_u32(unsigned* p, int64_t n) {
 
 // D part of the output: flat = sorted index, value = x (src/fri_utils.cpp:494,498-500)
 __global__ void k_out_d(const double* __restrict__ x, const unsigned* __restrict__ sidx, int64_t nd_max,
-                        const Ctl* __restrict__ c, int64_t* __restrict__ flat, double* __restrict__ vals) {
+                        const Ctl* __restrict__ c, int64_t* __restrict__ flat, double* __restrict__ vals,
+                        Rep rp = Rep{}) {
+  {
+    const int64_t r = blockIdx.y;
+    x += r * rp.n;
+    sidx += r * rp.n;
+    if (c) c += r * rp.one;
+    flat += r * rp.m;
+    vals += r * rp.m;
+  }
   const int64_t nd = c ? c->nd : nd_max;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < nd; i += (int64_t)gridDim.x * blockDim.x) {
     const unsigned j = sidx[i];
@@ -290,8 +348,12 @@ __global__ void k_out_d(const double* __restrict__ x, const unsigned* __restrict
 
 // S part: flat = S_k, value = x / p (src/fri_utils.cpp:495,502-504)
 template <class G>
-__global__ void k_out_s(G gp, const unsigned* __restrict__ S, int64_t* __restrict__ flat,
-                        double* __restrict__ vals) {
+__global__ void k_out_s(G gp0, const unsigned* __restrict__ S, int64_t* __restrict__ flat,
+                        double* __restrict__ vals, Rep rp = Rep{}) {
+  const G gp = exact::replica_of(gp0, blockIdx.y);
+  S += blockIdx.y * rp.m;
+  flat += blockIdx.y * rp.m;
+  vals += blockIdx.y * rp.m;
   const int64_t mp = gp.c->mp, nd = gp.c->nd;
   for (int64_t k = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; k < mp; k += (int64_t)gridDim.x * blockDim.x) {
     const unsigned j = S[k];
@@ -301,15 +363,24 @@ __global__ void k_out_s(G gp, const unsigned* __restrict__ S, int64_t* __restric
 }
 
 __global__ void k_unpack(const int64_t* __restrict__ flat, int64_t m, int64_t d0, int64_t d1, int64_t d2, int64_t d3,
-                         int* __restrict__ slots, unsigned* err) {
+                         int* __restrict__ slots, unsigned* err, Rep rp = Rep{}) {
+  flat += blockIdx.y * rp.m;
+  slots += 4 * blockIdx.y * rp.m;
+  err += blockIdx.y * rp.one;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m; s += (int64_t)gridDim.x * blockDim.x) {
-    const unsigned long long f = (unsigned long long)flat[s];
+    unsigned long long f = (unsigned long long)flat[s];
     const unsigned long long D1 = d1, D2 = d2, D3 = d3;
+    if (f >= (unsigned long long)d0 * D1 * D2 * D3) {
+      // an index a failed compression left behind: flagged, and unpacked as
+      // (0,0,0,0) so that the contractions launched before the status is
+      // read stay inside their operands
+      atomicOr(err, FRICC_DEV_INDEX);
+      f = 0;
+    }
     const unsigned long long i0 = f / (D1 * D2 * D3);
     const unsigned long long i1 = f % (D1 * D2 * D3) / (D2 * D3);
     const unsigned long long i2 = f % (D2 * D3) / D3;
     const unsigned long long i3 = f % D3;
-    if (i0 >= (unsigned long long)d0) atomicOr(err, FRICC_DEV_INDEX);
     slots[4 * s + 0] = (int)i0;
     slots[4 * s + 1] = (int)i1;
     slots[4 * s + 2] = (int)i2;
@@ -335,7 +406,10 @@ __global__ void k_unpack(const int64_t* __restrict__ flat, int64_t m, int64_t d0
 // element emits, bit 2 it emits the pivot.
 constexpr unsigned char PV_TAKE = 1, PV_EMIT = 2, PV_PIVOT = 4;
 
-__global__ void k_pvec(GenP gp, int64_t n, double* __restrict__ P, unsigned* err) {
+__global__ void k_pvec(GenP gp0, int64_t n, double* __restrict__ P, unsigned* err, Rep rp = Rep{}) {
+  const GenP gp = gp0.at(blockIdx.y);
+  P += blockIdx.y * rp.n;
+  err += blockIdx.y * rp.one;
   bool bad = false;
   for (int64_t i = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; i < n; i += (int64_t)gridDim.x * blockDim.x) {
     const double p = gp.value(i);
@@ -571,7 +645,11 @@ __global__ void k_piv_final(const double* __restrict__ A, int64_t n, Ctl* c, uns
 __global__ void k_set_u64(unsigned long long* p, unsigned long long v) { *p = v; }
 
 // |D| (m for "largest") and the error word into a handle's status block
-__global__ void k_put_meta(const Ctl* c, int64_t nd_fixed, const unsigned* err, unsigned long long* meta) {
+__global__ void k_put_meta(const Ctl* c, int64_t nd_fixed, const unsigned* err, unsigned long long* meta,
+                           Rep rp = Rep{}) {
+  if (c) c += blockIdx.x * rp.one;
+  err += blockIdx.x * rp.one;
+  meta += 2 * blockIdx.x * rp.one;
   meta[0] = (unsigned long long)(c ? c->nd : nd_fixed);
   meta[1] |= (unsigned long long)*err;
 }
@@ -1139,6 +1217,209 @@ done:
   fricc_free(ctl2, st);
   fricc_free(S2, st);
   return rc;
+}
+
+// ---------------------------------------------------------------------------
+// Replica batches: the paired systematic compression of R tensors of one
+// shape (replica r's tensor x + r n) in one set of launches -- every kernel
+// of the single path with the replica on its grid's y (or x) dimension, each
+// replica's arithmetic that of its own single compression, so each output is
+// bit for bit the one fricc_sp_recompress_pair would give.
+namespace {
+
+__global__ void k_fill_u64_b(unsigned long long* p, unsigned long long v, int R) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < R) p[r] = v;
+}
+
+// R0[r] = the exact one_norm of replica r (the end of its chain)
+__global__ void k_chain_end_b(const double* cstart, int64_t nch, double* R0, int R) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < R) R0[r] = cstart[(int64_t)r * (nch + 1) + nch];
+}
+
+// the replicas' draws into their two compression states
+__global__ void k_set_rn_b(Ctl* a, Ctl* b, const double* rn, int R) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < R) {
+    a[r].rn = rn[2 * r];
+    b[r].rn = rn[2 * r + 1];
+  }
+}
+
+__global__ void k_meta_or_b(const unsigned* err, unsigned long long* meta, int R) {
+  const int r = blockIdx.x * blockDim.x + threadIdx.x;
+  if (r < R) meta[2 * r + 1] |= (unsigned long long)err[r];
+}
+
+}  // namespace
+
+int fricc_compress_pair_batch_device(const double* x, int64_t n, int64_t m, int R, const double* rn_dev,
+                                     int64_t* flatA, double* valsA, unsigned long long* metaA, int64_t* flatB,
+                                     double* valsB, unsigned long long* metaB, cudaStream_t st) {
+  if (!x || !rn_dev || !flatA || !valsA || !metaA || !flatB || !valsB || !metaB || R < 1 || R > 65535) {
+    fricc_set_error("compress batch: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  if (n <= 0 || m <= 0 || m > n || n >= 0xffffffffLL) {
+    fricc_set_error("Bad m_keep value: need 0 < m <= tensor size < 2^32 (m=%lld, size=%lld)", (long long)m,
+                    (long long)n);
+    return FRICC_ERR_ARG;
+  }
+  const int64_t ntile = fricc_cdiv(n, 4096);
+  const int64_t nch_n = fricc_cdiv(n, exact::CH), nch_m = fricc_cdiv(m, exact::CH);
+  const int64_t rhw = radix::hist_words(n);
+  Rep rp;
+  rp.n = n;
+  rp.m = m;
+  rp.tile = ntile + 1;
+  rp.one = 1;
+  CompressScratch s;
+  Ctl *ctl = nullptr, *ctl2 = nullptr;
+  unsigned* S2 = nullptr;
+  double* R0 = nullptr;
+  int rc = FRICC_OK;
+#define TRY(x)         \
+  do {                 \
+    rc = (x);          \
+    if (rc) goto done; \
+  } while (0)
+  {
+    const unsigned rb = (unsigned)fricc_cdiv(R, 256);
+    TRY(fricc_alloc_t(&ctl, R, st));
+    TRY(fricc_alloc_t(&ctl2, R, st));
+    TRY(fricc_alloc_t(&s.hist, (size_t)R * NDIG, st));
+    TRY(fricc_alloc_t(&s.err, R, st));
+    TRY(fricc_alloc_t(&s.ckey, (size_t)R * n, st));
+    TRY(fricc_alloc_t(&s.cidx, (size_t)R * n, st));
+    TRY(fricc_alloc_t(&s.ktmp, (size_t)R * n, st));
+    TRY(fricc_alloc_t(&s.vtmp, (size_t)R * n, st));
+    TRY(fricc_alloc_t(&s.tstate, (size_t)R * (ntile + 1), st));
+    TRY(fricc_alloc_t(&s.ticket, R, st));
+    TRY(fricc_alloc_t(&s.rhist, (size_t)R * rhw, st));
+    TRY(fricc_alloc_t(&s.dzero, 1, st));
+    TRY(fricc_alloc_t(&R0, R, st));
+    TRY(fricc_alloc_t(&s.Rb, (size_t)R * (m + 1), st));
+    TRY(fricc_alloc_t(&s.ffail, R, st));
+    TRY(fricc_alloc_t(&s.S, (size_t)R * m, st));
+    TRY(fricc_alloc_t(&S2, (size_t)R * m, st));
+    TRY(fricc_alloc_t(&s.P, (size_t)R * n, st));
+    {
+      const int64_t nch = nch_n > nch_m ? nch_n : nch_m;
+      TRY(fricc_alloc_t(&s.chain.csum, (size_t)R * (nch + 1), st));
+      TRY(fricc_alloc_t(&s.chain.cbin, (size_t)R * (nch + 1), st));
+      TRY(fricc_alloc_t(&s.chain.cmap, (size_t)R * (nch + 1), st));
+      TRY(fricc_alloc_t(&s.chain.cstart, (size_t)R * (nch + 1), st));
+      s.chain.cap = R * (nch + 1);
+    }
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.hist, 0, (size_t)R * NDIG * sizeof(unsigned), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.err, 0, (size_t)R * sizeof(unsigned), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.tstate, 0, (size_t)R * (ntile + 1) * sizeof(unsigned long long), st),
+                         "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.ticket, 0, (size_t)R * sizeof(unsigned), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(ctl, 0, (size_t)R * sizeof(Ctl), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.dzero, 0, sizeof(double), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(s.S, 0, (size_t)R * m * sizeof(unsigned), st), "memset"));
+    TRY(fricc_cuda_check(cudaMemsetAsync(S2, 0, (size_t)R * m * sizeof(unsigned), st), "memset"));
+    const unsigned gn = grid_for(n, 256), gm = grid_for(m, 256);
+
+    // 1-2. select digit, candidates, sort
+    k_hist12<<<dim3(gn, R), 256, 0, st>>>(x, n, s.hist, rp);
+    k_select_digit<<<R, 1, 0, st>>>(s.hist, m, ctl, rp);
+    k_compact<<<dim3((unsigned)ntile, R), 256, 0, st>>>(x, n, ctl, s.ckey, s.cidx, s.tstate, s.ticket, s.err,
+                                                        s.tstate + ntile,
+                                                        (long long)fricc_tune_get(FRICC_TUNE_TEST_WAIT), rp);
+    fricc_note_launch(3);
+    {
+      radix::Batch bt;
+      bt.kv_stride = n;
+      bt.hist_stride = rhw;
+      bt.n_stride = (int64_t)(sizeof(Ctl) / sizeof(int64_t));
+      static_assert(sizeof(Ctl) % sizeof(int64_t) == 0, "Ctl must be a whole number of int64 words");
+      TRY(radix::sort_pairs(s.ckey, s.cidx, s.ktmp, s.vtmp, n, 64, true, s.rhist, st, &ctl->ncand, R, bt));
+    }
+
+    // 3. one_norm
+    {
+      exact::ChainStride cs;
+      cs.s_init = 0;
+      cs.err = 1;
+      TRY((exact::run_chain<GenAbs, exact::ConsNull, false, false>(GenAbs{x, n}, n, s.dzero, false,
+                                                                   exact::ConsNull{}, s.chain, s.err, st, R, cs)));
+      k_chain_end_b<<<rb, 256, 0, st>>>(s.chain.cstart, nch_n, R0, R);
+      fricc_note_launch();
+    }
+
+    // 4. remaining-norm chain and acceptance test
+    k_fill_u64_b<<<rb, 256, 0, st>>>(s.ffail, (unsigned long long)m, R);
+    fricc_note_launch();
+    {
+      exact::ChainStride cs;
+      cs.s_init = 1;
+      cs.err = 1;
+      ConsAccept ca{m, s.Rb, s.ffail, 1};
+      TRY((exact::run_chain<GenSorted, ConsAccept, false, true>(GenSorted{s.ckey, n}, m, R0, true, ca, s.chain,
+                                                                s.err, st, R, cs)));
+    }
+    k_finish_d<<<R, 1, 0, st>>>(s.ffail, s.Rb, s.ckey, s.cidx, m, ctl, rp);
+    fricc_note_launch();
+    // the second compression: the same state, its own draw
+    TRY(fricc_cuda_check(cudaMemcpyAsync(ctl2, ctl, (size_t)R * sizeof(Ctl), cudaMemcpyDeviceToDevice, st), "ctl"));
+    k_set_rn_b<<<rb, 256, 0, st>>>(ctl, ctl2, rn_dev, R);
+    fricc_note_launch();
+
+    // 5. probabilities, exact partial sums, both samplers
+    const GenP gp{x, ctl, n, 1};
+    k_pvec<<<dim3(gn, R), 256, 0, st>>>(gp, n, s.P, s.err, rp);
+    fricc_note_launch();
+    const GenPv gpv{s.P, x, ctl, n, 1};
+    {
+      exact::ChainStride cs;
+      cs.s_init = 0;
+      cs.err = 1;
+      ConsSample2 cs2{ConsSample{ctl, s.S, 1, m}, ConsSample{ctl2, S2, 1, m}};
+      TRY((exact::run_chain<GenPv, ConsSample2, false, true>(gpv, n, s.dzero, false, cs2, s.chain, s.err, st, R,
+                                                             cs)));
+    }
+
+    // 6. outputs
+    k_out_d<<<dim3(gm, R), 256, 0, st>>>(x, s.cidx, m, ctl, flatA, valsA, rp);
+    k_out_s<<<dim3(gm, R), 256, 0, st>>>(gpv, s.S, flatA, valsA, rp);
+    k_put_meta<<<R, 1, 0, st>>>(ctl, 0, s.err, metaA, rp);
+    const GenPv gpv2{s.P, x, ctl2, n, 1};
+    k_out_d<<<dim3(gm, R), 256, 0, st>>>(x, s.cidx, m, ctl2, flatB, valsB, rp);
+    k_out_s<<<dim3(gm, R), 256, 0, st>>>(gpv2, S2, flatB, valsB, rp);
+    k_put_meta<<<R, 1, 0, st>>>(ctl2, 0, s.err, metaB, rp);
+    fricc_note_launch(6);
+    TRY(fricc_cuda_check(cudaGetLastError(), "compress batch"));
+  }
+done:
+#undef TRY
+  free_scratch(s, st);
+  fricc_free(ctl, st);
+  fricc_free(ctl2, st);
+  fricc_free(S2, st);
+  fricc_free(R0, st);
+  return rc;
+}
+
+// Unpack the flat indices of R compressions (m each, stacked) into slots;
+// an out-of-range index is ORed into the replica's meta[1].
+int fricc_unpack_batch_async(const int64_t* flat, int64_t m, int R, const int64_t dims[4], int* slots,
+                             unsigned long long* meta, cudaStream_t st) {
+  unsigned* err = nullptr;
+  int rc = fricc_alloc_t(&err, R, st);
+  if (rc) return rc;
+  cudaMemsetAsync(err, 0, (size_t)R * sizeof(unsigned), st);
+  Rep rp;
+  rp.m = m;
+  rp.one = 1;
+  k_unpack<<<dim3(grid_for(m, 256), R), 256, 0, st>>>(flat, m, dims[0], dims[1], dims[2], dims[3], slots, err, rp);
+  k_meta_or_b<<<(unsigned)fricc_cdiv(R, 256), 256, 0, st>>>(err, meta, R);
+  fricc_note_launch(2);
+  cudaError_t ce = cudaGetLastError();
+  fricc_free(err, st);
+  return ce == cudaSuccess ? FRICC_OK : fricc_cuda_fail(ce, "unpack batch", __FILE__, __LINE__);
 }
 
 // The error bits of a deferred status word, as a status code (and message).

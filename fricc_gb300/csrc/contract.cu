@@ -67,8 +67,19 @@ const TermSpec* find_term(const char* name) {
   return nullptr;
 }
 
+// Replica batches: per-replica strides (elements) of the m-sized arrays
+// (slots count 4 per entry), of bptr, of W' and of the output; the replica
+// is blockIdx.y (blockIdx.z in the contraction kernels).  Zero outside a
+// batch.
+struct RepC {
+  int64_t m = 0, b = 0, w = 0, o = 0;
+};
+
 __global__ void k_pair_keys(const int* __restrict__ slots, int64_t m, int pa, int pb, int64_t dpb,
-                            unsigned long long* __restrict__ keys, unsigned* __restrict__ idx) {
+                            unsigned long long* __restrict__ keys, unsigned* __restrict__ idx, RepC rp = RepC{}) {
+  slots += 4 * blockIdx.y * rp.m;
+  keys += blockIdx.y * rp.m;
+  idx += blockIdx.y * rp.m;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m; s += (int64_t)gridDim.x * blockDim.x) {
     keys[s] = (unsigned long long)slots[4 * s + pa] * (unsigned long long)dpb + (unsigned long long)slots[4 * s + pb];
     idx[s] = (unsigned)s;
@@ -76,7 +87,10 @@ __global__ void k_pair_keys(const int* __restrict__ slots, int64_t m, int pa, in
 }
 
 // bptr[P] = first position whose key >= P (keys sorted ascending)
-__global__ void k_bptr(const unsigned long long* __restrict__ keys, int64_t m, int64_t nb, int* __restrict__ bptr) {
+__global__ void k_bptr(const unsigned long long* __restrict__ keys, int64_t m, int64_t nb, int* __restrict__ bptr,
+                       RepC rp = RepC{}) {
+  keys += blockIdx.y * rp.m;
+  bptr += blockIdx.y * rp.b;
   for (int64_t P = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; P <= nb; P += (int64_t)gridDim.x * blockDim.x) {
     int64_t lo = 0, hi = m;
     while (lo < hi) {
@@ -91,7 +105,12 @@ __global__ void k_bptr(const unsigned long long* __restrict__ keys, int64_t m, i
 // per-term entry list in bucket order: W' row and coef * value
 __global__ void k_entries(const int* __restrict__ slots, const double* __restrict__ vals,
                           const unsigned* __restrict__ order, int64_t m, int ka, int kb, int64_t dkb, double coef,
-                          int* __restrict__ erow, double* __restrict__ eval) {
+                          int* __restrict__ erow, double* __restrict__ eval, RepC rp = RepC{}) {
+  slots += 4 * blockIdx.y * rp.m;
+  vals += blockIdx.y * rp.m;
+  order += blockIdx.y * rp.m;
+  erow += blockIdx.y * rp.m;
+  eval += blockIdx.y * rp.m;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
     const unsigned s = order[e];
     erow[e] = (int)((int64_t)slots[4 * s + ka] * dkb + slots[4 * s + kb]);
@@ -104,7 +123,15 @@ constexpr int SP_QPT = 2;
 
 __global__ void __launch_bounds__(SP_NT) k_spmm(const int* __restrict__ bptr, const int* __restrict__ erow,
                                                 const double* __restrict__ eval, const double* __restrict__ Wp,
-                                                double* __restrict__ Op, int64_t QS) {
+                                                double* __restrict__ Op, int64_t QS, RepC rp = RepC{}) {
+  {
+    const int64_t r = blockIdx.z;
+    bptr += r * rp.b;
+    erow += r * rp.m;
+    eval += r * rp.m;
+    Wp += r * rp.w;
+    Op += r * rp.o;
+  }
   __shared__ int srow[SP_NT];
   __shared__ double sval[SP_NT];
   const int64_t P = blockIdx.x;
@@ -232,7 +259,16 @@ __device__ __forceinline__ void df_tile(const int* __restrict__ srow, const ulon
 template <int DF_PPT>
 __global__ void __launch_bounds__(DF_NT, 8) k_spmm_df(const int* __restrict__ bptr, const int* __restrict__ erow,
                                                    const float2* __restrict__ eval, const float4* __restrict__ Wp4,
-                                                   double* __restrict__ Op, int64_t QS, int qtile0) {
+                                                   double* __restrict__ Op, int64_t QS, int qtile0,
+                                                   RepC rp = RepC{}) {
+  {
+    const int64_t r = blockIdx.z;
+    bptr += r * rp.b;
+    erow += r * rp.m;
+    eval += r * rp.m;
+    Wp4 += r * rp.w;
+    Op += r * rp.o;
+  }
   __shared__ int srow[DF_NT];
   __shared__ ulonglong2 sv[DF_NT];
   __shared__ f32x2 snv[DF_NT];
@@ -450,7 +486,12 @@ __global__ void __launch_bounds__(DF_NT) k_spmm_f32(const int* __restrict__ bptr
 
 __global__ void k_entries_df(const int* __restrict__ slots, const double* __restrict__ vals,
                              const unsigned* __restrict__ order, int64_t m, int ka, int kb, int64_t dkb, double coef,
-                             int* __restrict__ erow, float2* __restrict__ eval) {
+                             int* __restrict__ erow, float2* __restrict__ eval, RepC rp = RepC{}) {
+  slots += 4 * blockIdx.y * rp.m;
+  vals += blockIdx.y * rp.m;
+  order += blockIdx.y * rp.m;
+  erow += blockIdx.y * rp.m;
+  eval += blockIdx.y * rp.m;
   for (int64_t e = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; e < m; e += (int64_t)gridDim.x * blockDim.x) {
     const unsigned s = order[e];
     erow[e] = (int)((int64_t)slots[4 * s + ka] * dkb + slots[4 * s + kb]);
@@ -856,4 +897,149 @@ double fricc_contract_flops_impl(const char* term, const FriccSparse* T) {
   if (std::strcmp(ts->name, "2323") == 0) q = v * v;               // O^2V^4
   else if (std::strcmp(ts->name, "0101") == 0 || std::strcmp(ts->name, "1323") == 0) q = o * o;  // O^4V^2
   return 2.0 * (double)T->m * q;
+}
+
+// ---------------------------------------------------------------------------
+// Replica batches: the bucketing and the sparse terms of R compressed tensors
+// of one shape in one set of launches, each replica's arithmetic (entry
+// order, accumulation order) that of its own single call.
+int fricc_batch_bucketing(FriccSparseBatch* B, int which, int pa, int pb, cudaStream_t st, BatchBucketing** out) {
+  BatchBucketing* slot = nullptr;
+  for (auto& b : B->buck[which])
+    if (b.pa == pa && b.pb == pb && b.bptr) {
+      if (b.valid) {
+        *out = &b;
+        return FRICC_OK;
+      }
+      slot = &b;
+      break;
+    }
+  if (!slot)
+    for (auto& b : B->buck[which])
+      if (!b.bptr) {
+        slot = &b;
+        break;
+      }
+  if (!slot) return FRICC_ERR_ARG;
+  const bool fresh = slot->bptr == nullptr;
+  const int R = B->R;
+  const int64_t m = B->m;
+  const int64_t nb = B->dims[pa] * B->dims[pb];
+  int bits = 8;
+  while (bits < 64 && (1ll << bits) < nb) bits += 8;
+  unsigned long long *keys = nullptr, *ktmp = nullptr;
+  unsigned *vtmp = nullptr, *hist = nullptr;
+  const int64_t hw = radix::hist_words(m);
+  int rc = fricc_alloc_t(&keys, (size_t)R * m, st);
+  if (!rc) rc = fricc_alloc_t(&ktmp, (size_t)R * m, st);
+  if (!rc) rc = fricc_alloc_t(&vtmp, (size_t)R * m, st);
+  if (!rc) rc = fricc_alloc_t(&hist, (size_t)R * hw, st);
+  if (!rc && fresh) rc = fricc_alloc_t(&slot->order, (size_t)R * m, st);
+  if (!rc && fresh) rc = fricc_alloc_t(&slot->bptr, (size_t)R * (nb + 1), st);
+  if (!rc) {
+    RepC rp;
+    rp.m = m;
+    rp.b = nb + 1;
+    k_pair_keys<<<dim3(grid_for(m, 256), R), 256, 0, st>>>(B->slots[which], m, pa, pb, B->dims[pb], keys,
+                                                          slot->order, rp);
+    radix::Batch bt;
+    bt.kv_stride = m;
+    bt.hist_stride = hw;
+    rc = radix::sort_pairs(keys, slot->order, ktmp, vtmp, m, bits, false, hist, st, nullptr, R, bt);
+    fricc_note_launch(1);
+    if (!rc) {
+      k_bptr<<<dim3(grid_for(nb + 1, 256), R), 256, 0, st>>>(keys, m, nb, slot->bptr, rp);
+      fricc_note_launch();
+      cudaError_t e = cudaGetLastError();
+      if (e != cudaSuccess) rc = fricc_cuda_fail(e, "batch bucketing", __FILE__, __LINE__);
+    }
+  }
+  fricc_free(keys, st);
+  fricc_free(ktmp, st);
+  fricc_free(vtmp, st);
+  fricc_free(hist, st);
+  if (rc) {
+    fricc_free(slot->order, st);
+    fricc_free(slot->bptr, st);
+    slot->order = nullptr;
+    slot->bptr = nullptr;
+    return rc;
+  }
+  slot->pa = pa;
+  slot->pb = pb;
+  slot->nbuckets = nb;
+  slot->valid = true;
+  *out = slot;
+  return FRICC_OK;
+}
+
+// Op_r[P][q] += coef * sum_e W'_r[key_e][q] value_e for every replica r:
+// W'_r = Wp + r w_stride (w_stride 0: one W' for all), Op_r = Op + r o_stride.
+// f2: W' in the q-pair float layout of fricc_spmm_f2 (w_stride in float4s).
+int fricc_batch_spmm_device(FriccSparseBatch* B, int which, int pa, int pb, int ka, int kb, double coef,
+                            const void* Wp, int64_t w_stride, int64_t QS, double* Op, int64_t o_stride, bool f2,
+                            cudaStream_t st) {
+  if (!B || !Wp || !Op || which < 0 || which > 1 || QS <= 0 || pa < 0 || pa > 3 || pb < 0 || pb > 3 || ka < 0 ||
+      ka > 3 || kb < 0 || kb > 3 || pa == pb || ka == kb || w_stride < 0 || o_stride < 0) {
+    fricc_set_error("batch spmm: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  if (!B->compressed) {
+    fricc_set_error("batch spmm: the batch has not been compressed yet");
+    return FRICC_ERR_ARG;
+  }
+  if (f2 && reinterpret_cast<uintptr_t>(Wp) % 16 != 0) {
+    fricc_set_error("batch spmm: W' (q-pair layout) must be 16-byte aligned");
+    return FRICC_ERR_ARG;
+  }
+  const int R = B->R;
+  const int64_t m = B->m;
+  BatchBucketing* bk = nullptr;
+  int rc = fricc_batch_bucketing(B, which, pa, pb, st, &bk);
+  if (rc) return rc;
+  int* erow = nullptr;
+  void* eval = nullptr;
+  rc = fricc_alloc_t(&erow, (size_t)R * m, st);
+  if (!rc) rc = fricc_alloc(&eval, (size_t)R * m * (f2 ? sizeof(float2) : sizeof(double)), st);
+  const int64_t QS2 = (QS + 1) / 2;
+  const int ppt = f2 ? (fricc_tune_get(FRICC_TUNE_SPMM_PPT) > 0 ? fricc_tune_get(FRICC_TUNE_SPMM_PPT) : 2) : 0;
+  const int64_t ntq = f2 ? fricc_cdiv(QS2, DF_NT * ppt) : fricc_cdiv(QS, SP_NT * SP_QPT);
+  if (!rc && (ntq > 65535 || bk->nbuckets > 0x7fffffffLL)) {
+    fricc_set_error("batch spmm: problem too large for one launch");
+    rc = FRICC_ERR_ARG;
+  }
+  if (!rc) {
+    RepC rp;
+    rp.m = m;
+    rp.b = bk->nbuckets + 1;
+    rp.w = w_stride;
+    rp.o = o_stride;
+    const int* slots = B->slots[which];
+    const double* vals = B->vals[which];
+    const bool prof = fricc_prof_on();
+    const dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq, (unsigned)R);
+    if (f2) {
+      k_entries_df<<<dim3(grid_for(m, 256), R), 256, 0, st>>>(slots, vals, bk->order, m, ka, kb, B->dims[kb], coef,
+                                                             erow, static_cast<float2*>(eval), rp);
+      if (prof) fricc_prof_record(st, true, 0.0);
+      const float4* W4 = static_cast<const float4*>(Wp);
+      const float2* ev = static_cast<const float2*>(eval);
+      if (ppt == 1) k_spmm_df<1><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, ev, W4, Op, QS, 0, rp);
+      else if (ppt == 4) k_spmm_df<4><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, ev, W4, Op, QS, 0, rp);
+      else k_spmm_df<2><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, ev, W4, Op, QS, 0, rp);
+    } else {
+      k_entries<<<dim3(grid_for(m, 256), R), 256, 0, st>>>(slots, vals, bk->order, m, ka, kb, B->dims[kb], coef,
+                                                          erow, static_cast<double*>(eval), rp);
+      if (prof) fricc_prof_record(st, true, 0.0);
+      k_spmm<<<grid, SP_NT, 0, st>>>(bk->bptr, erow, static_cast<const double*>(eval),
+                                     static_cast<const double*>(Wp), Op, QS, rp);
+    }
+    if (prof) fricc_prof_record(st, false, 2.0 * (double)R * (double)m * (double)QS);
+    fricc_note_launch(2);
+    cudaError_t e = cudaGetLastError();
+    if (e != cudaSuccess) rc = fricc_cuda_fail(e, "batch spmm", __FILE__, __LINE__);
+  }
+  fricc_free(erow, st);
+  fricc_free(eval, st);
+  return rc;
 }

@@ -20,7 +20,18 @@ __global__ void __launch_bounds__(256) k_t2_energy(const double* __restrict__ t2
                                                    const double* __restrict__ eia, const double* __restrict__ ovov,
                                                    const double* __restrict__ t2old, double* __restrict__ t2out,
                                                    int64_t o, int64_t v, double* __restrict__ part_e,
-                                                   double* __restrict__ part_n) {
+                                                   double* __restrict__ part_n, int64_t np = 0) {
+  // replica batches: replica blockIdx.z's amplitudes follow o v (t1) and
+  // o^2 v^2 (t2) elements after the previous replica's; np partial sums each
+  {
+    const int64_t r = blockIdx.z, n2 = o * o * v * v;
+    t2num += r * n2;
+    t1 += r * o * v;
+    t2old += r * n2;
+    t2out += r * n2;
+    part_e += r * np;
+    part_n += r * np;
+  }
   __shared__ double xt[TB][TB + 1];  // xt[b][a] = (ib|ja)
   __shared__ double red[32];
   const int64_t ij = blockIdx.y;
@@ -62,6 +73,10 @@ __global__ void __launch_bounds__(256) k_t2_energy(const double* __restrict__ t2
 __global__ void __launch_bounds__(256) k_t1(const double* __restrict__ t1num, const double* __restrict__ eia,
                                             const double* __restrict__ fov, const double* __restrict__ t1old,
                                             double* __restrict__ t1out, int64_t nov, double* __restrict__ res) {
+  t1num += blockIdx.x * nov;  // replica blockIdx.x (one block per replica)
+  t1old += blockIdx.x * nov;
+  t1out += blockIdx.x * nov;
+  res += 4 * blockIdx.x;
   __shared__ double red[32];
   double e = 0.0, n = 0.0;
   for (int64_t k = threadIdx.x; k < nov; k += 256) {
@@ -81,6 +96,9 @@ __global__ void __launch_bounds__(256) k_t1(const double* __restrict__ t1num, co
 
 __global__ void __launch_bounds__(256) k_final(const double* __restrict__ part_e, const double* __restrict__ part_n,
                                                int64_t np, double* __restrict__ res) {
+  part_e += blockIdx.x * np;  // replica blockIdx.x (one block per replica)
+  part_n += blockIdx.x * np;
+  res += 4 * blockIdx.x;
   __shared__ double red[32];
   double e = 0.0, n = 0.0;
   for (int64_t k = threadIdx.x; k < np; k += 256) {
@@ -126,5 +144,37 @@ int fricc_energy_update_device(const double* t1num, const double* t2num, const d
   cudaError_t e = cudaGetLastError();
   fricc_free(part, st);
   if (e != cudaSuccess) return fricc_cuda_fail(e, "energy_update", __FILE__, __LINE__);
+  return FRICC_OK;
+}
+
+// R replicas at once: t1num/t1old/t1out [R][o][v], t2num/t2old/t2out
+// [R][o][o][v][v], res [R][4]; eia, fov and ovov shared.  Each replica's
+// arithmetic is that of its own call (the same reduction trees).
+int fricc_energy_update_batch_device(int R, const double* t1num, const double* t2num, const double* eia,
+                                     const double* fov, const double* ovov, const double* t1old, const double* t2old,
+                                     int64_t o, int64_t v, double* t1out, double* t2out, double* res,
+                                     cudaStream_t st) {
+  if (o <= 0 || v <= 0 || R < 1 || R > 65535) {
+    fricc_set_error("energy_update_batch: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t ntb = fricc_cdiv(v, TB);
+  const int64_t gx = ntb * ntb, gy = o * o;
+  if (gy > 65535) {
+    fricc_set_error("energy_update_batch: nocc too large");
+    return FRICC_ERR_ARG;
+  }
+  double* part = nullptr;
+  const int64_t np = gx * gy;
+  int rc = fricc_alloc_t(&part, (size_t)2 * np * R, st);
+  if (rc) return rc;
+  k_t1<<<R, 256, 0, st>>>(t1num, eia, fov, t1old, t1out, o * v, res);
+  const dim3 grid((unsigned)gx, (unsigned)gy, (unsigned)R);
+  k_t2_energy<false><<<grid, 256, 0, st>>>(t2num, t1out, eia, ovov, t2old, t2out, o, v, part, part + np * R, np);
+  k_final<<<R, 256, 0, st>>>(part, part + np * R, np, res);
+  fricc_note_launch(3);
+  cudaError_t e = cudaGetLastError();
+  fricc_free(part, st);
+  if (e != cudaSuccess) return fricc_cuda_fail(e, "energy_update_batch", __FILE__, __LINE__);
   return FRICC_OK;
 }

@@ -29,10 +29,33 @@
 //   FP64 add, continue.  Correctness never depends on the prediction.
 #pragma once
 #include <climits>
+#include <type_traits>
+#include <utility>
 
 #include "common.cuh"
 
 namespace exact {
+
+// Replica batches: a chain can run for R independent sequences at once
+// (blockIdx.y, or blockIdx.x for the one-block kernels, is the replica).  A
+// generator or consumer with a method at(r) gives replica r's copy (its
+// pointers moved to that replica's data); one without is shared by all.
+template <class G, class = void>
+struct has_at : std::false_type {};
+template <class G>
+struct has_at<G, std::void_t<decltype(std::declval<const G&>().at(0))>> : std::true_type {};
+template <class G>
+__device__ __forceinline__ G replica_of(const G& g, int r) {
+  if constexpr (has_at<G>::value) return g.at(r);
+  else return g;
+}
+
+// Per-replica strides of a chain's device arguments (elements); the
+// scratch arrays always hold nch + 1 entries per replica.
+struct ChainStride {
+  int64_t s_init = 0;  // the start values
+  int64_t err = 0;     // the error words
+};
 
 constexpr int64_t TWO52 = 1LL << 52;
 constexpr int64_t TWO53 = 1LL << 53;
@@ -256,7 +279,12 @@ __device__ double block_exact_chunk(const Gen& gen, int64_t base, int n_in, doub
 // K_A: approximate sum of each chunk (fixed reduction tree).  With CHECK_P,
 // any addend above 1 sets FRICC_DEV_P_GT_ONE (make_probability_vector's check).
 template <class Gen, bool CHECK_P>
-__global__ void __launch_bounds__(256) k_chunk_sums(Gen gen, int64_t len, double* csum, unsigned* err) {
+__global__ void __launch_bounds__(256) k_chunk_sums(Gen gen0, int64_t len, double* csum, unsigned* err,
+                                                    ChainStride cs) {
+  const int rep = blockIdx.y;
+  const Gen gen = replica_of(gen0, rep);
+  csum += (int64_t)rep * (fricc_cdiv(len, CH) + 1);
+  err += rep * cs.err;
   __shared__ double red[32];
   const int64_t base = (int64_t)blockIdx.x * CH;
   double acc = 0.0;
@@ -277,8 +305,11 @@ __global__ void __launch_bounds__(256) k_chunk_sums(Gen gen, int64_t len, double
 // K_B (one block of 1024): approximate prefix of the chunk sums and the
 // per-chunk binade prediction: cbin[c] = binade if clean, 0 if not.
 static __global__ void __launch_bounds__(1024) k_classify(const double* csum, int64_t nch, const double* s_init_dev,
-                                                   int sub, int* cbin) {
-  const double s_init = *s_init_dev;
+                                                   int sub, int* cbin, ChainStride cs) {
+  const int rep = blockIdx.x;
+  csum += (int64_t)rep * (nch + 1);
+  cbin += (int64_t)rep * (nch + 1);
+  const double s_init = s_init_dev[rep * cs.s_init];
   __shared__ double part[1024];
   __shared__ double red[32];
   const int64_t per = fricc_cdiv(nch, 1024);
@@ -318,8 +349,12 @@ static __global__ void __launch_bounds__(1024) k_classify(const double* csum, in
 
 // K_C: composite map of each clean chunk under its predicted binade.
 template <class Gen>
-__global__ void __launch_bounds__(256) k_chunk_maps(Gen gen, int64_t len, int sub, const int* cbin, Map* cmap) {
+__global__ void __launch_bounds__(256) k_chunk_maps(Gen gen0, int64_t len, int sub, const int* cbin, Map* cmap) {
   constexpr int NT = 256, ITEMS = CH / NT;
+  const int rep = blockIdx.y;
+  const Gen gen = replica_of(gen0, rep);
+  cbin += (int64_t)rep * (fricc_cdiv(len, CH) + 1);
+  cmap += (int64_t)rep * (fricc_cdiv(len, CH) + 1);
   __shared__ Map smaps[33];
   const int b = cbin[blockIdx.x];
   if (b == 0) return;  // uniform per block
@@ -338,9 +373,17 @@ __global__ void __launch_bounds__(256) k_chunk_maps(Gen gen, int64_t len, int su
 // K_D (one block of 1024): the exact chain over chunks.  cstart[c] receives
 // the exact running value at the start of chunk c, cstart[nch] the total.
 template <class Gen>
-__global__ void __launch_bounds__(1024) k_walk(Gen gen, int64_t len, const double* s_init_dev, int sub,
-                                               const int* cbin, const Map* cmap, double* cstart) {
-  const double s_init = *s_init_dev;
+__global__ void __launch_bounds__(1024) k_walk(Gen gen0, int64_t len, const double* s_init_dev, int sub,
+                                               const int* cbin, const Map* cmap, double* cstart, ChainStride cs) {
+  const int rep = blockIdx.x;
+  const Gen gen = replica_of(gen0, rep);
+  {
+    const int64_t st = (int64_t)rep * (fricc_cdiv(len, CH) + 1);
+    cbin += st;
+    cmap += st;
+    cstart += st;
+  }
+  const double s_init = s_init_dev[rep * cs.s_init];
   constexpr int NT = 1024;
   __shared__ Map smaps[33];
   __shared__ int simin[32];
@@ -388,8 +431,12 @@ __global__ void __launch_bounds__(1024) k_walk(Gen gen, int64_t len, const doubl
 
 // K_E: every element's exact before/after values, from the exact chunk starts.
 template <class Gen, class Cons>
-__global__ void __launch_bounds__(256) k_emit(Gen gen, Cons cons, int64_t len, int sub, const double* cstart) {
+__global__ void __launch_bounds__(256) k_emit(Gen gen0, Cons cons0, int64_t len, int sub, const double* cstart) {
   constexpr int NT = 256;
+  const int rep = blockIdx.y;
+  const Gen gen = replica_of(gen0, rep);
+  const Cons cons = replica_of(cons0, rep);
+  cstart += (int64_t)rep * (fricc_cdiv(len, CH) + 1);
   __shared__ ChunkSmem csm;
   const int64_t base = (int64_t)blockIdx.x * CH;
   const int n_in = (int)(len - base < CH ? len - base : CH);
@@ -409,10 +456,13 @@ struct ChainScratch {
 // every element.
 template <class Gen, class Cons, bool CHECK_P, bool EMIT>
 int run_chain(const Gen& gen, int64_t len, const double* s_init_dev, bool sub, const Cons& cons,
-              ChainScratch& sc, unsigned* dev_err, cudaStream_t st) {
+              ChainScratch& sc, unsigned* dev_err, cudaStream_t st, int R = 1, ChainStride cs = ChainStride{}) {
   const int64_t nch = fricc_cdiv(len, CH);
-  if (nch > INT_MAX / 2) return FRICC_ERR_ARG;
-  if (sc.cap < nch + 1) {
+  if (nch > INT_MAX / 2 || R < 1 || R > 65535) return FRICC_ERR_ARG;
+  if (R > 1) {  // the batch's scratch: nch + 1 entries per replica, sized by the caller
+    if (sc.cap < R * (nch + 1)) return FRICC_ERR_ARG;
+    if (nch == 0) return FRICC_ERR_ARG;
+  } else if (sc.cap < nch + 1) {
     fricc_free(sc.csum, st);
     fricc_free(sc.cbin, st);
     fricc_free(sc.cmap, st);
@@ -428,11 +478,12 @@ int run_chain(const Gen& gen, int64_t len, const double* s_init_dev, bool sub, c
     FRICC_CUDA(cudaMemcpyAsync(sc.cstart, s_init_dev, sizeof(double), cudaMemcpyDeviceToDevice, st));
     return FRICC_OK;
   }
-  k_chunk_sums<Gen, CHECK_P><<<(unsigned)nch, 256, 0, st>>>(gen, len, sc.csum, dev_err);
-  k_classify<<<1, 1024, 0, st>>>(sc.csum, nch, s_init_dev, sub ? 1 : 0, sc.cbin);
-  k_chunk_maps<Gen><<<(unsigned)nch, 256, 0, st>>>(gen, len, sub ? 1 : 0, sc.cbin, sc.cmap);
-  k_walk<Gen><<<1, 1024, 0, st>>>(gen, len, s_init_dev, sub ? 1 : 0, sc.cbin, sc.cmap, sc.cstart);
-  if (EMIT) k_emit<Gen, Cons><<<(unsigned)nch, 256, 0, st>>>(gen, cons, len, sub ? 1 : 0, sc.cstart);
+  const dim3 gch((unsigned)nch, (unsigned)R);
+  k_chunk_sums<Gen, CHECK_P><<<gch, 256, 0, st>>>(gen, len, sc.csum, dev_err, cs);
+  k_classify<<<R, 1024, 0, st>>>(sc.csum, nch, s_init_dev, sub ? 1 : 0, sc.cbin, cs);
+  k_chunk_maps<Gen><<<gch, 256, 0, st>>>(gen, len, sub ? 1 : 0, sc.cbin, sc.cmap);
+  k_walk<Gen><<<R, 1024, 0, st>>>(gen, len, s_init_dev, sub ? 1 : 0, sc.cbin, sc.cmap, sc.cstart, cs);
+  if (EMIT) k_emit<Gen, Cons><<<gch, 256, 0, st>>>(gen, cons, len, sub ? 1 : 0, sc.cstart);
   fricc_note_launch(EMIT ? 5 : 4);
   FRICC_LAUNCH_CHECK();
   return FRICC_OK;

@@ -10,7 +10,8 @@
 // (one FMA recovers the rounding error of hi*hi) and accumulated with an
 // error-free two-sum, renormalised every K tile, two adjacent outputs per
 // packed f32x2 instruction.  Relative error of each
-// output ~1e-14.  A long K is split over blockIdx.z; the partial tiles are
+// output ~1e-14.  A long K is split over blockIdx.x (beside the N tiles;
+// blockIdx.z is the batch); the partial tiles are
 // summed afterwards in a fixed order, so results are deterministic.
 #include "common.cuh"
 
@@ -61,10 +62,23 @@ struct GemmArgs {
   double* part;   // [batch][splits][M][N] partials (splits > 1)
   int64_t M, N, K;
   int64_t sAm, sAk, sAb, sBk, sBn, sBb, sCm, sCn, sCb;
+  // a second batch level (replicas): batch index bz = b2 * nb1 + b
+  int64_t nb1, sAb2, sBb2, sCb2;
   double alpha, beta;
   int splits;
+  int64_t ntn;     // N tiles: blockIdx.x = split * ntn + N tile
   int64_t kchunk;  // K per split (multiple of BK)
 };
+
+__device__ __forceinline__ int64_t boffA(const GemmArgs& g, int64_t bz) {
+  return (bz % g.nb1) * g.sAb + (bz / g.nb1) * g.sAb2;
+}
+__device__ __forceinline__ int64_t boffB(const GemmArgs& g, int64_t bz) {
+  return (bz % g.nb1) * g.sBb + (bz / g.nb1) * g.sBb2;
+}
+__device__ __forceinline__ int64_t boffC(const GemmArgs& g, int64_t bz) {
+  return (bz % g.nb1) * g.sCb + (bz / g.nb1) * g.sCb2;
+}
 
 // 256 threads as 16 x 16.  Thread (tx, ty) owns rows ty + 16 i (i < TM) and
 // the column pairs 2 (tx + 16 j) + {0, 1} (j < TN / 2) of a (16 TM) x (16 TN)
@@ -81,13 +95,13 @@ __global__ void __launch_bounds__(NT, 2) k_gemm_df(GemmArgs g) {
   __shared__ ulonglong2 Bs[BK][NP + 1];
   __shared__ f32x2 Bn[BK][NP + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
-  const int64_t bz = blockIdx.z / g.splits;
-  const int sp = blockIdx.z % g.splits;
+  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)(blockIdx.x % g.ntn) * BN;
+  const int64_t bz = blockIdx.z;
+  const int sp = (int)(blockIdx.x / g.ntn);
   const int64_t k_begin = (int64_t)sp * g.kchunk;
   const int64_t k_end = k_begin + g.kchunk < g.K ? k_begin + g.kchunk : g.K;
-  const double* A = g.A + bz * g.sAb;
-  const double* B = g.B + bz * g.sBb;
+  const double* A = g.A + boffA(g, bz);
+  const double* B = g.B + boffB(g, bz);
 
   f32x2 ah[TM][JP], al[TM][JP];
 #pragma unroll
@@ -197,7 +211,7 @@ __global__ void __launch_bounds__(NT, 2) k_gemm_df(GemmArgs g) {
       for (int c = 0; c < 2; ++c) {
         if (m < g.M && n + c < g.N) {
           if (g.splits == 1) {
-            double* cp = g.C + bz * g.sCb + m * g.sCm + (n + c) * g.sCn;
+            double* cp = g.C + boffC(g, bz) + m * g.sCm + (n + c) * g.sCn;
             // FP64 work per output kept to one operation in the common cases
             if (g.beta == 0.0) *cp = g.alpha == 1.0 ? acc[c] : (g.alpha == -1.0 ? -acc[c] : g.alpha * acc[c]);
             else if (g.beta == 1.0 && g.alpha == 1.0) *cp = *cp + acc[c];
@@ -219,7 +233,7 @@ __global__ void k_gemm_reduce(GemmArgs g, int64_t batch) {
     const int64_t b = t / MN, r = t % MN, m = r / g.N, n = r % g.N;
     double acc = 0.0;
     for (int s = 0; s < g.splits; ++s) acc += g.part[(b * g.splits + s) * MN + r];
-    double* c = g.C + b * g.sCb + m * g.sCm + n * g.sCn;
+    double* c = g.C + boffC(g, b) + m * g.sCm + n * g.sCn;
     *c = g.beta == 0.0 ? g.alpha * acc : fma(g.alpha, acc, g.beta * *c);
   }
 }
@@ -228,7 +242,7 @@ __global__ void k_gemm_reduce(GemmArgs g, int64_t batch) {
 
 int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
                          const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
-                         cudaStream_t st) {
+                         cudaStream_t st, int64_t batch2, const int64_t* s2) {
   if (!A || !B || !C || batch <= 0 || M <= 0 || N <= 0 || K < 0) {
     fricc_set_error("gemm_df: bad arguments");
     return FRICC_ERR_ARG;
@@ -245,6 +259,17 @@ int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t ba
   g.sCm = sC[0]; g.sCn = sC[1]; g.sCb = sC[2];
   g.alpha = alpha;
   g.beta = beta;
+  // a second batch level: batch2 groups of `batch` products, group strides
+  // s2 = {A, B, C}; from here on `batch` counts every product
+  if (batch2 < 1 || batch2 > 65535) {
+    fricc_set_error("gemm: bad second batch count");
+    return FRICC_ERR_ARG;
+  }
+  g.nb1 = batch;
+  g.sAb2 = s2 ? s2[0] : 0;
+  g.sBb2 = s2 ? s2[1] : 0;
+  g.sCb2 = s2 ? s2[2] : 0;
+  batch *= batch2;
   // tile shape: the one of 64x64, 128x32, 32x128, 32x160 that pads C least
   // (a side as short as nocc would waste half of a 64-wide tile)
   int tm = 4, tn = 4;
@@ -263,7 +288,10 @@ int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t ba
     }
   }
   const int64_t BM = 16 * tm, BN = 16 * tn;
-  const int64_t tiles = fricc_cdiv(M, BM) * fricc_cdiv(N, BN) * batch;
+  // split K as for a single product, so that each product's sums are the
+  // same whatever batch it runs in (a long K comes with few output tiles;
+  // the batched products of an iteration have short K and never split)
+  const int64_t tiles = fricc_cdiv(M, BM) * fricc_cdiv(N, BN);
   // split K until the grid covers the GPU about four (or the tuned number
   // of) times over
   const int cover = fricc_tune_get(FRICC_TUNE_GEMM_COVER) > 0 ? fricc_tune_get(FRICC_TUNE_GEMM_COVER) : 4;
@@ -271,7 +299,8 @@ int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t ba
   while (splits < 1024 && tiles * splits < 152 * cover && K / (2 * splits) >= 8 * BK) splits *= 2;
   g.splits = splits;
   g.kchunk = fricc_cdiv(fricc_cdiv(K, splits), BK) * BK;
-  if (fricc_cdiv(M, BM) > 65535 || batch * splits > 65535) {
+  g.ntn = fricc_cdiv(N, BN);
+  if (fricc_cdiv(M, BM) > 65535 || batch > 65535 || g.ntn * splits > 0x7fffffff) {
     fricc_set_error("gemm_df: grid too large (M=%lld, batch=%lld)", (long long)M, (long long)batch);
     return FRICC_ERR_ARG;
   }
@@ -281,7 +310,7 @@ int fricc_gemm_df_device(const double* A, const double* B, double* C, int64_t ba
     if (rc) return rc;
     g.part = part;
   }
-  dim3 grid((unsigned)fricc_cdiv(N, BN), (unsigned)fricc_cdiv(M, BM), (unsigned)(batch * splits));
+  dim3 grid((unsigned)(g.ntn * splits), (unsigned)fricc_cdiv(M, BM), (unsigned)batch);
   if (tm == 8) k_gemm_df<8, 2><<<grid, NT, 0, st>>>(g);
   else if (tn == 8) k_gemm_df<2, 8><<<grid, NT, 0, st>>>(g);
   else if (tn == 10) k_gemm_df<2, 10><<<grid, NT, 0, st>>>(g);

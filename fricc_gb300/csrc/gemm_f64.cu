@@ -10,7 +10,8 @@
 // memory, bounds any tile that keeps a few accumulators per thread, and a
 // tile only has to keep enough warps on every SM.  Each output is summed in
 // k order (deterministic); a long K with few output tiles is split over
-// blockIdx.z and the partial tiles summed afterwards in slice order.
+// blockIdx.x (beside the N tiles; blockIdx.z is the batch) and the partial
+// tiles summed afterwards in slice order.
 #include "common.cuh"
 
 namespace {
@@ -24,14 +25,27 @@ struct GemmArgs {
   double* part;   // [batch][splits][M][N] partials (splits > 1)
   int64_t M, N, K;
   int64_t sAm, sAk, sAb, sBk, sBn, sBb, sCm, sCn, sCb;
+  // a second batch level (replicas): batch index bz = b2 * nb1 + b
+  int64_t nb1, sAb2, sBb2, sCb2;
   double alpha, beta;
   int splits;
+  int64_t ntn;     // N tiles: blockIdx.x = split * ntn + N tile
   int64_t kchunk;  // K per split (multiple of BK)
 };
 
+__device__ __forceinline__ int64_t boffA(const GemmArgs& g, int64_t bz) {
+  return (bz % g.nb1) * g.sAb + (bz / g.nb1) * g.sAb2;
+}
+__device__ __forceinline__ int64_t boffB(const GemmArgs& g, int64_t bz) {
+  return (bz % g.nb1) * g.sBb + (bz / g.nb1) * g.sBb2;
+}
+__device__ __forceinline__ int64_t boffC(const GemmArgs& g, int64_t bz) {
+  return (bz % g.nb1) * g.sCb + (bz / g.nb1) * g.sCb2;
+}
+
 __device__ __forceinline__ void store_out(const GemmArgs& g, int64_t bz, int sp, int64_t m, int64_t n, double acc) {
   if (g.splits == 1) {
-    double* cp = g.C + bz * g.sCb + m * g.sCm + n * g.sCn;
+    double* cp = g.C + boffC(g, bz) + m * g.sCm + n * g.sCn;
     if (g.beta == 0.0) *cp = g.alpha == 1.0 ? acc : (g.alpha == -1.0 ? -acc : g.alpha * acc);
     else if (g.beta == 1.0 && g.alpha == 1.0) *cp = *cp + acc;
     else if (g.beta == 1.0 && g.alpha == -1.0) *cp = *cp - acc;
@@ -51,13 +65,13 @@ __global__ void __launch_bounds__(NT, 2) k_gemm_f64(GemmArgs g) {
   __shared__ double As[BK][BM + 1];
   __shared__ double Bs[BK][BN + 1];
   const int tx = threadIdx.x & 15, ty = threadIdx.x >> 4;
-  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)blockIdx.x * BN;
-  const int64_t bz = blockIdx.z / g.splits;
-  const int sp = blockIdx.z % g.splits;
+  const int64_t m0 = (int64_t)blockIdx.y * BM, n0 = (int64_t)(blockIdx.x % g.ntn) * BN;
+  const int64_t bz = blockIdx.z;
+  const int sp = (int)(blockIdx.x / g.ntn);
   const int64_t k_begin = (int64_t)sp * g.kchunk;
   const int64_t k_end = k_begin + g.kchunk < g.K ? k_begin + g.kchunk : g.K;
-  const double* A = g.A + bz * g.sAb;
-  const double* B = g.B + bz * g.sBb;
+  const double* A = g.A + boffA(g, bz);
+  const double* B = g.B + boffB(g, bz);
 
   double acc[TM][TN];
 #pragma unroll
@@ -148,7 +162,7 @@ __global__ void k_gemm_f64_reduce(GemmArgs g, int64_t batch) {
     const int64_t b = t / MN, r = t % MN, m = r / g.N, n = r % g.N;
     double acc = 0.0;
     for (int s = 0; s < g.splits; ++s) acc += g.part[(b * g.splits + s) * MN + r];
-    double* c = g.C + b * g.sCb + m * g.sCm + n * g.sCn;
+    double* c = g.C + boffC(g, b) + m * g.sCm + n * g.sCn;
     *c = g.beta == 0.0 ? g.alpha * acc : fma(g.alpha, acc, g.beta * *c);
   }
 }
@@ -163,8 +177,8 @@ __global__ void __launch_bounds__(256) k_gemv_warp(GemmArgs g, int64_t batch) {
   const int64_t w = ((int64_t)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
   if (w >= batch * g.M * g.N) return;
   const int64_t n = w % g.N, m = (w / g.N) % g.M, b = w / (g.N * g.M);
-  const double* A = g.A + b * g.sAb + m * g.sAm;
-  const double* B = g.B + b * g.sBb + n * g.sBn;
+  const double* A = g.A + boffA(g, b) + m * g.sAm;
+  const double* B = g.B + boffB(g, b) + n * g.sBn;
   double acc = 0.0;
   for (int64_t k = lane; k < g.K; k += 32) acc = fma(__ldg(A + k * g.sAk), __ldg(B + k * g.sBk), acc);
 #pragma unroll
@@ -185,8 +199,8 @@ __global__ void __launch_bounds__(256) k_gemv_cols(GemmArgs g) {
   const int64_t bm = blockIdx.z, m = bm % g.M, b = bm / g.M;
   const int64_t k0 = (int64_t)sp * g.kchunk;
   const int64_t k1 = k0 + g.kchunk < g.K ? k0 + g.kchunk : g.K;
-  const double* A = g.A + b * g.sAb + m * g.sAm;
-  const double* B = g.B + b * g.sBb + n * g.sBn;
+  const double* A = g.A + boffA(g, b) + m * g.sAm;
+  const double* B = g.B + boffB(g, b) + n * g.sBn;
   double acc = 0.0;
   for (int64_t k = k0; k < k1; ++k) acc = fma(__ldg(A + k * g.sAk), __ldg(B + k * g.sBk), acc);
   store_out(g, b, sp, m, n, acc);
@@ -196,7 +210,7 @@ __global__ void __launch_bounds__(256) k_gemv_cols(GemmArgs g) {
 
 int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t batch, int64_t M, int64_t N, int64_t K,
                           const int64_t sA[3], const int64_t sB[3], const int64_t sC[3], double alpha, double beta,
-                          cudaStream_t st) {
+                          cudaStream_t st, int64_t batch2, const int64_t* s2) {
   if (((!A || !B) && K > 0) || !C || batch <= 0 || M <= 0 || N <= 0 || K < 0 || !sA || !sB || !sC) {
     fricc_set_error("gemm_f64: bad arguments");
     return FRICC_ERR_ARG;
@@ -213,6 +227,17 @@ int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t b
   g.sCm = sC[0]; g.sCn = sC[1]; g.sCb = sC[2];
   g.alpha = alpha;
   g.beta = beta;
+  // a second batch level: batch2 groups of `batch` products, group strides
+  // s2 = {A, B, C}; from here on `batch` counts every product
+  if (batch2 < 1 || batch2 > 65535) {
+    fricc_set_error("gemm: bad second batch count");
+    return FRICC_ERR_ARG;
+  }
+  g.nb1 = batch;
+  g.sAb2 = s2 ? s2[0] : 0;
+  g.sBb2 = s2 ? s2[1] : 0;
+  g.sCb2 = s2 ? s2[2] : 0;
+  batch *= batch2;
   const bool prof = fricc_prof_on();
   const double flops = 2.0 * (double)batch * (double)M * (double)N * (double)K;
   if (K > 0 && ((N <= 4 && (g.sAk == 1 || M <= 4)) || (M <= 4 && g.sBn != 1 && N <= 64))) {
@@ -233,7 +258,7 @@ int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t b
   if (K > 0 && M <= 4) {
     // a few rows: one thread per output column, K split until the grid
     // covers the GPU about four times over (slices of at least 64)
-    const int64_t cols = fricc_cdiv(N, 256) * batch * M;
+    const int64_t cols = fricc_cdiv(N, 256) * M;  // per product, as the tiled path
     if (batch * M > 65535) {
       fricc_set_error("gemm_f64: batch x rows too large for the column kernel");
       return FRICC_ERR_ARG;
@@ -280,7 +305,10 @@ int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t b
     }
   }
   const int64_t BM = 16 * tm, BN = 16 * tn;
-  const int64_t tiles = fricc_cdiv(M, BM) * fricc_cdiv(N, BN) * batch;
+  // split K as for a single product, so that each product's sums are the
+  // same whatever batch it runs in (a long K comes with few output tiles;
+  // the batched products of an iteration have short K and never split)
+  const int64_t tiles = fricc_cdiv(M, BM) * fricc_cdiv(N, BN);
   // split K until the grid covers the GPU about four (or the tuned number
   // of) times over
   const int cover = fricc_tune_get(FRICC_TUNE_GEMM_COVER) > 0 ? fricc_tune_get(FRICC_TUNE_GEMM_COVER) : 4;
@@ -288,7 +316,8 @@ int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t b
   while (splits < 1024 && tiles * splits < 152 * cover && K / (2 * splits) >= 8 * BK) splits *= 2;
   g.splits = splits;
   g.kchunk = fricc_cdiv(fricc_cdiv(K, splits), BK) * BK;
-  if (fricc_cdiv(M, BM) > 65535 || batch * splits > 65535 || fricc_cdiv(N, BN) > 0x7fffffff) {
+  g.ntn = fricc_cdiv(N, BN);
+  if (fricc_cdiv(M, BM) > 65535 || batch > 65535 || g.ntn * splits > 0x7fffffff) {
     fricc_set_error("gemm_f64: grid too large (M=%lld, batch=%lld)", (long long)M, (long long)batch);
     return FRICC_ERR_ARG;
   }
@@ -299,7 +328,7 @@ int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t b
     g.part = part;
   }
   if (prof) fricc_prof_record(st, true, 0.0, 2);
-  dim3 grid((unsigned)fricc_cdiv(N, BN), (unsigned)fricc_cdiv(M, BM), (unsigned)(batch * splits));
+  dim3 grid((unsigned)(g.ntn * splits), (unsigned)fricc_cdiv(M, BM), (unsigned)batch);
   if (tm == 8) k_gemm_f64<8, 2><<<grid, NT, 0, st>>>(g);
   else if (tn == 8) k_gemm_f64<2, 8><<<grid, NT, 0, st>>>(g);
   else if (tn == 10) k_gemm_f64<2, 10><<<grid, NT, 0, st>>>(g);

@@ -34,3 +34,31 @@ struct FriccSparse {
 
 // Index of the cached bucketing for (pa, pb), building it on first use.
 int fricc_sparse_bucketing(FriccSparse* T, int pa, int pb, cudaStream_t st, Bucketing** out);
+
+// R compressed tensors of one shape (a replica batch), stacked: replica r's
+// arrays start r*m entries (flat, vals, slots: r*4*m ints) after the base.
+// which = 0: the compression the T2 terms use, 1: the one the W
+// intermediates use (the two compressions of an iteration).
+struct BatchBucketing {
+  int pa = -1, pb = -1;
+  int64_t nbuckets = 0;
+  int* bptr = nullptr;        // [R][nbuckets + 1]
+  unsigned* order = nullptr;  // [R][m]
+  bool valid = false;
+};
+
+struct FriccSparseBatch {
+  int R = 0;
+  int64_t dims[4] = {0, 0, 0, 0};
+  int64_t m = 0;
+  int64_t* flat[2] = {nullptr, nullptr};              // [R][m]
+  double* vals[2] = {nullptr, nullptr};               // [R][m]
+  int* slots[2] = {nullptr, nullptr};                 // [R][m][4]
+  unsigned long long* meta[2] = {nullptr, nullptr};   // [R][2]: |D|, error bits
+  BatchBucketing buck[2][6];
+  bool compressed = false;
+  cudaStream_t owner_stream = nullptr;
+  int device = 0;
+};
+
+int fricc_batch_bucketing(FriccSparseBatch* B, int which, int pa, int pb, cudaStream_t st, BatchBucketing** out);

@@ -33,9 +33,15 @@ __device__ __forceinline__ void load_tile(double (*tile)[TD + 1], const double* 
 
 __global__ void __launch_bounds__(TD* TR) k_symadd(double* __restrict__ out, const double* __restrict__ X, int64_t o,
                                                     int64_t v, int64_t s0, int64_t s1, int64_t s2, int64_t s3,
-                                                    double coef, int first_along_b, int second_along_b) {
+                                                    double coef, int first_along_b, int second_along_b,
+                                                    int64_t xr = 0) {
   __shared__ double t1[TD][TD + 1], t2[TD][TD + 1];
-  const int64_t ij = blockIdx.z;
+  // replica batches: blockIdx.z = r o^2 + ij; replica r's X starts xr
+  // elements after the previous one's, its output o^2 v^2 after
+  const int64_t rep = blockIdx.z / (o * o);
+  const int64_t ij = blockIdx.z - rep * o * o;
+  X += rep * xr;
+  out += rep * o * o * v * v;
   const int64_t i = ij / o, j = ij - i * o;
   const int64_t a0 = (int64_t)blockIdx.y * TD, b0 = (int64_t)blockIdx.x * TD;
   // X[i,j,a,b] over (a,b): strides (s2, s3); X[j,i,b,a] over (a,b): strides (s3, s2)
@@ -72,4 +78,27 @@ extern "C" int fricc_symadd(double* out, const double* X, int64_t nocc, int64_t 
   fricc_note_launch();
   const cudaError_t e = cudaGetLastError();
   return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "symadd", __FILE__, __LINE__);
+}
+
+// R replicas: out [R][o][o][v][v] (C order), X replica r at X + r xr with
+// the per-replica strides of fricc_symadd.
+extern "C" int fricc_symadd_b(double* out, const double* X, int64_t R, int64_t nocc, int64_t nvir,
+                              const int64_t strides[5], double coef, void* stream) {
+  if (!out || !X || !strides || nocc <= 0 || nvir <= 0 || R < 1) {
+    fricc_set_error("symadd_b: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  if (R * nocc * nocc > 65535) {
+    fricc_set_error("symadd_b: replicas x nocc^2 above the grid limit");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t s0 = strides[1], s1 = strides[2], s2 = strides[3], s3 = strides[4];
+  const int first_along_b = std::llabs(s3) <= std::llabs(s2) ? 1 : 0;
+  const int second_along_b = std::llabs(s2) <= std::llabs(s3) ? 1 : 0;
+  const dim3 grid((unsigned)fricc_cdiv(nvir, TD), (unsigned)fricc_cdiv(nvir, TD), (unsigned)(R * nocc * nocc));
+  k_symadd<<<grid, dim3(TD, TR), 0, (cudaStream_t)stream>>>(out, X, nocc, nvir, s0, s1, s2, s3, coef, first_along_b,
+                                                           second_along_b, strides[0]);
+  fricc_note_launch();
+  const cudaError_t e = cudaGetLastError();
+  return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "symadd_b", __FILE__, __LINE__);
 }

@@ -239,20 +239,20 @@ def sym_add(out: torch.Tensor, X: torch.Tensor, coef: float = 1.0) -> torch.Tens
     return out
 
 
-def _view4(t: torch.Tensor, shape):
-    """Element strides of ``t`` broadcast to ``shape``, padded to 4 dims."""
+def _view5(t: torch.Tensor, shape):
+    """Element strides of ``t`` broadcast to ``shape``, padded to 5 dims."""
     b = t.expand(*shape) if tuple(t.shape) != tuple(shape) else t
     st = list(b.stride())
-    return [0] * (4 - len(st)) + st
+    return [0] * (5 - len(st)) + st
 
 
 def combine(outs, xs=(), coefs=None, prod=(), accumulate=False):
-    """One pass of the library's strided elementwise kernel (fricc_combine):
+    """One pass of the library's strided elementwise kernel (fricc_combine5):
     out_k = sum_t coefs[k][t] xs[t] (+ coefs[k][-1] * prod[0] * prod[1] ...
     when ``prod`` is given), or out_k += that with ``accumulate``.  Every
     tensor is an FP64 device view; inputs broadcast to the outputs' shape
-    (at most 4 dims); the last dim should be the first output's contiguous
-    one.  Outputs must not overlap the inputs."""
+    (at most 5 dims); the kernel walks the first output's memory order.
+    Outputs must not overlap the inputs."""
     import ctypes
 
     from . import _lib as L
@@ -260,8 +260,8 @@ def combine(outs, xs=(), coefs=None, prod=(), accumulate=False):
     xs = list(xs)
     prod = list(prod)
     shape = tuple(outs[0].shape)
-    if len(shape) > 4 or any(tuple(o.shape) != shape for o in outs):
-        raise ValueError("combine: outputs of one shape, at most 4 dims")
+    if len(shape) > 5 or any(tuple(o.shape) != shape for o in outs):
+        raise ValueError("combine: outputs of one shape, at most 5 dims")
     for t in outs + xs + prod:
         if t.dtype != torch.float64 or t.device.type != "cuda":
             raise ValueError("combine: FP64 CUDA tensors only")
@@ -270,7 +270,7 @@ def combine(outs, xs=(), coefs=None, prod=(), accumulate=False):
         coefs = [[1.0] * nc for _ in outs]
     if len(coefs) != len(outs) or any(len(c) != nc for c in coefs):
         raise ValueError("combine: one coefficient per input (and one for the product) per output")
-    dims = [1] * (4 - len(shape)) + list(shape)
+    dims = [1] * (5 - len(shape)) + list(shape)
     vp = ctypes.c_void_p
 
     def ptrs(ts):
@@ -278,20 +278,20 @@ def combine(outs, xs=(), coefs=None, prod=(), accumulate=False):
 
     # walk the index space in the first output's memory order (its
     # smallest stride innermost), so its reads and writes coalesce
-    s0 = _view4(outs[0], shape)
-    perm = sorted(range(4), key=lambda d: (dims[d] != 1, -s0[d]))
+    s0 = _view5(outs[0], shape)
+    perm = sorted(range(5), key=lambda d: (dims[d] != 1, -s0[d]))
 
     def strides(ts):
         flat = []
         for t in ts:
-            st = _view4(t, shape)
+            st = _view5(t, shape)
             flat.extend(st[d] for d in perm)
         return L.i64arr(flat if flat else [0])
 
     cf = (ctypes.c_double * (len(outs) * nc))(*[float(c) for row in coefs for c in row])
-    L.check(L.load().fricc_combine(L.i64arr([dims[d] for d in perm]), len(xs), ptrs(xs), strides(xs), len(prod),
-                                   ptrs(prod), strides(prod), len(outs), ptrs(outs), strides(outs), cf,
-                                   int(bool(accumulate)), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    L.check(L.load().fricc_combine5(L.i64arr([dims[d] for d in perm]), len(xs), ptrs(xs), strides(xs), len(prod),
+                                    ptrs(prod), strides(prod), len(outs), ptrs(outs), strides(outs), cf,
+                                    int(bool(accumulate)), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
     return outs[0]
 
 
@@ -319,20 +319,41 @@ def _strides3(t: torch.Tensor):
     return (t.stride(1), t.stride(2), t.stride(0)), t.shape[0]
 
 
+def _bstrides(t: torch.Tensor):
+    """(row, col, batch, batch2) element strides and (batch, batch2) extents of
+    a 2-D, 3-D ([batch, M, K]) or 4-D ([batch2, batch, M, K]) operand."""
+    if t.dim() == 2:
+        return (t.stride(0), t.stride(1), 0, 0), 1, 1
+    if t.dim() == 3:
+        return (t.stride(1), t.stride(2), t.stride(0), 0), t.shape[0], 1
+    if t.dim() == 4:
+        return (t.stride(2), t.stride(3), t.stride(1), t.stride(0)), t.shape[1], t.shape[0]
+    raise ValueError("gemm: operands are 2-D, 3-D or 4-D")
+
+
 def _gemm_call(fn, A, B, C, alpha, beta):
     import ctypes
 
     from . import _lib as L
-    sA, bA = _strides3(A)
-    sB, bB = _strides3(B)
-    sC, batch = _strides3(C)
+    sA, bA, b2A = _bstrides(A)
+    sB, bB, b2B = _bstrides(B)
+    sC, batch, batch2 = _bstrides(C)
     M, N = C.shape[-2], C.shape[-1]
     K = A.shape[-1]
-    assert A.shape[-2] == M and B.shape[-2] == K and B.shape[-1] == N and bA in (1, batch) and bB in (1, batch)
-    L.check(getattr(L.load(), fn)(ctypes.c_void_p(A.data_ptr()), ctypes.c_void_p(B.data_ptr()),
-                                  ctypes.c_void_p(C.data_ptr()), batch, M, N, K, L.i64arr(sA), L.i64arr(sB),
-                                  L.i64arr(sC), float(alpha), float(beta),
-                                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+    assert A.shape[-2] == M and B.shape[-2] == K and B.shape[-1] == N
+    assert bA in (1, batch) and bB in (1, batch) and b2A in (1, batch2) and b2B in (1, batch2)
+    # a size-1 batch level of an operand is shared: stride 0
+    sA = (sA[0], sA[1], sA[2] if bA == batch and batch > 1 else 0, sA[3] if b2A == batch2 and batch2 > 1 else 0)
+    sB = (sB[0], sB[1], sB[2] if bB == batch and batch > 1 else 0, sB[3] if b2B == batch2 and batch2 > 1 else 0)
+    lib = L.load()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    pA, pB, pC = (ctypes.c_void_p(t.data_ptr()) for t in (A, B, C))
+    if batch2 == 1:
+        L.check(getattr(lib, fn)(pA, pB, pC, batch, M, N, K, L.i64arr(sA[:3]), L.i64arr(sB[:3]), L.i64arr(sC[:3]),
+                                 float(alpha), float(beta), st))
+    else:
+        L.check(getattr(lib, fn + "_b2")(pA, pB, pC, batch, batch2, M, N, K, L.i64arr(sA), L.i64arr(sB),
+                                         L.i64arr(sC), float(alpha), float(beta), st))
     return C
 
 

@@ -2,7 +2,9 @@
 
   --mode replicas : R independent FRI replicas (distinct seeds) of the
                     o20v100 system (naux=600, m = 5% of o^2 v^2), all resident,
-                    iterated together on a pool of streams; prints iterations/s
+                    iterated together on a pool of streams (--fused: as one
+                    stacked iteration, each kernel launched once for all
+                    replicas); prints iterations/s
                     of the whole batch, the replica mean and variance of E_corr and
                     each replica's trace error bar (fri-cc's mcmc_std).
   --mode serve    : a Poisson stream of solve requests (nocc ~ U{5..30},
@@ -37,8 +39,12 @@ def run_replicas(args):
         E = DeviceERIs.from_system(system)
     settings = {"m_keep": w["m"]}
     seeds = [1000 + r for r in range(args.replicas)]
-    batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision,
-                         graph=args.graph and not args.batch_graph)
+    if args.fused:
+        from .replicas import FusedReplicaBatch
+        batch = FusedReplicaBatch(E, settings, seeds, precision=args.precision)
+    else:
+        batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision,
+                             graph=args.graph and not args.batch_graph)
     step = batch.step
     for i in range(args.warmup):
         step()
@@ -54,7 +60,8 @@ def run_replicas(args):
     burn = min(args.warmup, len(batch.history[0]) - 2)
     tmeans, terrs, taus = batch.trace_stats(burn=max(burn, 0))
     return {"mode": "replicas", "workload": "o20v100: nocc=20 nvir=100 naux=600 m=200000 per replica",
-            "replicas": args.replicas, "streams": args.streams, "precision": args.precision,
+            "replicas": args.replicas, "streams": 1 if args.fused else args.streams, "precision": args.precision,
+            "form": "fused: one launch per kernel for all replicas" if args.fused else "one solver per replica",
             "graph": "one graph per batch step" if args.batch_graph else args.graph,
             "iterations_per_s": args.replicas * args.steps / dt, "batch_steps_per_s": args.steps / dt,
             "e_corr_mean": mean, "e_corr_var": var, "iterations_each": args.warmup + args.steps,
@@ -121,6 +128,8 @@ def main():
     p.add_argument("--graph", action="store_true", help="replay each solver's iteration from a CUDA graph")
     p.add_argument("--batch-graph", action="store_true",
                    help="replicas: capture every replica's iteration into one CUDA graph per batch step")
+    p.add_argument("--fused", action="store_true",
+                   help="replicas: one launch per kernel for the whole batch (fp64 or df64)")
     args = p.parse_args()
     line = run_replicas(args) if args.mode == "replicas" else run_serve(args)
     print(json.dumps(line))

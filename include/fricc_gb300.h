@@ -55,6 +55,7 @@ extern "C" {
 #define FRICC_SAMPLING_PIVOTAL 1
 
 typedef struct FriccSparse fricc_sparse; /* opaque device-resident SparseTensor4d */
+typedef struct FriccSparseBatch fricc_spbatch; /* opaque: R compressed tensors of one shape, two per replica */
 
 /* Library version (major*10000 + minor*100 + patch). */
 int fricc_version(void);
@@ -267,6 +268,62 @@ int fricc_combine(const int64_t dims[4], int n_in, const double* const* x, const
  * outputs), sec[4] "Total". */
 int fricc_phase_timing_set(int on);
 int fricc_phase_timing_read(double sec[5]);
+
+/* ---- Replica batches (no reference counterpart: the reference runs one
+ * FRI replica per process; fricc/__init__.py:8-11 aggregates replicas'
+ * energies afterwards).  R independent replicas of one system, each kernel
+ * launched once for all R: the replica is one more grid dimension.  Each
+ * replica's results are bit for bit those of its own single calls. ---- */
+
+/* The batched GEMMs: batch2 groups of `batch` products; element strides
+ * s*[0..2] as in fricc_gemm_f64 / fricc_gemm_df, s*[3] between groups
+ * (0 = shared by all groups). */
+int fricc_gemm_f64_b2(const double* A, const double* B, double* C, int64_t batch, int64_t batch2, int64_t M,
+                      int64_t N, int64_t K, const int64_t sA[4], const int64_t sB[4], const int64_t sC[4], double alpha,
+                      double beta, void* stream);
+int fricc_gemm_df_b2(const double* A, const double* B, double* C, int64_t batch, int64_t batch2, int64_t M, int64_t N,
+                     int64_t K, const int64_t sA[4], const int64_t sB[4], const int64_t sC[4], double alpha,
+                     double beta, void* stream);
+
+/* fricc_combine over a 5-D index space (five strides per operand). */
+int fricc_combine5(const int64_t dims[5], int n_in, const double* const* x, const int64_t* sx, int n_prod,
+                   const double* const* p, const int64_t* sp, int n_out, double* const* out, const int64_t* so,
+                   const double* coef, int accumulate, void* stream);
+
+/* A batch of R replicas' compressed T2s (dims, m kept each), two
+ * compressions per replica and iteration (which = 0: the one the T2 terms
+ * contract, fricc/friccsd.py:100-107; which = 1: the one the W intermediates
+ * contract, :108-117). */
+int fricc_spb_create(int R, const int64_t dims[4], int64_t m, void* stream, fricc_spbatch** out);
+int fricc_spb_destroy(fricc_spbatch* B);
+/* Both systematic FRI compressions of every replica's T2 (t2: R tensors of
+ * dims, stacked) with the draws rn_dev[2r], rn_dev[2r+1] (device memory),
+ * as fricc_sp_recompress_pair does for one replica (fri_compression,
+ * src/fri_utils.cpp:439-522).  Stream-ordered; the status is read by
+ * fricc_spb_status. */
+int fricc_spb_recompress_pair(fricc_spbatch* B, const double* t2, const double* rn_dev, void* stream);
+/* Waits for the last compression; FRICC_OK or its error, *replica the
+ * first failing replica (-1 if none). */
+int fricc_spb_status(fricc_spbatch* B, int* replica);
+/* Replica r's entries of compression `which` to host memory (synchronous). */
+int fricc_spb_export(fricc_spbatch* B, int which, int r, int64_t* flat_host, double* vals_host, void* stream);
+/* The generic sparse term of fricc_spmm (FP64) / fricc_spmm_f2 (FP32 pairs,
+ * W' in the q-pair layout) for every replica: W'_r = Wp + r w_stride
+ * (w_stride 0: one W' for all replicas; in float4 units for the pair form),
+ * out'_r = Op + r o_stride.  Stream-ordered. */
+int fricc_spb_spmm(fricc_spbatch* B, int which, int pa, int pb, int ka, int kb, double coef, const double* Wp,
+                   int64_t w_stride, int64_t QS, double* Op, int64_t o_stride, void* stream);
+int fricc_spb_spmm_f2(fricc_spbatch* B, int which, int pa, int pb, int ka, int kb, double coef, const void* W2,
+                      int64_t w2_stride, int64_t QS, double* Op, int64_t o_stride, void* stream);
+/* fricc_symadd for R replicas: out [R][o][o][v][v] (C order), X with
+ * strides {replica, i, j, a, b}. */
+int fricc_symadd_b(double* out, const double* X, int64_t R, int64_t nocc, int64_t nvir, const int64_t strides[5],
+                   double coef, void* stream);
+/* fricc_energy_update for R replicas (t1/t2 arrays stacked, res [R][4];
+ * eia, fov and ovov shared).  Stream-ordered. */
+int fricc_energy_update_batch(int R, const double* t1num, const double* t2num, const double* eia, const double* fov,
+                              const double* ovov, const double* t1old, const double* t2old, int64_t o, int64_t v,
+                              double* t1out, double* t2out, double* res, void* stream);
 
 /* Zero `bytes` bytes of device memory at p (no reference counterpart; the
  * np.zeros of the reference's scratch outputs).  Stream-ordered. */

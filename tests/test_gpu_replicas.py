@@ -1,0 +1,122 @@
+"""The fused replica batch: R replicas of one system, each kernel launched
+once for all of them (fricc_gb300.replicas.FusedReplicaBatch).
+
+* Each replica's trajectory -- E_corr every iteration, t1 and t2 after
+  several -- is bit for bit the one a lone FRICCSDGPU solve with the same
+  seed and precision gives (FP64 and FP32-pair forms).
+* Both batched compressions of every replica keep the lone solve's entries
+  bit for bit (o20v100, m = 200,000, 16 replicas).
+* A bounded device wait that runs out inside the batched compression is
+  reported by fricc_spb_status with the failing replica; the next
+  compression on the same handle keeps the oracle's entries bit for bit.
+"""
+import ctypes
+
+import numpy as np
+import pytest
+import torch
+
+pytestmark = pytest.mark.gpu
+
+SETTINGS = {"compression": "fri", "sampling_method": "systematic", "verbose": False,
+            "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"]}
+
+
+def _bits(t):
+    return t.contiguous().view(torch.int64)
+
+
+def _lone(E, m, seed, precision, steps):
+    from fricc_gb300.batch import mp2_device
+    from fricc_gb300.friccsd import FRICCSDGPU
+    from fricc_gb300.rng import GlibcRand
+    lone = FRICCSDGPU(E, dict(SETTINGS, m_keep=m), rn_draw=GlibcRand(seed), precision=precision)
+    t1, t2 = mp2_device(E)
+    energies = []
+    for _ in range(steps):
+        t1, t2 = lone.update_amps(t1, t2)
+        energies.append(lone.read_energy()[0])
+    return lone, t1, t2, energies
+
+
+@pytest.mark.parametrize("precision", ["fp64", "df64"])
+def test_fused_replicas_equal_their_lone_solves(gpulib, precision):
+    from fricc_gb300.rccsd_dense import DeviceERIs
+    from fricc_gb300.replicas import FusedReplicaBatch
+    from fricc_gb300.synthetic import SyntheticSystem
+    E = DeviceERIs.from_system(SyntheticSystem(6, 24, 120, 0.05, 3))
+    m, seeds, steps = 3000, [7, 11, 12345], 3
+    fb = FusedReplicaBatch(E, {"m_keep": m}, seeds, precision=precision)
+    for _ in range(steps):
+        fb.step()
+    for r, seed in enumerate(seeds):
+        _, t1, t2, energies = _lone(E, m, seed, precision, steps)
+        assert energies == fb.history[r], (r, energies, fb.history[r])
+        assert torch.equal(_bits(t1), _bits(fb.t1[r])), r
+        assert torch.equal(_bits(t2), _bits(fb.t2[r])), r
+    assert len({h[-1] for h in fb.history}) == len(seeds)   # distinct seeds, distinct trajectories
+
+
+def test_fused_o20v100_sixteen_replicas_compress_and_step_as_alone(gpulib):
+    from fricc_gb300 import _lib as L
+    from fricc_gb300.rccsd_dense import DeviceERIs
+    from fricc_gb300.replicas import FusedReplicaBatch
+    from fricc_gb300.synthetic import WORKLOADS, make_system
+    w = WORKLOADS["o20v100x64"]
+    m = w["m"]
+    E = DeviceERIs.from_system(make_system("o20v100x64", seed=0))
+    seeds = list(range(100, 116))
+    fb = FusedReplicaBatch(E, {"m_keep": m}, seeds, precision="fp64")
+    fb.step()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    for r in (0, 7, 15):
+        lone, t1, t2, energies = _lone(E, m, seeds[r], "fp64", 1)
+        assert energies == fb.history[r]
+        assert torch.equal(_bits(t2), _bits(fb.t2[r])), r
+        for which, h in ((0, lone._sp), (1, lone._sp_w)):
+            flat = np.empty(m, dtype=np.int64)
+            vals = np.empty(m, dtype=np.float64)
+            L.check(gpulib.fricc_sp_export(h.h, ctypes.c_void_p(flat.ctypes.data), ctypes.c_void_p(vals.ctypes.data),
+                                           st))
+            bf, bv = fb.export(which, r)
+            assert np.array_equal(flat, bf) and np.array_equal(vals.view(np.int64), bv.view(np.int64)), (r, which)
+    mean, var = fb.stats()
+    assert np.isfinite(mean) and var > 0.0
+
+
+def test_batched_compression_wait_runs_out_and_recovers(gpulib, oracle):
+    from fricc_gb300 import _lib as L
+    rng = np.random.default_rng(21)
+    R, dims, m = 2, (8, 8, 40, 40), 20000
+    x_h = rng.standard_normal((R,) + dims) * rng.random((R,) + dims) ** 4
+    x = torch.from_numpy(x_h).cuda()
+    draws = [[0.5, 0.25], [0.125, 0.875]]
+    rn = torch.tensor(draws, dtype=torch.float64).cuda()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    spb = ctypes.c_void_p()
+    L.check(gpulib.fricc_spb_create(R, L.i64arr(dims), m, st, ctypes.byref(spb)))
+    try:
+        rep = ctypes.c_int(-2)
+        L.check(gpulib.fricc_tune_set(3, 2000))   # knob 3: the test-only wait of 2000 polls
+        try:
+            L.check(gpulib.fricc_spb_recompress_pair(spb, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(rn.data_ptr()),
+                                                     st))
+            assert gpulib.fricc_spb_status(spb, ctypes.byref(rep)) == 5   # FRICC_ERR_TIMEOUT
+            assert rep.value in range(R)
+        finally:
+            L.check(gpulib.fricc_tune_set(3, -1))
+        # the same handle, re-compressed: every replica's entries as the oracle's
+        L.check(gpulib.fricc_spb_recompress_pair(spb, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(rn.data_ptr()), st))
+        L.check(gpulib.fricc_spb_status(spb, ctypes.byref(rep)))
+        assert rep.value == -1
+        for r in range(R):
+            for which in (0, 1):
+                flat = np.empty(m, dtype=np.int64)
+                vals = np.empty(m, dtype=np.float64)
+                L.check(gpulib.fricc_spb_export(spb, which, r, ctypes.c_void_p(flat.ctypes.data),
+                                                ctypes.c_void_p(vals.ctypes.data), st))
+                ref = oracle.SparseTensor4d(x_h[r], dims, m, "fri", "systematic", rn=draws[r][which])
+                assert np.array_equal(flat, ref.flat), (r, which)
+                assert np.array_equal(vals.view(np.int64), ref.vals.view(np.int64)), (r, which)
+    finally:
+        gpulib.fricc_spb_destroy(spb)
