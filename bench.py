@@ -116,10 +116,9 @@ def measured_peaks() -> dict:
 
 
 def dist_setup():
-    world = int(os.environ.get("WORLD_SIZE", "1"))
-    rank = int(os.environ.get("RANK", "0"))
-    local = int(os.environ.get("LOCAL_RANK", "0"))
-    return world, rank, local
+    """(world_size, rank, local_rank) from the torchrun environment."""
+    from fricc_gb300.dist import world
+    return world()
 
 
 class ClockSampler:
@@ -390,6 +389,7 @@ def run_gpu(args):
     import torch.distributed as dist
 
     from fricc_gb300 import _lib
+    from fricc_gb300.dist import max_over_ranks, replica_seed
     from fricc_gb300.friccsd import FRICCSDGPU
     from fricc_gb300.rccsd_dense import DeviceERIs
     from fricc_gb300.synthetic import WORKLOADS, make_system
@@ -412,7 +412,7 @@ def run_gpu(args):
     if args.precision == "split":
         from fricc_gb300.cholesky import split_eris
         Es = split_eris(system, device=dev)
-    solver = FRICCSDGPU(Es if Es is not None else E, {"m_keep": m}, rn_draw=seeded_draws(1000 + rank),
+    solver = FRICCSDGPU(Es if Es is not None else E, {"m_keep": m}, rn_draw=seeded_draws(replica_seed(1000, rank)),
                         precision=args.precision, autotune=args.autotune, graph=args.graph)
     stream = torch.cuda.current_stream()
 
@@ -458,10 +458,7 @@ def run_gpu(args):
     lib.fricc_prof_enable(0)
     energy_last = solver.read_energy()[0]
 
-    t_max = torch.tensor([ms], dtype=torch.float64, device=dev)
-    if world > 1:
-        dist.all_reduce(t_max, op=dist.ReduceOp.MAX)
-    ms_max = float(t_max.item())
+    ms_max = max_over_ranks(ms, dev)
     value = world * args.steps / (ms_max / 1000.0)
 
     # end to end through the host entry point: numpy in, numpy out
@@ -478,11 +475,9 @@ def run_gpu(args):
             t1p, t2p = solver.update_amps_host(t1p, t2p)
         barrier()
         e2e_s = time.perf_counter() - t0
-        te = torch.tensor([e2e_s], dtype=torch.float64, device=dev)
-        if world > 1:
-            dist.all_reduce(te, op=dist.ReduceOp.MAX)
+        te = max_over_ranks(e2e_s, dev)
         nb = 8 * (o * v + o * o * v * v)
-        e2e = {"value": world * args.steps / float(te.item()), "unit": "iter/s", "h2d_bytes_per_step": nb,
+        e2e = {"value": world * args.steps / te, "unit": "iter/s", "h2d_bytes_per_step": nb,
                "d2h_bytes_per_step": nb}
     del solver
     torch.cuda.empty_cache()

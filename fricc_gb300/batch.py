@@ -177,6 +177,8 @@ class Request:
     started: float = math.nan
     finished: float = math.nan
     iterations: int = 0
+    build_s: float = math.nan    # system, integrals, solver and MP2 guess (stream-synchronised)
+    iterate_s: float = math.nan  # the iterations to convergence
     converged: bool = False
     e_corr: float = math.nan
     energies: list = field(default_factory=list)
@@ -233,6 +235,7 @@ class SolveServer:
         self._cv = threading.Condition()
 
     def _solve(self, req: Request, t0: float, stream):
+        tb = time.perf_counter()
         with torch.cuda.stream(stream):
             if self.device_inputs:
                 system = DeviceSystem(req.nocc, req.nvir, req.naux, req.sigma, req.seed, device=self.device)
@@ -246,7 +249,10 @@ class SolveServer:
             solver = FRICCSDGPU(E, {"m_keep": req.m}, rn_draw=GlibcRand(req.seed), precision=self.precision,
                                 graph=self.graph, rebuild_vvvv=self.rebuild_vvvv)
             t1, t2 = mp2_device(E)
-            req.started = time.perf_counter() - t0
+            stream.synchronize()
+            ti = time.perf_counter()
+            req.started = ti - t0
+            req.build_s = ti - tb
             eold = solver.energy(t1, t2)
             for it in range(self.max_cycle):
                 t1, t2 = solver.update_amps(t1, t2)
@@ -261,6 +267,7 @@ class SolveServer:
                 eold = e
             req.e_corr = req.energies[-1] if req.energies else math.nan
             stream.synchronize()
+            req.iterate_s = time.perf_counter() - ti
             del solver, E, t1, t2
 
     def run(self, requests, time_scale: float = 1.0):
@@ -314,6 +321,13 @@ class SolveServer:
 def latency_summary(reqs, time_scale=1.0):
     lat = np.array([r.finished - r.arrival * time_scale for r in reqs])
     span = max(r.finished for r in reqs) - min(r.arrival * time_scale for r in reqs)
+    build = float(sum(r.build_s for r in reqs))
+    iterate = float(sum(r.iterate_s for r in reqs))
+    its = int(sum(r.iterations for r in reqs))
     return {"p50_s": float(np.percentile(lat, 50)), "p99_s": float(np.percentile(lat, 99)),
-            "solves_per_s": len(reqs) / span, "iterations": int(sum(r.iterations for r in reqs)),
-            "converged": int(sum(r.converged for r in reqs)), "n": len(reqs)}
+            "solves_per_s": len(reqs) / span, "iterations": its,
+            "converged": int(sum(r.converged for r in reqs)), "n": len(reqs),
+            # summed over requests (concurrent requests overlap, so these add
+            # up to more than the span when several workers run)
+            "build_s_sum": build, "iterate_s_sum": iterate, "build_share": build / max(build + iterate, 1e-30),
+            "iterations_per_iterate_s": its / max(iterate, 1e-30)}
