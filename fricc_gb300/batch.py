@@ -329,5 +329,4 @@ def latency_summary(reqs, time_scale=1.0):
             "converged": int(sum(r.converged for r in reqs)), "n": len(reqs),
             # summed over requests (concurrent requests overlap, so these add
             # up to more than the span when several workers run)
-            "build_s_sum": build, "iterate_s_sum": iterate, "build_share": build / max(build + iterate, 1e-30),
-            "iterations_per_iterate_s": its / max(iterate, 1e-30)}
+            "build_s_sum": build, "iterate_s_sum": iterate, "build_share": build / max(build + iterate, 1e-30)}
