@@ -91,6 +91,11 @@ SIGNATURES = [
     ("fricc_spb_spmm_f2", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
                                          ctypes.c_double, _vp, _i64, _i64, _dp, _i64, _vp]),
     ("fricc_symadd_b", ctypes.c_int, [_dp, _dp, _i64, _i64, _i64, _i64p, ctypes.c_double, _vp]),
+    ("fricc_spb_densify_bf16x3", ctypes.c_int, [_vp, ctypes.c_int, ctypes.c_int, ctypes.c_int, ctypes.c_int,
+                                                 ctypes.c_int, ctypes.c_double, _vp, _i64, _vp]),
+    ("fricc_gemm_bf16_tn_strided_b", ctypes.c_int, [_vp, _i64, _vp, _i64, _i64, _i64, _i64, _dp, _i64, _i64, _i64,
+                                                     _i64, _i64, _i64, ctypes.c_double, ctypes.c_double, ctypes.c_int,
+                                                     ctypes.c_int, _i64, _i64, _i64, _vp, _vp]),
     ("fricc_energy_update_batch", ctypes.c_int, [ctypes.c_int, _dp, _dp, _dp, _dp, _dp, _dp, _dp, _i64, _i64, _dp,
                                                  _dp, _dp, _vp]),
     ("fricc_phase_timing_set", ctypes.c_int, [ctypes.c_int]),

@@ -1,8 +1,10 @@
 """Per-shape launch-configuration autotuning.
 
 The library exposes thread-local overrides of its launch configurations
-(``fricc_tune_set``): the float-pair sparse kernel's output pairs per thread
-and the FP32-pair GEMM's tile shape and split-K target.  ``Autotuner`` times
+(``fricc_tune_set``): the float-pair sparse kernel's output pairs per thread,
+the FP32-pair GEMM's tile shape and split-K target, and the width of the
+compression's first select digit (how many candidates its exact top-m sort
+takes).  ``Autotuner`` times
 every candidate configuration of an operation the first time it meets that
 operation's shape -- on scratch copies of the outputs, so the real result is
 computed once, after the choice -- and replays the fastest configuration for
@@ -19,11 +21,14 @@ import torch
 
 from . import _lib as L
 
-SPMM_PPT, GEMM_TILE, GEMM_COVER = 0, 1, 2
+SPMM_PPT, GEMM_TILE, GEMM_COVER, SELECT_BITS = 0, 1, 2, 4
 
 # candidate configurations: {knob: value}; {} is the library's own choice
 SPMM_CANDIDATES = [{SPMM_PPT: p} for p in (1, 2, 4)]
-GEMM_CANDIDATES = [{}] + [{GEMM_TILE: t, GEMM_COVER: c} for t, c in itertools.product(range(4), (2, 4, 8))]
+GEMM_CANDIDATES = [{}] + [{GEMM_TILE: t, GEMM_COVER: c} for t, c in itertools.product(range(5), (2, 4, 8))]
+# the compression's top-m selection schedule: the first select digit's width
+# (candidates left for the exact sort), 12 bits by default
+COMPRESS_CANDIDATES = [{SELECT_BITS: b} for b in (10, 11, 12, 13)]
 
 
 @contextlib.contextmanager
@@ -84,6 +89,6 @@ class Autotuner:
         """{key: (best config, best ms, default ms)} for the tuned shapes."""
         out = {}
         for k, res in self.trials.items():
-            default = [ms for ms, cfg in res if cfg == {} or cfg == {SPMM_PPT: 2}]
+            default = [ms for ms, cfg in res if cfg in ({}, {SPMM_PPT: 2}, {SELECT_BITS: 12})]
             out[k] = (res[0][1], res[0][0], default[0] if default else None)
         return out

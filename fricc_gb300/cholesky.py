@@ -345,3 +345,133 @@ def split_eris(system, device="cuda"):
     blocks["S0"] = s.t() @ s                          # sum_cd (ac|bd)
     blocks["vvvv_rebuild"] = VvvvRebuild(Lf, o)
     return DeviceERIs(_dev_tensor(system.fock, dev), _dev_tensor(system.mo_energy, dev), o, blocks, device)
+
+
+# ---------------------------------------------------------------------------
+# Replica batches: each replica's GEMM exactly as gemm_tc / dense_spmm run it
+# alone (same flattening, swap, K split and tiles), all replicas in one launch
+# of the tensor-core kernel.
+
+def _rep_operand(X: torch.Tensor, cdim: int, R: int):
+    """(the replica-0 operand as gemm_tc sees it alone, replica stride or 0
+    when shared): with a 3-D output [R, M, N] an operand is 3-D (per
+    replica) or 2-D (shared); with a 4-D output [R, b, M, N] it is 4-D, per
+    replica unless its leading extent is 1 or its leading stride 0."""
+    if cdim == 3:
+        return (X[0], X.stride(0)) if X.dim() == 3 else (X, 0)
+    assert X.dim() == 4, "a 4-D output takes 4-D operands ([1, ...] when shared)"
+    shared = X.shape[0] == 1 or X.stride(0) == 0 or R == 1
+    return X[0], (0 if shared else X.stride(0))
+
+
+def gemm_tc_rep(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float, beta: float, R: int,
+                status: torch.Tensor | None = None, a_split: torch.Tensor | None = None,
+                b_split: torch.Tensor | None = None):
+    """gemm_tc(A_r, B_r, C_r) for every replica r = 0..R-1 in one launch:
+    C is [R, M, N] or [R, b, M, N]; operands follow ``_rep_operand``.  The
+    flattening, the narrow-side swap, the K split and the FP32-pair fallback
+    are decided from one replica's shapes, so every replica's result is bit
+    for bit that of its own gemm_tc call."""
+    from . import rccsd_dense as D
+    cdim = C.dim()
+    A0, ra = _rep_operand(A, cdim, R)
+    B0, rb = _rep_operand(B, cdim, R)
+    C0 = C[0]
+
+    def stacked(X, X0, rx):
+        # the (replica, batch) rows of a batched per-replica operand must be
+        # one stride apart: copy X when its replicas are not stacked so
+        s0, bx = D._strides3(X0)
+        if rx and bx > 1 and s0[2] != 0 and rx != bx * s0[2]:
+            Xc = torch.empty(X.shape, dtype=X.dtype, device=X.device)
+            D.combine([Xc], [X])
+            return Xc, Xc[0], Xc.stride(0)
+        return X, X0, rx
+    A, A0, ra = stacked(A, A0, ra)
+    B, B0, rb = stacked(B, B0, rb)
+    sA, bA = D._strides3(A0)
+    sB, bB = D._strides3(B0)
+    sC, batch = D._strides3(C0)
+    M, N, K = C0.shape[-2], C0.shape[-1], A0.shape[-1]
+    assert A0.shape[-2] == M and B0.shape[-2] == K and B0.shape[-1] == N and bA in (1, batch) and bB in (1, batch)
+    a_b = batch > 1 and bA > 1 and sA[2] != 0
+    b_b = batch > 1 and bB > 1 and sB[2] != 0
+
+    def df():  # the FP32-pair GEMM, every replica as the second batch level
+        def four(X, Xr, lone):
+            if cdim == 4:
+                return X
+            return X.unsqueeze(1) if Xr else lone.unsqueeze(0).unsqueeze(0)
+        return D.gemm_df(four(A, ra, A0), four(B, rb, B0), C if cdim == 4 else C.unsqueeze(1), alpha, beta)
+
+    if batch > 1 and a_b == b_b:
+        df()
+        return C
+    Mf = M * (batch if a_b else 1)
+    Nf = N * (batch if b_b else 1)
+    swap = Mf <= 64 < Nf
+    ks = _ksplit(_tiles(Nf, Mf) if swap else _tiles(Mf, Nf), _kp(K)) if K > 0 else 0
+    if ks == 0:
+        df()
+        return C
+    # A' rows: (replica, batch, m) or (replica, m); one split for a shared A
+    if a_split is not None:
+        assert ra == 0 and Mf == M and a_split.shape == (M, _kp(K))
+        Ap, a_rep = a_split, 0
+        mi, sro, sri = M, 0, sC[0]
+    else:
+        if ra:
+            Ap = _split_view(A0, R * Mf, K, M, sA[2] if a_b else ra, sA[0], sA[1], True, False)
+        else:
+            Ap = _split_view(A0, Mf, K, M, sA[2] if a_b else 0, sA[0], sA[1], True, False)
+        a_rep = Mf if ra else 0
+        mi, sro, sri = M, (sC[2] if a_b else 0), sC[0]
+    if b_split is not None:
+        assert rb == 0 and Nf == N and b_split.shape == (N, _kp(K))
+        Bp, b_rep = b_split, 0
+        ni, sco, sci = N, 0, sC[1]
+    else:
+        if rb:
+            Bp = _split_view(B0, R * Nf, K, N, sB[2] if b_b else rb, sB[1], sB[0], False, True)
+        else:
+            Bp = _split_view(B0, Nf, K, N, sB[2] if b_b else 0, sB[1], sB[0], False, True)
+        b_rep = Nf if rb else 0
+        ni, sco, sci = N, (sC[2] if b_b else 0), sC[1]
+    kp = Ap.shape[1]
+    if swap:
+        Ap, Bp, Mf, Nf, a_rep, b_rep = Bp, Ap, Nf, Mf, b_rep, a_rep
+        mi, sro, sri, ni, sco, sci = ni, sco, sci, mi, sro, sri
+    L.check(L.load().fricc_gemm_bf16_tn_strided_b(_p(Ap), kp, _p(Bp), kp, Mf, Nf, kp, _p(C), mi, ni, sro, sri, sco,
+                                                  sci, float(alpha), float(beta), ks, R, a_rep, b_rep, C.stride(0),
+                                                  _p(status) if status is not None else None, _st()))
+    return C
+
+
+def dense_spmm_rep(spb, which: int, R: int, dims, pa, pb, ka, kb, coef, Bt: torch.Tensor, b_rep: int, QS: int,
+                   Op: torch.Tensor, status: torch.Tensor | None = None) -> bool:
+    """dense_spmm for every replica of a compressed batch (``spb``, a
+    fricc_spbatch handle; compression ``which``) in one densify and one
+    tensor-core launch: replica r's A' rows r nP.., its W^T split at row
+    r b_rep of Bt (b_rep 0: one W for all), its output Op[r] ([R, nP*QS]
+    contiguous).  False (nothing done) where dense_spmm would decline."""
+    nP, Rk = dims[pa] * dims[pb], dims[ka] * dims[kb]
+    kp = _kp(Rk)
+    assert Bt.shape[1] == kp and Bt.shape[0] >= QS and Op.is_contiguous() and Op.numel() == R * nP * QS
+    ks = _ksplit(_tiles(nP, QS), kp)
+    if ks == 0:
+        return False
+    Ap = torch.empty(R * nP, kp, dtype=torch.bfloat16, device=Op.device)
+    lib = L.load()
+    L.check(lib.fricc_spb_densify_bf16x3(spb, which, pa, pb, ka, kb, float(coef), _p(Ap), kp, _st()))
+    L.check(lib.fricc_gemm_bf16_tn_strided_b(_p(Ap), kp, _p(Bt), kp, nP, QS, kp, _p(Op), nP, QS, 0, QS, 0, 1, 1.0,
+                                             1.0, ks, R, nP, b_rep, nP * QS,
+                                             _p(status) if status is not None else None, _st()))
+    return True
+
+
+def split_b_rep(W: torch.Tensor, R: int, QS: int) -> torch.Tensor:
+    """split_b(W[r].reshape(-1, QS)) of every replica, stacked: rows
+    (r, q), R*QS of them (W contiguous [R, ...])."""
+    assert W.is_contiguous()
+    krows = W[0].numel() // QS
+    return _split_view(W, R * QS, krows, QS, krows * QS, 1, QS, False, True)

@@ -53,6 +53,8 @@ int fricc_unpack_batch_async(const int64_t* flat, int64_t m, int R, const int64_
 int fricc_batch_spmm_device(FriccSparseBatch* B, int which, int pa, int pb, int ka, int kb, double coef,
                             const void* Wp, int64_t w_stride, int64_t QS, double* Op, int64_t o_stride, bool f2,
                             cudaStream_t st);
+int fricc_batch_densify_device(FriccSparseBatch* B, int which, int pa, int pb, int ka, int kb, double coef, void* Ap,
+                               int64_t kp, cudaStream_t st);
 int fricc_energy_update_batch_device(int R, const double* t1num, const double* t2num, const double* eia,
                                      const double* fov, const double* ovov, const double* t1old, const double* t2old,
                                      int64_t o, int64_t v, double* t1out, double* t2out, double* res,
@@ -98,7 +100,7 @@ static cudaEvent_t g_prof_pending[kProfChannels] = {nullptr, nullptr, nullptr};
 
 void fricc_note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
-static thread_local int g_tune[FRICC_TUNE_KNOBS] = {-1, -1, -1, -1};
+static thread_local int g_tune[FRICC_TUNE_KNOBS] = {-1, -1, -1, -1, -1};
 int fricc_tune_get(int knob) { return knob >= 0 && knob < FRICC_TUNE_KNOBS ? g_tune[knob] : -1; }
 bool fricc_prof_on() { return g_prof.load(std::memory_order_relaxed); }
 
@@ -188,7 +190,7 @@ long long fricc_launch_count(void) { return g_launches.load(); }
 long long fricc_alloc_count(void) { return g_allocs.load(); }
 
 int fricc_tune_set(int knob, int value) {
-  static const int lo[FRICC_TUNE_KNOBS] = {1, 0, 1, 1}, hi[FRICC_TUNE_KNOBS] = {4, 3, 16, 1 << 20};
+  static const int lo[FRICC_TUNE_KNOBS] = {1, 0, 1, 1, 10}, hi[FRICC_TUNE_KNOBS] = {4, 4, 16, 1 << 20, 13};
   if (knob < 0 || knob >= FRICC_TUNE_KNOBS || (value != -1 && (value < lo[knob] || value > hi[knob]))) {
     fricc_set_error("tune_set: bad knob or value");
     return FRICC_ERR_ARG;
@@ -814,6 +816,11 @@ int fricc_spb_spmm_f2(fricc_spbatch* B, int which, int pa, int pb, int ka, int k
                       int64_t w2_stride, int64_t QS, double* Op, int64_t o_stride, void* stream) {
   return fricc_batch_spmm_device(B, which, pa, pb, ka, kb, coef, W2, w2_stride, QS, Op, o_stride, true,
                                  as_stream(stream));
+}
+
+int fricc_spb_densify_bf16x3(fricc_spbatch* B, int which, int pa, int pb, int ka, int kb, double coef, void* Ap,
+                             int64_t kp, void* stream) {
+  return fricc_batch_densify_device(B, which, pa, pb, ka, kb, coef, Ap, kp, as_stream(stream));
 }
 
 int fricc_energy_update_batch(int R, const double* t1num, const double* t2num, const double* eia, const double* fov,

@@ -118,7 +118,10 @@ void fricc_note_launch(int n = 1);
 // polls a word nothing sets this many times, then reports FRICC_DEV_TIMEOUT
 // (the compaction itself then runs as usual, so every result stays valid)
 #define FRICC_TUNE_TEST_WAIT 3
-#define FRICC_TUNE_KNOBS 4
+// the width in bits (10..13) of a compression's first select digit, which
+// decides how many candidates the exact sort takes (never which are kept)
+#define FRICC_TUNE_SELECT_BITS 4
+#define FRICC_TUNE_KNOBS 5
 int fricc_tune_get(int knob);
 bool fricc_prof_on();
 void fricc_prof_record(cudaStream_t st, bool start, double flops, int channel = 0);

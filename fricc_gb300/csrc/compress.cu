@@ -30,9 +30,17 @@
 
 namespace {
 
-constexpr int DIG_BITS = 12;                 // first select digit: |x| bits [62:51]
-constexpr int DIG_SHIFT = 63 - DIG_BITS;
-constexpr int NDIG = 1 << DIG_BITS;
+// The first select digit: the top `bits` bits of |x| below the sign, 12 by
+// default (bits [62:51]: the exponent and one mantissa bit, half an octave
+// per bin), 10-13 through FRICC_TUNE_SELECT_BITS.  A wider digit leaves
+// fewer candidates for the sort; every width selects the same elements.
+constexpr int DIG_BITS_DEFAULT = 12, DIG_BITS_MIN = 10, DIG_BITS_MAX = 13;
+constexpr int NDIG = 1 << DIG_BITS_MAX;  // histogram words per compression
+
+int select_bits() {
+  const int b = fricc_tune_get(FRICC_TUNE_SELECT_BITS);
+  return b >= DIG_BITS_MIN && b <= DIG_BITS_MAX ? b : DIG_BITS_DEFAULT;
+}
 
 __device__ __forceinline__ unsigned long long abs_key(double v) {
   return (unsigned long long)__double_as_longlong(v) & 0x7fffffffffffffffull;
@@ -47,18 +55,20 @@ struct Rep {
   int64_t n = 0, m = 0, tile = 0, one = 0;
 };
 
-__global__ void __launch_bounds__(256) k_hist12(const double* __restrict__ x, int64_t n, unsigned* __restrict__ hist,
-                                                Rep rp = Rep{}) {
+// histogram of the first select digit (1 << bits bins of dynamic shared memory)
+__global__ void __launch_bounds__(256) k_hist_sel(const double* __restrict__ x, int64_t n, unsigned* __restrict__ hist,
+                                                  int bits, Rep rp = Rep{}) {
   x += blockIdx.y * rp.n;
   hist += blockIdx.y * rp.one * NDIG;
-  __shared__ unsigned h[NDIG];
-  for (int i = threadIdx.x; i < NDIG; i += 256) h[i] = 0;
+  extern __shared__ unsigned h[];
+  const int nb = 1 << bits, shift = 63 - bits;
+  for (int i = threadIdx.x; i < nb; i += 256) h[i] = 0;
   __syncthreads();
   const int64_t stride = (int64_t)gridDim.x * 256;
   for (int64_t i = (int64_t)blockIdx.x * 256 + threadIdx.x; i < n; i += stride)
-    atomicAdd(&h[abs_key(x[i]) >> DIG_SHIFT], 1u);
+    atomicAdd(&h[abs_key(x[i]) >> shift], 1u);
   __syncthreads();
-  for (int i = threadIdx.x; i < NDIG; i += 256)
+  for (int i = threadIdx.x; i < nb; i += 256)
     if (h[i]) atomicAdd(&hist[i], h[i]);
 }
 
@@ -97,7 +107,7 @@ __global__ void __launch_bounds__(256) k_compact(const double* __restrict__ x, i
                                                  unsigned long long* __restrict__ ckey, unsigned* __restrict__ cidx,
                                                  unsigned long long* tstate, unsigned* ticket, unsigned* err,
                                                  const unsigned long long* never_set, long long test_spins,
-                                                 Rep rp = Rep{}) {
+                                                 int shift, Rep rp = Rep{}) {
   constexpr int NT = 256, ITEMS = 16, TILE = NT * ITEMS;
   {
     const int64_t r = blockIdx.y;
@@ -124,7 +134,7 @@ __global__ void __launch_bounds__(256) k_compact(const double* __restrict__ x, i
   for (int k = 0; k < ITEMS; ++k) {
     const int64_t i = base + k;
     key[k] = i < n ? abs_key(x[i]) : 0ull;
-    if (i < n && (unsigned)(key[k] >> DIG_SHIFT) >= dmin) ++cnt;
+    if (i < n && (unsigned)(key[k] >> shift) >= dmin) ++cnt;
   }
   int64_t tot;
   const int64_t excl = block_excl_sum(cnt, sm, &tot);
@@ -169,7 +179,7 @@ __global__ void __launch_bounds__(256) k_compact(const double* __restrict__ x, i
 #pragma unroll
   for (int k = 0; k < ITEMS; ++k) {
     const int64_t i = base + k;
-    if (i < n && (unsigned)(key[k] >> DIG_SHIFT) >= dmin) {
+    if (i < n && (unsigned)(key[k] >> shift) >= dmin) {
       ckey[o] = key[k];
       cidx[o] = (unsigned)i;
       ++o;
@@ -286,11 +296,11 @@ struct ConsSample2 {
 };
 
 // The select digit: the largest d with count(digit >= d) >= m (one thread).
-__global__ void k_select_digit(const unsigned* __restrict__ hist, int64_t m, Ctl* c, Rep rp = Rep{}) {
+__global__ void k_select_digit(const unsigned* __restrict__ hist, int64_t m, Ctl* c, int bits, Rep rp = Rep{}) {
   hist += blockIdx.x * rp.one * NDIG;
   c += blockIdx.x * rp.one;
   int64_t cum = 0;
-  int d = NDIG - 1;
+  int d = (1 << bits) - 1;
   for (; d >= 0; --d) {
     cum += hist[d];
     if (cum >= m) break;
@@ -1073,10 +1083,14 @@ int fricc_compress_device(const double* x, int64_t n, int64_t m, int mode, doubl
 
     // 1-2. select digit, candidates, sort (argsort, src/fri_utils.cpp:11-36)
     phase_mark(0, st);
-    k_hist12<<<grid_for(n, 256), 256, 0, st>>>(x, n, s.hist);
-    k_select_digit<<<1, 1, 0, st>>>(s.hist, m, ctl);
-    k_compact<<<(unsigned)ntile, 256, 0, st>>>(x, n, ctl, s.ckey, s.cidx, s.tstate, s.ticket, s.err,
-                                               s.tstate + ntile, (long long)fricc_tune_get(FRICC_TUNE_TEST_WAIT));
+    {
+      const int bits = select_bits();
+      k_hist_sel<<<grid_for(n, 256), 256, sizeof(unsigned) << bits, st>>>(x, n, s.hist, bits);
+      k_select_digit<<<1, 1, 0, st>>>(s.hist, m, ctl, bits);
+      k_compact<<<(unsigned)ntile, 256, 0, st>>>(x, n, ctl, s.ckey, s.cidx, s.tstate, s.ticket, s.err,
+                                                 s.tstate + ntile, (long long)fricc_tune_get(FRICC_TUNE_TEST_WAIT),
+                                                 63 - bits);
+    }
     fricc_note_launch(3);
     TRY(radix::sort_pairs(s.ckey, s.cidx, s.ktmp, s.vtmp, n, 64, true, s.rhist, st, &ctl->ncand));
 
@@ -1324,11 +1338,13 @@ int fricc_compress_pair_batch_device(const double* x, int64_t n, int64_t m, int 
     const unsigned gn = grid_for(n, 256), gm = grid_for(m, 256);
 
     // 1-2. select digit, candidates, sort
-    k_hist12<<<dim3(gn, R), 256, 0, st>>>(x, n, s.hist, rp);
-    k_select_digit<<<R, 1, 0, st>>>(s.hist, m, ctl, rp);
+    const int bits = select_bits();
+    k_hist_sel<<<dim3(gn, R), 256, sizeof(unsigned) << bits, st>>>(x, n, s.hist, bits, rp);
+    k_select_digit<<<R, 1, 0, st>>>(s.hist, m, ctl, bits, rp);
     k_compact<<<dim3((unsigned)ntile, R), 256, 0, st>>>(x, n, ctl, s.ckey, s.cidx, s.tstate, s.ticket, s.err,
                                                         s.tstate + ntile,
-                                                        (long long)fricc_tune_get(FRICC_TUNE_TEST_WAIT), rp);
+                                                        (long long)fricc_tune_get(FRICC_TUNE_TEST_WAIT), 63 - bits,
+                                                        rp);
     fricc_note_launch(3);
     {
       radix::Batch bt;

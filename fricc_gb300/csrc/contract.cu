@@ -326,9 +326,14 @@ __global__ void __launch_bounds__(DF_NT, 8) k_spmm_df(const int* __restrict__ bp
 // (rows of kp elements, zeroed beforehand): the split-precision form runs
 // every sparse term as a dense GEMM on the tensor cores.  (P, r) is unique
 // per nonzero, so the scatter has no collisions.
+// (A batch of replicas: replica blockIdx.y reads its m entries at
+// blockIdx.y * m and writes its own nP rows of A' at blockIdx.y * a_rep.)
 __global__ void k_densify_bf16x3(const int* __restrict__ slots, const double* __restrict__ vals, int64_t m, int pa,
                                  int pb, int64_t dpb, int ka, int kb, int64_t dkb, double coef, int64_t R, int64_t kp,
-                                 __nv_bfloat16* __restrict__ Ap) {
+                                 __nv_bfloat16* __restrict__ Ap, int64_t a_rep = 0) {
+  slots += 4 * (int64_t)blockIdx.y * m;
+  vals += (int64_t)blockIdx.y * m;
+  Ap += (int64_t)blockIdx.y * a_rep;
   for (int64_t s = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; s < m; s += (int64_t)gridDim.x * blockDim.x) {
     const int64_t P = (int64_t)slots[4 * s + pa] * dpb + slots[4 * s + pb];
     const int64_t r = (int64_t)slots[4 * s + ka] * dkb + slots[4 * s + kb];
@@ -869,6 +874,35 @@ int fricc_densify_bf16x3_device(FriccSparse* T, int pa, int pb, int ka, int kb, 
     e = cudaGetLastError();
   }
   return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "densify_bf16x3", __FILE__, __LINE__);
+}
+
+// The batch form: every replica's compression `which` into its own nP rows
+// of A' ([R][nP][kp], zeroed here), one launch.
+int fricc_batch_densify_device(FriccSparseBatch* B, int which, int pa, int pb, int ka, int kb, double coef, void* Ap,
+                               int64_t kp, cudaStream_t st) {
+  if (!B || !Ap || which < 0 || which > 1 || pa < 0 || pa > 3 || pb < 0 || pb > 3 || ka < 0 || ka > 3 || kb < 0 ||
+      kb > 3 || pa == pb || ka == kb) {
+    fricc_set_error("batch densify_bf16x3: bad arguments");
+    return FRICC_ERR_ARG;
+  }
+  if (!B->compressed) {
+    fricc_set_error("batch densify_bf16x3: the batch has not been compressed yet");
+    return FRICC_ERR_ARG;
+  }
+  const int64_t nP = B->dims[pa] * B->dims[pb], R = B->dims[ka] * B->dims[kb];
+  if (kp < 3 * R) {
+    fricc_set_error("batch densify_bf16x3: kp must be >= 3 * dims[ka] * dims[kb]");
+    return FRICC_ERR_ARG;
+  }
+  cudaError_t e = cudaMemsetAsync(Ap, 0, sizeof(__nv_bfloat16) * (size_t)(B->R * nP * kp), st);
+  if (e == cudaSuccess) {
+    k_densify_bf16x3<<<dim3(grid_for(B->m, 256), B->R), 256, 0, st>>>(
+        B->slots[which], B->vals[which], B->m, pa, pb, B->dims[pb], ka, kb, B->dims[kb], coef, R, kp,
+        static_cast<__nv_bfloat16*>(Ap), nP * kp);
+    fricc_note_launch();
+    e = cudaGetLastError();
+  }
+  return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "batch densify_bf16x3", __FILE__, __LINE__);
 }
 
 int fricc_split_f2_device(const double* x, int64_t rows, int64_t qs, float4* out, cudaStream_t st) {

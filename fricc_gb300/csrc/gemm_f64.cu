@@ -288,19 +288,25 @@ int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t b
     fricc_free(part, st);
     return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "gemm_f64", __FILE__, __LINE__);
   }
-  // tile shape: the one of 64x64, 128x32, 32x128, 32x160 that pads C least
+  // tile shape: the one of 64x64, 128x32, 32x128, 32x160, 32x32 that pads C
+  // least
   int tm = 4, tn = 4;
   {
-    const int cand[4][2] = {{4, 4}, {8, 2}, {2, 8}, {2, 10}};
+    // the small 32x32 tile counts 1.3 times its area (two rows and two
+    // columns per thread reuse each operand load less): it wins only for
+    // outputs of a few tens of rows and columns, such as cc_Foo's o x o
+    const int cand[5][2] = {{4, 4}, {8, 2}, {2, 8}, {2, 10}, {2, 2}};
+    const int weight10[5] = {10, 10, 10, 10, 13};
     const int forced = fricc_tune_get(FRICC_TUNE_GEMM_TILE);
     if (forced >= 0) {
       tm = cand[forced][0];
       tn = cand[forced][1];
     } else {
       int64_t best = -1;
-      for (const auto& c : cand) {
-        const int64_t pad = fricc_cdiv(M, 16 * c[0]) * 16 * c[0] * fricc_cdiv(N, 16 * c[1]) * 16 * c[1];
-        if (best < 0 || pad < best) { best = pad; tm = c[0]; tn = c[1]; }
+      for (int c = 0; c < 5; ++c) {
+        const int64_t pad = fricc_cdiv(M, 16 * cand[c][0]) * 16 * cand[c][0] * fricc_cdiv(N, 16 * cand[c][1]) * 16 *
+                            cand[c][1] * weight10[c];
+        if (best < 0 || pad < best) { best = pad; tm = cand[c][0]; tn = cand[c][1]; }
       }
     }
   }
@@ -332,6 +338,7 @@ int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t b
   if (tm == 8) k_gemm_f64<8, 2><<<grid, NT, 0, st>>>(g);
   else if (tn == 8) k_gemm_f64<2, 8><<<grid, NT, 0, st>>>(g);
   else if (tn == 10) k_gemm_f64<2, 10><<<grid, NT, 0, st>>>(g);
+  else if (tm == 2 && tn == 2) k_gemm_f64<2, 2><<<grid, NT, 0, st>>>(g);
   else k_gemm_f64<4, 4><<<grid, NT, 0, st>>>(g);
   fricc_note_launch();
   if (splits > 1) {

@@ -164,7 +164,7 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 struct EpiRowMajor {
   float* C;
   int64_t M, N, ldc;
-  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v, int) const {
+  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v, int, int) const {
     if (row >= M) return;
     float* c = C + row * ldc + col0;
     if (col0 + 16 <= N && (ldc & 3) == 0) {
@@ -182,7 +182,7 @@ struct EpiRowMajor {
 struct EpiRowMajorF64 {
   double* C;
   int64_t M, N, ldc;
-  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v, int) const {
+  __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v, int, int) const {
     if (row >= M) return;
     double* c = C + row * ldc + col0;
 #pragma unroll
@@ -198,10 +198,11 @@ struct EpiStridedF64 {
   double* C;
   int64_t M, N, mi, ni, sro, sri, sco, sci;
   double alpha, beta;
-  __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v, int) const {
+  int64_t srep;  // C offset of replica r: r * srep
+  __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v, int, int rep) const {
     if (r >= M) return;
     const int64_t ro = r / mi;
-    const int64_t rbase = ro * sro + (r - ro * mi) * sri;
+    const int64_t rbase = rep * srep + ro * sro + (r - ro * mi) * sri;
     int64_t co = c0 / ni, ci = c0 - co * ni;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
@@ -218,13 +219,14 @@ struct EpiStridedF64 {
   }
 };
 
-// split K: slice s of the sum into the FP32 partial P[s][M][N]
+// split K: slice s of replica rep's sum into the FP32 partial P[rep][s][M][N]
 struct EpiPartial {
   float* P;
   int64_t M, N;
-  __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v, int s) const {
+  int ks;
+  __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v, int s, int rep) const {
     if (r >= M) return;
-    float* p = P + ((int64_t)s * M + r) * N + c0;
+    float* p = P + (((int64_t)rep * ks + s) * M + r) * N + c0;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
       if (c0 + i < N) p[i] = v[i];
@@ -232,14 +234,18 @@ struct EpiPartial {
 };
 
 // C (the EpiStridedF64 mapping) = alpha sum_s P[s] + beta C, slices summed
-// in order (deterministic)
-__global__ void k_reduce_partials(const float* __restrict__ P, int ks, int64_t M, int64_t N, EpiStridedF64 o) {
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < M * N; t += (int64_t)gridDim.x * blockDim.x) {
+// in order (deterministic), for each of `reps` replicas
+__global__ void k_reduce_partials(const float* __restrict__ P, int ks, int64_t M, int64_t N, EpiStridedF64 o,
+                                  int reps) {
+  const int64_t MN = M * N;
+  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < reps * MN;
+       t += (int64_t)gridDim.x * blockDim.x) {
+    const int64_t rep = t / MN, tt = t - rep * MN;
     double acc = 0.0;
-    for (int s = 0; s < ks; ++s) acc += f2d_bits(P[(int64_t)s * M * N + t]);
-    const int64_t r = t / N, c = t - r * N;
+    for (int s = 0; s < ks; ++s) acc += f2d_bits(P[(rep * ks + s) * MN + tt]);
+    const int64_t r = tt / N, c = tt - r * N;
     const int64_t ro = r / o.mi, co = c / o.ni;
-    double* p = o.C + ro * o.sro + (r - ro * o.mi) * o.sri + co * o.sco + (c - co * o.ni) * o.sci;
+    double* p = o.C + rep * o.srep + ro * o.sro + (r - ro * o.mi) * o.sri + co * o.sco + (c - co * o.ni) * o.sci;
     const double x = o.alpha * acc;
     *p = o.beta == 0.0 ? x : x + o.beta * *p;
   }
@@ -255,7 +261,7 @@ __global__ void k_reduce_partials(const float* __restrict__ P, int ks, int64_t M
 struct EpiVvvv {
   float* W;
   int64_t v, ldw;
-  __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x, int) const {
+  __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x, int, int) const {
     if (r1 >= v * v) return;
     const int64_t d = r1 / v, b = r1 - d * v;
     int64_t c = r2 / v, a = r2 - c * v;
@@ -299,7 +305,7 @@ __device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, in
 struct EpiVvvvSplitB {
   __nv_bfloat16* B;
   int64_t v, kpo;
-  __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x, int) const {
+  __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x, int, int) const {
     const int64_t R = v * v;
     if (r1 >= R) return;
     const int64_t b = r1 / v, d = r1 - b * v;
@@ -322,10 +328,19 @@ struct EpiVvvvSplitB {
   }
 };
 
+// Replicas: `reps` GEMMs of one shape in one launch (work units replica-
+// major); replica r reads A' rows from r * a_rep (0: one A' for all) and B'
+// rows from r * b_rep, and its epilogue gets r.  Each replica's tiles, K
+// slices and accumulation order are those of a launch of its GEMM alone.
+struct RepTC {
+  int reps = 1;
+  int a_rep = 0, b_rep = 0;
+};
+
 template <class TC, class Epi>
 __global__ void __launch_bounds__(NT, 1)
     k_gemm_tc(const __grid_constant__ CUtensorMap tma, const __grid_constant__ CUtensorMap tmb, int K, int tiles_m,
-              int tiles_n, int ksplit, Epi epi, unsigned* err) {
+              int tiles_n, int ksplit, Epi epi, unsigned* err, RepTC rt) {
   constexpr int BN = TC::BN, STAGES = TC::STAGES, B_BYTES = TC::B_BYTES;
   constexpr uint32_t IDESC = TC::IDESC;
   extern __shared__ uint8_t dsm[];
@@ -340,7 +355,8 @@ __global__ void __launch_bounds__(NT, 1)
   // split K: work unit u = (tile u % ntiles, K slice u / ntiles), each slice
   // nkc k blocks (the last one shorter, never empty)
   const int nkc = (nk + ksplit - 1) / ksplit;
-  const int nunits = ntiles * ksplit;
+  const int per_rep = ntiles * ksplit;
+  const int nunits = per_rep * rt.reps;
 
   if (threadIdx.x == 0) {
     for (int s = 0; s < STAGES; ++s) {
@@ -369,10 +385,11 @@ __global__ void __launch_bounds__(NT, 1)
     if (lane == 0) {  // TMA producer
       int g = 0;      // k blocks issued over all tiles
       for (int u = blockIdx.x; u < nunits && !*(volatile int*)&failed; u += gridDim.x) {
+        const int rep = u / per_rep, w = u - rep * per_rep;
         int mt, nt;
-        tile_coords(u % ntiles, tiles_m, tiles_n, mt, nt);
-        const int kb1 = min(nk, (u / ntiles + 1) * nkc);
-        for (int kb = (u / ntiles) * nkc; kb < kb1; ++kb, ++g) {
+        tile_coords(w % ntiles, tiles_m, tiles_n, mt, nt);
+        const int kb1 = min(nk, (w / ntiles + 1) * nkc);
+        for (int kb = (w / ntiles) * nkc; kb < kb1; ++kb, ++g) {
           const int s = g % STAGES;
           const uint32_t ph = (uint32_t)(g / STAGES) & 1u;
           if (g >= STAGES && !mbar_wait(smem_u32(&empty[s]), ph ^ 1u)) {
@@ -381,8 +398,8 @@ __global__ void __launch_bounds__(NT, 1)
             break;
           }
           mbar_expect_tx(smem_u32(&full[s]), A_BYTES + B_BYTES);
-          tma_load_2d(sA + s * A_BYTES, &tma, kb * BK, mt * BM, smem_u32(&full[s]));
-          tma_load_2d(sB + s * B_BYTES, &tmb, kb * BK, nt * BN, smem_u32(&full[s]));
+          tma_load_2d(sA + s * A_BYTES, &tma, kb * BK, rep * rt.a_rep + mt * BM, smem_u32(&full[s]));
+          tma_load_2d(sB + s * B_BYTES, &tmb, kb * BK, rep * rt.b_rep + nt * BN, smem_u32(&full[s]));
         }
       }
       if (*(volatile int*)&failed) {
@@ -394,7 +411,8 @@ __global__ void __launch_bounds__(NT, 1)
   } else if (warp == 1) {
     if (lane == 0) {  // MMA issuer
       int g = 0, i = 0;
-      for (int w = blockIdx.x; w < nunits; w += gridDim.x, ++i) {
+      for (int uu = blockIdx.x; uu < nunits; uu += gridDim.x, ++i) {
+        const int w = uu % per_rep;
         const int b = i & 1;
         const uint32_t u = (uint32_t)(i >> 1);
         const int kb0 = (w / ntiles) * nkc, kb1 = min(nk, kb0 + nkc);
@@ -429,7 +447,8 @@ __global__ void __launch_bounds__(NT, 1)
     const int quad = warp & 3;
     const int half = (warp - 2) >> 2;
     int i = 0;
-    for (int w = blockIdx.x; w < nunits; w += gridDim.x, ++i) {
+    for (int uu = blockIdx.x; uu < nunits; uu += gridDim.x, ++i) {
+      const int rep = uu / per_rep, w = uu - rep * per_rep;
       const int b = i & 1;
       const uint32_t u = (uint32_t)(i >> 1);
       bool ok = mbar_wait(smem_u32(&tfull[b]), u & 1u);
@@ -450,7 +469,7 @@ __global__ void __launch_bounds__(NT, 1)
       for (int c = half * (BN / 32); c < (half + 1) * (BN / 32); ++c) {
         float v[16];
         tc_ld16(lane_base + (uint32_t)(c * 16), v);
-        epi(row, (int64_t)nt * BN + c * 16, v, w / ntiles);
+        epi(row, (int64_t)nt * BN + c * 16, v, w / ntiles, rep);
       }
       tc_fence_before();
       __syncwarp();
@@ -602,21 +621,31 @@ int sm_count(int* out) {
 
 template <class TC, class Epi>
 int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K,
-                const Epi& epi, cudaStream_t st, unsigned* status, int ksplit) {
+                const Epi& epi, cudaStream_t st, unsigned* status, int ksplit, RepTC rt) {
   constexpr int BN = TC::BN, SMEM_BYTES = TC::SMEM_BYTES;
   if (!A || !B || M <= 0 || N <= 0 || K <= 0 || lda < K || ldb < K || (lda % 8) || (ldb % 8) ||
       (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16)) {
     fricc_set_error("gemm_tc: bad arguments (K-major BF16 operands: 16-byte aligned, ld >= K, ld %% 8 == 0)");
     return FRICC_ERR_ARG;
   }
+  // a replica's operand rows must not overlap the next replica's
+  if (rt.reps < 1 || (rt.a_rep != 0 && rt.a_rep < M) || (rt.b_rep != 0 && rt.b_rep < N) || rt.a_rep < 0 ||
+      rt.b_rep < 0) {
+    fricc_set_error("gemm_tc: bad replica layout");
+    return FRICC_ERR_ARG;
+  }
+  // the rows of A' and B' over all replicas (TMA coordinates are 32-bit)
+  const int64_t rows_a = rt.a_rep ? (int64_t)rt.reps * rt.a_rep : M;
+  const int64_t rows_b = rt.b_rep ? (int64_t)rt.reps * rt.b_rep : N;
   const int64_t tm = fricc_cdiv(M, BM), tn = fricc_cdiv(N, BN);
-  if (tm * tn * ksplit > 0x7fffffffLL || K > 0x7fffffffLL) {
+  if (tm * tn * ksplit * rt.reps > 0x7fffffffLL || K > 0x7fffffffLL || rows_a + BM > 0x7fffffffLL ||
+      rows_b + BN > 0x7fffffffLL) {
     fricc_set_error("gemm_tc: problem too large for one launch");
     return FRICC_ERR_ARG;
   }
   CUtensorMap ma, mb;
-  int rc = make_map(&ma, A, M, K, lda, BM);
-  if (!rc) rc = make_map(&mb, B, N, K, ldb, BN);
+  int rc = make_map(&ma, A, rows_a, K, lda, BM);
+  if (!rc) rc = make_map(&mb, B, rows_b, K, ldb, BN);
   if (rc) return rc;
   // per instantiation; threads that race here all set the same attribute
   static std::atomic<bool> attr{false};
@@ -636,13 +665,13 @@ int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t 
   }
   const int64_t nkc = fricc_cdiv(nk, ksplit);
   ksplit = (int)fricc_cdiv(nk, nkc);  // every slice non-empty
-  const int64_t units = tm * tn * ksplit;
+  const int64_t units = tm * tn * ksplit * rt.reps;
   const unsigned grid = (unsigned)(units < nsm ? units : nsm);  // persistent: one CTA per SM
   const bool prof = fricc_prof_on();
   if (status) {
     if (prof) fricc_prof_record(st, true, 0.0, 1);
-    k_gemm_tc<TC, Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, status);
-    if (prof) fricc_prof_record(st, false, 2.0 * (double)M * (double)N * (double)K, 1);
+    k_gemm_tc<TC, Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, status, rt);
+    if (prof) fricc_prof_record(st, false, 2.0 * rt.reps * (double)M * (double)N * (double)K, 1);
     fricc_note_launch();
     e = cudaGetLastError();
     return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "gemm_tc", __FILE__, __LINE__);
@@ -653,8 +682,8 @@ int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t 
   e = cudaMemsetAsync(err, 0, sizeof(unsigned), st);
   if (e == cudaSuccess) {
     if (prof) fricc_prof_record(st, true, 0.0, 1);
-    k_gemm_tc<TC, Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, err);
-    if (prof) fricc_prof_record(st, false, 2.0 * (double)M * (double)N * (double)K, 1);
+    k_gemm_tc<TC, Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, err, rt);
+    if (prof) fricc_prof_record(st, false, 2.0 * rt.reps * (double)M * (double)N * (double)K, 1);
     fricc_note_launch();
     e = cudaGetLastError();
   }
@@ -673,9 +702,9 @@ int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t 
 // tile width by the output's N: 64 when N <= 64 (nocc-wide outputs), else 256
 template <class Epi>
 int launch(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K, const Epi& epi,
-           cudaStream_t st, unsigned* status = nullptr, int ksplit = 1) {
-  if (N <= 64) return launch_tile<Tile<64>>(A, lda, B, ldb, M, N, K, epi, st, status, ksplit);
-  return launch_tile<Tile<256>>(A, lda, B, ldb, M, N, K, epi, st, status, ksplit);
+           cudaStream_t st, unsigned* status = nullptr, int ksplit = 1, RepTC rt = RepTC{}) {
+  if (N <= 64) return launch_tile<Tile<64>>(A, lda, B, ldb, M, N, K, epi, st, status, ksplit, rt);
+  return launch_tile<Tile<256>>(A, lda, B, ldb, M, N, K, epi, st, status, ksplit, rt);
 }
 
 }  // namespace tc
@@ -733,34 +762,47 @@ int fricc_split_bf16x3(const double* x, int64_t rows, int64_t k, int64_t ld, int
   return fricc_split_bf16x3_strided(x, rows, k, 1, ld, ld, 1, kp, Ap, Bp, stream);
 }
 
-int fricc_gemm_bf16_tn_strided(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N,
-                               int64_t K, double* C, int64_t mi, int64_t ni, int64_t sro, int64_t sri, int64_t sco,
-                               int64_t sci, double alpha, double beta, int ksplit, unsigned* status, void* stream) {
-  if (!C || mi <= 0 || ni <= 0 || ksplit < 1) {
-    fricc_set_error("gemm_bf16_tn_strided: bad output or split");
+int fricc_gemm_bf16_tn_strided_b(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N,
+                                 int64_t K, double* C, int64_t mi, int64_t ni, int64_t sro, int64_t sri, int64_t sco,
+                                 int64_t sci, double alpha, double beta, int ksplit, int reps, int64_t a_rep,
+                                 int64_t b_rep, int64_t c_rep, unsigned* status, void* stream) {
+  if (!C || mi <= 0 || ni <= 0 || ksplit < 1 || reps < 1 || reps > 65535 || a_rep < 0 || b_rep < 0 ||
+      a_rep > 0x7fffffffLL || b_rep > 0x7fffffffLL) {
+    fricc_set_error("gemm_bf16_tn_strided: bad output, split or replica layout");
     return FRICC_ERR_ARG;
   }
-  const tc::EpiStridedF64 out{C, M, N, mi, ni, sro, sri, sco, sci, alpha, beta};
+  const tc::EpiStridedF64 out{C, M, N, mi, ni, sro, sri, sco, sci, alpha, beta, c_rep};
+  tc::RepTC rt;
+  rt.reps = reps;
+  rt.a_rep = (int)a_rep;
+  rt.b_rep = (int)b_rep;
   cudaStream_t st = (cudaStream_t)stream;
-  if (ksplit == 1) return tc::launch(A, lda, B, ldb, M, N, K, out, st, status);
+  if (ksplit == 1) return tc::launch(A, lda, B, ldb, M, N, K, out, st, status, 1, rt);
   // split K: FP32 partials per slice, then one ordered reduction into C
   const int64_t nk = fricc_cdiv(K, tc::BK);
   if (ksplit > nk) ksplit = (int)nk;
   const int ks = (int)fricc_cdiv(nk, fricc_cdiv(nk, ksplit));
   float* P = nullptr;
-  int rc = fricc_alloc_t(&P, (size_t)ks * M * N, st);
+  int rc = fricc_alloc_t(&P, (size_t)reps * ks * M * N, st);
   if (rc) return rc;
-  rc = tc::launch(A, lda, B, ldb, M, N, K, tc::EpiPartial{P, M, N}, st, status, ks);
+  rc = tc::launch(A, lda, B, ldb, M, N, K, tc::EpiPartial{P, M, N, ks}, st, status, ks, rt);
   if (!rc) {
-    int64_t g = fricc_cdiv(M * N, 256);
+    int64_t g = fricc_cdiv(reps * M * N, 256);
     if (g > 152 * 16) g = 152 * 16;
-    tc::k_reduce_partials<<<(unsigned)g, 256, 0, st>>>(P, ks, M, N, out);
+    tc::k_reduce_partials<<<(unsigned)g, 256, 0, st>>>(P, ks, M, N, out, reps);
     fricc_note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = fricc_cuda_fail(e, "gemm_tc reduce", __FILE__, __LINE__);
   }
   fricc_free(P, st);
   return rc;
+}
+
+int fricc_gemm_bf16_tn_strided(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N,
+                               int64_t K, double* C, int64_t mi, int64_t ni, int64_t sro, int64_t sri, int64_t sco,
+                               int64_t sci, double alpha, double beta, int ksplit, unsigned* status, void* stream) {
+  return fricc_gemm_bf16_tn_strided_b(A, lda, B, ldb, M, N, K, C, mi, ni, sro, sri, sco, sci, alpha, beta, ksplit, 1,
+                                      0, 0, 0, status, stream);
 }
 
 int fricc_vvvv_rebuild_bf16x3(const void* Ap, const void* Bp, int64_t v, int64_t kp, float* W, int64_t ldw,

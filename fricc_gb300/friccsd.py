@@ -256,6 +256,16 @@ class FRICCSDGPU:
         else:
             L.check(self.lib.fricc_spmm(T, pa, pb, ka, kb, float(coef), _ptr(Wp), int(QS), _ptr(Op), stream))
 
+    def _tuned_compress(self, t2, m, launch):
+        """Run a paired compression; with the autotuner, its select-digit
+        width is timed over the candidates on first use of the shape (each
+        candidate recompresses the same T2 with the same draws, and every
+        width keeps the same entries) and the fastest replayed."""
+        if self._tuner is None:
+            return launch(None)
+        from .autotune import COMPRESS_CANDIDATES
+        self._tuner.run(("compress_pair", tuple(t2.shape), int(m)), COMPRESS_CANDIDATES, launch, [])
+
     def update_amps(self, t1, t2, rn=None, t1_old=None, t2_old=None):
         """One iteration on device tensors; returns (t1new, t2new).  With
         ``graph=True`` (and systematic or "largest" compression, no unbiased
@@ -359,12 +369,12 @@ class FRICCSDGPU:
             paired = (need_w and s["compression"] == "fri" and s["sampling_method"] == "systematic"
                       and self._sp.ready_for(t2, m) and self._sp_w.ready_for(t2, m) and ws is t2 and not verbose)
             if paired and rn_dev is not None:  # captured: draws from device memory
-                L.check(self.lib.fricc_sp_recompress_pair_dev(self._sp.h, self._sp_w.h, _ptr(t2),
-                                                              ctypes.c_void_p(rn_dev.data_ptr()), sst))
+                self._tuned_compress(t2, m, lambda _: L.check(self.lib.fricc_sp_recompress_pair_dev(
+                    self._sp.h, self._sp_w.h, _ptr(t2), ctypes.c_void_p(rn_dev.data_ptr()), sst)))
                 T, Tw = self._sp.h, self._sp_w.h
             elif paired:
-                L.check(self.lib.fricc_sp_recompress_pair(self._sp.h, self._sp_w.h, _ptr(t2), float(rn[0]),
-                                                          float(rn[1]), sst))
+                self._tuned_compress(t2, m, lambda _: L.check(self.lib.fricc_sp_recompress_pair(
+                    self._sp.h, self._sp_w.h, _ptr(t2), float(rn[0]), float(rn[1]), sst)))
                 T, Tw = self._sp.h, self._sp_w.h
             elif rn_dev is not None:  # captured: draws from device memory, handles exist
                 T = self._sp.compress_dev(t2, m, s["compression"], ctypes.c_void_p(rn_dev.data_ptr()), sst)

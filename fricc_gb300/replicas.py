@@ -89,10 +89,13 @@ def einsum_rep(spec: str, A: torch.Tensor, B: torch.Tensor, gemm, za: bool, zb: 
 class FusedReplicaBatch:
     """R replicas of one system, one launch per kernel for all of them.
 
-    ``precision`` "fp64" or "df64"; systematic FRI with every contraction
-    class compressed (the configuration of the batched-replica workload);
-    replica r draws from GlibcRand(seeds[r]), in the reference's order (the
-    T2-term compression first, then the W-intermediate one)."""
+    ``precision`` "fp64", "df64" or "split" (the integrals of
+    fricc_gb300.cholesky.split_eris; every sparse term a dense split-BF16x3
+    GEMM on the tensor cores, as FRICCSDGPU(precision="split") runs it with
+    its defaults); systematic FRI with every contraction class compressed
+    (the configuration of the batched-replica workload); replica r draws
+    from GlibcRand(seeds[r]), in the reference's order (the T2-term
+    compression first, then the W-intermediate one)."""
 
     def __init__(self, eris: D.DeviceERIs, settings: dict, seeds, precision: str = "df64", level_shift: float = 0.0):
         s = {"compression": "fri", "sampling_method": "systematic", "compressed_contractions": ALL_TERMS,
@@ -101,16 +104,34 @@ class FusedReplicaBatch:
         if s["compression"] != "fri" or s["sampling_method"] != "systematic" or s.get("unbiased", False) or \
                 sorted(s["compressed_contractions"]) != sorted(ALL_TERMS):
             raise ValueError("FusedReplicaBatch runs systematic FRI with every contraction class compressed")
-        if precision not in ("fp64", "df64"):
-            raise ValueError("FusedReplicaBatch: precision 'fp64' or 'df64'")
-        if eris.vvvvT is None:
-            raise ValueError("FusedReplicaBatch needs the FP64 (vv|vv) block")
+        if precision not in ("fp64", "df64", "split"):
+            raise ValueError("FusedReplicaBatch: precision 'fp64', 'df64' or 'split'")
+        self.split = precision == "split"
+        if self.split and getattr(eris, "vvvv_rebuild", None) is None:
+            raise ValueError("precision 'split' needs the integrals of fricc_gb300.cholesky.split_eris")
+        if not self.split and eris.vvvvT is None:
+            raise ValueError("FusedReplicaBatch needs the FP64 (vv|vv) block (or precision 'split')")
         from .batch import mp2_device
         self.E = eris
         self.precision = precision
         self.df = precision == "df64"
         if self.df:
             eris.prepare_splits()
+        if self.split:
+            from .cholesky import dense_spmm_ok
+            o_, v_ = eris.nocc, eris.mo_energy.numel() - eris.nocc
+            ovv, ov = o_ * v_ * v_, o_ * v_
+            dims = (o_, o_, v_, v_)
+            terms = [(0, 1, 2, 3, o_ * o_), (3, 0, 1, 2, ov), (2, 0, 1, 3, ov), (2, 3, 0, 1, o_ * o_),
+                     (0, 1, 2, 3, v_ * v_), (0, 1, 2, 3, 2 * ov), (1, 3, 0, 2, ov), (1, 2, 0, 3, ov)]
+            if not all(dense_spmm_ok(dims, *t) for t in terms):
+                raise ValueError("FusedReplicaBatch 'split': a sparse term of this size is too small for the "
+                                 "tensor cores (run FRICCSDGPU or ReplicaBatch)")
+            eris.prepare_tc({"ovvv_iabc": ("A", ovv, v_), "ovvv": ("A", ovv, v_), "ovvv_kacd": ("A", ovv, v_),
+                             "g_klcd": ("A", o_, ovv), "g_kldc": ("B", o_ * o_ * v_, v_),
+                             "G_t1": ("B", ovv, v_)})
+            self._tc_status = torch.zeros(1, dtype=torch.int32, device=eris.device)
+            self._vvvv_bt = None
         self.seeds = list(seeds)
         self.R = R = len(self.seeds)
         self.rng = [GlibcRand(sd) for sd in self.seeds]
@@ -144,7 +165,15 @@ class FusedReplicaBatch:
             self.spb = None
 
     # ------------------------------------------------------------------
-    def _mm(self, A, B, C, alpha=1.0, beta=0.0):
+    def _mm(self, A, B, C, alpha=1.0, beta=0.0, const=None, const_b=None):
+        """The precision's GEMM for every replica; ``const`` / ``const_b``
+        name a constant integral operand whose tensor-core split is kept."""
+        if self.split:
+            from .cholesky import gemm_tc_rep
+            E = self.E
+            return gemm_tc_rep(A, B, C, alpha, beta, self.R, status=self._tc_status,
+                               a_split=E.tc(const, "A") if const else None,
+                               b_split=E.tc(const_b, "B") if const_b else None)
         return (D.gemm_df if self.df else D.gemm_f64)(A, B, C, alpha, beta)
 
     def _spmm(self, which, pa, pb, ka, kb, coef, W, QS, Op, st, const=None):
@@ -152,7 +181,16 @@ class FusedReplicaBatch:
         constant integral block) or stacked [R, ...]; Op stacked."""
         R = self.R
         o_stride = Op[0].numel()
-        if self.df:
+        if self.split:
+            from .cholesky import dense_spmm_rep, split_b_rep
+            if const is not None:
+                Bt, b_rep = self.E.tc_w(const, QS), 0
+            else:
+                Bt, b_rep = split_b_rep(W, R, QS), QS
+            done = dense_spmm_rep(self.spb, which, R, tuple(self.t2.shape[1:]), pa, pb, ka, kb, coef, Bt, b_rep, QS,
+                                  Op, self._tc_status)
+            assert done, "checked at construction"
+        elif self.df:
             if const is not None:
                 W2, w_stride = self.E.split(const), 0
             else:
@@ -179,6 +217,10 @@ class FusedReplicaBatch:
         rc = self.lib.fricc_spb_status(self.spb, ctypes.byref(rep))
         if rc:
             L.check(rc)
+        if self.split:
+            self.E.vvvv_rebuild.check()
+            if int(self._tc_status.item()):
+                raise L.FriccError(5, "split-precision GEMM: a bounded tensor-core pipeline wait gave up")
         if record:
             for k in range(self.R):
                 self.history[k].append(float(r[k, 0]))
@@ -234,10 +276,10 @@ class FusedReplicaBatch:
              prod=[t1[:, :, None, :, None], t1[:, None, :, None, :]])
         Foo0 = new(R, o, o)
         comb([Foo0], [C["foo"]])
-        mm(E.g_klcd.view(o, ovv), tt.view(R, o, ovv).transpose(1, 2), Foo0, 1.0, 1.0)
+        mm(E.g_klcd.view(o, ovv), tt.view(R, o, ovv).transpose(1, 2), Foo0, 1.0, 1.0, const="g_klcd")
         Fvv0 = new(R, v, v)
         comb([Fvv0], [C["fvv"]])
-        mm(ttp.view(R, v, oov), E.g_kldc.view(oov, v), Fvv0, -1.0, 1.0)
+        mm(ttp.view(R, v, oov), E.g_kldc.view(oov, v), Fvv0, -1.0, 1.0, const_b="g_kldc")
         del tt, ttp
         Fov = new(R, o, v)
         comb([Fov], [fov])
@@ -264,7 +306,7 @@ class FusedReplicaBatch:
         mmf(B_ik, t1, t1new, 1.0, 1.0)
         comb([t1new], [fov], accumulate=True)
         mmf(t1.reshape(R, 1, ov), E.G_t1_kcia.view(ov, ov), t1new.view(R, 1, ov), 1.0, 1.0)
-        mm(t2.view(R, o, ovv), E.G_t1.view(ovv, v), t1new, 1.0, 1.0)
+        mm(t2.view(R, o, ovv), E.G_t1.view(ovv, v), t1new, 1.0, 1.0, const_b="G_t1")
         X = new(R, v, v)
         mmf(t1.reshape(R, 1, ov), E.G_t1_kdca.view(ov, v * v), X.view(R, 1, v * v))
         mmf(t1, X, t1new, 1.0, 1.0)
@@ -276,7 +318,7 @@ class FusedReplicaBatch:
         # T2 driver terms (:179-187)
         Y1 = ein("kibc,jc->kibj", E.oovv, t1, False, True)
         Rr = new(R, ovv, o)
-        mm(E.ovvv_iabc.view(ovv, v), t1.transpose(1, 2), Rr, 1.0, 0.0)
+        mm(E.ovvv_iabc.view(ovv, v), t1.transpose(1, 2), Rr, 1.0, 0.0, const="ovvv_iabc")
         tmp = new(R, o, o, v, v)
         comb([tmp], [Rr.view(R, o, v, v, o).permute(0, 1, 4, 2, 3), ein("ka,kibj->ijab", t1, Y1, True, True)],
              [[1.0, -1.0]])
@@ -313,7 +355,7 @@ class FusedReplicaBatch:
 
         # sparse_cc_Wvoov / sparse_cc_Wvovo (:334-376)
         Rr = new(R, ovv, o)
-        mm(E.ovvv.view(ovv, v), t1.transpose(1, 2), Rr, 1.0, 0.0)
+        mm(E.ovvv.view(ovv, v), t1.transpose(1, 2), Rr, 1.0, 0.0, const="ovvv")
         Wp = new(R, v, o, o, v)                                                   # [a,i,k,c]
         Wvoov = Wp.permute(0, 1, 3, 2, 4)                                         # (a,k,i,c)
         comb([Wvoov], [Rr.view(R, o, v, v, o).permute(0, 3, 1, 4, 2), ein("kcli,la->akic", E.ovoo, t1, False, True),
@@ -322,7 +364,7 @@ class FusedReplicaBatch:
         self._spmm(1, 2, 0, 1, 3, 1.0, E.ovov_0313_0113, ov, Wp, st, const="ovov_0313_0113")     # 0313+0113
         comb([Wvoov], [ein("lkci,la->akic", ein("ldkc,id->lkci", E.ovov, t1, False, True), t1, True, True)],
              [[-1.0]], accumulate=True)
-        mm(E.ovvv_kacd.view(ovv, v), t1.transpose(1, 2), Rr, 1.0, 0.0)
+        mm(E.ovvv_kacd.view(ovv, v), t1.transpose(1, 2), Rr, 1.0, 0.0, const="ovvv_kacd")
         Wq = new(R, v, o, o, v)                                                   # [a,i,k,c]
         Wvovo = Wq.permute(0, 1, 3, 4, 2)                                         # (a,k,c,i)
         comb([Wvovo], [Rr.view(R, o, v, v, o).permute(0, 2, 1, 3, 4), ein("lcki,la->akci", E.ovoo, t1, False, True),
@@ -350,7 +392,13 @@ class FusedReplicaBatch:
         mmf(t1.transpose(1, 2), E.U, S, -1.0, 1.0)
         comb([t2new], [], [[1.0]], prod=[S[:, None, None, :, :], t1[:, :, None, :, None], t1[:, None, :, None, :]],
              accumulate=True)
-        self._spmm(0, 0, 1, 2, 3, 1.0, E.vvvvT, v * v, t2new, st, const="vvvvT")             # 2323
+        if self.split:   # (ac|bd) rebuilt from the split factor straight into the B operand
+            from .cholesky import dense_spmm_rep
+            self._vvvv_bt = E.vvvv_rebuild.rebuild_split_b(self._vvvv_bt)
+            dense_spmm_rep(self.spb, 0, R, (o, o, v, v), 0, 1, 2, 3, 1.0, self._vvvv_bt, 0, v * v, t2new,
+                           self._tc_status)                                       # 2323
+        else:
+            self._spmm(0, 0, 1, 2, 3, 1.0, E.vvvvT, v * v, t2new, st, const="vvvvT")             # 2323
         XY = D.zero(new(R, o, o, 2, o, v))
         self._spmm(0, 0, 1, 2, 3, 1.0, E.ovvv_XY, 2 * ov, XY, st, const="ovvv_XY")           # t1 parts
         XYv = XY.view(R, o * o, 2, o, v)

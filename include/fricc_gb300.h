@@ -315,6 +315,19 @@ int fricc_spb_spmm(fricc_spbatch* B, int which, int pa, int pb, int ka, int kb, 
                    int64_t w_stride, int64_t QS, double* Op, int64_t o_stride, void* stream);
 int fricc_spb_spmm_f2(fricc_spbatch* B, int which, int pa, int pb, int ka, int kb, double coef, const void* W2,
                       int64_t w2_stride, int64_t QS, double* Op, int64_t o_stride, void* stream);
+/* fricc_densify_bf16x3 for every replica of a batch: replica r's
+ * compression `which` into rows [r nP, (r+1) nP) of A' ([R][nP][kp], zeroed
+ * here).  Stream-ordered. */
+int fricc_spb_densify_bf16x3(fricc_spbatch* B, int which, int pa, int pb, int ka, int kb, double coef, void* Ap,
+                             int64_t kp, void* stream);
+/* fricc_gemm_bf16_tn_strided for `reps` replicas of one shape in one launch:
+ * replica r reads A' from row r a_rep (a_rep = 0: one A' for all replicas;
+ * else a_rep >= M), B' from row r b_rep (likewise) and writes C + r c_rep.
+ * Each replica's tiles, K split and sums are those of its single call. */
+int fricc_gemm_bf16_tn_strided_b(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N,
+                                 int64_t K, double* C, int64_t mi, int64_t ni, int64_t sro, int64_t sri, int64_t sco,
+                                 int64_t sci, double alpha, double beta, int ksplit, int reps, int64_t a_rep,
+                                 int64_t b_rep, int64_t c_rep, unsigned* status, void* stream);
 /* fricc_symadd for R replicas: out [R][o][o][v][v] (C order), X with
  * strides {replica, i, j, a, b}. */
 int fricc_symadd_b(double* out, const double* X, int64_t R, int64_t nocc, int64_t nvir, const int64_t strides[5],
@@ -466,14 +479,18 @@ int fricc_stream_destroy(void* stream);
  * counterpart), thread-local; value -1 restores the built-in choice.
  * knob 0: output pairs per thread of the float-pair sparse kernel (1, 2, 4);
  * knob 1: tile of the FP32-pair GEMM (0 = 64x64, 1 = 128x32, 2 = 32x128,
- * 3 = 32x160; the FP64 GEMM's candidate set too); knob 2: CTAs per SM the
+ * 3 = 32x160, 4 = 32x32; the FP64 GEMM's candidate set too); knob 2: CTAs per SM the
  * FP32-pair and FP64 GEMMs' split K aims for (1..16); knob 3 (a test of the
  * error path, 1..2^20): in every later compression on this thread, one
  * tile of the candidate compaction first polls a device word that nothing
  * sets, gives up after that many polls and reports FRICC_ERR_TIMEOUT
  * through the compression's status (its results stay valid: the
- * compaction then runs as usual).  No knob changes a result's arithmetic
- * except the GEMMs' tile and split, which reorder their sums. */
+ * compaction then runs as usual); knob 4: the width in bits (10..13,
+ * default 12) of a compression's first select digit -- how many candidates
+ * the exact sort of the top-m selection (argsort / get_d_largest,
+ * src/fri_utils.cpp:11-36,400-437) takes; every width keeps the same
+ * entries.  No knob changes a result's arithmetic except the GEMMs' tile
+ * and split, which reorder their sums. */
 int fricc_tune_set(int knob, int value);
 
 /* Instrumentation (no reference counterpart): the number of kernels this

@@ -58,7 +58,8 @@ class _Ctx:
 
 def test_candidate_sets():
     assert {tuple(c.items()) for c in AT.SPMM_CANDIDATES} == {((0, 1),), ((0, 2),), ((0, 4),)}
-    assert AT.GEMM_CANDIDATES[0] == {} and len(AT.GEMM_CANDIDATES) == 13
+    assert AT.GEMM_CANDIDATES[0] == {} and len(AT.GEMM_CANDIDATES) == 16
+    assert [c[AT.SELECT_BITS] for c in AT.COMPRESS_CANDIDATES] == [10, 11, 12, 13]
 
 
 def test_tune_set_checks_arguments():
@@ -66,10 +67,12 @@ def test_tune_set_checks_arguments():
     lib = L.load()
     assert lib.fricc_tune_set(0, 4) == 0 and lib.fricc_tune_set(0, -1) == 0
     assert lib.fricc_tune_set(0, 3) == 1   # pairs per thread: 1, 2 or 4
-    assert lib.fricc_tune_set(1, 4) == 1   # four tiles, 0..3
+    assert lib.fricc_tune_set(1, 5) == 1   # five tiles, 0..4
     assert lib.fricc_tune_set(2, 17) == 1  # cover 1..16
     assert lib.fricc_tune_set(3, 0) == 1   # the test-only wait: 1..2^20 polls
     assert lib.fricc_tune_set(3, 1 << 21) == 1
     assert lib.fricc_tune_set(3, 5) == 0 and lib.fricc_tune_set(3, -1) == 0
-    assert lib.fricc_tune_set(4, 1) == 1   # no such knob
-    assert lib.fricc_tune_set(1, 3) == 0 and lib.fricc_tune_set(1, -1) == 0
+    assert lib.fricc_tune_set(4, 9) == 1 and lib.fricc_tune_set(4, 14) == 1   # select digit: 10..13 bits
+    assert lib.fricc_tune_set(4, 13) == 0 and lib.fricc_tune_set(4, -1) == 0
+    assert lib.fricc_tune_set(5, 1) == 1   # no such knob
+    assert lib.fricc_tune_set(1, 4) == 0 and lib.fricc_tune_set(1, -1) == 0

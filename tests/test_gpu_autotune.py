@@ -1,6 +1,8 @@
 """Autotuned launch configurations: the sparse kernel's output pairs per
-thread change no result bit; a tuned df64 iteration agrees with the
-untuned one to rounding (the GEMM tile and split order its sums)."""
+thread and the compression's select-digit width change no result bit; a
+tuned df64 iteration (GEMM tiles and splits, sparse kernel, compression
+schedule) agrees with the untuned one to rounding (the GEMM tile and split
+order its sums)."""
 import ctypes
 
 import numpy as np
@@ -34,6 +36,50 @@ def test_spmm_ppt_knob_bit_identical(gpulib):
     assert torch.equal(outs[0], outs[1]) and torch.equal(outs[1], outs[2])
 
 
+@pytest.mark.parametrize("shape,m", [((8, 8, 40, 40), 20000), ((12, 12, 50, 50), 90000)])
+def test_select_digit_width_keeps_the_same_entries(gpulib, oracle, shape, m):
+    """The top-m selection schedule (the first select digit's width, 10-13
+    bits) changes how many candidates the exact sort takes, never the
+    compression: single and batched compressions at every width keep the
+    oracle's entries bit for bit."""
+    from fricc_gb300 import _lib as L
+    from fricc_gb300.friccsd import _Handle
+    rng = np.random.default_rng(5)
+    x_h = rng.standard_normal((2,) + shape) * rng.random((2,) + shape) ** 4
+    x = torch.from_numpy(x_h).cuda()
+    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    refs = [[oracle.SparseTensor4d(x_h[r], shape, m, "fri", "systematic", rn=rn) for rn in (0.3, 0.7)]
+            for r in range(2)]
+    rn = torch.tensor([[0.3, 0.7], [0.3, 0.7]], dtype=torch.float64, device="cuda")
+    spb = ctypes.c_void_p()
+    L.check(gpulib.fricc_spb_create(2, L.i64arr(shape), m, st, ctypes.byref(spb)))
+    flat = np.empty(m, dtype=np.int64)
+    vals = np.empty(m, dtype=np.float64)
+    try:
+        for bits in (10, 11, 12, 13):
+            L.check(gpulib.fricc_tune_set(4, bits))
+            h = _Handle()
+            h.compress(x[0], m, "fri", 0.3, st)
+            L.check(gpulib.fricc_sp_status(h.h))
+            L.check(gpulib.fricc_sp_export(h.h, ctypes.c_void_p(flat.ctypes.data), ctypes.c_void_p(vals.ctypes.data),
+                                           st))
+            assert np.array_equal(flat, refs[0][0].flat), bits
+            assert np.array_equal(vals.view(np.int64), refs[0][0].vals.view(np.int64)), bits
+            h.free()
+            L.check(gpulib.fricc_spb_recompress_pair(spb, ctypes.c_void_p(x.data_ptr()), ctypes.c_void_p(rn.data_ptr()),
+                                                     st))
+            L.check(gpulib.fricc_spb_status(spb, None))
+            for r in range(2):
+                for which in (0, 1):
+                    L.check(gpulib.fricc_spb_export(spb, which, r, ctypes.c_void_p(flat.ctypes.data),
+                                                    ctypes.c_void_p(vals.ctypes.data), st))
+                    assert np.array_equal(flat, refs[r][which].flat), (bits, r, which)
+                    assert np.array_equal(vals.view(np.int64), refs[r][which].vals.view(np.int64)), (bits, r, which)
+    finally:
+        L.check(gpulib.fricc_tune_set(4, -1))
+        gpulib.fricc_spb_destroy(spb)
+
+
 def test_autotuned_iteration_matches(gpulib):
     from fricc_gb300.friccsd import FRICCSDGPU
     from fricc_gb300.rccsd_dense import DeviceERIs
@@ -51,6 +97,7 @@ def test_autotuned_iteration_matches(gpulib):
         torch.testing.assert_close(a2, b2, rtol=1e-12, atol=1e-16)
         t1, t2 = a1, a2
     assert a._tuner.best and a._tuner.tuning_s > 0
+    assert any(k[0] == "compress_pair" for k in a._tuner.best)
     # replays are deterministic
     c1, c2 = a.update_amps(t1, t2, rn=[0.5, 0.5])
     d1, d2 = a.update_amps(t1, t2, rn=[0.5, 0.5])

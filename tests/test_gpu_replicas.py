@@ -3,7 +3,8 @@ once for all of them (fricc_gb300.replicas.FusedReplicaBatch).
 
 * Each replica's trajectory -- E_corr every iteration, t1 and t2 after
   several -- is bit for bit the one a lone FRICCSDGPU solve with the same
-  seed and precision gives (FP64 and FP32-pair forms).
+  seed and precision gives (FP64, FP32-pair and split-BF16x3 forms; the
+  replica-batched tensor-core GEMM also against gemm_tc per replica).
 * Both batched compressions of every replica keep the lone solve's entries
   bit for bit (o20v100, m = 200,000, 16 replicas).
 * A bounded device wait that runs out inside the batched compression is
@@ -120,3 +121,75 @@ def test_batched_compression_wait_runs_out_and_recovers(gpulib, oracle):
                 assert np.array_equal(vals.view(np.int64), ref.vals.view(np.int64)), (r, which)
     finally:
         gpulib.fricc_spb_destroy(spb)
+
+
+@pytest.mark.parametrize("case", ["shared_a", "batched_a", "swap", "split_k", "pair_fallback"])
+def test_gemm_tc_rep_equals_gemm_tc_per_replica(gpulib, case):
+    """The replica-batched tensor-core GEMM against gemm_tc called replica by
+    replica: bit for bit, through each of its routes (a constant split A,
+    batch-flattened rows, the narrow-side swap, split K with per-replica
+    partials, and the FP32-pair fallback)."""
+    from fricc_gb300.cholesky import gemm_tc, gemm_tc_rep, split_a
+    g = torch.Generator(device="cuda").manual_seed(3)
+    R = 3
+
+    def rnd(*shape):
+        return torch.randn(*shape, generator=g, device="cuda", dtype=torch.float64)
+    a_split = None
+    if case == "shared_a":        # R = ovvv . t1^T: a constant A, per-replica B (a transposed view)
+        A, B, C0 = rnd(8000, 100), rnd(R, 20, 100).transpose(1, 2), rnd(R, 8000, 20)
+        a_split = split_a(A)
+        lone = lambda r, C: gemm_tc(A, B[r], C, -1.0, 1.0, a_split=a_split)  # noqa: E731
+        alpha, beta = -1.0, 1.0
+    elif case == "batched_a":     # the X t1 term: a batched A, B one per replica (batch stride 0)
+        A = rnd(R, 100, 20, 100).transpose(2, 3)
+        B = rnd(R, 1, 20, 100).expand(R, 100, 20, 100)
+        C0 = rnd(R, 100, 100, 100)
+        lone = lambda r, C: gemm_tc(A[r], B[r], C, -1.0, 1.0)  # noqa: E731
+        alpha, beta = -1.0, 1.0
+    elif case == "swap":          # Loo t2: M = 20 <= 64 < N
+        A, B, C0 = rnd(R, 20, 20).transpose(1, 2), rnd(R, 20, 40000), rnd(R, 20, 40000)
+        lone = lambda r, C: gemm_tc(A[r], B[r], C, 1.0, 0.0)  # noqa: E731
+        alpha, beta = 1.0, 0.0
+    elif case == "split_k":       # cc_Foo: one 20 x 20 tile, K = 20,000
+        A, B, C0 = rnd(20, 20000), rnd(R, 20, 20000).transpose(1, 2), rnd(R, 20, 20)
+        a_split = split_a(A)
+        lone = lambda r, C: gemm_tc(A, B[r], C, 1.0, 1.0, a_split=a_split)  # noqa: E731
+        alpha, beta = 1.0, 1.0
+    else:                         # few tiles, short K: the FP32-pair GEMM
+        A, B, C0 = rnd(R, 20, 30), rnd(30, 20), rnd(R, 20, 20)
+        lone = lambda r, C: gemm_tc(A[r], B, C, 1.0, 0.0)  # noqa: E731
+        alpha, beta = 1.0, 0.0
+    want = C0.clone()
+    for r in range(R):
+        lone(r, want[r])
+    got = C0.clone()
+    gemm_tc_rep(A, B, got, alpha, beta, R, a_split=a_split)
+    torch.cuda.synchronize()
+    assert torch.equal(_bits(got), _bits(want))
+    assert not torch.equal(got, C0)
+
+
+def test_fused_split_replicas_equal_their_lone_solves(gpulib):
+    from fricc_gb300.cholesky import split_eris
+    from fricc_gb300.replicas import FusedReplicaBatch
+    from fricc_gb300.synthetic import SyntheticSystem
+    E = split_eris(SyntheticSystem(10, 80, 400, 0.05, 3))
+    m, seeds, steps = 32000, [7, 11, 12345], 2
+    fb = FusedReplicaBatch(E, {"m_keep": m}, seeds, precision="split")
+    for _ in range(steps):
+        fb.step()
+    for r, seed in enumerate(seeds):
+        _, t1, t2, energies = _lone(E, m, seed, "split", steps)
+        assert energies == fb.history[r], (r, energies, fb.history[r])
+        assert torch.equal(_bits(t1), _bits(fb.t1[r])), r
+        assert torch.equal(_bits(t2), _bits(fb.t2[r])), r
+
+
+def test_fused_split_declines_terms_too_small_for_the_tensor_cores(gpulib):
+    from fricc_gb300.cholesky import split_eris
+    from fricc_gb300.replicas import FusedReplicaBatch
+    from fricc_gb300.synthetic import SyntheticSystem
+    E = split_eris(SyntheticSystem(6, 24, 120, 0.05, 3))
+    with pytest.raises(ValueError):
+        FusedReplicaBatch(E, {"m_keep": 3000}, [1, 2], precision="split")
