@@ -66,8 +66,14 @@ struct CombineArgs {
   double* out[kMaxOut];
   int64_t so[kMaxOut][D];
   double c[kMaxOut][kMaxIn + 1];
+  // each coefficient's kind, decided on the host: 0 (the term is left out),
+  // 1 (+x), -1 (-x), 2 (c x).  GB300's FP64 unit is slow enough that
+  // comparing the coefficients per element in FP64 bounded these passes.
+  signed char cc[kMaxOut][kMaxIn + 1];
   int acc[kMaxOut];  // per output: add to its current value (1) or overwrite it (0)
 };
+
+inline signed char coef_kind(double c) { return c == 0.0 ? 0 : (c == 1.0 ? 1 : (c == -1.0 ? -1 : 2)); }
 
 template <typename I>
 __device__ __forceinline__ I off5(const int64_t s[D], I i0, I i1, I i2, I i3, I i4) {
@@ -85,16 +91,16 @@ __device__ __forceinline__ void finish(const CombineArgs& a, const double* xv, d
     bool first = true;
 #pragma unroll
     for (int s = 0; s < NIN; ++s) {
-      const double c = a.c[k][s];
-      if (c != 0.0) {
-        const double term = c == 1.0 ? xv[s] : (c == -1.0 ? -xv[s] : c * xv[s]);
+      const int kind = a.cc[k][s];
+      if (kind != 0) {
+        const double term = kind == 1 ? xv[s] : (kind == -1 ? -xv[s] : a.c[k][s] * xv[s]);
         acc = first ? term : acc + term;
         first = false;
       }
     }
-    if (NPROD > 0 && a.c[k][NIN] != 0.0) {
-      const double c = a.c[k][NIN];
-      const double term = c == 1.0 ? pv : (c == -1.0 ? -pv : c * pv);
+    if (NPROD > 0 && a.cc[k][NIN] != 0) {
+      const int kind = a.cc[k][NIN];
+      const double term = kind == 1 ? pv : (kind == -1 ? -pv : a.c[k][NIN] * pv);
       acc = first ? term : acc + term;
     }
     *o[k] = a.acc[k] ? old[k] + acc : acc;
@@ -176,12 +182,23 @@ template <int NIN, int NOUT, typename I>
 __global__ void __launch_bounds__(256) k_combine_t(const CombineArgs a, const TileArgs ta) {
   extern __shared__ double sm[];  // [NIN][32][33]
   const int x = threadIdx.x & 31, y = threadIdx.x >> 5;
-  const I t4 = (I)(blockIdx.x % ta.nt4), t3 = (I)(blockIdx.x / ta.nt4);
+  const unsigned nt4 = (unsigned)ta.nt4;  // tiles along 4: a few (32-bit division)
+  const I t4 = (I)(blockIdx.x % nt4), t3 = (I)(blockIdx.x / nt4);
   const I d3 = (I)a.d[3], d4 = (I)a.d[4];
   for (int64_t rest = blockIdx.y; rest < ta.nrest; rest += gridDim.y) {
-    const I i2 = (I)(rest % a.d[2]);
-    const int64_t r01 = rest / a.d[2];
-    const I i1 = (I)(r01 % a.d[1]), i0 = (I)(r01 / a.d[1]);
+    I i0, i1, i2;
+    if constexpr (sizeof(I) == 4) {  // multiply-high divisions (every index < 2^31)
+      const unsigned rr = (unsigned)rest;
+      const unsigned q2 = a.f2.div(rr);
+      i2 = rr - q2 * (unsigned)a.d[2];
+      i0 = a.f1.div(q2);
+      i1 = q2 - i0 * (unsigned)a.d[1];
+    } else {
+      i2 = (I)(rest % a.d[2]);
+      const int64_t r01 = rest / a.d[2];
+      i1 = (I)(r01 % a.d[1]);
+      i0 = (I)(r01 / a.d[1]);
+    }
     __syncthreads();  // the previous tile's reads of shared memory are done
     double v[NIN][4];
 #pragma unroll
@@ -368,6 +385,21 @@ int fricc_combine_device(const int64_t dims[5], int n_in, const double* const* x
       for (int d = 0; d < 4; ++d)
         if (d != gsel) order[nr++] = d;
       order[3] = gsel;
+      // the three remaining dimensions, walked by consecutive tiles, in the
+      // first input's memory order (its smallest stride fastest; a
+      // broadcast dimension, stride 0, slowest), so that tiles running at
+      // once read neighbouring memory
+      const int64_t* s0 = sx + D * members[0];
+      auto key = [&](int d) { return s0[d] == 0 ? INT64_MAX : (s0[d] < 0 ? -s0[d] : s0[d]); };
+      for (int a = 0; a < 2; ++a)
+        for (int b = 0; b < 2 - a; ++b) {
+          const int64_t sa = key(order[b]), sb = key(order[b + 1]);
+          if (sa < sb) {
+            const int t = order[b];
+            order[b] = order[b + 1];
+            order[b + 1] = t;
+          }
+        }
     }
     for (int d = 0; d < D; ++d) a.d[d] = dims[order[d]];
     a.n = n;
@@ -384,8 +416,14 @@ int fricc_combine_device(const int64_t dims[5], int n_in, const double* const* x
       const int k = outs[q];
       a.out[q] = out[k];
       for (int d = 0; d < D; ++d) a.so[q][d] = so[D * k + order[d]];
-      for (int j = 0; j < nm; ++j) a.c[q][j] = coef[k * nc + members[j]];
-      if (with_prod) a.c[q][nm] = coef[k * nc + n_in];
+      for (int j = 0; j < nm; ++j) {
+        a.c[q][j] = coef[k * nc + members[j]];
+        a.cc[q][j] = coef_kind(a.c[q][j]);
+      }
+      if (with_prod) {
+        a.c[q][nm] = coef[k * nc + n_in];
+        a.cc[q][nm] = coef_kind(a.c[q][nm]);
+      }
       a.acc[q] = touched[k] ? 1 : 0;
       touched[k] = true;
     }

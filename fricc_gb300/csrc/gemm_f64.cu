@@ -28,6 +28,10 @@ struct GemmArgs {
   // a second batch level (replicas): batch index bz = b2 * nb1 + b
   int64_t nb1, sAb2, sBb2, sCb2;
   double alpha, beta;
+  // the epilogue's case, from alpha and beta on the host (GB300's FP64 unit
+  // is too slow for per-output FP64 comparisons): 0 C = acc, 1 C = -acc,
+  // 2 C = alpha acc, 3 C += acc, 4 C -= acc, 5 C = alpha acc + beta C
+  int emode;
   int splits;
   int64_t ntn;     // N tiles: blockIdx.x = split * ntn + N tile
   int64_t kchunk;  // K per split (multiple of BK)
@@ -46,10 +50,14 @@ __device__ __forceinline__ int64_t boffC(const GemmArgs& g, int64_t bz) {
 __device__ __forceinline__ void store_out(const GemmArgs& g, int64_t bz, int sp, int64_t m, int64_t n, double acc) {
   if (g.splits == 1) {
     double* cp = g.C + boffC(g, bz) + m * g.sCm + n * g.sCn;
-    if (g.beta == 0.0) *cp = g.alpha == 1.0 ? acc : (g.alpha == -1.0 ? -acc : g.alpha * acc);
-    else if (g.beta == 1.0 && g.alpha == 1.0) *cp = *cp + acc;
-    else if (g.beta == 1.0 && g.alpha == -1.0) *cp = *cp - acc;
-    else *cp = fma(g.alpha, acc, g.beta * *cp);
+    switch (g.emode) {
+      case 0: *cp = acc; break;
+      case 1: *cp = -acc; break;
+      case 2: *cp = g.alpha * acc; break;
+      case 3: *cp = *cp + acc; break;
+      case 4: *cp = *cp - acc; break;
+      default: *cp = fma(g.alpha, acc, g.beta * *cp);
+    }
   } else {
     g.part[((bz * g.splits + sp) * g.M + m) * g.N + n] = acc;
   }
@@ -163,7 +171,7 @@ __global__ void k_gemm_f64_reduce(GemmArgs g, int64_t batch) {
     double acc = 0.0;
     for (int s = 0; s < g.splits; ++s) acc += g.part[(b * g.splits + s) * MN + r];
     double* c = g.C + boffC(g, b) + m * g.sCm + n * g.sCn;
-    *c = g.beta == 0.0 ? g.alpha * acc : fma(g.alpha, acc, g.beta * *c);
+    *c = g.emode <= 2 ? g.alpha * acc : fma(g.alpha, acc, g.beta * *c);
   }
 }
 
@@ -227,6 +235,8 @@ int fricc_gemm_f64_device(const double* A, const double* B, double* C, int64_t b
   g.sCm = sC[0]; g.sCn = sC[1]; g.sCb = sC[2];
   g.alpha = alpha;
   g.beta = beta;
+  g.emode = beta == 0.0 ? (alpha == 1.0 ? 0 : (alpha == -1.0 ? 1 : 2))
+                        : (beta == 1.0 && alpha == 1.0 ? 3 : (beta == 1.0 && alpha == -1.0 ? 4 : 5));
   // a second batch level: batch2 groups of `batch` products, group strides
   // s2 = {A, B, C}; from here on `batch` counts every product
   if (batch2 < 1 || batch2 > 65535) {

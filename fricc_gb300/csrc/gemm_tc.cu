@@ -199,6 +199,7 @@ struct EpiStridedF64 {
   int64_t M, N, mi, ni, sro, sri, sco, sci;
   double alpha, beta;
   int64_t srep;  // C offset of replica r: r * srep
+  int beta0;     // beta == 0 (decided on the host: no per-element FP64 compare)
   __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v, int, int rep) const {
     if (r >= M) return;
     const int64_t ro = r / mi;
@@ -209,7 +210,7 @@ struct EpiStridedF64 {
       if (c0 + i < N) {
         double* p = C + rbase + co * sco + ci * sci;
         const double x = alpha * f2d_bits(v[i]);
-        *p = beta == 0.0 ? x : x + beta * *p;
+        *p = beta0 ? x : x + beta * *p;
       }
       if (++ci == ni) {
         ci = 0;
@@ -219,35 +220,74 @@ struct EpiStridedF64 {
   }
 };
 
-// split K: slice s of replica rep's sum into the FP32 partial P[rep][s][M][N]
+// split K: slice s of replica rep's sum into the FP32 partial
+// P[rep][s][N][M], column-major, so that a warp's 32 lanes (32 consecutive
+// rows) store 128 contiguous bytes per column
 struct EpiPartial {
   float* P;
   int64_t M, N;
   int ks;
   __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v, int s, int rep) const {
     if (r >= M) return;
-    float* p = P + (((int64_t)rep * ks + s) * M + r) * N + c0;
+    float* p = P + (((int64_t)rep * ks + s) * N + c0) * M + r;
 #pragma unroll
     for (int i = 0; i < 16; ++i)
-      if (c0 + i < N) p[i] = v[i];
+      if (c0 + i < N) p[(int64_t)i * M] = v[i];
   }
 };
 
 // C (the EpiStridedF64 mapping) = alpha sum_s P[s] + beta C, slices summed
-// in order (deterministic), for each of `reps` replicas
-__global__ void k_reduce_partials(const float* __restrict__ P, int ks, int64_t M, int64_t N, EpiStridedF64 o,
-                                  int reps) {
-  const int64_t MN = M * N;
-  for (int64_t t = (int64_t)blockIdx.x * blockDim.x + threadIdx.x; t < reps * MN;
-       t += (int64_t)gridDim.x * blockDim.x) {
-    const int64_t rep = t / MN, tt = t - rep * MN;
-    double acc = 0.0;
-    for (int s = 0; s < ks; ++s) acc += f2d_bits(P[(rep * ks + s) * MN + tt]);
-    const int64_t r = tt / N, c = tt - r * N;
-    const int64_t ro = r / o.mi, co = c / o.ni;
-    double* p = o.C + rep * o.srep + ro * o.sro + (r - ro * o.mi) * o.sri + co * o.sco + (c - co * o.ni) * o.sci;
-    const double x = o.alpha * acc;
-    *p = o.beta == 0.0 ? x : x + o.beta * *p;
+// in order (deterministic), for each of `reps` replicas.  32 x 32 tiles of
+// (row, column): the partials are read with the lanes along rows (their
+// contiguous index), the sums pass through shared memory, and C is written
+// with the lanes along whichever of its rows or columns is contiguous.
+// Block 32 x 8 threads.
+__global__ void __launch_bounds__(256) k_reduce_partials(const float* __restrict__ P, int ks, int64_t M, int64_t N,
+                                                         EpiStridedF64 o, int reps, int rows_fast) {
+  __shared__ double t[32][33];  // [column][row] of the tile
+  const int lane = threadIdx.x, wy = threadIdx.y;
+  const int64_t tm = (M + 31) / 32, tn = (N + 31) / 32, per = tm * tn, NM = N * M;
+  for (int64_t b = blockIdx.x; b < reps * per; b += gridDim.x) {
+    const int64_t rep = b / per, rem = b - rep * per;
+    const int64_t r0 = (rem / tn) * 32, c0 = (rem % tn) * 32;
+    // a thread's four elements (columns wy + 8 jj), eight slices' loads in
+    // flight at a time, each sum in slice order
+    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    const float* q[4];
+    bool in[4];
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) {
+      const int64_t r = r0 + lane, c = c0 + wy + 8 * jj;
+      in[jj] = r < M && c < N;
+      q[jj] = in[jj] ? P + (rep * ks * N + c) * M + r : P;
+    }
+    for (int s0 = 0; s0 < ks; s0 += 8) {
+      const int cnt = ks - s0 < 8 ? ks - s0 : 8;
+      float v[4][8];
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+        for (int u = 0; u < 8; ++u) v[jj][u] = (in[jj] && u < cnt) ? q[jj][(int64_t)(s0 + u) * NM] : 0.0f;
+#pragma unroll
+      for (int jj = 0; jj < 4; ++jj)
+#pragma unroll
+        for (int u = 0; u < 8; ++u)
+          if (u < cnt) acc[jj] += f2d_bits(v[jj][u]);
+    }
+#pragma unroll
+    for (int jj = 0; jj < 4; ++jj) t[wy + 8 * jj][lane] = acc[jj];
+    __syncthreads();
+    for (int j = wy; j < 32; j += 8) {
+      const int64_t r = r0 + (rows_fast ? lane : j), c = c0 + (rows_fast ? j : lane);
+      if (r < M && c < N) {
+        const double acc = rows_fast ? t[j][lane] : t[lane][j];
+        const int64_t ro = r / o.mi, co = c / o.ni;
+        double* p = o.C + rep * o.srep + ro * o.sro + (r - ro * o.mi) * o.sri + co * o.sco + (c - co * o.ni) * o.sci;
+        const double x = o.alpha * acc;
+        *p = o.beta0 ? x : x + o.beta * *p;
+      }
+    }
+    __syncthreads();
   }
 }
 
@@ -771,7 +811,7 @@ int fricc_gemm_bf16_tn_strided_b(const void* A, int64_t lda, const void* B, int6
     fricc_set_error("gemm_bf16_tn_strided: bad output, split or replica layout");
     return FRICC_ERR_ARG;
   }
-  const tc::EpiStridedF64 out{C, M, N, mi, ni, sro, sri, sco, sci, alpha, beta, c_rep};
+  const tc::EpiStridedF64 out{C, M, N, mi, ni, sro, sri, sco, sci, alpha, beta, c_rep, beta == 0.0 ? 1 : 0};
   tc::RepTC rt;
   rt.reps = reps;
   rt.a_rep = (int)a_rep;
@@ -787,9 +827,11 @@ int fricc_gemm_bf16_tn_strided_b(const void* A, int64_t lda, const void* B, int6
   if (rc) return rc;
   rc = tc::launch(A, lda, B, ldb, M, N, K, tc::EpiPartial{P, M, N, ks}, st, status, ks, rt);
   if (!rc) {
-    int64_t g = fricc_cdiv(reps * M * N, 256);
+    int64_t g = reps * fricc_cdiv(M, 32) * fricc_cdiv(N, 32);
     if (g > 152 * 16) g = 152 * 16;
-    tc::k_reduce_partials<<<(unsigned)g, 256, 0, st>>>(P, ks, M, N, out, reps);
+    // write C along its rows when they are the contiguous index
+    const int rows_fast = (sri == 1 && sci != 1) ? 1 : 0;
+    tc::k_reduce_partials<<<(unsigned)g, dim3(32, 8), 0, st>>>(P, ks, M, N, out, reps, rows_fast);
     fricc_note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = fricc_cuda_fail(e, "gemm_tc reduce", __FILE__, __LINE__);

@@ -38,11 +38,12 @@ __global__ void __launch_bounds__(TD* TR) k_symadd(double* __restrict__ out, con
   __shared__ double t1[TD][TD + 1], t2[TD][TD + 1];
   // replica batches: blockIdx.z = r o^2 + ij; replica r's X starts xr
   // elements after the previous one's, its output o^2 v^2 after
-  const int64_t rep = blockIdx.z / (o * o);
-  const int64_t ij = blockIdx.z - rep * o * o;
+  const unsigned oo = (unsigned)(o * o);  // blockIdx.z < 65536: 32-bit divisions
+  const unsigned rep = blockIdx.z / oo;
+  const int64_t ij = blockIdx.z - rep * oo;
   X += rep * xr;
   out += rep * o * o * v * v;
-  const int64_t i = ij / o, j = ij - i * o;
+  const int64_t i = (unsigned)ij / (unsigned)o, j = ij - i * o;
   const int64_t a0 = (int64_t)blockIdx.y * TD, b0 = (int64_t)blockIdx.x * TD;
   // X[i,j,a,b] over (a,b): strides (s2, s3); X[j,i,b,a] over (a,b): strides (s3, s2)
   load_tile(t1, X, i * s0 + j * s1, s2, s3, a0, b0, v, v, first_along_b != 0);
