@@ -80,6 +80,12 @@ __device__ __forceinline__ I off5(const int64_t s[D], I i0, I i1, I i2, I i3, I 
   return i0 * (I)s[0] + i1 * (I)s[1] + i2 * (I)s[2] + i3 * (I)s[3] + i4 * (I)s[4];
 }
 
+// -x by flipping the sign bit (an integer operation: an FP64 negation would
+// occupy GB300's slow FP64 unit)
+__device__ __forceinline__ double neg_bits(double x) {
+  return __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+}
+
 // r_k from the loaded values; old[k] is out_k's value before the call
 // (read only with accumulate)
 template <int NIN, int NPROD, int NOUT>
@@ -93,14 +99,14 @@ __device__ __forceinline__ void finish(const CombineArgs& a, const double* xv, d
     for (int s = 0; s < NIN; ++s) {
       const int kind = a.cc[k][s];
       if (kind != 0) {
-        const double term = kind == 1 ? xv[s] : (kind == -1 ? -xv[s] : a.c[k][s] * xv[s]);
+        const double term = kind == 1 ? xv[s] : (kind == -1 ? neg_bits(xv[s]) : a.c[k][s] * xv[s]);
         acc = first ? term : acc + term;
         first = false;
       }
     }
     if (NPROD > 0 && a.cc[k][NIN] != 0) {
       const int kind = a.cc[k][NIN];
-      const double term = kind == 1 ? pv : (kind == -1 ? -pv : a.c[k][NIN] * pv);
+      const double term = kind == 1 ? pv : (kind == -1 ? neg_bits(pv) : a.c[k][NIN] * pv);
       acc = first ? term : acc + term;
     }
     *o[k] = a.acc[k] ? old[k] + acc : acc;

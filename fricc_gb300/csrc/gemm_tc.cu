@@ -236,12 +236,18 @@ struct EpiPartial {
   }
 };
 
-// C (the EpiStridedF64 mapping) = alpha sum_s P[s] + beta C, slices summed
-// in order (deterministic), for each of `reps` replicas.  32 x 32 tiles of
-// (row, column): the partials are read with the lanes along rows (their
-// contiguous index), the sums pass through shared memory, and C is written
-// with the lanes along whichever of its rows or columns is contiguous.
-// Block 32 x 8 threads.
+// C (the EpiStridedF64 mapping) = alpha sum_s P[s] + beta C, for each of
+// `reps` replicas.  The FP32 slices are summed in slice order in FP32-pair
+// arithmetic on the FP32 pipe (an error-free two-sum per slice, Knuth's
+// TwoSum; the running pair carries ~48 bits) and rounded once to FP64:
+// GB300's FP64 unit, not memory, bounded the FP64 sum of the slices.
+// MODE 0: C = sum, 1: C = sum + C, 2: C = alpha sum + beta C (the host
+// picks it, so no FP64 work is spent deciding per element).
+// 32 x 32 tiles of (row, column): the partials are read with the lanes
+// along rows (their contiguous index), the sums pass through shared memory,
+// and C is written with the lanes along whichever of its rows or columns is
+// contiguous.  Block 32 x 8 threads.
+template <int MODE>
 __global__ void __launch_bounds__(256) k_reduce_partials(const float* __restrict__ P, int ks, int64_t M, int64_t N,
                                                          EpiStridedF64 o, int reps, int rows_fast) {
   __shared__ double t[32][33];  // [column][row] of the tile
@@ -252,7 +258,7 @@ __global__ void __launch_bounds__(256) k_reduce_partials(const float* __restrict
     const int64_t r0 = (rem / tn) * 32, c0 = (rem % tn) * 32;
     // a thread's four elements (columns wy + 8 jj), eight slices' loads in
     // flight at a time, each sum in slice order
-    double acc[4] = {0.0, 0.0, 0.0, 0.0};
+    float hs[4] = {0.0f, 0.0f, 0.0f, 0.0f}, ls[4] = {0.0f, 0.0f, 0.0f, 0.0f};
     const float* q[4];
     bool in[4];
 #pragma unroll
@@ -272,10 +278,17 @@ __global__ void __launch_bounds__(256) k_reduce_partials(const float* __restrict
       for (int jj = 0; jj < 4; ++jj)
 #pragma unroll
         for (int u = 0; u < 8; ++u)
-          if (u < cnt) acc[jj] += f2d_bits(v[jj][u]);
+          if (u < cnt) {
+            const float x = v[jj][u];
+            const float sh = __fadd_rn(hs[jj], x);
+            const float bp = __fsub_rn(sh, hs[jj]);
+            const float e = __fadd_rn(__fsub_rn(hs[jj], __fsub_rn(sh, bp)), __fsub_rn(x, bp));
+            hs[jj] = sh;
+            ls[jj] = __fadd_rn(ls[jj], e);
+          }
     }
 #pragma unroll
-    for (int jj = 0; jj < 4; ++jj) t[wy + 8 * jj][lane] = acc[jj];
+    for (int jj = 0; jj < 4; ++jj) t[wy + 8 * jj][lane] = pair_to_f64(hs[jj], ls[jj]);
     __syncthreads();
     for (int j = wy; j < 32; j += 8) {
       const int64_t r = r0 + (rows_fast ? lane : j), c = c0 + (rows_fast ? j : lane);
@@ -283,8 +296,9 @@ __global__ void __launch_bounds__(256) k_reduce_partials(const float* __restrict
         const double acc = rows_fast ? t[j][lane] : t[lane][j];
         const int64_t ro = r / o.mi, co = c / o.ni;
         double* p = o.C + rep * o.srep + ro * o.sro + (r - ro * o.mi) * o.sri + co * o.sco + (c - co * o.ni) * o.sci;
-        const double x = o.alpha * acc;
-        *p = o.beta0 ? x : x + o.beta * *p;
+        if (MODE == 0) *p = acc;
+        else if (MODE == 1) *p = acc + *p;
+        else *p = o.beta0 ? o.alpha * acc : o.alpha * acc + o.beta * *p;
       }
     }
     __syncthreads();
@@ -831,7 +845,11 @@ int fricc_gemm_bf16_tn_strided_b(const void* A, int64_t lda, const void* B, int6
     if (g > 152 * 16) g = 152 * 16;
     // write C along its rows when they are the contiguous index
     const int rows_fast = (sri == 1 && sci != 1) ? 1 : 0;
-    tc::k_reduce_partials<<<(unsigned)g, dim3(32, 8), 0, st>>>(P, ks, M, N, out, reps, rows_fast);
+    const dim3 blk(32, 8);
+    if (alpha == 1.0 && beta == 0.0) tc::k_reduce_partials<0><<<(unsigned)g, blk, 0, st>>>(P, ks, M, N, out, reps, rows_fast);
+    else if (alpha == 1.0 && beta == 1.0)
+      tc::k_reduce_partials<1><<<(unsigned)g, blk, 0, st>>>(P, ks, M, N, out, reps, rows_fast);
+    else tc::k_reduce_partials<2><<<(unsigned)g, blk, 0, st>>>(P, ks, M, N, out, reps, rows_fast);
     fricc_note_launch();
     cudaError_t e = cudaGetLastError();
     if (e != cudaSuccess) rc = fricc_cuda_fail(e, "gemm_tc reduce", __FILE__, __LINE__);
