@@ -92,6 +92,11 @@ _MIN_TILES = 38
 _SMS = 152
 
 
+def _bn(N: int) -> int:
+    """The tensor-core GEMM's tile width for an output N wide."""
+    return 64 if N <= 64 else 256
+
+
 def _tiles(M: int, N: int) -> int:
     """Output tiles of the tensor-core GEMM (128 x 64 when N <= 64, else 128 x 256)."""
     return -(-M // 128) * -(-N // (64 if N <= 64 else 256))
@@ -103,24 +108,37 @@ def _wave_eff(units: int) -> float:
     return units / (-(-units // _SMS) * _SMS)
 
 
-def _ksplit(tiles: int, kp: int) -> int:
-    """The K split for a GEMM of ``tiles`` output tiles and K' = kp: none
-    from two rounds of tiles up; below that the smallest split that fills
-    the SMs' rounds to 90% (each slice at least 8 K blocks; a split must
-    gain 5 points of occupancy to be taken); 0 (use the FP32-pair GEMM)
-    when there are few tiles and K is short."""
+# the time model of the K split: a tile's MMA time per 64-wide K block
+# (128 x BN x 64 BF16 products at the sustained tensor rate shared by the
+# SMs) and the DRAM time of the FP32 partials a split writes and the
+# reduction reads back
+_TC_SM_RATE = 1.74e15 / _SMS   # flop/s per SM
+_HBM_BPS = 6.0e12              # bytes/s
+
+
+def _ksplit(tiles: int, kp: int, mn: int | None = None, bn: int = 256) -> int:
+    """The K split for a GEMM of ``tiles`` output tiles (``bn`` wide), K' =
+    kp and ``mn`` outputs: 0 (use the FP32-pair GEMM) when there are few
+    tiles and K is short; else the split (slices of at least 8 K blocks)
+    that minimises rounds of tiles x slice time + the partials' DRAM time,
+    so a split fills idle SMs only where that pays for its partials.
+    Without ``mn`` the partials are taken as free."""
     nk = -(-kp // 64)
     if tiles < _MIN_TILES and nk < 16:
         return 0
-    if tiles >= 2 * _SMS:  # two or more rounds already: a split's partials cost more than the tail
-        return 1
-    best, best_eff = 1, (_wave_eff(tiles) if tiles >= _MIN_TILES else 0.0)
+    t_blk = 2.0 * 128 * bn * 64 / _TC_SM_RATE
+
+    def cost(ks):
+        rounds = -(-(tiles * ks) // _SMS)
+        part = 0.0 if ks == 1 or mn is None else 8.0 * ks * mn / _HBM_BPS
+        return rounds * -(-nk // ks) * t_blk + part
+    best, best_t = 1, cost(1)
     for ks in (2, 3, 4, 6, 8, 12, 16, 24, 32, 48, 64, 96, 128, 152):
-        if best_eff >= 0.9 or nk // ks < 8:
+        if nk // ks < 8:
             break
-        e = _wave_eff(tiles * ks)
-        if e > best_eff + 0.05:
-            best, best_eff = ks, e
+        t = cost(ks)
+        if t < 0.95 * best_t:
+            best, best_t = ks, t
     return best
 
 
@@ -162,7 +180,8 @@ def gemm_tc(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float = 1.
     Nf = N * (batch if b_b else 1)
     # a narrow side goes to N (64-wide tiles): C^T = B^T A^T when M is small
     swap = Mf <= 64 < Nf
-    ks = _ksplit(_tiles(Nf, Mf) if swap else _tiles(Mf, Nf), _kp(K)) if K > 0 else 0
+    ks = _ksplit(_tiles(Nf, Mf) if swap else _tiles(Mf, Nf), _kp(K), Mf * Nf,
+                 _bn(Mf if swap else Nf)) if K > 0 else 0
     if ks == 0:
         return D.gemm_df(A, B, C, alpha, beta)
     # rows of A' are (b, m) or m; rows of B' are (b, n) or n; both K-major
@@ -200,7 +219,7 @@ def dense_spmm_ok(dims, pa, pb, ka, kb, QS: int) -> bool:
     """Whether ``dense_spmm`` takes this term (enough tiles, or a K long
     enough to split)."""
     nP, R = dims[pa] * dims[pb], dims[ka] * dims[kb]
-    return _ksplit(_tiles(nP, QS), _kp(R)) > 0
+    return _ksplit(_tiles(nP, QS), _kp(R), nP * QS, _bn(QS)) > 0
 
 
 def dense_spmm(T, dims, pa, pb, ka, kb, coef, Bt: torch.Tensor, QS: int, Op: torch.Tensor,
@@ -213,7 +232,7 @@ def dense_spmm(T, dims, pa, pb, ka, kb, coef, Bt: torch.Tensor, QS: int, Op: tor
     nP, R = dims[pa] * dims[pb], dims[ka] * dims[kb]
     kp = _kp(R)
     assert Bt.shape == (QS, kp) and Op.is_contiguous() and Op.numel() == nP * QS
-    ks = _ksplit(_tiles(nP, QS), kp)
+    ks = _ksplit(_tiles(nP, QS), kp, nP * QS, _bn(QS))
     if ks == 0:
         return False
     Ap = torch.empty(nP, kp, dtype=torch.bfloat16, device=Op.device)
@@ -410,7 +429,8 @@ def gemm_tc_rep(A: torch.Tensor, B: torch.Tensor, C: torch.Tensor, alpha: float,
     Mf = M * (batch if a_b else 1)
     Nf = N * (batch if b_b else 1)
     swap = Mf <= 64 < Nf
-    ks = _ksplit(_tiles(Nf, Mf) if swap else _tiles(Mf, Nf), _kp(K)) if K > 0 else 0
+    ks = _ksplit(_tiles(Nf, Mf) if swap else _tiles(Mf, Nf), _kp(K), Mf * Nf,
+                 _bn(Mf if swap else Nf)) if K > 0 else 0
     if ks == 0:
         df()
         return C
@@ -457,7 +477,7 @@ def dense_spmm_rep(spb, which: int, R: int, dims, pa, pb, ka, kb, coef, Bt: torc
     nP, Rk = dims[pa] * dims[pb], dims[ka] * dims[kb]
     kp = _kp(Rk)
     assert Bt.shape[1] == kp and Bt.shape[0] >= QS and Op.is_contiguous() and Op.numel() == R * nP * QS
-    ks = _ksplit(_tiles(nP, QS), kp)
+    ks = _ksplit(_tiles(nP, QS), kp, nP * QS, _bn(QS))
     if ks == 0:
         return False
     Ap = torch.empty(R * nP, kp, dtype=torch.bfloat16, device=Op.device)

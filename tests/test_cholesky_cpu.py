@@ -31,6 +31,19 @@ def test_ksplit_policy():
         assert ks >= 1 and (kp // 64) // ks >= 8
 
 
+def test_ksplit_weighs_the_partials():
+    # 128 tiles of a 2000 x 2000 output, K' = 6000: a split would fill the
+    # idle SMs, but its FP32 partials (8 x 4M floats written and read back)
+    # cost more than the round it saves
+    assert C._ksplit(128, 6000) > 1
+    assert C._ksplit(128, 6000, 2000 * 2000, 256) == 1
+    # the O^2V^4 term at o20v100 (160 tiles, K' = 30000): still split, less
+    ks = C._ksplit(160, 30000, 400 * 10000, 256)
+    assert 1 < ks < C._ksplit(160, 30000)
+    # a 20 x 20 output with a long K: every SM (its partials are tiny)
+    assert C._ksplit(1, 600000, 400, 64) == 152
+
+
 def test_dense_spmm_eligibility():
     # o10v40 terms: 2323 dense (long K), 0101 too small and short (falls back)
     dims = (10, 10, 40, 40)
