@@ -22,23 +22,14 @@ import json
 import os
 import time
 
-# One pool for torch and the library: torch allocates through
-# cudaMallocAsync on the device's default pool, the one the library's own
-# stream-ordered scratch comes from, so memory a finished request frees is
-# there for the next request's library scratch (with torch's caching
-# allocator the two pools grew apart over a long stream of differently
-# sized requests until a library allocation failed).
-os.environ.setdefault("PYTORCH_CUDA_ALLOC_CONF", "backend:cudaMallocAsync")
-
-import numpy as np  # noqa: E402
-import torch  # noqa: E402
-
-from .batch import ReplicaBatch, SolveServer, latency_summary, request_stream  # noqa: E402
-from .rccsd_dense import DeviceERIs  # noqa: E402
-from .synthetic import WORKLOADS, make_system  # noqa: E402
-
 
 def run_replicas(args):
+    import numpy as np
+    import torch
+
+    from .batch import ReplicaBatch
+    from .rccsd_dense import DeviceERIs
+    from .synthetic import WORKLOADS, make_system
     w = WORKLOADS["o20v100x64"]
     system = make_system("o20v100x64", seed=0)
     if args.precision == "split":
@@ -82,12 +73,16 @@ def _warm(server, args):
     """One untimed pass of a few requests through the same server: the
     first requests of a process pay one-time set-up (kernel modules loaded
     on first launch, per-thread library handles, allocator growth)."""
+    from .batch import request_stream
     warm = request_stream(max(2, min(args.streams, 8)), 1e6, seed=args.seed + 7919,
                           nocc=(args.nocc_min, args.nocc_max))
     server.run(warm, time_scale=0.0)
 
 
 def run_serve(args):
+    import numpy as np
+
+    from .batch import SolveServer, latency_summary, request_stream
     reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
     server = SolveServer(n_workers=args.streams, precision=args.precision, max_cycle=args.max_cycle, graph=args.graph,
                          device_inputs=not args.host_inputs, rebuild_vvvv=not args.rebuild_once)
@@ -151,8 +146,19 @@ def main():
     p.add_argument("--batch-graph", action="store_true",
                    help="replicas: capture every replica's iteration into one CUDA graph per batch step")
     p.add_argument("--fused", action="store_true",
-                   help="replicas: one launch per kernel for the whole batch (fp64 or df64)")
+                   help="replicas: one launch per kernel for the whole batch (fp64, df64 or split)")
     args = p.parse_args()
+    if args.mode == "serve" and not args.graph:
+        # One pool for torch and the library: torch allocates through
+        # cudaMallocAsync on the device's default pool, the one the
+        # library's own stream-ordered scratch comes from, so memory a
+        # finished request frees is there for the next request's library
+        # scratch (with torch's caching allocator the two pools grew apart
+        # over a long stream of differently sized requests until a library
+        # allocation failed).  Set before torch is first imported; not with
+        # CUDA graphs, whose multi-threaded captures crashed the host
+        # process under this allocator.
+        os.environ.setdefault("PYTORCH_CUDA_ALLOC_CONF", "backend:cudaMallocAsync")
     line = run_replicas(args) if args.mode == "replicas" else run_serve(args)
     print(json.dumps(line))
 
