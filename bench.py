@@ -16,11 +16,14 @@ figures, each with its |dE_corr| against the FP64 path for one step.
 resident in HBM; e2e = the same step through the host entry point
 (update_amps_host: numpy amplitudes in, numpy out, copies timed).
 --impl reference: the reference algorithm on the host cores (the oracle port
-of fri-cc's C++ plus numpy for the dense algebra), each step one sampled
-iteration: both compressions in full, the dense algebra in full, and every
-contraction term on one contiguous block of its outer-index pairs, the block
-rotating from step to step (B consecutive steps cover every pair once),
-scaled by the pair count.
+of fri-cc's C++ plus numpy for the dense algebra).  Warm-up steps are
+sampled iterations: both compressions in full, the dense algebra in full,
+and every contraction term on one contiguous block of its outer-index
+pairs, scaled by the pair count.  Each timed step is one whole iteration
+when the warm-up's estimate puts the timed steps within REF_FULL_BUDGET_S
+(--ref-steps auto, the default); otherwise each timed step is a sampled
+iteration, the block rotating from step to step (B consecutive steps cover
+every pair once), and the line says "extrapolated".
 --validate-sample (with --impl reference): one full iteration timed beside
 the B block estimates of the same iteration.
 
@@ -90,6 +93,9 @@ def parse():
                    help="use the recorded FMA peaks instead of running the FMA probe")
     p.add_argument("--validate-sample", action="store_true",
                    help="with --impl reference: time one iteration in full beside its sampled estimate")
+    p.add_argument("--ref-steps", default="auto", choices=["auto", "full", "blocks"],
+                   help="with --impl reference: time whole iterations ('full'), block-sampled ones ('blocks'), or "
+                        "whole ones when the warm-up's estimate puts the timed steps within the time budget")
     p.add_argument("--graph", action="store_true",
                    help="replay each iteration from one captured CUDA graph (after the first, eager one)")
     p.add_argument("--autotune", action="store_true",
@@ -248,16 +254,23 @@ def n_blocks_for(steps: int, cap: int = 10) -> int:
     return best if best > 1 or steps == 1 else min(steps, cap)
 
 
-def cpu_full_iteration(eris_np, t1, t2, m, rn_draw):
-    """One reference iteration on the host with every term in full: seconds
-    and the per-term times."""
+def cpu_full_iteration(eris_np, t1, t2, m, rn_draw, amplitudes=False):
+    """One reference iteration on the host with every term in full: seconds,
+    the per-term times and (``amplitudes``) the new (t1, t2)."""
     from oracle import ccsd_oracle as CO
     settings = {"m_keep": m, "compression": "fri", "sampling_method": "systematic", "verbose": False,
                 "compressed_contractions": ["O^2V^4", "O^3V^3", "O^4V^2"]}
     tim = {}
     t0 = time.perf_counter()
-    CO.update_amps(settings, t1, t2, eris_np, rn_draw=rn_draw, timings=tim)
-    return time.perf_counter() - t0, tim
+    new = CO.update_amps(settings, t1, t2, eris_np, rn_draw=rn_draw, timings=tim)
+    secs = time.perf_counter() - t0
+    return (secs, tim, new) if amplitudes else (secs, tim)
+
+
+# The reference arm times whole iterations when the estimate (from its
+# warm-up steps) says the timed steps fit in this many seconds; otherwise
+# every step runs the block sample.
+REF_FULL_BUDGET_S = 1200.0
 
 
 def _sample_text(workload, cores, n_blocks, wall, steps):
@@ -627,26 +640,44 @@ def run_reference(args):
                           "compress_s": per_full.get("compress")}))
         return
     draw = seeded_draws(1000)
-    # warm-up: one small compression (the CPU path has nothing to warm)
-    for _ in range(args.warmup):
-        fri_oracle.fri_compression(t2.ravel()[:100000], 1000, rn=0.5)
+    # warm-up: block-sampled iterations (every code path of the iteration
+    # runs once per step); their estimates decide whether the timed steps
+    # can run whole iterations within the budget
+    n_warm_blocks = 10
+    warm_est = []
+    for step in range(args.warmup):
+        secs, _, _, _ = cpu_sampled_iteration(eris_np, t1, t2, m, n_warm_blocks, step, draw)
+        warm_est.append(secs)
+    est = min(warm_est) if warm_est else float("inf")
+    full = args.ref_steps == "full" or (args.ref_steps == "auto" and est * args.steps <= REF_FULL_BUDGET_S)
     per = []
     walls = []
     for step in range(args.steps):
-        secs, wall, _, _ = cpu_sampled_iteration(eris_np, t1, t2, m, n_blocks, step, draw)
+        if full:  # whole iterations, continuing the trajectory from the MP2 start
+            secs, _, (t1, t2) = cpu_full_iteration(eris_np, t1, t2, m, draw, amplitudes=True)
+            wall = secs
+        else:
+            secs, wall, _, _ = cpu_sampled_iteration(eris_np, t1, t2, m, n_blocks, step, draw)
         per.append(secs)
         walls.append(wall)
     total = sum(per)
     value = args.steps / total
+    if full:
+        sample = (f"each step: one whole {args.workload} iteration of the oracle port of fri-cc's C++ (OpenMP, "
+                  f"{cores} threads) and numpy dense algebra, continuing the trajectory from the MP2 start; "
+                  f"{args.steps} step(s), {total:.1f} s of CPU work timed (warm-up: {args.warmup} block-sampled "
+                  f"iteration(s), estimate {est:.1f} s/iteration)")
+    else:
+        sample = _sample_text(args.workload, cores, n_blocks, sum(walls), args.steps)
     line = {
         "impl": "reference", "metric": METRIC, "value": value, "unit": "iter/s", "n_gpus": world,
         "steps": args.steps, "warmup": args.warmup, "ms_per_step": 1000.0 * total / args.steps,
-        "timed_wall_ms_per_step": 1000.0 * sum(walls) / args.steps, "extrapolated": True,
+        "timed_wall_ms_per_step": 1000.0 * sum(walls) / args.steps, "extrapolated": not full,
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
         "config": {"workload": workload_text(args.workload, system.nocc, system.nvir, w),
                    "parallelism": "host cores", "precision": "fp64"},
-        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": cores, "kind": "port", "extrapolated": True,
-                         "sample": _sample_text(args.workload, cores, n_blocks, sum(walls), args.steps)},
+        "cpu_baseline": {"value": value, "unit": "iter/s", "cores": cores, "kind": "port", "extrapolated": not full,
+                         "sample": sample},
         "e2e": {"value": value, "unit": "iter/s", "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
         "gpu_launches": 0,
     }

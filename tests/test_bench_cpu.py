@@ -24,6 +24,18 @@ def test_reference_arm_json_line():
     cb = d["cpu_baseline"]
     assert cb["kind"] in ("port", "reference") and cb["cores"] >= 1 and cb["sample"]
     assert d["config"]["workload"].startswith("o10v40")
+    # a small workload fits the time budget: whole iterations, nothing extrapolated
+    assert d["extrapolated"] is False and cb["extrapolated"] is False and "whole" in cb["sample"]
+    assert abs(d["ms_per_step"] - d["timed_wall_ms_per_step"]) < 1e-9
+
+
+def test_reference_arm_block_sample_mode():
+    r = subprocess.run([sys.executable, "bench.py", "--impl", "reference", "--workload", "o10v40", "--steps", "2",
+                        "--warmup", "1", "--ref-steps", "blocks"], cwd=REPO, capture_output=True, text=True,
+                       timeout=600)
+    assert r.returncode == 0, r.stderr[-2000:]
+    d = json.loads([ln for ln in r.stdout.splitlines() if ln.startswith("{")][0])
+    assert d["extrapolated"] is True and "block" in d["cpu_baseline"]["sample"] and d["value"] > 0
 
 
 def test_clock_sampler_reads_a_fake_nvidia_smi(tmp_path, monkeypatch):
