@@ -200,3 +200,12 @@ class OwnStream:
             except Exception:
                 pass
             self.handle = None
+
+
+def cur_stream() -> ctypes.c_void_p:
+    """This thread's current CUDA stream on the current device (torch's
+    current stream) as a C pointer, read without torch.cuda's Python
+    wrappers: an iteration asks for it a few hundred times, and the wrapped
+    lookup cost more host time than some of the launches it feeds."""
+    import torch
+    return ctypes.c_void_p(torch._C._cuda_getCurrentRawStream(torch._C._cuda_getDevice()))

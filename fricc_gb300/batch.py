@@ -213,10 +213,44 @@ def footprint_bytes(o: int, v: int, precision: str = "df64") -> int:
     return int(8 * (vvvv + ovvv + 16 * o * o * v * v + 4 * o**4 + 8 * o**3 * v))
 
 
+class _Live:
+    """A served request between its build and its last iteration: its
+    solver, amplitudes and stream, the energy it compares the next one
+    with, and the event its iteration in flight records."""
+
+    __slots__ = ("req", "solver", "E", "stream", "t1", "t2", "eold", "event", "ti", "owner")
+
+    def __init__(self, req, solver, E, stream, t1, t2, eold, ti):
+        self.req, self.solver, self.E, self.stream = req, solver, E, stream
+        self.t1, self.t2, self.eold, self.ti = t1, t2, eold, ti
+        self.event = None
+        self.owner = None
+
+
 class SolveServer:
+    """Serve solve requests on one GPU.
+
+    schedule="iterations" (continuous batching at iteration level): builder
+    threads make each admitted request's system, integrals, solver and first
+    iteration on a stream of the request's own; one scheduler thread then
+    drives every built request an iteration at a time, issuing a request's
+    next iteration as soon as its last one has finished on the device
+    (polled through an event), so the iterations of all requests in flight
+    overlap on the GPU while one host thread issues them -- requests join
+    and leave between iterations as they are built and converge.
+    schedule="workers": n_workers threads each solve one request at a time
+    from build to convergence (several host threads issuing at once contend
+    for the interpreter lock, which measured slower than one issuing thread).
+    """
+
     def __init__(self, n_workers: int = 8, hbm_budget: float = 200e9, precision: str = "df64", max_cycle: int = 30,
                  tol: float = 1e-7, device="cuda", graph: bool = False, device_inputs: bool = True,
-                 rebuild_vvvv: bool = True):
+                 rebuild_vvvv: bool = True, schedule: str = "workers", max_active: int = 24, n_builders: int = 2):
+        if schedule not in ("workers", "iterations"):
+            raise ValueError("schedule must be 'workers' or 'iterations'")
+        self.schedule = schedule
+        self.max_active = max(1, int(max_active))
+        self.n_builders = max(1, int(n_builders))
         self.graph = graph
         # split precision: rebuild (vv|vv) every iteration, or once per solve
         self.rebuild_vvvv = rebuild_vvvv
@@ -232,9 +266,27 @@ class SolveServer:
         if self.device.index is None:
             self.device = torch.device("cuda", torch.cuda.current_device())
         self._in_use = 0
+        self._n_live = 0
         self._cv = threading.Condition()
+        self._streams = []  # idle streams of finished requests, reused
 
-    def _solve(self, req: Request, t0: float, stream):
+    def _take_stream(self):
+        """A stream of the request's own (created for it, not torch's shared
+        pool, whose few streams would tie requests together)."""
+        with self._cv:
+            if self._streams:
+                return self._streams.pop()
+        from ._lib import OwnStream
+        return OwnStream(self.device)
+
+    def _give_stream(self, own) -> None:
+        with self._cv:
+            self._streams.append(own)
+
+    # ------------------------------------------------------------ one request
+    def _build(self, req: Request, t0: float, stream) -> _Live:
+        """System, integrals, solver and MP2 guess of a request on ``stream``
+        (waited for: build_s is its time)."""
         tb = time.perf_counter()
         with torch.cuda.stream(stream):
             if self.device_inputs:
@@ -254,21 +306,53 @@ class SolveServer:
             req.started = ti - t0
             req.build_s = ti - tb
             eold = solver.energy(t1, t2)
-            for it in range(self.max_cycle):
-                t1, t2 = solver.update_amps(t1, t2)
-                e, normt = solver.read_energy()
-                req.energies.append(e)
-                req.iterations = it + 1
-                if abs(e - eold) < self.tol:
-                    req.converged = True
-                    break
-                if not math.isfinite(e) or abs(e - eold) > 1e5:
-                    break
-                eold = e
-            req.e_corr = req.energies[-1] if req.energies else math.nan
-            stream.synchronize()
-            req.iterate_s = time.perf_counter() - ti
-            del solver, E, t1, t2
+        return _Live(req, solver, E, stream, t1, t2, eold, ti)
+
+    def _issue(self, lv: _Live) -> None:
+        """Launch the request's next iteration; its event marks the end."""
+        with torch.cuda.stream(lv.stream):
+            lv.t1, lv.t2 = lv.solver.update_amps(lv.t1, lv.t2)
+            ev = torch.cuda.Event()
+            ev.record(lv.stream)
+        lv.event = ev
+
+    def _settle(self, lv: _Live) -> bool:
+        """Read the finished iteration's energy; True when the request is
+        done (converged, diverged or out of iterations)."""
+        req = lv.req
+        with torch.cuda.stream(lv.stream):
+            e, _ = lv.solver.read_energy()
+        req.energies.append(e)
+        req.iterations += 1
+        if abs(e - lv.eold) < self.tol:
+            req.converged = True
+            return True
+        if not math.isfinite(e) or abs(e - lv.eold) > 1e5:
+            return True
+        lv.eold = e
+        return req.iterations >= self.max_cycle
+
+    def _close(self, lv: _Live) -> None:
+        req = lv.req
+        req.e_corr = req.energies[-1] if req.energies else math.nan
+        lv.stream.synchronize()
+        req.iterate_s = time.perf_counter() - lv.ti
+        lv.solver = lv.E = lv.t1 = lv.t2 = lv.event = None
+
+    def _solve(self, req: Request, t0: float, stream):
+        lv = self._build(req, t0, stream)
+        done = self.max_cycle <= 0
+        while not done:
+            self._issue(lv)
+            done = self._settle(lv)
+        self._close(lv)
+
+    # ----------------------------------------------------------- the stream
+    def _release(self, req: Request) -> None:
+        with self._cv:
+            self._in_use -= footprint_bytes(req.nocc, req.nvir, self.precision)
+            self._n_live -= 1
+            self._cv.notify_all()
 
     def run(self, requests, time_scale: float = 1.0):
         """Serve the requests (arrival times scaled by time_scale); returns them filled in."""
@@ -276,6 +360,9 @@ class SolveServer:
         admitted = queue.Queue()
         t0 = time.perf_counter()
         errors = []
+        iterations = self.schedule == "iterations"
+        n_consumers = self.n_builders if iterations else self.k
+        cap = self.max_active if iterations else 1 << 30
 
         def dispatcher():
             for r in reqs:
@@ -284,12 +371,13 @@ class SolveServer:
                     time.sleep(delay)
                 need = footprint_bytes(r.nocc, r.nvir, self.precision)
                 with self._cv:
-                    while self._in_use + need > self.budget and self._in_use > 0:
+                    while (self._in_use + need > self.budget or self._n_live >= cap) and self._n_live > 0:
                         self._cv.wait()
                     self._in_use += need
+                    self._n_live += 1
                 r.admitted = time.perf_counter() - t0
                 admitted.put(r)
-            for _ in range(self.k):
+            for _ in range(n_consumers):
                 admitted.put(None)
 
         def worker(w):
@@ -304,11 +392,72 @@ class SolveServer:
                 except BaseException as e:
                     errors.append(e)
                 r.finished = time.perf_counter() - t0
-                with self._cv:
-                    self._in_use -= footprint_bytes(r.nocc, r.nvir, self.precision)
-                    self._cv.notify_all()
+                self._release(r)
 
-        th = [threading.Thread(target=dispatcher)] + [threading.Thread(target=worker, args=(w,)) for w in range(self.k)]
+        built = queue.Queue()
+
+        def builder(w):
+            torch.cuda.set_device(self.device)
+            try:
+                while True:
+                    r = admitted.get()
+                    if r is None:
+                        return
+                    try:
+                        own = self._take_stream()
+                        lv = self._build(r, t0, own.stream)
+                        lv.owner = own
+                        if self.max_cycle > 0:
+                            self._issue(lv)  # the first iteration (handles and first-use splits) here
+                        built.put(lv)
+                    except BaseException as e:
+                        errors.append(e)
+                        r.finished = time.perf_counter() - t0
+                        self._release(r)
+            finally:
+                built.put(None)
+
+        def scheduler():
+            torch.cuda.set_device(self.device)
+            active = []
+            open_builders = self.n_builders
+            while open_builders or active:
+                while True:  # requests built since the last pass join
+                    try:
+                        lv = built.get_nowait() if active or not open_builders else built.get(timeout=0.05)
+                    except queue.Empty:
+                        break
+                    if lv is None:
+                        open_builders -= 1
+                    else:
+                        active.append(lv)
+                progressed = False
+                for lv in list(active):
+                    if lv.event is not None and not lv.event.query():
+                        continue
+                    progressed = True
+                    try:
+                        done = lv.event is None or self._settle(lv)
+                        if not done:
+                            self._issue(lv)
+                            continue
+                        self._close(lv)
+                    except BaseException as e:
+                        errors.append(e)
+                    lv.req.finished = time.perf_counter() - t0
+                    active.remove(lv)
+                    if lv.solver is None:  # closed: its stream is idle
+                        self._give_stream(lv.owner)
+                    self._release(lv.req)
+                if active and not progressed:
+                    time.sleep(2e-4)
+
+        if iterations:
+            th = ([threading.Thread(target=dispatcher), threading.Thread(target=scheduler)]
+                  + [threading.Thread(target=builder, args=(w,)) for w in range(self.n_builders)])
+        else:
+            th = [threading.Thread(target=dispatcher)] + [threading.Thread(target=worker, args=(w,))
+                                                          for w in range(self.k)]
         for t in th:
             t.start()
         for t in th:

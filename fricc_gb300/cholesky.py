@@ -25,8 +25,7 @@ def _p(t):
 
 
 def _st(stream=None):
-    s = stream if stream is not None else torch.cuda.current_stream()
-    return ctypes.c_void_p(s.cuda_stream)
+    return ctypes.c_void_p(stream.cuda_stream) if stream is not None else L.cur_stream()
 
 
 def _check_operand(x, name):

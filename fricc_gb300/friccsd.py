@@ -344,7 +344,7 @@ class FRICCSDGPU:
         comp = s["compressed_contractions"]
         o, v = t1.shape
         ov = o * v
-        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        st = L.cur_stream()
         t2 = t2.contiguous()
         t1 = t1.contiguous()
         ein = torch.einsum

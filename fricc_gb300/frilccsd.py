@@ -96,7 +96,7 @@ class FRILCCSDGPU(FRICCSDGPU):
         comp = s["compressed_contractions"]
         o, v = t1.shape
         ov = o * v
-        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        st = L.cur_stream()
         t2 = t2.contiguous()
         e_o = E.mo_energy[:o]
         e_v = E.mo_energy[o:] + self.level_shift

@@ -71,7 +71,7 @@ def parallel_sample(n_sample: int, probs, chunks: int = 1, rng=None) -> np.ndarr
 
 
 def _stream() -> ctypes.c_void_p:
-    return ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    return L.cur_stream()
 
 
 def _to_device(a, dtype=torch.float64):

@@ -24,6 +24,8 @@ import threading
 import numpy as np
 import torch
 
+from . import _lib as L
+
 ein = torch.einsum
 
 
@@ -228,14 +230,13 @@ def sym_add(out: torch.Tensor, X: torch.Tensor, coef: float = 1.0) -> torch.Tens
     device, X any [o,o,v,v] FP64 view not overlapping out."""
     import ctypes
 
-    from . import _lib as L
     o, v = out.shape[0], out.shape[2]
     if (not out.is_contiguous() or out.dtype != torch.float64 or X.dtype != torch.float64
             or tuple(X.shape) != tuple(out.shape) or out.shape != (o, o, v, v)):
         raise ValueError("sym_add: out contiguous [o,o,v,v] float64 and X a float64 view of the same shape")
     L.check(L.load().fricc_symadd(ctypes.c_void_p(out.data_ptr()), ctypes.c_void_p(X.data_ptr()), o, v,
                                   L.i64arr(X.stride()), float(coef),
-                                  ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+                                  L.cur_stream()))
     return out
 
 
@@ -255,7 +256,6 @@ def combine(outs, xs=(), coefs=None, prod=(), accumulate=False):
     Outputs must not overlap the inputs."""
     import ctypes
 
-    from . import _lib as L
     outs = list(outs)
     xs = list(xs)
     prod = list(prod)
@@ -291,7 +291,7 @@ def combine(outs, xs=(), coefs=None, prod=(), accumulate=False):
     cf = (ctypes.c_double * (len(outs) * nc))(*[float(c) for row in coefs for c in row])
     L.check(L.load().fricc_combine5(L.i64arr([dims[d] for d in perm]), len(xs), ptrs(xs), strides(xs), len(prod),
                                     ptrs(prod), strides(prod), len(outs), ptrs(outs), strides(outs), cf,
-                                    int(bool(accumulate)), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+                                    int(bool(accumulate)), L.cur_stream()))
     return outs[0]
 
 
@@ -299,11 +299,10 @@ def zero(t: torch.Tensor) -> torch.Tensor:
     """t[...] = 0 for a contiguous device tensor, through the library."""
     import ctypes
 
-    from . import _lib as L
     if not t.is_contiguous():
         raise ValueError("zero: contiguous tensors only")
     L.check(L.load().fricc_zero(ctypes.c_void_p(t.data_ptr()), t.numel() * t.element_size(),
-                                ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+                                L.cur_stream()))
     return t
 
 
@@ -334,7 +333,6 @@ def _bstrides(t: torch.Tensor):
 def _gemm_call(fn, A, B, C, alpha, beta):
     import ctypes
 
-    from . import _lib as L
     sA, bA, b2A = _bstrides(A)
     sB, bB, b2B = _bstrides(B)
     sC, batch, batch2 = _bstrides(C)
@@ -346,7 +344,7 @@ def _gemm_call(fn, A, B, C, alpha, beta):
     sA = (sA[0], sA[1], sA[2] if bA == batch and batch > 1 else 0, sA[3] if b2A == batch2 and batch2 > 1 else 0)
     sB = (sB[0], sB[1], sB[2] if bB == batch and batch > 1 else 0, sB[3] if b2B == batch2 and batch2 > 1 else 0)
     lib = L.load()
-    st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    st = L.cur_stream()
     pA, pB, pC = (ctypes.c_void_p(t.data_ptr()) for t in (A, B, C))
     if batch2 == 1:
         L.check(getattr(lib, fn)(pA, pB, pC, batch, M, N, K, L.i64arr(sA[:3]), L.i64arr(sB[:3]), L.i64arr(sC[:3]),
@@ -466,14 +464,13 @@ def split_f2(x: torch.Tensor, qs: int = None) -> torch.Tensor:
     dimensions after the first two (W' is always [key1, key2, q...])."""
     import ctypes
 
-    from . import _lib as L
     x = x.contiguous()
     if qs is None:
         qs = math.prod(x.shape[2:]) if x.dim() > 2 else x.shape[-1]
     rows = x.numel() // qs
     out = torch.empty(rows * ((qs + 1) // 2) * 4, dtype=torch.float32, device=x.device)
     L.check(L.load().fricc_split_f2(ctypes.c_void_p(x.data_ptr()), rows, qs, ctypes.c_void_p(out.data_ptr()),
-                                    ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+                                    L.cur_stream()))
     return out
 
 

@@ -144,7 +144,7 @@ class FusedReplicaBatch:
         self.t2 = t2.unsqueeze(0).repeat(R, 1, 1, 1, 1).contiguous()
         self.lib = L.load()
         self.spb = ctypes.c_void_p()
-        st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+        st = L.cur_stream()
         L.check(self.lib.fricc_spb_create(R, L.i64arr(t2.shape), self.m, st, ctypes.byref(self.spb)))
         dev = eris.device
         self.rn_dev = torch.zeros(R, 2, dtype=torch.float64, device=dev)
@@ -205,7 +205,7 @@ class FusedReplicaBatch:
 
     def _symadd(self, out, X, coef):
         L.check(self.lib.fricc_symadd_b(_ptr(out), _ptr(X), self.R, self.o, self.v, L.i64arr(X.stride()),
-                                        float(coef), ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+                                        float(coef), L.cur_stream()))
 
     def step(self, record: bool = True):
         """One iteration of every replica."""
@@ -247,7 +247,7 @@ class FusedReplicaBatch:
         vals = np.empty(self.m, dtype=np.float64)
         L.check(self.lib.fricc_spb_export(self.spb, int(which), int(r), ctypes.c_void_p(flat.ctypes.data),
                                           ctypes.c_void_p(vals.ctypes.data),
-                                          ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)))
+                                          L.cur_stream()))
         return flat, vals
 
     def _update(self, t1, t2):

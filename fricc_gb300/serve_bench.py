@@ -10,7 +10,10 @@
   --mode serve    : a Poisson stream of solve requests (nocc ~ U{5..30},
                     nvir = ceil(r nocc) with r ~ U[4,6], naux = 8(o+v), kept
                     fraction ~ U[5%,20%], converged at |dE| < 1e-7 Eh or
-                    after --max-cycle iterations) served concurrently, against
+                    after --max-cycle iterations) served concurrently (by
+                    default at iteration level: one scheduler thread issues
+                    each request's next iteration when its last one is done),
+                    against
                     the same requests solved one at a time in plain FP64;
                     prints solves/s and p50/p99 time to converged energy.
 One JSON line per mode.
@@ -85,11 +88,15 @@ def run_serve(args):
     from .batch import SolveServer, latency_summary, request_stream
     reqs = request_stream(args.requests, args.rate, seed=args.seed, nocc=(args.nocc_min, args.nocc_max))
     server = SolveServer(n_workers=args.streams, precision=args.precision, max_cycle=args.max_cycle, graph=args.graph,
-                         device_inputs=not args.host_inputs, rebuild_vvvv=not args.rebuild_once)
+                         device_inputs=not args.host_inputs, rebuild_vvvv=not args.rebuild_once,
+                         schedule=args.schedule, max_active=args.max_active, n_builders=args.builders)
     _warm(server, args)
     out = server.run(reqs, time_scale=1.0)
     served = latency_summary(out)
-    line = {"mode": "serve", "requests": args.requests, "rate_per_s": args.rate, "workers": args.streams,
+    line = {"mode": "serve", "requests": args.requests, "rate_per_s": args.rate, "schedule": args.schedule,
+            "workers": args.streams if args.schedule == "workers" else None,
+            "max_active": args.max_active if args.schedule == "iterations" else None,
+            "builders": args.builders if args.schedule == "iterations" else None,
             "inputs": "host (numpy)" if args.host_inputs else "device (torch Philox)",
             "vvvv_rebuild": "once per solve" if args.rebuild_once else "every iteration",
             "precision": args.precision, "max_cycle": args.max_cycle, "graph": args.graph, "served": served}
@@ -138,6 +145,12 @@ def main():
     p.add_argument("--max-cycle", type=int, default=30)
     p.add_argument("--plain", action="store_true", help="serve: also solve the requests one at a time in plain FP64")
     p.add_argument("--plain-every", type=int, default=1, help="serve: the plain arm solves every k-th request")
+    p.add_argument("--schedule", default="iterations", choices=["iterations", "workers"],
+                   help="serve: one scheduler thread driving every built request an iteration at a time "
+                        "(builder threads make the requests), or --streams worker threads each solving one request "
+                        "at a time")
+    p.add_argument("--max-active", type=int, default=24, help="serve, iterations: requests built or iterating at once")
+    p.add_argument("--builders", type=int, default=2, help="serve, iterations: builder threads")
     p.add_argument("--rebuild-once", action="store_true",
                    help="split precision: rebuild (vv|vv) once per solve instead of every iteration")
     p.add_argument("--host-inputs", action="store_true",

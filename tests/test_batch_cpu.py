@@ -77,3 +77,87 @@ def test_server_admission_respects_hbm_budget(monkeypatch):
     assert state["max"] <= budget
     s = latency_summary(out)
     assert s["n"] == 16 and s["converged"] == 16 and s["solves_per_s"] > 0
+
+
+def test_iteration_scheduler_interleaves_requests(monkeypatch):
+    """schedule="iterations": builder threads build each request and issue
+    its first iteration; one scheduler thread issues every later iteration,
+    a request's next one only after its last one finished, with the
+    iterations of different requests interleaved; the active-request cap
+    and the HBM budget hold, and every request finishes (device work faked
+    on CPU: an iteration "finishes" a few milliseconds after it is issued)."""
+    import threading
+    import time
+
+    from fricc_gb300 import batch as B
+    monkeypatch.setattr(B.torch.cuda, "set_device", lambda d: None)
+    lock = threading.Lock()
+    log = []            # (thread name, rid, iteration) of every issue
+    state = {"live": 0, "max_live": 0, "in_use": 0, "max_in_use": 0}
+
+    class FakeEvent:
+        def __init__(self, ready_at):
+            self.ready_at = ready_at
+
+        def query(self):
+            return time.perf_counter() >= self.ready_at
+
+    class FakeOwn:
+        stream = None
+
+    def fake_build(self, req, t0, stream):
+        need = B.footprint_bytes(req.nocc, req.nvir, self.precision)
+        with lock:
+            state["live"] += 1
+            state["max_live"] = max(state["max_live"], state["live"])
+            state["in_use"] += need
+            state["max_in_use"] = max(state["max_in_use"], state["in_use"])
+        req.started = time.perf_counter() - t0
+        return B._Live(req, object(), None, stream, None, None, 0.0, time.perf_counter())
+
+    def fake_issue(self, lv):
+        with lock:
+            log.append((threading.current_thread().name, lv.req.rid, lv.req.iterations))
+        assert lv.event is None or lv.event.query()  # never ahead of the last iteration
+        lv.event = FakeEvent(time.perf_counter() + 0.002 * (1 + lv.req.rid % 3))
+
+    def fake_settle(self, lv):
+        lv.req.iterations += 1
+        lv.req.energies.append(-1.0 / lv.req.iterations)
+        done = lv.req.iterations >= 3 + lv.req.rid % 2
+        lv.req.converged = done
+        return done
+
+    def fake_close(self, lv):
+        req = lv.req
+        req.e_corr = req.energies[-1]
+        with lock:
+            state["live"] -= 1
+            state["in_use"] -= B.footprint_bytes(req.nocc, req.nvir, self.precision)
+        lv.solver = None
+
+    monkeypatch.setattr(B.SolveServer, "_build", fake_build)
+    monkeypatch.setattr(B.SolveServer, "_issue", fake_issue)
+    monkeypatch.setattr(B.SolveServer, "_settle", fake_settle)
+    monkeypatch.setattr(B.SolveServer, "_close", fake_close)
+    monkeypatch.setattr(B.SolveServer, "_take_stream", lambda self: FakeOwn())
+    reqs = request_stream(20, rate=2000.0, seed=4, nocc=(5, 12))
+    sizes = sorted(B.footprint_bytes(r.nocc, r.nvir, "split") for r in reqs)
+    budget = sum(sizes[-3:])
+    srv = B.SolveServer(precision="split", device="cuda:0", schedule="iterations", max_active=5, n_builders=2,
+                        hbm_budget=budget)
+    out = srv.run(reqs, time_scale=0.0)
+    assert all(r.iterations == 3 + r.rid % 2 and r.converged and r.finished >= r.started >= 0 for r in out)
+    assert state["max_live"] <= 5 and state["max_in_use"] <= budget and state["live"] == 0
+    first = {}
+    later_threads = set()
+    for name, rid, it in log:
+        if it == 0:
+            first[rid] = name
+        else:
+            later_threads.add(name)
+    assert len(first) == 20 and len(later_threads) == 1   # one scheduler issues every later iteration
+    assert not set(first.values()) & later_threads          # first iterations come from the builders
+    later = [rid for _, rid, it in log if it > 0]
+    switches = sum(a != b for a, b in zip(later, later[1:]))
+    assert switches > len(set(later))                        # requests' iterations interleave

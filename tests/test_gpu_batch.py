@@ -57,10 +57,11 @@ def test_batch_graph_matches_eager(gpulib, precision):
     torch.testing.assert_close(g.t2[0], e.t2[0], rtol=1e-12, atol=1e-18)
 
 
-def test_served_requests_match_lone_solves(gpulib):
+@pytest.mark.parametrize("schedule", ["workers", "iterations"])
+def test_served_requests_match_lone_solves(gpulib, schedule):
     from fricc_gb300.batch import SolveServer, request_stream
     reqs = request_stream(6, rate=200.0, seed=5, nocc=(4, 7))
-    out = SolveServer(n_workers=3, precision="df64", max_cycle=4).run(reqs)
+    out = SolveServer(n_workers=3, precision="df64", max_cycle=4, schedule=schedule, max_active=4).run(reqs)
     for r in out:
         assert r.iterations >= 1 and np.isfinite(r.e_corr)
         assert r.admitted >= r.arrival - 1e-6 and r.finished >= r.started
@@ -71,17 +72,19 @@ def test_served_requests_match_lone_solves(gpulib):
         assert abs(a.e_corr - b.e_corr) < 1e-10, (a.rid, a.e_corr, b.e_corr)
 
 
-def test_served_split_requests_alone_in_the_mix_and_against_fp64(gpulib):
+@pytest.mark.parametrize("schedule", ["workers", "iterations"])
+def test_served_split_requests_alone_in_the_mix_and_against_fp64(gpulib, schedule):
     """The served split-precision form: each request's energies are the same
-    served among others (3 workers, overlapping solves) as solved alone, and
-    every iteration's energy is within 1e-6 Eh of the plain FP64 GPU form's
-    (same synthetic system, same draws)."""
+    served among others (3 workers, or the iteration-level scheduler with up
+    to 4 requests in flight: overlapping solves) as solved alone, and every
+    iteration's energy is within 1e-6 Eh of the plain FP64 GPU form's (same
+    synthetic system, same draws)."""
     from fricc_gb300.batch import SolveServer, request_stream
 
     def stream():
         return request_stream(6, rate=200.0, seed=11, nocc=(5, 8))
 
-    served = SolveServer(n_workers=3, precision="split", max_cycle=4).run(stream())
+    served = SolveServer(n_workers=3, precision="split", max_cycle=4, schedule=schedule, max_active=4).run(stream())
     lone, plain = stream(), stream()
     for r in lone:
         SolveServer(n_workers=1, precision="split", max_cycle=4).run([r])
