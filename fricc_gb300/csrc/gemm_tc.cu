@@ -162,6 +162,7 @@ __device__ __forceinline__ void tc_ld16(uint32_t taddr, float* v) {
 
 // C row-major FP32 [M][ldc]
 struct EpiRowMajor {
+  static constexpr int kStageBytes = 0;
   float* C;
   int64_t M, N, ldc;
   __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v, int, int) const {
@@ -180,6 +181,7 @@ struct EpiRowMajor {
 
 // C row-major FP64 [M][ldc] (the FP32 accumulators widened exactly)
 struct EpiRowMajorF64 {
+  static constexpr int kStageBytes = 0;
   double* C;
   int64_t M, N, ldc;
   __device__ __forceinline__ void operator()(int64_t row, int64_t col0, const float* v, int, int) const {
@@ -195,6 +197,7 @@ struct EpiRowMajorF64 {
 // flatten a (batch, index) pair: element (r, c) sits at
 // (r / mi) sro + (r % mi) sri + (c / ni) sco + (c % ni) sci.
 struct EpiStridedF64 {
+  static constexpr int kStageBytes = 0;
   double* C;
   int64_t M, N, mi, ni, sro, sri, sco, sci;
   double alpha, beta;
@@ -224,6 +227,7 @@ struct EpiStridedF64 {
 // P[rep][s][N][M], column-major, so that a warp's 32 lanes (32 consecutive
 // rows) store 128 contiguous bytes per column
 struct EpiPartial {
+  static constexpr int kStageBytes = 0;
   float* P;
   int64_t M, N;
   int ks;
@@ -313,6 +317,7 @@ __global__ void __launch_bounds__(256) k_reduce_partials(const float* __restrict
 // consecutive r1, i.e. consecutive b: each of its stores writes one
 // contiguous 128-byte run (two where the warp crosses a d boundary).
 struct EpiVvvv {
+  static constexpr int kStageBytes = 0;
   float* W;
   int64_t v, ldw;
   __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x, int, int) const {
@@ -339,7 +344,7 @@ __device__ __forceinline__ void mbar_arrive(uint32_t a) {
 
 // linear tile index -> (m tile, n tile): groups of 16 M tiles sweep all N
 // tiles, so the CTAs working at once share a few operand panels in L2
-__device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, int& mt, int& nt) {
+__host__ __device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, int& mt, int& nt) {
   constexpr int GROUP = 16;
   const int per_group = GROUP * tiles_n;
   const int g = id / per_group, rem = id - g * per_group;
@@ -357,8 +362,20 @@ __device__ __forceinline__ void tile_coords(int id, int tiles_m, int tiles_n, in
 // (L[:, b, d]) and column r2 = a v + c give (bd|ac) = (ac|bd); a warp's 32
 // lanes are 32 consecutive d, so each store is one contiguous run.
 struct EpiVvvvSplitB {
+  // each epilogue warp stages a 32 x 16 block (rows padded to 17 floats)
+  static constexpr int kStageBytes = EPI_WARPS * 32 * 17 * 4;
   __nv_bfloat16* B;
   int64_t v, kpo;
+  int tri;  // only the tiles of the upper triangle run (RepTC::tri): write (r1, r2) and its mirror (r2, r1)
+  __device__ __forceinline__ void put(int64_t a, int64_t b, int64_t c, int64_t d, float x) const {
+    const int64_t R = v * v;
+    const __nv_bfloat16 hi = __float2bfloat16(x);
+    const __nv_bfloat16 lo = __float2bfloat16(x - __bfloat162float(hi));
+    __nv_bfloat16* row = B + (a * v + b) * kpo + c * v + d;
+    row[0] = hi;
+    row[R] = lo;
+    row[2 * R] = hi;
+  }
   __device__ __forceinline__ void operator()(int64_t r1, int64_t r2, const float* x, int, int) const {
     const int64_t R = v * v;
     if (r1 >= R) return;
@@ -366,21 +383,110 @@ struct EpiVvvvSplitB {
     int64_t a = r2 / v, c = r2 - a * v;
 #pragma unroll
     for (int i = 0; i < 16; ++i) {
-      if (a < v) {
-        const __nv_bfloat16 hi = __float2bfloat16(x[i]);
-        const __nv_bfloat16 lo = __float2bfloat16(x[i] - __bfloat162float(hi));
-        __nv_bfloat16* row = B + (a * v + b) * kpo + c * v + d;
-        row[0] = hi;
-        row[R] = lo;
-        row[2 * R] = hi;
-      }
+      if (a < v) put(a, b, c, d, x[i]);
       if (++c == v) {
         c = 0;
         ++a;
       }
     }
   }
+  // Triangle: the GEMM is symmetric (value (r1, r2) = (bd|ac) = (ac|bd) =
+  // value (r2, r1)), so only tiles touching r1 <= r2 run, and each element
+  // with r1 <= r2 is written at (r1, r2) and, for r1 < r2, at its mirror
+  // (r2, r1); elements with r1 > r2 in a diagonal tile are written by their
+  // mirror only, so every element is written once.  The direct stores are
+  // contiguous along the lanes' rows (consecutive d); the mirror's
+  // contiguous index is the column, so the warp's 32 x 16 block goes
+  // through shared memory and each half-warp stores one mirrored row of 16.
+  __device__ __forceinline__ void staged(int64_t r1, int64_t r2, const float* x, float* stg, int lane) const {
+    if (!tri) {
+      (*this)(r1, r2, x, 0, 0);
+      return;
+    }
+    const int64_t R = v * v;
+    if (r1 < R) {
+      const int64_t b = r1 / v, d = r1 - b * v;
+      int64_t a = r2 / v, c = r2 - a * v;
+#pragma unroll
+      for (int i = 0; i < 16; ++i) {
+        if (a < v && r1 <= r2 + i) put(a, b, c, d, x[i]);
+        if (++c == v) {
+          c = 0;
+          ++a;
+        }
+      }
+    }
+    __syncwarp();
+#pragma unroll
+    for (int i = 0; i < 16; ++i) stg[lane * 17 + i] = x[i];
+    __syncwarp();
+    // lane -> column i = lane & 15 of the block, rows j = 2 s + (lane >> 4)
+    const int i = lane & 15;
+    const int64_t q2 = r2 + i;  // (a, c) of the mirror's row and column
+    if (q2 < R) {
+      const int64_t a = q2 / v, c = q2 - a * v;
+      const int64_t q1 = r1 - lane + (lane >> 4);  // the warp's first row, plus this lane's half
+      int64_t b = q1 / v, d = q1 - b * v;
+#pragma unroll 4
+      for (int s = 0; s < 16; ++s) {
+        const int64_t rr1 = q1 + 2 * s;
+        if (rr1 < q2 && rr1 < R) put(b, a, d, c, stg[(2 * s + (lane >> 4)) * 17 + i]);
+        d += 2;
+        while (d >= v) {
+          d -= v;
+          ++b;
+        }
+      }
+    }
+    __syncwarp();
+  }
 };
+
+// Upper-triangle tile enumeration of a symmetric GEMM with BN = 2 BM: tile
+// (mt, nt) holds an element with row <= column iff mt <= 2 nt + 1.  The
+// order is tile_coords' (groups of 16 M tiles, each sweeping its N tiles,
+// M fastest) with the tiles below the diagonal left out; group g's needed
+// tiles start at column 8 g, whose k-th column (k = nt - 8 g) holds
+// min(2 k + 2, gm) of them.
+__host__ __device__ __forceinline__ int tri_group_count(int g, int tiles_m, int tiles_n) {
+  const int gm = min(16, tiles_m - 16 * g);
+  const int kcols = tiles_n - 8 * g;  // columns from 8 g on
+  if (gm <= 0 || kcols <= 0) return 0;
+  const int kf = (gm - 1) / 2;        // first column holding all gm
+  const int kp = min(kcols, kf);      // partial columns present
+  return kp * (kp + 1) + max(0, kcols - kf) * gm;
+}
+
+__host__ __device__ __forceinline__ int tri_count(int tiles_m, int tiles_n) {
+  int n = 0;
+  for (int g = 0; 16 * g < tiles_m; ++g) n += tri_group_count(g, tiles_m, tiles_n);
+  return n;
+}
+
+__host__ __device__ __forceinline__ void tri_coords(int id, int tiles_m, int tiles_n, int& mt, int& nt) {
+  int g = 0;
+  for (;; ++g) {
+    const int cnt = tri_group_count(g, tiles_m, tiles_n);
+    if (id < cnt || 16 * (g + 1) >= tiles_m) break;
+    id -= cnt;
+  }
+  const int gm = min(16, tiles_m - 16 * g);
+  const int kcols = tiles_n - 8 * g;
+  const int kp = min(kcols, (gm - 1) / 2);
+  const int P = kp * (kp + 1);
+  int k;
+  if (id < P) {  // column k holds 2 k + 2 tiles: k (k + 1) <= id < (k + 1)(k + 2)
+    k = (int)((sqrtf(4.0f * (float)id + 1.0f) - 1.0f) * 0.5f);
+    while ((k + 1) * (k + 2) <= id) ++k;
+    while (k * (k + 1) > id) --k;
+    mt = 16 * g + (id - k * (k + 1));
+  } else {
+    id -= P;
+    k = kp + id / gm;
+    mt = 16 * g + id % gm;
+  }
+  nt = 8 * g + k;
+}
 
 // Replicas: `reps` GEMMs of one shape in one launch (work units replica-
 // major); replica r reads A' rows from r * a_rep (0: one A' for all) and B'
@@ -389,6 +495,7 @@ struct EpiVvvvSplitB {
 struct RepTC {
   int reps = 1;
   int a_rep = 0, b_rep = 0;
+  int tri = 0;  // symmetric output, BN = 2 BM, M = N: only the upper-triangle tiles (tri_coords)
 };
 
 template <class TC, class Epi>
@@ -404,7 +511,7 @@ __global__ void __launch_bounds__(NT, 1)
   const uint32_t base = (smem_u32(dsm) + 1023u) & ~1023u;
   const uint32_t sA = base, sB = base + STAGES * A_BYTES;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int ntiles = tiles_m * tiles_n;
+  const int ntiles = rt.tri ? tri_count(tiles_m, tiles_n) : tiles_m * tiles_n;
   const int nk = (K + BK - 1) / BK;
   // split K: work unit u = (tile u % ntiles, K slice u / ntiles), each slice
   // nkc k blocks (the last one shorter, never empty)
@@ -441,7 +548,8 @@ __global__ void __launch_bounds__(NT, 1)
       for (int u = blockIdx.x; u < nunits && !*(volatile int*)&failed; u += gridDim.x) {
         const int rep = u / per_rep, w = u - rep * per_rep;
         int mt, nt;
-        tile_coords(w % ntiles, tiles_m, tiles_n, mt, nt);
+        if (rt.tri) tri_coords(w % ntiles, tiles_m, tiles_n, mt, nt);
+        else tile_coords(w % ntiles, tiles_m, tiles_n, mt, nt);
         const int kb1 = min(nk, (w / ntiles + 1) * nkc);
         for (int kb = (w / ntiles) * nkc; kb < kb1; ++kb, ++g) {
           const int s = g % STAGES;
@@ -516,14 +624,21 @@ __global__ void __launch_bounds__(NT, 1)
       }
       tc_fence_after();
       int mt, nt;
-      tile_coords(w % ntiles, tiles_m, tiles_n, mt, nt);
+      if (rt.tri) tri_coords(w % ntiles, tiles_m, tiles_n, mt, nt);
+        else tile_coords(w % ntiles, tiles_m, tiles_n, mt, nt);
       const int64_t row = (int64_t)mt * BM + quad * 32 + lane;
       const uint32_t lane_base = tmem + ((uint32_t)(quad * 32) << 16) + (uint32_t)(b * BN);
 #pragma unroll 1
       for (int c = half * (BN / 32); c < (half + 1) * (BN / 32); ++c) {
         float v[16];
         tc_ld16(lane_base + (uint32_t)(c * 16), v);
-        epi(row, (int64_t)nt * BN + c * 16, v, w / ntiles, rep);
+        if constexpr (Epi::kStageBytes > 0) {
+          float* stg = reinterpret_cast<float*>(dsm + (base - smem_u32(dsm)) + STAGES * (A_BYTES + B_BYTES)) +
+                       (warp - 2) * 32 * 17;
+          epi.staged(row, (int64_t)nt * BN + c * 16, v, stg, lane);
+        } else {
+          epi(row, (int64_t)nt * BN + c * 16, v, w / ntiles, rep);
+        }
       }
       tc_fence_before();
       __syncwarp();
@@ -676,7 +791,8 @@ int sm_count(int* out) {
 template <class TC, class Epi>
 int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t M, int64_t N, int64_t K,
                 const Epi& epi, cudaStream_t st, unsigned* status, int ksplit, RepTC rt) {
-  constexpr int BN = TC::BN, SMEM_BYTES = TC::SMEM_BYTES;
+  constexpr int BN = TC::BN, SMEM_BYTES = TC::SMEM_BYTES + Epi::kStageBytes;
+  static_assert(SMEM_BYTES <= 227 * 1024, "shared memory");
   if (!A || !B || M <= 0 || N <= 0 || K <= 0 || lda < K || ldb < K || (lda % 8) || (ldb % 8) ||
       (reinterpret_cast<uintptr_t>(A) % 16) || (reinterpret_cast<uintptr_t>(B) % 16)) {
     fricc_set_error("gemm_tc: bad arguments (K-major BF16 operands: 16-byte aligned, ld >= K, ld %% 8 == 0)");
@@ -686,6 +802,10 @@ int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t 
   if (rt.reps < 1 || (rt.a_rep != 0 && rt.a_rep < M) || (rt.b_rep != 0 && rt.b_rep < N) || rt.a_rep < 0 ||
       rt.b_rep < 0) {
     fricc_set_error("gemm_tc: bad replica layout");
+    return FRICC_ERR_ARG;
+  }
+  if (rt.tri && (BN != 2 * BM || M != N || rt.reps != 1)) {
+    fricc_set_error("gemm_tc: the triangle schedule needs BN = 2 BM, M = N and one replica");
     return FRICC_ERR_ARG;
   }
   // the rows of A' and B' over all replicas (TMA coordinates are 32-bit)
@@ -719,13 +839,16 @@ int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t 
   }
   const int64_t nkc = fricc_cdiv(nk, ksplit);
   ksplit = (int)fricc_cdiv(nk, nkc);  // every slice non-empty
-  const int64_t units = tm * tn * ksplit * rt.reps;
+  const int64_t tiles = rt.tri ? tri_count((int)tm, (int)tn) : tm * tn;
+  const int64_t units = tiles * ksplit * rt.reps;
+  // flops the tensor cores run: the triangle's share of M N
+  const double mn = (double)M * (double)N * (double)tiles / (double)(tm * tn);
   const unsigned grid = (unsigned)(units < nsm ? units : nsm);  // persistent: one CTA per SM
   const bool prof = fricc_prof_on();
   if (status) {
     if (prof) fricc_prof_record(st, true, 0.0, 1);
     k_gemm_tc<TC, Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, status, rt);
-    if (prof) fricc_prof_record(st, false, 2.0 * rt.reps * (double)M * (double)N * (double)K, 1);
+    if (prof) fricc_prof_record(st, false, 2.0 * rt.reps * mn * (double)K, 1);
     fricc_note_launch();
     e = cudaGetLastError();
     return e == cudaSuccess ? FRICC_OK : fricc_cuda_fail(e, "gemm_tc", __FILE__, __LINE__);
@@ -737,7 +860,7 @@ int launch_tile(const void* A, int64_t lda, const void* B, int64_t ldb, int64_t 
   if (e == cudaSuccess) {
     if (prof) fricc_prof_record(st, true, 0.0, 1);
     k_gemm_tc<TC, Epi><<<grid, NT, SMEM_BYTES, st>>>(ma, mb, (int)K, (int)tm, (int)tn, ksplit, epi, err, rt);
-    if (prof) fricc_prof_record(st, false, 2.0 * rt.reps * (double)M * (double)N * (double)K, 1);
+    if (prof) fricc_prof_record(st, false, 2.0 * rt.reps * mn * (double)K, 1);
     fricc_note_launch();
     e = cudaGetLastError();
   }
@@ -887,8 +1010,17 @@ int fricc_vvvv_rebuild_split_b(const void* Ap, const void* Bp, int64_t v, int64_
                                       sizeof(__nv_bfloat16) * (kpo - 3 * v * v), v * v, st);
     if (e != cudaSuccess) return fricc_cuda_fail(e, "vvvv_rebuild_split_b padding", __FILE__, __LINE__);
   }
+  // the GEMM is symmetric: above 64 columns (the 256-wide tile) only its
+  // upper-triangle tiles run, each writing its elements and their mirrors
+  if (v * v > 64) {
+    tc::RepTC rt;
+    rt.tri = 1;
+    return tc::launch_tile<tc::Tile<256>>(Ap, kp, Bp, kp, v * v, v * v, kp,
+                                          tc::EpiVvvvSplitB{static_cast<__nv_bfloat16*>(Bout), v, kpo, 1}, st,
+                                          status, 1, rt);
+  }
   return tc::launch(Ap, kp, Bp, kp, v * v, v * v, kp,
-                    tc::EpiVvvvSplitB{static_cast<__nv_bfloat16*>(Bout), v, kpo}, st, status);
+                    tc::EpiVvvvSplitB{static_cast<__nv_bfloat16*>(Bout), v, kpo, 0}, st, status);
 }
 
 }  // extern "C"

@@ -132,6 +132,40 @@ def test_dense_spmm_and_split_b_rebuild(gpulib, systems):
     assert bool(((a - b).abs() <= 2.0 ** -14 * c + 1e-18).all())
 
 
+@pytest.mark.parametrize("o,v", [(3, 17), (4, 40), (5, 80), (6, 131)])
+def test_split_b_rebuild_triangle(gpulib, o, v):
+    """The (vv|vv) rebuild into the B' operand runs only the upper-triangle
+    tiles of its symmetric GEMM and mirrors them: every element of a
+    NaN-filled output is written, B'[(a,b)][(c,d)] equals B'[(b,a)][(d,c)]
+    bit for bit (both written from one computed value), hi + lo is within
+    2^-14 of sum |L||L| of the FP32 rebuild of the whole block, the second
+    hi copy equals the first and the padding columns are zero."""
+    from fricc_gb300.cholesky import VvvvRebuild, _kp
+    g = torch.Generator(device="cuda")
+    g.manual_seed(v)
+    nmo, naux = o + v, 3 * (o + v)
+    A = torch.randn(naux, nmo, nmo, generator=g, device="cuda", dtype=torch.float64) * 0.05
+    Lf = torch.triu(A) + torch.triu(A, 1).transpose(1, 2)
+    R = VvvvRebuild(Lf, o)
+    vv = v * v
+    out = torch.full((vv, _kp(vv)), float("nan"), dtype=torch.bfloat16, device="cuda")
+    Bt = R.rebuild_split_b(out)
+    W = R.rebuild()
+    R.check()
+    torch.cuda.synchronize()
+    assert not bool(torch.isnan(Bt).any())
+    assert torch.equal(Bt[:, :vv], Bt[:, 2 * vv:3 * vv]) and bool((Bt[:, 3 * vv:] == 0).all())
+    B4 = Bt[:, :vv].reshape(v, v, v, v)  # [a, b, c, d]
+    assert torch.equal(B4, B4.permute(1, 0, 3, 2))
+    L4 = Bt[:, vv:2 * vv].reshape(v, v, v, v)
+    assert torch.equal(L4, L4.permute(1, 0, 3, 2))
+    hi, lo = Bt[:, :vv].double(), Bt[:, vv:2 * vv].double()
+    ref = W[:, :vv].double().T  # W[(c,d), (a,b)] = (ac|bd) -> [q=(a,b)][k=(c,d)]
+    Lv = Lf[:, o:, o:].abs()
+    scale = torch.einsum("Pac,Pbd->abcd", Lv, Lv).reshape(vv, vv)
+    assert float(((hi + lo - ref).abs() / scale).max()) < 2.0 ** -14
+
+
 @pytest.mark.parametrize("sums", ["dense", "fp32", "pairs"])
 def test_split_iteration_delta_e_sums(gpulib, systems, sums):
     from fricc_gb300.friccsd import FRICCSDGPU
