@@ -97,7 +97,8 @@ class FusedReplicaBatch:
     from GlibcRand(seeds[r]), in the reference's order (the T2-term
     compression first, then the W-intermediate one)."""
 
-    def __init__(self, eris: D.DeviceERIs, settings: dict, seeds, precision: str = "df64", level_shift: float = 0.0):
+    def __init__(self, eris: D.DeviceERIs, settings: dict, seeds, precision: str = "df64", level_shift: float = 0.0,
+                 graph: bool = False):
         s = {"compression": "fri", "sampling_method": "systematic", "compressed_contractions": ALL_TERMS,
              "unbiased": False}
         s.update(settings)
@@ -150,6 +151,13 @@ class FusedReplicaBatch:
         self.rn_dev = torch.zeros(R, 2, dtype=torch.float64, device=dev)
         self.res = torch.zeros(R, 4, dtype=torch.float64, device=dev)
         self._side_owner = L.OwnStream(dev)
+        # graph=True: the first step runs eagerly (it makes the compressed
+        # handles' bucketings and the first-use operand splits), the second
+        # is captured into one CUDA graph that every later step replays
+        self.graph = bool(graph)
+        self._g = None
+        self._cap_owner = None
+        self._steps = 0
         self.history = [[] for _ in range(R)]
         o, v = self.o, self.v
         e_o = eris.mo_energy[:o].contiguous()
@@ -207,11 +215,43 @@ class FusedReplicaBatch:
         L.check(self.lib.fricc_symadd_b(_ptr(out), _ptr(X), self.R, self.o, self.v, L.i64arr(X.stride()),
                                         float(coef), L.cur_stream()))
 
+    def _capture(self):
+        """One batch step as a CUDA graph on a capture stream of this batch's
+        own: it reads the draws from ``rn_dev`` and the amplitudes from
+        ``t1``/``t2``, and copies the new amplitudes back into them, so each
+        replay advances every replica by one iteration."""
+        from .friccsd import _CAPTURE_LOCK
+        cur = torch.cuda.current_stream()
+        if self._cap_owner is None:
+            self._cap_owner = L.OwnStream(self.E.device)
+        cap = self._cap_owner.stream
+        g = torch.cuda.CUDAGraph()
+        with _CAPTURE_LOCK:
+            cap.wait_stream(cur)
+            with torch.cuda.stream(cap):
+                g.capture_begin(capture_error_mode="thread_local")
+                try:
+                    t1n, t2n = self._update(self.t1, self.t2)
+                    self.t1.copy_(t1n)
+                    self.t2.copy_(t2n)
+                    del t1n, t2n
+                finally:
+                    g.capture_end()
+            cur.wait_stream(cap)
+        self._g = g
+
     def step(self, record: bool = True):
-        """One iteration of every replica."""
+        """One iteration of every replica (with ``graph``, a replay of the
+        captured batch step from the second step on)."""
         rn = [[g(), g()] for g in self.rng]
         self.rn_dev.copy_(torch.tensor(rn, dtype=torch.float64))
-        self.t1, self.t2 = self._update(self.t1, self.t2)
+        if self.graph and self._steps > 0:
+            if self._g is None:
+                self._capture()
+            self._g.replay()
+        else:
+            self.t1, self.t2 = self._update(self.t1, self.t2)
+        self._steps += 1
         r = self.res[:, :2].cpu()
         rep = ctypes.c_int(-1)
         rc = self.lib.fricc_spb_status(self.spb, ctypes.byref(rep))

@@ -44,7 +44,7 @@ def run_replicas(args):
     seeds = [1000 + r for r in range(args.replicas)]
     if args.fused:
         from .replicas import FusedReplicaBatch
-        batch = FusedReplicaBatch(E, settings, seeds, precision=args.precision)
+        batch = FusedReplicaBatch(E, settings, seeds, precision=args.precision, graph=args.graph)
     else:
         batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision,
                              graph=args.graph and not args.batch_graph)
@@ -65,7 +65,7 @@ def run_replicas(args):
     return {"mode": "replicas", "workload": "o20v100: nocc=20 nvir=100 naux=600 m=200000 per replica",
             "replicas": args.replicas, "streams": 1 if args.fused else args.streams, "precision": args.precision,
             "form": "fused: one launch per kernel for all replicas" if args.fused else "one solver per replica",
-            "graph": "one graph per batch step" if args.batch_graph else args.graph,
+            "graph": ("one graph per batch step" if args.batch_graph or (args.fused and args.graph) else args.graph),
             "iterations_per_s": args.replicas * args.steps / dt, "batch_steps_per_s": args.steps / dt,
             "e_corr_mean": mean, "e_corr_var": var, "iterations_each": args.warmup + args.steps,
             "trace_after_warmup": {"mean_of_means": float(tmeans.mean()), "mcmc_std_median": float(np.median(terrs)),
@@ -155,7 +155,8 @@ def main():
                    help="split precision: rebuild (vv|vv) once per solve instead of every iteration")
     p.add_argument("--host-inputs", action="store_true",
                    help="draw each request's synthetic system with numpy on the host (default: on the GPU)")
-    p.add_argument("--graph", action="store_true", help="replay each solver's iteration from a CUDA graph")
+    p.add_argument("--graph", action="store_true",
+                   help="replay each solver's iteration from a CUDA graph (--fused: the whole batch step, one graph)")
     p.add_argument("--batch-graph", action="store_true",
                    help="replicas: capture every replica's iteration into one CUDA graph per batch step")
     p.add_argument("--fused", action="store_true",

@@ -193,3 +193,27 @@ def test_fused_split_declines_terms_too_small_for_the_tensor_cores(gpulib):
     E = split_eris(SyntheticSystem(6, 24, 120, 0.05, 3))
     with pytest.raises(ValueError):
         FusedReplicaBatch(E, {"m_keep": 3000}, [1, 2], precision="split")
+
+
+@pytest.mark.parametrize("precision", ["df64", "split"])
+def test_fused_replicas_graph_replays_equal_eager(gpulib, precision):
+    """graph=True: the first batch step eager, the second captured into one
+    CUDA graph and every later step a replay of it; each replica's E_corr at
+    every step and t1, t2 after four steps are bit for bit the eager batch's."""
+    from fricc_gb300.replicas import FusedReplicaBatch
+    from fricc_gb300.synthetic import SyntheticSystem
+    if precision == "split":
+        from fricc_gb300.cholesky import split_eris
+        E, m = split_eris(SyntheticSystem(10, 80, 400, 0.05, 3)), 32000
+    else:
+        from fricc_gb300.rccsd_dense import DeviceERIs
+        E, m = DeviceERIs.from_system(SyntheticSystem(6, 24, 120, 0.05, 3)), 3000
+    seeds, steps = [7, 11, 12345], 4
+    eager = FusedReplicaBatch(E, {"m_keep": m}, seeds, precision=precision)
+    graph = FusedReplicaBatch(E, {"m_keep": m}, seeds, precision=precision, graph=True)
+    for _ in range(steps):
+        eager.step()
+        graph.step()
+    assert graph._g is not None
+    assert graph.history == eager.history
+    assert torch.equal(_bits(graph.t1), _bits(eager.t1)) and torch.equal(_bits(graph.t2), _bits(eager.t2))
