@@ -100,7 +100,7 @@ static cudaEvent_t g_prof_pending[kProfChannels] = {nullptr, nullptr, nullptr};
 
 void fricc_note_launch(int n) { g_launches.fetch_add(n, std::memory_order_relaxed); }
 
-static thread_local int g_tune[FRICC_TUNE_KNOBS] = {-1, -1, -1, -1, -1};
+static thread_local int g_tune[FRICC_TUNE_KNOBS] = {-1, -1, -1, -1, -1, -1};
 int fricc_tune_get(int knob) { return knob >= 0 && knob < FRICC_TUNE_KNOBS ? g_tune[knob] : -1; }
 bool fricc_prof_on() { return g_prof.load(std::memory_order_relaxed); }
 
@@ -190,7 +190,7 @@ long long fricc_launch_count(void) { return g_launches.load(); }
 long long fricc_alloc_count(void) { return g_allocs.load(); }
 
 int fricc_tune_set(int knob, int value) {
-  static const int lo[FRICC_TUNE_KNOBS] = {1, 0, 1, 1, 10}, hi[FRICC_TUNE_KNOBS] = {4, 4, 16, 1 << 20, 13};
+  static const int lo[FRICC_TUNE_KNOBS] = {1, 0, 1, 1, 10, 1}, hi[FRICC_TUNE_KNOBS] = {4, 4, 16, 1 << 20, 13, 8};
   if (knob < 0 || knob >= FRICC_TUNE_KNOBS || (value != -1 && (value < lo[knob] || value > hi[knob]))) {
     fricc_set_error("tune_set: bad knob or value");
     return FRICC_ERR_ARG;

@@ -121,7 +121,10 @@ void fricc_note_launch(int n = 1);
 // the width in bits (10..13) of a compression's first select digit, which
 // decides how many candidates the exact sort takes (never which are kept)
 #define FRICC_TUNE_SELECT_BITS 4
-#define FRICC_TUNE_KNOBS 5
+// the float-pair sparse kernel as a persistent, q-tile-major launch of this
+// many CTAs per SM (1..8; unset: one CTA per (bucket, q tile) item)
+#define FRICC_TUNE_SPMM_PERSIST 5
+#define FRICC_TUNE_KNOBS 6
 int fricc_tune_get(int knob);
 bool fricc_prof_on();
 void fricc_prof_record(cudaStream_t st, bool start, double flops, int channel = 0);

@@ -253,30 +253,16 @@ __device__ __forceinline__ void df_tile(const int* __restrict__ srow, const ulon
   }
 }
 
-// At least 8 CTAs per SM (a 64-register cap): measured 6% less time in
-// this kernel over the o30v150 terms than the compiler's own register choice
-// (62), which left the same occupancy but scheduled the loads worse.
+// One (bucket P, q tile qt) work item of the float-pair sparse kernel:
+// out'[P][q tile] += sum over the bucket's entries, staged DF_NT at a time.
 template <int DF_PPT>
-__global__ void __launch_bounds__(DF_NT, 8) k_spmm_df(const int* __restrict__ bptr, const int* __restrict__ erow,
-                                                   const float2* __restrict__ eval, const float4* __restrict__ Wp4,
-                                                   double* __restrict__ Op, int64_t QS, int qtile0,
-                                                   RepC rp = RepC{}) {
-  {
-    const int64_t r = blockIdx.z;
-    bptr += r * rp.b;
-    erow += r * rp.m;
-    eval += r * rp.m;
-    Wp4 += r * rp.w;
-    Op += r * rp.o;
-  }
-  __shared__ int srow[DF_NT];
-  __shared__ ulonglong2 sv[DF_NT];
-  __shared__ f32x2 snv[DF_NT];
-  const int64_t P = blockIdx.x;
+__device__ __forceinline__ void spmm_df_item(int64_t P, int64_t qt, const int* __restrict__ bptr,
+                                             const int* __restrict__ erow, const float2* __restrict__ eval,
+                                             const float4* __restrict__ Wp4, double* __restrict__ Op, int64_t QS,
+                                             int* srow, ulonglong2* sv, f32x2* snv) {
   const int e0 = bptr[P], e1 = bptr[P + 1];
   if (e0 == e1) return;
   const int64_t QS2 = (QS + 1) >> 1;
-  const int64_t qt = (int64_t)blockIdx.y + qtile0;
   const int64_t t0 = qt * (DF_NT * DF_PPT) + threadIdx.x;
   const int64_t trem = QS2 - t0;  // this thread's pairs are t0 + k*DF_NT < QS2  <=>  k*DF_NT < trem
   const bool full = (qt + 1) * (DF_NT * DF_PPT) <= QS2;  // uniform per block
@@ -317,6 +303,55 @@ __global__ void __launch_bounds__(DF_NT, 8) k_spmm_df(const int* __restrict__ bp
     const float2 h = upk2(ah[k]), l = upk2(al[k]);
     if (q < QS) orow[q] = pair_to_f64(h.x, l.x);
     if (q + 1 < QS) orow[q + 1] = pair_to_f64(h.y, l.y);
+  }
+}
+
+// At least 8 CTAs per SM (a 64-register cap): measured 6% less time in
+// this kernel over the o30v150 terms than the compiler's own register choice
+// (62), which left the same occupancy but scheduled the loads worse.
+template <int DF_PPT>
+__global__ void __launch_bounds__(DF_NT, 8) k_spmm_df(const int* __restrict__ bptr, const int* __restrict__ erow,
+                                                   const float2* __restrict__ eval, const float4* __restrict__ Wp4,
+                                                   double* __restrict__ Op, int64_t QS, int qtile0,
+                                                   RepC rp = RepC{}) {
+  {
+    const int64_t r = blockIdx.z;
+    bptr += r * rp.b;
+    erow += r * rp.m;
+    eval += r * rp.m;
+    Wp4 += r * rp.w;
+    Op += r * rp.o;
+  }
+  __shared__ int srow[DF_NT];
+  __shared__ ulonglong2 sv[DF_NT];
+  __shared__ f32x2 snv[DF_NT];
+  spmm_df_item<DF_PPT>(blockIdx.x, (int64_t)blockIdx.y + qtile0, bptr, erow, eval, Wp4, Op, QS, srow, sv, snv);
+}
+
+// Persistent form: gridDim.x CTAs take (bucket, q tile) items from a
+// counter in q-tile-major order (all buckets of q tile 0, then q tile 1,
+// ...), so the W' columns in use at once are those of the items the
+// resident CTAs hold -- a window set by the grid size rather than by the
+// hardware's occupancy.  Same arithmetic and order per output as k_spmm_df.
+template <int DF_PPT>
+__global__ void __launch_bounds__(DF_NT, 8) k_spmm_df_persist(const int* __restrict__ bptr,
+                                                           const int* __restrict__ erow,
+                                                           const float2* __restrict__ eval,
+                                                           const float4* __restrict__ Wp4, double* __restrict__ Op,
+                                                           int64_t QS, int64_t nb, int64_t nitems,
+                                                           unsigned long long* __restrict__ counter) {
+  __shared__ int srow[DF_NT];
+  __shared__ ulonglong2 sv[DF_NT];
+  __shared__ f32x2 snv[DF_NT];
+  __shared__ long long item;
+  for (;;) {
+    __syncthreads();  // the previous item's staged entries are no longer read
+    if (threadIdx.x == 0) item = (long long)atomicAdd(counter, 1ull);
+    __syncthreads();
+    const long long w = item;
+    if (w >= nitems) return;
+    const int64_t qt = w / nb;
+    spmm_df_item<DF_PPT>(w - qt * nb, qt, bptr, erow, eval, Wp4, Op, QS, srow, sv, snv);
   }
 }
 
@@ -790,10 +825,29 @@ int fricc_spmm_f2_device(FriccSparse* T, int pa, int pb, int ka, int kb, double 
     // once exceed L2 and DRAM sees ~9x the W' bytes, yet only 1.6 TB/s;
     // launching one q tile at a time cut that traffic 6x but ran 50% longer
     // (900-CTA launches leave SMs idle at each tail), so it is not done.
-    const dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq);
-    if (ppt == 1) k_spmm_df<1><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
-    else if (ppt == 4) k_spmm_df<4><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
-    else k_spmm_df<2><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
+    const int persist = fricc_tune_get(FRICC_TUNE_SPMM_PERSIST);
+    if (persist > 0) {
+      // persistent, q-tile-major: `persist` CTAs per SM
+      unsigned long long* ctr = nullptr;
+      rc = fricc_alloc_t(&ctr, 1, st);
+      int nsm = 0;
+      if (!rc) rc = fricc_cuda_check(cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, T->device), "sm count");
+      if (!rc) rc = fricc_cuda_check(cudaMemsetAsync(ctr, 0, sizeof(unsigned long long), st), "counter");
+      if (!rc) {
+        const int64_t nitems = bk->nbuckets * ntq;
+        const int64_t g64 = (int64_t)nsm * (persist > 8 ? 8 : persist);
+        const unsigned g = (unsigned)(g64 < nitems ? g64 : nitems);
+        if (ppt == 1) k_spmm_df_persist<1><<<g, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, bk->nbuckets, nitems, ctr);
+        else if (ppt == 4) k_spmm_df_persist<4><<<g, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, bk->nbuckets, nitems, ctr);
+        else k_spmm_df_persist<2><<<g, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, bk->nbuckets, nitems, ctr);
+      }
+      fricc_free(ctr, st);
+    } else {
+      const dim3 grid((unsigned)bk->nbuckets, (unsigned)ntq);
+      if (ppt == 1) k_spmm_df<1><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
+      else if (ppt == 4) k_spmm_df<4><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
+      else k_spmm_df<2><<<grid, DF_NT, 0, st>>>(bk->bptr, erow, eval, Wp, Op, QS, 0);
+    }
     fricc_note_launch();
     if (prof) fricc_prof_record(st, false, 2.0 * (double)T->m * (double)QS);
     fricc_note_launch();

@@ -489,8 +489,11 @@ int fricc_stream_destroy(void* stream);
  * default 12) of a compression's first select digit -- how many candidates
  * the exact sort of the top-m selection (argsort / get_d_largest,
  * src/fri_utils.cpp:11-36,400-437) takes; every width keeps the same
- * entries.  No knob changes a result's arithmetic except the GEMMs' tile
- * and split, which reorder their sums. */
+ * entries; knob 5: the float-pair sparse kernel as a persistent launch of
+ * this many CTAs per SM (1..8) taking its (bucket, q tile) items in
+ * q-tile-major order (unset: one CTA per item).  No knob changes a
+ * result's arithmetic except the GEMMs' tile and split, which reorder
+ * their sums. */
 int fricc_tune_set(int knob, int value);
 
 /* Instrumentation (no reference counterpart): the number of kernels this
