@@ -21,10 +21,13 @@ import torch
 
 from . import _lib as L
 
-SPMM_PPT, GEMM_TILE, GEMM_COVER, SELECT_BITS = 0, 1, 2, 4
+SPMM_PPT, GEMM_TILE, GEMM_COVER, SELECT_BITS, SPMM_PERSIST = 0, 1, 2, 4, 5
 
-# candidate configurations: {knob: value}; {} is the library's own choice
-SPMM_CANDIDATES = [{SPMM_PPT: p} for p in (1, 2, 4)]
+# candidate configurations: {knob: value}; {} is the library's own choice.
+# The sparse kernel's gather tiles: pairs per thread (the q tile of a CTA is
+# 256 x that many outputs), each as one CTA per (bucket, q tile) item or as
+# a persistent q-tile-major launch of 8 CTAs per SM
+SPMM_CANDIDATES = [{SPMM_PPT: p} for p in (1, 2, 4)] + [{SPMM_PPT: p, SPMM_PERSIST: 8} for p in (1, 2)]
 GEMM_CANDIDATES = [{}] + [{GEMM_TILE: t, GEMM_COVER: c} for t, c in itertools.product(range(5), (2, 4, 8))]
 # the compression's top-m selection schedule: the first select digit's width
 # (candidates left for the exact sort), 12 bits by default

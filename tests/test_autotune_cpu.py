@@ -34,7 +34,7 @@ def test_picks_fastest_and_replays(monkeypatch):
     assert tuner.best["k"] == {AT.SPMM_PPT: 2}
     # every candidate ran on scratch (warm-up + 2 timed), then the chosen one on the real output
     assert launches[-1] == (2, True) and sum(1 for _, real in launches if real) == 1
-    assert len(launches) == 3 * 3 + 1
+    assert len(launches) == len(AT.SPMM_CANDIDATES) * 3 + 1
     n = len(launches)
     tuner.run("k", AT.SPMM_CANDIDATES, launch, [out])  # replay: one launch, no timing
     assert launches[n:] == [(2, True)]
@@ -57,7 +57,8 @@ class _Ctx:
 
 
 def test_candidate_sets():
-    assert {tuple(c.items()) for c in AT.SPMM_CANDIDATES} == {((0, 1),), ((0, 2),), ((0, 4),)}
+    assert {tuple(sorted(c.items())) for c in AT.SPMM_CANDIDATES} == {((0, 1),), ((0, 2),), ((0, 4),), ((0, 1), (5, 8)),
+                                                                     ((0, 2), (5, 8))}
     assert AT.GEMM_CANDIDATES[0] == {} and len(AT.GEMM_CANDIDATES) == 16
     assert [c[AT.SELECT_BITS] for c in AT.COMPRESS_CANDIDATES] == [10, 11, 12, 13]
 
@@ -68,11 +69,13 @@ def test_tune_set_checks_arguments():
     assert lib.fricc_tune_set(0, 4) == 0 and lib.fricc_tune_set(0, -1) == 0
     assert lib.fricc_tune_set(0, 3) == 1   # pairs per thread: 1, 2 or 4
     assert lib.fricc_tune_set(1, 5) == 1   # five tiles, 0..4
+    assert lib.fricc_tune_set(5, 8) == 0 and lib.fricc_tune_set(5, -1) == 0
+    assert lib.fricc_tune_set(5, 9) == 1 and lib.fricc_tune_set(5, 0) == 1   # persistent: 1..8 CTAs per SM
     assert lib.fricc_tune_set(2, 17) == 1  # cover 1..16
     assert lib.fricc_tune_set(3, 0) == 1   # the test-only wait: 1..2^20 polls
     assert lib.fricc_tune_set(3, 1 << 21) == 1
     assert lib.fricc_tune_set(3, 5) == 0 and lib.fricc_tune_set(3, -1) == 0
     assert lib.fricc_tune_set(4, 9) == 1 and lib.fricc_tune_set(4, 14) == 1   # select digit: 10..13 bits
     assert lib.fricc_tune_set(4, 13) == 0 and lib.fricc_tune_set(4, -1) == 0
-    assert lib.fricc_tune_set(5, 1) == 1   # no such knob
+    assert lib.fricc_tune_set(6, 1) == 1   # no such knob
     assert lib.fricc_tune_set(1, 4) == 0 and lib.fricc_tune_set(1, -1) == 0

@@ -26,14 +26,19 @@ def test_spmm_ppt_knob_bit_identical(gpulib):
     W2 = split_f2(W, QS)
     st = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     outs = []
+    # pairs per thread, each as a grid launch (knob 5 unset) and as the
+    # persistent q-tile-major launch at 1, 3 and 8 CTAs per SM
     for ppt in (1, 2, 4):
-        L.check(gpulib.fricc_tune_set(0, ppt))
-        o_ = torch.zeros(o * o, QS, dtype=torch.float64, device="cuda")
-        L.check(gpulib.fricc_spmm_f2(T.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(W2.data_ptr()), QS,
-                                     ctypes.c_void_p(o_.data_ptr()), st))
-        outs.append(o_)
+        for persist in (-1, 1, 3, 8):
+            L.check(gpulib.fricc_tune_set(0, ppt))
+            L.check(gpulib.fricc_tune_set(5, persist))
+            o_ = torch.zeros(o * o, QS, dtype=torch.float64, device="cuda")
+            L.check(gpulib.fricc_spmm_f2(T.handle, 0, 1, 2, 3, 1.0, ctypes.c_void_p(W2.data_ptr()), QS,
+                                         ctypes.c_void_p(o_.data_ptr()), st))
+            outs.append(o_)
     L.check(gpulib.fricc_tune_set(0, -1))
-    assert torch.equal(outs[0], outs[1]) and torch.equal(outs[1], outs[2])
+    L.check(gpulib.fricc_tune_set(5, -1))
+    assert all(torch.equal(outs[0], x) for x in outs[1:])
 
 
 @pytest.mark.parametrize("shape,m", [((8, 8, 40, 40), 20000), ((12, 12, 50, 50), 90000)])
