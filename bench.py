@@ -54,9 +54,11 @@ FP64_PEAK_FALLBACK = 1.2557
 FP32_PEAK_FALLBACK = 74.2
 # DRAM bytes (read + write) per launch of the dominant sparse kernel, from
 # one single-pass ncu capture (dram__bytes_read.sum + dram__bytes_write.sum)
-# of a whole o30v150 iteration: a constant, not measured by this run.
-# Keys: (precision, workload) -> {term: bytes per launch}.
+# of a whole o30v150 iteration: constants, not measured by this run.
+# Keys: (precision, workload) -> {term: bytes per launch}; "mean" is the
+# mean over the iteration's launches of that kernel.
 SPMM_TRAFFIC_CAPTURED = {
+    ("fp64", "o30v150"): {"mean": 3.97e9, "2323": 26.0e9, "XY": 9.64e9, "O3V3": 0.54e9},
     ("df64", "o30v150"): {"2323": 36.1e9, "XY": 13.85e9},
 }
 
@@ -533,10 +535,12 @@ def run_gpu(args):
     roof = {"kernel": kname, "bound": bound,
             "achieved": achieved, "peak": peak, "unit": "TFLOP/s",
             "frac": (achieved / peak) if achieved else None,
-            "traffic": None,
+            "traffic": traffic.get("mean") if traffic else None,
             "traffic_per_launch_captured": traffic,
-            "traffic_note": ("DRAM bytes per launch are not measured live; the captured figures (when present) "
-                             "come from one single-pass ncu capture of an iteration of this workload"),
+            "traffic_note": ("DRAM bytes per launch (mean over the iteration's launches of the kernel) from one "
+                             "single-pass ncu capture of an iteration of this workload with this build, not measured "
+                             "by this run; the 2323 launch re-reads its W' (algorithmic 4.37 GB) ~6x without "
+                             "costing time: the kernel is bound by the FP64 pipe, not DRAM"),
             "flops_counted": "2 m Q per launch (m nonzeros, Q outputs per nonzero): algorithmic, no padding",
             "launches": int(p_n.value), "kernel_ms": p_ms.value,
             "kernel_share_of_step": p_ms.value / ms if ms > 0 else None,
