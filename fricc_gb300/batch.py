@@ -418,39 +418,55 @@ class SolveServer:
                 built.put(None)
 
         def scheduler():
-            torch.cuda.set_device(self.device)
             active = []
             open_builders = self.n_builders
-            while open_builders or active:
-                while True:  # requests built since the last pass join
-                    try:
-                        lv = built.get_nowait() if active or not open_builders else built.get(timeout=0.05)
-                    except queue.Empty:
-                        break
+            try:
+                torch.cuda.set_device(self.device)
+                while open_builders or active:
+                    while True:  # requests built since the last pass join
+                        try:
+                            lv = built.get_nowait() if active or not open_builders else built.get(timeout=0.05)
+                        except queue.Empty:
+                            break
+                        if lv is None:
+                            open_builders -= 1
+                        else:
+                            active.append(lv)
+                    progressed = False
+                    for lv in list(active):
+                        if lv.event is not None and not lv.event.query():
+                            continue
+                        progressed = True
+                        try:
+                            done = lv.event is None or self._settle(lv)
+                            if not done:
+                                self._issue(lv)
+                                continue
+                            self._close(lv)
+                        except BaseException as e:
+                            errors.append(e)
+                        lv.req.finished = time.perf_counter() - t0
+                        active.remove(lv)
+                        if lv.solver is None:  # closed: its stream is idle
+                            self._give_stream(lv.owner)
+                        self._release(lv.req)
+                    if active and not progressed:
+                        time.sleep(2e-4)
+            except BaseException as e:
+                # the scheduler itself failed (e.g. a device error seen by an
+                # event query): hand back every live request so that the
+                # dispatcher and the builders run to their end
+                errors.append(e)
+                for lv in active:
+                    lv.req.finished = time.perf_counter() - t0
+                    self._release(lv.req)
+                while open_builders:
+                    lv = built.get()
                     if lv is None:
                         open_builders -= 1
                     else:
-                        active.append(lv)
-                progressed = False
-                for lv in list(active):
-                    if lv.event is not None and not lv.event.query():
-                        continue
-                    progressed = True
-                    try:
-                        done = lv.event is None or self._settle(lv)
-                        if not done:
-                            self._issue(lv)
-                            continue
-                        self._close(lv)
-                    except BaseException as e:
-                        errors.append(e)
-                    lv.req.finished = time.perf_counter() - t0
-                    active.remove(lv)
-                    if lv.solver is None:  # closed: its stream is idle
-                        self._give_stream(lv.owner)
-                    self._release(lv.req)
-                if active and not progressed:
-                    time.sleep(2e-4)
+                        lv.req.finished = time.perf_counter() - t0
+                        self._release(lv.req)
 
         if iterations:
             th = ([threading.Thread(target=dispatcher), threading.Thread(target=scheduler)]

@@ -161,3 +161,40 @@ def test_iteration_scheduler_interleaves_requests(monkeypatch):
     later = [rid for _, rid, it in log if it > 0]
     switches = sum(a != b for a, b in zip(later, later[1:]))
     assert switches > len(set(later))                        # requests' iterations interleave
+
+
+def test_iteration_scheduler_failure_releases_every_request(monkeypatch):
+    """A failure inside the scheduler's own loop (here: the event query of a
+    request's iteration raises, as it would after a device error) ends the
+    run with that error instead of leaving the dispatcher waiting for HBM
+    that no request gives back (device work faked on CPU)."""
+    import time
+
+    from fricc_gb300 import batch as B
+    monkeypatch.setattr(B.torch.cuda, "set_device", lambda d: None)
+
+    class BadEvent:
+        def query(self):
+            raise RuntimeError("device error seen by the event query")
+
+    class FakeOwn:
+        stream = None
+
+    def fake_build(self, req, t0, stream):
+        req.started = time.perf_counter() - t0
+        return B._Live(req, object(), None, stream, None, None, 0.0, time.perf_counter())
+
+    def fake_issue(self, lv):
+        lv.event = BadEvent()
+
+    monkeypatch.setattr(B.SolveServer, "_build", fake_build)
+    monkeypatch.setattr(B.SolveServer, "_issue", fake_issue)
+    monkeypatch.setattr(B.SolveServer, "_take_stream", lambda self: FakeOwn())
+    reqs = request_stream(12, rate=5000.0, seed=2, nocc=(5, 8))
+    budget = 3 * max(B.footprint_bytes(r.nocc, r.nvir, "split") for r in reqs)
+    srv = B.SolveServer(precision="split", device="cuda:0", schedule="iterations", max_active=2, n_builders=2,
+                        hbm_budget=budget)
+    import pytest
+    with pytest.raises(RuntimeError, match="device error"):
+        srv.run(reqs, time_scale=0.0)
+    assert srv._in_use == 0 and srv._n_live == 0
