@@ -48,6 +48,7 @@ def run_replicas(args):
     else:
         batch = ReplicaBatch(E, settings, seeds, n_streams=args.streams, precision=args.precision,
                              graph=args.graph and not args.batch_graph)
+    hist = batch.history
     step = batch.step
     for i in range(args.warmup):
         step()
@@ -62,6 +63,18 @@ def run_replicas(args):
     mean, var = batch.stats()
     burn = min(args.warmup, len(batch.history[0]) - 2)
     tmeans, terrs, taus = batch.trace_stats(burn=max(burn, 0))
+    vs_fp64 = None
+    if args.vs_fp64 and args.precision != "fp64":
+        # the same replicas (same seeds, same number of steps) in FP64: every
+        # replica's E_corr at every step against the FP64 batch's
+        from .replicas import FusedReplicaBatch
+        E64 = DeviceERIs.from_system(system)
+        ref = FusedReplicaBatch(E64, settings, seeds, precision="fp64")
+        for _ in range(args.warmup + args.steps):
+            ref.step()
+        d = np.abs(np.array(hist) - np.array(ref.history))
+        vs_fp64 = {"max_abs_dE_any_step": float(d.max()), "max_abs_dE_first_step": float(d[:, 0].max()),
+                   "steps": int(d.shape[1])}
     return {"mode": "replicas", "workload": "o20v100: nocc=20 nvir=100 naux=600 m=200000 per replica",
             "replicas": args.replicas, "streams": 1 if args.fused else args.streams, "precision": args.precision,
             "form": "fused: one launch per kernel for all replicas" if args.fused else "one solver per replica",
@@ -69,7 +82,8 @@ def run_replicas(args):
             "iterations_per_s": args.replicas * args.steps / dt, "batch_steps_per_s": args.steps / dt,
             "e_corr_mean": mean, "e_corr_var": var, "iterations_each": args.warmup + args.steps,
             "trace_after_warmup": {"mean_of_means": float(tmeans.mean()), "mcmc_std_median": float(np.median(terrs)),
-                                   "tau_median": float(np.median(taus))}}
+                                   "tau_median": float(np.median(taus))},
+            "vs_fp64": vs_fp64}
 
 
 def _warm(server, args):
@@ -159,6 +173,8 @@ def main():
                    help="replay each solver's iteration from a CUDA graph (--fused: the whole batch step, one graph)")
     p.add_argument("--batch-graph", action="store_true",
                    help="replicas: capture every replica's iteration into one CUDA graph per batch step")
+    p.add_argument("--vs-fp64", action="store_true",
+                   help="replicas: afterwards run the same replicas in FP64 (fused) and report |dE_corr| per step")
     p.add_argument("--fused", action="store_true",
                    help="replicas: one launch per kernel for the whole batch (fp64, df64 or split)")
     args = p.parse_args()
