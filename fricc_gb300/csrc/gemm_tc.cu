@@ -203,6 +203,13 @@ struct EpiStridedF64 {
   double alpha, beta;
   int64_t srep;  // C offset of replica r: r * srep
   int beta0;     // beta == 0 (decided on the host: no per-element FP64 compare)
+  // The cases of alpha and beta, decided on the host: GB300's FP64 unit runs
+  // 2 operations per SM per clock, so a tile's 32K outputs cost ~16 us of
+  // FP64 work at one multiply and one FMA each, far above the MMA time of
+  // a GEMM with a short K.  amode 0: alpha = 1, 1: alpha = -1 (a sign-bit
+  // flip), 2: alpha x.  bmode 0: beta = 0, 1: beta = 1 (one add), 2: beta C
+  // (one FMA).  Each case gives the bits of alpha * x + beta * C.
+  int amode = 2, bmode = 2;
   __device__ __forceinline__ void operator()(int64_t r, int64_t c0, const float* v, int, int rep) const {
     if (r >= M) return;
     const int64_t ro = r / mi;
@@ -212,8 +219,12 @@ struct EpiStridedF64 {
     for (int i = 0; i < 16; ++i) {
       if (c0 + i < N) {
         double* p = C + rbase + co * sco + ci * sci;
-        const double x = alpha * f2d_bits(v[i]);
-        *p = beta0 ? x : x + beta * *p;
+        double x = f2d_bits(v[i]);
+        if (amode == 1) x = __longlong_as_double(__double_as_longlong(x) ^ (long long)0x8000000000000000ull);
+        else if (amode == 2) x = alpha * x;
+        if (bmode == 0) *p = x;
+        else if (bmode == 1) *p = x + *p;
+        else *p = fma(beta, *p, x);
       }
       if (++ci == ni) {
         ci = 0;
@@ -948,7 +959,9 @@ int fricc_gemm_bf16_tn_strided_b(const void* A, int64_t lda, const void* B, int6
     fricc_set_error("gemm_bf16_tn_strided: bad output, split or replica layout");
     return FRICC_ERR_ARG;
   }
-  const tc::EpiStridedF64 out{C, M, N, mi, ni, sro, sri, sco, sci, alpha, beta, c_rep, beta == 0.0 ? 1 : 0};
+  tc::EpiStridedF64 out{C, M, N, mi, ni, sro, sri, sco, sci, alpha, beta, c_rep, beta == 0.0 ? 1 : 0};
+  out.amode = alpha == 1.0 ? 0 : (alpha == -1.0 ? 1 : 2);
+  out.bmode = beta == 0.0 ? 0 : (beta == 1.0 ? 1 : 2);
   tc::RepTC rt;
   rt.reps = reps;
   rt.a_rep = (int)a_rep;
