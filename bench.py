@@ -14,7 +14,9 @@ figures, each with its |dE_corr| against the FP64 path for one step.
 
 --impl gb300 (default): the CUDA path.  value = iterations/s with everything
 resident in HBM; e2e = the same step through the host entry point
-(update_amps_host: numpy amplitudes in, numpy out, copies timed).
+(update_amps_host: numpy amplitudes in, numpy out, copies timed);
+served_form = a short served request stream (the metric's solves/s against
+the plain FP64 form and p50/p99 latency; --served-requests, 0 to skip).
 --impl reference: the reference algorithm on the host cores (the oracle port
 of fri-cc's C++ plus numpy for the dense algebra).  Warm-up steps are
 sampled iterations: both compressions in full, the dense algebra in full,
@@ -89,6 +91,8 @@ def parse():
     p.add_argument("--workload", default="o30v150")
     p.add_argument("--no-cpu-baseline", action="store_true")
     p.add_argument("--no-e2e", action="store_true")
+    p.add_argument("--served-requests", type=int, default=150,
+                   help="requests of the served-stream sample reported as served_form (0: none)")
     p.add_argument("--no-secondary", action="store_true",
                    help="skip the secondary measurements of the other arithmetic forms")
     p.add_argument("--no-peak-probe", action="store_true",
@@ -309,6 +313,36 @@ def cpu_baseline_line(eris_np, t1, t2, m, workload, seed, n_blocks=10, blocks=(0
             + f" (blocks {list(blocks)}; {secs:.1f} s/iteration estimated)"}
 
 
+def served_sample(n_requests: int, timeout_s: float = 420.0) -> dict:
+    """The served form on a short stream of the request distribution (split
+    precision, iteration-level scheduling) beside the plain FP64 form on
+    every 10th of the same requests, one at a time: solves/s, p50/p99 time
+    to converged energy and the largest |dE_corr| against the plain form.
+    Runs in a child process (its own allocator settings; a failure there
+    is reported, never fatal to the headline)."""
+    cmd = [sys.executable, "-m", "fricc_gb300.serve_bench", "--mode", "serve", "--requests", str(n_requests),
+           "--rate", "50", "--precision", "split", "--schedule", "iterations", "--max-active", "8", "--plain",
+           "--plain-every", "10"]
+    try:
+        r = subprocess.run(cmd, cwd=REPO, capture_output=True, text=True, timeout=timeout_s)
+        lines = [ln for ln in r.stdout.splitlines() if ln.startswith("{")]
+        if r.returncode != 0 or not lines:
+            return {"error": f"serve_bench rc {r.returncode}: {r.stderr[-300:]}"}
+        d = json.loads(lines[-1])
+    except Exception as ex:
+        return {"error": f"{type(ex).__name__}: {str(ex)[:300]}"}
+    sv, pl = d["served"], d["plain"]
+    return {"unit": "solves/s", "solves_per_s": sv["solves_per_s"], "p50_s": sv["p50_s"], "p99_s": sv["p99_s"],
+            "plain_fp64_solves_per_s": pl["solves_per_s"], "speedup_vs_plain_fp64": d["speedup_solves_per_s"],
+            "max_abs_dE_vs_plain_fp64": d["max_abs_dE_vs_plain"], "converged": sv["converged"], "requests": sv["n"],
+            "workload": (f"{n_requests} requests, Poisson arrivals at 50/s: nocc ~ U{{5..30}}, nvir = ceil(r nocc), "
+                         "r ~ U[4,6], naux = 8 (nocc + nvir), kept fraction ~ U[5%, 20%], converged at |dE| < 1e-7 "
+                         "Eh; served in split precision at iteration level (one scheduler thread, at most 8 live "
+                         "requests); plain arm: every 10th request, one at a time, FP64"),
+            "note": ("a short stream: arrivals outpace the server, so p50/p99 include queueing; plain-arm solves/s "
+                     "from its 1-in-10 sample")}
+
+
 WORKLOAD_TEXT = ("{wl}: nocc={o} nvir={v} naux={naux} Cholesky factor entries N(0, {sigma}^2/naux) (a factor "
                  "normalised by naux; entries N(0, {sigma}^2) put every workload outside CCSD's convergence "
                  "regime), m={m} FRI systematic, 2 compressions/iteration, MP2 start")
@@ -517,6 +551,13 @@ def run_gpu(args):
         t1h, t2h = system.mp2_amplitudes()
         cpu = cpu_baseline_line(eris_np, t1h, t2h, m, args.workload, 7)
 
+    # the served request stream (the metric's solves/s and p50/p99), a
+    # short sample in a child process
+    served = None
+    if rank == 0 and world == 1 and args.served_requests > 0:
+        torch.cuda.empty_cache()
+        served = served_sample(args.served_requests)
+
     pk = fma_peaks_cached() if rank == 0 else {"fp64": FP64_PEAK_FALLBACK, "fp32": FP32_PEAK_FALLBACK,
                                                 "source": "recorded pool figures"}
     achieved = (p_fl.value / (p_ms.value / 1000.0)) / 1e12 if p_ms.value > 0 else None
@@ -592,6 +633,8 @@ def run_gpu(args):
         if gemm is not None:
             line["dense_gemm"] = gemm
         line.update(secondary)
+        if served is not None:
+            line["served_form"] = served
         print(json.dumps(line))
     if world > 1:
         dist.destroy_process_group()

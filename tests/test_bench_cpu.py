@@ -120,3 +120,25 @@ def test_block_plan_covers_every_pair_once():
                 seen.extend(range(lo, hi))
             assert seen == list(range(n))
     assert [bench.n_blocks_for(k) for k in (1, 2, 5, 7, 20, 30)] == [1, 2, 5, 7, 10, 10]
+
+
+def test_served_sample_parses_the_server_line_and_survives_failure(monkeypatch):
+    """bench.py's served_form: the child serve_bench line becomes solves/s,
+    p50/p99, the plain FP64 rate, the speed-up and the largest |dE|; a
+    failing child is reported as an error, never raised."""
+    sys.path.insert(0, REPO)
+    import bench
+
+    line = {"served": {"solves_per_s": 15.0, "p50_s": 3.0, "p99_s": 7.5, "converged": 150, "n": 150},
+            "plain": {"solves_per_s": 1.25}, "speedup_solves_per_s": 12.0, "max_abs_dE_vs_plain": 4e-7}
+
+    class R:
+        def __init__(self, rc, out, err=""):
+            self.returncode, self.stdout, self.stderr = rc, out, err
+
+    monkeypatch.setattr(bench.subprocess, "run", lambda *a, **k: R(0, "noise\n" + json.dumps(line) + "\n"))
+    d = bench.served_sample(150)
+    assert d["solves_per_s"] == 15.0 and d["plain_fp64_solves_per_s"] == 1.25 and d["speedup_vs_plain_fp64"] == 12.0
+    assert d["p50_s"] == 3.0 and d["p99_s"] == 7.5 and d["max_abs_dE_vs_plain_fp64"] == 4e-7 and d["requests"] == 150
+    monkeypatch.setattr(bench.subprocess, "run", lambda *a, **k: R(1, "", "no device"))
+    assert "error" in bench.served_sample(150)
